@@ -1,0 +1,118 @@
+"""Seeded synthetic workloads with the shapes of the benchmark configurations.
+
+No dataset exists for these problems; each builder returns host (numpy) arrays of the whole
+padded fields so that the GPU path and the CPU oracle start from identical bits.
+
+stokes2d_inclusions: 2D incompressible VE Stokes (examples/stokes_2d_inc_ve_T.jl form) on
+  [-0.5, 0.5]^2 with background viscosity 1 and 8 circular inclusions (centres uniform,
+  radius U[0.02, 0.08], log10 viscosity U[-3, 3], seed 3), pure shear eps = 1 imposed as
+  Dirichlet normal velocity -eps*x (x faces) and +eps*y (y faces) with free slip
+  (Neumann) tangentially, G = 1, dt = 1e-2, PT parameters of the example (:86-93).
+"""
+
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .bcs import Dirichlet, Neumann, to_cg_bc
+from .grids import Center, UniformGrid, Vertex, expand_loc
+from .kernels import stokes_params
+
+
+def padded_coords(grid: UniformGrid, loc, halo=1):
+    """Coordinates of every padded index (logical 1-2H .. n+2H) per dim, in the grid type."""
+    locs = expand_loc(grid.ndim, loc)
+    out = []
+    for d, (ax, l) in enumerate(zip(grid.axes, locs)):
+        n = ax.size(l)
+        idx = np.arange(1 - 2 * halo, n + 2 * halo + 1)
+        o = ax.origin if isinstance(l, Vertex) else ax.origin + 0.5 * ax.spacing
+        out.append((o + (idx - 1) * ax.spacing).astype(grid.dtype))
+    return out
+
+
+def padded_mesh(grid: UniformGrid, loc, halo=1):
+    """[z, y, x] ordered meshes of the padded coordinates (matching the storage order)."""
+    c = padded_coords(grid, loc, halo)
+    mesh = np.meshgrid(*reversed(c), indexing="ij")
+    return list(reversed(mesh))  # x, y[, z] arrays shaped [z, y, x]
+
+
+@dataclass
+class StokesProblem:
+    grid: UniformGrid
+    host: dict = field(default_factory=dict)  # name -> padded numpy array or list of them
+    params: object = None
+    bc_V: list = field(default_factory=list)
+    eps: float = 1e-8
+    tau_scale: float = 1.0
+    v_scale: float = 1.0
+    ncheck: int = 512
+    max_iter: int = 0
+
+
+def inclusions(seed=3, count=8):
+    rng = np.random.default_rng(seed)
+    cx = rng.uniform(-0.5, 0.5, count)
+    cy = rng.uniform(-0.5, 0.5, count)
+    r = rng.uniform(0.02, 0.08, count)
+    leta = rng.uniform(-3.0, 3.0, count)
+    return cx, cy, r, leta
+
+
+def stokes2d_inclusions(n=2048, dtype=np.float64, seed=3, eps=1e-8, ncheck=None, max_iter=None, re_m_pi=4.0) -> StokesProblem:
+    T = np.dtype(dtype).type
+    lx = ly = 1.0
+    grid = UniformGrid(origin=(T(-lx / 2), T(-ly / 2)), extent=(T(lx), T(ly)), dims=(n, n), dtype=T)
+    C, V = Center(), Vertex()
+    # viscosity at cell centres, evaluated over the whole padded array
+    x, y = padded_mesh(grid, C)
+    eta = np.ones_like(x)
+    for cx, cy, r, le in zip(*inclusions(seed)):
+        eta[(x - cx) ** 2 + (y - cy) ** 2 < r * r] = 10.0**le
+    erate = 1.0
+    xv, _ = padded_mesh(grid, (V, C))
+    _, yv = padded_mesh(grid, (C, V))
+    Vx = (-erate * xv).astype(T)
+    Vy = (erate * yv).astype(T)
+
+    def zeros(loc):
+        m = padded_mesh(grid, loc)[0]
+        return np.zeros_like(m, dtype=T)
+
+    tau_locs = [(C, C), (C, C), (V, V)]
+    host = {
+        "V": [Vx, Vy],
+        "r_V": [zeros((V, C)), zeros((C, V))],
+        "P": zeros(C),
+        "divV": zeros(C),
+        "tau": [zeros(l) for l in tau_locs],
+        "tau_old": [zeros(l) for l in tau_locs],
+        "eta": eta.astype(T),
+    }
+    G, dt = 1.0, 1e-2
+    dx = float(min(grid.spacing()))
+    re_m, r = re_m_pi * math.pi, 0.5
+    lt = min(lx, ly) / re_m
+    vdt = dx / math.sqrt(2 * 1.1)
+    th = lt * (r + 4.0 / 3.0) / vdt
+    params = stokes_params(eta=1.0, eta_ve=1.0 / (1.0 + 1.0 / (G * dt)), G=G, dt=dt, dtau_Pr=r / th, dtau_r=1.0 / (th + 1.0), nu_dtau=vdt * lt)
+    bc_V = [
+        to_cg_bc(2, {"x": (Dirichlet(erate * lx / 2), Dirichlet(-erate * lx / 2)), "y": Neumann()}),
+        to_cg_bc(2, {"x": Neumann(), "y": (Dirichlet(-erate * ly / 2), Dirichlet(erate * ly / 2))}),
+    ]
+    eta_bg, psc = 1.0, G
+    return StokesProblem(
+        grid=grid,
+        host=host,
+        params=params,
+        bc_V=bc_V,
+        eps=eps,
+        tau_scale=eta_bg / psc,
+        v_scale=ly / psc,
+        ncheck=ncheck or max(n // 4, 1),
+        max_iter=max_iter or 200 * n,
+    )

@@ -1,0 +1,164 @@
+"""Field, VectorField, TensorField, interior and set! (Chmy.jl src/Fields/field.jl).
+
+A Field stores its padded array (extent n + 4H per dimension, x fastest) in a torch CUDA
+tensor. The tensor is indexed [z, y, x] (C order, reversed dims); `interior(f)` returns a
+view indexed [x, y, z] like Chmy's column-major `interior`.
+"""
+
+from __future__ import annotations
+
+from collections import namedtuple
+
+import numpy as np
+import torch
+
+from . import _abi
+from .grids import Center, Location, UniformGrid, Vertex, expand_loc
+
+_TORCH = {np.float32: torch.float32, np.float64: torch.float64}
+_CODE = {np.float32: _abi.CG_F32, np.float64: _abi.CG_F64}
+
+
+def _np_type(dtype) -> type:
+    if dtype in (torch.float32, np.float32, "float32", "f32"):
+        return np.float32
+    if dtype in (torch.float64, np.float64, "float64", "f64", float):
+        return np.float64
+    if isinstance(dtype, np.dtype):
+        return dtype.type
+    raise TypeError(f"unsupported field type {dtype!r}")
+
+
+class Field:
+    """Field(arch, grid, loc, type=eltype(grid); halo=1) (src/Fields/field.jl:56-62).
+
+    `pitch_align` (bytes, 0 = dense Chmy layout) pads x rows so that logical x index 0 of each
+    row is aligned, which lets kernels issue aligned vector loads."""
+
+    def __init__(self, arch, grid: UniformGrid, loc, dtype=None, halo=1, pitch_align: int = 0):
+        self.arch = arch
+        self.grid = grid
+        nd = grid.ndim
+        self.loc = expand_loc(nd, loc)
+        self.dtype = _np_type(dtype if dtype is not None else grid.dtype)
+        self.halo = tuple(halo) if isinstance(halo, (tuple, list)) else tuple(int(halo) for _ in range(nd))
+        if any(h < 1 for h in self.halo):
+            raise ValueError("the GB300 kernels need halo >= 1 in every dimension")
+        self.dims = grid.size(self.loc)
+        self.ext = tuple(n + 4 * h for n, h in zip(self.dims, self.halo))
+        tdt = _TORCH[self.dtype]
+        esz = np.dtype(self.dtype).itemsize
+        dev = arch.device
+        if pitch_align:
+            a = pitch_align // esz
+            front = (a - (2 * self.halo[0] - 1) % a) % a
+            pitch = ((front + self.ext[0] + a - 1) // a) * a
+            storage = torch.zeros(tuple(reversed(self.ext[1:])) + (pitch,), dtype=tdt, device=dev)
+            self._storage = storage
+            self.data = storage[..., front : front + self.ext[0]]
+        else:
+            self._storage = None
+            self.data = torch.zeros(tuple(reversed(self.ext)), dtype=tdt, device=dev)
+
+    @property
+    def ndim(self) -> int:
+        return len(self.dims)
+
+    def location(self) -> tuple[Location, ...]:
+        return self.loc
+
+    def size(self) -> tuple[int, ...]:
+        return self.dims
+
+    def desc(self) -> _abi.cg_field:
+        strides = tuple(reversed(self.data.stride()))
+        return _abi.make_field(
+            self.data.data_ptr(),
+            _CODE[self.dtype],
+            self.dims,
+            tuple(l.code for l in self.loc),
+            self.halo,
+            strides,
+        )
+
+    # -- host transfer helpers (padded array, stored [z, y, x]) --
+    def to_numpy(self) -> np.ndarray:
+        return self.data.detach().cpu().numpy().copy()
+
+    def from_numpy(self, arr: np.ndarray) -> None:
+        arr = np.asarray(arr, dtype=self.dtype)
+        if arr.shape != tuple(reversed(self.ext)):
+            raise ValueError(f"expected padded shape {tuple(reversed(self.ext))}, got {arr.shape}")
+        self.data.copy_(torch.from_numpy(np.ascontiguousarray(arr)))
+
+    def __repr__(self):
+        return f"Field(dims={self.dims}, loc={self.loc}, dtype={self.dtype.__name__}, halo={self.halo})"
+
+
+def interior(f: Field, with_halo: bool = False) -> torch.Tensor:
+    """interior(f; with_halo=false) (src/Fields/field.jl:33-37) as an [x, y, z] view."""
+    sl = []
+    for n, h in zip(reversed(f.dims), reversed(f.halo)):
+        lo = 2 * h - (h if with_halo else 0)
+        hi = 2 * h + n + (h if with_halo else 0)
+        sl.append(slice(lo, hi))
+    v = f.data[tuple(sl)]
+    return v.permute(*reversed(range(f.ndim)))
+
+
+def evaluate(grid: UniformGrid, loc, dims, fun, discrete: bool = False, parameters=(), dtype=np.float64) -> np.ndarray:
+    """Values of `fun` on the interior points of a field at `loc`, [x, y, z] indexed: the
+    continuous form calls fun(coords..., params...) (_set_continuous!, field.jl:121-124); the
+    discrete form calls fun(grid, loc, I..., params...) (_set_discrete!, field.jl:126-129)."""
+    if discrete:
+        out = np.empty(dims, dtype=dtype)
+        for idx in np.ndindex(*dims):
+            I = tuple(i + 1 for i in idx)
+            out[idx] = fun(grid, loc, *I, *parameters)
+        return out
+    axes = [grid.coords(loc, d + 1) for d in range(len(dims))]
+    mesh = np.meshgrid(*axes, indexing="ij")
+    out = np.asarray(fun(*mesh, *parameters), dtype=dtype)
+    return np.ascontiguousarray(np.broadcast_to(out, dims), dtype=dtype)
+
+
+def set_(f: Field, value, grid: UniformGrid | None = None, *, discrete: bool = False, parameters=()) -> None:
+    """set!(f, val) / set!(f, A) / set!(f, grid, fun; discrete, parameters) (field.jl:87-142)."""
+    dst = interior(f)
+    if callable(value):
+        g = grid if grid is not None else f.grid
+        out = evaluate(g, f.loc, f.dims, value, discrete, parameters, f.dtype)
+        dst.copy_(torch.from_numpy(out))
+    elif isinstance(value, (int, float, np.floating, np.integer)):
+        dst.fill_(float(value))
+    else:
+        src = value if isinstance(value, torch.Tensor) else torch.from_numpy(np.asarray(value, dtype=f.dtype))
+        dst.copy_(src.to(dst.dtype))
+
+
+def vector_location(dim: int, ndim: int):
+    """vector_location(Val(dim), Val(N)) (field.jl:148): Vertex along `dim`, Center elsewhere."""
+    return tuple(Vertex() if i == dim else Center() for i in range(ndim))
+
+
+_VEC = {1: namedtuple("VectorField1", "x"), 2: namedtuple("VectorField2", "x y"), 3: namedtuple("VectorField3", "x y z")}
+_TEN = {2: namedtuple("TensorField2", "xx yy xy"), 3: namedtuple("TensorField3", "xx yy zz xy xz yz")}
+
+
+def VectorField(arch, grid: UniformGrid, dtype=None, halo=1, pitch_align: int = 0):
+    """VectorField(backend, grid) (field.jl:161-169): component d at Vertex along d."""
+    nd = grid.ndim
+    return _VEC[nd](*[Field(arch, grid, vector_location(d, nd), dtype, halo, pitch_align) for d in range(nd)])
+
+
+def TensorField(arch, grid: UniformGrid, dtype=None, halo=1, pitch_align: int = 0):
+    """TensorField(backend, grid) (field.jl:182-206): diagonal at Center, shear on edges."""
+    nd = grid.ndim
+    C, V = Center(), Vertex()
+    if nd == 2:
+        locs = [(C, C), (C, C), (V, V)]
+    elif nd == 3:
+        locs = [(C, C, C), (C, C, C), (C, C, C), (V, V, C), (V, C, V), (C, V, V)]
+    else:
+        raise ValueError("TensorField needs a 2D or 3D grid")
+    return _TEN[nd](*[Field(arch, grid, l, dtype, halo, pitch_align) for l in locs])

@@ -1,0 +1,127 @@
+"""Device-resident PT solvers over the library (the PT loops of the reference examples).
+
+StokesSolver holds a VE Stokes field set on the GPU and runs the PT loop of
+examples/stokes_2d_inc_ve_T.jl:144-163 through the library: graph-replayed chunks of
+`ncheck` iterations (update_stress!, update_velocity!, bc!(V)), then the convergence
+measures of :154-157, until every measure is below eps.
+"""
+
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _abi
+from .configs import StokesProblem
+from .fields import Field
+from .grids import Center, Vertex
+from .kernels import stokes_fields
+
+
+def _loc_of(arr_name: str, idx: int, nd: int):
+    C, V = Center(), Vertex()
+    if arr_name in ("V", "r_V", "rho_g", "qT"):
+        return tuple(V if d == idx else C for d in range(nd))
+    if arr_name in ("tau", "tau_old"):
+        if nd == 2:
+            return [(C, C), (C, C), (V, V)][idx]
+        return [(C, C, C), (C, C, C), (C, C, C), (V, V, C), (V, C, V), (C, V, V)][idx]
+    return tuple(C for _ in range(nd))
+
+
+class StokesSolver:
+    """VE Stokes state on the device plus the library's PT entry points."""
+
+    def __init__(self, arch, problem: StokesProblem, pitch_align: int = 0, precompute_inv_eta: bool = True):
+        self.arch = arch
+        self.pb = problem
+        g = problem.grid
+        nd = g.ndim
+        self.fields: dict = {}
+        for name, val in problem.host.items():
+            if isinstance(val, list):
+                fs = []
+                for i, a in enumerate(val):
+                    if a is None:
+                        fs.append(None)
+                        continue
+                    f = Field(arch, g, _loc_of(name, i, nd), a.dtype.type, pitch_align=pitch_align)
+                    f.from_numpy(a)
+                    fs.append(f)
+                self.fields[name] = fs
+            else:
+                f = Field(arch, g, _loc_of(name, 0, nd), val.dtype.type, pitch_align=pitch_align)
+                f.from_numpy(val)
+                self.fields[name] = f
+        if precompute_inv_eta and "eta" in self.fields:
+            inv = Field(arch, g, Center(), self.fields["eta"].dtype, pitch_align=pitch_align)
+            inv.data.copy_(1.0 / self.fields["eta"].data)
+            self.fields["inv_eta"] = inv
+        self.desc = stokes_fields(**self.fields)
+        self.grid_desc = g.desc()
+        self.bc_arr = (_abi.cg_bc * 3)(*problem.bc_V)
+        self.iterations = 0
+
+    def upload(self, host: dict) -> None:
+        """Copy host arrays (same layout as problem.host) into the device fields."""
+        for name, val in host.items():
+            if isinstance(val, list):
+                for f, a in zip(self.fields[name], val):
+                    if f is not None and a is not None:
+                        f.data.copy_(a if not isinstance(a, np.ndarray) else __import__("torch").from_numpy(a), non_blocking=True)
+            else:
+                f = self.fields[name]
+                f.data.copy_(val if not isinstance(val, np.ndarray) else __import__("torch").from_numpy(val), non_blocking=True)
+
+    def iterate(self, niter: int) -> None:
+        """`niter` PT iterations (one CUDA graph replay)."""
+        self.arch.call(
+            "cg_stokes_pt_iterations",
+            ctypes.byref(self.grid_desc),
+            ctypes.byref(self.desc),
+            ctypes.byref(self.pb.params),
+            self.bc_arr,
+            int(niter),
+        )
+        self.iterations += niter
+
+    def residual(self) -> list[float]:
+        err = (ctypes.c_double * 4)()
+        self.arch.call(
+            "cg_stokes_residual",
+            ctypes.byref(self.grid_desc),
+            ctypes.byref(self.desc),
+            float(self.pb.tau_scale),
+            float(self.pb.v_scale),
+            err,
+        )
+        return [err[i] for i in range(self.pb.grid.ndim + 1)]
+
+    def solve(self, max_iter: int | None = None, precision: int = _abi.CG_F64, max_outer: int = 8, inner_rtol: float = 1e-5):
+        o = _abi.cg_solve_opts()
+        o.max_iter = int(max_iter or self.pb.max_iter)
+        o.ncheck = int(self.pb.ncheck)
+        o.eps = float(self.pb.eps)
+        o.tau_scale = float(self.pb.tau_scale)
+        o.v_scale = float(self.pb.v_scale)
+        o.precision = precision
+        o.max_outer = max_outer
+        o.inner_rtol = inner_rtol
+        res = _abi.cg_solve_result()
+        rc = self.arch.lib.cg_stokes_solve(
+            self.arch.ctx,
+            ctypes.byref(self.grid_desc),
+            ctypes.byref(self.desc),
+            ctypes.byref(self.pb.params),
+            self.bc_arr,
+            ctypes.byref(o),
+            ctypes.byref(res),
+        )
+        if rc not in (_abi.CG_OK, _abi.CG_ERR_NOCONV):
+            _abi.check(self.arch.lib, rc, "cg_stokes_solve", self.arch.ctx)
+        return res
+
+    def apply_bc(self) -> None:
+        fa = (_abi.cg_field * 3)(*[f.desc() for f in self.fields["V"]])
+        self.arch.call("cg_bc_apply", ctypes.byref(self.grid_desc), self.pb.grid.ndim, fa, self.bc_arr)

@@ -1,0 +1,132 @@
+// cg_common.cuh — shared pieces of libchmy_gb300: context, error plumbing, device field views.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "../../include/chmy_gb300.h"
+
+struct cg_graph_entry {
+    std::string key;            // bytes of the launch arguments the graph was captured with
+    cudaGraphExec_t exec = nullptr;
+};
+
+struct cg_ctx {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    // reduction scratch: per-field 64-bit max slots (device) and their host mirror (pinned)
+    unsigned long long* d_red = nullptr;
+    unsigned long long* h_red = nullptr;
+    static constexpr int kRedSlots = 64;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    char err[512] = {0};
+    cg_graph_entry graphs[8];
+    int graph_next = 0;
+    // FP32 work arrays of the defect-correction solver (allocated on first use)
+    void* dc_pool = nullptr;
+    size_t dc_pool_bytes = 0;
+};
+
+// Record an error message on ctx and return `code`.
+int cg_fail(cg_ctx* ctx, int code, const char* fmt, ...);
+
+#define CG_CUDA(ctx, call)                                                                       \
+    do {                                                                                         \
+        cudaError_t e_ = (call);                                                                 \
+        if (e_ != cudaSuccess) return cg_fail((ctx), CG_ERR_CUDA, "%s: %s (%s:%d)", #call,      \
+                                              cudaGetErrorString(e_), __FILE__, __LINE__);       \
+    } while (0)
+
+#define CG_CHECK_LAUNCH(ctx) CG_CUDA(ctx, cudaGetLastError())
+
+// Device view of a field: `p` points at logical index (0,0,0); element (i,j,k) is
+// p[i + j*s1 + k*s2]. Logical indices -1 .. n+2 are inside the padded allocation (H >= 1).
+template <class T>
+struct DF {
+    T* __restrict__ p;
+    long s1, s2;
+    __host__ __device__ __forceinline__ T& operator()(int i, int j, int k) const {
+        return p[i + (long)j * s1 + (long)k * s2];
+    }
+    __host__ __device__ __forceinline__ T* ptr(int i, int j, int k) const {
+        return p + i + (long)j * s1 + (long)k * s2;
+    }
+};
+
+// Offset (elements) of logical index 0 from the allocation start.
+inline long cg_origin_offset(const cg_field& f) {
+    long off = 0;
+    for (int d = 0; d < f.ndim; ++d) off += (long)(2 * f.halo[d] - 1) * f.stride[d];
+    return off;
+}
+
+template <class T>
+inline DF<T> cg_view(const cg_field& f) {
+    DF<T> v;
+    v.p = static_cast<T*>(f.data) + cg_origin_offset(f);
+    v.s1 = f.ndim > 1 ? (long)f.stride[1] : 0;
+    v.s2 = f.ndim > 2 ? (long)f.stride[2] : 0;
+    return v;
+}
+
+// Validate a field against the expected dtype, ndim and per-dim location on `grid`.
+// loc_mask bit d set => Vertex along d. Returns CG_OK or records CG_ERR_ARG.
+int cg_check_field(cg_ctx* ctx, const cg_grid* grid, const cg_field& f, int dtype, int loc_mask,
+                   const char* name);
+int cg_check_grid(cg_ctx* ctx, const cg_grid* grid);
+
+inline bool cg_present(const cg_field& f) { return f.data != nullptr; }
+
+// Run `capture(stream)` into a CUDA graph cached under `key` and launch it.
+template <class F>
+int cg_graph_run(cg_ctx* ctx, const std::string& key, F&& capture);
+
+// ---- small helpers -------------------------------------------------------------------------
+inline int cg_div_up(long a, long b) { return (int)((a + b - 1) / b); }
+
+template <class F>
+int cg_graph_run(cg_ctx* ctx, const std::string& key, F&& capture) {
+    cg_graph_entry* hit = nullptr;
+    for (auto& g : ctx->graphs)
+        if (g.exec && g.key == key) hit = &g;
+    if (!hit) {
+        cg_graph_entry& slot = ctx->graphs[ctx->graph_next];
+        ctx->graph_next = (ctx->graph_next + 1) % 8;
+        if (slot.exec) {
+            cudaGraphExecDestroy(slot.exec);
+            slot.exec = nullptr;
+        }
+        cudaGraph_t graph = nullptr;
+        CG_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        int rc = capture(ctx->stream);
+        cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
+        if (rc != CG_OK) {
+            if (graph) cudaGraphDestroy(graph);
+            return rc;
+        }
+        if (ce != cudaSuccess) return cg_fail(ctx, CG_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+        cudaError_t ie = cudaGraphInstantiate(&slot.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ie != cudaSuccess) {
+            slot.exec = nullptr;
+            return cg_fail(ctx, CG_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ie));
+        }
+        slot.key = key;
+        hit = &slot;
+    }
+    CG_CUDA(ctx, cudaGraphLaunch(hit->exec, ctx->stream));
+    return CG_OK;
+}
+
+// Append the raw bytes of a POD value to a graph key.
+template <class V>
+inline void cg_key_add(std::string& k, const V& v) {
+    k.append(reinterpret_cast<const char*>(&v), sizeof(V));
+}

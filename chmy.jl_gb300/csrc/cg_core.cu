@@ -1,0 +1,581 @@
+// cg_core.cu — context, memory, argument checks, the fused boundary-condition kernel and the
+// max-norm reduction of libchmy_gb300.
+#include <cstdarg>
+#include <vector>
+
+#include "cg_common.cuh"
+
+static char g_init_err[512] = "";
+
+int cg_fail(cg_ctx* ctx, int code, const char* fmt, ...) {
+    char* dst = ctx ? ctx->err : g_init_err;
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(dst, 512, fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+extern "C" int cg_abi_version(void) { return CG_ABI_VERSION; }
+
+extern "C" const char* cg_last_error(const cg_ctx* ctx) { return ctx ? ctx->err : g_init_err; }
+
+extern "C" int cg_init(int device, cg_ctx** out) {
+    if (!out) return cg_fail(nullptr, CG_ERR_ARG, "cg_init: out is NULL");
+    *out = nullptr;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess) return cg_fail(nullptr, CG_ERR_CUDA, "cudaGetDeviceCount: %s", cudaGetErrorString(e));
+    if (device < 0 || device >= ndev)
+        return cg_fail(nullptr, CG_ERR_ARG, "cg_init: device %d not in [0, %d)", device, ndev);
+    e = cudaSetDevice(device);
+    if (e != cudaSuccess) return cg_fail(nullptr, CG_ERR_CUDA, "cudaSetDevice: %s", cudaGetErrorString(e));
+    cg_ctx* ctx = new cg_ctx();
+    ctx->device = device;
+    cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+    e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_red, sizeof(unsigned long long) * cg_ctx::kRedSlots);
+    if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_red, sizeof(unsigned long long) * cg_ctx::kRedSlots);
+    if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
+    if (e != cudaSuccess) {
+        cg_fail(nullptr, CG_ERR_CUDA, "cg_init: %s", cudaGetErrorString(e));
+        cg_destroy(ctx);
+        return CG_ERR_CUDA;
+    }
+    ctx->stream = ctx->own_stream;
+    *out = ctx;
+    return CG_OK;
+}
+
+extern "C" int cg_destroy(cg_ctx* ctx) {
+    if (!ctx) return CG_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->own_stream) cudaStreamSynchronize(ctx->own_stream);
+    for (auto& g : ctx->graphs)
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+    if (ctx->dc_pool) cudaFree(ctx->dc_pool);
+    if (ctx->d_red) cudaFree(ctx->d_red);
+    if (ctx->h_red) cudaFreeHost(ctx->h_red);
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+    delete ctx;
+    return CG_OK;
+}
+
+extern "C" int cg_set_stream(cg_ctx* ctx, void* stream) {
+    if (!ctx) return cg_fail(nullptr, CG_ERR_ARG, "cg_set_stream: ctx is NULL");
+    ctx->stream = stream ? static_cast<cudaStream_t>(stream) : ctx->own_stream;
+    return CG_OK;
+}
+
+extern "C" int cg_sync(cg_ctx* ctx) {
+    if (!ctx) return cg_fail(nullptr, CG_ERR_ARG, "cg_sync: ctx is NULL");
+    CG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return CG_OK;
+}
+
+// ---- argument checks -----------------------------------------------------------------------
+
+int cg_check_grid(cg_ctx* ctx, const cg_grid* grid) {
+    if (!ctx) return cg_fail(nullptr, CG_ERR_ARG, "ctx is NULL");
+    if (!grid) return cg_fail(ctx, CG_ERR_ARG, "grid is NULL");
+    if (grid->ndim < 1 || grid->ndim > 3) return cg_fail(ctx, CG_ERR_ARG, "grid ndim %d not in 1..3", grid->ndim);
+    for (int d = 0; d < grid->ndim; ++d)
+        if (grid->n[d] < 2) return cg_fail(ctx, CG_ERR_ARG, "grid n[%d] = %d < 2", d, grid->n[d]);
+    return CG_OK;
+}
+
+int cg_check_field(cg_ctx* ctx, const cg_grid* grid, const cg_field& f, int dtype, int loc_mask, const char* name) {
+    if (!f.data) return cg_fail(ctx, CG_ERR_ARG, "%s: data is NULL", name);
+    if (f.dtype != dtype) return cg_fail(ctx, CG_ERR_ARG, "%s: dtype %d, expected %d", name, f.dtype, dtype);
+    if (f.ndim != grid->ndim) return cg_fail(ctx, CG_ERR_ARG, "%s: ndim %d, grid has %d", name, f.ndim, grid->ndim);
+    for (int d = 0; d < f.ndim; ++d) {
+        const int want_loc = (loc_mask >> d) & 1;
+        if (loc_mask >= 0 && f.loc[d] != want_loc)
+            return cg_fail(ctx, CG_ERR_ARG, "%s: location along dim %d is %s, expected %s", name, d,
+                           f.loc[d] ? "Vertex" : "Center", want_loc ? "Vertex" : "Center");
+        if (f.n[d] != grid->n[d] + f.loc[d])
+            return cg_fail(ctx, CG_ERR_ARG, "%s: extent n[%d] = %d does not match grid (%d)", name, d, f.n[d],
+                           grid->n[d] + f.loc[d]);
+        if (f.halo[d] < 1) return cg_fail(ctx, CG_ERR_ARG, "%s: halo[%d] = %d < 1", name, d, f.halo[d]);
+    }
+    if (f.stride[0] != 1) return cg_fail(ctx, CG_ERR_ARG, "%s: stride[0] must be 1", name);
+    if (f.ndim > 1 && f.stride[1] < f.n[0] + 4 * f.halo[0])
+        return cg_fail(ctx, CG_ERR_ARG, "%s: stride[1] smaller than the padded x extent", name);
+    if (f.ndim > 2 && f.stride[2] < f.stride[1] * (f.n[1] + 4 * f.halo[1]))
+        return cg_fail(ctx, CG_ERR_ARG, "%s: stride[2] smaller than the padded xy plane", name);
+    return CG_OK;
+}
+
+// ---- memory ----------------------------------------------------------------------------------
+
+extern "C" int cg_field_alloc(cg_ctx* ctx, int dtype, int ndim, const int32_t n[3], const int32_t loc[3],
+                              const int32_t halo[3], int pitch_align, cg_field* out) {
+    if (!ctx || !out || !n || !loc || !halo) return cg_fail(ctx, CG_ERR_ARG, "cg_field_alloc: NULL argument");
+    if (dtype != CG_F32 && dtype != CG_F64) return cg_fail(ctx, CG_ERR_ARG, "cg_field_alloc: bad dtype %d", dtype);
+    if (ndim < 1 || ndim > 3) return cg_fail(ctx, CG_ERR_ARG, "cg_field_alloc: bad ndim %d", ndim);
+    if (pitch_align && (pitch_align < 16 || (pitch_align & (pitch_align - 1))))
+        return cg_fail(ctx, CG_ERR_ARG, "cg_field_alloc: pitch_align %d is not a power of two >= 16", pitch_align);
+    const int esz = dtype == CG_F64 ? 8 : 4;
+    cg_field f;
+    std::memset(&f, 0, sizeof(f));
+    f.dtype = dtype;
+    f.ndim = ndim;
+    long ext[3] = {1, 1, 1};
+    for (int d = 0; d < 3; ++d) {
+        if (d < ndim) {
+            if (n[d] < 1 || halo[d] < 0 || (loc[d] != 0 && loc[d] != 1))
+                return cg_fail(ctx, CG_ERR_ARG, "cg_field_alloc: bad extent/halo/location along dim %d", d);
+            f.n[d] = n[d];
+            f.loc[d] = loc[d];
+            f.halo[d] = halo[d];
+            ext[d] = n[d] + 4L * halo[d];
+        } else {
+            f.n[d] = 1;
+        }
+    }
+    long front = 0, pitch = ext[0];
+    if (pitch_align) {
+        const long a = pitch_align / esz;
+        front = (a - (2L * f.halo[0] - 1) % a) % a;
+        pitch = ((front + ext[0] + a - 1) / a) * a;
+    }
+    f.stride[0] = 1;
+    f.stride[1] = ndim > 1 ? pitch : 0;
+    f.stride[2] = ndim > 2 ? pitch * ext[1] : 0;
+    const size_t count = (size_t)pitch * ext[1] * ext[2] + (size_t)front;
+    void* base = nullptr;
+    CG_CUDA(ctx, cudaMalloc(&base, count * esz));
+    CG_CUDA(ctx, cudaMemsetAsync(base, 0, count * esz, ctx->stream));
+    f.data = static_cast<char*>(base) + front * esz;
+    f.pad_ = (int32_t)front;
+    *out = f;
+    return CG_OK;
+}
+
+extern "C" int cg_field_free(cg_ctx* ctx, cg_field* f) {
+    if (!ctx || !f) return cg_fail(ctx, CG_ERR_ARG, "cg_field_free: NULL argument");
+    if (!f->data) return CG_OK;
+    const int esz = f->dtype == CG_F64 ? 8 : 4;
+    void* base = static_cast<char*>(f->data) - (long)f->pad_ * esz;
+    CG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    CG_CUDA(ctx, cudaFree(base));
+    f->data = nullptr;
+    return CG_OK;
+}
+
+static int field_copy(cg_ctx* ctx, const cg_field* f, void* host, bool up) {
+    if (!ctx || !f || !f->data || !host) return cg_fail(ctx, CG_ERR_ARG, "field copy: NULL argument");
+    const int esz = f->dtype == CG_F64 ? 8 : 4;
+    long ext[3] = {1, 1, 1};
+    for (int d = 0; d < f->ndim; ++d) ext[d] = f->n[d] + 4L * f->halo[d];
+    const size_t row = (size_t)ext[0] * esz;
+    const size_t dpitch = f->ndim > 1 ? (size_t)f->stride[1] * esz : row;
+    const size_t plane = f->ndim > 2 ? (size_t)f->stride[2] * esz : dpitch * ext[1];
+    const bool dense_planes = (plane == dpitch * ext[1]);
+    cudaMemcpyKind kind = up ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost;
+    if (dense_planes) {
+        if (up)
+            CG_CUDA(ctx, cudaMemcpy2DAsync(f->data, dpitch, host, row, row, ext[1] * ext[2], kind, ctx->stream));
+        else
+            CG_CUDA(ctx, cudaMemcpy2DAsync(host, row, f->data, dpitch, row, ext[1] * ext[2], kind, ctx->stream));
+    } else {
+        for (long k = 0; k < ext[2]; ++k) {
+            char* dev = static_cast<char*>(f->data) + k * plane;
+            char* hst = static_cast<char*>(host) + k * row * ext[1];
+            if (up)
+                CG_CUDA(ctx, cudaMemcpy2DAsync(dev, dpitch, hst, row, row, ext[1], kind, ctx->stream));
+            else
+                CG_CUDA(ctx, cudaMemcpy2DAsync(hst, row, dev, dpitch, row, ext[1], kind, ctx->stream));
+        }
+    }
+    CG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return CG_OK;
+}
+
+extern "C" int cg_field_upload(cg_ctx* ctx, const cg_field* f, const void* host_dense) {
+    return field_copy(ctx, f, const_cast<void*>(host_dense), true);
+}
+extern "C" int cg_field_download(cg_ctx* ctx, const cg_field* f, void* host_dense) {
+    return field_copy(ctx, f, host_dense, false);
+}
+
+// ---- boundary conditions: one launch per batch ------------------------------------------------
+//
+// Chmy applies a batch as 2N launches, Dim N -> 1 and Side(1) then Side(2), each over the
+// tangential indices 0..n+2 (src/BoundaryConditions/batch.jl:104-113,243-268); a phase
+// reads the value one step inward, so a later phase can read what an earlier one wrote
+// (edges and corners). Here every written point is handled by exactly one thread — the
+// one of its LAST writing phase — which evaluates the chain of ghost rules back to a
+// point no phase writes (or to a Dirichlet constant). Points no phase writes are never
+// modified during the launch, so the single launch has no read/write race.
+
+namespace {
+
+constexpr int kBcMaxFields = 8;
+constexpr int kBcMaxItems = kBcMaxFields * 12;
+
+template <class T>
+struct BcField {
+    T* p;          // logical index 0
+    long s[3];
+    int ext[3];    // field extent per dim
+    int loc[3];
+    int kind[3][2];
+    T val[3][2];
+    T h[3];
+};
+
+struct BcItem {
+    int field, d, s, plane, start;
+};
+
+template <class T>
+struct BcBatch {
+    int nd;
+    int n[3];
+    int nitems;
+    int total;
+    BcField<T> f[kBcMaxFields];
+    BcItem items[kBcMaxItems];
+};
+
+enum { R_CONST = 0, R_DIR_C = 1, R_NEU = 2, R_COPY = 3 };
+
+// Planes written by phase (d, s): ghost index g, source index src and rule.
+template <class T>
+__host__ __device__ inline int phase_planes(const BcField<T>& F, const int* n, int d, int s, int* g, int* src,
+                                            int* rule) {
+    const int kind = F.kind[d][s];
+    const int ext = F.ext[d];
+    const bool vtx = F.loc[d] == CG_VERTEX;
+    switch (kind) {
+        case CG_BC_DIRICHLET:
+            if (vtx) {
+                g[0] = s ? ext : 1;
+                src[0] = -1;
+                rule[0] = R_CONST;
+            } else {
+                g[0] = s ? ext + 1 : 0;
+                src[0] = s ? ext : 1;
+                rule[0] = R_DIR_C;
+            }
+            return 1;
+        case CG_BC_NEUMANN:
+            g[0] = s ? ext + 1 : 0;
+            src[0] = s ? ext : 1;
+            rule[0] = R_NEU;
+            return 1;
+        case CG_BC_PERIODIC:
+            if (s == 0) {
+                g[0] = 0;
+                src[0] = n[d];
+                rule[0] = R_COPY;
+                return 1;
+            }
+            g[0] = n[d] + 1;
+            src[0] = 1;
+            rule[0] = R_COPY;
+            if (vtx) {
+                g[1] = n[d] + 2;
+                src[1] = 2;
+                rule[1] = R_COPY;
+                return 2;
+            }
+            return 1;
+        default:
+            return 0;
+    }
+}
+
+// Phase order index k <-> (d, s): k = (nd-1-d)*2 + s.
+template <class T>
+__device__ inline bool phase_member(const BcField<T>& F, int nd, const int* n, int k, const int* p, int* src,
+                                    int* rule) {
+    const int d = nd - 1 - (k >> 1), s = k & 1;
+    for (int t = 0; t < nd; ++t)
+        if (t != d && (p[t] < 0 || p[t] > n[t] + 2)) return false;
+    int g[2], sr[2], ru[2];
+    const int np = phase_planes(F, n, d, s, g, sr, ru);
+    for (int q = 0; q < np; ++q)
+        if (p[d] == g[q]) {
+            *src = sr[q];
+            *rule = ru[q];
+            return true;
+        }
+    return false;
+}
+
+template <class T>
+__global__ void bc_apply_kernel(const BcBatch<T> b) {
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid >= b.total) return;
+    int it = 0;
+    while (it + 1 < b.nitems && b.items[it + 1].start <= tid) ++it;
+    const BcItem item = b.items[it];
+    const BcField<T>& F = b.f[item.field];
+    const int nd = b.nd;
+    // decode the tangential coordinates (extent n_t + 3 each, index 0..n_t+2)
+    int p[3] = {0, 0, 0};
+    int rem = tid - item.start;
+    for (int t = 0; t < nd; ++t) {
+        if (t == item.d) continue;
+        const int e = b.n[t] + 3;
+        p[t] = rem % e;
+        rem /= e;
+    }
+    p[item.d] = item.plane;
+    const int k0 = (nd - 1 - item.d) * 2 + item.s;
+    int src, rule;
+    // only the last writing phase handles the point
+    for (int k = k0 + 1; k < 2 * nd; ++k)
+        if (phase_member(F, nd, b.n, k, p, &src, &rule)) return;
+    // walk the chain of rules back to an unwritten point or a constant
+    int stack_k[6], stack_r[6], depth = 0;
+    int q[3] = {p[0], p[1], p[2]};
+    int k = k0;
+    T base;
+    phase_member(F, nd, b.n, k, q, &src, &rule);
+    for (;;) {
+        const int d = nd - 1 - (k >> 1), s = k & 1;
+        if (rule == R_CONST) {
+            base = F.val[d][s];
+            break;
+        }
+        stack_k[depth] = k;
+        stack_r[depth] = rule;
+        ++depth;
+        q[d] = src;
+        int kn = -1;
+        for (int kk = k - 1; kk >= 0; --kk)
+            if (phase_member(F, nd, b.n, kk, q, &src, &rule)) {
+                kn = kk;
+                break;
+            }
+        if (kn < 0) {
+            base = F.p[q[0] + q[1] * F.s[1] + q[2] * F.s[2]];
+            break;
+        }
+        k = kn;
+    }
+    for (int i = depth - 1; i >= 0; --i) {
+        const int kk = stack_k[i];
+        const int d = nd - 1 - (kk >> 1), s = kk & 1;
+        switch (stack_r[i]) {
+            case R_DIR_C: base = fma(T(2), F.val[d][s] - base, base); break;
+            case R_NEU: base = fma(F.h[d], s == 0 ? -F.val[d][s] : F.val[d][s], base); break;
+            default: break;
+        }
+    }
+    F.p[p[0] + p[1] * F.s[1] + p[2] * F.s[2]] = base;
+}
+
+template <class T>
+int bc_apply_t(cg_ctx* ctx, const cg_grid* grid, int nfields, const cg_field* fields, const cg_bc* bcs) {
+    BcBatch<T> b;
+    std::memset(&b, 0, sizeof(b));
+    b.nd = grid->ndim;
+    for (int d = 0; d < 3; ++d) b.n[d] = d < b.nd ? grid->n[d] : 1;
+    int total = 0, ni = 0;
+    for (int fi = 0; fi < nfields; ++fi) {
+        const cg_field& f = fields[fi];
+        BcField<T>& F = b.f[fi];
+        F.p = static_cast<T*>(f.data) + cg_origin_offset(f);
+        for (int d = 0; d < 3; ++d) {
+            F.s[d] = d < f.ndim ? (long)f.stride[d] : 0;
+            F.ext[d] = d < f.ndim ? f.n[d] : 1;
+            F.loc[d] = d < f.ndim ? f.loc[d] : 0;
+            F.h[d] = (T)grid->spacing[d];
+            for (int s = 0; s < 2; ++s) {
+                F.kind[d][s] = d < f.ndim ? bcs[fi].kind[d][s] : CG_BC_NONE;
+                F.val[d][s] = (T)bcs[fi].value[d][s];
+            }
+        }
+        for (int d = 0; d < b.nd; ++d) {
+            const bool p0 = F.kind[d][0] == CG_BC_PERIODIC, p1 = F.kind[d][1] == CG_BC_PERIODIC;
+            if (p0 != p1) return cg_fail(ctx, CG_ERR_ARG, "bc: periodic must be set on both sides of dim %d", d);
+        }
+        for (int d = b.nd - 1; d >= 0; --d)
+            for (int s = 0; s < 2; ++s) {
+                int g[2], src[2], rule[2];
+                const int np = phase_planes(F, b.n, d, s, g, src, rule);
+                long cnt = 1;
+                for (int t = 0; t < b.nd; ++t)
+                    if (t != d) cnt *= (b.n[t] + 3);
+                for (int q = 0; q < np; ++q) {
+                    if (ni >= kBcMaxItems) return cg_fail(ctx, CG_ERR_ARG, "bc: too many boundary planes");
+                    b.items[ni] = BcItem{fi, d, s, g[q], total};
+                    ++ni;
+                    total += (int)cnt;
+                }
+            }
+    }
+    b.nitems = ni;
+    b.total = total;
+    if (total == 0) return CG_OK;
+    const int threads = 256;
+    bc_apply_kernel<T><<<cg_div_up(total, threads), threads, 0, ctx->stream>>>(b);
+    CG_CHECK_LAUNCH(ctx);
+    return CG_OK;
+}
+
+}  // namespace
+
+int cg_bc_apply_impl(cg_ctx* ctx, const cg_grid* grid, int nfields, const cg_field* fields, const cg_bc* bcs) {
+    int rc = cg_check_grid(ctx, grid);
+    if (rc) return rc;
+    if (nfields < 0 || nfields > kBcMaxFields)
+        return cg_fail(ctx, CG_ERR_ARG, "cg_bc_apply: nfields %d not in 0..%d", nfields, kBcMaxFields);
+    if (nfields == 0) return CG_OK;
+    if (!fields || !bcs) return cg_fail(ctx, CG_ERR_ARG, "cg_bc_apply: NULL fields or bcs");
+    if (grid->ndim >= 2)
+        for (int d = 0; d < grid->ndim; ++d)
+            if (grid->n[d] < 2) return cg_fail(ctx, CG_ERR_ARG, "cg_bc_apply: grid too small");
+    const int dtype = fields[0].dtype;
+    for (int i = 0; i < nfields; ++i) {
+        rc = cg_check_field(ctx, grid, fields[i], dtype, -1, "cg_bc_apply field");
+        if (rc) return rc;
+    }
+    return dtype == CG_F64 ? bc_apply_t<double>(ctx, grid, nfields, fields, bcs)
+                           : bc_apply_t<float>(ctx, grid, nfields, fields, bcs);
+}
+
+extern "C" int cg_bc_apply(cg_ctx* ctx, const cg_grid* grid, int nfields, const cg_field* fields, const cg_bc* bcs) {
+    if (!ctx) return cg_fail(nullptr, CG_ERR_ARG, "cg_bc_apply: ctx is NULL");
+    cudaSetDevice(ctx->device);
+    return cg_bc_apply_impl(ctx, grid, nfields, fields, bcs);
+}
+
+// ---- max-norm over interiors: one launch for up to kRedSlots fields --------------------------
+
+namespace {
+
+constexpr int kMaxRedFields = 16;
+
+struct RedField {
+    const void* p;  // logical index (1,1,1)
+    long s1, s2;
+    int n0, n1, n2;
+    int is64;
+};
+struct RedBatch {
+    int nfields;
+    RedField f[kMaxRedFields];
+};
+
+__device__ __forceinline__ unsigned long long abs_bits(double v) {
+    return (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull;
+}
+__device__ __forceinline__ unsigned long long abs_bits(float v) {
+    return (unsigned long long)((unsigned)__float_as_int(v) & 0x7FFFFFFFu);
+}
+
+__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long w = __shfl_xor_sync(0xFFFFFFFFu, v, o);
+        v = w > v ? w : v;
+    }
+    return v;
+}
+
+// IEEE bit patterns of non-negative values order like the values (NaN above +Inf), so an
+// integer max over |x| bits is the max-norm and propagates NaN.
+__global__ void maxabs_kernel(const RedBatch b, unsigned long long* out) {
+    const RedField F = b.f[blockIdx.y];
+    const long plane = (long)F.n0 * F.n1;
+    const long total = plane * F.n2;
+    unsigned long long m = 0;
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+        const int k = (int)(t / plane);
+        const long r = t - (long)k * plane;
+        const int j = (int)(r / F.n0);
+        const int i = (int)(r - (long)j * F.n0);
+        const long off = i + j * F.s1 + k * F.s2;
+        const unsigned long long v = F.is64 ? abs_bits(static_cast<const double*>(F.p)[off])
+                                            : abs_bits(static_cast<const float*>(F.p)[off]);
+        m = v > m ? v : m;
+    }
+    m = warp_max_u64(m);
+    __shared__ unsigned long long sm[32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) sm[w] = m;
+    __syncthreads();
+    if (w == 0) {
+        m = lane < (int)(blockDim.x >> 5) ? sm[lane] : 0ull;
+        m = warp_max_u64(m);
+        if (lane == 0) atomicMax(out + blockIdx.y, m);
+    }
+}
+
+}  // namespace
+
+// Enqueue the reduction of `nfields` fields into ctx->d_red[0..nfields).
+int cg_maxabs_enqueue(cg_ctx* ctx, int nfields, const cg_field* fields) {
+    if (nfields < 1 || nfields > kMaxRedFields)
+        return cg_fail(ctx, CG_ERR_ARG, "cg_maxabs: nfields %d not in 1..%d", nfields, kMaxRedFields);
+    RedBatch b;
+    std::memset(&b, 0, sizeof(b));
+    b.nfields = nfields;
+    long biggest = 1;
+    for (int i = 0; i < nfields; ++i) {
+        const cg_field& f = fields[i];
+        if (!f.data || (f.dtype != CG_F32 && f.dtype != CG_F64) || f.ndim < 1 || f.ndim > 3)
+            return cg_fail(ctx, CG_ERR_ARG, "cg_maxabs: field %d invalid", i);
+        const int esz = f.dtype == CG_F64 ? 8 : 4;
+        long off = cg_origin_offset(f);
+        for (int d = 0; d < f.ndim; ++d) off += f.stride[d];  // logical index 1 along each dim
+        RedField& R = b.f[i];
+        R.p = static_cast<const char*>(f.data) + off * esz;
+        R.s1 = f.ndim > 1 ? f.stride[1] : 0;
+        R.s2 = f.ndim > 2 ? f.stride[2] : 0;
+        R.n0 = f.n[0];
+        R.n1 = f.ndim > 1 ? f.n[1] : 1;
+        R.n2 = f.ndim > 2 ? f.n[2] : 1;
+        R.is64 = f.dtype == CG_F64;
+        biggest = std::max(biggest, (long)R.n0 * R.n1 * R.n2);
+    }
+    CG_CUDA(ctx, cudaMemsetAsync(ctx->d_red, 0, sizeof(unsigned long long) * nfields, ctx->stream));
+    const int threads = 512;
+    int blocks = (int)std::min<long>(cg_div_up(biggest, threads), (long)ctx->num_sms * 4);
+    blocks = std::max(blocks, 1);
+    maxabs_kernel<<<dim3(blocks, nfields), threads, 0, ctx->stream>>>(b, ctx->d_red);
+    CG_CHECK_LAUNCH(ctx);
+    return CG_OK;
+}
+
+// Copy the reduction slots to the host and decode them.
+int cg_maxabs_collect(cg_ctx* ctx, int nfields, const cg_field* fields, double* out, int32_t* nonfinite) {
+    CG_CUDA(ctx, cudaMemcpyAsync(ctx->h_red, ctx->d_red, sizeof(unsigned long long) * nfields,
+                                 cudaMemcpyDeviceToHost, ctx->stream));
+    CG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    int bad = 0;
+    for (int i = 0; i < nfields; ++i) {
+        const unsigned long long v = ctx->h_red[i];
+        if (fields[i].dtype == CG_F64) {
+            double x;
+            std::memcpy(&x, &v, 8);
+            out[i] = x;
+            if (v >= 0x7FF0000000000000ull) bad = 1;
+        } else {
+            const unsigned u = (unsigned)v;
+            float x;
+            std::memcpy(&x, &u, 4);
+            out[i] = (double)x;
+            if (u >= 0x7F800000u) bad = 1;
+        }
+    }
+    if (nonfinite) *nonfinite = bad;
+    return CG_OK;
+}
+
+extern "C" int cg_maxabs(cg_ctx* ctx, int nfields, const cg_field* fields, double* out_host, int32_t* nonfinite) {
+    if (!ctx) return cg_fail(nullptr, CG_ERR_ARG, "cg_maxabs: ctx is NULL");
+    if (!fields || !out_host) return cg_fail(ctx, CG_ERR_ARG, "cg_maxabs: NULL argument");
+    cudaSetDevice(ctx->device);
+    int rc = cg_maxabs_enqueue(ctx, nfields, fields);
+    if (rc) return rc;
+    return cg_maxabs_collect(ctx, nfields, fields, out_host, nonfinite);
+}

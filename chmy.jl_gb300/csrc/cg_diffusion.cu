@@ -1,0 +1,203 @@
+// cg_diffusion.cu — explicit linear diffusion (Chmy.jl examples/diffusion_2d.jl:8-19).
+#include "cg_common.cuh"
+
+int cg_bc_apply_impl(cg_ctx* ctx, const cg_grid* grid, int nfields, const cg_field* fields, const cg_bc* bcs);
+
+namespace {
+
+template <class T>
+struct Spacing {
+    T i[3];
+};
+
+// Threads cover the launcher range [0, n+1] in x and y; z (3D) is blockIdx.z.
+template <int ND>
+inline dim3 range_grid(const cg_grid* g, dim3 block) {
+    return dim3(cg_div_up(g->n[0] + 2, block.x), ND > 1 ? cg_div_up(g->n[1] + 2, block.y) : 1,
+                ND > 2 ? g->n[2] + 2 : 1);
+}
+
+template <class T, int ND>
+__global__ void compute_q_kernel(DF<T> q0, DF<T> q1, DF<T> q2, DF<T> C, T mchi, Spacing<T> s, int e0, int e1) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = ND > 1 ? blockIdx.y * blockDim.y + threadIdx.y : 0;
+    const int k = ND > 2 ? blockIdx.z : 0;
+    if (i > e0 || j > e1) return;
+    const T c = C(i, j, k);
+    // q.d = -χ * ∂d(C): C is Center, seen from the face: (C[I] - C[I - e_d]) * iΔ_d
+    q0(i, j, k) = mchi * ((c - C(i - 1, j, k)) * s.i[0]);
+    if (ND > 1) q1(i, j, k) = mchi * ((c - C(i, j - 1, k)) * s.i[1]);
+    if (ND > 2) q2(i, j, k) = mchi * ((c - C(i, j, k - 1)) * s.i[2]);
+}
+
+template <class T, int ND>
+__global__ void update_C_kernel(DF<T> C, DF<T> q0, DF<T> q1, DF<T> q2, T dt, Spacing<T> s, int e0, int e1) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = ND > 1 ? blockIdx.y * blockDim.y + threadIdx.y : 0;
+    const int k = ND > 2 ? blockIdx.z : 0;
+    if (i > e0 || j > e1) return;
+    // divg(q) = Σ_d (q_d[I + e_d] - q_d[I]) * iΔ_d, summed in dim order
+    T dv = (q0(i + 1, j, k) - q0(i, j, k)) * s.i[0];
+    if (ND > 1) dv = dv + (q1(i, j + 1, k) - q1(i, j, k)) * s.i[1];
+    if (ND > 2) dv = dv + (q2(i, j, k + 1) - q2(i, j, k)) * s.i[2];
+    C(i, j, k) = C(i, j, k) - dt * dv;
+}
+
+// Fused compute_q! + update_C!: the face fluxes are recomputed from C_in; a face with index
+// n+2 along its dimension is outside compute_q!'s range and reads as zero (fresh q arrays).
+template <class T, int ND>
+__global__ void diffusion_step_kernel(DF<T> Co, DF<T> Ci, T mchi, T dt, Spacing<T> s, int e0, int e1, int e2) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = ND > 1 ? blockIdx.y * blockDim.y + threadIdx.y : 0;
+    const int k = ND > 2 ? blockIdx.z : 0;
+    if (i > e0 || j > e1) return;
+    const T c = Ci(i, j, k);
+    const T qxl = mchi * ((c - Ci(i - 1, j, k)) * s.i[0]);
+    const T qxr = i + 1 <= e0 ? mchi * ((Ci(i + 1, j, k) - c) * s.i[0]) : T(0);
+    T dv = (qxr - qxl) * s.i[0];
+    if (ND > 1) {
+        const T ql = mchi * ((c - Ci(i, j - 1, k)) * s.i[1]);
+        const T qr = j + 1 <= e1 ? mchi * ((Ci(i, j + 1, k) - c) * s.i[1]) : T(0);
+        dv = dv + (qr - ql) * s.i[1];
+    }
+    if (ND > 2) {
+        const T ql = mchi * ((c - Ci(i, j, k - 1)) * s.i[2]);
+        const T qr = k + 1 <= e2 ? mchi * ((Ci(i, j, k + 1) - c) * s.i[2]) : T(0);
+        dv = dv + (qr - ql) * s.i[2];
+    }
+    Co(i, j, k) = c - dt * dv;
+}
+
+template <class T>
+Spacing<T> spacing_of(const cg_grid* g) {
+    Spacing<T> s;
+    for (int d = 0; d < 3; ++d) s.i[d] = (T)g->inv_spacing[d];
+    return s;
+}
+
+inline int field_dtype(const cg_field& f) { return f.dtype; }
+
+int check_q(cg_ctx* ctx, const cg_grid* grid, const cg_field* q, int dtype) {
+    for (int d = 0; d < grid->ndim; ++d) {
+        int rc = cg_check_field(ctx, grid, q[d], dtype, 1 << d, "q");
+        if (rc) return rc;
+    }
+    return CG_OK;
+}
+
+template <class T, int ND>
+int compute_q_t(cg_ctx* ctx, const cg_grid* g, const cg_field* q, const cg_field* C, double chi) {
+    dim3 block(32, 8);
+    DF<T> Q[3] = {cg_view<T>(q[0]), ND > 1 ? cg_view<T>(q[1]) : DF<T>{}, ND > 2 ? cg_view<T>(q[2]) : DF<T>{}};
+    compute_q_kernel<T, ND><<<range_grid<ND>(g, block), block, 0, ctx->stream>>>(
+        Q[0], Q[1], Q[2], cg_view<T>(*C), -(T)chi, spacing_of<T>(g), g->n[0] + 1, ND > 1 ? g->n[1] + 1 : 0);
+    CG_CHECK_LAUNCH(ctx);
+    return CG_OK;
+}
+
+template <class T, int ND>
+int update_C_t(cg_ctx* ctx, const cg_grid* g, const cg_field* C, const cg_field* q, double dt) {
+    dim3 block(32, 8);
+    DF<T> Q[3] = {cg_view<T>(q[0]), ND > 1 ? cg_view<T>(q[1]) : DF<T>{}, ND > 2 ? cg_view<T>(q[2]) : DF<T>{}};
+    update_C_kernel<T, ND><<<range_grid<ND>(g, block), block, 0, ctx->stream>>>(
+        cg_view<T>(*C), Q[0], Q[1], Q[2], (T)dt, spacing_of<T>(g), g->n[0] + 1, ND > 1 ? g->n[1] + 1 : 0);
+    CG_CHECK_LAUNCH(ctx);
+    return CG_OK;
+}
+
+template <class T, int ND>
+int step_t(cg_ctx* ctx, const cg_grid* g, const cg_field* Co, const cg_field* Ci, double chi, double dt) {
+    dim3 block(32, 8);
+    diffusion_step_kernel<T, ND><<<range_grid<ND>(g, block), block, 0, ctx->stream>>>(
+        cg_view<T>(*Co), cg_view<T>(*Ci), -(T)chi, (T)dt, spacing_of<T>(g), g->n[0] + 1,
+        ND > 1 ? g->n[1] + 1 : 0, ND > 2 ? g->n[2] + 1 : 0);
+    CG_CHECK_LAUNCH(ctx);
+    return CG_OK;
+}
+
+template <template <class, int> class Fn, class... A>
+int dispatch(int dtype, int nd, A&&... a);
+
+}  // namespace
+
+#define CG_DISPATCH(fn, dtype, nd, ...)                                                              \
+    ((dtype) == CG_F64 ? ((nd) == 1 ? fn<double, 1>(__VA_ARGS__)                                    \
+                                    : (nd) == 2 ? fn<double, 2>(__VA_ARGS__) : fn<double, 3>(__VA_ARGS__)) \
+                       : ((nd) == 1 ? fn<float, 1>(__VA_ARGS__)                                     \
+                                    : (nd) == 2 ? fn<float, 2>(__VA_ARGS__) : fn<float, 3>(__VA_ARGS__)))
+
+extern "C" int cg_diffusion_compute_q(cg_ctx* ctx, const cg_grid* grid, const cg_field* q, const cg_field* C,
+                                      double chi) {
+    int rc = cg_check_grid(ctx, grid);
+    if (rc) return rc;
+    if (!q || !C) return cg_fail(ctx, CG_ERR_ARG, "cg_diffusion_compute_q: NULL field");
+    cudaSetDevice(ctx->device);
+    if ((rc = cg_check_field(ctx, grid, *C, C->dtype, 0, "C"))) return rc;
+    if ((rc = check_q(ctx, grid, q, C->dtype))) return rc;
+    return CG_DISPATCH(compute_q_t, C->dtype, grid->ndim, ctx, grid, q, C, chi);
+}
+
+extern "C" int cg_diffusion_update_C(cg_ctx* ctx, const cg_grid* grid, const cg_field* C, const cg_field* q,
+                                     double dt) {
+    int rc = cg_check_grid(ctx, grid);
+    if (rc) return rc;
+    if (!q || !C) return cg_fail(ctx, CG_ERR_ARG, "cg_diffusion_update_C: NULL field");
+    cudaSetDevice(ctx->device);
+    if ((rc = cg_check_field(ctx, grid, *C, C->dtype, 0, "C"))) return rc;
+    if ((rc = check_q(ctx, grid, q, C->dtype))) return rc;
+    return CG_DISPATCH(update_C_t, C->dtype, grid->ndim, ctx, grid, C, q, dt);
+}
+
+static int step_checked(cg_ctx* ctx, const cg_grid* grid, const cg_field* Co, const cg_field* Ci, double chi,
+                        double dt, const cg_bc* bc) {
+    int rc = CG_DISPATCH(step_t, Ci->dtype, grid->ndim, ctx, grid, Co, Ci, chi, dt);
+    if (rc) return rc;
+    if (bc) return cg_bc_apply_impl(ctx, grid, 1, Co, bc);
+    return CG_OK;
+}
+
+static int step_args(cg_ctx* ctx, const cg_grid* grid, const cg_field* Co, const cg_field* Ci) {
+    int rc = cg_check_grid(ctx, grid);
+    if (rc) return rc;
+    if (!Co || !Ci) return cg_fail(ctx, CG_ERR_ARG, "diffusion step: NULL field");
+    if ((rc = cg_check_field(ctx, grid, *Ci, Ci->dtype, 0, "C_in"))) return rc;
+    if ((rc = cg_check_field(ctx, grid, *Co, Ci->dtype, 0, "C_out"))) return rc;
+    if (Co->data == Ci->data) return cg_fail(ctx, CG_ERR_ARG, "diffusion step: C_out aliases C_in");
+    return CG_OK;
+}
+
+extern "C" int cg_diffusion_step(cg_ctx* ctx, const cg_grid* grid, const cg_field* C_out, const cg_field* C_in,
+                                 double chi, double dt, const cg_bc* bc) {
+    int rc = step_args(ctx, grid, C_out, C_in);
+    if (rc) return rc;
+    cudaSetDevice(ctx->device);
+    return step_checked(ctx, grid, C_out, C_in, chi, dt, bc);
+}
+
+extern "C" int cg_diffusion_run(cg_ctx* ctx, const cg_grid* grid, const cg_field* A, const cg_field* B, double chi,
+                                double dt, const cg_bc* bc, int nsteps) {
+    int rc = step_args(ctx, grid, B, A);
+    if (rc) return rc;
+    if (nsteps < 0) return cg_fail(ctx, CG_ERR_ARG, "cg_diffusion_run: nsteps < 0");
+    if (nsteps == 0) return CG_OK;
+    cudaSetDevice(ctx->device);
+    std::string key = "diffusion_run";
+    cg_key_add(key, *grid);
+    cg_key_add(key, *A);
+    cg_key_add(key, *B);
+    cg_key_add(key, chi);
+    cg_key_add(key, dt);
+    cg_key_add(key, nsteps);
+    cg_bc none;
+    std::memset(&none, 0, sizeof(none));
+    cg_key_add(key, bc ? *bc : none);
+    return cg_graph_run(ctx, key, [&](cudaStream_t) {
+        for (int s = 0; s < nsteps; ++s) {
+            const cg_field* in = (s % 2 == 0) ? A : B;
+            const cg_field* out = (s % 2 == 0) ? B : A;
+            int r = step_checked(ctx, grid, out, in, chi, dt, bc);
+            if (r) return r;
+        }
+        return (int)CG_OK;
+    });
+}

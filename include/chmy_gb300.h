@@ -1,0 +1,261 @@
+/*
+ * chmy_gb300.h — C ABI of libchmy_gb300.so, the GB300 (sm_103a) implementation of
+ * Chmy.jl's staggered-grid finite-difference hot path.
+ *
+ * Every entry point is `extern "C"`, takes plain pointers, sizes and POD descriptors,
+ * returns an int status (CG_OK = 0) and never throws or aborts. A failing call records a
+ * message retrievable with cg_last_error(). Work is stream-ordered on the context's
+ * stream (cg_set_stream); cg_sync() gives the blocking semantics of Chmy's Launcher,
+ * which synchronizes after every launch (Chmy.jl src/KernelLaunch.jl:117).
+ *
+ * Memory layout (identical to Chmy.Field, src/Fields/field.jl:6-22,56-62): a field of
+ * logical extent n_d per dimension (n cells at Center, n+1 at Vertex, src/Grids/
+ * abstract_axis.jl:47-50) and halo H_d is stored with padded extent n_d + 4 H_d, x fastest.
+ * Logical index I_d (1-based like Julia, valid range 1-2H_d .. n_d+2H_d) lives at element
+ *     data[ sum_d (I_d + 2 H_d - 1) * stride[d] ].
+ * A dense Chmy array has stride = (1, nx+4Hx, (nx+4Hx)(ny+4Hy)); pitched layouts (padded
+ * rows for aligned vector loads) are expressed through larger strides. All kernels need
+ * H_d >= 1 in every used dimension.
+ */
+#ifndef CHMY_GB300_H
+#define CHMY_GB300_H
+
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define CG_API __attribute__((visibility("default")))
+#else
+#define CG_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CG_ABI_VERSION 1
+
+/* ---- status codes --------------------------------------------------------------- */
+enum {
+    CG_OK            = 0,
+    CG_ERR_ARG       = 1, /* bad pointer, size, dtype, location or halo                  */
+    CG_ERR_CUDA      = 2, /* a CUDA runtime call failed (message holds cudaGetErrorString) */
+    CG_ERR_NONFINITE = 3, /* a residual or field contains NaN/Inf                          */
+    CG_ERR_TIMEOUT   = 4, /* a bounded device-side wait ran out                            */
+    CG_ERR_UNSUPPORTED = 5, /* valid request outside what this build implements           */
+    CG_ERR_NOCONV    = 6  /* iterative solve hit its iteration cap before the tolerance   */
+};
+
+/* ---- element types and locations ---------------------------------------------------- */
+enum { CG_F32 = 1, CG_F64 = 2 };
+enum { CG_CENTER = 0, CG_VERTEX = 1 }; /* Chmy.Grids.Center / Vertex (src/Grids/Grids.jl:33,40) */
+
+/* ---- boundary-condition kinds (src/BoundaryConditions/first_order_boundary_condition.jl) */
+enum {
+    CG_BC_NONE      = 0, /* `nothing` in a Chmy batch: side untouched                       */
+    CG_BC_DIRICHLET = 1, /* FirstOrderBC{DirichletKind}, constant value                     */
+    CG_BC_NEUMANN   = 2, /* FirstOrderBC{NeumannKind}, constant flux                        */
+    CG_BC_PERIODIC  = 3  /* ghost <- opposite interior (both sides of a dimension at once)  */
+};
+
+/* A field view. `data` is the start of the padded allocation (see the layout note). */
+typedef struct cg_field {
+    void*   data;
+    int32_t dtype;     /* CG_F32 or CG_F64                                   */
+    int32_t ndim;      /* 1, 2 or 3                                          */
+    int32_t n[3];      /* logical extent per dim (unused dims: 1)            */
+    int32_t loc[3];    /* CG_CENTER / CG_VERTEX per dim                       */
+    int32_t halo[3];   /* H per dim (Chmy default 1; unused dims: 0)          */
+    int32_t pad_;
+    int64_t stride[3]; /* element strides, stride[0] == 1; unused dims: 0     */
+} cg_field;
+
+/* A UniformGrid (src/Grids/structured_grid.jl:27-39, src/Grids/uniform_axis.jl:1-31).
+ * spacing = extent / n and inv_spacing = 1 / spacing are computed by the caller in the
+ * grid's element type (Float32 grids round both to float) and passed here exactly. */
+typedef struct cg_grid {
+    int32_t ndim;
+    int32_t n[3];          /* cells per dim (unused dims: 1) */
+    double  origin[3];
+    double  extent[3];
+    double  spacing[3];
+    double  inv_spacing[3];
+} cg_grid;
+
+/* Boundary conditions of one field: kind and constant value per dimension and side
+ * (side 0 = Side(1) = left, side 1 = Side(2) = right). Dirichlet value `nothing` and
+ * Neumann value `nothing` are 0 (first_order_boundary_condition.jl:34). */
+typedef struct cg_bc {
+    int32_t kind[3][2];
+    double  value[3][2];
+} cg_bc;
+
+typedef struct cg_ctx cg_ctx;
+
+/* ---- context and memory ----------------------------------------------------------- */
+
+/* Library ABI version (CG_ABI_VERSION). */
+CG_API int cg_abi_version(void);
+
+/* Arch(backend; device_id) + activate! (src/Architectures.jl:46-49,71-74): binds the calling
+ * thread to `device` (0-based CUDA ordinal; Chmy's device_id is 1-based) and creates a
+ * context with its own non-blocking stream. */
+CG_API int cg_init(int device, cg_ctx** out);
+CG_API int cg_destroy(cg_ctx* ctx);
+/* Message of the last failing call on `ctx` (or of the last cg_init failure if ctx == NULL). */
+CG_API const char* cg_last_error(const cg_ctx* ctx);
+/* Use `stream` (a cudaStream_t; NULL restores the context's own stream) for later calls. */
+CG_API int cg_set_stream(cg_ctx* ctx, void* stream);
+/* KernelAbstractions.synchronize(backend) (src/KernelLaunch.jl:117). */
+CG_API int cg_sync(cg_ctx* ctx);
+
+/* Field(backend, grid, loc, T; halo) storage (src/Fields/field.jl:56-62): zero-filled,
+ * dense Chmy layout when `pitch_align` is 0, otherwise rows padded so that logical x index
+ * 0 of every row starts on a `pitch_align`-byte boundary (a power of two >= 16). */
+CG_API int cg_field_alloc(cg_ctx* ctx, int dtype, int ndim, const int32_t n[3], const int32_t loc[3],
+                   const int32_t halo[3], int pitch_align, cg_field* out);
+CG_API int cg_field_free(cg_ctx* ctx, cg_field* f);
+/* Copies between a dense host array holding the whole padded field and the device field. */
+CG_API int cg_field_upload(cg_ctx* ctx, const cg_field* f, const void* host_dense);
+CG_API int cg_field_download(cg_ctx* ctx, const cg_field* f, void* host_dense);
+
+/* ---- boundary conditions ---------------------------------------------------------- */
+
+/* bc!(arch, grid, batch) for a FieldBatch of `nfields` fields
+ * (src/BoundaryConditions/batch.jl:104-113,247-268). The result equals Chmy's 2N
+ * per-side launches applied Dim N -> 1, Side 1 then 2, over tangential indices
+ * 0 .. n+2, but runs as ONE launch: each boundary point's final value is evaluated
+ * through its chain of ghost rules. */
+CG_API int cg_bc_apply(cg_ctx* ctx, const cg_grid* grid, int nfields, const cg_field* fields,
+                const cg_bc* bcs);
+
+/* ---- reductions --------------------------------------------------------------------- */
+
+/* maximum(abs.(interior(f))) for each of `nfields` fields, as used by the PT convergence
+ * checks (e.g. examples/stokes_2d_inc_ve_T.jl:155-157). One launch; `out_host[i]` gets the
+ * maximum (NaN if any interior value is NaN); `*nonfinite` is set to 1 if any value is
+ * NaN or Inf. Blocks until the values are on the host. */
+CG_API int cg_maxabs(cg_ctx* ctx, int nfields, const cg_field* fields, double* out_host,
+              int32_t* nonfinite);
+
+/* ---- explicit diffusion (examples/diffusion_2d.jl:8-19, diffusion_2d_perf.jl:11-23) -- */
+
+/* compute_q!: q.d = -chi * d(C)/dx_d at I in [0, n+1]^N. `q` holds ndim face fields. */
+CG_API int cg_diffusion_compute_q(cg_ctx* ctx, const cg_grid* grid, const cg_field* q,
+                           const cg_field* C, double chi);
+/* update_C!: C -= dt * divg(q) at I in [0, n+1]^N. */
+CG_API int cg_diffusion_update_C(cg_ctx* ctx, const cg_grid* grid, const cg_field* C,
+                          const cg_field* q, double dt);
+/* One fused step: C_out = C_in - dt*divg(-chi*grad C_in) over [0, n+1]^N, followed by
+ * bc!(C_out => bc). Equals compute_q! + update_C! + bc! with freshly zeroed q arrays.
+ * C_out and C_in must not alias (ping-pong buffers); their outer halos must match. */
+CG_API int cg_diffusion_step(cg_ctx* ctx, const cg_grid* grid, const cg_field* C_out,
+                      const cg_field* C_in, double chi, double dt, const cg_bc* bc);
+/* `nsteps` fused steps ping-ponging between A and B (result in A if nsteps is even,
+ * else in B), captured once into a CUDA graph and replayed. */
+CG_API int cg_diffusion_run(cg_ctx* ctx, const cg_grid* grid, const cg_field* A, const cg_field* B,
+                     double chi, double dt, const cg_bc* bc, int nsteps);
+
+/* ---- viscoelastic Stokes (examples/stokes_{2,3}d_inc_ve_T.jl) ---------------------- */
+
+/* Field set of the VE Stokes examples. Tensor order: 2D (xx, yy, xy); 3D (xx, yy, zz,
+ * xy, xz, yz) at the TensorField locations of src/Fields/field.jl:182-206.
+ * Optional fields have data == NULL:
+ *   eta      Center viscosity. NULL: scalar params.eta / params.eta_ve, arithmetic exactly
+ *            as in the examples. Present (variable-viscosity extension; the examples have a
+ *            scalar eta), with ieta = 1/eta, inv_Gdt = 1/(G dt), eta_ve = 1/(ieta + inv_Gdt):
+ *              diagonal tau and P use the cell's ieta;
+ *              shear tau uses ieta linearly interpolated (Chmy `lerp` rule) to its edge,
+ *              i.e. the harmonic (`hlerp`-type) average of the surrounding viscosities;
+ *              r_tau = -(tau - tau_old)*inv_Gdt - tau*ieta + 2(eps - divV/3);
+ *              the velocity PT step is V += r_V * (nu_dtau * (min(ieta_l, ieta_r) + inv_Gdt)),
+ *              i.e. nu_dtau / max(eta_ve) of the two cells beside the face.
+ *   inv_eta  Center 1/eta precomputed by the caller (optional; bit-identical to computing
+ *            1/eta in the kernel, saves the divisions).
+ *   rho_g[d] body force subtracted from r_V.d (the examples use only the last component).
+ *   r_V, divV are written every call unless NULL.                                       */
+typedef struct cg_stokes_fields {
+    cg_field V[3];
+    cg_field r_V[3];
+    cg_field P;
+    cg_field divV;
+    cg_field tau[6];
+    cg_field tau_old[6];
+    cg_field eta;
+    cg_field inv_eta;
+    cg_field rho_g[3];
+    cg_field T;
+    cg_field T_old;
+    cg_field qT[3];
+} cg_stokes_fields;
+
+/* Scalars of the PT loop (examples/stokes_2d_inc_ve_T.jl:86-93,142). */
+typedef struct cg_stokes_params {
+    double eta;          /* scalar viscosity (used when fields.eta.data == NULL)       */
+    double eta_ve;       /* 1/(1/eta + 1/(G dt)) (scalar case)                          */
+    double G;
+    double dt;
+    double dtau_Pr;
+    double dtau_r;
+    double nu_dtau;
+    double lambda_rhoCp; /* thermal diffusivity for the thermal kernels                  */
+} cg_stokes_params;
+
+/* update_old!: T_old = T; tau_old = tau at I in [0, n+1]^N. */
+CG_API int cg_stokes_update_old(cg_ctx* ctx, const cg_grid* grid, const cg_stokes_fields* f);
+/* update_stress!: strain rates, divV, P and tau PT update at I in [0, n+1]^N. */
+CG_API int cg_stokes_update_stress(cg_ctx* ctx, const cg_grid* grid, const cg_stokes_fields* f,
+                            const cg_stokes_params* p);
+/* update_velocity!: r_V and V PT update at I in [0, n+1]^N (no bc; see cg_bc_apply). */
+CG_API int cg_stokes_update_velocity(cg_ctx* ctx, const cg_grid* grid, const cg_stokes_fields* f,
+                              const cg_stokes_params* p);
+/* update_thermal_flux! and update_thermal! (examples/stokes_2d_inc_ve_T.jl:45-60). */
+CG_API int cg_stokes_update_thermal_flux(cg_ctx* ctx, const cg_grid* grid,
+                                  const cg_stokes_fields* f, const cg_stokes_params* p);
+CG_API int cg_stokes_update_thermal(cg_ctx* ctx, const cg_grid* grid, const cg_stokes_fields* f,
+                             const cg_stokes_params* p);
+
+/* `niter` PT iterations: update_stress!, update_velocity!, bc!(V => bc_V[d]) each, captured
+ * into a CUDA graph per (fields, niter) and replayed. divV and r_V are written only on the
+ * last iteration (they are only read by the convergence check). */
+CG_API int cg_stokes_pt_iterations(cg_ctx* ctx, const cg_grid* grid, const cg_stokes_fields* f,
+                            const cg_stokes_params* p, const cg_bc* bc_V, int niter);
+
+/* Convergence measures of examples/stokes_2d_inc_ve_T.jl:154-157: applies
+ * bc!(r_V.d => Dirichlet on dim d) and returns err[0] = max|divV| * tau_scale,
+ * err[1 + d] = max|r_V.d| * v_scale. Blocks. */
+CG_API int cg_stokes_residual(cg_ctx* ctx, const cg_grid* grid, const cg_stokes_fields* f,
+                       double tau_scale, double v_scale, double* err_host);
+
+/* PT solve options and result. */
+typedef struct cg_solve_opts {
+    int32_t max_iter;    /* niter                                                        */
+    int32_t ncheck;      /* iterations between convergence checks                         */
+    double  eps;         /* tolerance on every err component                              */
+    double  tau_scale;   /* err[0] = max|divV| * tau_scale                                */
+    double  v_scale;     /* err[1..] = max|r_V| * v_scale                                 */
+    int32_t precision;   /* CG_F64: plain FP64 PT; CG_F32: FP32 PT inside FP64 defect
+                            correction (fields stay FP64; FP32 work arrays are internal)  */
+    int32_t max_outer;   /* defect-correction cycles (precision == CG_F32)                */
+    double  inner_rtol;  /* FP32 inner solve stops at this residual reduction              */
+} cg_solve_opts;
+
+typedef struct cg_solve_result {
+    int32_t iterations;       /* total PT iterations (FP32 + FP64)                         */
+    int32_t outer;            /* defect-correction cycles used                             */
+    int32_t checks;
+    int32_t converged;
+    double  err[4];           /* last FP64 convergence measures                            */
+    double  seconds;          /* device time of the solve (CUDA events)                    */
+} cg_solve_result;
+
+/* Full PT solve of one physical step (examples/stokes_2d_inc_ve_T.jl:144-163) on FP64
+ * fields. Returns CG_ERR_NONFINITE on NaN/Inf, CG_ERR_NOCONV when max_iter is reached. */
+CG_API int cg_stokes_solve(cg_ctx* ctx, const cg_grid* grid, const cg_stokes_fields* f,
+                    const cg_stokes_params* p, const cg_bc* bc_V, const cg_solve_opts* o,
+                    cg_solve_result* res);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CHMY_GB300_H */

@@ -1,0 +1,695 @@
+/*
+ * chmy_oracle.cpp — CPU restatement of Chmy.jl's staggered-grid hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY. This file is the parity oracle: it is loaded by tests/,
+ * by __graft_entry__.smoke() as the checker and by bench.py for the CPU-baseline leg.
+ * The product (libchmy_gb300.so) never links or calls it.
+ *
+ * Every function restates the reference's arithmetic in the reference's operation order;
+ * Julia `muladd` sites use std::fma (Julia lowers muladd to FMA on FMA-capable CPUs) and
+ * everything else is compiled with -ffp-contract=off. Index ranges follow Chmy's Launcher:
+ * kernels run over I in [0, n+1]^N (src/KernelLaunch.jl:41,109) where n = grid cells.
+ *
+ * Parity pin: the grid, field-layout, operator, interpolation and boundary-condition
+ * pieces are checked against the known answers of the reference's own test-suite
+ * (test/test_grids.jl, test_fields.jl, test_grid_operators.jl, test_interpolations.jl,
+ * test_boundary_conditions.jl) by tests/test_oracle_kat.py. The solver kernels (the
+ * examples) have no reference golden vectors (no reference test runs them): they are
+ * pinned by that restated operator layer plus physics self-checks.
+ */
+#include "../include/chmy_gb300.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+/* Field view: element at logical index I is p[off + sum I_d * s_d] (src/Fields/field.jl:18). */
+template <class T>
+struct Fd {
+    T* p = nullptr;
+    int nd = 0;
+    int n[3] = {1, 1, 1};
+    int loc[3] = {0, 0, 0};
+    long off = 0;
+    long s[3] = {0, 0, 0};
+    Fd() = default;
+    explicit Fd(const cg_field& f) {
+        p = static_cast<T*>(f.data);
+        nd = f.ndim;
+        for (int d = 0; d < 3; ++d) {
+            n[d] = d < nd ? f.n[d] : 1;
+            loc[d] = d < nd ? f.loc[d] : 0;
+            s[d] = d < nd ? (long)f.stride[d] : 0;
+            if (d < nd) off += (long)(2 * f.halo[d] - 1) * s[d];
+        }
+    }
+    bool ok() const { return p != nullptr; }
+    T& at(const int* I) const { return p[off + I[0] * s[0] + I[1] * s[1] + I[2] * s[2]]; }
+    T& operator()(int i, int j, int k) const { return p[off + i * s[0] + j * s[1] + k * s[2]]; }
+};
+
+struct Gd {
+    int nd;
+    int n[3];
+};
+
+template <class T>
+struct GridT {
+    int nd;
+    int n[3];
+    T dx[3];
+    T idx[3];
+    explicit GridT(const cg_grid& g) {
+        nd = g.ndim;
+        for (int d = 0; d < 3; ++d) {
+            n[d] = d < nd ? g.n[d] : 1;
+            dx[d] = (T)g.spacing[d];
+            idx[d] = (T)g.inv_spacing[d];
+        }
+    }
+};
+
+/* Loop over the Launcher range [0, n+1] in used dims, {0} in unused ones. */
+template <class G, class F>
+void launch_range(const G& g, F&& fn) {
+    const int e0 = g.n[0] + 1;
+    const int e1 = g.nd > 1 ? g.n[1] + 1 : 0;
+    const int e2 = g.nd > 2 ? g.n[2] + 1 : 0;
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int k = 0; k <= e2; ++k)
+        for (int j = 0; j <= e1; ++j)
+            for (int i = 0; i <= e0; ++i) fn(i, j, k);
+}
+
+/* Loop over the interior-cell range [1, n]^N (sia.jl launches with ws = size(grid, Center())). */
+template <class G, class F>
+void cell_range(const G& g, F&& fn) {
+    const int e0 = g.n[0];
+    const int e1 = g.nd > 1 ? g.n[1] : 0;
+    const int e2 = g.nd > 2 ? g.n[2] : 0;
+    const int b1 = g.nd > 1 ? 1 : 0;
+    const int b2 = g.nd > 2 ? 1 : 0;
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int k = b2; k <= e2; ++k)
+        for (int j = b1; j <= e1; ++j)
+            for (int i = 1; i <= e0; ++i) fn(i, j, k);
+}
+
+/* ---- operators (src/GridOperators/GridOperators.jl:23-38, partial_derivatives.jl) ---- */
+
+/* left/right of a field evaluated from flipped(loc, dim): a Vertex field seen from a
+ * Center point has (I, I+1); a Center field seen from a Vertex point has (I-1, I). */
+template <class T>
+inline T left(const Fd<T>& f, int d, int i, int j, int k) {
+    int I[3] = {i, j, k};
+    if (f.loc[d] == CG_CENTER) I[d] -= 1;
+    return f.at(I);
+}
+template <class T>
+inline T right(const Fd<T>& f, int d, int i, int j, int k) {
+    int I[3] = {i, j, k};
+    if (f.loc[d] == CG_VERTEX) I[d] += 1;
+    return f.at(I);
+}
+/* δ = right - left; ∂ = δ * iΔ (multiply by the inverse spacing, partial_derivatives.jl:2-5). */
+template <class T>
+inline T delta(const Fd<T>& f, int d, int i, int j, int k) {
+    return right(f, d, i, j, k) - left(f, d, i, j, k);
+}
+template <class T>
+inline T partial(const Fd<T>& f, const GridT<T>& g, int d, int i, int j, int k) {
+    return delta(f, d, i, j, k) * g.idx[d];
+}
+
+/* itp(f, to, rule) (src/GridOperators/interpolation.jl:14-56,225-229,262-278): weights 0.5 on
+ * uniform axes; knots split on the LAST differing dimension first, so the first differing
+ * dimension is interpolated innermost. rule 0 = Linear muladd(t, b-a, a); 1 = Harmonic. */
+template <class T>
+T itp_rec(const Fd<T>& f, const int* to, const int* dims, int m, const int* I, int rule) {
+    if (m == 0) return f.at(I);
+    const int d = dims[m - 1];
+    int Il[3] = {I[0], I[1], I[2]}, Ir[3] = {I[0], I[1], I[2]};
+    /* il(loc=from_d, from=to_d): il(Vertex, Center) = I, il(Center, Vertex) = I-1;
+       ir(Vertex, Center) = I+1, ir(Center, Vertex) = I. */
+    if (f.loc[d] == CG_VERTEX) {
+        Ir[d] += 1;
+    } else {
+        Il[d] -= 1;
+    }
+    (void)to;
+    const T a = itp_rec(f, to, dims, m - 1, Il, rule);
+    const T b = itp_rec(f, to, dims, m - 1, Ir, rule);
+    const T t = T(0.5);
+    if (rule == 0) return std::fma(t, b - a, a);
+    const T ia = T(1) / a, ib = T(1) / b;
+    return T(1) / std::fma(t, ib - ia, ia);
+}
+template <class T>
+T itp(const Fd<T>& f, const int* to, int i, int j, int k, int rule) {
+    int dims[3], m = 0;
+    for (int d = 0; d < f.nd; ++d)
+        if (f.loc[d] != to[d]) dims[m++] = d;
+    const int I[3] = {i, j, k};
+    return itp_rec(f, to, dims, m, I, rule);
+}
+
+/* divg(V) = Σ_d ∂(V_d) summed in dim order (field_operators.jl:121-126). */
+template <class T>
+inline T divg(const Fd<T>* V, const GridT<T>& g, int i, int j, int k) {
+    T s = partial(V[0], g, 0, i, j, k);
+    for (int d = 1; d < g.nd; ++d) s = s + partial(V[d], g, d, i, j, k);
+    return s;
+}
+
+/* ∂(f, grid, dim, I) for the field-level entry (from = flipped(loc(f), dim)). */
+template <class T>
+inline T partial_at(const Fd<T>& f, const GridT<T>& g, int d, const int* I) {
+    return partial(f, g, d, I[0], I[1], I[2]);
+}
+
+/* ∂²(f, dim, I) for f at its own location (partial_derivatives.jl:7-12). */
+template <class T>
+T partial2(const Fd<T>& f, const GridT<T>& g, int d, int i, int j, int k) {
+    /* floc = flipped(loc, d); Ir = ir(floc_d, loc_d), Il = il(floc_d, loc_d). */
+    int Il[3] = {i, j, k}, Ir[3] = {i, j, k};
+    if (f.loc[d] == CG_CENTER) {
+        Ir[d] += 1; /* ir(Vertex from Center) = I+1, il(Vertex from Center) = I */
+    } else {
+        Il[d] -= 1; /* ir(Center from Vertex) = I, il(Center from Vertex) = I-1 */
+    }
+    return (partial_at(f, g, d, Ir) - partial_at(f, g, d, Il)) * g.idx[d];
+}
+
+/* ∂k∂(f, k, dim, I) (partial_derivatives.jl:14-21): lerp(k, floc) * ∂f at the two fluxes. */
+template <class T>
+T partial_k_partial(const Fd<T>& f, const Fd<T>& kk, const GridT<T>& g, int d, int i, int j,
+                    int k) {
+    int Il[3] = {i, j, k}, Ir[3] = {i, j, k};
+    if (f.loc[d] == CG_CENTER) {
+        Ir[d] += 1;
+    } else {
+        Il[d] -= 1;
+    }
+    int floc[3] = {f.loc[0], f.loc[1], f.loc[2]};
+    floc[d] = 1 - floc[d];
+    const T kr = itp(kk, floc, Ir[0], Ir[1], Ir[2], 0);
+    const T kl = itp(kk, floc, Il[0], Il[1], Il[2], 0);
+    return (kr * partial_at(f, g, d, Ir) - kl * partial_at(f, g, d, Il)) * g.idx[d];
+}
+
+/* ---- boundary conditions (first_order_boundary_condition.jl:34-84, batch.jl:104-268) -- */
+
+/* Phase (dim d, side s) of one field, applied literally over tangential indices 0..n_t+2
+ * (worksize remove_dim(dim, size(grid, Vertex()) .+ 2), index J-1, batch.jl:243,265). */
+template <class T>
+void bc_phase(const Gd& g, const Fd<T>& f, const cg_bc& bc, int d, int s, T spacing_d) {
+    const int kind = bc.kind[d][s];
+    if (kind == CG_BC_NONE) return;
+    const T val = (T)bc.value[d][s];
+    const int ext = f.n[d]; /* firstindex = 1, lastindex = ext */
+    int tdims[2], nt = 0;
+    for (int t = 0; t < g.nd; ++t)
+        if (t != d) tdims[nt++] = t;
+    const int e0 = nt > 0 ? g.n[tdims[0]] + 2 : 0;
+    const int e1 = nt > 1 ? g.n[tdims[1]] + 2 : 0;
+    for (int b = 0; b <= e1; ++b)
+        for (int a = 0; a <= e0; ++a) {
+            int I[3] = {0, 0, 0};
+            if (nt > 0) I[tdims[0]] = a;
+            if (nt > 1) I[tdims[1]] = b;
+            if (kind == CG_BC_PERIODIC) {
+                /* ghost <- periodic image: Center 0 <- n, n+1 <- 1; Vertex 0 <- n, n+1 <- 1,
+                   n+2 <- 2 (node n+1 is node 1). */
+                const int n = g.n[d];
+                if (s == 0) {
+                    int Is[3] = {I[0], I[1], I[2]};
+                    I[d] = 0;
+                    Is[d] = n;
+                    f.at(I) = f.at(Is);
+                } else {
+                    int Is[3] = {I[0], I[1], I[2]};
+                    I[d] = n + 1;
+                    Is[d] = 1;
+                    f.at(I) = f.at(Is);
+                    if (f.loc[d] == CG_VERTEX) {
+                        I[d] = n + 2;
+                        Is[d] = 2;
+                        f.at(I) = f.at(Is);
+                    }
+                }
+                continue;
+            }
+            if (kind == CG_BC_DIRICHLET && f.loc[d] == CG_VERTEX) {
+                I[d] = s == 0 ? 1 : ext; /* halo_index: the boundary node itself */
+                f.at(I) = val;
+                continue;
+            }
+            const int gi = s == 0 ? 0 : ext + 1;  /* itp_halo_index */
+            const int ni = s == 0 ? 1 : ext;      /* neighbor_index */
+            int In[3] = {I[0], I[1], I[2]};
+            I[d] = gi;
+            In[d] = ni;
+            const T b0 = f.at(In);
+            if (kind == CG_BC_DIRICHLET) {
+                /* Center: muladd(t, a - b, b), t = 2 on a UniformGrid */
+                f.at(I) = std::fma(T(2), val - b0, b0);
+            } else {
+                /* Neumann: muladd(h, ±q, f[in]), minus on Side(1) */
+                const T qs = s == 0 ? -val : val;
+                f.at(I) = std::fma(spacing_d, qs, b0);
+            }
+        }
+}
+
+template <class T>
+int bc_apply_t(const cg_grid* grid, int nfields, const cg_field* fields, const cg_bc* bcs) {
+    Gd g{grid->ndim, {grid->n[0], grid->ndim > 1 ? grid->n[1] : 1, grid->ndim > 2 ? grid->n[2] : 1}};
+    /* batch.jl:104-113: Dim N -> 1, Side(1) then Side(2); within a side, fields in order. */
+    for (int d = g.nd - 1; d >= 0; --d)
+        for (int s = 0; s < 2; ++s)
+            for (int fi = 0; fi < nfields; ++fi) {
+                Fd<T> f(fields[fi]);
+                bc_phase(g, f, bcs[fi], d, s, (T)grid->spacing[d]);
+            }
+    return CG_OK;
+}
+
+/* ---- explicit diffusion (examples/diffusion_2d.jl:8-19) ---------------------------- */
+
+template <class T>
+void diffusion_compute_q_t(const cg_grid* grid, const cg_field* q, const cg_field* C, double chi) {
+    GridT<T> g(*grid);
+    Fd<T> c(*C);
+    Fd<T> Q[3];
+    for (int d = 0; d < g.nd; ++d) Q[d] = Fd<T>(q[d]);
+    const T mchi = -(T)chi;
+    launch_range(g, [&](int i, int j, int k) {
+        for (int d = 0; d < g.nd; ++d) Q[d](i, j, k) = mchi * partial(c, g, d, i, j, k);
+    });
+}
+
+template <class T>
+void diffusion_update_C_t(const cg_grid* grid, const cg_field* C, const cg_field* q, double dt) {
+    GridT<T> g(*grid);
+    Fd<T> c(*C);
+    Fd<T> Q[3];
+    for (int d = 0; d < g.nd; ++d) Q[d] = Fd<T>(q[d]);
+    const T Dt = (T)dt;
+    launch_range(g, [&](int i, int j, int k) { c(i, j, k) = c(i, j, k) - Dt * divg(Q, g, i, j, k); });
+}
+
+/* ---- VE Stokes (examples/stokes_{2,3}d_inc_ve_T.jl) -------------------------------- */
+
+struct Tens {
+    int xx, yy, zz, xy, xz, yz;
+};
+inline Tens tens_index(int nd) {
+    if (nd == 2) return Tens{0, 1, -1, 2, -1, -1};
+    return Tens{0, 1, 2, 3, 4, 5};
+}
+
+template <class T>
+void stokes_update_old_t(const cg_grid* grid, const cg_stokes_fields* f) {
+    GridT<T> g(*grid);
+    const int nt = g.nd == 2 ? 3 : 6;
+    Fd<T> tau[6], tau_old[6];
+    for (int c = 0; c < nt; ++c) {
+        tau[c] = Fd<T>(f->tau[c]);
+        tau_old[c] = Fd<T>(f->tau_old[c]);
+    }
+    Fd<T> Tt(f->T), To(f->T_old);
+    launch_range(g, [&](int i, int j, int k) {
+        if (Tt.ok() && To.ok()) To(i, j, k) = Tt(i, j, k);
+        for (int c = 0; c < nt; ++c) tau_old[c](i, j, k) = tau[c](i, j, k);
+    });
+}
+
+/* Variable-viscosity extension (the examples have a scalar eta): with ieta = 1/eta (cell),
+ * inv_Gdt = 1/(G dt), eta_ve = 1/(ieta + inv_Gdt); shear components use ieta interpolated
+ * with Chmy's Linear rule (a harmonic average of eta); the velocity PT step uses
+ * nu_dtau * (min(ieta_l, ieta_r) + inv_Gdt) = nu_dtau / max(eta_ve_l, eta_ve_r). */
+template <class T>
+struct InvEta {
+    Fd<T> eta, ieta;
+    bool var = false, have_inv = false;
+    explicit InvEta(const cg_stokes_fields* f) : eta(f->eta), ieta(f->inv_eta) {
+        var = eta.ok() || ieta.ok();
+        have_inv = ieta.ok();
+    }
+    T at(int i, int j, int k) const { return have_inv ? ieta(i, j, k) : T(1) / eta(i, j, k); }
+    T at(const int* I) const { return have_inv ? ieta.at(I) : T(1) / eta.at(I); }
+};
+
+template <class T>
+void stokes_update_stress_t(const cg_grid* grid, const cg_stokes_fields* f, const cg_stokes_params* p) {
+    GridT<T> g(*grid);
+    const int nd = g.nd;
+    const Tens ti = tens_index(nd);
+    Fd<T> V[3], tau[6], tau_old[6];
+    for (int d = 0; d < nd; ++d) V[d] = Fd<T>(f->V[d]);
+    const int nt = nd == 2 ? 3 : 6;
+    for (int c = 0; c < nt; ++c) {
+        tau[c] = Fd<T>(f->tau[c]);
+        tau_old[c] = Fd<T>(f->tau_old[c]);
+    }
+    Fd<T> P(f->P), divV(f->divV);
+    const InvEta<T> ie(f);
+    const T G = (T)p->G, dt = (T)p->dt, dtau_Pr = (T)p->dtau_Pr, dtau_r = (T)p->dtau_r;
+    const T eta_s = (T)p->eta, eta_ve_s = (T)p->eta_ve;
+    const T inv_Gdt = T(1) / (G * dt), third = T(1) / T(3);
+    launch_range(g, [&](int i, int j, int k) {
+        const T exx = partial(V[0], g, 0, i, j, k);
+        const T eyy = partial(V[1], g, 1, i, j, k);
+        const T dv = divg(V, g, i, j, k);
+        T dvm = dv;
+        if (divV.ok()) {
+            divV(i, j, k) = dv;
+            dvm = divV(i, j, k);
+        }
+        T ieta_c = 0, eve_c = eta_ve_s;
+        if (ie.var) {
+            ieta_c = ie.at(i, j, k);
+            eve_c = T(1) / (ieta_c + inv_Gdt);
+        }
+        P(i, j, k) = P(i, j, k) - dvm * eve_c * dtau_Pr;
+        auto upd_diag = [&](int c, T edd) {
+            const T t = tau[c](i, j, k), to_ = tau_old[c](i, j, k);
+            T r;
+            if (ie.var)
+                r = -(t - to_) * inv_Gdt - t * ieta_c + T(2.0) * (edd - dvm * third);
+            else  /* examples/stokes_2d_inc_ve_T.jl:28-29 */
+                r = -(t - to_) / (G * dt) - t / eta_s + T(2.0) * (edd - dvm / T(3.0));
+            tau[c](i, j, k) = t + r * eve_c * dtau_r;
+        };
+        auto upd_off = [&](int c, T eod, int a, int b) {
+            const T t = tau[c](i, j, k), to_ = tau_old[c](i, j, k);
+            if (ie.var) {
+                /* ieta at the (a, b) edge: Linear rule over the 4 cells, dim a innermost */
+                int I00[3] = {i, j, k}, I10[3] = {i, j, k}, I01[3] = {i, j, k}, I11[3] = {i, j, k};
+                I00[a] -= 1; I00[b] -= 1;
+                I10[b] -= 1;
+                I01[a] -= 1;
+                const T e00 = ie.at(I00), e10 = ie.at(I10), e01 = ie.at(I01), e11 = ie.at(I11);
+                const T lo = std::fma(T(0.5), e10 - e00, e00);
+                const T hi = std::fma(T(0.5), e11 - e01, e01);
+                const T iev = std::fma(T(0.5), hi - lo, lo);
+                const T eve = T(1) / (iev + inv_Gdt);
+                const T r = -(t - to_) * inv_Gdt - t * iev + T(2.0) * eod;
+                tau[c](i, j, k) = t + r * eve * dtau_r;
+            } else {  /* examples/stokes_2d_inc_ve_T.jl:30 */
+                const T r = -(t - to_) / (G * dt) - t / eta_s + T(2.0) * eod;
+                tau[c](i, j, k) = t + r * eta_ve_s * dtau_r;
+            }
+        };
+        if (nd == 2) {
+            const T exy = T(0.5) * (partial(V[0], g, 1, i, j, k) + partial(V[1], g, 0, i, j, k));
+            upd_diag(ti.xx, exx);
+            upd_diag(ti.yy, eyy);
+            upd_off(ti.xy, exy, 0, 1);
+        } else {
+            const T ezz = partial(V[2], g, 2, i, j, k);
+            const T exy = T(0.5) * (partial(V[0], g, 1, i, j, k) + partial(V[1], g, 0, i, j, k));
+            const T exz = T(0.5) * (partial(V[0], g, 2, i, j, k) + partial(V[2], g, 0, i, j, k));
+            const T eyz = T(0.5) * (partial(V[1], g, 2, i, j, k) + partial(V[2], g, 1, i, j, k));
+            upd_diag(ti.xx, exx);
+            upd_diag(ti.yy, eyy);
+            upd_diag(ti.zz, ezz);
+            upd_off(ti.xy, exy, 0, 1);
+            upd_off(ti.xz, exz, 0, 2);
+            upd_off(ti.yz, eyz, 1, 2);
+        }
+    });
+}
+
+template <class T>
+void stokes_update_velocity_t(const cg_grid* grid, const cg_stokes_fields* f, const cg_stokes_params* p) {
+    GridT<T> g(*grid);
+    const int nd = g.nd;
+    const Tens ti = tens_index(nd);
+    Fd<T> V[3], rV[3], rho[3], tau[6];
+    for (int d = 0; d < nd; ++d) {
+        V[d] = Fd<T>(f->V[d]);
+        rV[d] = Fd<T>(f->r_V[d]);
+        rho[d] = Fd<T>(f->rho_g[d]);
+    }
+    const int nt = nd == 2 ? 3 : 6;
+    for (int c = 0; c < nt; ++c) tau[c] = Fd<T>(f->tau[c]);
+    Fd<T> P(f->P);
+    const InvEta<T> ie(f);
+    const T G = (T)p->G, dt = (T)p->dt, nu_dtau = (T)p->nu_dtau, eta_ve_s = (T)p->eta_ve;
+    const T inv_Gdt = T(1) / (G * dt);
+    /* tensor component coupling momentum d with dimension e */
+    auto comp = [&](int d, int e) -> int {
+        if (d == e) return d == 0 ? ti.xx : (d == 1 ? ti.yy : ti.zz);
+        const int a = std::min(d, e), b = std::max(d, e);
+        if (a == 0 && b == 1) return ti.xy;
+        if (a == 0 && b == 2) return ti.xz;
+        return ti.yz;
+    };
+    launch_range(g, [&](int i, int j, int k) {
+        for (int d = 0; d < nd; ++d) {
+            /* r_V.d = -∂d(P) + ∂d(τ_dd) + Σ_{e≠d} ∂e(τ_de) [- ρg_d], summed left to right in
+               the examples' order: x: (xx, xy, xz); y: (yy, xy, yz); z: (zz, xz, yz). */
+            T r = -partial(P, g, d, i, j, k) + partial(tau[comp(d, d)], g, d, i, j, k);
+            for (int e = 0; e < nd; ++e) {
+                if (e == d) continue;
+                r = r + partial(tau[comp(d, e)], g, e, i, j, k);
+            }
+            if (rho[d].ok()) r = r - rho[d](i, j, k);
+            T rv = r;
+            if (rV[d].ok()) {
+                rV[d](i, j, k) = r;
+                rv = rV[d](i, j, k);
+            }
+            if (ie.var) {
+                int Il[3] = {i, j, k};
+                Il[d] -= 1;
+                const T m = std::min(ie.at(Il), ie.at(i, j, k));
+                V[d](i, j, k) = V[d](i, j, k) + rv * (nu_dtau * (m + inv_Gdt));
+            } else {  /* examples/stokes_2d_inc_ve_T.jl:41-42 */
+                V[d](i, j, k) = V[d](i, j, k) + rv * nu_dtau / eta_ve_s;
+            }
+        }
+    });
+}
+
+template <class T>
+void stokes_update_thermal_flux_t(const cg_grid* grid, const cg_stokes_fields* f, const cg_stokes_params* p) {
+    GridT<T> g(*grid);
+    const int nd = g.nd;
+    Fd<T> V[3], qT[3];
+    for (int d = 0; d < nd; ++d) {
+        V[d] = Fd<T>(f->V[d]);
+        qT[d] = Fd<T>(f->qT[d]);
+    }
+    Fd<T> Tt(f->T);
+    const T lam = (T)p->lambda_rhoCp;
+    launch_range(g, [&](int i, int j, int k) {
+        for (int d = 0; d < nd; ++d) {
+            /* T is Center: leftd(T, I) = T[I - e_d], rightd(T, I) = T[I] */
+            const T v = V[d](i, j, k);
+            qT[d](i, j, k) = -lam * partial(Tt, g, d, i, j, k) + std::max(v, T(0.0)) * left(Tt, d, i, j, k) +
+                             std::min(v, T(0.0)) * right(Tt, d, i, j, k);
+        }
+    });
+}
+
+template <class T>
+void stokes_update_thermal_t(const cg_grid* grid, const cg_stokes_fields* f, const cg_stokes_params* p) {
+    GridT<T> g(*grid);
+    Fd<T> qT[3];
+    for (int d = 0; d < g.nd; ++d) qT[d] = Fd<T>(f->qT[d]);
+    Fd<T> Tt(f->T), To(f->T_old);
+    const T dt = (T)p->dt;
+    launch_range(g, [&](int i, int j, int k) { Tt(i, j, k) = To(i, j, k) - dt * divg(qT, g, i, j, k); });
+}
+
+/* ---- reductions ------------------------------------------------------------------- */
+
+template <class T>
+double maxabs_t(const cg_field& fd, int* nonfinite) {
+    Fd<T> f(fd);
+    double m = 0.0;
+    int bad = 0;
+    const int e1 = f.nd > 1 ? f.n[1] : 1, e2 = f.nd > 2 ? f.n[2] : 1;
+    for (int k = 1; k <= e2; ++k)
+        for (int j = 1; j <= e1; ++j)
+            for (int i = 1; i <= f.n[0]; ++i) {
+                const double v = std::fabs((double)f(i, f.nd > 1 ? j : 0, f.nd > 2 ? k : 0));
+                if (!std::isfinite(v)) bad = 1;
+                if (std::isnan(v)) m = v;
+                else if (!std::isnan(m) && v > m) m = v;
+            }
+    if (bad) *nonfinite = 1;
+    return m;
+}
+
+/* ---- operator test kernels (test/test_grid_operators.jl, test_interpolations.jl) ---- */
+
+/* op 0 divg1!: V.d = ∂d(C) ; op 1 divg2!: C1 = Σ∂(V.d), C2 = divg(V) ;
+ * op 2 lapl!: C1 = Σ∂²(C), C2 = lapl(C) ; op 3 divg_grad1!: V.d = lerp(χ, loc(V.d))·∂d(C) ;
+ * op 4 divg_grad2!: C1 = Σ∂(V.d), C2 = divg_grad(C, χ) ; op 5 vmag: C1 = vmag(V) ;
+ * op 6 lerp: C1 (at its own loc) = lerp(C, loc(C1)) over [1, n_C1]^N (set! discrete range) ;
+ * op 7 hlerp: as 6 with the harmonic rule. */
+template <class T>
+void op_kernel_t(int op, const cg_grid* grid, const cg_field* C, const cg_field* C1, const cg_field* C2,
+                 const cg_field* V, const cg_field* chi) {
+    GridT<T> g(*grid);
+    Fd<T> c, c1, c2, k, v[3];
+    if (C) c = Fd<T>(*C);
+    if (C1) c1 = Fd<T>(*C1);
+    if (C2) c2 = Fd<T>(*C2);
+    if (chi) k = Fd<T>(*chi);
+    if (V)
+        for (int d = 0; d < g.nd; ++d) v[d] = Fd<T>(V[d]);
+    if (op == 6 || op == 7) {
+        const int e1 = c1.nd > 1 ? c1.n[1] : 0, e2 = c1.nd > 2 ? c1.n[2] : 0;
+        for (int kk = c1.nd > 2 ? 1 : 0; kk <= e2; ++kk)
+            for (int j = c1.nd > 1 ? 1 : 0; j <= e1; ++j)
+                for (int i = 1; i <= c1.n[0]; ++i) c1(i, j, kk) = itp(c, c1.loc, i, j, kk, op - 6);
+        return;
+    }
+    launch_range(g, [&](int i, int j, int kk) {
+        switch (op) {
+            case 0:
+                for (int d = 0; d < g.nd; ++d) v[d](i, j, kk) = partial(c, g, d, i, j, kk);
+                break;
+            case 1: {
+                T s = partial(v[0], g, 0, i, j, kk);
+                for (int d = 1; d < g.nd; ++d) s = s + partial(v[d], g, d, i, j, kk);
+                c1(i, j, kk) = s;
+                c2(i, j, kk) = divg(v, g, i, j, kk);
+                break;
+            }
+            case 2: {
+                T s = partial2(c, g, 0, i, j, kk);
+                for (int d = 1; d < g.nd; ++d) s = s + partial2(c, g, d, i, j, kk);
+                c1(i, j, kk) = s;
+                T l = partial2(c, g, 0, i, j, kk);
+                for (int d = 1; d < g.nd; ++d) l = l + partial2(c, g, d, i, j, kk);
+                c2(i, j, kk) = l;
+                break;
+            }
+            case 3:
+                for (int d = 0; d < g.nd; ++d) v[d](i, j, kk) = itp(k, v[d].loc, i, j, kk, 0) * partial(c, g, d, i, j, kk);
+                break;
+            case 4: {
+                T s = partial(v[0], g, 0, i, j, kk);
+                for (int d = 1; d < g.nd; ++d) s = s + partial(v[d], g, d, i, j, kk);
+                c1(i, j, kk) = s;
+                T t = partial_k_partial(c, k, g, 0, i, j, kk);
+                for (int d = 1; d < g.nd; ++d) t = t + partial_k_partial(c, k, g, d, i, j, kk);
+                c2(i, j, kk) = t;
+                break;
+            }
+            case 5: {
+                const int to[3] = {CG_CENTER, CG_CENTER, CG_CENTER};
+                T s = itp(v[0], to, i, j, kk, 0);
+                s = s * s;
+                for (int d = 1; d < g.nd; ++d) {
+                    const T a = itp(v[d], to, i, j, kk, 0);
+                    s = s + a * a;
+                }
+                c1(i, j, kk) = std::sqrt(s);
+                break;
+            }
+            default:
+                break;
+        }
+    });
+}
+
+}  // namespace
+
+/* ==== extern "C" surface (names mirror the library's cg_* entry points) =============== */
+extern "C" {
+
+int or_num_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+void or_set_threads(int n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}
+
+int or_bc_apply(const cg_grid* grid, int nfields, const cg_field* fields, const cg_bc* bcs) {
+    if (nfields <= 0) return CG_OK;
+    if (fields[0].dtype == CG_F64) return bc_apply_t<double>(grid, nfields, fields, bcs);
+    return bc_apply_t<float>(grid, nfields, fields, bcs);
+}
+
+int or_maxabs(int nfields, const cg_field* fields, double* out, int32_t* nonfinite) {
+    int bad = 0;
+    for (int i = 0; i < nfields; ++i)
+        out[i] = fields[i].dtype == CG_F64 ? maxabs_t<double>(fields[i], &bad) : maxabs_t<float>(fields[i], &bad);
+    if (nonfinite) *nonfinite = bad;
+    return CG_OK;
+}
+
+int or_diffusion_compute_q(const cg_grid* grid, const cg_field* q, const cg_field* C, double chi) {
+    if (C->dtype == CG_F64) diffusion_compute_q_t<double>(grid, q, C, chi);
+    else diffusion_compute_q_t<float>(grid, q, C, chi);
+    return CG_OK;
+}
+
+int or_diffusion_update_C(const cg_grid* grid, const cg_field* C, const cg_field* q, double dt) {
+    if (C->dtype == CG_F64) diffusion_update_C_t<double>(grid, C, q, dt);
+    else diffusion_update_C_t<float>(grid, C, q, dt);
+    return CG_OK;
+}
+
+int or_stokes_update_old(const cg_grid* grid, const cg_stokes_fields* f) {
+    if (f->tau[0].dtype == CG_F64) stokes_update_old_t<double>(grid, f);
+    else stokes_update_old_t<float>(grid, f);
+    return CG_OK;
+}
+
+int or_stokes_update_stress(const cg_grid* grid, const cg_stokes_fields* f, const cg_stokes_params* p) {
+    if (f->tau[0].dtype == CG_F64) stokes_update_stress_t<double>(grid, f, p);
+    else stokes_update_stress_t<float>(grid, f, p);
+    return CG_OK;
+}
+
+int or_stokes_update_velocity(const cg_grid* grid, const cg_stokes_fields* f, const cg_stokes_params* p) {
+    if (f->tau[0].dtype == CG_F64) stokes_update_velocity_t<double>(grid, f, p);
+    else stokes_update_velocity_t<float>(grid, f, p);
+    return CG_OK;
+}
+
+int or_stokes_update_thermal_flux(const cg_grid* grid, const cg_stokes_fields* f, const cg_stokes_params* p) {
+    if (f->T.dtype == CG_F64) stokes_update_thermal_flux_t<double>(grid, f, p);
+    else stokes_update_thermal_flux_t<float>(grid, f, p);
+    return CG_OK;
+}
+
+int or_stokes_update_thermal(const cg_grid* grid, const cg_stokes_fields* f, const cg_stokes_params* p) {
+    if (f->T.dtype == CG_F64) stokes_update_thermal_t<double>(grid, f, p);
+    else stokes_update_thermal_t<float>(grid, f, p);
+    return CG_OK;
+}
+
+int or_op_kernel(int op, const cg_grid* grid, const cg_field* C, const cg_field* C1, const cg_field* C2,
+                 const cg_field* V, const cg_field* chi) {
+    const cg_field* any = C ? C : (C1 ? C1 : V);
+    if (any->dtype == CG_F64) op_kernel_t<double>(op, grid, C, C1, C2, V, chi);
+    else op_kernel_t<float>(op, grid, C, C1, C2, V, chi);
+    return CG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,173 @@
+"""Test-side access to the CPU oracle (oracle/liboracle.so) and numpy-backed fields.
+
+Only tests, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this module.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent.parent
+sys.path.insert(0, str(ROOT / "chmy.jl_gb300"))
+sys.path.insert(0, str(ROOT / "oracle"))
+
+from chmy_gb300 import _abi  # noqa: E402
+from chmy_gb300.grids import Center, UniformGrid, Vertex, expand_loc  # noqa: E402
+
+import build as _oracle_build  # noqa: E402  (oracle/build.py)
+
+P = C.POINTER
+_vp = C.c_void_p
+_SIGS = {
+    "or_num_threads": ([], C.c_int),
+    "or_set_threads": ([C.c_int], None),
+    "or_bc_apply": ([P(_abi.cg_grid), C.c_int, P(_abi.cg_field), P(_abi.cg_bc)], C.c_int),
+    "or_maxabs": ([C.c_int, P(_abi.cg_field), P(C.c_double), P(C.c_int32)], C.c_int),
+    "or_diffusion_compute_q": ([P(_abi.cg_grid), P(_abi.cg_field), P(_abi.cg_field), C.c_double], C.c_int),
+    "or_diffusion_update_C": ([P(_abi.cg_grid), P(_abi.cg_field), P(_abi.cg_field), C.c_double], C.c_int),
+    "or_stokes_update_old": ([P(_abi.cg_grid), P(_abi.cg_stokes_fields)], C.c_int),
+    "or_stokes_update_stress": ([P(_abi.cg_grid), P(_abi.cg_stokes_fields), P(_abi.cg_stokes_params)], C.c_int),
+    "or_stokes_update_velocity": ([P(_abi.cg_grid), P(_abi.cg_stokes_fields), P(_abi.cg_stokes_params)], C.c_int),
+    "or_stokes_update_thermal_flux": ([P(_abi.cg_grid), P(_abi.cg_stokes_fields), P(_abi.cg_stokes_params)], C.c_int),
+    "or_stokes_update_thermal": ([P(_abi.cg_grid), P(_abi.cg_stokes_fields), P(_abi.cg_stokes_params)], C.c_int),
+    "or_op_kernel": (
+        [C.c_int, P(_abi.cg_grid), P(_abi.cg_field), P(_abi.cg_field), P(_abi.cg_field), P(_abi.cg_field), P(_abi.cg_field)],
+        C.c_int,
+    ),
+}
+
+_LIB = None
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        path = _oracle_build.build()
+        L = C.CDLL(str(path))
+        for name, (args, res) in _SIGS.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+        _LIB = L
+    return _LIB
+
+
+_CODE = {np.float32: _abi.CG_F32, np.float64: _abi.CG_F64}
+
+
+class NpField:
+    """Host field with Chmy's padded layout, stored [z, y, x] in a numpy array."""
+
+    def __init__(self, grid: UniformGrid, loc, dtype=None, halo=1, fill=0.0):
+        nd = grid.ndim
+        self.grid = grid
+        self.loc = expand_loc(nd, loc)
+        self.dtype = np.dtype(dtype if dtype is not None else grid.dtype).type
+        self.halo = tuple(halo for _ in range(nd)) if isinstance(halo, int) else tuple(halo)
+        self.dims = grid.size(self.loc)
+        self.ext = tuple(n + 4 * h for n, h in zip(self.dims, self.halo))
+        self.a = np.full(tuple(reversed(self.ext)), fill, dtype=self.dtype)
+
+    @property
+    def ndim(self):
+        return len(self.dims)
+
+    def desc(self) -> _abi.cg_field:
+        strides = tuple(s // self.a.itemsize for s in reversed(self.a.strides))
+        return _abi.make_field(
+            self.a.ctypes.data, _CODE[self.dtype], self.dims, tuple(l.code for l in self.loc), self.halo, strides
+        )
+
+    def at(self, *I):
+        """Value at 1-based logical index I (x, y, z)."""
+        idx = tuple(i + 2 * h - 1 for i, h in zip(I, self.halo))
+        return self.a[tuple(reversed(idx))]
+
+    def interior(self, with_halo=False) -> np.ndarray:
+        sl = []
+        for n, h in zip(reversed(self.dims), reversed(self.halo)):
+            lo = 2 * h - (h if with_halo else 0)
+            hi = 2 * h + n + (h if with_halo else 0)
+            sl.append(slice(lo, hi))
+        return self.a[tuple(sl)].transpose(*reversed(range(self.ndim)))
+
+    def copy(self) -> "NpField":
+        g = NpField.__new__(NpField)
+        g.__dict__.update(self.__dict__)
+        g.a = self.a.copy()
+        return g
+
+
+def vec_fields(grid, dtype=None, fill=0.0):
+    nd = grid.ndim
+    return [NpField(grid, tuple(Vertex() if i == d else Center() for i in range(nd)), dtype, fill=fill) for d in range(nd)]
+
+
+def tensor_fields(grid, dtype=None, fill=0.0):
+    C_, V_ = Center(), Vertex()
+    if grid.ndim == 2:
+        locs = [(C_, C_), (C_, C_), (V_, V_)]
+    else:
+        locs = [(C_, C_, C_), (C_, C_, C_), (C_, C_, C_), (V_, V_, C_), (V_, C_, V_), (C_, V_, V_)]
+    return [NpField(grid, l, dtype, fill=fill) for l in locs]
+
+
+def desc_array(fields, n=None):
+    n = n or max(len(fields), 1)
+    arr = (_abi.cg_field * n)()
+    for i, f in enumerate(fields):
+        if f is not None:
+            arr[i] = f.desc()
+    return arr
+
+
+def stokes_desc(V=None, r_V=None, P=None, divV=None, tau=None, tau_old=None, eta=None, inv_eta=None, rho_g=None, T=None, T_old=None, qT=None):
+    s = _abi.cg_stokes_fields()
+    if V is not None:
+        s.V = desc_array(V, 3)
+    if r_V is not None:
+        s.r_V = desc_array(r_V, 3)
+    if P is not None:
+        s.P = P.desc()
+    if divV is not None:
+        s.divV = divV.desc()
+    if tau is not None:
+        s.tau = desc_array(tau, 6)
+    if tau_old is not None:
+        s.tau_old = desc_array(tau_old, 6)
+    if eta is not None:
+        s.eta = eta.desc()
+    if inv_eta is not None:
+        s.inv_eta = inv_eta.desc()
+    if rho_g is not None:
+        s.rho_g = desc_array(rho_g, 3)
+    if T is not None:
+        s.T = T.desc()
+    if T_old is not None:
+        s.T_old = T_old.desc()
+    if qT is not None:
+        s.qT = desc_array(qT, 3)
+    return s
+
+
+def bc_apply(grid, fields, bcs):
+    g = grid.desc()
+    fa = desc_array(fields)
+    ba = (_abi.cg_bc * len(bcs))(*bcs)
+    rc = lib().or_bc_apply(C.byref(g), len(fields), fa, ba)
+    assert rc == 0
+
+
+def op(opcode, grid, Cf=None, C1=None, C2=None, V=None, chi=None):
+    g = grid.desc()
+
+    def ref(f):
+        return C.byref(f.desc()) if f is not None else None
+
+    Va = desc_array(V, 3) if V is not None else None
+    rc = lib().or_op_kernel(opcode, C.byref(g), ref(Cf), ref(C1), ref(C2), Va, ref(chi))
+    assert rc == 0

@@ -1,0 +1,169 @@
+"""GPU parity of the VE Stokes kernels (examples/stokes_{2,3}d_inc_ve_T.jl) against the oracle,
+per launch and over graph-replayed PT iterations, through the C ABI."""
+
+import ctypes
+
+import numpy as np
+import pytest
+
+from _oracle import NpField, bc_apply, lib, stokes_desc, tensor_fields, vec_fields
+from chmy_gb300 import _abi
+from chmy_gb300.bcs import Dirichlet, Neumann, to_cg_bc
+from chmy_gb300.grids import Center, UniformGrid, Vertex
+from chmy_gb300.kernels import stokes_params
+from gpu_helpers import assert_close, random_field, rtol_for, to_gpu
+
+pytestmark = pytest.mark.gpu
+TYPES = [np.float32, np.float64]
+C_, V_ = Center(), Vertex()
+
+
+class StokesSet:
+    """Seeded random VE Stokes state on host and device."""
+
+    def __init__(self, arch, dims, T, seed, var_eta, rho=True, thermal=False):
+        rng = np.random.default_rng(seed)
+        nd = len(dims)
+        self.grid = UniformGrid(origin=(T(-1),) * nd, extent=(T(2),) * nd, dims=dims, dtype=T)
+        g = self.grid
+        self.h = {}
+        self.h["V"] = [random_field(g, f.loc, T, rng) for f in vec_fields(g, T)]
+        self.h["r_V"] = vec_fields(g, T)
+        self.h["P"] = random_field(g, C_, T, rng)
+        self.h["divV"] = NpField(g, C_, T)
+        self.h["tau"] = [random_field(g, f.loc, T, rng, 0.1) for f in tensor_fields(g, T)]
+        self.h["tau_old"] = [random_field(g, f.loc, T, rng, 0.1) for f in tensor_fields(g, T)]
+        if var_eta:
+            e = NpField(g, C_, T)
+            e.a[...] = np.exp(rng.uniform(-3, 3, e.a.shape)).astype(T)
+            self.h["eta"] = e
+        if rho:
+            r = [None] * 3
+            r[nd - 1] = random_field(g, vec_fields(g, T)[nd - 1].loc, T, rng)
+            self.h["rho_g"] = r
+        if thermal:
+            self.h["T"] = random_field(g, C_, T, rng, 1.0, 1.0)
+            self.h["T_old"] = random_field(g, C_, T, rng, 1.0, 1.0)
+            self.h["qT"] = vec_fields(g, T)
+        self.d = {}
+        for k, v in self.h.items():
+            if isinstance(v, list):
+                self.d[k] = [to_gpu(arch, f) if f is not None else None for f in v]
+            else:
+                self.d[k] = to_gpu(arch, v)
+
+    def host_desc(self):
+        return stokes_desc(**self.h)
+
+    def dev_desc(self):
+        return stokes_desc(**self.d)
+
+    def pairs(self):
+        for k, v in self.h.items():
+            if isinstance(v, list):
+                for i, f in enumerate(v):
+                    if f is not None:
+                        yield f"{k}[{i}]", self.d[k][i], f
+            else:
+                yield k, self.d[k], v
+
+
+def pt_params(grid, var_eta):
+    nd = grid.ndim
+    lx = 2.0
+    dx = min(float(s) for s in grid.spacing())
+    re_m, r = 2.3 * np.pi, 0.5
+    lt = lx / re_m
+    vdt = dx / np.sqrt(nd * 1.1)
+    th = lt * (r + 4 / 3) / vdt
+    eta, G, dt = 1.0, 1.0, 1e-2
+    return stokes_params(
+        eta=eta, eta_ve=1.0 / (1.0 / eta + 1.0 / (G * dt)), G=G, dt=dt, dtau_Pr=r / th, dtau_r=1.0 / (th + 1.0), nu_dtau=vdt * lt,
+        lambda_rhoCp=1e-3,
+    )
+
+
+def _compare(s, T, what, scale=1.0):
+    for name, a, b in s.pairs():
+        assert_close(a, b, rtol_for(T) * scale, f"{what}: {name}")
+
+
+@pytest.mark.parametrize("T", TYPES)
+@pytest.mark.parametrize("dims", [(23, 17), (12, 9, 10)])
+@pytest.mark.parametrize("var_eta", [False, True])
+def test_stress_velocity_kernels(arch, T, dims, var_eta):
+    s = StokesSet(arch, dims, T, 17, var_eta)
+    p = pt_params(s.grid, var_eta)
+    g = s.grid.desc()
+    hd, dd = s.host_desc(), s.dev_desc()
+    assert lib().or_stokes_update_stress(ctypes.byref(g), ctypes.byref(hd), ctypes.byref(p)) == 0
+    arch.call("cg_stokes_update_stress", ctypes.byref(g), ctypes.byref(dd), ctypes.byref(p))
+    arch.synchronize()
+    _compare(s, T, "update_stress")
+    assert lib().or_stokes_update_velocity(ctypes.byref(g), ctypes.byref(hd), ctypes.byref(p)) == 0
+    arch.call("cg_stokes_update_velocity", ctypes.byref(g), ctypes.byref(dd), ctypes.byref(p))
+    arch.synchronize()
+    _compare(s, T, "update_velocity")
+
+
+@pytest.mark.parametrize("T", TYPES)
+@pytest.mark.parametrize("dims", [(20, 14), (9, 11, 8)])
+def test_update_old_and_thermal(arch, T, dims):
+    s = StokesSet(arch, dims, T, 23, False, thermal=True)
+    p = pt_params(s.grid, False)
+    g = s.grid.desc()
+    hd, dd = s.host_desc(), s.dev_desc()
+    for name in ("update_thermal_flux", "update_thermal", "update_old"):
+        fo = getattr(lib(), "or_stokes_" + name)
+        if name == "update_old":
+            assert fo(ctypes.byref(g), ctypes.byref(hd)) == 0
+            arch.call("cg_stokes_" + name, ctypes.byref(g), ctypes.byref(dd))
+        else:
+            assert fo(ctypes.byref(g), ctypes.byref(hd), ctypes.byref(p)) == 0
+            arch.call("cg_stokes_" + name, ctypes.byref(g), ctypes.byref(dd), ctypes.byref(p))
+        arch.synchronize()
+        _compare(s, T, name)
+
+
+def _bc_V(nd):
+    bcs = []
+    for d in range(nd):
+        spec = {"xyz"[e]: (Neumann() if e != d else (Dirichlet(0.5), Dirichlet(-0.5))) for e in range(nd)}
+        bcs.append(to_cg_bc(nd, spec))
+    return bcs
+
+
+@pytest.mark.parametrize("T", TYPES)
+@pytest.mark.parametrize("dims", [(31, 26), (13, 12, 11)])
+@pytest.mark.parametrize("var_eta", [False, True])
+def test_pt_iterations_graph(arch, T, dims, var_eta):
+    """cg_stokes_pt_iterations == niter x (update_stress!, update_velocity!, bc!(V)) on the oracle."""
+    s = StokesSet(arch, dims, T, 29, var_eta, rho=True)
+    nd = len(dims)
+    p = pt_params(s.grid, var_eta)
+    g = s.grid.desc()
+    bcs = _bc_V(nd)
+    bc_apply(s.grid, s.h["V"], bcs)
+    for f, d in zip(s.h["V"], s.d["V"]):
+        d.from_numpy(f.a)
+    hd, dd = s.host_desc(), s.dev_desc()
+    niter = 7
+    for _ in range(niter):
+        lib().or_stokes_update_stress(ctypes.byref(g), ctypes.byref(hd), ctypes.byref(p))
+        lib().or_stokes_update_velocity(ctypes.byref(g), ctypes.byref(hd), ctypes.byref(p))
+        bc_apply(s.grid, s.h["V"], bcs)
+    barr = (_abi.cg_bc * 3)(*bcs)
+    arch.call("cg_stokes_pt_iterations", ctypes.byref(g), ctypes.byref(dd), ctypes.byref(p), barr, niter)
+    arch.synchronize()
+    _compare(s, T, "pt_iterations", scale=niter * 10)
+    # residual measures equal the oracle's max-norms after bc!(r_V => Dirichlet)
+    err = (ctypes.c_double * 4)()
+    arch.call("cg_stokes_residual", ctypes.byref(g), ctypes.byref(dd), 1.0, 2.0, err)
+    rb = []
+    for d in range(nd):
+        spec = {"xyz"[d]: Dirichlet()}
+        rb.append(to_cg_bc(nd, spec))
+    bc_apply(s.grid, s.h["r_V"], rb)
+    want = [np.max(np.abs(s.h["divV"].interior()))] + [2.0 * np.max(np.abs(f.interior())) for f in s.h["r_V"]]
+    for i in range(nd + 1):
+        assert abs(err[i] - want[i]) <= rtol_for(T) * niter * 10 * max(abs(want[i]), 1.0)

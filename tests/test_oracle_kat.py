@@ -1,0 +1,353 @@
+"""The CPU oracle against the known answers of Chmy.jl's own test-suite.
+
+Ports test/test_grids.jl, test_fields.jl, test_grid_operators.jl, test_interpolations.jl
+and test_boundary_conditions.jl (TEST_TYPES = [Float32, Float64], test/common.jl:9).
+"""
+
+import json
+import math
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from _oracle import NpField, bc_apply, op, tensor_fields, vec_fields
+from chmy_gb300 import _abi
+from chmy_gb300.bcs import Dirichlet, Neumann, to_cg_bc
+from chmy_gb300.fields import evaluate
+from chmy_gb300.grids import Center, UniformGrid, Vertex
+
+KATS = json.loads((Path(__file__).parent / "golden" / "reference_kats.json").read_text())
+TYPES = [np.float32, np.float64]
+
+
+def approx(a, b, T):
+    tol = 1e-5 if T == np.float32 else 1e-12
+    return np.allclose(np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64), rtol=tol, atol=tol)
+
+
+# ---- test/test_grids.jl -----------------------------------------------------------------------
+
+
+@pytest.mark.parametrize("T", TYPES)
+def test_grid_kats(T):
+    g = KATS["grids"]
+    nx, ny = g["nx"], g["ny"]
+    grid = UniformGrid(origin=tuple(T(o) for o in g["origin"]), extent=tuple(T(e) for e in g["extent"]), dims=(nx, ny), dtype=T)
+    assert grid.size(Center()) == (nx, ny)
+    assert grid.size(Vertex()) == (nx + 1, ny + 1)
+    assert grid.size((Center(), Vertex())) == (nx, ny + 1)
+    assert grid.size((Vertex(), Center())) == (nx + 1, ny)
+    locs = {"Vertex": Vertex(), "Center": Center()}
+    for case in g["cases"]:
+        loc, dim = locs[case["loc"]], case["dim"]
+        fn = case["fn"]
+        if fn == "bounds":
+            got = grid.bounds(loc, dim)
+        elif fn == "extent":
+            got = grid.extent(loc, dim)
+        elif fn == "origin":
+            got = grid.origin(loc, dim)
+        elif fn == "spacing":
+            got = grid.spacing()[dim - 1]
+        elif fn == "inv_spacing":
+            got = grid.inv_spacing()[dim - 1]
+        else:
+            idx = eval(case["index"], {"nx": nx, "ny": ny})
+            got = grid.coord(loc, dim, idx)
+        assert approx(got, case["expected"], T), (case, got)
+    assert grid.dtype == T
+
+
+# ---- test/test_fields.jl ------------------------------------------------------------------------
+
+
+@pytest.mark.parametrize("T", TYPES)
+def test_field_set_kats(T):
+    f = KATS["fields"]
+    grid = UniformGrid(origin=(T(0),) * 3, extent=(T(1),) * 3, dims=(2, 2, 2), dtype=T)
+    loc = (Center(), Vertex(), Center())
+    dims = grid.size(loc)
+    assert dims == (2, 3, 2)
+    funs = [
+        (lambda g, l, ix, iy, iz: g.coord(l, 2, iy), True, ()),
+        (lambda g, l, ix, iy, iz: g.coord(l, 1, ix), True, ()),
+        (lambda g, l, ix, iy, iz, sc: g.coord(l, 2, iy) * sc, True, (T(2.0),)),
+        (lambda x, y, z: y, False, ()),
+        (lambda x, y, z: x, False, ()),
+        (lambda x, y, z, sc: y * sc, False, (T(2.0),)),
+    ]
+    for (fun, discrete, params), case in zip(funs, f["cases"]):
+        got = evaluate(grid, loc, dims, fun, discrete, params, T)
+        want = np.array(case["array_zyx"]).transpose(2, 1, 0)  # -> [x, y, z]
+        assert np.array_equal(got, want.astype(T)), (case["line"], got, want)
+
+
+# ---- test/test_grid_operators.jl ------------------------------------------------------------------
+
+
+def _gauss(grid, f):
+    val = evaluate(grid, f.loc, f.dims, lambda x, y, z: np.exp(-x**2 - y**2 - z**2), False, (), f.dtype)
+    f.interior()[...] = val
+
+
+@pytest.mark.parametrize("T", TYPES)
+def test_divg_lapl_identities(T):
+    grid = UniformGrid(origin=(T(-5),) * 3, extent=(T(10),) * 3, dims=(12, 10, 8), dtype=T)
+    Ci, C1, C2 = (NpField(grid, Center()) for _ in range(3))
+    V = vec_fields(grid)
+    _gauss(grid, Ci)
+    op(0, grid, Cf=Ci, V=V)  # divg1!
+    op(1, grid, C1=C1, C2=C2, V=V)  # divg2!
+    assert np.array_equal(C1.interior(), C2.interior())
+    # independent restatement: V.x[i] = (C[i] - C[i-1]) * iΔx over i in 0..n+1
+    a = Ci.a
+    idx = grid.inv_spacing()
+    vx = V[0].a  # [z, y, x] with halo 1: logical i at index i+1
+    ref = (a[1:-1, 1:-1, 1:-1] - a[1:-1, 1:-1, :-2]) * idx[0]
+    assert np.array_equal(vx[1:-1, 1:-1, 1:-2], ref.astype(T))
+    C1.a[...] = 0
+    C2.a[...] = 0
+    op(2, grid, Cf=Ci, C1=C1, C2=C2)  # lapl!
+    assert np.array_equal(C1.interior(), C2.interior())
+    # ∂²x at Center: ((C[i+1]-C[i])iΔ - (C[i]-C[i-1])iΔ) iΔ
+    c = a.astype(np.float64)
+    lx = ((c[2:-2, 2:-2, 3:-1] - c[2:-2, 2:-2, 2:-2]) * idx[0] - (c[2:-2, 2:-2, 2:-2] - c[2:-2, 2:-2, 1:-3]) * idx[0]) * idx[0]
+    ly = ((c[2:-2, 3:-1, 2:-2] - c[2:-2, 2:-2, 2:-2]) * idx[1] - (c[2:-2, 2:-2, 2:-2] - c[2:-2, 1:-3, 2:-2]) * idx[1]) * idx[1]
+    lz = ((c[3:-1, 2:-2, 2:-2] - c[2:-2, 2:-2, 2:-2]) * idx[2] - (c[2:-2, 2:-2, 2:-2] - c[1:-3, 2:-2, 2:-2]) * idx[2]) * idx[2]
+    assert approx(C1.interior().transpose(2, 1, 0), lx + ly + lz, T)
+
+
+@pytest.mark.parametrize("T", TYPES)
+@pytest.mark.parametrize("chi_loc", ["center", "vertex"])
+def test_divg_grad_identity(T, chi_loc):
+    grid = UniformGrid(origin=(T(-5),) * 3, extent=(T(10),) * 3, dims=(12, 10, 8), dtype=T)
+    Ci, C1, C2 = (NpField(grid, Center()) for _ in range(3))
+    chi = NpField(grid, Center() if chi_loc == "center" else Vertex())
+    V = vec_fields(grid)
+    _gauss(grid, Ci)
+    _gauss(grid, chi)
+    op(3, grid, Cf=Ci, V=V, chi=chi)  # divg_grad1!
+    op(4, grid, Cf=Ci, C1=C1, C2=C2, V=V, chi=chi)  # divg_grad2!
+    # the reference asserts ≈ (test_grid_operators.jl:98,110)
+    assert approx(C1.interior(), C2.interior(), T)
+
+
+@pytest.mark.parametrize("T", TYPES)
+def test_vmag_kat(T):
+    grid = UniformGrid(origin=(T(-5),) * 3, extent=(T(10),) * 3, dims=(12, 10, 8), dtype=T)
+    V = vec_fields(grid)
+    for v in V:
+        v.interior()[...] = T(KATS["vmag"]["value"])
+    C1 = NpField(grid, Center())
+    op(5, grid, C1=C1, V=V)
+    got = C1.interior().astype(np.float64)
+    rounded = np.vectorize(lambda x: float(f"{x:.5g}"))(got)
+    assert np.all(np.isclose(rounded, KATS["vmag"]["expected_sigdigits5"]))
+
+
+# ---- test/test_interpolations.jl ------------------------------------------------------------------
+
+
+def av4(A):
+    return 0.25 * (A[:-1, :-1] + A[1:, :-1] + A[1:, 1:] + A[:-1, 1:])
+
+
+def avx(A):
+    return 0.5 * (A[:-1, :] + A[1:, :])
+
+
+def avy(A):
+    return 0.5 * (A[:, :-1] + A[:, 1:])
+
+
+@pytest.mark.parametrize("T", TYPES)
+def test_interpolation_kats(T):
+    grid = UniformGrid(origin=(T(0), T(0)), extent=(T(1), T(1)), dims=(2, 2), dtype=T)
+    C_, V_ = Center(), Vertex()
+    f_c = NpField(grid, C_)
+    f_c.interior()[...] = np.arange(1, 5).reshape(2, 2, order="F")
+    fci = f_c.interior().astype(np.float64)
+
+    def lerp_to(src, loc):
+        dst = NpField(grid, loc)
+        op(6, grid, Cf=src, C1=dst)
+        return dst.interior().astype(np.float64)
+
+    assert np.allclose(lerp_to(f_c, (V_, V_))[1:-1, 1:-1], av4(fci))
+    assert np.allclose(lerp_to(f_c, (C_, C_)), fci)
+    assert np.allclose(lerp_to(f_c, (C_, V_))[:, 1:-1], avy(fci))
+    assert np.allclose(lerp_to(f_c, (V_, C_))[1:-1, :], avx(fci))
+    f_v = NpField(grid, V_)
+    f_v.interior()[...] = np.arange(1, 10).reshape(3, 3, order="F")
+    fvi = f_v.interior().astype(np.float64)
+    assert np.allclose(lerp_to(f_v, (C_, C_)), av4(fvi))
+    assert np.allclose(lerp_to(f_v, (V_, V_)), fvi)
+    assert np.allclose(lerp_to(f_v, (C_, V_)), avx(fvi))
+    assert np.allclose(lerp_to(f_v, (V_, C_)), avy(fvi))
+
+
+def test_harmonic_rule():
+    # hlerp rule: 1/(1/a + t(1/b - 1/a)) (interpolation.jl:211,297)
+    grid = UniformGrid(origin=(0.0,), extent=(1.0,), dims=(4,))
+    f = NpField(grid, Center())
+    f.interior()[...] = [1.0, 3.0, 2.0, 5.0]
+    dst = NpField(grid, Vertex())
+    op(7, grid, Cf=f, C1=dst)
+    got = dst.interior()[1:-1]
+    want = [1 / (0.5 * (1 / 1 + 1 / 3)), 1 / (0.5 * (1 / 3 + 1 / 2)), 1 / (0.5 * (1 / 2 + 1 / 5))]
+    assert np.allclose(got, want, rtol=1e-15)
+
+
+# ---- test/test_boundary_conditions.jl -------------------------------------------------------------
+
+
+def _bc(grid, f, spec):
+    bc_apply(grid, [f], [to_cg_bc(grid.ndim, spec)])
+    return f.interior(with_halo=True).astype(np.float64)
+
+
+@pytest.mark.parametrize("T", TYPES)
+def test_bc_1d_center(T):
+    grid = UniformGrid(origin=(T(-math.pi),), extent=(T(2 * math.pi),), dims=(8,), dtype=T)
+    f = NpField(grid, Center())
+    f.interior()[...] = 1
+    fi = _bc(grid, f, Dirichlet())
+    assert approx(fi[0], -fi[1], T) and approx(fi[-1], -fi[-2], T)
+    f.interior()[...] = 1
+    fi = _bc(grid, f, Neumann())
+    assert approx(fi[0], fi[1], T) and approx(fi[-1], fi[-2], T)
+    f.interior()[...] = 1
+    fi = _bc(grid, f, Dirichlet(T(2.0)))
+    assert approx(fi[0], -fi[1] + 4, T) and approx(fi[-1], -fi[-2] + 4, T)
+    f.interior()[...] = 1
+    fi = _bc(grid, f, Neumann(T(2.0)))
+    dx = grid.spacing()[0]
+    assert approx((fi[1] - fi[0]) / dx, 2.0, T) and approx((fi[-1] - fi[-2]) / dx, 2.0, T)
+
+
+@pytest.mark.parametrize("T", TYPES)
+def test_bc_1d_vertex(T):
+    grid = UniformGrid(origin=(T(-math.pi),), extent=(T(2 * math.pi),), dims=(8,), dtype=T)
+    f = NpField(grid, Vertex())
+    f.interior()[...] = 1
+    fi = _bc(grid, f, Dirichlet())
+    assert fi[1] == 0 and fi[-2] == 0
+    f.interior()[...] = 1
+    fi = _bc(grid, f, Neumann())
+    assert approx(fi[0], fi[1], T) and approx(fi[-1], fi[-2], T)
+    f.interior()[...] = 1
+    fi = _bc(grid, f, Dirichlet(T(2.0)))
+    assert approx(fi[1], 2.0, T) and approx(fi[-2], 2.0, T)
+    f.interior()[...] = 1
+    fi = _bc(grid, f, Neumann(T(2.0)))
+    dx = grid.spacing()[0]
+    assert approx((fi[1] - fi[0]) / dx, 2.0, T) and approx((fi[-1] - fi[-2]) / dx, 2.0, T)
+
+
+@pytest.mark.parametrize("T", TYPES)
+def test_bc_2d(T):
+    grid = UniformGrid(origin=(T(-math.pi),) * 2, extent=(T(2 * math.pi),) * 2, dims=(8, 8), dtype=T)
+    f = NpField(grid, (Center(), Vertex()))
+    f.interior()[...] = 1
+    fi = _bc(grid, f, Dirichlet())
+    assert approx(fi[0, 1:-1], -fi[1, 1:-1], T) and approx(fi[-1, 1:-1], -fi[-2, 1:-1], T)
+    assert np.all(fi[1:-1, 1] == 0) and np.all(fi[1:-1, -2] == 0)
+    f.interior()[...] = 1
+    fi = _bc(grid, f, Neumann())
+    assert approx(fi[0, 1:-1], fi[1, 1:-1], T) and approx(fi[-1, 1:-1], fi[-2, 1:-1], T)
+    assert approx(fi[1:-1, 0], fi[1:-1, 1], T) and approx(fi[1:-1, -1], fi[1:-1, -2], T)
+    f.interior()[...] = 1
+    fi = _bc(grid, f, Dirichlet(T(2.0)))
+    assert approx(fi[0, 1:-1], -fi[1, 1:-1] + 4, T) and approx(fi[-1, 1:-1], -fi[-2, 1:-1] + 4, T)
+    assert approx(fi[1:-1, 1], 2.0, T) and approx(fi[1:-1, -2], 2.0, T)
+    f.interior()[...] = 1
+    fi = _bc(grid, f, Neumann(T(2.0)))
+    dx, dy = grid.spacing()
+    assert approx((fi[1, 1:-1] - fi[0, 1:-1]) / dx, 2.0, T) and approx((fi[-1, 1:-1] - fi[-2, 1:-1]) / dx, 2.0, T)
+    assert approx((fi[1:-1, 1] - fi[1:-1, 0]) / dy, 2.0, T) and approx((fi[1:-1, -1] - fi[1:-1, -2]) / dy, 2.0, T)
+
+
+@pytest.mark.parametrize("T", TYPES)
+def test_bc_3d(T):
+    grid = UniformGrid(origin=(T(-math.pi),) * 3, extent=(T(2 * math.pi),) * 3, dims=(8, 8, 6), dtype=T)
+    f = NpField(grid, (Center(), Vertex(), Center()))
+    s = slice(1, -1)
+    f.interior()[...] = 1
+    fi = _bc(grid, f, Dirichlet())
+    assert approx(fi[0, s, s], -fi[1, s, s], T) and approx(fi[-1, s, s], -fi[-2, s, s], T)
+    assert np.all(fi[s, 1, s] == 0) and np.all(fi[s, -2, s] == 0)
+    assert approx(fi[s, s, 0], -fi[s, s, 1], T) and approx(fi[s, s, -1], -fi[s, s, -2], T)
+    f.interior()[...] = 1
+    fi = _bc(grid, f, Neumann(T(2.0)))
+    dx, dy, dz = grid.spacing()
+    assert approx((fi[1, s, s] - fi[0, s, s]) / dx, 2.0, T) and approx((fi[-1, s, s] - fi[-2, s, s]) / dx, 2.0, T)
+    assert approx((fi[s, 1, s] - fi[s, 0, s]) / dy, 2.0, T) and approx((fi[s, -1, s] - fi[s, -2, s]) / dy, 2.0, T)
+    assert approx((fi[s, s, 1] - fi[s, s, 0]) / dz, 2.0, T) and approx((fi[s, s, -1] - fi[s, s, -2]) / dz, 2.0, T)
+    f.interior()[...] = 1
+    fi = _bc(grid, f, Dirichlet(T(2.0)))
+    assert approx(fi[s, 1, s], 2.0, T) and approx(fi[s, s, 0], -fi[s, s, 1] + 4, T)
+
+
+def test_bc_order_corners():
+    """Corners follow Chmy's order: Dim N -> 1, so the last dim's rule writes the corner
+    (batch.jl:104-113), reading the value the earlier dims left one step inward."""
+    grid = UniformGrid(origin=(0.0, 0.0), extent=(1.0, 1.0), dims=(4, 5))
+    f = NpField(grid, Center())
+    rng = np.random.default_rng(0)
+    f.a[...] = rng.standard_normal(f.a.shape)
+    before = f.copy()
+    bc_apply(grid, [f], [to_cg_bc(2, {"x": Dirichlet(1.5), "y": Neumann(-0.5)})])
+    # y phase first: f[i,0] = f[i,1] + Δy*0.5 for i in 0..n+2 ; then x: f[0,j] = 2*(1.5 - f[1,j]) + f[1,j]
+    dy = grid.spacing()[1]
+    y0 = before.at(1, 1) + dy * 0.5
+    corner = math.fma(2.0, 1.5 - y0, y0) if hasattr(math, "fma") else 2.0 * (1.5 - y0) + y0
+    assert np.isclose(f.at(0, 0), corner, rtol=0, atol=1e-15)
+
+
+# ---- explicit diffusion restated independently ----------------------------------------------------
+
+
+@pytest.mark.parametrize("T", TYPES)
+def test_diffusion_oracle_matches_numpy(T):
+    from _oracle import lib
+    import ctypes as C
+
+    grid = UniformGrid(origin=(T(-1), T(-1)), extent=(T(2), T(2)), dims=(14, 11), dtype=T)
+    rng = np.random.default_rng(1)
+    Cf = NpField(grid, Center())
+    Cf.a[1:-1, 1:-1] = rng.random((Cf.a.shape[0] - 2, Cf.a.shape[1] - 2)).astype(T)
+    q = vec_fields(grid)
+    chi, dt = T(1.0), T(1e-4)
+    c0 = Cf.a.copy()
+    from _oracle import desc_array
+
+    g = grid.desc()
+    assert lib().or_diffusion_compute_q(C.byref(g), desc_array(q, 3), C.byref(Cf.desc()), float(chi)) == 0
+    assert lib().or_diffusion_update_C(C.byref(g), C.byref(Cf.desc()), desc_array(q, 3), float(dt)) == 0
+    idx, idy = grid.inv_spacing()
+    # numpy: q.x[i] = -χ (C[i]-C[i-1]) iΔ for i in 0..n+1 (array index i+1); q.x[n+2] = 0
+    qx = np.zeros_like(c0)
+    qy = np.zeros((c0.shape[0], c0.shape[1] + 1), dtype=T)
+    qx = np.zeros((c0.shape[0] + 1, c0.shape[1]), dtype=T)  # y-extent n+4, x-extent n+4 for Center in x
+    qxv = np.zeros((c0.shape[0], c0.shape[1] + 1), dtype=T)  # V.x: Vertex in x -> x ext +1
+    qyv = np.zeros((c0.shape[0] + 1, c0.shape[1]), dtype=T)
+    ny, nx = grid.dims[1], grid.dims[0]
+    for j in range(0, ny + 2):
+        for i in range(0, nx + 2):
+            qxv[j + 1, i + 1] = (-chi) * ((c0[j + 1, i + 1] - c0[j + 1, i]) * idx)
+            qyv[j + 1, i + 1] = (-chi) * ((c0[j + 1, i + 1] - c0[j, i + 1]) * idy)
+    assert np.array_equal(q[0].a, qxv) and np.array_equal(q[1].a, qyv)
+    c1 = c0.copy()
+    for j in range(0, ny + 2):
+        for i in range(0, nx + 2):
+            dv = (qxv[j + 1, i + 2] - qxv[j + 1, i + 1]) * idx + (qyv[j + 2, i + 1] - qyv[j + 1, i + 1]) * idy
+            c1[j + 1, i + 1] = c0[j + 1, i + 1] - dt * dv
+    assert np.array_equal(Cf.a, c1)
+
+
+def test_cg_bc_struct_roundtrip():
+    b = to_cg_bc(3, {"x": Dirichlet(1.0), "z": (Neumann(2.0), None)})
+    assert b.kind[0][0] == _abi.CG_BC_DIRICHLET and b.value[0][1] == 1.0
+    assert b.kind[1][0] == _abi.CG_BC_NONE and b.kind[2][1] == _abi.CG_BC_NONE
+    assert b.kind[2][0] == _abi.CG_BC_NEUMANN and b.value[2][0] == 2.0
