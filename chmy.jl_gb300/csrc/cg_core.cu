@@ -33,7 +33,9 @@ extern "C" int cg_init(int device, cg_ctx** out) {
     cg_ctx* ctx = new cg_ctx();
     ctx->device = device;
     cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
-    e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
+    // a blocking stream: ordered with work on the legacy default stream (e.g. host-side
+    // copies issued by PyTorch or CUDA.jl) without extra synchronisation
+    e = cudaStreamCreate(&ctx->own_stream);
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_red, sizeof(unsigned long long) * cg_ctx::kRedSlots);
     if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_red, sizeof(unsigned long long) * cg_ctx::kRedSlots);
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev0);

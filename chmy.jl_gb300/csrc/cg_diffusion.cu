@@ -10,7 +10,13 @@ struct Spacing {
     T i[3];
 };
 
-// Threads cover the launcher range [0, n+1] in x and y; z (3D) is blockIdx.z.
+// Threads cover the launcher range [0, n+1] in x and y; z (3D) is blockIdx.z. 1D launches use
+// a flat block so that no two threads own the same point.
+template <int ND>
+inline dim3 block_for() {
+    return ND == 1 ? dim3(256, 1) : dim3(32, 8);
+}
+
 template <int ND>
 inline dim3 range_grid(const cg_grid* g, dim3 block) {
     return dim3(cg_div_up(g->n[0] + 2, block.x), ND > 1 ? cg_div_up(g->n[1] + 2, block.y) : 1,
@@ -87,7 +93,7 @@ int check_q(cg_ctx* ctx, const cg_grid* grid, const cg_field* q, int dtype) {
 
 template <class T, int ND>
 int compute_q_t(cg_ctx* ctx, const cg_grid* g, const cg_field* q, const cg_field* C, double chi) {
-    dim3 block(32, 8);
+    const dim3 block = block_for<ND>();
     DF<T> Q[3] = {cg_view<T>(q[0]), ND > 1 ? cg_view<T>(q[1]) : DF<T>{}, ND > 2 ? cg_view<T>(q[2]) : DF<T>{}};
     compute_q_kernel<T, ND><<<range_grid<ND>(g, block), block, 0, ctx->stream>>>(
         Q[0], Q[1], Q[2], cg_view<T>(*C), -(T)chi, spacing_of<T>(g), g->n[0] + 1, ND > 1 ? g->n[1] + 1 : 0);
@@ -97,7 +103,7 @@ int compute_q_t(cg_ctx* ctx, const cg_grid* g, const cg_field* q, const cg_field
 
 template <class T, int ND>
 int update_C_t(cg_ctx* ctx, const cg_grid* g, const cg_field* C, const cg_field* q, double dt) {
-    dim3 block(32, 8);
+    const dim3 block = block_for<ND>();
     DF<T> Q[3] = {cg_view<T>(q[0]), ND > 1 ? cg_view<T>(q[1]) : DF<T>{}, ND > 2 ? cg_view<T>(q[2]) : DF<T>{}};
     update_C_kernel<T, ND><<<range_grid<ND>(g, block), block, 0, ctx->stream>>>(
         cg_view<T>(*C), Q[0], Q[1], Q[2], (T)dt, spacing_of<T>(g), g->n[0] + 1, ND > 1 ? g->n[1] + 1 : 0);
@@ -107,7 +113,7 @@ int update_C_t(cg_ctx* ctx, const cg_grid* g, const cg_field* C, const cg_field*
 
 template <class T, int ND>
 int step_t(cg_ctx* ctx, const cg_grid* g, const cg_field* Co, const cg_field* Ci, double chi, double dt) {
-    dim3 block(32, 8);
+    const dim3 block = block_for<ND>();
     diffusion_step_kernel<T, ND><<<range_grid<ND>(g, block), block, 0, ctx->stream>>>(
         cg_view<T>(*Co), cg_view<T>(*Ci), -(T)chi, (T)dt, spacing_of<T>(g), g->n[0] + 1,
         ND > 1 ? g->n[1] + 1 : 0, ND > 2 ? g->n[2] + 1 : 0);
