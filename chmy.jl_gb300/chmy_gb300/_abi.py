@@ -128,6 +128,20 @@ class cg_solve_result(C.Structure):
     ]
 
 
+class cg_sia_params(C.Structure):
+    _fields_ = [
+        ("Gamma", C.c_double),
+        ("As", C.c_double),
+        ("n", C.c_int32),
+        ("pad_", C.c_int32),
+        ("beta", C.c_double),
+        ("ela", C.c_double),
+        ("m_max", C.c_double),
+        ("dt_max", C.c_double),
+        ("cfl", C.c_double),
+    ]
+
+
 P = C.POINTER
 _vp = C.c_void_p
 
@@ -165,6 +179,9 @@ SIGNATURES: dict[str, list] = {
         P(cg_solve_opts),
         P(cg_solve_result),
     ],
+    "cg_sia_update_q": [_vp, P(cg_grid), P(cg_field), P(cg_field), P(cg_field), P(cg_sia_params), P(C.c_double)],
+    "cg_sia_update_H": [_vp, P(cg_grid), P(cg_field), P(cg_field), P(cg_field), C.c_double, P(cg_sia_params)],
+    "cg_sia_run": [_vp, P(cg_grid), P(cg_field), P(cg_field), P(cg_field), P(cg_sia_params), C.c_int, P(C.c_double)],
 }
 _RESTYPES = {"cg_last_error": C.c_char_p}
 

@@ -32,7 +32,15 @@ struct cg_ctx {
     // FP32 work arrays of the defect-correction solver (allocated on first use)
     void* dc_pool = nullptr;
     size_t dc_pool_bytes = 0;
+    // numbered scratch buffers of the time-stepping loops (grown on demand, freed by cg_destroy)
+    static constexpr int kScratchSlots = 4;
+    void* scratch[kScratchSlots] = {nullptr, nullptr, nullptr, nullptr};
+    size_t scratch_bytes[kScratchSlots] = {0, 0, 0, 0};
 };
+
+// Device scratch buffer `slot` of at least `bytes` (reallocated when too small; contents are
+// not preserved across growth). Sets *rc on failure and returns NULL.
+void* cg_scratch(cg_ctx* ctx, int slot, size_t bytes, int* rc);
 
 // Record an error message on ctx and return `code`.
 int cg_fail(cg_ctx* ctx, int code, const char* fmt, ...);

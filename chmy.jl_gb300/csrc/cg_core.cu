@@ -57,6 +57,8 @@ extern "C" int cg_destroy(cg_ctx* ctx) {
     for (auto& g : ctx->graphs)
         if (g.exec) cudaGraphExecDestroy(g.exec);
     if (ctx->dc_pool) cudaFree(ctx->dc_pool);
+    for (int s = 0; s < cg_ctx::kScratchSlots; ++s)
+        if (ctx->scratch[s]) cudaFree(ctx->scratch[s]);
     if (ctx->d_red) cudaFree(ctx->d_red);
     if (ctx->h_red) cudaFreeHost(ctx->h_red);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
@@ -64,6 +66,28 @@ extern "C" int cg_destroy(cg_ctx* ctx) {
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     delete ctx;
     return CG_OK;
+}
+
+void* cg_scratch(cg_ctx* ctx, int slot, size_t bytes, int* rc) {
+    *rc = CG_OK;
+    if (slot < 0 || slot >= cg_ctx::kScratchSlots) {
+        *rc = cg_fail(ctx, CG_ERR_ARG, "scratch slot %d out of range", slot);
+        return nullptr;
+    }
+    if (ctx->scratch_bytes[slot] >= bytes) return ctx->scratch[slot];
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e == cudaSuccess && ctx->scratch[slot]) e = cudaFree(ctx->scratch[slot]);
+    ctx->scratch[slot] = nullptr;
+    ctx->scratch_bytes[slot] = 0;
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->scratch[slot], bytes);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ctx->scratch[slot], 0, bytes, ctx->stream);
+    if (e != cudaSuccess) {
+        ctx->scratch[slot] = nullptr;
+        *rc = cg_fail(ctx, CG_ERR_CUDA, "scratch allocation of %zu bytes: %s", bytes, cudaGetErrorString(e));
+        return nullptr;
+    }
+    ctx->scratch_bytes[slot] = bytes;
+    return ctx->scratch[slot];
 }
 
 extern "C" int cg_set_stream(cg_ctx* ctx, void* stream) {

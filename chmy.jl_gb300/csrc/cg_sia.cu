@@ -1,0 +1,296 @@
+// cg_sia.cu — shallow-ice flow (Chmy.jl examples/sia.jl:7-16,30-54,71-81).
+#include "cg_common.cuh"
+
+int cg_bc_apply_impl(cg_ctx* ctx, const cg_grid* grid, int nfields, const cg_field* fields, const cg_bc* bcs);
+int cg_maxabs_collect(cg_ctx* ctx, int nfields, const cg_field* fields, double* out, int32_t* nonfinite);
+void* cg_scratch(cg_ctx* ctx, int slot, size_t bytes, int* rc);
+
+namespace {
+
+template <class T>
+struct SiaV {
+    DF<T> H, B, qx, qy, D;
+    T Gamma, As, beta, ela, m_max;
+    T idx, idy;
+    int n;
+};
+
+template <class T>
+__device__ __forceinline__ T ipow(T x, int m) {
+    if (m <= 0) return T(1);
+    T r = x;
+    for (int k = 1; k < m; ++k) r = r * x;
+    return r;
+}
+
+template <class T>
+__device__ __forceinline__ T S_at(const SiaV<T>& v, int i, int j) {
+    return v.B(i, j, 0) + v.H(i, j, 0);
+}
+
+// D = (Gamma H^(n+2) + As H^n) vmag(∇S)^(n-1) at cell (i, j) (sia.jl:43-49)
+template <class T>
+__device__ __forceinline__ T D_at(const SiaV<T>& v, int i, int j) {
+    const T s = S_at(v, i, j);
+    const T a0 = (s - S_at(v, i - 1, j)) * v.idx;
+    const T a1 = (S_at(v, i + 1, j) - s) * v.idx;
+    const T b0 = (s - S_at(v, i, j - 1)) * v.idy;
+    const T b1 = (S_at(v, i, j + 1) - s) * v.idy;
+    const T ax = fma(T(0.5), a1 - a0, a0);
+    const T ay = fma(T(0.5), b1 - b0, b0);
+    const T vm = sqrt(ax * ax + ay * ay);
+    const T h = v.H(i, j, 0);
+    return (v.Gamma * ipow(h, v.n + 2) + v.As * ipow(h, v.n)) * ipow(vm, v.n - 1);
+}
+
+__device__ __forceinline__ unsigned long long bits_of(double d) { return (unsigned long long)__double_as_longlong(d); }
+__device__ __forceinline__ unsigned long long bits_of(float f) { return (unsigned long long)(unsigned)__float_as_int(f); }
+
+// update_q! over [1, n]^2 with D evaluated on the fly (the reference's FunctionField);
+// optional max(interior D) into *dmax_bits (D >= 0, so the bit patterns order like values).
+template <class T>
+__global__ void sia_q_kernel(const SiaV<T> v, int nx, int ny, unsigned long long* dmax_bits) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    if (i > nx || j > ny) return;
+    const T dc = D_at(v, i, j), dl = D_at(v, i - 1, j), dd = D_at(v, i, j - 1);
+    const T Dx = fma(T(0.5), dc - dl, dl);
+    const T Dy = fma(T(0.5), dc - dd, dd);
+    const T sc = S_at(v, i, j);
+    v.qx(i, j, 0) = -Dx * ((sc - S_at(v, i - 1, j)) * v.idx);
+    v.qy(i, j, 0) = -Dy * ((sc - S_at(v, i, j - 1)) * v.idy);
+    if (dmax_bits) atomicMax(dmax_bits, bits_of(dc));
+}
+
+// D over cells [0, n]^2 into v.D and max over the interior [1, n]^2.
+template <class T>
+__global__ void sia_D_kernel(const SiaV<T> v, int nx, int ny, unsigned long long* dmax_bits) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i > nx || j > ny) return;
+    const T d = D_at(v, i, j);
+    v.D(i, j, 0) = d;
+    if (i >= 1 && j >= 1) atomicMax(dmax_bits, bits_of(d));
+}
+
+// update_q! from the precomputed D (same arithmetic as sia_q_kernel).
+template <class T>
+__global__ void sia_q_from_D_kernel(const SiaV<T> v, int nx, int ny) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    if (i > nx || j > ny) return;
+    const T dc = v.D(i, j, 0), dl = v.D(i - 1, j, 0), dd = v.D(i, j - 1, 0);
+    const T Dx = fma(T(0.5), dc - dl, dl);
+    const T Dy = fma(T(0.5), dc - dd, dd);
+    const T sc = S_at(v, i, j);
+    v.qx(i, j, 0) = -Dx * ((sc - S_at(v, i - 1, j)) * v.idx);
+    v.qy(i, j, 0) = -Dy * ((sc - S_at(v, i, j - 1)) * v.idy);
+}
+
+// update_H! over [1, n]^2; dt from a scalar or from device memory.
+template <class T>
+__global__ void sia_H_kernel(const SiaV<T> v, int nx, int ny, T dt_scalar, const double* dt_dev) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    if (i > nx || j > ny) return;
+    const T dt = dt_dev ? (T)*dt_dev : dt_scalar;
+    const T h = v.H(i, j, 0);
+    const T m = fmin(v.beta * (S_at(v, i, j) - v.ela), v.m_max);
+    T dv = (v.qx(i + 1, j, 0) - v.qx(i, j, 0)) * v.idx;
+    dv = dv + (v.qy(i, j + 1, 0) - v.qy(i, j, 0)) * v.idy;
+    v.H(i, j, 0) = fmax(h + dt * (-dv + m), T(0.0));
+}
+
+// Δt = min(min(Δ)^2 / max(D) / cfl, dt_max); t += Δt; reset the max slot for the next step.
+template <class T>
+__global__ void sia_dt_kernel(unsigned long long* dmax_bits, double* dt, double* t, double dx2, double cfl,
+                              double dt_max) {
+    const unsigned long long b = *dmax_bits;
+    double dmax;
+    if (sizeof(T) == 8) {
+        dmax = __longlong_as_double((long long)b);
+    } else {
+        dmax = (double)__int_as_float((int)(unsigned)b);
+    }
+    // Julia: Δ^2 / maximum(D) / 4.1 in the grid type
+    const T v = (T)dx2 / (T)dmax / (T)cfl;
+    double d = fmin((double)v, dt_max);
+    if (!(dmax > 0.0)) d = dt_max;
+    *dt = d;
+    *t = *t + d;
+    *dmax_bits = 0ull;
+}
+
+template <class T>
+SiaV<T> make_view(const cg_grid* g, const cg_field* H, const cg_field* B, const cg_field* q, const cg_sia_params* p,
+                  void* D) {
+    SiaV<T> v;
+    std::memset(&v, 0, sizeof(v));
+    v.H = cg_view<T>(*H);
+    v.B = cg_view<T>(*B);
+    if (q) {
+        v.qx = cg_view<T>(q[0]);
+        v.qy = cg_view<T>(q[1]);
+    }
+    if (D) {
+        v.D = v.H;  // same layout as H
+        v.D.p = static_cast<T*>(D) + cg_origin_offset(*H);
+    }
+    v.Gamma = (T)p->Gamma;
+    v.As = (T)p->As;
+    v.beta = (T)p->beta;
+    v.ela = (T)p->ela;
+    v.m_max = (T)p->m_max;
+    v.idx = (T)g->inv_spacing[0];
+    v.idy = (T)g->inv_spacing[1];
+    v.n = p->n;
+    return v;
+}
+
+int check_sia(cg_ctx* ctx, const cg_grid* g, const cg_field* H, const cg_field* B, const cg_field* q,
+              const cg_sia_params* p) {
+    int rc = cg_check_grid(ctx, g);
+    if (rc) return rc;
+    if (g->ndim != 2) return cg_fail(ctx, CG_ERR_UNSUPPORTED, "sia: 2D grids only");
+    if (!H || !B || !p) return cg_fail(ctx, CG_ERR_ARG, "sia: NULL argument");
+    if ((rc = cg_check_field(ctx, g, *H, H->dtype, 0, "H"))) return rc;
+    if ((rc = cg_check_field(ctx, g, *B, H->dtype, 0, "B"))) return rc;
+    if (q) {
+        if ((rc = cg_check_field(ctx, g, q[0], H->dtype, 1, "q.x"))) return rc;
+        if ((rc = cg_check_field(ctx, g, q[1], H->dtype, 2, "q.y"))) return rc;
+    }
+    if (p->n < 1 || p->n > 16) return cg_fail(ctx, CG_ERR_ARG, "sia: Glen exponent %d not in 1..16", p->n);
+    return CG_OK;
+}
+
+void sia_bcs(cg_bc* qb, cg_bc* hb) {
+    std::memset(qb, 0, 2 * sizeof(cg_bc));
+    qb[0].kind[0][0] = qb[0].kind[0][1] = CG_BC_DIRICHLET;
+    qb[1].kind[1][0] = qb[1].kind[1][1] = CG_BC_DIRICHLET;
+    std::memset(hb, 0, sizeof(cg_bc));
+    hb->kind[0][0] = hb->kind[0][1] = hb->kind[1][0] = hb->kind[1][1] = CG_BC_NEUMANN;
+}
+
+template <class T>
+int update_q_t(cg_ctx* ctx, const cg_grid* g, const cg_field* q, const cg_field* H, const cg_field* B,
+               const cg_sia_params* p, double* dmax) {
+    const SiaV<T> v = make_view<T>(g, H, B, q, p, nullptr);
+    const dim3 block(32, 8), grid(cg_div_up(g->n[0], 32), cg_div_up(g->n[1], 8));
+    if (dmax) CG_CUDA(ctx, cudaMemsetAsync(ctx->d_red, 0, sizeof(unsigned long long), ctx->stream));
+    sia_q_kernel<T><<<grid, block, 0, ctx->stream>>>(v, g->n[0], g->n[1], dmax ? ctx->d_red : nullptr);
+    CG_CHECK_LAUNCH(ctx);
+    cg_bc qb[2], hb;
+    sia_bcs(qb, &hb);
+    int rc = cg_bc_apply_impl(ctx, g, 2, q, qb);
+    if (rc) return rc;
+    if (dmax) {
+        cg_field probe = *H;  // dtype of the reduction slot
+        double m;
+        return cg_maxabs_collect(ctx, 1, &probe, &m, nullptr) ? CG_ERR_CUDA : ((*dmax = m), CG_OK);
+    }
+    return CG_OK;
+}
+
+template <class T>
+int update_H_t(cg_ctx* ctx, const cg_grid* g, const cg_field* H, const cg_field* q, const cg_field* B, double dt,
+               const cg_sia_params* p) {
+    const SiaV<T> v = make_view<T>(g, H, B, q, p, nullptr);
+    const dim3 block(32, 8), grid(cg_div_up(g->n[0], 32), cg_div_up(g->n[1], 8));
+    sia_H_kernel<T><<<grid, block, 0, ctx->stream>>>(v, g->n[0], g->n[1], (T)dt, nullptr);
+    CG_CHECK_LAUNCH(ctx);
+    cg_bc qb[2], hb;
+    sia_bcs(qb, &hb);
+    return cg_bc_apply_impl(ctx, g, 1, H, &hb);
+}
+
+template <class T>
+int run_t(cg_ctx* ctx, const cg_grid* g, const cg_field* H, const cg_field* B, const cg_field* q,
+          const cg_sia_params* p, int nsteps, double* t_host) {
+    // scratch: D (same padded layout as H) + 3 words (max bits, dt, t)
+    long cnt = 1;
+    for (int d = 0; d < 2; ++d) cnt *= (H->n[d] + 4L * H->halo[d]);
+    cnt = std::max<long>(cnt, (long)H->stride[1] * (H->n[1] + 4L * H->halo[1]));
+    int rc = CG_OK;
+    char* base = static_cast<char*>(cg_scratch(ctx, 1, cnt * sizeof(T) + 256 + 64, &rc));
+    if (rc) return rc;
+    unsigned long long* words = reinterpret_cast<unsigned long long*>(base + ((cnt * sizeof(T) + 255) & ~255L));
+    double* dt = reinterpret_cast<double*>(words + 1);
+    double* t = reinterpret_cast<double*>(words + 2);
+    CG_CUDA(ctx, cudaMemsetAsync(words, 0, 3 * sizeof(unsigned long long), ctx->stream));
+    const SiaV<T> v = make_view<T>(g, H, B, q, p, base);
+    const int nx = g->n[0], ny = g->n[1];
+    const dim3 block(32, 8);
+    const dim3 gD(cg_div_up(nx + 1, 32), cg_div_up(ny + 1, 8)), gI(cg_div_up(nx, 32), cg_div_up(ny, 8));
+    const double dx = std::min(g->spacing[0], g->spacing[1]);
+    const double dx2 = (double)((T)dx * (T)dx);
+    cg_bc qb[2], hb;
+    sia_bcs(qb, &hb);
+    std::string key = "sia_run";
+    cg_key_add(key, *g);
+    cg_key_add(key, *H);
+    cg_key_add(key, *B);
+    cg_key_add(key, q[0]);
+    cg_key_add(key, q[1]);
+    cg_key_add(key, *p);
+    cg_key_add(key, nsteps);
+    cg_key_add(key, base);
+    rc = cg_graph_run(ctx, key, [&](cudaStream_t st) {
+        for (int s = 0; s < nsteps; ++s) {
+            sia_D_kernel<T><<<gD, block, 0, st>>>(v, nx, ny, words);
+            sia_q_from_D_kernel<T><<<gI, block, 0, st>>>(v, nx, ny);
+            CG_CHECK_LAUNCH(ctx);
+            int r = cg_bc_apply_impl(ctx, g, 2, q, qb);
+            if (r) return r;
+            sia_dt_kernel<T><<<1, 1, 0, st>>>(words, dt, t, dx2, p->cfl, p->dt_max);
+            sia_H_kernel<T><<<gI, block, 0, st>>>(v, nx, ny, T(0), dt);
+            CG_CHECK_LAUNCH(ctx);
+            r = cg_bc_apply_impl(ctx, g, 1, H, &hb);
+            if (r) return r;
+        }
+        return (int)CG_OK;
+    });
+    if (rc) return rc;
+    if (t_host) {
+        CG_CUDA(ctx, cudaMemcpyAsync(t_host, t, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        CG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    return CG_OK;
+}
+
+}  // namespace
+
+extern "C" int cg_sia_update_q(cg_ctx* ctx, const cg_grid* grid, const cg_field* q, const cg_field* H,
+                               const cg_field* B, const cg_sia_params* p, double* dmax_host) {
+    int rc = check_sia(ctx, grid, H, B, q, p);
+    if (rc) return rc;
+    if (!q) return cg_fail(ctx, CG_ERR_ARG, "sia_update_q: q is NULL");
+    cudaSetDevice(ctx->device);
+    return H->dtype == CG_F64 ? update_q_t<double>(ctx, grid, q, H, B, p, dmax_host)
+                              : update_q_t<float>(ctx, grid, q, H, B, p, dmax_host);
+}
+
+extern "C" int cg_sia_update_H(cg_ctx* ctx, const cg_grid* grid, const cg_field* H, const cg_field* q,
+                               const cg_field* B, double dt, const cg_sia_params* p) {
+    int rc = check_sia(ctx, grid, H, B, q, p);
+    if (rc) return rc;
+    if (!q) return cg_fail(ctx, CG_ERR_ARG, "sia_update_H: q is NULL");
+    cudaSetDevice(ctx->device);
+    return H->dtype == CG_F64 ? update_H_t<double>(ctx, grid, H, q, B, dt, p)
+                              : update_H_t<float>(ctx, grid, H, q, B, dt, p);
+}
+
+extern "C" int cg_sia_run(cg_ctx* ctx, const cg_grid* grid, const cg_field* H, const cg_field* B, const cg_field* q,
+                          const cg_sia_params* p, int nsteps, double* t_host) {
+    int rc = check_sia(ctx, grid, H, B, q, p);
+    if (rc) return rc;
+    if (!q) return cg_fail(ctx, CG_ERR_ARG, "sia_run: q is NULL");
+    if (nsteps < 0) return cg_fail(ctx, CG_ERR_ARG, "sia_run: nsteps < 0");
+    if (p->cfl <= 0 || p->dt_max <= 0) return cg_fail(ctx, CG_ERR_ARG, "sia_run: cfl and dt_max must be > 0");
+    cudaSetDevice(ctx->device);
+    if (nsteps == 0) {
+        if (t_host) *t_host = 0.0;
+        return CG_OK;
+    }
+    return H->dtype == CG_F64 ? run_t<double>(ctx, grid, H, B, q, p, nsteps, t_host)
+                              : run_t<float>(ctx, grid, H, B, q, p, nsteps, t_host);
+}

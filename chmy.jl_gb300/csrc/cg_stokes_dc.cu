@@ -1,0 +1,440 @@
+// cg_stokes_dc.cu — VE Stokes PT solve with FP32 pseudo-transient iterations inside an FP64
+// defect-correction loop.
+//
+// Outer loop (FP64): the defect kernel evaluates the true residuals of the current FP64
+// state — continuity R_P = divV, constitutive R_tau and momentum R_V — and the convergence
+// measures of examples/stokes_2d_inc_ve_T.jl:154-157. The residuals are folded into the
+// FP32 inputs of the UNCHANGED PT kernels: tau_old' = G dt R_tau (the constitutive residual
+// of the correction then carries +R_tau), rho_g' = -R_V (the momentum residual carries
+// +R_V) and a continuity forcing fP = R_P.
+// Inner loop (FP32): PT iterations on the correction (dV, dP, dtau) from zero with
+// homogeneous boundary conditions (same kinds, zero values), graph-replayed, until the
+// FP32 measures fall below max(0.5 eps, inner_rtol * outer measure) or stagnate.
+// Update (FP64): V += dV, P += dP, tau += dtau, then bc!(V).
+#include "cg_stokes_kernels.cuh"
+
+int cg_bc_apply_impl(cg_ctx* ctx, const cg_grid* grid, int nfields, const cg_field* fields, const cg_bc* bcs);
+int cg_maxabs_enqueue(cg_ctx* ctx, int nfields, const cg_field* fields);
+int cg_maxabs_collect(cg_ctx* ctx, int nfields, const cg_field* fields, double* out, int32_t* nonfinite);
+
+namespace {
+using namespace cgk;
+
+struct DC32 {
+    DF<float> fP, told[6], rho[3];
+};
+
+// FP64 residuals of the current state; FP32 forcing of the correction problem.
+template <int ND>
+__global__ void defect_kernel(const SV<double> v, const SP<double> s, const DC32 w, int e0, int e1) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = ND > 2 ? blockIdx.z : 0;
+    if (i > e0 || j > e1) return;
+    const DF<double>& Vx = v.V[0];
+    const DF<double>& Vy = v.V[1];
+    const double exx = (Vx(i + 1, j, k) - Vx(i, j, k)) * s.idx[0];
+    const double eyy = (Vy(i, j + 1, k) - Vy(i, j, k)) * s.idx[1];
+    double dv = exx + eyy, ezz = 0.0;
+    if (ND > 2) {
+        ezz = (v.V[2](i, j, k + 1) - v.V[2](i, j, k)) * s.idx[2];
+        dv = dv + ezz;
+    }
+    v.divV(i, j, k) = dv;
+    w.fP(i, j, k) = (float)dv;
+    const double Gdt = s.G * s.dt;
+    double ieta_c = 0.0;
+    if (v.has_eta) ieta_c = v.inv_eta(i, j, k);
+    auto diag = [&](int c, double edd) {
+        const double t = v.tau[c](i, j, k), to = v.tau_old[c](i, j, k);
+        double r;
+        if (v.has_eta)
+            r = -(t - to) * s.inv_Gdt - t * ieta_c + 2.0 * (edd - dv * s.third);
+        else
+            r = -(t - to) / Gdt - t / s.eta + 2.0 * (edd - dv / 3.0);
+        w.told[c](i, j, k) = (float)(Gdt * r);
+    };
+    auto shear = [&](int c, double eod, int a, int b) {
+        const double t = v.tau[c](i, j, k), to = v.tau_old[c](i, j, k);
+        double r;
+        if (v.has_eta) {
+            const int ai = a == 0, aj = a == 1, ak = a == 2;
+            const int bi = b == 0, bj = b == 1, bk = b == 2;
+            const double e00 = v.inv_eta(i - ai - bi, j - aj - bj, k - ak - bk);
+            const double e10 = v.inv_eta(i - bi, j - bj, k - bk);
+            const double e01 = v.inv_eta(i - ai, j - aj, k - ak);
+            const double e11 = v.inv_eta(i, j, k);
+            const double lo = fma(0.5, e10 - e00, e00);
+            const double hi = fma(0.5, e11 - e01, e01);
+            const double iev = fma(0.5, hi - lo, lo);
+            r = -(t - to) * s.inv_Gdt - t * iev + 2.0 * eod;
+        } else {
+            r = -(t - to) / Gdt - t / s.eta + 2.0 * eod;
+        }
+        w.told[c](i, j, k) = (float)(Gdt * r);
+    };
+    const double exy = 0.5 * ((Vx(i, j, k) - Vx(i, j - 1, k)) * s.idx[1] + (Vy(i, j, k) - Vy(i - 1, j, k)) * s.idx[0]);
+    if (ND == 2) {
+        diag(0, exx);
+        diag(1, eyy);
+        shear(2, exy, 0, 1);
+    } else {
+        const DF<double>& Vz = v.V[2];
+        const double exz = 0.5 * ((Vx(i, j, k) - Vx(i, j, k - 1)) * s.idx[2] + (Vz(i, j, k) - Vz(i - 1, j, k)) * s.idx[0]);
+        const double eyz = 0.5 * ((Vy(i, j, k) - Vy(i, j, k - 1)) * s.idx[2] + (Vz(i, j, k) - Vz(i, j - 1, k)) * s.idx[1]);
+        diag(0, exx);
+        diag(1, eyy);
+        diag(2, ezz);
+        shear(3, exy, 0, 1);
+        shear(4, exz, 0, 2);
+        shear(5, eyz, 1, 2);
+    }
+    // momentum residuals at the faces of index I
+    const DF<double>& P = v.P;
+    const int XY = ND == 2 ? 2 : 3;
+    const DF<double>& txx = v.tau[0];
+    const DF<double>& tyy = v.tau[1];
+    const DF<double>& txy = v.tau[XY];
+    double rx = -((P(i, j, k) - P(i - 1, j, k)) * s.idx[0]) + (txx(i, j, k) - txx(i - 1, j, k)) * s.idx[0];
+    rx = rx + (txy(i, j + 1, k) - txy(i, j, k)) * s.idx[1];
+    double ry = -((P(i, j, k) - P(i, j - 1, k)) * s.idx[1]) + (tyy(i, j, k) - tyy(i, j - 1, k)) * s.idx[1];
+    ry = ry + (txy(i + 1, j, k) - txy(i, j, k)) * s.idx[0];
+    double rz = 0.0;
+    if (ND > 2) {
+        const DF<double>& tzz = v.tau[2];
+        const DF<double>& txz = v.tau[4];
+        const DF<double>& tyz = v.tau[5];
+        rx = rx + (txz(i, j, k + 1) - txz(i, j, k)) * s.idx[2];
+        ry = ry + (tyz(i, j, k + 1) - tyz(i, j, k)) * s.idx[2];
+        rz = -((P(i, j, k) - P(i, j, k - 1)) * s.idx[2]) + (tzz(i, j, k) - tzz(i, j, k - 1)) * s.idx[2];
+        rz = rz + (txz(i + 1, j, k) - txz(i, j, k)) * s.idx[0];
+        rz = rz + (tyz(i, j + 1, k) - tyz(i, j, k)) * s.idx[1];
+    }
+    if (v.has_rho[0]) rx = rx - v.rho[0](i, j, k);
+    if (v.has_rho[1]) ry = ry - v.rho[1](i, j, k);
+    if (ND > 2 && v.has_rho[2]) rz = rz - v.rho[2](i, j, k);
+    v.rV[0](i, j, k) = rx;
+    v.rV[1](i, j, k) = ry;
+    w.rho[0](i, j, k) = (float)(-rx);
+    w.rho[1](i, j, k) = (float)(-ry);
+    if (ND > 2) {
+        v.rV[2](i, j, k) = rz;
+        w.rho[2](i, j, k) = (float)(-rz);
+    }
+}
+
+// dst += src over whole padded arrays (logical -1 .. n+2 with H = 1), one launch for a table.
+constexpr int kMaxUpd = 10;
+struct UpdItem {
+    DF<double> dst;
+    DF<float> src;
+    int n0, n1, n2;  // padded extents (n + 4)
+};
+struct UpdTable {
+    int count;
+    UpdItem it[kMaxUpd];
+};
+
+__global__ void update_kernel(const UpdTable t) {
+    const UpdItem u = t.it[blockIdx.y];
+    const long plane = (long)u.n0 * u.n1;
+    const long total = plane * u.n2;
+    for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (long)gridDim.x * blockDim.x) {
+        const int k = (int)(q / plane);
+        const long r = q - (long)k * plane;
+        const int j = (int)(r / u.n0);
+        const int i = (int)(r - (long)j * u.n0);
+        // logical index = padded index - 1 in every used dim
+        const int li = i - 1, lj = u.n1 > 1 ? j - 1 : 0, lk = u.n2 > 1 ? k - 1 : 0;
+        double* d = u.dst.ptr(li, lj, lk);
+        *d = *d + (double)u.src(li, lj, lk);
+    }
+}
+
+struct Work {
+    cg_field dV[3], dP, dtau[6], told[6], fP, rho[3], ieta, divV, rV[3];
+};
+
+// FP32 dense field like `f` (same extents, locations, halo 1).
+cg_field like32(const cg_field& f, char*& cursor, size_t& bytes, bool dry) {
+    cg_field g;
+    std::memset(&g, 0, sizeof(g));
+    g.dtype = CG_F32;
+    g.ndim = f.ndim;
+    long ext[3] = {1, 1, 1};
+    for (int d = 0; d < 3; ++d) {
+        g.n[d] = f.n[d];
+        g.loc[d] = f.loc[d];
+        g.halo[d] = d < f.ndim ? 1 : 0;
+        if (d < f.ndim) ext[d] = f.n[d] + 4;
+    }
+    g.stride[0] = 1;
+    g.stride[1] = f.ndim > 1 ? ext[0] : 0;
+    g.stride[2] = f.ndim > 2 ? ext[0] * ext[1] : 0;
+    const size_t sz = ((size_t)ext[0] * ext[1] * ext[2] * 4 + 255) & ~(size_t)255;
+    if (!dry) g.data = cursor;
+    cursor += sz;
+    bytes += sz;
+    return g;
+}
+
+int make_work(cg_ctx* ctx, const cg_stokes_fields* f, int nd, Work* w) {
+    const int nt = nd == 2 ? 3 : 6;
+    for (int pass = 0; pass < 2; ++pass) {
+        const bool dry = pass == 0;
+        char* cur = dry ? nullptr : static_cast<char*>(ctx->dc_pool);
+        size_t bytes = 0;
+        for (int d = 0; d < nd; ++d) {
+            w->dV[d] = like32(f->V[d], cur, bytes, dry);
+            w->rho[d] = like32(f->V[d], cur, bytes, dry);
+            w->rV[d] = like32(f->V[d], cur, bytes, dry);
+        }
+        w->dP = like32(f->P, cur, bytes, dry);
+        w->fP = like32(f->P, cur, bytes, dry);
+        w->ieta = like32(f->P, cur, bytes, dry);
+        w->divV = like32(f->P, cur, bytes, dry);
+        for (int c = 0; c < nt; ++c) {
+            w->dtau[c] = like32(f->tau[c], cur, bytes, dry);
+            w->told[c] = like32(f->tau[c], cur, bytes, dry);
+        }
+        if (dry && bytes > ctx->dc_pool_bytes) {
+            if (ctx->dc_pool) {
+                CG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+                CG_CUDA(ctx, cudaFree(ctx->dc_pool));
+                ctx->dc_pool = nullptr;
+                ctx->dc_pool_bytes = 0;
+            }
+            CG_CUDA(ctx, cudaMalloc(&ctx->dc_pool, bytes));
+            CG_CUDA(ctx, cudaMemsetAsync(ctx->dc_pool, 0, bytes, ctx->stream));
+            ctx->dc_pool_bytes = bytes;
+        }
+    }
+    return CG_OK;
+}
+
+size_t padded_count(const cg_field& f) {
+    size_t c = 1;
+    for (int d = 0; d < f.ndim; ++d) c *= (size_t)(f.n[d] + 4);
+    return c;
+}
+
+__global__ void reciprocal_kernel(float* dst, const double* src, long dst_s1, long dst_s2, long src_s1, long src_s2,
+                                  int n0, int n1, int n2) {
+    const long plane = (long)n0 * n1;
+    const long total = plane * n2;
+    for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (long)gridDim.x * blockDim.x) {
+        const int k = (int)(q / plane);
+        const long r = q - (long)k * plane;
+        const int j = (int)(r / n0);
+        const int i = (int)(r - (long)j * n0);
+        dst[i + j * dst_s1 + k * dst_s2] = (float)(1.0 / src[i + j * src_s1 + k * src_s2]);
+    }
+}
+
+}  // namespace
+
+int cg_stokes_solve_dc(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f, const cg_stokes_params* p,
+                       const cg_bc* bc_V, const cg_solve_opts* o, cg_solve_result* res) {
+    const int nd = g->ndim;
+    const int nt = nd == 2 ? 3 : 6;
+    for (int d = 0; d < nd; ++d)
+        if (f->V[d].halo[d] != 1) return cg_fail(ctx, CG_ERR_UNSUPPORTED, "stokes_solve (FP32): halo 1 fields only");
+    for (int c = 0; c < nt; ++c)
+        if (f->tau[c].halo[0] != 1) return cg_fail(ctx, CG_ERR_UNSUPPORTED, "stokes_solve (FP32): halo 1 fields only");
+    if (f->P.halo[0] != 1) return cg_fail(ctx, CG_ERR_UNSUPPORTED, "stokes_solve (FP32): halo 1 fields only");
+    Work w;
+    int rc = make_work(ctx, f, nd, &w);
+    if (rc) return rc;
+    std::memset(res, 0, sizeof(*res));
+    CG_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
+
+    // FP32 1/eta (and its use flag) for the correction operator
+    const bool var = cg_present(f->eta) || cg_present(f->inv_eta);
+    if (var) {
+        const cg_field& e = cg_present(f->eta) ? f->eta : f->inv_eta;
+        const int n0 = e.n[0] + 4, n1 = nd > 1 ? e.n[1] + 4 : 1, n2 = nd > 2 ? e.n[2] + 4 : 1;
+        if (cg_present(f->eta)) {
+            reciprocal_kernel<<<ctx->num_sms * 4, 256, 0, ctx->stream>>>(
+                static_cast<float*>(w.ieta.data), static_cast<const double*>(e.data), w.ieta.stride[1], w.ieta.stride[2],
+                e.stride[1], e.stride[2], n0, n1, n2);
+        } else {
+            return cg_fail(ctx, CG_ERR_UNSUPPORTED, "stokes_solve (FP32): pass eta (inv_eta alone is not enough)");
+        }
+        CG_CHECK_LAUNCH(ctx);
+    }
+
+    // FP64 views of the state and FP32 views of the correction
+    SV<double> v64 = views<double>(f, nd);
+    v64.has_rV = 1;
+    v64.has_divV = 1;
+    const SP<double> s64 = scalars<double>(g, p);
+    DC32 d32;
+    std::memset(&d32, 0, sizeof(d32));
+    d32.fP = cg_view<float>(w.fP);
+    for (int c = 0; c < nt; ++c) d32.told[c] = cg_view<float>(w.told[c]);
+    for (int d = 0; d < nd; ++d) d32.rho[d] = cg_view<float>(w.rho[d]);
+
+    cg_stokes_fields f32;
+    std::memset(&f32, 0, sizeof(f32));
+    for (int d = 0; d < nd; ++d) {
+        f32.V[d] = w.dV[d];
+        f32.r_V[d] = w.rV[d];
+        f32.rho_g[d] = w.rho[d];
+    }
+    f32.P = w.dP;
+    f32.divV = w.divV;
+    for (int c = 0; c < nt; ++c) {
+        f32.tau[c] = w.dtau[c];
+        f32.tau_old[c] = w.told[c];
+    }
+    if (var) f32.inv_eta = w.ieta;
+    SV<float> v32 = views<float>(&f32, nd);
+    v32.fP = cg_view<float>(w.fP);
+    v32.has_fP = 1;
+    const SP<float> s32 = scalars<float>(g, p);
+
+    cg_bc bc0[3];
+    for (int d = 0; d < nd; ++d) {
+        bc0[d] = bc_V ? bc_V[d] : cg_bc{};
+        for (int a = 0; a < 3; ++a) bc0[d].value[a][0] = bc0[d].value[a][1] = 0.0;
+    }
+    cg_field red64[4], red32[4];
+    red64[0] = f->divV;
+    red32[0] = w.divV;
+    for (int d = 0; d < nd; ++d) {
+        red64[1 + d] = f->r_V[d];
+        red32[1 + d] = w.rV[d];
+    }
+    cg_bc rbc[3];
+    std::memset(rbc, 0, sizeof(rbc));
+    for (int d = 0; d < nd; ++d) rbc[d].kind[d][0] = rbc[d].kind[d][1] = CG_BC_DIRICHLET;
+
+    UpdTable upd;
+    std::memset(&upd, 0, sizeof(upd));
+    auto add_upd = [&](const cg_field& dst, const cg_field& src) {
+        UpdItem& u = upd.it[upd.count++];
+        u.dst = cg_view<double>(dst);
+        u.src = cg_view<float>(src);
+        u.n0 = dst.n[0] + 4;
+        u.n1 = nd > 1 ? dst.n[1] + 4 : 1;
+        u.n2 = nd > 2 ? dst.n[2] + 4 : 1;
+    };
+    for (int d = 0; d < nd; ++d) add_upd(f->V[d], w.dV[d]);
+    add_upd(f->P, w.dP);
+    for (int c = 0; c < nt; ++c) add_upd(f->tau[c], w.dtau[c]);
+
+    const dim3 block(32, 8);
+    const dim3 grid3(cg_div_up(g->n[0] + 2, block.x), cg_div_up(g->n[1] + 2, block.y), nd > 2 ? g->n[2] + 2 : 1);
+    const int e0 = g->n[0] + 1, e1 = g->n[1] + 1;
+    const int ncheck = o->ncheck;
+    const double inner_rtol = o->inner_rtol > 0 ? o->inner_rtol : 1e-5;
+    const int max_outer = o->max_outer > 0 ? o->max_outer : 8;
+    int total_iter = 0, status = CG_ERR_NOCONV;
+
+    // the PT chunk of the correction, captured once and replayed
+    std::string key = "stokes_dc_chunk";
+    cg_key_add(key, *g);
+    cg_key_add(key, f32);
+    cg_key_add(key, *p);
+    cg_key_add(key, ncheck);
+    auto chunk = [&]() {
+        return cg_graph_run(ctx, key, [&](cudaStream_t st) {
+            for (int it = 0; it < ncheck; ++it) {
+                const bool last = it == ncheck - 1;
+                if (nd == 2) {
+                    if (last) stress_kernel<float, 2, true><<<grid3, block, 0, st>>>(v32, s32, e0, e1);
+                    else stress_kernel<float, 2, false><<<grid3, block, 0, st>>>(v32, s32, e0, e1);
+                    if (last) velocity_kernel<float, 2, true><<<grid3, block, 0, st>>>(v32, s32, e0, e1);
+                    else velocity_kernel<float, 2, false><<<grid3, block, 0, st>>>(v32, s32, e0, e1);
+                } else {
+                    if (last) stress_kernel<float, 3, true><<<grid3, block, 0, st>>>(v32, s32, e0, e1);
+                    else stress_kernel<float, 3, false><<<grid3, block, 0, st>>>(v32, s32, e0, e1);
+                    if (last) velocity_kernel<float, 3, true><<<grid3, block, 0, st>>>(v32, s32, e0, e1);
+                    else velocity_kernel<float, 3, false><<<grid3, block, 0, st>>>(v32, s32, e0, e1);
+                }
+                CG_CHECK_LAUNCH(ctx);
+                int r = cg_bc_apply_impl(ctx, g, nd, f32.V, bc0);
+                if (r) return r;
+            }
+            return (int)CG_OK;
+        });
+    };
+
+    double outer_err[4] = {0, 0, 0, 0};
+    for (int outer = 0; outer <= max_outer; ++outer) {
+        // FP64 defect of the current state
+        if (nd == 2) defect_kernel<2><<<grid3, block, 0, ctx->stream>>>(v64, s64, d32, e0, e1);
+        else defect_kernel<3><<<grid3, block, 0, ctx->stream>>>(v64, s64, d32, e0, e1);
+        CG_CHECK_LAUNCH(ctx);
+        if ((rc = cg_bc_apply_impl(ctx, g, nd, f->r_V, rbc))) return rc;
+        if ((rc = cg_maxabs_enqueue(ctx, nd + 1, red64))) return rc;
+        double m[4];
+        int32_t bad = 0;
+        if ((rc = cg_maxabs_collect(ctx, nd + 1, red64, m, &bad))) return rc;
+        res->checks++;
+        outer_err[0] = m[0] * o->tau_scale;
+        for (int d = 0; d < nd; ++d) outer_err[1 + d] = m[1 + d] * o->v_scale;
+        for (int c = 0; c <= nd; ++c) res->err[c] = outer_err[c];
+        if (bad) {
+            status = CG_ERR_NONFINITE;
+            cg_fail(ctx, CG_ERR_NONFINITE, "stokes_solve (FP32): non-finite FP64 residual");
+            break;
+        }
+        double emax = 0;
+        for (int c = 0; c <= nd; ++c) emax = std::max(emax, outer_err[c]);
+        if (emax < o->eps) {
+            status = CG_OK;
+            res->converged = 1;
+            break;
+        }
+        if (outer == max_outer || total_iter >= o->max_iter) break;
+        // FP32 correction solve from zero
+        for (int d = 0; d < nd; ++d)
+            CG_CUDA(ctx, cudaMemsetAsync(w.dV[d].data, 0, padded_count(w.dV[d]) * 4, ctx->stream));
+        CG_CUDA(ctx, cudaMemsetAsync(w.dP.data, 0, padded_count(w.dP) * 4, ctx->stream));
+        for (int c = 0; c < nt; ++c)
+            CG_CUDA(ctx, cudaMemsetAsync(w.dtau[c].data, 0, padded_count(w.dtau[c]) * 4, ctx->stream));
+        const double target = std::max(0.5 * o->eps, inner_rtol * emax);
+        double best = 1e300;
+        int stall = 0;
+        while (total_iter < o->max_iter) {
+            if ((rc = chunk())) return rc;
+            total_iter += ncheck;
+            if ((rc = cg_bc_apply_impl(ctx, g, nd, f32.r_V, rbc))) return rc;
+            if ((rc = cg_maxabs_enqueue(ctx, nd + 1, red32))) return rc;
+            double e32[4];
+            if ((rc = cg_maxabs_collect(ctx, nd + 1, red32, e32, &bad))) return rc;
+            res->checks++;
+            if (bad) {
+                status = CG_ERR_NONFINITE;
+                cg_fail(ctx, CG_ERR_NONFINITE, "stokes_solve (FP32): non-finite correction residual");
+                break;
+            }
+            double em = e32[0] * o->tau_scale;
+            for (int d = 0; d < nd; ++d) em = std::max(em, e32[1 + d] * o->v_scale);
+            if (em < target) break;
+            if (em < 0.9 * best) {
+                best = em;
+                stall = 0;
+            } else if (++stall >= 4) {
+                break;  // FP32 floor reached: hand back to the FP64 defect
+            }
+        }
+        if (status == CG_ERR_NONFINITE) break;
+        // FP64 update and boundary values
+        update_kernel<<<dim3(ctx->num_sms * 2, upd.count), 256, 0, ctx->stream>>>(upd);
+        CG_CHECK_LAUNCH(ctx);
+        if ((rc = cg_bc_apply_impl(ctx, g, nd, f->V, bc_V))) return rc;
+        res->outer++;
+    }
+    CG_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
+    CG_CUDA(ctx, cudaEventSynchronize(ctx->ev1));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    res->seconds = ms * 1e-3;
+    res->iterations = total_iter;
+    if (status == CG_ERR_NOCONV)
+        cg_fail(ctx, CG_ERR_NOCONV, "stokes_solve (FP32): not converged after %d iterations, %d corrections",
+                total_iter, res->outer);
+    return status;
+}

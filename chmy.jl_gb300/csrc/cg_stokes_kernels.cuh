@@ -1,0 +1,272 @@
+// cg_stokes_kernels.cuh — device code of the VE Stokes PT kernels shared by the per-kernel
+// entry points (cg_stokes.cu) and the defect-correction solver (cg_stokes_dc.cu).
+#pragma once
+
+#include "cg_common.cuh"
+
+namespace cgk {
+
+
+template <class T>
+struct SV {  // device views of the Stokes field set
+    DF<T> V[3], rV[3], P, divV, tau[6], tau_old[6], eta, ieta, rho[3], Tt, To, qT[3];
+    // continuity forcing of the defect-correction solve: the pressure update and the divV
+    // output use (divV + fP); the deviatoric strain rate uses divV alone
+    DF<T> fP;
+    int has_rV, has_divV, has_eta, has_ieta, has_rho[3], has_fP;
+    // 1/eta at a cell: the precomputed field when given, else an IEEE division (same bits)
+    __device__ __forceinline__ T inv_eta(int i, int j, int k) const {
+        return has_ieta ? ieta(i, j, k) : T(1) / eta(i, j, k);
+    }
+};
+
+template <class T>
+struct SP {  // scalars in the field precision
+    T eta, eta_ve, G, dt, dtau_Pr, dtau_r, nu_dtau, lam;
+    T inv_Gdt, third;
+    T idx[3];
+};
+
+template <class T>
+SV<T> views(const cg_stokes_fields* f, int nd) {
+    SV<T> v;
+    std::memset(&v, 0, sizeof(v));
+    const int nt = nd == 2 ? 3 : 6;
+    for (int d = 0; d < nd; ++d) {
+        v.V[d] = cg_view<T>(f->V[d]);
+        if (cg_present(f->r_V[d])) v.rV[d] = cg_view<T>(f->r_V[d]);
+        if (cg_present(f->rho_g[d])) {
+            v.rho[d] = cg_view<T>(f->rho_g[d]);
+            v.has_rho[d] = 1;
+        }
+        if (cg_present(f->qT[d])) v.qT[d] = cg_view<T>(f->qT[d]);
+    }
+    v.has_rV = cg_present(f->r_V[0]);
+    for (int c = 0; c < nt; ++c) {
+        v.tau[c] = cg_view<T>(f->tau[c]);
+        if (cg_present(f->tau_old[c])) v.tau_old[c] = cg_view<T>(f->tau_old[c]);
+    }
+    v.P = cg_view<T>(f->P);
+    if (cg_present(f->divV)) {
+        v.divV = cg_view<T>(f->divV);
+        v.has_divV = 1;
+    }
+    if (cg_present(f->eta)) {
+        v.eta = cg_view<T>(f->eta);
+        v.has_eta = 1;
+    }
+    if (cg_present(f->inv_eta)) {
+        v.ieta = cg_view<T>(f->inv_eta);
+        v.has_ieta = 1;
+        v.has_eta = 1;
+    }
+    if (cg_present(f->T)) v.Tt = cg_view<T>(f->T);
+    if (cg_present(f->T_old)) v.To = cg_view<T>(f->T_old);
+    return v;
+}
+
+template <class T>
+SP<T> scalars(const cg_grid* g, const cg_stokes_params* p) {
+    SP<T> s;
+    s.eta = (T)p->eta;
+    s.eta_ve = (T)p->eta_ve;
+    s.G = (T)p->G;
+    s.dt = (T)p->dt;
+    s.dtau_Pr = (T)p->dtau_Pr;
+    s.dtau_r = (T)p->dtau_r;
+    s.nu_dtau = (T)p->nu_dtau;
+    s.lam = (T)p->lambda_rhoCp;
+    s.inv_Gdt = T(1) / (s.G * s.dt);
+    s.third = T(1) / T(3);
+    for (int d = 0; d < 3; ++d) s.idx[d] = (T)g->inv_spacing[d];
+    return s;
+}
+
+template <class T>
+__device__ __forceinline__ T eta_ve_of(T eta, T G, T dt) {
+    return T(1.0) / (T(1.0) / eta + T(1.0) / (G * dt));
+}
+
+// 2D/3D launch: x, y threads over [0, n+1]; z over blockIdx.z.
+template <int ND>
+inline dim3 range_grid(const cg_grid* g, dim3 block) {
+    return dim3(cg_div_up(g->n[0] + 2, block.x), cg_div_up(g->n[1] + 2, block.y), ND > 2 ? g->n[2] + 2 : 1);
+}
+
+// update_stress! at one point. Tensor order 2D (xx, yy, xy), 3D (xx, yy, zz, xy, xz, yz).
+template <class T, int ND, bool WRITE_RES>
+__global__ void stress_kernel(const SV<T> v, const SP<T> s, int e0, int e1) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = ND > 2 ? blockIdx.z : 0;
+    if (i > e0 || j > e1) return;
+    const DF<T>& Vx = v.V[0];
+    const DF<T>& Vy = v.V[1];
+    // ∂x(V.x) at Center: V.x is Vertex in x -> V.x[i+1] - V.x[i]
+    const T exx = (Vx(i + 1, j, k) - Vx(i, j, k)) * s.idx[0];
+    const T eyy = (Vy(i, j + 1, k) - Vy(i, j, k)) * s.idx[1];
+    T dv = exx + eyy;
+    T ezz = T(0);
+    if (ND > 2) {
+        const DF<T>& Vz = v.V[2];
+        ezz = (Vz(i, j, k + 1) - Vz(i, j, k)) * s.idx[2];
+        dv = dv + ezz;
+    }
+    const T dvP = v.has_fP ? dv + v.fP(i, j, k) : dv;
+    if (WRITE_RES && v.has_divV) v.divV(i, j, k) = dvP;
+    T ieta_c = T(0), eve_c = s.eta_ve;
+    if (v.has_eta) {
+        ieta_c = v.inv_eta(i, j, k);
+        eve_c = T(1) / (ieta_c + s.inv_Gdt);
+    }
+    v.P(i, j, k) = v.P(i, j, k) - dvP * eve_c * s.dtau_Pr;
+    auto diag = [&](int c, T edd) {
+        const T t = v.tau[c](i, j, k), to = v.tau_old[c](i, j, k);
+        T r;
+        if (v.has_eta)
+            r = -(t - to) * s.inv_Gdt - t * ieta_c + T(2.0) * (edd - dv * s.third);
+        else  // examples/stokes_2d_inc_ve_T.jl:28-29, literally
+            r = -(t - to) / (s.G * s.dt) - t / s.eta + T(2.0) * (edd - dv / T(3.0));
+        v.tau[c](i, j, k) = t + r * eve_c * s.dtau_r;
+    };
+    // shear component on the (a, b) edge: 1/eta interpolated with the Linear rule over the 4
+    // cells around it, dim a innermost (interpolation.jl:217-221) = harmonic mean of eta
+    auto shear = [&](int c, T eod, int a, int b) {
+        const T t = v.tau[c](i, j, k), to = v.tau_old[c](i, j, k);
+        if (v.has_eta) {
+            const int ai = a == 0, aj = a == 1, ak = a == 2;
+            const int bi = b == 0, bj = b == 1, bk = b == 2;
+            const T e00 = v.inv_eta(i - ai - bi, j - aj - bj, k - ak - bk);
+            const T e10 = v.inv_eta(i - bi, j - bj, k - bk);
+            const T e01 = v.inv_eta(i - ai, j - aj, k - ak);
+            const T e11 = v.inv_eta(i, j, k);
+            const T lo = fma(T(0.5), e10 - e00, e00);
+            const T hi = fma(T(0.5), e11 - e01, e01);
+            const T iev = fma(T(0.5), hi - lo, lo);
+            const T eve = T(1) / (iev + s.inv_Gdt);
+            const T r = -(t - to) * s.inv_Gdt - t * iev + T(2.0) * eod;
+            v.tau[c](i, j, k) = t + r * eve * s.dtau_r;
+        } else {  // examples/stokes_2d_inc_ve_T.jl:30
+            const T r = -(t - to) / (s.G * s.dt) - t / s.eta + T(2.0) * eod;
+            v.tau[c](i, j, k) = t + r * s.eta_ve * s.dtau_r;
+        }
+    };
+    // ∂y(V.x) at the xy vertex: V.x is Center in y -> V.x[j] - V.x[j-1]
+    const T exy = T(0.5) * ((Vx(i, j, k) - Vx(i, j - 1, k)) * s.idx[1] + (Vy(i, j, k) - Vy(i - 1, j, k)) * s.idx[0]);
+    if (ND == 2) {
+        diag(0, exx);
+        diag(1, eyy);
+        shear(2, exy, 0, 1);
+    } else {
+        const DF<T>& Vz = v.V[2];
+        const T exz = T(0.5) * ((Vx(i, j, k) - Vx(i, j, k - 1)) * s.idx[2] + (Vz(i, j, k) - Vz(i - 1, j, k)) * s.idx[0]);
+        const T eyz = T(0.5) * ((Vy(i, j, k) - Vy(i, j, k - 1)) * s.idx[2] + (Vz(i, j, k) - Vz(i, j - 1, k)) * s.idx[1]);
+        diag(0, exx);
+        diag(1, eyy);
+        diag(2, ezz);
+        shear(3, exy, 0, 1);
+        shear(4, exz, 0, 2);
+        shear(5, eyz, 1, 2);
+    }
+}
+
+// update_velocity! at one point.
+template <class T, int ND, bool WRITE_RES>
+__global__ void velocity_kernel(const SV<T> v, const SP<T> s, int e0, int e1) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = ND > 2 ? blockIdx.z : 0;
+    if (i > e0 || j > e1) return;
+    const DF<T>& P = v.P;
+    // tensor components: 2D xx=0 yy=1 xy=2; 3D xx=0 yy=1 zz=2 xy=3 xz=4 yz=5
+    const int XY = ND == 2 ? 2 : 3;
+    const DF<T>& txx = v.tau[0];
+    const DF<T>& tyy = v.tau[1];
+    const DF<T>& txy = v.tau[XY];
+    // P, τ_dd are Center: at a face along d, left = I - e_d, right = I.
+    // τ_xy is Vertex in x and y: ∂y(τxy) at a V.x face (Vertex x, Center y) -> τxy[j+1] - τxy[j].
+    T rx = -((P(i, j, k) - P(i - 1, j, k)) * s.idx[0]) + (txx(i, j, k) - txx(i - 1, j, k)) * s.idx[0];
+    rx = rx + (txy(i, j + 1, k) - txy(i, j, k)) * s.idx[1];
+    T ry = -((P(i, j, k) - P(i, j - 1, k)) * s.idx[1]) + (tyy(i, j, k) - tyy(i, j - 1, k)) * s.idx[1];
+    ry = ry + (txy(i + 1, j, k) - txy(i, j, k)) * s.idx[0];
+    T rz = T(0);
+    if (ND > 2) {
+        const DF<T>& tzz = v.tau[2];
+        const DF<T>& txz = v.tau[4];
+        const DF<T>& tyz = v.tau[5];
+        rx = rx + (txz(i, j, k + 1) - txz(i, j, k)) * s.idx[2];
+        ry = ry + (tyz(i, j, k + 1) - tyz(i, j, k)) * s.idx[2];
+        rz = -((P(i, j, k) - P(i, j, k - 1)) * s.idx[2]) + (tzz(i, j, k) - tzz(i, j, k - 1)) * s.idx[2];
+        rz = rz + (txz(i + 1, j, k) - txz(i, j, k)) * s.idx[0];
+        rz = rz + (tyz(i, j + 1, k) - tyz(i, j, k)) * s.idx[1];
+    }
+    if (v.has_rho[0]) rx = rx - v.rho[0](i, j, k);
+    if (v.has_rho[1]) ry = ry - v.rho[1](i, j, k);
+    if (ND > 2 && v.has_rho[2]) rz = rz - v.rho[2](i, j, k);
+    if (WRITE_RES && v.has_rV) {
+        v.rV[0](i, j, k) = rx;
+        v.rV[1](i, j, k) = ry;
+        if (ND > 2) v.rV[2](i, j, k) = rz;
+    }
+    if (v.has_eta) {
+        // nu_dtau / max(eta_ve) of the two cells beside the face, without a division
+        const T c = v.inv_eta(i, j, k);
+        v.V[0](i, j, k) = v.V[0](i, j, k) + rx * (s.nu_dtau * (fmin(v.inv_eta(i - 1, j, k), c) + s.inv_Gdt));
+        v.V[1](i, j, k) = v.V[1](i, j, k) + ry * (s.nu_dtau * (fmin(v.inv_eta(i, j - 1, k), c) + s.inv_Gdt));
+        if (ND > 2)
+            v.V[2](i, j, k) = v.V[2](i, j, k) + rz * (s.nu_dtau * (fmin(v.inv_eta(i, j, k - 1), c) + s.inv_Gdt));
+    } else {  // examples/stokes_2d_inc_ve_T.jl:41-42
+        v.V[0](i, j, k) = v.V[0](i, j, k) + rx * s.nu_dtau / s.eta_ve;
+        v.V[1](i, j, k) = v.V[1](i, j, k) + ry * s.nu_dtau / s.eta_ve;
+        if (ND > 2) v.V[2](i, j, k) = v.V[2](i, j, k) + rz * s.nu_dtau / s.eta_ve;
+    }
+}
+
+template <class T, int ND>
+__global__ void update_old_kernel(const SV<T> v, int has_T, int e0, int e1) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = ND > 2 ? blockIdx.z : 0;
+    if (i > e0 || j > e1) return;
+    if (has_T) v.To(i, j, k) = v.Tt(i, j, k);
+#pragma unroll
+    for (int c = 0; c < (ND == 2 ? 3 : 6); ++c) v.tau_old[c](i, j, k) = v.tau[c](i, j, k);
+}
+
+template <class T, int ND>
+__global__ void thermal_flux_kernel(const SV<T> v, const SP<T> s, int e0, int e1) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = ND > 2 ? blockIdx.z : 0;
+    if (i > e0 || j > e1) return;
+    const DF<T>& Tt = v.Tt;
+    const T c = Tt(i, j, k);
+    const T mlam = -s.lam;
+    {
+        const T l = Tt(i - 1, j, k), vv = v.V[0](i, j, k);
+        v.qT[0](i, j, k) = mlam * ((c - l) * s.idx[0]) + fmax(vv, T(0.0)) * l + fmin(vv, T(0.0)) * c;
+    }
+    {
+        const T l = Tt(i, j - 1, k), vv = v.V[1](i, j, k);
+        v.qT[1](i, j, k) = mlam * ((c - l) * s.idx[1]) + fmax(vv, T(0.0)) * l + fmin(vv, T(0.0)) * c;
+    }
+    if (ND > 2) {
+        const T l = Tt(i, j, k - 1), vv = v.V[2](i, j, k);
+        v.qT[2](i, j, k) = mlam * ((c - l) * s.idx[2]) + fmax(vv, T(0.0)) * l + fmin(vv, T(0.0)) * c;
+    }
+}
+
+template <class T, int ND>
+__global__ void thermal_kernel(const SV<T> v, const SP<T> s, int e0, int e1) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = ND > 2 ? blockIdx.z : 0;
+    if (i > e0 || j > e1) return;
+    T dv = (v.qT[0](i + 1, j, k) - v.qT[0](i, j, k)) * s.idx[0];
+    dv = dv + (v.qT[1](i, j + 1, k) - v.qT[1](i, j, k)) * s.idx[1];
+    if (ND > 2) dv = dv + (v.qT[2](i, j, k + 1) - v.qT[2](i, j, k)) * s.idx[2];
+    v.Tt(i, j, k) = v.To(i, j, k) - s.dt * dv;
+}
+
+
+}  // namespace cgk

@@ -254,6 +254,39 @@ CG_API int cg_stokes_solve(cg_ctx* ctx, const cg_grid* grid, const cg_stokes_fie
                     const cg_stokes_params* p, const cg_bc* bc_V, const cg_solve_opts* o,
                     cg_solve_result* res);
 
+/* ---- shallow ice (examples/sia.jl) ----------------------------------------------------- */
+
+/* Parameters of the SIA step. examples/sia.jl:24-54 is Gamma = 1, As = 0.5, n = 3, beta = 0.5,
+ * ela = 0.3, m_max = 0.25, dt_max = 0.5 (Δt_mb), cfl = 4.1. The flux of the benchmark
+ * ensemble, -Gamma H^(n+2) |∇S|^(n-1) ∇S, is As = 0. */
+typedef struct cg_sia_params {
+    double  Gamma;  /* coefficient of H^(n+2) in D                                           */
+    double  As;     /* coefficient of H^n in D                                               */
+    int32_t n;      /* Glen exponent (integer powers by repeated multiplication)             */
+    int32_t pad_;
+    double  beta;   /* mass balance M = min(beta (S - ela), m_max), S = B + H                */
+    double  ela;
+    double  m_max;
+    double  dt_max; /* Δt = min(min(Δ)^2 / max(interior D) / cfl, dt_max)                    */
+    double  cfl;
+} cg_sia_params;
+
+/* update_q! (examples/sia.jl:12-16) over the interior cells [1, n]^2 with D evaluated on the
+ * fly as the FunctionField of :46-49, D = (Gamma H^(n+2) + As H^n) vmag(∇S)^(n-1),
+ * followed by bc!(q.x => (x = Dirichlet()), q.y => (y = Dirichlet())) (:73). B holds the bed
+ * over the whole padded array. If dmax_host is not NULL it receives maximum(interior(D)). */
+CG_API int cg_sia_update_q(cg_ctx* ctx, const cg_grid* grid, const cg_field* q, const cg_field* H,
+                           const cg_field* B, const cg_sia_params* p, double* dmax_host);
+/* update_H! (examples/sia.jl:7-10) over [1, n]^2: H = max(H + dt (-divg(q) + M), 0), followed
+ * by bc!(H => Neumann()) (:81). */
+CG_API int cg_sia_update_H(cg_ctx* ctx, const cg_grid* grid, const cg_field* H, const cg_field* q,
+                           const cg_field* B, double dt, const cg_sia_params* p);
+/* `nsteps` SIA time steps with the adaptive Δt computed on the device every step (no host
+ * synchronisation), replayed from one CUDA graph. q is the flux work array (its final
+ * values are those of the last step). `t_host` (optional) receives the simulated time. */
+CG_API int cg_sia_run(cg_ctx* ctx, const cg_grid* grid, const cg_field* H, const cg_field* B,
+                      const cg_field* q, const cg_sia_params* p, int nsteps, double* t_host);
+
 #ifdef __cplusplus
 }
 #endif

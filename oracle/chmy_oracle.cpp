@@ -607,6 +607,107 @@ void op_kernel_t(int op, const cg_grid* grid, const cg_field* C, const cg_field*
     });
 }
 
+/* ---- shallow ice (examples/sia.jl) --------------------------------------------------- */
+
+/* x^m by repeated multiplication (the restatement of Julia's integer power). */
+template <class T>
+inline T ipow(T x, int m) {
+    if (m <= 0) return T(1);
+    T r = x;
+    for (int k = 1; k < m; ++k) r = r * x;
+    return r;
+}
+
+template <class T>
+struct Sia {
+    GridT<T> g;
+    Fd<T> H, B;
+    T Gamma, As, beta, ela, m_max;
+    int n;
+    Sia(const cg_grid* grid, const cg_field* Hf, const cg_field* Bf, const cg_sia_params* p)
+        : g(*grid), H(*Hf), B(*Bf) {
+        Gamma = (T)p->Gamma;
+        As = (T)p->As;
+        beta = (T)p->beta;
+        ela = (T)p->ela;
+        m_max = (T)p->m_max;
+        n = p->n;
+    }
+    /* S = B + H (examples/sia.jl:38-41) */
+    T S(int i, int j) const { return B(i, j, 0) + H(i, j, 0); }
+    /* ∇S.x at vertex-x index i: ∂x(S) = (S[i] - S[i-1]) iΔx; ∇S.y likewise (:43-44) */
+    T gx(int i, int j) const { return (S(i, j) - S(i - 1, j)) * g.idx[0]; }
+    T gy(int i, int j) const { return (S(i, j) - S(i, j - 1)) * g.idx[1]; }
+    /* vmag(∇S) at cell (i, j): sqrt(lerp(∇S.x → C)^2 + lerp(∇S.y → C)^2) (field_operators.jl:187-191) */
+    T vmag(int i, int j) const {
+        const T a0 = gx(i, j), a1 = gx(i + 1, j);
+        const T ax = std::fma(T(0.5), a1 - a0, a0);
+        const T b0 = gy(i, j), b1 = gy(i, j + 1);
+        const T ay = std::fma(T(0.5), b1 - b0, b0);
+        return std::sqrt(ax * ax + ay * ay);
+    }
+    /* D = (Gamma H^(n+2) + As H^n) vmag^(n-1) (:46-49) */
+    T D(int i, int j) const {
+        const T h = H(i, j, 0);
+        return (Gamma * ipow(h, n + 2) + As * ipow(h, n)) * ipow(vmag(i, j), n - 1);
+    }
+    /* M = min(beta (S - ela), m_max) (:51-54) */
+    T M(int i, int j) const { return std::min(beta * (S(i, j) - ela), m_max); }
+};
+
+template <class T>
+void sia_update_q_t(const cg_grid* grid, const cg_field* q, const cg_field* Hf, const cg_field* Bf,
+                    const cg_sia_params* p, double* dmax) {
+    Sia<T> s(grid, Hf, Bf, p);
+    Fd<T> qx(q[0]), qy(q[1]);
+    const int nx = s.g.n[0], ny = s.g.n[1];
+    /* update_q! over ws = size(grid, Center()) = [1, n]^2 (:62-63,72) */
+#pragma omp parallel for schedule(static)
+    for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i) {
+            /* lerp(D, (Vertex, Center)): D Center seen from the x face -> cells i-1, i */
+            const T dl = s.D(i - 1, j), dc = s.D(i, j), dd = s.D(i, j - 1);
+            const T Dx = std::fma(T(0.5), dc - dl, dl);
+            const T Dy = std::fma(T(0.5), dc - dd, dd);
+            qx(i, j, 0) = -Dx * s.gx(i, j);
+            qy(i, j, 0) = -Dy * s.gy(i, j);
+        }
+    if (dmax) {
+        double m = 0;
+        for (int j = 1; j <= ny; ++j)
+            for (int i = 1; i <= nx; ++i) m = std::max(m, (double)s.D(i, j));
+        *dmax = m;
+    }
+    /* bc!(arch, grid, q.x => (x = Dirichlet()), q.y => (y = Dirichlet())) (:73) */
+    cg_bc b[2];
+    std::memset(b, 0, sizeof(b));
+    b[0].kind[0][0] = b[0].kind[0][1] = CG_BC_DIRICHLET;
+    b[1].kind[1][0] = b[1].kind[1][1] = CG_BC_DIRICHLET;
+    bc_apply_t<T>(grid, 2, q, b);
+}
+
+template <class T>
+void sia_update_H_t(const cg_grid* grid, const cg_field* Hf, const cg_field* q, const cg_field* Bf, double dt,
+                    const cg_sia_params* p) {
+    Sia<T> s(grid, Hf, Bf, p);
+    Fd<T> Q[3] = {Fd<T>(q[0]), Fd<T>(q[1]), Fd<T>()};
+    const T Dt = (T)dt;
+    const int nx = s.g.n[0], ny = s.g.n[1];
+    /* M depends on S = B + H: evaluate it for all cells before H changes (the kernel reads
+       H[I] and M[I] of the same cell only) */
+#pragma omp parallel for schedule(static)
+    for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i) {
+            const T h = s.H(i, j, 0);
+            const T m = s.M(i, j);
+            s.H(i, j, 0) = std::max(h + Dt * (-divg(Q, s.g, i, j, 0) + m), T(0.0));
+        }
+    cg_bc b;
+    std::memset(&b, 0, sizeof(b));
+    b.kind[0][0] = b.kind[0][1] = b.kind[1][0] = b.kind[1][1] = CG_BC_NEUMANN;
+    bc_apply_t<T>(grid, 1, Hf, &b);
+}
+
 }  // namespace
 
 /* ==== extern "C" surface (names mirror the library's cg_* entry points) =============== */
@@ -681,6 +782,20 @@ int or_stokes_update_thermal_flux(const cg_grid* grid, const cg_stokes_fields* f
 int or_stokes_update_thermal(const cg_grid* grid, const cg_stokes_fields* f, const cg_stokes_params* p) {
     if (f->T.dtype == CG_F64) stokes_update_thermal_t<double>(grid, f, p);
     else stokes_update_thermal_t<float>(grid, f, p);
+    return CG_OK;
+}
+
+int or_sia_update_q(const cg_grid* grid, const cg_field* q, const cg_field* H, const cg_field* B,
+                    const cg_sia_params* p, double* dmax) {
+    if (H->dtype == CG_F64) sia_update_q_t<double>(grid, q, H, B, p, dmax);
+    else sia_update_q_t<float>(grid, q, H, B, p, dmax);
+    return CG_OK;
+}
+
+int or_sia_update_H(const cg_grid* grid, const cg_field* H, const cg_field* q, const cg_field* B, double dt,
+                    const cg_sia_params* p) {
+    if (H->dtype == CG_F64) sia_update_H_t<double>(grid, H, q, B, dt, p);
+    else sia_update_H_t<float>(grid, H, q, B, dt, p);
     return CG_OK;
 }
 

@@ -34,6 +34,14 @@ _SIGS = {
     "or_stokes_update_velocity": ([P(_abi.cg_grid), P(_abi.cg_stokes_fields), P(_abi.cg_stokes_params)], C.c_int),
     "or_stokes_update_thermal_flux": ([P(_abi.cg_grid), P(_abi.cg_stokes_fields), P(_abi.cg_stokes_params)], C.c_int),
     "or_stokes_update_thermal": ([P(_abi.cg_grid), P(_abi.cg_stokes_fields), P(_abi.cg_stokes_params)], C.c_int),
+    "or_sia_update_q": (
+        [P(_abi.cg_grid), P(_abi.cg_field), P(_abi.cg_field), P(_abi.cg_field), P(_abi.cg_sia_params), P(C.c_double)],
+        C.c_int,
+    ),
+    "or_sia_update_H": (
+        [P(_abi.cg_grid), P(_abi.cg_field), P(_abi.cg_field), P(_abi.cg_field), C.c_double, P(_abi.cg_sia_params)],
+        C.c_int,
+    ),
     "or_op_kernel": (
         [C.c_int, P(_abi.cg_grid), P(_abi.cg_field), P(_abi.cg_field), P(_abi.cg_field), P(_abi.cg_field), P(_abi.cg_field)],
         C.c_int,
