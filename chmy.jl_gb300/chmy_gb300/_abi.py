@@ -125,6 +125,7 @@ class cg_solve_result(C.Structure):
         ("converged", C.c_int32),
         ("err", C.c_double * 4),
         ("seconds", C.c_double),
+        ("err_tau", C.c_double),
     ]
 
 
@@ -169,6 +170,15 @@ SIGNATURES: dict[str, list] = {
     "cg_stokes_update_thermal_flux": [_vp, P(cg_grid), P(cg_stokes_fields), P(cg_stokes_params)],
     "cg_stokes_update_thermal": [_vp, P(cg_grid), P(cg_stokes_fields), P(cg_stokes_params)],
     "cg_stokes_pt_iterations": [_vp, P(cg_grid), P(cg_stokes_fields), P(cg_stokes_params), P(cg_bc), C.c_int],
+    "cg_stokes_pt_iterations_pp": [
+        _vp,
+        P(cg_grid),
+        P(cg_stokes_fields),
+        P(cg_stokes_fields),
+        P(cg_stokes_params),
+        P(cg_bc),
+        C.c_int,
+    ],
     "cg_stokes_residual": [_vp, P(cg_grid), P(cg_stokes_fields), C.c_double, C.c_double, P(C.c_double)],
     "cg_stokes_solve": [
         _vp,

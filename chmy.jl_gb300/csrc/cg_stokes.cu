@@ -241,6 +241,96 @@ extern "C" int cg_stokes_pt_iterations(cg_ctx* ctx, const cg_grid* grid, const c
     return pt_iterations(ctx, grid, f, p, bc_V, niter, dtype);
 }
 
+namespace {
+
+template <class T>
+Fused2D<T> fused_view(const cg_stokes_fields* in, const cg_stokes_fields* out, const cg_stokes_fields* a) {
+    Fused2D<T> f;
+    std::memset(&f, 0, sizeof(f));
+    f.Vx_in = cg_view<T>(in->V[0]);
+    f.Vy_in = cg_view<T>(in->V[1]);
+    f.Vx_out = cg_view<T>(out->V[0]);
+    f.Vy_out = cg_view<T>(out->V[1]);
+    f.txx_in = cg_view<T>(in->tau[0]);
+    f.tyy_in = cg_view<T>(in->tau[1]);
+    f.txy_in = cg_view<T>(in->tau[2]);
+    f.txx_out = cg_view<T>(out->tau[0]);
+    f.tyy_out = cg_view<T>(out->tau[1]);
+    f.txy_out = cg_view<T>(out->tau[2]);
+    f.P_in = cg_view<T>(in->P);
+    f.P_out = cg_view<T>(out->P);
+    f.txx_o = cg_view<T>(a->tau_old[0]);
+    f.tyy_o = cg_view<T>(a->tau_old[1]);
+    f.txy_o = cg_view<T>(a->tau_old[2]);
+    f.ieta = cg_view<T>(a->inv_eta);
+    f.has_rho = cg_present(a->rho_g[0]) && cg_present(a->rho_g[1]);
+    if (f.has_rho) {
+        f.rhox = cg_view<T>(a->rho_g[0]);
+        f.rhoy = cg_view<T>(a->rho_g[1]);
+    }
+    if (cg_present(a->divV)) f.divV = cg_view<T>(a->divV);
+    if (cg_present(a->r_V[0])) {
+        f.rVx = cg_view<T>(a->r_V[0]);
+        f.rVy = cg_view<T>(a->r_V[1]);
+    }
+    return f;
+}
+
+template <class T>
+int pp_iterations_t(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* a, const cg_stokes_fields* b,
+                    const cg_stokes_params* p, const cg_bc* bc_V, int niter) {
+    const Fused2D<T> fab = fused_view<T>(a, b, a), fba = fused_view<T>(b, a, a);
+    const SP<T> s = scalars<T>(g, p);
+    const bool res = cg_present(a->divV) && cg_present(a->r_V[0]);
+    const dim3 block(32, 8), grid(cg_div_up(g->n[0] + 2, 32), cg_div_up(g->n[1] + 2, 32));
+    const int e0 = g->n[0] + 1, e1 = g->n[1] + 1;
+    std::string key = "stokes_pp";
+    cg_key_add(key, *g);
+    cg_key_add(key, *a);
+    cg_key_add(key, *b);
+    cg_key_add(key, *p);
+    cg_key_add(key, niter);
+    cg_bc none[2];
+    std::memset(none, 0, sizeof(none));
+    for (int d = 0; d < 2; ++d) cg_key_add(key, bc_V ? bc_V[d] : none[d]);
+    return cg_graph_run(ctx, key, [&](cudaStream_t st) {
+        for (int it = 0; it < niter; ++it) {
+            const Fused2D<T>& fk = (it % 2 == 0) ? fab : fba;
+            if (res && it == niter - 1) fused2d_kernel<T, 4, true><<<grid, block, 0, st>>>(fk, s, e0, e1);
+            else fused2d_kernel<T, 4, false><<<grid, block, 0, st>>>(fk, s, e0, e1);
+            CG_CHECK_LAUNCH(ctx);
+            if (bc_V) {
+                int r = cg_bc_apply_impl(ctx, g, 2, (it % 2 == 0) ? b->V : a->V, bc_V);
+                if (r) return r;
+            }
+        }
+        return (int)CG_OK;
+    });
+}
+
+}  // namespace
+
+extern "C" int cg_stokes_pt_iterations_pp(cg_ctx* ctx, const cg_grid* grid, const cg_stokes_fields* a,
+                                          const cg_stokes_fields* b, const cg_stokes_params* p, const cg_bc* bc_V,
+                                          int niter) {
+    int dtype;
+    int rc = check_stokes(ctx, grid, a, NEED_V | NEED_TAU | NEED_TAU_OLD | NEED_P, &dtype);
+    if (rc) return rc;
+    if (!b || !p) return cg_fail(ctx, CG_ERR_ARG, "pt_iterations_pp: NULL argument");
+    if (grid->ndim != 2) return cg_fail(ctx, CG_ERR_UNSUPPORTED, "pt_iterations_pp: 2D grids only");
+    if (!cg_present(a->inv_eta)) return cg_fail(ctx, CG_ERR_ARG, "pt_iterations_pp: inv_eta is required");
+    if (niter < 0 || (niter & 1)) return cg_fail(ctx, CG_ERR_ARG, "pt_iterations_pp: niter must be even and >= 0");
+    int dtb;
+    if ((rc = check_stokes(ctx, grid, b, NEED_V | NEED_TAU | NEED_P, &dtb))) return rc;
+    if (dtb != dtype) return cg_fail(ctx, CG_ERR_ARG, "pt_iterations_pp: a and b dtypes differ");
+    if (cg_present(a->divV) != cg_present(a->r_V[0]))
+        return cg_fail(ctx, CG_ERR_ARG, "pt_iterations_pp: divV and r_V together");
+    if (niter == 0) return CG_OK;
+    cudaSetDevice(ctx->device);
+    return dtype == CG_F64 ? pp_iterations_t<double>(ctx, grid, a, b, p, bc_V, niter)
+                           : pp_iterations_t<float>(ctx, grid, a, b, p, bc_V, niter);
+}
+
 extern "C" int cg_stokes_residual(cg_ctx* ctx, const cg_grid* grid, const cg_stokes_fields* f, double tau_scale,
                                   double v_scale, double* err_host) {
     int dtype;

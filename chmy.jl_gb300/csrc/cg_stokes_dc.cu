@@ -153,6 +153,7 @@ __global__ void update_kernel(const UpdTable t) {
 
 struct Work {
     cg_field dV[3], dP, dtau[6], told[6], fP, rho[3], ieta, divV, rV[3];
+    cg_field dV2[3], dP2, dtau2[6];  // ping-pong partners of the fused 2D kernel
 };
 
 // FP32 dense field like `f` (same extents, locations, halo 1).
@@ -186,15 +187,18 @@ int make_work(cg_ctx* ctx, const cg_stokes_fields* f, int nd, Work* w) {
         size_t bytes = 0;
         for (int d = 0; d < nd; ++d) {
             w->dV[d] = like32(f->V[d], cur, bytes, dry);
+            w->dV2[d] = like32(f->V[d], cur, bytes, dry);
             w->rho[d] = like32(f->V[d], cur, bytes, dry);
             w->rV[d] = like32(f->V[d], cur, bytes, dry);
         }
         w->dP = like32(f->P, cur, bytes, dry);
+        w->dP2 = like32(f->P, cur, bytes, dry);
         w->fP = like32(f->P, cur, bytes, dry);
         w->ieta = like32(f->P, cur, bytes, dry);
         w->divV = like32(f->P, cur, bytes, dry);
         for (int c = 0; c < nt; ++c) {
             w->dtau[c] = like32(f->tau[c], cur, bytes, dry);
+            w->dtau2[c] = like32(f->tau[c], cur, bytes, dry);
             w->told[c] = like32(f->tau[c], cur, bytes, dry);
         }
         if (dry && bytes > ctx->dc_pool_bytes) {
@@ -298,11 +302,15 @@ int cg_stokes_solve_dc(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f,
         bc0[d] = bc_V ? bc_V[d] : cg_bc{};
         for (int a = 0; a < 3; ++a) bc0[d].value[a][0] = bc0[d].value[a][1] = 0.0;
     }
-    cg_field red64[4], red32[4];
+    // FP64 measures: divV, r_V (the reference's) and the constitutive residuals, read from the
+    // FP32 forcing tau_old' = G dt R_tau (the initial guess of a PT solve can have zero divV and
+    // r_V while tau is far from its constitutive value)
+    cg_field red64[4 + 6], red32[4];
     red64[0] = f->divV;
     red32[0] = w.divV;
     for (int d = 0; d < nd; ++d) {
         red64[1 + d] = f->r_V[d];
+    for (int c = 0; c < nt; ++c) red64[1 + nd + c] = w.told[c];
         red32[1 + d] = w.rV[d];
     }
     cg_bc rbc[3];
@@ -337,24 +345,60 @@ int cg_stokes_solve_dc(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f,
     cg_key_add(key, f32);
     cg_key_add(key, *p);
     cg_key_add(key, ncheck);
+    // 2D: fused kernel, ping-pong A -> B -> A, an even number of iterations per chunk
+    Fused2D<float> fa, fb;
+    std::memset(&fa, 0, sizeof(fa));
+    if (nd == 2) {
+        fa.txx_o = cg_view<float>(w.told[0]);
+        fa.tyy_o = cg_view<float>(w.told[1]);
+        fa.txy_o = cg_view<float>(w.told[2]);
+        fa.ieta = cg_view<float>(w.ieta);
+        fa.fP = cg_view<float>(w.fP);
+        fa.has_fP = 1;
+        fa.rhox = cg_view<float>(w.rho[0]);
+        fa.rhoy = cg_view<float>(w.rho[1]);
+        fa.has_rho = 1;
+        fa.divV = cg_view<float>(w.divV);
+        fa.rVx = cg_view<float>(w.rV[0]);
+        fa.rVy = cg_view<float>(w.rV[1]);
+        fb = fa;
+        fa.Vx_in = fb.Vx_out = cg_view<float>(w.dV[0]);
+        fa.Vy_in = fb.Vy_out = cg_view<float>(w.dV[1]);
+        fa.txx_in = fb.txx_out = cg_view<float>(w.dtau[0]);
+        fa.tyy_in = fb.tyy_out = cg_view<float>(w.dtau[1]);
+        fa.txy_in = fb.txy_out = cg_view<float>(w.dtau[2]);
+        fa.P_in = fb.P_out = cg_view<float>(w.dP);
+        fa.Vx_out = fb.Vx_in = cg_view<float>(w.dV2[0]);
+        fa.Vy_out = fb.Vy_in = cg_view<float>(w.dV2[1]);
+        fa.txx_out = fb.txx_in = cg_view<float>(w.dtau2[0]);
+        fa.tyy_out = fb.tyy_in = cg_view<float>(w.dtau2[1]);
+        fa.txy_out = fb.txy_in = cg_view<float>(w.dtau2[2]);
+        fa.P_out = fb.P_in = cg_view<float>(w.dP2);
+    }
+    constexpr int kFR = 4;  // rows per thread: 32 x 32 tiles
+    const dim3 gridF(cg_div_up(g->n[0] + 2, 32), cg_div_up(g->n[1] + 2, 8 * kFR));
+    const int nchunk = nd == 2 ? ncheck + (ncheck & 1) : ncheck;
+    cg_key_add(key, nchunk);
     auto chunk = [&]() {
         return cg_graph_run(ctx, key, [&](cudaStream_t st) {
-            for (int it = 0; it < ncheck; ++it) {
-                const bool last = it == ncheck - 1;
+            for (int it = 0; it < nchunk; ++it) {
+                const bool last = it == nchunk - 1;
                 if (nd == 2) {
-                    if (last) stress_kernel<float, 2, true><<<grid3, block, 0, st>>>(v32, s32, e0, e1);
-                    else stress_kernel<float, 2, false><<<grid3, block, 0, st>>>(v32, s32, e0, e1);
-                    if (last) velocity_kernel<float, 2, true><<<grid3, block, 0, st>>>(v32, s32, e0, e1);
-                    else velocity_kernel<float, 2, false><<<grid3, block, 0, st>>>(v32, s32, e0, e1);
+                    const Fused2D<float>& fk = (it % 2 == 0) ? fa : fb;
+                    if (last) fused2d_kernel<float, kFR, true><<<gridF, block, 0, st>>>(fk, s32, e0, e1);
+                    else fused2d_kernel<float, kFR, false><<<gridF, block, 0, st>>>(fk, s32, e0, e1);
+                    CG_CHECK_LAUNCH(ctx);
+                    int r = cg_bc_apply_impl(ctx, g, nd, (it % 2 == 0) ? w.dV2 : w.dV, bc0);
+                    if (r) return r;
                 } else {
                     if (last) stress_kernel<float, 3, true><<<grid3, block, 0, st>>>(v32, s32, e0, e1);
                     else stress_kernel<float, 3, false><<<grid3, block, 0, st>>>(v32, s32, e0, e1);
                     if (last) velocity_kernel<float, 3, true><<<grid3, block, 0, st>>>(v32, s32, e0, e1);
                     else velocity_kernel<float, 3, false><<<grid3, block, 0, st>>>(v32, s32, e0, e1);
+                    CG_CHECK_LAUNCH(ctx);
+                    int r = cg_bc_apply_impl(ctx, g, nd, f32.V, bc0);
+                    if (r) return r;
                 }
-                CG_CHECK_LAUNCH(ctx);
-                int r = cg_bc_apply_impl(ctx, g, nd, f32.V, bc0);
-                if (r) return r;
             }
             return (int)CG_OK;
         });
@@ -367,20 +411,23 @@ int cg_stokes_solve_dc(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f,
         else defect_kernel<3><<<grid3, block, 0, ctx->stream>>>(v64, s64, d32, e0, e1);
         CG_CHECK_LAUNCH(ctx);
         if ((rc = cg_bc_apply_impl(ctx, g, nd, f->r_V, rbc))) return rc;
-        if ((rc = cg_maxabs_enqueue(ctx, nd + 1, red64))) return rc;
-        double m[4];
+        if ((rc = cg_maxabs_enqueue(ctx, nd + 1 + nt, red64))) return rc;
+        double m[4 + 6];
         int32_t bad = 0;
-        if ((rc = cg_maxabs_collect(ctx, nd + 1, red64, m, &bad))) return rc;
+        if ((rc = cg_maxabs_collect(ctx, nd + 1 + nt, red64, m, &bad))) return rc;
         res->checks++;
         outer_err[0] = m[0] * o->tau_scale;
         for (int d = 0; d < nd; ++d) outer_err[1 + d] = m[1 + d] * o->v_scale;
         for (int c = 0; c <= nd; ++c) res->err[c] = outer_err[c];
+        double etau = 0.0;
+        for (int c = 0; c < nt; ++c) etau = std::max(etau, m[1 + nd + c]);
+        res->err_tau = etau / (p->G * p->dt) * o->tau_scale;
         if (bad) {
             status = CG_ERR_NONFINITE;
             cg_fail(ctx, CG_ERR_NONFINITE, "stokes_solve (FP32): non-finite FP64 residual");
             break;
         }
-        double emax = 0;
+        double emax = res->err_tau;
         for (int c = 0; c <= nd; ++c) emax = std::max(emax, outer_err[c]);
         if (emax < o->eps) {
             status = CG_OK;
@@ -389,17 +436,22 @@ int cg_stokes_solve_dc(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f,
         }
         if (outer == max_outer || total_iter >= o->max_iter) break;
         // FP32 correction solve from zero
-        for (int d = 0; d < nd; ++d)
+        for (int d = 0; d < nd; ++d) {
             CG_CUDA(ctx, cudaMemsetAsync(w.dV[d].data, 0, padded_count(w.dV[d]) * 4, ctx->stream));
+            CG_CUDA(ctx, cudaMemsetAsync(w.dV2[d].data, 0, padded_count(w.dV2[d]) * 4, ctx->stream));
+        }
         CG_CUDA(ctx, cudaMemsetAsync(w.dP.data, 0, padded_count(w.dP) * 4, ctx->stream));
-        for (int c = 0; c < nt; ++c)
+        CG_CUDA(ctx, cudaMemsetAsync(w.dP2.data, 0, padded_count(w.dP2) * 4, ctx->stream));
+        for (int c = 0; c < nt; ++c) {
             CG_CUDA(ctx, cudaMemsetAsync(w.dtau[c].data, 0, padded_count(w.dtau[c]) * 4, ctx->stream));
+            CG_CUDA(ctx, cudaMemsetAsync(w.dtau2[c].data, 0, padded_count(w.dtau2[c]) * 4, ctx->stream));
+        }
         const double target = std::max(0.5 * o->eps, inner_rtol * emax);
         double best = 1e300;
         int stall = 0;
         while (total_iter < o->max_iter) {
             if ((rc = chunk())) return rc;
-            total_iter += ncheck;
+            total_iter += nchunk;
             if ((rc = cg_bc_apply_impl(ctx, g, nd, f32.r_V, rbc))) return rc;
             if ((rc = cg_maxabs_enqueue(ctx, nd + 1, red32))) return rc;
             double e32[4];

@@ -268,5 +268,122 @@ __global__ void thermal_kernel(const SV<T> v, const SP<T> s, int e0, int e1) {
     v.Tt(i, j, k) = v.To(i, j, k) - s.dt * dv;
 }
 
+// ---- fused 2D PT iteration (variable viscosity): update_stress! + update_velocity! -----------
+//
+// One launch per PT iteration. A block owns a 32 x TY tile of launch points I; it stages V and
+// 1/eta with a halo in shared memory, recomputes the new tau/P on the one-cell halo it needs
+// (bitwise the same values the owning block computes), then updates the velocity of its own
+// faces. Reads come from the `in` buffers and writes go to the `out` buffers (ping-pong), so the
+// redundant halo recomputation never sees a neighbour's new values. Points outside Chmy's
+// launch range [0, n+1] keep their old values, exactly as in the two-kernel form.
+template <class T>
+struct Fused2D {
+    DF<T> Vx_in, Vy_in, Vx_out, Vy_out;
+    DF<T> txx_in, tyy_in, txy_in, txx_out, tyy_out, txy_out, P_in, P_out;
+    DF<T> txx_o, tyy_o, txy_o, ieta, fP, rhox, rhoy, divV, rVx, rVy;
+    int has_fP, has_rho;
+};
+
+template <class T, int R, bool WRITE_RES>
+__global__ void __launch_bounds__(256) fused2d_kernel(const Fused2D<T> f, const SP<T> s, int e0, int e1) {
+    constexpr int TX = 32, TY = 8 * R;
+    constexpr int HX = TX + 2, HY = TY + 2;  // V, 1/eta from (i0-1, j0-1)
+    constexpr int CX = TX + 1, CY = TY + 1;  // new cells from (i0-1, j0-1); new vertices from (i0, j0)
+    __shared__ T sVx[HY][HX], sVy[HY][HX], sIe[HY][HX];
+    __shared__ T sTxx[CY][CX], sTyy[CY][CX], sP[CY][CX], sTxy[CY][CX];
+    const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
+    const int tid = threadIdx.y * 32 + threadIdx.x;
+    // stage V and 1/eta over logical [i0-1, i0+TX] x [j0-1, j0+TY], clipped to [-1, n+2]
+    for (int t = tid; t < HX * HY; t += 256) {
+        const int a = t % HX, b = t / HX;
+        const int i = i0 - 1 + a, j = j0 - 1 + b;
+        const bool ok = i <= e0 + 1 && j <= e1 + 1;
+        sVx[b][a] = ok ? f.Vx_in(i, j, 0) : T(0);
+        sVy[b][a] = ok ? f.Vy_in(i, j, 0) : T(0);
+        sIe[b][a] = ok ? f.ieta(i, j, 0) : T(0);
+    }
+    __syncthreads();
+    const T half = T(0.5);
+    // phase 1a: new tau_xx, tau_yy, P at cells (i0-1+a, j0-1+b)
+    for (int t = tid; t < CX * CY; t += 256) {
+        const int a = t % CX, b = t / CX;
+        const int i = i0 - 1 + a, j = j0 - 1 + b;
+        if (i > e0 || j > e1) continue;  // never read by an in-range face
+        if (i < 0 || j < 0) {            // outside the launch range: old values
+            sTxx[b][a] = f.txx_in(i, j, 0);
+            sTyy[b][a] = f.tyy_in(i, j, 0);
+            sP[b][a] = f.P_in(i, j, 0);
+            continue;
+        }
+        // V.x at (i, j), (i+1, j): smem (a, b+... ) with offsets (a, b) -> logical (i0-1+a, j0-1+b)
+        const T exx = (sVx[b][a + 1] - sVx[b][a]) * s.idx[0];
+        const T eyy = (sVy[b + 1][a] - sVy[b][a]) * s.idx[1];
+        const T dv = exx + eyy;
+        const T dvP = f.has_fP ? dv + f.fP(i, j, 0) : dv;
+        const T ie = sIe[b][a];
+        const T eve = T(1) / (ie + s.inv_Gdt);
+        const T p = f.P_in(i, j, 0) - dvP * eve * s.dtau_Pr;
+        const T t0 = f.txx_in(i, j, 0), o0 = f.txx_o(i, j, 0);
+        const T r0 = -(t0 - o0) * s.inv_Gdt - t0 * ie + T(2.0) * (exx - dv * s.third);
+        const T t1 = f.tyy_in(i, j, 0), o1 = f.tyy_o(i, j, 0);
+        const T r1 = -(t1 - o1) * s.inv_Gdt - t1 * ie + T(2.0) * (eyy - dv * s.third);
+        sTxx[b][a] = t0 + r0 * eve * s.dtau_r;
+        sTyy[b][a] = t1 + r1 * eve * s.dtau_r;
+        sP[b][a] = p;
+        const bool own = a >= 1 && b >= 1;
+        if (own) {
+            f.txx_out(i, j, 0) = sTxx[b][a];
+            f.tyy_out(i, j, 0) = sTyy[b][a];
+            f.P_out(i, j, 0) = p;
+            if (WRITE_RES) f.divV(i, j, 0) = dvP;
+        }
+    }
+    // phase 1b: new tau_xy at vertices (i0+a, j0+b)
+    for (int t = tid; t < CX * CY; t += 256) {
+        const int a = t % CX, b = t / CX;
+        const int i = i0 + a, j = j0 + b;
+        if (i > e0 + 1 || j > e1 + 1) continue;
+        if (i > e0 || j > e1) {  // vertex n+2: outside the launch range, old value
+            sTxy[b][a] = f.txy_in(i, j, 0);
+            continue;
+        }
+        // smem (a+1, b+1) is logical (i, j)
+        const T exy = half * ((sVx[b + 1][a + 1] - sVx[b][a + 1]) * s.idx[1] + (sVy[b + 1][a + 1] - sVy[b + 1][a]) * s.idx[0]);
+        const T e00 = sIe[b][a], e10 = sIe[b][a + 1], e01 = sIe[b + 1][a], e11 = sIe[b + 1][a + 1];
+        const T lo = fma(half, e10 - e00, e00);
+        const T hi = fma(half, e11 - e01, e01);
+        const T iev = fma(half, hi - lo, lo);
+        const T eve = T(1) / (iev + s.inv_Gdt);
+        const T t2 = f.txy_in(i, j, 0), o2 = f.txy_o(i, j, 0);
+        const T r2 = -(t2 - o2) * s.inv_Gdt - t2 * iev + T(2.0) * exy;
+        const T tn = t2 + r2 * eve * s.dtau_r;
+        sTxy[b][a] = tn;
+        if (a < TX && b < TY) f.txy_out(i, j, 0) = tn;
+    }
+    __syncthreads();
+    // phase 2: velocity of the tile's own faces
+    for (int r = 0; r < R; ++r) {
+        const int a = threadIdx.x, b = threadIdx.y + 8 * r;  // tile coords
+        const int i = i0 + a, j = j0 + b;
+        if (i > e0 || j > e1) continue;
+        // cells: smem (a+1, b+1) = (i, j); vertices: smem (a, b) = (i, j)
+        T rx = -((sP[b + 1][a + 1] - sP[b + 1][a]) * s.idx[0]) + (sTxx[b + 1][a + 1] - sTxx[b + 1][a]) * s.idx[0];
+        rx = rx + (sTxy[b + 1][a] - sTxy[b][a]) * s.idx[1];
+        T ry = -((sP[b + 1][a + 1] - sP[b][a + 1]) * s.idx[1]) + (sTyy[b + 1][a + 1] - sTyy[b][a + 1]) * s.idx[1];
+        ry = ry + (sTxy[b][a + 1] - sTxy[b][a]) * s.idx[0];
+        if (f.has_rho) {
+            rx = rx - f.rhox(i, j, 0);
+            ry = ry - f.rhoy(i, j, 0);
+        }
+        if (WRITE_RES) {
+            f.rVx(i, j, 0) = rx;
+            f.rVy(i, j, 0) = ry;
+        }
+        // V at (i, j) is smem (a+1, b+1); cells i-1, i are smem x a, a+1
+        const T c = sIe[b + 1][a + 1];
+        f.Vx_out(i, j, 0) = sVx[b + 1][a + 1] + rx * (s.nu_dtau * (fmin(sIe[b + 1][a], c) + s.inv_Gdt));
+        f.Vy_out(i, j, 0) = sVy[b + 1][a + 1] + ry * (s.nu_dtau * (fmin(sIe[b][a + 1], c) + s.inv_Gdt));
+    }
+}
 
 }  // namespace cgk

@@ -220,6 +220,16 @@ CG_API int cg_stokes_update_thermal(cg_ctx* ctx, const cg_grid* grid, const cg_s
 CG_API int cg_stokes_pt_iterations(cg_ctx* ctx, const cg_grid* grid, const cg_stokes_fields* f,
                             const cg_stokes_params* p, const cg_bc* bc_V, int niter);
 
+/* Ping-pong form of cg_stokes_pt_iterations for 2D variable viscosity: one fused launch per
+ * iteration (update_stress! and update_velocity! together, tiles in shared memory) reading
+ * V, P, tau from `a` and writing them to `b`, then from `b` to `a`, each followed by bc!(V).
+ * `niter` must be even (the result is in `a`). All other fields (tau_old, inv_eta, rho_g,
+ * divV, r_V) are taken from `a`; inv_eta is required. divV and r_V are written on the last
+ * iteration. Values equal the two-kernel form up to FMA contraction. */
+CG_API int cg_stokes_pt_iterations_pp(cg_ctx* ctx, const cg_grid* grid, const cg_stokes_fields* a,
+                                      const cg_stokes_fields* b, const cg_stokes_params* p,
+                                      const cg_bc* bc_V, int niter);
+
 /* Convergence measures of examples/stokes_2d_inc_ve_T.jl:154-157: applies
  * bc!(r_V.d => Dirichlet on dim d) and returns err[0] = max|divV| * tau_scale,
  * err[1 + d] = max|r_V.d| * v_scale. Blocks. */
@@ -246,6 +256,8 @@ typedef struct cg_solve_result {
     int32_t converged;
     double  err[4];           /* last FP64 convergence measures                            */
     double  seconds;          /* device time of the solve (CUDA events)                    */
+    double  err_tau;          /* max constitutive residual * tau_scale (precision CG_F32;
+                                 part of its convergence test, 0 for CG_F64)               */
 } cg_solve_result;
 
 /* Full PT solve of one physical step (examples/stokes_2d_inc_ve_T.jl:144-163) on FP64

@@ -167,3 +167,48 @@ def test_pt_iterations_graph(arch, T, dims, var_eta):
     want = [np.max(np.abs(s.h["divV"].interior()))] + [2.0 * np.max(np.abs(f.interior())) for f in s.h["r_V"]]
     for i in range(nd + 1):
         assert abs(err[i] - want[i]) <= rtol_for(T) * niter * 10 * max(abs(want[i]), 1.0)
+
+
+@pytest.mark.parametrize("T", TYPES)
+@pytest.mark.parametrize("dims", [(45, 38), (70, 33), (33, 97)])
+def test_fused_pingpong_iterations(arch, T, dims):
+    """cg_stokes_pt_iterations_pp (one fused launch per iteration, ping-pong buffers) ==
+    niter x (update_stress!, update_velocity!, bc!(V)) on the oracle."""
+    s = StokesSet(arch, dims, T, 31, True, rho=True)
+    g2 = s.grid
+    rho_full = [random_field(g2, f.loc, T, np.random.default_rng(5)) for f in vec_fields(g2, T)]
+    s.h["rho_g"] = rho_full
+    s.d["rho_g"] = [to_gpu(arch, f) for f in rho_full]
+    ie = NpField(g2, C_, T)
+    ie.a[...] = (1.0 / s.h["eta"].a).astype(T)
+    s.h["inv_eta"] = ie
+    s.d["inv_eta"] = to_gpu(arch, ie)
+    p = pt_params(g2, True)
+    g = g2.desc()
+    bcs = _bc_V(2)
+    bc_apply(g2, s.h["V"], bcs)
+    for f, d in zip(s.h["V"], s.d["V"]):
+        d.from_numpy(f.a)
+    # partner buffers for V, P, tau hold the same initial state
+    partner = {k: ([to_gpu(arch, f) for f in s.h[k]] if isinstance(s.h[k], list) else to_gpu(arch, s.h[k])) for k in ("V", "P", "tau")}
+    hd, da = s.host_desc(), s.dev_desc()
+    from _oracle import stokes_desc as sd
+
+    db = sd(V=partner["V"], P=partner["P"], tau=partner["tau"])
+    niter = 6
+    for _ in range(niter):
+        lib().or_stokes_update_stress(ctypes.byref(g), ctypes.byref(hd), ctypes.byref(p))
+        lib().or_stokes_update_velocity(ctypes.byref(g), ctypes.byref(hd), ctypes.byref(p))
+        bc_apply(g2, s.h["V"], bcs)
+    barr = (_abi.cg_bc * 3)(*bcs)
+    arch.call("cg_stokes_pt_iterations_pp", ctypes.byref(g), ctypes.byref(da), ctypes.byref(db), ctypes.byref(p), barr, niter)
+    arch.synchronize()
+    for name in ("V", "P", "tau", "divV", "r_V"):
+        hv = s.h[name] if isinstance(s.h[name], list) else [s.h[name]]
+        dv = s.d[name] if isinstance(s.d[name], list) else [s.d[name]]
+        for a, b in zip(dv, hv):
+            if b is not None:
+                assert_close(a, b, rtol_for(T) * niter * 10, f"pp {name}")
+    # odd niter is rejected
+    rc = arch.lib.cg_stokes_pt_iterations_pp(arch.ctx, ctypes.byref(g), ctypes.byref(da), ctypes.byref(db), ctypes.byref(p), barr, 3)
+    assert rc == _abi.CG_ERR_ARG
