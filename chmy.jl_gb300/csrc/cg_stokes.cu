@@ -66,10 +66,83 @@ int check_stokes(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f, int n
     return CG_OK;
 }
 
+// Precomputed viscosity arrays of a solve (dense Center layout, halo 1, in the field type):
+// [inv_eta], eta_ve, and per shear component the interpolated 1/eta and its eta_ve.
+struct Pre {
+    char* base = nullptr;
+    long s1 = 0, s2 = 0, count = 0;  // element strides and elements per array
+    int ne = 0;                      // shear components
+    int own_ieta = 0;                // inv_eta computed here (the caller gave only eta)
+};
+
+template <class T>
+DF<T> pre_view(const Pre& pr, int idx) {
+    DF<T> v;
+    v.p = reinterpret_cast<T*>(pr.base) + (long)idx * pr.count + 1 + pr.s1 + pr.s2;
+    v.s1 = pr.s1;
+    v.s2 = pr.s2;
+    return v;
+}
+
+template <class T>
+void apply_pre(SV<T>& v, const Pre* pr) {
+    if (!pr || !pr->base) return;
+    int idx = 0;
+    if (pr->own_ieta) {
+        v.ieta = pre_view<T>(*pr, idx++);
+        v.has_ieta = 1;
+    }
+    v.eveC = pre_view<T>(*pr, idx++);
+    for (int e = 0; e < pr->ne; ++e) {
+        v.ievE[e] = pre_view<T>(*pr, idx++);
+        v.eveE[e] = pre_view<T>(*pr, idx++);
+    }
+    v.has_pre = 1;
+}
+
+template <class T>
+__global__ void inv_kernel(DF<T> dst, DF<T> src, int lo, int e0, int e1, int e2) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + lo;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + lo;
+    if (i > e0 || j > e1) return;
+    for (int k = e2 < 0 ? 0 : lo; k <= (e2 < 0 ? 0 : e2); ++k) dst(i, j, k) = T(1) / src(i, j, k);
+}
+
+// Fill `pr` for the variable-viscosity field set `f` (scratch slot 2) and run the precompute.
 template <class T, int ND>
-int launch_stress(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f, const cg_stokes_params* p, bool res) {
+int setup_pre(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f, const cg_stokes_params* p, Pre* pr) {
+    const long e0 = g->n[0] + 4, e1 = g->n[1] + 4, e2 = ND > 2 ? g->n[2] + 4 : 1;
+    pr->s1 = e0;
+    pr->s2 = ND > 2 ? e0 * e1 : 0;
+    pr->count = e0 * e1 * e2;
+    pr->ne = ND == 2 ? 1 : 3;
+    pr->own_ieta = !cg_present(f->inv_eta);
+    const int narr = pr->own_ieta + 1 + 2 * pr->ne;
+    int rc = CG_OK;
+    pr->base = static_cast<char*>(cg_scratch(ctx, 2, (size_t)narr * pr->count * sizeof(T), &rc));
+    if (rc) return rc;
+    SV<T> v = views<T>(f, ND);
+    const dim3 block(32, 8);
+    if (pr->own_ieta) {
+        // 1/eta over the whole padded range the kernels read (logical -1 .. n+2)
+        const DF<T> dst = pre_view<T>(*pr, 0);
+        const dim3 gi(cg_div_up(g->n[0] + 4, 32), cg_div_up(g->n[1] + 4, 8));
+        inv_kernel<T><<<gi, block, 0, ctx->stream>>>(dst, v.eta, -1, g->n[0] + 2, g->n[1] + 2, ND > 2 ? g->n[2] + 2 : -1);
+        CG_CHECK_LAUNCH(ctx);
+    }
+    apply_pre(v, pr);
+    precompute_kernel<T, ND><<<range_grid<ND>(g, block), block, 0, ctx->stream>>>(v, scalars<T>(g, p), g->n[0] + 1,
+                                                                                 g->n[1] + 1);
+    CG_CHECK_LAUNCH(ctx);
+    return CG_OK;
+}
+
+template <class T, int ND>
+int launch_stress(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f, const cg_stokes_params* p, bool res,
+                  const Pre* pr = nullptr) {
     dim3 block(32, 8);
-    const SV<T> v = views<T>(f, ND);
+    SV<T> v = views<T>(f, ND);
+    apply_pre(v, pr);
     const SP<T> s = scalars<T>(g, p);
     if (res)
         stress_kernel<T, ND, true><<<range_grid<ND>(g, block), block, 0, ctx->stream>>>(v, s, g->n[0] + 1, g->n[1] + 1);
@@ -80,9 +153,11 @@ int launch_stress(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f, cons
 }
 
 template <class T, int ND>
-int launch_velocity(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f, const cg_stokes_params* p, bool res) {
+int launch_velocity(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f, const cg_stokes_params* p, bool res,
+                    const Pre* pr = nullptr) {
     dim3 block(32, 8);
-    const SV<T> v = views<T>(f, ND);
+    SV<T> v = views<T>(f, ND);
+    apply_pre(v, pr);
     const SP<T> s = scalars<T>(g, p);
     if (res)
         velocity_kernel<T, ND, true><<<range_grid<ND>(g, block), block, 0, ctx->stream>>>(v, s, g->n[0] + 1, g->n[1] + 1);
@@ -130,7 +205,7 @@ int apply_bc_V(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f, const c
 }
 
 int pt_iterations(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f, const cg_stokes_params* p,
-                  const cg_bc* bc_V, int niter, int dtype) {
+                  const cg_bc* bc_V, int niter, int dtype, const Pre* pr = nullptr) {
     std::string key = "stokes_pt";
     cg_key_add(key, *g);
     cg_key_add(key, *f);
@@ -139,13 +214,14 @@ int pt_iterations(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f, cons
     cg_bc none[3];
     std::memset(none, 0, sizeof(none));
     for (int d = 0; d < g->ndim; ++d) cg_key_add(key, bc_V ? bc_V[d] : none[d]);
+    cg_key_add(key, pr ? pr->base : nullptr);
     const int nd = g->ndim;
     return cg_graph_run(ctx, key, [&](cudaStream_t) {
         for (int it = 0; it < niter; ++it) {
             const bool last = it == niter - 1;
-            int rc = SDISPATCH(launch_stress, dtype, nd, ctx, g, f, p, last);
+            int rc = SDISPATCH(launch_stress, dtype, nd, ctx, g, f, p, last, pr);
             if (rc) return rc;
-            rc = SDISPATCH(launch_velocity, dtype, nd, ctx, g, f, p, last);
+            rc = SDISPATCH(launch_velocity, dtype, nd, ctx, g, f, p, last, pr);
             if (rc) return rc;
             rc = apply_bc_V(ctx, g, f, bc_V);
             if (rc) return rc;
@@ -358,13 +434,17 @@ extern "C" int cg_stokes_solve(cg_ctx* ctx, const cg_grid* grid, const cg_stokes
         return cg_fail(ctx, CG_ERR_ARG, "stokes_solve: precision must be CG_F64 or CG_F32");
     cudaSetDevice(ctx->device);
     if (o->precision == CG_F32) return cg_stokes_solve_dc(ctx, grid, f, p, bc_V, o, res);
+    // variable viscosity: precompute the viscosity terms once for the whole solve
+    Pre pre;
+    const bool var = cg_present(f->eta) || cg_present(f->inv_eta);
+    if (var && (rc = SDISPATCH(setup_pre, dtype, grid->ndim, ctx, grid, f, p, &pre))) return rc;
     std::memset(res, 0, sizeof(*res));
     CG_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
     int iter = 0;
     int status = CG_ERR_NOCONV;
     while (iter < o->max_iter) {
         const int chunk = std::min(o->ncheck, o->max_iter - iter);
-        if ((rc = pt_iterations(ctx, grid, f, p, bc_V, chunk, dtype))) return rc;
+        if ((rc = pt_iterations(ctx, grid, f, p, bc_V, chunk, dtype, var ? &pre : nullptr))) return rc;
         iter += chunk;
         if (chunk < o->ncheck) break;  // the reference only checks at multiples of ncheck
         int32_t bad = 0;

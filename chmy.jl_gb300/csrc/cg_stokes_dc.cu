@@ -447,8 +447,12 @@ int cg_stokes_solve_dc(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f,
             CG_CUDA(ctx, cudaMemsetAsync(w.dtau2[c].data, 0, padded_count(w.dtau2[c]) * 4, ctx->stream));
         }
         const double target = std::max(0.5 * o->eps, inner_rtol * emax);
+        // stagnation: no 10% gain over a window of 4 n iterations (accelerated PT converges
+        // with oscillations of that period, so shorter windows stop it too early)
+        const int nmax = std::max(g->n[0], std::max(g->n[1], nd > 2 ? g->n[2] : 1));
+        const int window = std::max(4 * nchunk, 4 * nmax);
         double best = 1e300;
-        int stall = 0;
+        int since_best = 0;
         while (total_iter < o->max_iter) {
             if ((rc = chunk())) return rc;
             total_iter += nchunk;
@@ -467,8 +471,8 @@ int cg_stokes_solve_dc(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f,
             if (em < target) break;
             if (em < 0.9 * best) {
                 best = em;
-                stall = 0;
-            } else if (++stall >= 4) {
+                since_best = 0;
+            } else if ((since_best += nchunk) >= window) {
                 break;  // FP32 floor reached: hand back to the FP64 defect
             }
         }

@@ -13,7 +13,11 @@ struct SV {  // device views of the Stokes field set
     // continuity forcing of the defect-correction solve: the pressure update and the divV
     // output use (divV + fP); the deviatoric strain rate uses divV alone
     DF<T> fP;
-    int has_rV, has_divV, has_eta, has_ieta, has_rho[3], has_fP;
+    // precomputed viscosity terms of the variable-viscosity form (bit-identical to computing
+    // them in the kernel; saves the FP64 divisions): eta_ve at cells, and per shear component
+    // the interpolated 1/eta and its eta_ve (2D: [0] = xy; 3D: [0..2] = xy, xz, yz)
+    DF<T> eveC, ievE[3], eveE[3];
+    int has_rV, has_divV, has_eta, has_ieta, has_rho[3], has_fP, has_pre;
     // 1/eta at a cell: the precomputed field when given, else an IEEE division (same bits)
     __device__ __forceinline__ T inv_eta(int i, int j, int k) const {
         return has_ieta ? ieta(i, j, k) : T(1) / eta(i, j, k);
@@ -93,6 +97,38 @@ inline dim3 range_grid(const cg_grid* g, dim3 block) {
     return dim3(cg_div_up(g->n[0] + 2, block.x), cg_div_up(g->n[1] + 2, block.y), ND > 2 ? g->n[2] + 2 : 1);
 }
 
+// 1/eta on the (a, b) shear edge of point I: the Linear rule over the 4 cells around it, dim a
+// innermost (interpolation.jl:217-221), i.e. the harmonic average of eta.
+template <class T>
+__device__ __forceinline__ T shear_inv_eta(const SV<T>& v, int i, int j, int k, int a, int b) {
+    const int ai = a == 0, aj = a == 1, ak = a == 2;
+    const int bi = b == 0, bj = b == 1, bk = b == 2;
+    const T e00 = v.inv_eta(i - ai - bi, j - aj - bj, k - ak - bk);
+    const T e10 = v.inv_eta(i - bi, j - bj, k - bk);
+    const T e01 = v.inv_eta(i - ai, j - aj, k - ak);
+    const T e11 = v.inv_eta(i, j, k);
+    const T lo = fma(T(0.5), e10 - e00, e00);
+    const T hi = fma(T(0.5), e11 - e01, e01);
+    return fma(T(0.5), hi - lo, lo);
+}
+
+// Viscosity terms used by every PT iteration, computed once per solve over [0, n+1]^N with the
+// stress kernel's own expressions (so the values are bit-identical).
+template <class T, int ND>
+__global__ void precompute_kernel(const SV<T> v, const SP<T> s, int e0, int e1) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = ND > 2 ? blockIdx.z : 0;
+    if (i > e0 || j > e1) return;
+    v.eveC(i, j, k) = T(1) / (v.inv_eta(i, j, k) + s.inv_Gdt);
+    const int pairs[3][2] = {{0, 1}, {0, 2}, {1, 2}};
+    for (int e = 0; e < (ND == 2 ? 1 : 3); ++e) {
+        const T iev = shear_inv_eta(v, i, j, k, pairs[e][0], pairs[e][1]);
+        v.ievE[e](i, j, k) = iev;
+        v.eveE[e](i, j, k) = T(1) / (iev + s.inv_Gdt);
+    }
+}
+
 // update_stress! at one point. Tensor order 2D (xx, yy, xy), 3D (xx, yy, zz, xy, xz, yz).
 template <class T, int ND, bool WRITE_RES>
 __global__ void stress_kernel(const SV<T> v, const SP<T> s, int e0, int e1) {
@@ -117,7 +153,7 @@ __global__ void stress_kernel(const SV<T> v, const SP<T> s, int e0, int e1) {
     T ieta_c = T(0), eve_c = s.eta_ve;
     if (v.has_eta) {
         ieta_c = v.inv_eta(i, j, k);
-        eve_c = T(1) / (ieta_c + s.inv_Gdt);
+        eve_c = v.has_pre ? v.eveC(i, j, k) : T(1) / (ieta_c + s.inv_Gdt);
     }
     v.P(i, j, k) = v.P(i, j, k) - dvP * eve_c * s.dtau_Pr;
     auto diag = [&](int c, T edd) {
@@ -134,16 +170,15 @@ __global__ void stress_kernel(const SV<T> v, const SP<T> s, int e0, int e1) {
     auto shear = [&](int c, T eod, int a, int b) {
         const T t = v.tau[c](i, j, k), to = v.tau_old[c](i, j, k);
         if (v.has_eta) {
-            const int ai = a == 0, aj = a == 1, ak = a == 2;
-            const int bi = b == 0, bj = b == 1, bk = b == 2;
-            const T e00 = v.inv_eta(i - ai - bi, j - aj - bj, k - ak - bk);
-            const T e10 = v.inv_eta(i - bi, j - bj, k - bk);
-            const T e01 = v.inv_eta(i - ai, j - aj, k - ak);
-            const T e11 = v.inv_eta(i, j, k);
-            const T lo = fma(T(0.5), e10 - e00, e00);
-            const T hi = fma(T(0.5), e11 - e01, e01);
-            const T iev = fma(T(0.5), hi - lo, lo);
-            const T eve = T(1) / (iev + s.inv_Gdt);
+            T iev, eve;
+            if (v.has_pre) {
+                const int e = ND == 2 ? 0 : c - 3;
+                iev = v.ievE[e](i, j, k);
+                eve = v.eveE[e](i, j, k);
+            } else {
+                iev = shear_inv_eta(v, i, j, k, a, b);
+                eve = T(1) / (iev + s.inv_Gdt);
+            }
             const T r = -(t - to) * s.inv_Gdt - t * iev + T(2.0) * eod;
             v.tau[c](i, j, k) = t + r * eve * s.dtau_r;
         } else {  // examples/stokes_2d_inc_ve_T.jl:30

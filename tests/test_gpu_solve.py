@@ -102,7 +102,10 @@ def test_fp32_defect_correction_reaches_fp64_tolerance(arch, n):
         for fa, fb in zip(ref.fields[name], dc.fields[name]):
             a, b = fa.to_numpy(), fb.to_numpy()
             assert np.max(np.abs(a - b)) <= 1e-5 * max(np.abs(a).max(), 1.0), name
-    pa, pb_ = ref.fields["P"].to_numpy(), dc.fields["P"].to_numpy()
+    # with normal velocity prescribed on every side the pressure is defined up to a constant,
+    # which each PT path fixes differently: compare the interior pressure minus its mean
+    pa, pb_ = ref.fields["P"].to_numpy()[2:-2, 2:-2], dc.fields["P"].to_numpy()[2:-2, 2:-2]
+    pa, pb_ = pa - pa.mean(), pb_ - pb_.mean()
     assert np.max(np.abs(pa - pb_)) <= 1e-5 * np.abs(pa).max()
 
 
