@@ -129,6 +129,14 @@ class cg_solve_result(C.Structure):
     ]
 
 
+class cg_ptdiff_fields(C.Structure):
+    _fields_ = [("C", cg_field), ("C_old", cg_field), ("D", cg_field), ("q", cg_field * 3), ("R", cg_field)]
+
+
+class cg_ptdiff_params(C.Structure):
+    _fields_ = [("dt", C.c_double), ("omega_q", C.c_double), ("dtau_C", C.c_double)]
+
+
 class cg_sia_params(C.Structure):
     _fields_ = [
         ("Gamma", C.c_double),
@@ -189,6 +197,9 @@ SIGNATURES: dict[str, list] = {
         P(cg_solve_opts),
         P(cg_solve_result),
     ],
+    "cg_ptdiff_update_q": [_vp, P(cg_grid), P(cg_ptdiff_fields), P(cg_ptdiff_params)],
+    "cg_ptdiff_update_C": [_vp, P(cg_grid), P(cg_ptdiff_fields), P(cg_ptdiff_params)],
+    "cg_ptdiff_run": [_vp, P(cg_grid), P(cg_ptdiff_fields), P(cg_ptdiff_params), P(cg_bc), C.c_int, C.c_int],
     "cg_sia_update_q": [_vp, P(cg_grid), P(cg_field), P(cg_field), P(cg_field), P(cg_sia_params), P(C.c_double)],
     "cg_sia_update_H": [_vp, P(cg_grid), P(cg_field), P(cg_field), P(cg_field), C.c_double, P(cg_sia_params)],
     "cg_sia_run": [_vp, P(cg_grid), P(cg_field), P(cg_field), P(cg_field), P(cg_sia_params), C.c_int, P(C.c_double)],

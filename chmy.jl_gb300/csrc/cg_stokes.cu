@@ -372,8 +372,8 @@ int pp_iterations_t(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* a, co
     return cg_graph_run(ctx, key, [&](cudaStream_t st) {
         for (int it = 0; it < niter; ++it) {
             const Fused2D<T>& fk = (it % 2 == 0) ? fab : fba;
-            if (res && it == niter - 1) fused2d_kernel<T, 4, true><<<grid, block, 0, st>>>(fk, s, e0, e1);
-            else fused2d_kernel<T, 4, false><<<grid, block, 0, st>>>(fk, s, e0, e1);
+            if (res && it == niter - 1) fused2d_kernel<T, true><<<grid, block, 0, st>>>(fk, s, e0, e1);
+            else fused2d_kernel<T, false><<<grid, block, 0, st>>>(fk, s, e0, e1);
             CG_CHECK_LAUNCH(ctx);
             if (bc_V) {
                 int r = cg_bc_apply_impl(ctx, g, 2, (it % 2 == 0) ? b->V : a->V, bc_V);

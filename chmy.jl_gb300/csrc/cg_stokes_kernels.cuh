@@ -319,87 +319,201 @@ struct Fused2D {
     int has_fP, has_rho;
 };
 
-template <class T, int R, bool WRITE_RES>
-__global__ void __launch_bounds__(256) fused2d_kernel(const Fused2D<T> f, const SP<T> s, int e0, int e1) {
-    constexpr int TX = 32, TY = 8 * R;
-    constexpr int HX = TX + 2, HY = TY + 2;  // V, 1/eta from (i0-1, j0-1)
+// Cell update of the fused kernel: new tau_xx, tau_yy, P at cell (i, j) whose smem coordinates
+// in the staged V / 1/eta tile are (a, b) (the staged tile starts at (i0-1, j0-1)).
+template <class T>
+struct CellIn {
+    T P, txx, tyy, txo, tyo, fp;
+};
+
+template <class T, int HX>
+__device__ __forceinline__ void fused_cell(const Fused2D<T>& f, const SP<T>& s, const T (*sVx)[HX],
+                                           const T (*sVy)[HX], const T (*sIe)[HX], int a, int b, const CellIn<T>& c,
+                                           T& nxx, T& nyy, T& nP, T& dvP_out) {
+    const T exx = (sVx[b][a + 1] - sVx[b][a]) * s.idx[0];
+    const T eyy = (sVy[b + 1][a] - sVy[b][a]) * s.idx[1];
+    const T dv = exx + eyy;
+    const T dvP = f.has_fP ? dv + c.fp : dv;
+    const T ie = sIe[b][a];
+    const T eve = T(1) / (ie + s.inv_Gdt);
+    nP = c.P - dvP * eve * s.dtau_Pr;
+    const T r0 = -(c.txx - c.txo) * s.inv_Gdt - c.txx * ie + T(2.0) * (exx - dv * s.third);
+    const T r1 = -(c.tyy - c.tyo) * s.inv_Gdt - c.tyy * ie + T(2.0) * (eyy - dv * s.third);
+    nxx = c.txx + r0 * eve * s.dtau_r;
+    nyy = c.tyy + r1 * eve * s.dtau_r;
+    dvP_out = dvP;
+}
+
+// Vertex update: new tau_xy at vertex (i, j) = staged smem coordinates (a+1, b+1).
+template <class T, int HX>
+__device__ __forceinline__ T fused_vertex(const SP<T>& s, const T (*sVx)[HX], const T (*sVy)[HX],
+                                          const T (*sIe)[HX], int a, int b, T t2, T o2) {
+    const T half = T(0.5);
+    const T exy = half * ((sVx[b + 1][a + 1] - sVx[b][a + 1]) * s.idx[1] + (sVy[b + 1][a + 1] - sVy[b + 1][a]) * s.idx[0]);
+    const T e00 = sIe[b][a], e10 = sIe[b][a + 1], e01 = sIe[b + 1][a], e11 = sIe[b + 1][a + 1];
+    const T lo = fma(half, e10 - e00, e00);
+    const T hi = fma(half, e11 - e01, e01);
+    const T iev = fma(half, hi - lo, lo);
+    const T eve = T(1) / (iev + s.inv_Gdt);
+    const T r2 = -(t2 - o2) * s.inv_Gdt - t2 * iev + T(2.0) * exy;
+    return t2 + r2 * eve * s.dtau_r;
+}
+
+template <class T>
+__device__ __forceinline__ CellIn<T> load_cell(const Fused2D<T>& f, int i, int j) {
+    CellIn<T> c;
+    c.P = f.P_in(i, j, 0);
+    c.txx = f.txx_in(i, j, 0);
+    c.tyy = f.tyy_in(i, j, 0);
+    c.txo = f.txx_o(i, j, 0);
+    c.tyo = f.tyy_o(i, j, 0);
+    c.fp = f.has_fP ? f.fP(i, j, 0) : T(0);
+    return c;
+}
+
+// Block (32, 8), tile 32 x 32 of launch points; every global load of a thread is issued before
+// the first barrier (own cells, vertices and faces in registers, V and 1/eta staged in shared
+// memory), so that ~50 loads per thread are in flight at once.
+template <class T, bool WRITE_RES>
+__global__ void __launch_bounds__(256, 2) fused2d_kernel(const Fused2D<T> f, const SP<T> s, int e0, int e1) {
+    constexpr int TX = 32, R = 4, TY = 8 * R;
+    constexpr int HX = TX + 2, HY = TY + 2;  // V, 1/eta staged from (i0-1, j0-1)
     constexpr int CX = TX + 1, CY = TY + 1;  // new cells from (i0-1, j0-1); new vertices from (i0, j0)
     __shared__ T sVx[HY][HX], sVy[HY][HX], sIe[HY][HX];
     __shared__ T sTxx[CY][CX], sTyy[CY][CX], sP[CY][CX], sTxy[CY][CX];
+    const int tx = threadIdx.x, ty = threadIdx.y;
     const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
-    const int tid = threadIdx.y * 32 + threadIdx.x;
-    // stage V and 1/eta over logical [i0-1, i0+TX] x [j0-1, j0+TY], clipped to [-1, n+2]
-    for (int t = tid; t < HX * HY; t += 256) {
-        const int a = t % HX, b = t / HX;
-        const int i = i0 - 1 + a, j = j0 - 1 + b;
-        const bool ok = i <= e0 + 1 && j <= e1 + 1;
-        sVx[b][a] = ok ? f.Vx_in(i, j, 0) : T(0);
-        sVy[b][a] = ok ? f.Vy_in(i, j, 0) : T(0);
-        sIe[b][a] = ok ? f.ieta(i, j, 0) : T(0);
+    const int i = i0 + tx;
+
+    // ---- loads: own cells / vertices / faces at (i, j0 + ty + 8r) ----
+    CellIn<T> cin[R];
+    T vxy[R], vxo[R], rhx[R], rhy[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int j = j0 + ty + 8 * r;
+        const bool cell_in = i <= e0 && j <= e1;
+        const bool vert_in = i <= e0 + 1 && j <= e1 + 1;
+        if (cell_in) cin[r] = load_cell(f, i, j);
+        vxy[r] = vert_in ? f.txy_in(i, j, 0) : T(0);
+        vxo[r] = cell_in ? f.txy_o(i, j, 0) : T(0);
+        rhx[r] = (cell_in && f.has_rho) ? f.rhox(i, j, 0) : T(0);
+        rhy[r] = (cell_in && f.has_rho) ? f.rhoy(i, j, 0) : T(0);
+    }
+    // halo items: warp 0 cell row j0-1 (a = tx, and a = 32 for lane 0); warp 1 cell column i0-1;
+    // warp 2 vertex row j0+32; warp 3 vertex column i0+32 (and the corner for lane 0)
+    CellIn<T> hc[2];
+    T hv[2], hvo[2];
+    int hi_[2], hj_[2], hn = 0;
+    if (ty == 0) {
+        hi_[0] = i0 - 1 + tx;
+        hj_[0] = j0 - 1;
+        hi_[1] = i0 - 1 + 32;
+        hj_[1] = j0 - 1;
+        hn = tx == 0 ? 2 : 1;
+    } else if (ty == 1) {
+        hi_[0] = i0 - 1;
+        hj_[0] = j0 + tx;
+        hn = 1;
+    } else if (ty == 2) {
+        hi_[0] = i0 + tx;
+        hj_[0] = j0 + 32;
+        hn = 1;
+    } else if (ty == 3) {
+        hi_[0] = i0 + 32;
+        hj_[0] = j0 + tx;
+        hi_[1] = i0 + 32;
+        hj_[1] = j0 + 32;
+        hn = tx == 0 ? 2 : 1;
+    }
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        if (h >= hn) break;
+        const int hi = hi_[h], hj = hj_[h];
+        if (ty <= 1) {
+            if (hi <= e0 && hj <= e1) hc[h] = load_cell(f, hi, hj);
+        } else {
+            hv[h] = (hi <= e0 + 1 && hj <= e1 + 1) ? f.txy_in(hi, hj, 0) : T(0);
+            hvo[h] = (hi <= e0 && hj <= e1) ? f.txy_o(hi, hj, 0) : T(0);
+        }
+    }
+    // staged V and 1/eta over logical [i0-1, i0+32] x [j0-1, j0+32], clipped to [-1, n+2]
+#pragma unroll
+    for (int bb = 0; bb < (HY + 7) / 8; ++bb) {
+        const int b = ty + 8 * bb;
+        if (b >= HY) break;
+#pragma unroll
+        for (int aa = 0; aa < 2; ++aa) {
+            const int a = tx + 32 * aa;
+            if (a >= HX) break;
+            const int ii = i0 - 1 + a, jj = j0 - 1 + b;
+            const bool ok = ii <= e0 + 1 && jj <= e1 + 1;
+            sVx[b][a] = ok ? f.Vx_in(ii, jj, 0) : T(0);
+            sVy[b][a] = ok ? f.Vy_in(ii, jj, 0) : T(0);
+            sIe[b][a] = ok ? f.ieta(ii, jj, 0) : T(0);
+        }
     }
     __syncthreads();
-    const T half = T(0.5);
-    // phase 1a: new tau_xx, tau_yy, P at cells (i0-1+a, j0-1+b)
-    for (int t = tid; t < CX * CY; t += 256) {
-        const int a = t % CX, b = t / CX;
-        const int i = i0 - 1 + a, j = j0 - 1 + b;
-        if (i > e0 || j > e1) continue;  // never read by an in-range face
-        if (i < 0 || j < 0) {            // outside the launch range: old values
-            sTxx[b][a] = f.txx_in(i, j, 0);
-            sTyy[b][a] = f.tyy_in(i, j, 0);
-            sP[b][a] = f.P_in(i, j, 0);
-            continue;
-        }
-        // V.x at (i, j), (i+1, j): smem (a, b+... ) with offsets (a, b) -> logical (i0-1+a, j0-1+b)
-        const T exx = (sVx[b][a + 1] - sVx[b][a]) * s.idx[0];
-        const T eyy = (sVy[b + 1][a] - sVy[b][a]) * s.idx[1];
-        const T dv = exx + eyy;
-        const T dvP = f.has_fP ? dv + f.fP(i, j, 0) : dv;
-        const T ie = sIe[b][a];
-        const T eve = T(1) / (ie + s.inv_Gdt);
-        const T p = f.P_in(i, j, 0) - dvP * eve * s.dtau_Pr;
-        const T t0 = f.txx_in(i, j, 0), o0 = f.txx_o(i, j, 0);
-        const T r0 = -(t0 - o0) * s.inv_Gdt - t0 * ie + T(2.0) * (exx - dv * s.third);
-        const T t1 = f.tyy_in(i, j, 0), o1 = f.tyy_o(i, j, 0);
-        const T r1 = -(t1 - o1) * s.inv_Gdt - t1 * ie + T(2.0) * (eyy - dv * s.third);
-        sTxx[b][a] = t0 + r0 * eve * s.dtau_r;
-        sTyy[b][a] = t1 + r1 * eve * s.dtau_r;
-        sP[b][a] = p;
-        const bool own = a >= 1 && b >= 1;
-        if (own) {
-            f.txx_out(i, j, 0) = sTxx[b][a];
-            f.tyy_out(i, j, 0) = sTyy[b][a];
-            f.P_out(i, j, 0) = p;
+
+    // ---- phase 1: new tau/P at own cells and vertices, then the halo ones ----
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int j = j0 + ty + 8 * r;
+        const int a = tx + 1, b = ty + 1 + 8 * r;  // cell smem coords
+        if (i <= e0 && j <= e1) {
+            T nxx, nyy, nP, dvP;
+            fused_cell<T, HX>(f, s, sVx, sVy, sIe, a, b, cin[r], nxx, nyy, nP, dvP);
+            sTxx[b][a] = nxx;
+            sTyy[b][a] = nyy;
+            sP[b][a] = nP;
+            f.txx_out(i, j, 0) = nxx;
+            f.tyy_out(i, j, 0) = nyy;
+            f.P_out(i, j, 0) = nP;
             if (WRITE_RES) f.divV(i, j, 0) = dvP;
         }
-    }
-    // phase 1b: new tau_xy at vertices (i0+a, j0+b)
-    for (int t = tid; t < CX * CY; t += 256) {
-        const int a = t % CX, b = t / CX;
-        const int i = i0 + a, j = j0 + b;
-        if (i > e0 + 1 || j > e1 + 1) continue;
-        if (i > e0 || j > e1) {  // vertex n+2: outside the launch range, old value
-            sTxy[b][a] = f.txy_in(i, j, 0);
-            continue;
+        // own vertex (tx, ty + 8r): in range -> new value; the vertex n+2 -> old value
+        const int va = tx, vb = ty + 8 * r;
+        if (i <= e0 + 1 && j <= e1 + 1) {
+            if (i <= e0 && j <= e1) {
+                const T tn = fused_vertex<T, HX>(s, sVx, sVy, sIe, va, vb, vxy[r], vxo[r]);
+                sTxy[vb][va] = tn;
+                f.txy_out(i, j, 0) = tn;
+            } else {
+                sTxy[vb][va] = vxy[r];
+            }
         }
-        // smem (a+1, b+1) is logical (i, j)
-        const T exy = half * ((sVx[b + 1][a + 1] - sVx[b][a + 1]) * s.idx[1] + (sVy[b + 1][a + 1] - sVy[b + 1][a]) * s.idx[0]);
-        const T e00 = sIe[b][a], e10 = sIe[b][a + 1], e01 = sIe[b + 1][a], e11 = sIe[b + 1][a + 1];
-        const T lo = fma(half, e10 - e00, e00);
-        const T hi = fma(half, e11 - e01, e01);
-        const T iev = fma(half, hi - lo, lo);
-        const T eve = T(1) / (iev + s.inv_Gdt);
-        const T t2 = f.txy_in(i, j, 0), o2 = f.txy_o(i, j, 0);
-        const T r2 = -(t2 - o2) * s.inv_Gdt - t2 * iev + T(2.0) * exy;
-        const T tn = t2 + r2 * eve * s.dtau_r;
-        sTxy[b][a] = tn;
-        if (a < TX && b < TY) f.txy_out(i, j, 0) = tn;
+    }
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        if (h >= hn) break;
+        const int hi = hi_[h], hj = hj_[h];
+        if (ty <= 1) {
+            const int a = hi - (i0 - 1), b = hj - (j0 - 1);
+            if (hi > e0 || hj > e1) continue;
+            if (hi < 0 || hj < 0) {  // outside the launch range: old values
+                sTxx[b][a] = hc[h].txx;
+                sTyy[b][a] = hc[h].tyy;
+                sP[b][a] = hc[h].P;
+            } else {
+                T nxx, nyy, nP, dvP;
+                fused_cell<T, HX>(f, s, sVx, sVy, sIe, a, b, hc[h], nxx, nyy, nP, dvP);
+                sTxx[b][a] = nxx;
+                sTyy[b][a] = nyy;
+                sP[b][a] = nP;
+            }
+        } else {
+            const int a = hi - i0, b = hj - j0;
+            if (hi > e0 + 1 || hj > e1 + 1) continue;
+            if (hi > e0 || hj > e1) sTxy[b][a] = hv[h];
+            else sTxy[b][a] = fused_vertex<T, HX>(s, sVx, sVy, sIe, a, b, hv[h], hvo[h]);
+        }
     }
     __syncthreads();
-    // phase 2: velocity of the tile's own faces
+
+    // ---- phase 2: velocity of the tile's own faces ----
+#pragma unroll
     for (int r = 0; r < R; ++r) {
-        const int a = threadIdx.x, b = threadIdx.y + 8 * r;  // tile coords
-        const int i = i0 + a, j = j0 + b;
+        const int a = tx, b = ty + 8 * r;
+        const int j = j0 + b;
         if (i > e0 || j > e1) continue;
         // cells: smem (a+1, b+1) = (i, j); vertices: smem (a, b) = (i, j)
         T rx = -((sP[b + 1][a + 1] - sP[b + 1][a]) * s.idx[0]) + (sTxx[b + 1][a + 1] - sTxx[b + 1][a]) * s.idx[0];
@@ -407,14 +521,13 @@ __global__ void __launch_bounds__(256) fused2d_kernel(const Fused2D<T> f, const 
         T ry = -((sP[b + 1][a + 1] - sP[b][a + 1]) * s.idx[1]) + (sTyy[b + 1][a + 1] - sTyy[b][a + 1]) * s.idx[1];
         ry = ry + (sTxy[b][a + 1] - sTxy[b][a]) * s.idx[0];
         if (f.has_rho) {
-            rx = rx - f.rhox(i, j, 0);
-            ry = ry - f.rhoy(i, j, 0);
+            rx = rx - rhx[r];
+            ry = ry - rhy[r];
         }
         if (WRITE_RES) {
             f.rVx(i, j, 0) = rx;
             f.rVy(i, j, 0) = ry;
         }
-        // V at (i, j) is smem (a+1, b+1); cells i-1, i are smem x a, a+1
         const T c = sIe[b + 1][a + 1];
         f.Vx_out(i, j, 0) = sVx[b + 1][a + 1] + rx * (s.nu_dtau * (fmin(sIe[b + 1][a], c) + s.inv_Gdt));
         f.Vy_out(i, j, 0) = sVy[b + 1][a + 1] + ry * (s.nu_dtau * (fmin(sIe[b][a + 1], c) + s.inv_Gdt));

@@ -266,6 +266,36 @@ CG_API int cg_stokes_solve(cg_ctx* ctx, const cg_grid* grid, const cg_stokes_fie
                     const cg_stokes_params* p, const cg_bc* bc_V, const cg_solve_opts* o,
                     cg_solve_result* res);
 
+/* ---- pseudo-transient variable-coefficient diffusion -------------------------------------
+ * Implicit (backward Euler) diffusion step (C - C_old)/dt = divg(D grad C) solved by damped
+ * PT iterations in the pattern of the Stokes PT loop; the flux is Chmy's ∂k∂/divg_grad form
+ * q = -lerp(D) ∂C (src/GridOperators/partial_derivatives.jl:14-21). Over I in [0, n+1]^N:
+ *   update_q:  q_d += (-(lerp(D -> face_d) * ∂_d C) - q_d) * omega_q
+ *   update_C:  R = -(C - C_old) / dt - divg(q);  C += R * dtau_C   (R written if given)
+ * then bc!(C => bc). Typical parameters (accelerated PT for diffusion): vdtau = min(Δ)/
+ * sqrt(N 1.1), Re = pi + sqrt(pi^2 + l^2/(D_max dt)), theta = l/(Re vdtau),
+ * beta = Re D_max/(vdtau l), omega_q = 1/(1 + theta), dtau_C = 1/(beta + 1/dt). */
+typedef struct cg_ptdiff_fields {
+    cg_field C, C_old, D, q[3];
+    cg_field R; /* optional residual output */
+} cg_ptdiff_fields;
+
+typedef struct cg_ptdiff_params {
+    double dt;
+    double omega_q;
+    double dtau_C;
+} cg_ptdiff_params;
+
+CG_API int cg_ptdiff_update_q(cg_ctx* ctx, const cg_grid* grid, const cg_ptdiff_fields* f,
+                              const cg_ptdiff_params* p);
+CG_API int cg_ptdiff_update_C(cg_ctx* ctx, const cg_grid* grid, const cg_ptdiff_fields* f,
+                              const cg_ptdiff_params* p);
+/* `nsteps` implicit steps of `npt` PT iterations each (C_old <- C at the start of every step;
+ * bc!(C => bc) after every iteration), replayed from one CUDA graph. R (if given) holds the
+ * residual of the last iteration. */
+CG_API int cg_ptdiff_run(cg_ctx* ctx, const cg_grid* grid, const cg_ptdiff_fields* f,
+                         const cg_ptdiff_params* p, const cg_bc* bc, int nsteps, int npt);
+
 /* ---- shallow ice (examples/sia.jl) ----------------------------------------------------- */
 
 /* Parameters of the SIA step. examples/sia.jl:24-54 is Gamma = 1, As = 0.5, n = 3, beta = 0.5,

@@ -607,6 +607,43 @@ void op_kernel_t(int op, const cg_grid* grid, const cg_field* C, const cg_field*
     });
 }
 
+/* ---- PT variable-coefficient diffusion (no reference example; restated from the PT pattern
+ *      of examples/stokes_2d_inc_ve_T.jl and the ∂k∂ flux of partial_derivatives.jl:14-21) --- */
+
+template <class T>
+void ptdiff_update_q_t(const cg_grid* grid, const cg_ptdiff_fields* f, const cg_ptdiff_params* p) {
+    GridT<T> g(*grid);
+    Fd<T> C(f->C), D(f->D), q[3];
+    for (int d = 0; d < g.nd; ++d) q[d] = Fd<T>(f->q[d]);
+    const T om = (T)p->omega_q;
+    launch_range(g, [&](int i, int j, int k) {
+        for (int d = 0; d < g.nd; ++d) {
+            /* lerp(D, face_d): D Center seen from the face -> cells I-e_d, I */
+            int Il[3] = {i, j, k};
+            Il[d] -= 1;
+            const T dl = D.at(Il), dc = D(i, j, k);
+            const T Df = std::fma(T(0.5), dc - dl, dl);
+            const T gC = partial(C, g, d, i, j, k);
+            const T qo = q[d](i, j, k);
+            q[d](i, j, k) = qo + (-(Df * gC) - qo) * om;
+        }
+    });
+}
+
+template <class T>
+void ptdiff_update_C_t(const cg_grid* grid, const cg_ptdiff_fields* f, const cg_ptdiff_params* p) {
+    GridT<T> g(*grid);
+    Fd<T> C(f->C), Co(f->C_old), R(f->R), q[3];
+    for (int d = 0; d < g.nd; ++d) q[d] = Fd<T>(f->q[d]);
+    const T inv_dt = T(1) / (T)p->dt, dtc = (T)p->dtau_C;
+    launch_range(g, [&](int i, int j, int k) {
+        const T c = C(i, j, k);
+        const T r = -(c - Co(i, j, k)) * inv_dt - divg(q, g, i, j, k);
+        if (R.ok()) R(i, j, k) = r;
+        C(i, j, k) = c + r * dtc;
+    });
+}
+
 /* ---- shallow ice (examples/sia.jl) --------------------------------------------------- */
 
 /* x^m by repeated multiplication (the restatement of Julia's integer power). */
@@ -782,6 +819,18 @@ int or_stokes_update_thermal_flux(const cg_grid* grid, const cg_stokes_fields* f
 int or_stokes_update_thermal(const cg_grid* grid, const cg_stokes_fields* f, const cg_stokes_params* p) {
     if (f->T.dtype == CG_F64) stokes_update_thermal_t<double>(grid, f, p);
     else stokes_update_thermal_t<float>(grid, f, p);
+    return CG_OK;
+}
+
+int or_ptdiff_update_q(const cg_grid* grid, const cg_ptdiff_fields* f, const cg_ptdiff_params* p) {
+    if (f->C.dtype == CG_F64) ptdiff_update_q_t<double>(grid, f, p);
+    else ptdiff_update_q_t<float>(grid, f, p);
+    return CG_OK;
+}
+
+int or_ptdiff_update_C(const cg_grid* grid, const cg_ptdiff_fields* f, const cg_ptdiff_params* p) {
+    if (f->C.dtype == CG_F64) ptdiff_update_C_t<double>(grid, f, p);
+    else ptdiff_update_C_t<float>(grid, f, p);
     return CG_OK;
 }
 

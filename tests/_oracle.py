@@ -34,6 +34,8 @@ _SIGS = {
     "or_stokes_update_velocity": ([P(_abi.cg_grid), P(_abi.cg_stokes_fields), P(_abi.cg_stokes_params)], C.c_int),
     "or_stokes_update_thermal_flux": ([P(_abi.cg_grid), P(_abi.cg_stokes_fields), P(_abi.cg_stokes_params)], C.c_int),
     "or_stokes_update_thermal": ([P(_abi.cg_grid), P(_abi.cg_stokes_fields), P(_abi.cg_stokes_params)], C.c_int),
+    "or_ptdiff_update_q": ([P(_abi.cg_grid), P(_abi.cg_ptdiff_fields), P(_abi.cg_ptdiff_params)], C.c_int),
+    "or_ptdiff_update_C": ([P(_abi.cg_grid), P(_abi.cg_ptdiff_fields), P(_abi.cg_ptdiff_params)], C.c_int),
     "or_sia_update_q": (
         [P(_abi.cg_grid), P(_abi.cg_field), P(_abi.cg_field), P(_abi.cg_field), P(_abi.cg_sia_params), P(C.c_double)],
         C.c_int,
