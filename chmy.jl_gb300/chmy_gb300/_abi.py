@@ -168,6 +168,7 @@ SIGNATURES: dict[str, list] = {
     "cg_field_download": [_vp, P(cg_field), _vp],
     "cg_bc_apply": [_vp, P(cg_grid), C.c_int, P(cg_field), P(cg_bc)],
     "cg_maxabs": [_vp, C.c_int, P(cg_field), P(C.c_double), P(C.c_int32)],
+    "cg_maxabs_noalloc": [C.c_int, _vp, C.c_int, P(cg_field), P(C.c_double), P(C.c_int32)],
     "cg_diffusion_compute_q": [_vp, P(cg_grid), P(cg_field), P(cg_field), C.c_double],
     "cg_diffusion_update_C": [_vp, P(cg_grid), P(cg_field), P(cg_field), C.c_double],
     "cg_diffusion_step": [_vp, P(cg_grid), P(cg_field), P(cg_field), C.c_double, C.c_double, P(cg_bc)],

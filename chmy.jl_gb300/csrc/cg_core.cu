@@ -1,6 +1,7 @@
 // cg_core.cu — context, memory, argument checks, the fused boundary-condition kernel and the
 // max-norm reduction of libchmy_gb300.
 #include <cstdarg>
+#include <mutex>
 #include <vector>
 
 #include "cg_common.cuh"
@@ -604,4 +605,121 @@ extern "C" int cg_maxabs(cg_ctx* ctx, int nfields, const cg_field* fields, doubl
     int rc = cg_maxabs_enqueue(ctx, nfields, fields);
     if (rc) return rc;
     return cg_maxabs_collect(ctx, nfields, fields, out_host, nonfinite);
+}
+
+// ---- max-norm without any allocation ----------------------------------------------------------
+//
+// For callers that cannot allocate device memory: hosts whose memory is owned by their own pool
+// (a Julia or Python runtime that forbids foreign cudaMalloc), code running while a stream is
+// being captured into a CUDA graph, or embedded settings with a fixed memory budget. The
+// reduction slots live in this file-scope device array instead of a context's buffer. Every
+// GPU that loads the library holds these 128 bytes until the process exits.
+
+constexpr int kNoAllocMaxFields = CG_MAXABS_NOALLOC_MAX_FIELDS;
+static __device__ __align__(256) unsigned long long g_noalloc_red[kNoAllocMaxFields];
+
+namespace {
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+unsigned long long* g_noalloc_addr[kNoAllocMaxDevices] = {};  // device address per device
+char g_noalloc_err[256] = "";
+
+int noalloc_fail(int code, const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_noalloc_err, sizeof(g_noalloc_err), fmt, ap);
+    va_end(ap);
+    return cg_fail(nullptr, code, "%s", g_noalloc_err);
+}
+}  // namespace
+
+extern "C" int cg_maxabs_noalloc(int device, void* stream, int nfields, const cg_field* fields, double* out_host,
+                                 int32_t* nonfinite) {
+    if (!fields || !out_host) return noalloc_fail(CG_ERR_ARG, "cg_maxabs_noalloc: NULL argument");
+    if (nfields < 1 || nfields > kNoAllocMaxFields)
+        return noalloc_fail(CG_ERR_ARG, "cg_maxabs_noalloc: nfields %d outside 1..%d (the fixed scratch holds %d slots)",
+                            nfields, kNoAllocMaxFields, kNoAllocMaxFields);
+    if (device < 0 || device >= kNoAllocMaxDevices)
+        return noalloc_fail(CG_ERR_ARG, "cg_maxabs_noalloc: device %d outside 0..%d", device, kNoAllocMaxDevices - 1);
+    int prev = -1;
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) return noalloc_fail(CG_ERR_CUDA, "cudaSetDevice(%d): %s", device, cudaGetErrorString(e));
+    auto restore = [&]() {
+        if (prev >= 0 && prev != device) cudaSetDevice(prev);
+    };
+    // one-time set-up per device (with that device current): the host-side name of the array
+    // is not a device address, so fetch the device address of the symbol
+    unsigned long long* slots = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_noalloc_mu);
+        if (!g_noalloc_addr[device]) {
+            void* p = nullptr;
+            e = cudaGetSymbolAddress(&p, g_noalloc_red);
+            if (e != cudaSuccess) {
+                restore();
+                return noalloc_fail(CG_ERR_CUDA, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+            }
+            g_noalloc_addr[device] = static_cast<unsigned long long*>(p);
+        }
+        slots = g_noalloc_addr[device];
+    }
+    RedBatch b;
+    std::memset(&b, 0, sizeof(b));
+    b.nfields = nfields;
+    long biggest = 1;
+    for (int i = 0; i < nfields; ++i) {
+        const cg_field& f = fields[i];
+        if (!f.data || (f.dtype != CG_F32 && f.dtype != CG_F64) || f.ndim < 1 || f.ndim > 3) {
+            restore();
+            return noalloc_fail(CG_ERR_ARG, "cg_maxabs_noalloc: field %d invalid", i);
+        }
+        const int esz = f.dtype == CG_F64 ? 8 : 4;
+        long off = cg_origin_offset(f);
+        for (int d = 0; d < f.ndim; ++d) off += f.stride[d];
+        RedField& R = b.f[i];
+        R.p = static_cast<const char*>(f.data) + off * esz;
+        R.s1 = f.ndim > 1 ? f.stride[1] : 0;
+        R.s2 = f.ndim > 2 ? f.stride[2] : 0;
+        R.n0 = f.n[0];
+        R.n1 = f.ndim > 1 ? f.n[1] : 1;
+        R.n2 = f.ndim > 2 ? f.n[2] : 1;
+        R.is64 = f.dtype == CG_F64;
+        biggest = std::max(biggest, (long)R.n0 * R.n1 * R.n2);
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    int sms = 1;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    // the slots keep the previous call's maxima: clear them first
+    e = cudaMemsetAsync(slots, 0, sizeof(unsigned long long) * nfields, st);
+    if (e == cudaSuccess) {
+        const int threads = 512;
+        const int blocks = std::max(1, (int)std::min<long>(cg_div_up(biggest, threads), (long)sms * 4));
+        maxabs_kernel<<<dim3(blocks, nfields), threads, 0, st>>>(b, slots);
+        e = cudaGetLastError();
+    }
+    unsigned long long host_bits[kNoAllocMaxFields];
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(host_bits, slots, sizeof(unsigned long long) * nfields, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    restore();
+    if (e != cudaSuccess) return noalloc_fail(CG_ERR_CUDA, "cg_maxabs_noalloc: %s", cudaGetErrorString(e));
+    int bad = 0;
+    for (int i = 0; i < nfields; ++i) {
+        const unsigned long long v = host_bits[i];
+        if (fields[i].dtype == CG_F64) {
+            double x;
+            std::memcpy(&x, &v, 8);
+            out_host[i] = x;
+            if (v >= 0x7FF0000000000000ull) bad = 1;
+        } else {
+            const unsigned u = (unsigned)v;
+            float x;
+            std::memcpy(&x, &u, 4);
+            out_host[i] = (double)x;
+            if (u >= 0x7F800000u) bad = 1;
+        }
+    }
+    if (nonfinite) *nonfinite = bad;
+    return CG_OK;
 }

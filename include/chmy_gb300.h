@@ -137,6 +137,25 @@ CG_API int cg_bc_apply(cg_ctx* ctx, const cg_grid* grid, int nfields, const cg_f
 CG_API int cg_maxabs(cg_ctx* ctx, int nfields, const cg_field* fields, double* out_host,
               int32_t* nonfinite);
 
+/* The same max-norm reduction for callers that cannot allocate device memory: a host
+ * runtime that owns all device memory through its own pool, code issued while a stream is
+ * being captured into a CUDA graph, or a deployment with a fixed memory budget. It needs no
+ * context and calls no cudaMalloc/cudaFree (nor any allocating library routine): its
+ * reduction slots are a fixed array of CG_MAXABS_NOALLOC_MAX_FIELDS 64-bit words in the
+ * library's device memory, which every GPU that loads the library keeps until exit.
+ * This entry point has no counterpart in the reference.
+ * - `device`: CUDA ordinal to run on (made current for the call, then restored); `stream`:
+ *   a cudaStream_t or NULL. Blocks until the values are on the host.
+ * - nfields above CG_MAXABS_NOALLOC_MAX_FIELDS is rejected with CG_ERR_ARG.
+ * - The first call on a device looks up the array's device address (once per device); make
+ *   that first call before any stream capture.
+ * - All calls share the array (the slots are cleared at the start of each call): calls
+ *   that overlap on the GPU race and must not be issued concurrently.
+ * Errors are reported through cg_last_error(NULL). */
+#define CG_MAXABS_NOALLOC_MAX_FIELDS 16
+CG_API int cg_maxabs_noalloc(int device, void* stream, int nfields, const cg_field* fields,
+                             double* out_host, int32_t* nonfinite);
+
 /* ---- explicit diffusion (examples/diffusion_2d.jl:8-19, diffusion_2d_perf.jl:11-23) -- */
 
 /* compute_q!: q.d = -chi * d(C)/dx_d at I in [0, n+1]^N. `q` holds ndim face fields. */
