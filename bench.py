@@ -346,21 +346,7 @@ def run_ours(args, rank, world, dist):
     # roofline: the fused FP32 PT kernel timed alone (public ping-pong entry, no bc), CUDA events
     # on the launching stream, algorithmic bytes per launch over the mean launch time
     g = pb.grid
-    from chmy_gb300.grids import Center, Vertex
-
-    def f32(loc):
-        return Field(arch, g, loc, np.float32)
-
-    Cl, Vl = Center(), Vertex()
-    A = dict(V=[f32((Vl, Cl)), f32((Cl, Vl))], P=f32(Cl), tau=[f32(Cl), f32(Cl), f32(Vl)])
-    B = dict(V=[f32((Vl, Cl)), f32((Cl, Vl))], P=f32(Cl), tau=[f32(Cl), f32(Cl), f32(Vl)])
-    extra = dict(tau_old=[f32(Cl), f32(Cl), f32(Vl)], inv_eta=f32(Cl), rho_g=[f32((Vl, Cl)), f32((Cl, Vl))])
-    extra["inv_eta"].data.copy_((1.0 / solver.fields["eta"].data).float())
-    for lst in (A["V"], B["V"]):
-        for f, src in zip(lst, solver.fields["V"]):
-            f.data.copy_(src.data.float())
-    da = stokes_fields(V=A["V"], P=A["P"], tau=A["tau"], **extra)
-    db = stokes_fields(V=B["V"], P=B["P"], tau=B["tau"])
+    da, db, _keep = fused_kernel_fields(arch, pb)
     gd = g.desc()
     reps = 200
     arch.call("cg_stokes_pt_iterations_pp", ctypes.byref(gd), ctypes.byref(da), ctypes.byref(db), ctypes.byref(pb.params), None, 20)
@@ -447,8 +433,67 @@ def run_ours(args, rank, world, dist):
     arch.close()
 
 
+def fused_kernel_fields(arch, pb):
+    """FP32 ping-pong field sets of the fused 2D PT kernel on the problem's grid (V from the
+    initial state, 1/eta from eta, zero tau/P/tau_old/rho_g)."""
+    import torch
+
+    from chmy_gb300 import Field
+    from chmy_gb300.grids import Center, Vertex
+    from chmy_gb300.kernels import stokes_fields
+
+    g = pb.grid
+    Cl, Vl = Center(), Vertex()
+
+    def f32(loc):
+        return Field(arch, g, loc, np.float32)
+
+    A = dict(V=[f32((Vl, Cl)), f32((Cl, Vl))], P=f32(Cl), tau=[f32(Cl), f32(Cl), f32(Vl)])
+    B = dict(V=[f32((Vl, Cl)), f32((Cl, Vl))], P=f32(Cl), tau=[f32(Cl), f32(Cl), f32(Vl)])
+    extra = dict(tau_old=[f32(Cl), f32(Cl), f32(Vl)], inv_eta=f32(Cl), rho_g=[f32((Vl, Cl)), f32((Cl, Vl))])
+    extra["inv_eta"].data.copy_(torch.from_numpy(1.0 / pb.host["eta"]).float())
+    for lst in (A["V"], B["V"]):
+        for f, a in zip(lst, pb.host["V"]):
+            f.data.copy_(torch.from_numpy(a).float())
+    keep = (A, B, extra)
+    return stokes_fields(V=A["V"], P=A["P"], tau=A["tau"], **extra), stokes_fields(V=B["V"], P=B["P"], tau=B["tau"]), keep
+
+
+def run_kernel(args):
+    """--kernel fused2d: only the fused FP32 PT kernel, `--reps` launches timed with CUDA events
+    (the command the committed ncu summaries were captured with)."""
+    import torch
+
+    from chmy_gb300 import Arch, GB300Backend
+    from chmy_gb300.configs import stokes2d_inclusions
+
+    arch = Arch(GB300Backend())
+    pb = stokes2d_inclusions(args.n)
+    da, db, keep = fused_kernel_fields(arch, pb)
+    gd = pb.grid.desc()
+    reps = args.reps + (args.reps & 1)
+
+    def run(k):
+        arch.call("cg_stokes_pt_iterations_pp", ctypes.byref(gd), ctypes.byref(da), ctypes.byref(db), ctypes.byref(pb.params), None, k)
+
+    run(4)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    run(reps)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    byt = FUSED_ARRAYS * args.n * args.n * 4
+    print(json.dumps({"kernel": "fused2d_kernel<float>", "n": args.n, "us_per_launch": ms * 1e3,
+                      "algorithmic_gbs": byt / (ms * 1e-3) / 1e9, "frac_of_measured_hbm": byt / (ms * 1e-3) / 1e9 / measured_peaks()[0]}))
+    arch.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--kernel", choices=["fused2d"], help="time one kernel alone (profiling driver)")
+    ap.add_argument("--reps", type=int, default=200)
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
@@ -460,6 +505,9 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--skip-fp64", action="store_true", help="skip the one-off plain FP64 GPU solve")
     args = ap.parse_args()
+    if args.kernel:
+        run_kernel(args)
+        return
     world = _env_int("WORLD_SIZE", 1)
     rank = _env_int("RANK", 0)
     dist = None

@@ -151,6 +151,10 @@ class cg_sia_params(C.Structure):
     ]
 
 
+class cg_sia_member(C.Structure):
+    _fields_ = [("grid", cg_grid), ("H", cg_field), ("B", cg_field), ("q", cg_field * 2)]
+
+
 P = C.POINTER
 _vp = C.c_void_p
 
@@ -203,6 +207,7 @@ SIGNATURES: dict[str, list] = {
     "cg_ptdiff_run": [_vp, P(cg_grid), P(cg_ptdiff_fields), P(cg_ptdiff_params), P(cg_bc), C.c_int, C.c_int],
     "cg_sia_update_q": [_vp, P(cg_grid), P(cg_field), P(cg_field), P(cg_field), P(cg_sia_params), P(C.c_double)],
     "cg_sia_update_H": [_vp, P(cg_grid), P(cg_field), P(cg_field), P(cg_field), C.c_double, P(cg_sia_params)],
+    "cg_sia_ensemble_run": [_vp, C.c_int, P(cg_sia_member), P(cg_sia_params), C.c_int, P(C.c_double)],
     "cg_sia_run": [_vp, P(cg_grid), P(cg_field), P(cg_field), P(cg_field), P(cg_sia_params), C.c_int, P(C.c_double)],
 }
 _RESTYPES = {"cg_last_error": C.c_char_p}

@@ -81,8 +81,6 @@ Spacing<T> spacing_of(const cg_grid* g) {
     return s;
 }
 
-inline int field_dtype(const cg_field& f) { return f.dtype; }
-
 int check_q(cg_ctx* ctx, const cg_grid* grid, const cg_field* q, int dtype) {
     for (int d = 0; d < grid->ndim; ++d) {
         int rc = cg_check_field(ctx, grid, q[d], dtype, 1 << d, "q");
@@ -120,9 +118,6 @@ int step_t(cg_ctx* ctx, const cg_grid* g, const cg_field* Co, const cg_field* Ci
     CG_CHECK_LAUNCH(ctx);
     return CG_OK;
 }
-
-template <template <class, int> class Fn, class... A>
-int dispatch(int dtype, int nd, A&&... a);
 
 }  // namespace
 

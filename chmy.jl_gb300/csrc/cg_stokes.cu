@@ -358,8 +358,6 @@ int pp_iterations_t(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* a, co
     const Fused2D<T> fab = fused_view<T>(a, b, a), fba = fused_view<T>(b, a, a);
     const SP<T> s = scalars<T>(g, p);
     const bool res = cg_present(a->divV) && cg_present(a->r_V[0]);
-    const dim3 block(32, 8), grid(cg_div_up(g->n[0] + 2, 32), cg_div_up(g->n[1] + 2, 32));
-    const int e0 = g->n[0] + 1, e1 = g->n[1] + 1;
     std::string key = "stokes_pp";
     cg_key_add(key, *g);
     cg_key_add(key, *a);
@@ -372,9 +370,9 @@ int pp_iterations_t(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* a, co
     return cg_graph_run(ctx, key, [&](cudaStream_t st) {
         for (int it = 0; it < niter; ++it) {
             const Fused2D<T>& fk = (it % 2 == 0) ? fab : fba;
-            if (res && it == niter - 1) fused2d_kernel<T, true><<<grid, block, 0, st>>>(fk, s, e0, e1);
-            else fused2d_kernel<T, false><<<grid, block, 0, st>>>(fk, s, e0, e1);
-            CG_CHECK_LAUNCH(ctx);
+            const cudaError_t le = (res && it == niter - 1) ? launch_fused2d<T, true>(fk, s, g->n[0], g->n[1], st)
+                                                            : launch_fused2d<T, false>(fk, s, g->n[0], g->n[1], st);
+            if (le != cudaSuccess) return cg_fail(ctx, CG_ERR_CUDA, "fused2d launch: %s", cudaGetErrorString(le));
             if (bc_V) {
                 int r = cg_bc_apply_impl(ctx, g, 2, (it % 2 == 0) ? b->V : a->V, bc_V);
                 if (r) return r;

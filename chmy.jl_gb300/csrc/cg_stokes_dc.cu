@@ -385,9 +385,9 @@ int cg_stokes_solve_dc(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f,
                 const bool last = it == nchunk - 1;
                 if (nd == 2) {
                     const Fused2D<float>& fk = (it % 2 == 0) ? fa : fb;
-                    if (last) fused2d_kernel<float, true><<<gridF, block, 0, st>>>(fk, s32, e0, e1);
-                    else fused2d_kernel<float, false><<<gridF, block, 0, st>>>(fk, s32, e0, e1);
-                    CG_CHECK_LAUNCH(ctx);
+                    const cudaError_t le = last ? launch_fused2d<float, true>(fk, s32, g->n[0], g->n[1], st)
+                                                : launch_fused2d<float, false>(fk, s32, g->n[0], g->n[1], st);
+                    if (le != cudaSuccess) return cg_fail(ctx, CG_ERR_CUDA, "fused2d launch: %s", cudaGetErrorString(le));
                     int r = cg_bc_apply_impl(ctx, g, nd, (it % 2 == 0) ? w.dV2 : w.dV, bc0);
                     if (r) return r;
                 } else {

@@ -359,179 +359,183 @@ __device__ __forceinline__ T fused_vertex(const SP<T>& s, const T (*sVx)[HX], co
     return t2 + r2 * eve * s.dtau_r;
 }
 
+// Read-only loads: in the fused kernel the `in` buffers are never written (ping-pong), so
+// the non-coherent path is safe and lets loads move ahead of the stores.
+template <class T>
+__device__ __forceinline__ T ldg(const DF<T>& f, int i, int j) {
+    return __ldg(f.ptr(i, j, 0));
+}
+
 template <class T>
 __device__ __forceinline__ CellIn<T> load_cell(const Fused2D<T>& f, int i, int j) {
     CellIn<T> c;
-    c.P = f.P_in(i, j, 0);
-    c.txx = f.txx_in(i, j, 0);
-    c.tyy = f.tyy_in(i, j, 0);
-    c.txo = f.txx_o(i, j, 0);
-    c.tyo = f.tyy_o(i, j, 0);
-    c.fp = f.has_fP ? f.fP(i, j, 0) : T(0);
+    c.P = ldg(f.P_in, i, j);
+    c.txx = ldg(f.txx_in, i, j);
+    c.tyy = ldg(f.tyy_in, i, j);
+    c.txo = ldg(f.txx_o, i, j);
+    c.tyo = ldg(f.tyy_o, i, j);
+    c.fp = f.has_fP ? ldg(f.fP, i, j) : T(0);
     return c;
 }
 
-// Block (32, 8), tile 32 x 32 of launch points; every global load of a thread is issued before
-// the first barrier (own cells, vertices and faces in registers, V and 1/eta staged in shared
-// memory), so that ~50 loads per thread are in flight at once.
-template <class T, bool WRITE_RES>
-__global__ void __launch_bounds__(256, 2) fused2d_kernel(const Fused2D<T> f, const SP<T> s, int e0, int e1) {
-    constexpr int TX = 32, R = 4, TY = 8 * R;
-    constexpr int HX = TX + 2, HY = TY + 2;  // V, 1/eta staged from (i0-1, j0-1)
-    constexpr int CX = TX + 1, CY = TY + 1;  // new cells from (i0-1, j0-1); new vertices from (i0, j0)
-    __shared__ T sVx[HY][HX], sVy[HY][HX], sIe[HY][HX];
-    __shared__ T sTxx[CY][CX], sTyy[CY][CX], sP[CY][CX], sTxy[CY][CX];
-    const int tx = threadIdx.x, ty = threadIdx.y;
-    const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
-    const int i = i0 + tx;
+// Asynchronous global -> shared copy of one element (cp.async, Ampere+). `valid` false
+// zero-fills the destination without reading (src-size 0; src must still be a valid address).
+template <class T>
+__device__ __forceinline__ void cp_async_elem(T* smem, const T* gmem, bool valid) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    if (sizeof(T) == 4)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(s), "l"(gmem), "r"(valid ? 4 : 0) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(s), "l"(gmem), "r"(valid ? 8 : 0) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
-    // ---- loads: own cells / vertices / faces at (i, j0 + ty + 8r) ----
-    CellIn<T> cin[R];
-    T vxy[R], vxo[R], rhx[R], rhy[R];
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-        const int j = j0 + ty + 8 * r;
-        const bool cell_in = i <= e0 && j <= e1;
-        const bool vert_in = i <= e0 + 1 && j <= e1 + 1;
-        if (cell_in) cin[r] = load_cell(f, i, j);
-        vxy[r] = vert_in ? f.txy_in(i, j, 0) : T(0);
-        vxo[r] = cell_in ? f.txy_o(i, j, 0) : T(0);
-        rhx[r] = (cell_in && f.has_rho) ? f.rhox(i, j, 0) : T(0);
-        rhy[r] = (cell_in && f.has_rho) ? f.rhoy(i, j, 0) : T(0);
+// Shared-memory layout of the fused kernel (32 x 32 tile).
+template <class T>
+struct FusedSmem {
+    static constexpr int TX = 32, TY = 32;
+    static constexpr int HX = TX + 2, HY = TY + 2;  // V, 1/eta from (i0-1, j0-1)
+    static constexpr int CX = TX + 1, CY = TY + 1;  // cells from (i0-1, j0-1); vertices from (i0, j0)
+    T Vx[HY][HX], Vy[HY][HX], Ie[HY][HX];
+    T P[CY][CX], Txx[CY][CX], Tyy[CY][CX], Txo[CY][CX], Tyo[CY][CX], Fp[CY][CX];  // cells (in -> new)
+    T Txy[CY][CX], Txyo[CY][CX];                                                  // vertices (in -> new)
+};
+
+// Block (32, 8), tile 32 x 32 of launch points. Phase 0 issues every global read of the block
+// as asynchronous copies into shared memory (V and 1/eta on 34 x 34, cell and vertex inputs
+// on 33 x 33), so all of them are in flight at once; phase 1 computes the new tau/P on the
+// cells and vertices the tile's faces read (own plus a one-point halo) in place; phase 2
+// updates the velocity of the tile's own faces. The `in` buffers are never written (ping-pong).
+template <class T, bool WRITE_RES>
+__global__ void __launch_bounds__(256) fused2d_kernel(const Fused2D<T> f, const SP<T> s, int e0, int e1) {
+    using S = FusedSmem<T>;
+    constexpr int TX = S::TX, TY = S::TY, HX = S::HX, HY = S::HY, CX = S::CX, CY = S::CY;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    S& sm = *reinterpret_cast<S*>(smem_raw);
+    const int tid = threadIdx.y * 32 + threadIdx.x;
+    const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
+
+    // ---- phase 0: asynchronous staging ----
+    for (int t = tid; t < HX * HY; t += 256) {
+        const int a = t % HX, b = t / HX;
+        const int ii = i0 - 1 + a, jj = j0 - 1 + b;
+        const bool ok = ii <= e0 + 1 && jj <= e1 + 1;
+        const int ci = ok ? ii : -1, cj = ok ? jj : -1;  // a valid address when zero-filling
+        cp_async_elem(&sm.Vx[b][a], f.Vx_in.ptr(ci, cj, 0), ok);
+        cp_async_elem(&sm.Vy[b][a], f.Vy_in.ptr(ci, cj, 0), ok);
+        cp_async_elem(&sm.Ie[b][a], f.ieta.ptr(ci, cj, 0), ok);
     }
-    // halo items: warp 0 cell row j0-1 (a = tx, and a = 32 for lane 0); warp 1 cell column i0-1;
-    // warp 2 vertex row j0+32; warp 3 vertex column i0+32 (and the corner for lane 0)
-    CellIn<T> hc[2];
-    T hv[2], hvo[2];
-    int hi_[2], hj_[2], hn = 0;
-    if (ty == 0) {
-        hi_[0] = i0 - 1 + tx;
-        hj_[0] = j0 - 1;
-        hi_[1] = i0 - 1 + 32;
-        hj_[1] = j0 - 1;
-        hn = tx == 0 ? 2 : 1;
-    } else if (ty == 1) {
-        hi_[0] = i0 - 1;
-        hj_[0] = j0 + tx;
-        hn = 1;
-    } else if (ty == 2) {
-        hi_[0] = i0 + tx;
-        hj_[0] = j0 + 32;
-        hn = 1;
-    } else if (ty == 3) {
-        hi_[0] = i0 + 32;
-        hj_[0] = j0 + tx;
-        hi_[1] = i0 + 32;
-        hj_[1] = j0 + 32;
-        hn = tx == 0 ? 2 : 1;
-    }
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        if (h >= hn) break;
-        const int hi = hi_[h], hj = hj_[h];
-        if (ty <= 1) {
-            if (hi <= e0 && hj <= e1) hc[h] = load_cell(f, hi, hj);
-        } else {
-            hv[h] = (hi <= e0 + 1 && hj <= e1 + 1) ? f.txy_in(hi, hj, 0) : T(0);
-            hvo[h] = (hi <= e0 && hj <= e1) ? f.txy_o(hi, hj, 0) : T(0);
-        }
-    }
-    // staged V and 1/eta over logical [i0-1, i0+32] x [j0-1, j0+32], clipped to [-1, n+2]
-#pragma unroll
-    for (int bb = 0; bb < (HY + 7) / 8; ++bb) {
-        const int b = ty + 8 * bb;
-        if (b >= HY) break;
-#pragma unroll
-        for (int aa = 0; aa < 2; ++aa) {
-            const int a = tx + 32 * aa;
-            if (a >= HX) break;
+    for (int t = tid; t < CX * CY; t += 256) {
+        const int a = t % CX, b = t / CX;
+        // cells (i0-1+a, j0-1+b): needed up to the launch range
+        {
             const int ii = i0 - 1 + a, jj = j0 - 1 + b;
-            const bool ok = ii <= e0 + 1 && jj <= e1 + 1;
-            sVx[b][a] = ok ? f.Vx_in(ii, jj, 0) : T(0);
-            sVy[b][a] = ok ? f.Vy_in(ii, jj, 0) : T(0);
-            sIe[b][a] = ok ? f.ieta(ii, jj, 0) : T(0);
+            const bool ok = ii <= e0 && jj <= e1;
+            const int ci = ok ? ii : -1, cj = ok ? jj : -1;
+            cp_async_elem(&sm.P[b][a], f.P_in.ptr(ci, cj, 0), ok);
+            cp_async_elem(&sm.Txx[b][a], f.txx_in.ptr(ci, cj, 0), ok);
+            cp_async_elem(&sm.Tyy[b][a], f.tyy_in.ptr(ci, cj, 0), ok);
+            cp_async_elem(&sm.Txo[b][a], f.txx_o.ptr(ci, cj, 0), ok);
+            cp_async_elem(&sm.Tyo[b][a], f.tyy_o.ptr(ci, cj, 0), ok);
+            if (f.has_fP) cp_async_elem(&sm.Fp[b][a], f.fP.ptr(ci, cj, 0), ok);
+        }
+        // vertices (i0+a, j0+b): the old value is needed up to n+2
+        {
+            const int ii = i0 + a, jj = j0 + b;
+            const bool okv = ii <= e0 + 1 && jj <= e1 + 1;
+            const bool oko = ii <= e0 && jj <= e1;
+            cp_async_elem(&sm.Txy[b][a], f.txy_in.ptr(okv ? ii : 0, okv ? jj : 0, 0), okv);
+            cp_async_elem(&sm.Txyo[b][a], f.txy_o.ptr(oko ? ii : 0, oko ? jj : 0, 0), oko);
         }
     }
+    cp_async_wait_all();
     __syncthreads();
 
-    // ---- phase 1: new tau/P at own cells and vertices, then the halo ones ----
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-        const int j = j0 + ty + 8 * r;
-        const int a = tx + 1, b = ty + 1 + 8 * r;  // cell smem coords
-        if (i <= e0 && j <= e1) {
-            T nxx, nyy, nP, dvP;
-            fused_cell<T, HX>(f, s, sVx, sVy, sIe, a, b, cin[r], nxx, nyy, nP, dvP);
-            sTxx[b][a] = nxx;
-            sTyy[b][a] = nyy;
-            sP[b][a] = nP;
+    const T half = T(0.5);
+    // ---- phase 1a: new tau_xx, tau_yy, P at cells (i0-1+a, j0-1+b) in place ----
+    for (int t = tid; t < CX * CY; t += 256) {
+        const int a = t % CX, b = t / CX;
+        const int i = i0 - 1 + a, j = j0 - 1 + b;
+        if (i > e0 || j > e1 || i < 0 || j < 0) continue;  // beyond: unused; -1: keeps old value
+        const T exx = (sm.Vx[b][a + 1] - sm.Vx[b][a]) * s.idx[0];
+        const T eyy = (sm.Vy[b + 1][a] - sm.Vy[b][a]) * s.idx[1];
+        const T dv = exx + eyy;
+        const T dvP = f.has_fP ? dv + sm.Fp[b][a] : dv;
+        const T ie = sm.Ie[b][a];
+        const T eve = T(1) / (ie + s.inv_Gdt);
+        const T p = sm.P[b][a] - dvP * eve * s.dtau_Pr;
+        const T t0 = sm.Txx[b][a], o0 = sm.Txo[b][a];
+        const T r0 = -(t0 - o0) * s.inv_Gdt - t0 * ie + T(2.0) * (exx - dv * s.third);
+        const T t1 = sm.Tyy[b][a], o1 = sm.Tyo[b][a];
+        const T r1 = -(t1 - o1) * s.inv_Gdt - t1 * ie + T(2.0) * (eyy - dv * s.third);
+        const T nxx = t0 + r0 * eve * s.dtau_r, nyy = t1 + r1 * eve * s.dtau_r;
+        sm.Txx[b][a] = nxx;
+        sm.Tyy[b][a] = nyy;
+        sm.P[b][a] = p;
+        if (a >= 1 && b >= 1) {
             f.txx_out(i, j, 0) = nxx;
             f.tyy_out(i, j, 0) = nyy;
-            f.P_out(i, j, 0) = nP;
+            f.P_out(i, j, 0) = p;
             if (WRITE_RES) f.divV(i, j, 0) = dvP;
         }
-        // own vertex (tx, ty + 8r): in range -> new value; the vertex n+2 -> old value
-        const int va = tx, vb = ty + 8 * r;
-        if (i <= e0 + 1 && j <= e1 + 1) {
-            if (i <= e0 && j <= e1) {
-                const T tn = fused_vertex<T, HX>(s, sVx, sVy, sIe, va, vb, vxy[r], vxo[r]);
-                sTxy[vb][va] = tn;
-                f.txy_out(i, j, 0) = tn;
-            } else {
-                sTxy[vb][va] = vxy[r];
-            }
-        }
     }
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        if (h >= hn) break;
-        const int hi = hi_[h], hj = hj_[h];
-        if (ty <= 1) {
-            const int a = hi - (i0 - 1), b = hj - (j0 - 1);
-            if (hi > e0 || hj > e1) continue;
-            if (hi < 0 || hj < 0) {  // outside the launch range: old values
-                sTxx[b][a] = hc[h].txx;
-                sTyy[b][a] = hc[h].tyy;
-                sP[b][a] = hc[h].P;
-            } else {
-                T nxx, nyy, nP, dvP;
-                fused_cell<T, HX>(f, s, sVx, sVy, sIe, a, b, hc[h], nxx, nyy, nP, dvP);
-                sTxx[b][a] = nxx;
-                sTyy[b][a] = nyy;
-                sP[b][a] = nP;
-            }
-        } else {
-            const int a = hi - i0, b = hj - j0;
-            if (hi > e0 + 1 || hj > e1 + 1) continue;
-            if (hi > e0 || hj > e1) sTxy[b][a] = hv[h];
-            else sTxy[b][a] = fused_vertex<T, HX>(s, sVx, sVy, sIe, a, b, hv[h], hvo[h]);
-        }
+    // ---- phase 1b: new tau_xy at vertices (i0+a, j0+b) in place (smem (a+1, b+1) of V) ----
+    for (int t = tid; t < CX * CY; t += 256) {
+        const int a = t % CX, b = t / CX;
+        const int i = i0 + a, j = j0 + b;
+        if (i > e0 || j > e1) continue;  // beyond: unused; n+2: keeps old value
+        const T exy = half * ((sm.Vx[b + 1][a + 1] - sm.Vx[b][a + 1]) * s.idx[1] +
+                              (sm.Vy[b + 1][a + 1] - sm.Vy[b + 1][a]) * s.idx[0]);
+        const T e00 = sm.Ie[b][a], e10 = sm.Ie[b][a + 1], e01 = sm.Ie[b + 1][a], e11 = sm.Ie[b + 1][a + 1];
+        const T lo = fma(half, e10 - e00, e00);
+        const T hi = fma(half, e11 - e01, e01);
+        const T iev = fma(half, hi - lo, lo);
+        const T eve = T(1) / (iev + s.inv_Gdt);
+        const T t2 = sm.Txy[b][a], o2 = sm.Txyo[b][a];
+        const T r2 = -(t2 - o2) * s.inv_Gdt - t2 * iev + T(2.0) * exy;
+        const T tn = t2 + r2 * eve * s.dtau_r;
+        sm.Txy[b][a] = tn;
+        if (a < TX && b < TY) f.txy_out(i, j, 0) = tn;
     }
     __syncthreads();
 
     // ---- phase 2: velocity of the tile's own faces ----
+    const int a = threadIdx.x;
+    const int i = i0 + a;
 #pragma unroll
-    for (int r = 0; r < R; ++r) {
-        const int a = tx, b = ty + 8 * r;
+    for (int r = 0; r < TY / 8; ++r) {
+        const int b = threadIdx.y + 8 * r;
         const int j = j0 + b;
         if (i > e0 || j > e1) continue;
-        // cells: smem (a+1, b+1) = (i, j); vertices: smem (a, b) = (i, j)
-        T rx = -((sP[b + 1][a + 1] - sP[b + 1][a]) * s.idx[0]) + (sTxx[b + 1][a + 1] - sTxx[b + 1][a]) * s.idx[0];
-        rx = rx + (sTxy[b + 1][a] - sTxy[b][a]) * s.idx[1];
-        T ry = -((sP[b + 1][a + 1] - sP[b][a + 1]) * s.idx[1]) + (sTyy[b + 1][a + 1] - sTyy[b][a + 1]) * s.idx[1];
-        ry = ry + (sTxy[b][a + 1] - sTxy[b][a]) * s.idx[0];
+        T rx = -((sm.P[b + 1][a + 1] - sm.P[b + 1][a]) * s.idx[0]) + (sm.Txx[b + 1][a + 1] - sm.Txx[b + 1][a]) * s.idx[0];
+        rx = rx + (sm.Txy[b + 1][a] - sm.Txy[b][a]) * s.idx[1];
+        T ry = -((sm.P[b + 1][a + 1] - sm.P[b][a + 1]) * s.idx[1]) + (sm.Tyy[b + 1][a + 1] - sm.Tyy[b][a + 1]) * s.idx[1];
+        ry = ry + (sm.Txy[b][a + 1] - sm.Txy[b][a]) * s.idx[0];
         if (f.has_rho) {
-            rx = rx - rhx[r];
-            ry = ry - rhy[r];
+            rx = rx - __ldg(f.rhox.ptr(i, j, 0));
+            ry = ry - __ldg(f.rhoy.ptr(i, j, 0));
         }
         if (WRITE_RES) {
             f.rVx(i, j, 0) = rx;
             f.rVy(i, j, 0) = ry;
         }
-        const T c = sIe[b + 1][a + 1];
-        f.Vx_out(i, j, 0) = sVx[b + 1][a + 1] + rx * (s.nu_dtau * (fmin(sIe[b + 1][a], c) + s.inv_Gdt));
-        f.Vy_out(i, j, 0) = sVy[b + 1][a + 1] + ry * (s.nu_dtau * (fmin(sIe[b][a + 1], c) + s.inv_Gdt));
+        const T c = sm.Ie[b + 1][a + 1];
+        f.Vx_out(i, j, 0) = sm.Vx[b + 1][a + 1] + rx * (s.nu_dtau * (fmin(sm.Ie[b + 1][a], c) + s.inv_Gdt));
+        f.Vy_out(i, j, 0) = sm.Vy[b + 1][a + 1] + ry * (s.nu_dtau * (fmin(sm.Ie[b][a + 1], c) + s.inv_Gdt));
     }
+}
+
+// Launch helper: grid of 32 x 32 tiles over [0, n+1]^2, dynamic shared memory opted in.
+template <class T, bool WRITE_RES>
+inline cudaError_t launch_fused2d(const Fused2D<T>& f, const SP<T>& s, int n0, int n1, cudaStream_t st) {
+    const size_t smem = sizeof(FusedSmem<T>);
+    // opt in to more than 48 KB of dynamic shared memory (host-side, idempotent; each
+    // translation unit holds its own copy of the kernel, so it is set on every call)
+    cudaError_t e = cudaFuncSetAttribute(fused2d_kernel<T, WRITE_RES>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const dim3 block(32, 8), grid(cg_div_up(n0 + 2, 32), cg_div_up(n1 + 2, 32));
+    fused2d_kernel<T, WRITE_RES><<<grid, block, smem, st>>>(f, s, n0 + 1, n1 + 1);
+    return cudaGetLastError();
 }
 
 }  // namespace cgk

@@ -348,6 +348,24 @@ CG_API int cg_sia_update_H(cg_ctx* ctx, const cg_grid* grid, const cg_field* H, 
 CG_API int cg_sia_run(cg_ctx* ctx, const cg_grid* grid, const cg_field* H, const cg_field* B,
                       const cg_field* q, const cg_sia_params* p, int nsteps, double* t_host);
 
+/* One member of an SIA ensemble: its grid (2D), ice thickness H, bed B and flux work array q. */
+typedef struct cg_sia_member {
+    cg_grid  grid;
+    cg_field H;
+    cg_field B;
+    cg_field q[2];
+} cg_sia_member;
+
+/* `nsteps` SIA time steps of `nmembers` independent solves of uneven grid sizes, each with its
+ * own parameters and adaptive Δt (the reference loop of examples/sia.jl:71-81 per member).
+ * Every phase of a step is one launch over the tiles of all members; the q and H boundary
+ * conditions are folded into the kernels (q.x => (x = Dirichlet()), q.y => (y = Dirichlet()),
+ * H => Neumann(), with the reference's corner values; the outer halo is left untouched);
+ * the loop is replayed from one CUDA graph. `t_host` (optional, nmembers entries) receives
+ * each member's simulated time. All members share one dtype. */
+CG_API int cg_sia_ensemble_run(cg_ctx* ctx, int nmembers, const cg_sia_member* members,
+                               const cg_sia_params* params, int nsteps, double* t_host);
+
 #ifdef __cplusplus
 }
 #endif

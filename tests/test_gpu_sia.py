@@ -88,3 +88,42 @@ def test_run_matches_reference_time_loop(arch, T):
     assert abs(t.value - t_ref) <= rtol_for(T) * nsteps * t_ref
     # ice thickness stays non-negative
     assert (Hg.to_numpy() >= 0).all()
+
+
+def test_ensemble_matches_members(arch):
+    """cg_sia_ensemble_run (batched launches over members of uneven sizes, folded bc!) ==
+    cg_sia_run per member, for H over the interior and the ghost layer."""
+    from chmy_gb300.configs import sia_ensemble
+
+    T = np.float64
+    ens = sia_ensemble(members=5, nmin=40, nmax=130, seed=11)
+    nsteps = 30
+    rng = np.random.default_rng(1)
+    singles, batch = [], []
+    for grid, h, p in ens:
+        H0 = NpField(grid, Center(), T)
+        H0.interior()[...] = rng.random(H0.dims) * 0.3  # start with ice so that D > 0
+        B = NpField(grid, Center(), T)
+        B.a[...] = h["B"]
+        q = [NpField(grid, (Vertex(), Center()), T), NpField(grid, (Center(), Vertex()), T)]
+        for store in (singles, batch):
+            store.append((grid, to_gpu(arch, H0), to_gpu(arch, B), [to_gpu(arch, f) for f in q], p))
+    t_single = []
+    for grid, Hg, Bg, qg, p in singles:
+        t = ctypes.c_double()
+        arch.call("cg_sia_run", ctypes.byref(grid.desc()), ctypes.byref(Hg.desc()), ctypes.byref(Bg.desc()), desc_array(qg, 3), ctypes.byref(p), nsteps, ctypes.byref(t))
+        t_single.append(t.value)
+    mem = (_abi.cg_sia_member * len(batch))()
+    params = (_abi.cg_sia_params * len(batch))()
+    for k, (grid, Hg, Bg, qg, p) in enumerate(batch):
+        mem[k].grid = grid.desc()
+        mem[k].H, mem[k].B = Hg.desc(), Bg.desc()
+        mem[k].q[0], mem[k].q[1] = qg[0].desc(), qg[1].desc()
+        params[k] = p
+    ts = (ctypes.c_double * len(batch))()
+    arch.call("cg_sia_ensemble_run", len(batch), mem, params, nsteps, ts)
+    arch.synchronize()
+    for k, ((grid, Ha, _, _, _), (_, Hb, _, _, _)) in enumerate(zip(singles, batch)):
+        a, b = Ha.to_numpy()[1:-1, 1:-1], Hb.to_numpy()[1:-1, 1:-1]
+        assert np.max(np.abs(a - b)) <= 1e-12 * nsteps * max(np.abs(a).max(), 1e-30), k
+        assert abs(ts[k] - t_single[k]) <= 1e-12 * nsteps * t_single[k]
