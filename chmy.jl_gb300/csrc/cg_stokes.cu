@@ -370,8 +370,10 @@ int pp_iterations_t(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* a, co
     return cg_graph_run(ctx, key, [&](cudaStream_t st) {
         for (int it = 0; it < niter; ++it) {
             const Fused2D<T>& fk = (it % 2 == 0) ? fab : fba;
-            const cudaError_t le = (res && it == niter - 1) ? launch_fused2d<T, true>(fk, s, g->n[0], g->n[1], st)
-                                                            : launch_fused2d<T, false>(fk, s, g->n[0], g->n[1], st);
+            const int nsm = ctx->num_sms;
+            const cudaError_t le = (res && it == niter - 1)
+                                       ? launch_march2d<T, true>(fk, s, g->n[0], g->n[1], nsm, 0, st)
+                                       : launch_march2d<T, false>(fk, s, g->n[0], g->n[1], nsm, 0, st);
             if (le != cudaSuccess) return cg_fail(ctx, CG_ERR_CUDA, "fused2d launch: %s", cudaGetErrorString(le));
             if (bc_V) {
                 int r = cg_bc_apply_impl(ctx, g, 2, (it % 2 == 0) ? b->V : a->V, bc_V);

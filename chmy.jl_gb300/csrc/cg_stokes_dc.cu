@@ -156,8 +156,9 @@ struct Work {
     cg_field dV2[3], dP2, dtau2[6];  // ping-pong partners of the fused 2D kernel
 };
 
-// FP32 dense field like `f` (same extents, locations, halo 1).
-cg_field like32(const cg_field& f, char*& cursor, size_t& bytes, bool dry) {
+// FP32 field like `f` (same extents, locations, halo 1) with x rows of `pitch` elements. All
+// work arrays share one pitch, so the fused 2D kernel addresses every array with one row offset.
+cg_field like32(const cg_field& f, long pitch, char*& cursor, size_t& bytes, bool dry) {
     cg_field g;
     std::memset(&g, 0, sizeof(g));
     g.dtype = CG_F32;
@@ -169,6 +170,7 @@ cg_field like32(const cg_field& f, char*& cursor, size_t& bytes, bool dry) {
         g.halo[d] = d < f.ndim ? 1 : 0;
         if (d < f.ndim) ext[d] = f.n[d] + 4;
     }
+    if (f.ndim > 1) ext[0] = pitch;
     g.stride[0] = 1;
     g.stride[1] = f.ndim > 1 ? ext[0] : 0;
     g.stride[2] = f.ndim > 2 ? ext[0] * ext[1] : 0;
@@ -181,25 +183,27 @@ cg_field like32(const cg_field& f, char*& cursor, size_t& bytes, bool dry) {
 
 int make_work(cg_ctx* ctx, const cg_stokes_fields* f, int nd, Work* w) {
     const int nt = nd == 2 ? 3 : 6;
+    // the widest x extent (V.x is Vertex in x), rounded up to 32 elements (128 bytes)
+    const long pitch = ((long)f->V[0].n[0] + 4 + 31) / 32 * 32;
     for (int pass = 0; pass < 2; ++pass) {
         const bool dry = pass == 0;
         char* cur = dry ? nullptr : static_cast<char*>(ctx->dc_pool);
         size_t bytes = 0;
         for (int d = 0; d < nd; ++d) {
-            w->dV[d] = like32(f->V[d], cur, bytes, dry);
-            w->dV2[d] = like32(f->V[d], cur, bytes, dry);
-            w->rho[d] = like32(f->V[d], cur, bytes, dry);
-            w->rV[d] = like32(f->V[d], cur, bytes, dry);
+            w->dV[d] = like32(f->V[d], pitch, cur, bytes, dry);
+            w->dV2[d] = like32(f->V[d], pitch, cur, bytes, dry);
+            w->rho[d] = like32(f->V[d], pitch, cur, bytes, dry);
+            w->rV[d] = like32(f->V[d], pitch, cur, bytes, dry);
         }
-        w->dP = like32(f->P, cur, bytes, dry);
-        w->dP2 = like32(f->P, cur, bytes, dry);
-        w->fP = like32(f->P, cur, bytes, dry);
-        w->ieta = like32(f->P, cur, bytes, dry);
-        w->divV = like32(f->P, cur, bytes, dry);
+        w->dP = like32(f->P, pitch, cur, bytes, dry);
+        w->dP2 = like32(f->P, pitch, cur, bytes, dry);
+        w->fP = like32(f->P, pitch, cur, bytes, dry);
+        w->ieta = like32(f->P, pitch, cur, bytes, dry);
+        w->divV = like32(f->P, pitch, cur, bytes, dry);
         for (int c = 0; c < nt; ++c) {
-            w->dtau[c] = like32(f->tau[c], cur, bytes, dry);
-            w->dtau2[c] = like32(f->tau[c], cur, bytes, dry);
-            w->told[c] = like32(f->tau[c], cur, bytes, dry);
+            w->dtau[c] = like32(f->tau[c], pitch, cur, bytes, dry);
+            w->dtau2[c] = like32(f->tau[c], pitch, cur, bytes, dry);
+            w->told[c] = like32(f->tau[c], pitch, cur, bytes, dry);
         }
         if (dry && bytes > ctx->dc_pool_bytes) {
             if (ctx->dc_pool) {
@@ -216,10 +220,11 @@ int make_work(cg_ctx* ctx, const cg_stokes_fields* f, int nd, Work* w) {
     return CG_OK;
 }
 
+// Elements spanned by a work array (halo 1, rows of stride[1] elements).
 size_t padded_count(const cg_field& f) {
-    size_t c = 1;
-    for (int d = 0; d < f.ndim; ++d) c *= (size_t)(f.n[d] + 4);
-    return c;
+    if (f.ndim == 1) return (size_t)f.n[0] + 4;
+    if (f.ndim == 2) return (size_t)f.stride[1] * (f.n[1] + 4);
+    return (size_t)f.stride[2] * (f.n[2] + 4);
 }
 
 __global__ void reciprocal_kernel(float* dst, const double* src, long dst_s1, long dst_s2, long src_s1, long src_s2,
@@ -375,8 +380,6 @@ int cg_stokes_solve_dc(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f,
         fa.txy_out = fb.txy_in = cg_view<float>(w.dtau2[2]);
         fa.P_out = fb.P_in = cg_view<float>(w.dP2);
     }
-    constexpr int kFR = 4;  // rows per thread: 32 x 32 tiles
-    const dim3 gridF(cg_div_up(g->n[0] + 2, 32), cg_div_up(g->n[1] + 2, 8 * kFR));
     const int nchunk = nd == 2 ? ncheck + (ncheck & 1) : ncheck;
     cg_key_add(key, nchunk);
     auto chunk = [&]() {
@@ -385,8 +388,9 @@ int cg_stokes_solve_dc(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f,
                 const bool last = it == nchunk - 1;
                 if (nd == 2) {
                     const Fused2D<float>& fk = (it % 2 == 0) ? fa : fb;
-                    const cudaError_t le = last ? launch_fused2d<float, true>(fk, s32, g->n[0], g->n[1], st)
-                                                : launch_fused2d<float, false>(fk, s32, g->n[0], g->n[1], st);
+                    const int nsm = ctx->num_sms;
+                    const cudaError_t le = last ? launch_march2d<float, true>(fk, s32, g->n[0], g->n[1], nsm, 0, st)
+                                                : launch_march2d<float, false>(fk, s32, g->n[0], g->n[1], nsm, 0, st);
                     if (le != cudaSuccess) return cg_fail(ctx, CG_ERR_CUDA, "fused2d launch: %s", cudaGetErrorString(le));
                     int r = cg_bc_apply_impl(ctx, g, nd, (it % 2 == 0) ? w.dV2 : w.dV, bc0);
                     if (r) return r;

@@ -305,12 +305,9 @@ __global__ void thermal_kernel(const SV<T> v, const SP<T> s, int e0, int e1) {
 
 // ---- fused 2D PT iteration (variable viscosity): update_stress! + update_velocity! -----------
 //
-// One launch per PT iteration. A block owns a 32 x TY tile of launch points I; it stages V and
-// 1/eta with a halo in shared memory, recomputes the new tau/P on the one-cell halo it needs
-// (bitwise the same values the owning block computes), then updates the velocity of its own
-// faces. Reads come from the `in` buffers and writes go to the `out` buffers (ping-pong), so the
-// redundant halo recomputation never sees a neighbour's new values. Points outside Chmy's
-// launch range [0, n+1] keep their old values, exactly as in the two-kernel form.
+// One launch per PT iteration, reading the `in` buffers and writing the `out` buffers
+// (ping-pong). Points outside Chmy's launch range [0, n+1] keep their old values, exactly as in
+// the two-kernel form.
 template <class T>
 struct Fused2D {
     DF<T> Vx_in, Vy_in, Vx_out, Vy_out;
@@ -319,223 +316,311 @@ struct Fused2D {
     int has_fP, has_rho;
 };
 
-// Cell update of the fused kernel: new tau_xx, tau_yy, P at cell (i, j) whose smem coordinates
-// in the staged V / 1/eta tile are (a, b) (the staged tile starts at (i0-1, j0-1)).
-template <class T>
-struct CellIn {
-    T P, txx, tyy, txo, tyo, fp;
+// ---- warp-marching fused 2D PT iteration --------------------------------------------------
+//
+// update_stress! followed by update_velocity! in one launch, without shared memory. It writes
+// the new P, tau_xx, tau_yy, tau_xy and V on [0, n+1]^2 (and divV, r_V when asked); points
+// outside that range keep the values the out buffers hold. A warp owns 30
+// launch columns i = c0 .. c0+29 and a segment of rows js .. je. Lane l holds column
+// c0 - 1 + l, so lanes 0 and 31 are one-column halos. Each lane reads every input of its
+// column once per row; x-neighbours come from shuffles. The warp then marches up the rows,
+// keeping in registers the previous row's velocity, 1/eta and the new P, tau_yy and tau_xy.
+// Iteration j computes the new cell row j and vertex row j+1, then the velocity of row j.
+// The segment's prologue computes cell row js-1 and vertex row js.
+//
+// Shuffle validity: a cell at lane l needs Vx of lane l+1, so lane 31's cell is invalid; a
+// vertex at lane l needs Vy and 1/eta of lane l-1, so lane 0's vertex is invalid. The owned
+// lanes 1..30 read cells of lanes l-1, l and vertices of lanes l, l+1, all valid.
+// Ix is the element-offset type: int where every offset fits in 32 bits, else long.
+template <class T, class Ix, bool UNI>
+struct MAt {  // column i of a lane; UNI: every array has the row stride s1u
+    int i;
+    Ix s1u;
+    __device__ __forceinline__ Ix off(const DF<T>& f, int j) const { return (Ix)i + (Ix)j * (UNI ? s1u : (Ix)f.s1); }
+    __device__ __forceinline__ T ld(const DF<T>& f, int j, bool ok) const { return ok ? __ldg(f.p + off(f, j)) : T(0); }
+    __device__ __forceinline__ void st(const DF<T>& f, int j, T v) const { f.p[off(f, j)] = v; }
 };
 
-template <class T, int HX>
-__device__ __forceinline__ void fused_cell(const Fused2D<T>& f, const SP<T>& s, const T (*sVx)[HX],
-                                           const T (*sVy)[HX], const T (*sIe)[HX], int a, int b, const CellIn<T>& c,
-                                           T& nxx, T& nyy, T& nP, T& dvP_out) {
-    const T exx = (sVx[b][a + 1] - sVx[b][a]) * s.idx[0];
-    const T eyy = (sVy[b + 1][a] - sVy[b][a]) * s.idx[1];
-    const T dv = exx + eyy;
-    const T dvP = f.has_fP ? dv + c.fp : dv;
-    const T ie = sIe[b][a];
-    const T eve = T(1) / (ie + s.inv_Gdt);
-    nP = c.P - dvP * eve * s.dtau_Pr;
-    const T r0 = -(c.txx - c.txo) * s.inv_Gdt - c.txx * ie + T(2.0) * (exx - dv * s.third);
-    const T r1 = -(c.tyy - c.tyo) * s.inv_Gdt - c.tyy * ie + T(2.0) * (eyy - dv * s.third);
-    nxx = c.txx + r0 * eve * s.dtau_r;
-    nyy = c.tyy + r1 * eve * s.dtau_r;
-    dvP_out = dvP;
-}
-
-// Vertex update: new tau_xy at vertex (i, j) = staged smem coordinates (a+1, b+1).
-template <class T, int HX>
-__device__ __forceinline__ T fused_vertex(const SP<T>& s, const T (*sVx)[HX], const T (*sVy)[HX],
-                                          const T (*sIe)[HX], int a, int b, T t2, T o2) {
-    const T half = T(0.5);
-    const T exy = half * ((sVx[b + 1][a + 1] - sVx[b][a + 1]) * s.idx[1] + (sVy[b + 1][a + 1] - sVy[b + 1][a]) * s.idx[0]);
-    const T e00 = sIe[b][a], e10 = sIe[b][a + 1], e01 = sIe[b + 1][a], e11 = sIe[b + 1][a + 1];
-    const T lo = fma(half, e10 - e00, e00);
-    const T hi = fma(half, e11 - e01, e01);
-    const T iev = fma(half, hi - lo, lo);
-    const T eve = T(1) / (iev + s.inv_Gdt);
-    const T r2 = -(t2 - o2) * s.inv_Gdt - t2 * iev + T(2.0) * exy;
-    return t2 + r2 * eve * s.dtau_r;
-}
-
-// Read-only loads: in the fused kernel the `in` buffers are never written (ping-pong), so
-// the non-coherent path is safe and lets loads move ahead of the stores.
+// Inputs of one marching step at column i: row j+1 of the vertex-row inputs, row j of the
+// cell-row inputs.
 template <class T>
-__device__ __forceinline__ T ldg(const DF<T>& f, int i, int j) {
-    return __ldg(f.ptr(i, j, 0));
+struct MarchRow {
+    T Vx, Vy, ie, txy, txyo;                   // row j+1
+    T P, txx, tyy, txo, tyo, fp, rhox, rhoy;  // row j
+};
+
+template <class T, class Ix, bool UNI>
+__device__ __forceinline__ MarchRow<T> march_load(const Fused2D<T>& f, const MAt<T, Ix, UNI>& at, int j, int e1,
+                                                  bool inV, bool inC) {
+    MarchRow<T> r;
+    const int jn = j + 1;
+    const bool vn = inV && jn <= e1 + 1;
+    r.Vx = at.ld(f.Vx_in, jn, vn);
+    r.Vy = at.ld(f.Vy_in, jn, vn);
+    r.ie = at.ld(f.ieta, jn, vn);
+    r.txy = at.ld(f.txy_in, jn, vn);
+    r.txyo = at.ld(f.txy_o, jn, inC && jn <= e1);
+    const bool c = inC && j <= e1;
+    r.P = at.ld(f.P_in, j, c);
+    r.txx = at.ld(f.txx_in, j, c);
+    r.tyy = at.ld(f.tyy_in, j, c);
+    r.txo = at.ld(f.txx_o, j, c);
+    r.tyo = at.ld(f.tyy_o, j, c);
+    r.fp = f.has_fP ? at.ld(f.fP, j, c) : T(0);
+    r.rhox = f.has_rho ? at.ld(f.rhox, j, c) : T(0);
+    r.rhoy = f.has_rho ? at.ld(f.rhoy, j, c) : T(0);
+    return r;
+}
+
+// Arithmetic with explicit round-to-nearest and no contraction into FMA: every operation
+// rounds once, in the order the CPU oracle (built with -ffp-contract=off) evaluates it, so the
+// marching kernel matches it bitwise and a value recomputed at a segment edge rounds exactly
+// like the owner's copy.
+__device__ __forceinline__ float radd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double radd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float rsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double rsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float rmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double rmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float rdiv(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ double rdiv(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ float rfma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double rfma(double a, double b, double c) { return __fma_rn(a, b, c); }
+
+// -(t - t_old) * inv_Gdt - t * ieta + 2 * e: the VE stress residual, left to right.
+template <class T>
+__device__ __forceinline__ T stress_res(const SP<T>& s, T t, T to, T ie, T e) {
+    return radd(rsub(rmul(-rsub(t, to), s.inv_Gdt), rmul(t, ie)), rmul(T(2.0), e));
 }
 
 template <class T>
-__device__ __forceinline__ CellIn<T> load_cell(const Fused2D<T>& f, int i, int j) {
-    CellIn<T> c;
-    c.P = ldg(f.P_in, i, j);
-    c.txx = ldg(f.txx_in, i, j);
-    c.tyy = ldg(f.tyy_in, i, j);
-    c.txo = ldg(f.txx_o, i, j);
-    c.tyo = ldg(f.tyy_o, i, j);
-    c.fp = f.has_fP ? ldg(f.fP, i, j) : T(0);
+struct CellNew {
+    T P, txx, tyy, dvP;
+};
+
+// New P, tau_xx, tau_yy at cell (i, j) from Vx(i, j), Vx(i+1, j), Vy(i, j), Vy(i, j+1) and the
+// cell's inputs (update_stress!, variable-viscosity form).
+template <class T>
+__device__ __forceinline__ CellNew<T> march_cell(const SP<T>& s, bool has_fP, T vx, T vxR, T vy, T vyU, T ie, T P,
+                                                 T txx, T txo, T tyy, T tyo, T fp) {
+    const T exx = rmul(rsub(vxR, vx), s.idx[0]);
+    const T eyy = rmul(rsub(vyU, vy), s.idx[1]);
+    const T dv = radd(exx, eyy);
+    const T dvt = rmul(dv, s.third);
+    const T eve = rdiv(T(1), radd(ie, s.inv_Gdt));
+    CellNew<T> c;
+    c.dvP = has_fP ? radd(dv, fp) : dv;
+    c.P = rsub(P, rmul(rmul(c.dvP, eve), s.dtau_Pr));
+    c.txx = radd(txx, rmul(rmul(stress_res(s, txx, txo, ie, rsub(exx, dvt)), eve), s.dtau_r));
+    c.tyy = radd(tyy, rmul(rmul(stress_res(s, tyy, tyo, ie, rsub(eyy, dvt)), eve), s.dtau_r));
     return c;
 }
 
-// Asynchronous global -> shared copy of one element (cp.async, Ampere+). `valid` false
-// zero-fills the destination without reading (src-size 0; src must still be a valid address).
+// New tau_xy at vertex (i, jv) from Vx(i, jv-1), Vx(i, jv), Vy(i-1, jv), Vy(i, jv) and the four
+// cells' 1/eta around it (e00 = (i-1, jv-1), e10 = (i, jv-1), e01 = (i-1, jv), e11 = (i, jv)),
+// interpolated with the Linear rule, x innermost.
 template <class T>
-__device__ __forceinline__ void cp_async_elem(T* smem, const T* gmem, bool valid) {
-    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    if (sizeof(T) == 4)
-        asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(s), "l"(gmem), "r"(valid ? 4 : 0) : "memory");
-    else
-        asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(s), "l"(gmem), "r"(valid ? 8 : 0) : "memory");
-}
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
-
-// Shared-memory layout of the fused kernel (32 x 32 tile).
-template <class T>
-struct FusedSmem {
-    static constexpr int TX = 32, TY = 32;
-    static constexpr int HX = TX + 2, HY = TY + 2;  // V, 1/eta from (i0-1, j0-1)
-    static constexpr int CX = TX + 1, CY = TY + 1;  // cells from (i0-1, j0-1); vertices from (i0, j0)
-    T Vx[HY][HX], Vy[HY][HX], Ie[HY][HX];
-    T P[CY][CX], Txx[CY][CX], Tyy[CY][CX], Txo[CY][CX], Tyo[CY][CX], Fp[CY][CX];  // cells (in -> new)
-    T Txy[CY][CX], Txyo[CY][CX];                                                  // vertices (in -> new)
-};
-
-// Block (32, 8), tile 32 x 32 of launch points. Phase 0 issues every global read of the block
-// as asynchronous copies into shared memory (V and 1/eta on 34 x 34, cell and vertex inputs
-// on 33 x 33), so all of them are in flight at once; phase 1 computes the new tau/P on the
-// cells and vertices the tile's faces read (own plus a one-point halo) in place; phase 2
-// updates the velocity of the tile's own faces. The `in` buffers are never written (ping-pong).
-template <class T, bool WRITE_RES>
-__global__ void __launch_bounds__(256) fused2d_kernel(const Fused2D<T> f, const SP<T> s, int e0, int e1) {
-    using S = FusedSmem<T>;
-    constexpr int TX = S::TX, TY = S::TY, HX = S::HX, HY = S::HY, CX = S::CX, CY = S::CY;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    S& sm = *reinterpret_cast<S*>(smem_raw);
-    const int tid = threadIdx.y * 32 + threadIdx.x;
-    const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
-
-    // ---- phase 0: asynchronous staging ----
-    for (int t = tid; t < HX * HY; t += 256) {
-        const int a = t % HX, b = t / HX;
-        const int ii = i0 - 1 + a, jj = j0 - 1 + b;
-        const bool ok = ii <= e0 + 1 && jj <= e1 + 1;
-        const int ci = ok ? ii : -1, cj = ok ? jj : -1;  // a valid address when zero-filling
-        cp_async_elem(&sm.Vx[b][a], f.Vx_in.ptr(ci, cj, 0), ok);
-        cp_async_elem(&sm.Vy[b][a], f.Vy_in.ptr(ci, cj, 0), ok);
-        cp_async_elem(&sm.Ie[b][a], f.ieta.ptr(ci, cj, 0), ok);
-    }
-    for (int t = tid; t < CX * CY; t += 256) {
-        const int a = t % CX, b = t / CX;
-        // cells (i0-1+a, j0-1+b): needed up to the launch range
-        {
-            const int ii = i0 - 1 + a, jj = j0 - 1 + b;
-            const bool ok = ii <= e0 && jj <= e1;
-            const int ci = ok ? ii : -1, cj = ok ? jj : -1;
-            cp_async_elem(&sm.P[b][a], f.P_in.ptr(ci, cj, 0), ok);
-            cp_async_elem(&sm.Txx[b][a], f.txx_in.ptr(ci, cj, 0), ok);
-            cp_async_elem(&sm.Tyy[b][a], f.tyy_in.ptr(ci, cj, 0), ok);
-            cp_async_elem(&sm.Txo[b][a], f.txx_o.ptr(ci, cj, 0), ok);
-            cp_async_elem(&sm.Tyo[b][a], f.tyy_o.ptr(ci, cj, 0), ok);
-            if (f.has_fP) cp_async_elem(&sm.Fp[b][a], f.fP.ptr(ci, cj, 0), ok);
-        }
-        // vertices (i0+a, j0+b): the old value is needed up to n+2
-        {
-            const int ii = i0 + a, jj = j0 + b;
-            const bool okv = ii <= e0 + 1 && jj <= e1 + 1;
-            const bool oko = ii <= e0 && jj <= e1;
-            cp_async_elem(&sm.Txy[b][a], f.txy_in.ptr(okv ? ii : 0, okv ? jj : 0, 0), okv);
-            cp_async_elem(&sm.Txyo[b][a], f.txy_o.ptr(oko ? ii : 0, oko ? jj : 0, 0), oko);
-        }
-    }
-    cp_async_wait_all();
-    __syncthreads();
-
+__device__ __forceinline__ T march_vertex(const SP<T>& s, T vx0, T vx1, T vyl, T vy, T e00, T e10, T e01, T e11,
+                                          T t2, T o2) {
     const T half = T(0.5);
-    // ---- phase 1a: new tau_xx, tau_yy, P at cells (i0-1+a, j0-1+b) in place ----
-    for (int t = tid; t < CX * CY; t += 256) {
-        const int a = t % CX, b = t / CX;
-        const int i = i0 - 1 + a, j = j0 - 1 + b;
-        if (i > e0 || j > e1 || i < 0 || j < 0) continue;  // beyond: unused; -1: keeps old value
-        const T exx = (sm.Vx[b][a + 1] - sm.Vx[b][a]) * s.idx[0];
-        const T eyy = (sm.Vy[b + 1][a] - sm.Vy[b][a]) * s.idx[1];
-        const T dv = exx + eyy;
-        const T dvP = f.has_fP ? dv + sm.Fp[b][a] : dv;
-        const T ie = sm.Ie[b][a];
-        const T eve = T(1) / (ie + s.inv_Gdt);
-        const T p = sm.P[b][a] - dvP * eve * s.dtau_Pr;
-        const T t0 = sm.Txx[b][a], o0 = sm.Txo[b][a];
-        const T r0 = -(t0 - o0) * s.inv_Gdt - t0 * ie + T(2.0) * (exx - dv * s.third);
-        const T t1 = sm.Tyy[b][a], o1 = sm.Tyo[b][a];
-        const T r1 = -(t1 - o1) * s.inv_Gdt - t1 * ie + T(2.0) * (eyy - dv * s.third);
-        const T nxx = t0 + r0 * eve * s.dtau_r, nyy = t1 + r1 * eve * s.dtau_r;
-        sm.Txx[b][a] = nxx;
-        sm.Tyy[b][a] = nyy;
-        sm.P[b][a] = p;
-        if (a >= 1 && b >= 1) {
-            f.txx_out(i, j, 0) = nxx;
-            f.tyy_out(i, j, 0) = nyy;
-            f.P_out(i, j, 0) = p;
-            if (WRITE_RES) f.divV(i, j, 0) = dvP;
-        }
-    }
-    // ---- phase 1b: new tau_xy at vertices (i0+a, j0+b) in place (smem (a+1, b+1) of V) ----
-    for (int t = tid; t < CX * CY; t += 256) {
-        const int a = t % CX, b = t / CX;
-        const int i = i0 + a, j = j0 + b;
-        if (i > e0 || j > e1) continue;  // beyond: unused; n+2: keeps old value
-        const T exy = half * ((sm.Vx[b + 1][a + 1] - sm.Vx[b][a + 1]) * s.idx[1] +
-                              (sm.Vy[b + 1][a + 1] - sm.Vy[b + 1][a]) * s.idx[0]);
-        const T e00 = sm.Ie[b][a], e10 = sm.Ie[b][a + 1], e01 = sm.Ie[b + 1][a], e11 = sm.Ie[b + 1][a + 1];
-        const T lo = fma(half, e10 - e00, e00);
-        const T hi = fma(half, e11 - e01, e01);
-        const T iev = fma(half, hi - lo, lo);
-        const T eve = T(1) / (iev + s.inv_Gdt);
-        const T t2 = sm.Txy[b][a], o2 = sm.Txyo[b][a];
-        const T r2 = -(t2 - o2) * s.inv_Gdt - t2 * iev + T(2.0) * exy;
-        const T tn = t2 + r2 * eve * s.dtau_r;
-        sm.Txy[b][a] = tn;
-        if (a < TX && b < TY) f.txy_out(i, j, 0) = tn;
-    }
-    __syncthreads();
+    const T exy = rmul(half, radd(rmul(rsub(vx1, vx0), s.idx[1]), rmul(rsub(vy, vyl), s.idx[0])));
+    const T lo = rfma(half, rsub(e10, e00), e00);
+    const T hi = rfma(half, rsub(e11, e01), e01);
+    const T iev = rfma(half, rsub(hi, lo), lo);
+    const T eve = rdiv(T(1), radd(iev, s.inv_Gdt));
+    return radd(t2, rmul(rmul(stress_res(s, t2, o2, iev, exy), eve), s.dtau_r));
+}
 
-    // ---- phase 2: velocity of the tile's own faces ----
-    const int a = threadIdx.x;
-    const int i = i0 + a;
-#pragma unroll
-    for (int r = 0; r < TY / 8; ++r) {
-        const int b = threadIdx.y + 8 * r;
-        const int j = j0 + b;
-        if (i > e0 || j > e1) continue;
-        T rx = -((sm.P[b + 1][a + 1] - sm.P[b + 1][a]) * s.idx[0]) + (sm.Txx[b + 1][a + 1] - sm.Txx[b + 1][a]) * s.idx[0];
-        rx = rx + (sm.Txy[b + 1][a] - sm.Txy[b][a]) * s.idx[1];
-        T ry = -((sm.P[b + 1][a + 1] - sm.P[b][a + 1]) * s.idx[1]) + (sm.Tyy[b + 1][a + 1] - sm.Tyy[b][a + 1]) * s.idx[1];
-        ry = ry + (sm.Txy[b][a + 1] - sm.Txy[b][a]) * s.idx[0];
-        if (f.has_rho) {
-            rx = rx - __ldg(f.rhox.ptr(i, j, 0));
-            ry = ry - __ldg(f.rhoy.ptr(i, j, 0));
+template <class T, class Ix, bool UNI, bool WRITE_RES, int MINB = 1>
+__global__ void __launch_bounds__(128, MINB) march2d_kernel(const Fused2D<T> f, const SP<T> s, int e0, int e1,
+                                                            int nstrip, int nwarps, int seg_rows, long s1u) {
+    constexpr unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int gw = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    if (gw >= nwarps) return;  // whole warp
+    const int strip = gw % nstrip;
+    const int js = (gw / nstrip) * seg_rows;
+    if (js > e1) return;  // whole warp
+    const int je = min(js + seg_rows - 1, e1);
+    const int i = strip * 30 - 1 + lane;
+    const MAt<T, Ix, UNI> at{i, (Ix)s1u};
+    const bool own = lane >= 1 && lane <= 30 && i <= e0;
+    const bool inV = i <= e0 + 1;  // V, 1/eta, tau_xy readable
+    const bool inC = i <= e0;      // cell inputs, tau_xy_old readable
+    const bool oldcell = i < 0;    // column -1 keeps its old cell values
+
+    // ---- prologue: new cell row js-1 (P and tau_yy only) and new vertex row js ----
+    T Vx_c, Vy_c, ie_c, ieL_c, ie_p, Pn_p, Tyyn_p, txy_c;
+    {
+        const int jp = js - 1;  // >= -1
+        const T vxp = at.ld(f.Vx_in, jp, inV);
+        const T vyp = at.ld(f.Vy_in, jp, inV);
+        const T iep = at.ld(f.ieta, jp, inV);
+        const T pp = at.ld(f.P_in, jp, inC);
+        const T typ = at.ld(f.tyy_in, jp, inC);
+        const T tyop = at.ld(f.tyy_o, jp, inC);
+        const T fpp = f.has_fP ? at.ld(f.fP, jp, inC) : T(0);
+        Vx_c = at.ld(f.Vx_in, js, inV);
+        Vy_c = at.ld(f.Vy_in, js, inV);
+        ie_c = at.ld(f.ieta, js, inV);
+        const T t2 = at.ld(f.txy_in, js, inV);
+        const T o2 = at.ld(f.txy_o, js, inC);
+        // cell (i, js-1); row -1 and column -1 keep their old values
+        const T vxpR = __shfl_down_sync(FULL, vxp, 1);
+        const CellNew<T> cp = march_cell(s, f.has_fP != 0, vxp, vxpR, vyp, Vy_c, iep, pp, T(0), T(0), typ, tyop, fpp);
+        const bool keep = jp < 0 || oldcell;
+        Pn_p = keep ? pp : cp.P;
+        Tyyn_p = keep ? typ : cp.tyy;
+        // vertex (i, js)
+        const T vyL = __shfl_up_sync(FULL, Vy_c, 1);
+        const T iepL = __shfl_up_sync(FULL, iep, 1);
+        ieL_c = __shfl_up_sync(FULL, ie_c, 1);
+        txy_c = (i > e0) ? t2 : march_vertex(s, vxp, Vx_c, vyL, Vy_c, iepL, iep, ieL_c, ie_c, t2, o2);
+        if (own) at.st(f.txy_out, js, txy_c);
+        ie_p = iep;
+    }
+
+    // the next row's loads are issued before the current row is computed
+    MarchRow<T> cur = march_load(f, at, js, e1, inV, inC);
+    for (int j = js; j <= je; ++j) {
+        MarchRow<T> nxt;
+        if (j < je) nxt = march_load(f, at, j + 1, e1, inV, inC);
+        // new cell (i, j)
+        const T vxR = __shfl_down_sync(FULL, Vx_c, 1);
+        CellNew<T> c = march_cell(s, f.has_fP != 0, Vx_c, vxR, Vy_c, cur.Vy, ie_c, cur.P, cur.txx, cur.txo, cur.tyy,
+                                  cur.tyo, cur.fp);
+        if (oldcell) {
+            c.P = cur.P;
+            c.txx = cur.txx;
+            c.tyy = cur.tyy;
         }
-        if (WRITE_RES) {
-            f.rVx(i, j, 0) = rx;
-            f.rVy(i, j, 0) = ry;
+        // new vertex (i, j+1)
+        const T vyL = __shfl_up_sync(FULL, cur.Vy, 1);
+        const T ieL_n = __shfl_up_sync(FULL, cur.ie, 1);
+        const T tn = (i > e0 || j + 1 > e1)
+                         ? cur.txy
+                         : march_vertex(s, Vx_c, cur.Vx, vyL, cur.Vy, ieL_c, ie_c, ieL_n, cur.ie, cur.txy, cur.txyo);
+        // velocity (i, j): r_V = -d(P) + d(tau_dd) + d(tau_xy) - rho g, left to right
+        const T PL = __shfl_up_sync(FULL, c.P, 1);
+        const T TxxL = __shfl_up_sync(FULL, c.txx, 1);
+        const T txyR = __shfl_down_sync(FULL, txy_c, 1);
+        if (own) {
+            T rx = radd(-rmul(rsub(c.P, PL), s.idx[0]), rmul(rsub(c.txx, TxxL), s.idx[0]));
+            rx = radd(rx, rmul(rsub(tn, txy_c), s.idx[1]));
+            T ry = radd(-rmul(rsub(c.P, Pn_p), s.idx[1]), rmul(rsub(c.tyy, Tyyn_p), s.idx[1]));
+            ry = radd(ry, rmul(rsub(txyR, txy_c), s.idx[0]));
+            if (f.has_rho) {
+                rx = rsub(rx, cur.rhox);
+                ry = rsub(ry, cur.rhoy);
+            }
+            at.st(f.P_out, j, c.P);
+            at.st(f.txx_out, j, c.txx);
+            at.st(f.tyy_out, j, c.tyy);
+            if (j + 1 <= je) at.st(f.txy_out, j + 1, tn);
+            if (WRITE_RES) {
+                at.st(f.divV, j, c.dvP);
+                at.st(f.rVx, j, rx);
+                at.st(f.rVy, j, ry);
+            }
+            at.st(f.Vx_out, j, radd(Vx_c, rmul(rx, rmul(s.nu_dtau, radd(fmin(ieL_c, ie_c), s.inv_Gdt)))));
+            at.st(f.Vy_out, j, radd(Vy_c, rmul(ry, rmul(s.nu_dtau, radd(fmin(ie_p, ie_c), s.inv_Gdt)))));
         }
-        const T c = sm.Ie[b + 1][a + 1];
-        f.Vx_out(i, j, 0) = sm.Vx[b + 1][a + 1] + rx * (s.nu_dtau * (fmin(sm.Ie[b + 1][a], c) + s.inv_Gdt));
-        f.Vy_out(i, j, 0) = sm.Vy[b + 1][a + 1] + ry * (s.nu_dtau * (fmin(sm.Ie[b][a + 1], c) + s.inv_Gdt));
+        // advance one row
+        Vx_c = cur.Vx;
+        Vy_c = cur.Vy;
+        ie_p = ie_c;
+        ie_c = cur.ie;
+        ieL_c = ieL_n;
+        Pn_p = c.P;
+        Tyyn_p = c.tyy;
+        txy_c = tn;
+        cur = nxt;
     }
 }
 
-// Launch helper: grid of 32 x 32 tiles over [0, n+1]^2, dynamic shared memory opted in.
-template <class T, bool WRITE_RES>
-inline cudaError_t launch_fused2d(const Fused2D<T>& f, const SP<T>& s, int n0, int n1, cudaStream_t st) {
-    const size_t smem = sizeof(FusedSmem<T>);
-    // opt in to more than 48 KB of dynamic shared memory (host-side, idempotent; each
-    // translation unit holds its own copy of the kernel, so it is set on every call)
-    cudaError_t e = cudaFuncSetAttribute(fused2d_kernel<T, WRITE_RES>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    const dim3 block(32, 8), grid(cg_div_up(n0 + 2, 32), cg_div_up(n1 + 2, 32));
-    fused2d_kernel<T, WRITE_RES><<<grid, block, smem, st>>>(f, s, n0 + 1, n1 + 1);
+// The arrays of a fused view, for host-side checks.
+template <class T>
+inline void fused_arrays(const Fused2D<T>& f, const DF<T>* out[22]) {
+    const DF<T>* all[22] = {&f.Vx_in, &f.Vy_in, &f.Vx_out, &f.Vy_out, &f.txx_in, &f.tyy_in, &f.txy_in, &f.txx_out,
+                            &f.tyy_out, &f.txy_out, &f.P_in, &f.P_out, &f.txx_o, &f.tyy_o, &f.txy_o, &f.ieta,
+                            &f.fP, &f.rhox, &f.rhoy, &f.divV, &f.rVx, &f.rVy};
+    for (int k = 0; k < 22; ++k) out[k] = all[k];
+}
+
+// True when every element offset i + j*s1 the marching kernel forms (i, j in [-1, e+1]) fits
+// in a 32-bit int for all of f's arrays.
+template <class T>
+inline bool march_fits_int(const Fused2D<T>& f, int e0, int e1) {
+    const DF<T>* all[22];
+    fused_arrays(f, all);
+    const long lim = 2147483647L;
+    for (const DF<T>* d : all) {
+        const long s1 = d->s1 < 0 ? -d->s1 : d->s1;
+        if ((long)e0 + 1 + ((long)e1 + 1) * s1 > lim) return false;
+    }
+    return true;
+}
+
+// The row stride shared by every present array of f, or 0 when they differ.
+template <class T>
+inline long march_uniform_stride(const Fused2D<T>& f) {
+    const DF<T>* all[22];
+    fused_arrays(f, all);
+    long s1 = 0;
+    for (const DF<T>* d : all) {
+        if (!d->p) continue;
+        if (s1 == 0) s1 = d->s1;
+        else if (d->s1 != s1) return 0;
+    }
+    return s1;
+}
+
+// Rows per warp of the marching kernel: the length at which the strips x segments warps fill
+// every SM once at the kernel's occupancy (one wave), kept within [8, 32] rows. Shorter
+// segments re-read more boundary rows; longer ones leave the memory system fewer warps'
+// worth of loads in flight (measured on 1024^2 to 4096^2 grids).
+template <class T, class Ix, bool UNI, bool WRITE_RES, int MINB = 1>
+inline int march_seg_rows(int num_sms, int nstrip, int rows) {
+    static const int blocks_per_sm = [] {
+        int nb = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march2d_kernel<T, Ix, UNI, WRITE_RES, MINB>, 128,
+                                                          0) != cudaSuccess)
+            nb = 0;
+        return nb > 0 ? nb : 4;
+    }();
+    const long capacity = (long)num_sms * blocks_per_sm * 4;
+    const long nseg = capacity / nstrip > 1 ? capacity / nstrip : 1;
+    const int seg = (int)((rows + nseg - 1) / nseg);
+    return seg < 8 ? 8 : (seg > 32 ? 32 : seg);
+}
+
+template <class T, class Ix, bool UNI, bool WRITE_RES, int MINB = 1>
+inline cudaError_t launch_march2d_ix(const Fused2D<T>& f, const SP<T>& s, int n0, int n1, int num_sms, int seg_rows,
+                                     long s1u, cudaStream_t st) {
+    const int e0 = n0 + 1, e1 = n1 + 1;
+    const int nstrip = cg_div_up(e0 + 1, 30);
+    if (seg_rows <= 0) seg_rows = march_seg_rows<T, Ix, UNI, WRITE_RES, MINB>(num_sms, nstrip, e1 + 1);
+    const int nseg = cg_div_up(e1 + 1, seg_rows);
+    const int nwarps = nstrip * nseg;
+    march2d_kernel<T, Ix, UNI, WRITE_RES, MINB>
+        <<<cg_div_up(nwarps, 4), 128, 0, st>>>(f, s, e0, e1, nstrip, nwarps, seg_rows, s1u);
     return cudaGetLastError();
+}
+
+// Launch of the warp-marching kernel over [0, n0+1] x [0, n1+1]; seg_rows <= 0 picks the
+// segment length from the occupancy.
+template <class T, bool WRITE_RES>
+inline cudaError_t launch_march2d(const Fused2D<T>& f, const SP<T>& s, int n0, int n1, int num_sms, int seg_rows,
+                                  cudaStream_t st) {
+    const long s1u = march_uniform_stride(f);
+    // FP32 with one shared stride fits in 64 registers without spills: 8 blocks (32 warps) per SM
+    constexpr int minb = sizeof(T) == 4 ? 8 : 1;
+    if (march_fits_int(f, n0 + 1, n1 + 1)) {
+        if (s1u) return launch_march2d_ix<T, int, true, WRITE_RES, minb>(f, s, n0, n1, num_sms, seg_rows, s1u, st);
+        return launch_march2d_ix<T, int, false, WRITE_RES>(f, s, n0, n1, num_sms, seg_rows, 0, st);
+    }
+    if (s1u) return launch_march2d_ix<T, long, true, WRITE_RES>(f, s, n0, n1, num_sms, seg_rows, s1u, st);
+    return launch_march2d_ix<T, long, false, WRITE_RES>(f, s, n0, n1, num_sms, seg_rows, 0, st);
 }
 
 }  // namespace cgk
