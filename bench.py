@@ -43,6 +43,9 @@ import numpy as np  # noqa: E402
 A32 = 19  # arrays per FP32 PT iteration of the defect-correction solve
 A64 = 16  # arrays per FP64 PT iteration (reference form, variable viscosity, no body force)
 FUSED_ARRAYS = 18  # the timed fused kernel: no continuity forcing (public ping-pong entry)
+# 3D: read/write V x3, tau x6, P; read tau_old x6, 1/eta, rho_g.z (the reference's T_eff set
+# for 3D VE Stokes without the thermal arrays)
+FUSED3_ARRAYS = 28
 
 
 def _env_int(name, default):
@@ -460,17 +463,53 @@ def fused_kernel_fields(arch, pb):
     return stokes_fields(V=A["V"], P=A["P"], tau=A["tau"], **extra), stokes_fields(V=B["V"], P=B["P"], tau=B["tau"]), keep
 
 
+def fused3d_kernel_fields(arch, pb):
+    """FP32 ping-pong field sets of the fused 3D PT kernel on the problem's grid (1/eta from eta,
+    rho_g from the problem, zero V/tau/P/tau_old). Every array shares its row and plane strides,
+    as in the solver's work pool."""
+    import torch
+
+    from chmy_gb300 import Field
+    from chmy_gb300.grids import Center, Vertex
+    from chmy_gb300.kernels import stokes_fields
+
+    g = pb.grid
+    Cl, Vl = Center(), Vertex()
+    rows = g.dims[1] + 5
+
+    def f32(loc):
+        return Field(arch, g, loc, np.float32, pitch_align=128, plane_rows=rows)
+
+    vl = [(Vl, Cl, Cl), (Cl, Vl, Cl), (Cl, Cl, Vl)]
+    tl = [(Cl, Cl, Cl)] * 3 + [(Vl, Vl, Cl), (Vl, Cl, Vl), (Cl, Vl, Vl)]
+    A = dict(V=[f32(l) for l in vl], P=f32(Cl), tau=[f32(l) for l in tl])
+    B = dict(V=[f32(l) for l in vl], P=f32(Cl), tau=[f32(l) for l in tl])
+    # buoyancy on the vertical component only, as in examples/stokes_3d_inc_ve_T.jl
+    extra = dict(tau_old=[f32(l) for l in tl], inv_eta=f32(Cl), rho_g=[None, None, f32(vl[2])])
+    extra["inv_eta"].data.copy_(torch.from_numpy(1.0 / pb.host["eta"]).float())
+    extra["rho_g"][2].data.copy_(torch.from_numpy(pb.host["rho_g"][2]).float())
+    keep = (A, B, extra)
+    return stokes_fields(V=A["V"], P=A["P"], tau=A["tau"], **extra), stokes_fields(V=B["V"], P=B["P"], tau=B["tau"]), keep
+
+
 def run_kernel(args):
-    """--kernel fused2d: only the fused FP32 PT kernel, `--reps` launches timed with CUDA events
-    (the command the committed ncu summaries were captured with)."""
+    """--kernel fused2d | fused3d: only the fused FP32 PT kernel (2D inclusions n^2, or 3D random
+    viscosity n^3), `--reps` launches timed with CUDA events (the command the committed ncu
+    summaries were captured with)."""
     import torch
 
     from chmy_gb300 import Arch, GB300Backend
-    from chmy_gb300.configs import stokes2d_inclusions
+    from chmy_gb300.configs import stokes2d_inclusions, stokes3d_grf
 
     arch = Arch(GB300Backend())
-    pb = stokes2d_inclusions(args.n)
-    da, db, keep = fused_kernel_fields(arch, pb)
+    if args.kernel == "fused3d":
+        pb = stokes3d_grf(args.n, dtype=np.float32)
+        da, db, keep = fused3d_kernel_fields(arch, pb)
+        name, arrays, cells = "march3d_kernel<float>", FUSED3_ARRAYS, args.n**3
+    else:
+        pb = stokes2d_inclusions(args.n)
+        da, db, keep = fused_kernel_fields(arch, pb)
+        name, arrays, cells = "march2d_kernel<float>", FUSED_ARRAYS, args.n**2
     gd = pb.grid.desc()
     reps = args.reps + (args.reps & 1)
 
@@ -485,15 +524,15 @@ def run_kernel(args):
     e1.record()
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / reps
-    byt = FUSED_ARRAYS * args.n * args.n * 4
-    print(json.dumps({"kernel": "march2d_kernel<float>", "n": args.n, "us_per_launch": ms * 1e3,
+    byt = arrays * cells * 4
+    print(json.dumps({"kernel": name, "n": args.n, "arrays": arrays, "us_per_launch": ms * 1e3,
                       "algorithmic_gbs": byt / (ms * 1e-3) / 1e9, "frac_of_measured_hbm": byt / (ms * 1e-3) / 1e9 / measured_peaks()[0]}))
     arch.close()
 
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--kernel", choices=["fused2d"], help="time one kernel alone (profiling driver)")
+    ap.add_argument("--kernel", choices=["fused2d", "fused3d"], help="time one kernel alone (profiling driver)")
     ap.add_argument("--reps", type=int, default=200)
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)

@@ -33,9 +33,12 @@ class Field:
     """Field(arch, grid, loc, type=eltype(grid); halo=1) (src/Fields/field.jl:56-62).
 
     `pitch_align` (bytes, 0 = dense Chmy layout) pads x rows so that logical x index 0 of each
-    row is aligned, which lets kernels issue aligned vector loads."""
+    row is aligned, which lets kernels issue aligned vector loads. `plane_rows` (3D, with
+    `pitch_align`) pads every z plane to that many rows. Fields of different locations then
+    share their row and plane strides, and the fused kernels address them all with one
+    offset."""
 
-    def __init__(self, arch, grid: UniformGrid, loc, dtype=None, halo=1, pitch_align: int = 0):
+    def __init__(self, arch, grid: UniformGrid, loc, dtype=None, halo=1, pitch_align: int = 0, plane_rows: int = 0):
         self.arch = arch
         self.grid = grid
         nd = grid.ndim
@@ -53,9 +56,14 @@ class Field:
             a = pitch_align // esz
             front = (a - (2 * self.halo[0] - 1) % a) % a
             pitch = ((front + self.ext[0] + a - 1) // a) * a
-            storage = torch.zeros(tuple(reversed(self.ext[1:])) + (pitch,), dtype=tdt, device=dev)
+            outer = list(reversed(self.ext[1:]))
+            if nd == 3 and plane_rows:
+                if plane_rows < self.ext[1]:
+                    raise ValueError(f"plane_rows {plane_rows} < {self.ext[1]} rows of this field")
+                outer[-1] = plane_rows
+            storage = torch.zeros(tuple(outer) + (pitch,), dtype=tdt, device=dev)
             self._storage = storage
-            self.data = storage[..., front : front + self.ext[0]]
+            self.data = storage[..., : self.ext[1], front : front + self.ext[0]] if nd == 3 else storage[..., front : front + self.ext[0]]
         else:
             self._storage = None
             self.data = torch.zeros(tuple(reversed(self.ext)), dtype=tdt, device=dev)

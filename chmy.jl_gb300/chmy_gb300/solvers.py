@@ -55,8 +55,9 @@ class StokesSolver:
                 f.from_numpy(val)
                 self.fields[name] = f
         if precompute_inv_eta and "eta" in self.fields:
+            # 1/eta is an input of the kernels: prepared on the host, uploaded like eta
             inv = Field(arch, g, Center(), self.fields["eta"].dtype, pitch_align=pitch_align)
-            inv.data.copy_(1.0 / self.fields["eta"].data)
+            inv.from_numpy(1.0 / np.asarray(problem.host["eta"]))
             self.fields["inv_eta"] = inv
         self.desc = stokes_fields(**self.fields)
         self.grid_desc = g.desc()

@@ -8,6 +8,7 @@ int cg_maxabs_collect(cg_ctx* ctx, int nfields, const cg_field* fields, double* 
 int cg_stokes_solve_dc(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f, const cg_stokes_params* p,
                        const cg_bc* bc_V, const cg_solve_opts* o, cg_solve_result* res);
 
+#include "cg_march3d.cuh"
 #include "cg_stokes_kernels.cuh"
 
 namespace {
@@ -353,8 +354,64 @@ Fused2D<T> fused_view(const cg_stokes_fields* in, const cg_stokes_fields* out, c
 }
 
 template <class T>
+Fused3D<T> fused3_view(const cg_stokes_fields* in, const cg_stokes_fields* out, const cg_stokes_fields* a) {
+    Fused3D<T> f;
+    std::memset(&f, 0, sizeof(f));
+    for (int d = 0; d < 3; ++d) {
+        f.V_in[d] = cg_view<T>(in->V[d]);
+        f.V_out[d] = cg_view<T>(out->V[d]);
+        f.has_rho[d] = cg_present(a->rho_g[d]);
+        if (f.has_rho[d]) f.rho[d] = cg_view<T>(a->rho_g[d]);
+        if (cg_present(a->r_V[d])) f.rV[d] = cg_view<T>(a->r_V[d]);
+    }
+    for (int c = 0; c < 6; ++c) {
+        f.tau_in[c] = cg_view<T>(in->tau[c]);
+        f.tau_out[c] = cg_view<T>(out->tau[c]);
+        f.tau_o[c] = cg_view<T>(a->tau_old[c]);
+    }
+    f.P_in = cg_view<T>(in->P);
+    f.P_out = cg_view<T>(out->P);
+    f.ieta = cg_view<T>(a->inv_eta);
+    if (cg_present(a->divV)) f.divV = cg_view<T>(a->divV);
+    return f;
+}
+
+template <class T>
+int pp_iterations_3d(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* a, const cg_stokes_fields* b,
+                     const cg_stokes_params* p, const cg_bc* bc_V, int niter) {
+    const Fused3D<T> fab = fused3_view<T>(a, b, a), fba = fused3_view<T>(b, a, a);
+    const SP<T> s = scalars<T>(g, p);
+    const bool res = cg_present(a->divV) && cg_present(a->r_V[0]);
+    std::string key = "stokes_pp3";
+    cg_key_add(key, *g);
+    cg_key_add(key, *a);
+    cg_key_add(key, *b);
+    cg_key_add(key, *p);
+    cg_key_add(key, niter);
+    cg_bc none[3];
+    std::memset(none, 0, sizeof(none));
+    for (int d = 0; d < 3; ++d) cg_key_add(key, bc_V ? bc_V[d] : none[d]);
+    return cg_graph_run(ctx, key, [&](cudaStream_t st) {
+        for (int it = 0; it < niter; ++it) {
+            const Fused3D<T>& fk = (it % 2 == 0) ? fab : fba;
+            const int nsm = ctx->num_sms;
+            const cudaError_t le = (res && it == niter - 1)
+                                       ? launch_march3d<T, true>(fk, s, g->n[0], g->n[1], g->n[2], nsm, 0, st)
+                                       : launch_march3d<T, false>(fk, s, g->n[0], g->n[1], g->n[2], nsm, 0, st);
+            if (le != cudaSuccess) return cg_fail(ctx, CG_ERR_CUDA, "fused3d launch: %s", cudaGetErrorString(le));
+            if (bc_V) {
+                int r = cg_bc_apply_impl(ctx, g, 3, (it % 2 == 0) ? b->V : a->V, bc_V);
+                if (r) return r;
+            }
+        }
+        return (int)CG_OK;
+    });
+}
+
+template <class T>
 int pp_iterations_t(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* a, const cg_stokes_fields* b,
                     const cg_stokes_params* p, const cg_bc* bc_V, int niter) {
+    if (g->ndim == 3) return pp_iterations_3d<T>(ctx, g, a, b, p, bc_V, niter);
     const Fused2D<T> fab = fused_view<T>(a, b, a), fba = fused_view<T>(b, a, a);
     const SP<T> s = scalars<T>(g, p);
     const bool res = cg_present(a->divV) && cg_present(a->r_V[0]);
@@ -393,7 +450,7 @@ extern "C" int cg_stokes_pt_iterations_pp(cg_ctx* ctx, const cg_grid* grid, cons
     int rc = check_stokes(ctx, grid, a, NEED_V | NEED_TAU | NEED_TAU_OLD | NEED_P, &dtype);
     if (rc) return rc;
     if (!b || !p) return cg_fail(ctx, CG_ERR_ARG, "pt_iterations_pp: NULL argument");
-    if (grid->ndim != 2) return cg_fail(ctx, CG_ERR_UNSUPPORTED, "pt_iterations_pp: 2D grids only");
+    if (grid->ndim < 2) return cg_fail(ctx, CG_ERR_UNSUPPORTED, "pt_iterations_pp: 2D and 3D grids only");
     if (!cg_present(a->inv_eta)) return cg_fail(ctx, CG_ERR_ARG, "pt_iterations_pp: inv_eta is required");
     if (niter < 0 || (niter & 1)) return cg_fail(ctx, CG_ERR_ARG, "pt_iterations_pp: niter must be even and >= 0");
     int dtb;

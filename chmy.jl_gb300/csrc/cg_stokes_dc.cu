@@ -11,6 +11,7 @@
 // homogeneous boundary conditions (same kinds, zero values), graph-replayed, until the
 // FP32 measures fall below max(0.5 eps, inner_rtol * outer measure) or stagnate.
 // Update (FP64): V += dV, P += dP, tau += dtau, then bc!(V).
+#include "cg_march3d.cuh"
 #include "cg_stokes_kernels.cuh"
 
 int cg_bc_apply_impl(cg_ctx* ctx, const cg_grid* grid, int nfields, const cg_field* fields, const cg_bc* bcs);
@@ -156,9 +157,10 @@ struct Work {
     cg_field dV2[3], dP2, dtau2[6];  // ping-pong partners of the fused 2D kernel
 };
 
-// FP32 field like `f` (same extents, locations, halo 1) with x rows of `pitch` elements. All
-// work arrays share one pitch, so the fused 2D kernel addresses every array with one row offset.
-cg_field like32(const cg_field& f, long pitch, char*& cursor, size_t& bytes, bool dry) {
+// FP32 field like `f` (same extents, locations, halo 1) with x rows of `pitch` elements and, in
+// 3D, planes of `rows` rows. All work arrays share the row and plane strides, so the fused
+// kernels address every array with one offset.
+cg_field like32(const cg_field& f, long pitch, long rows, char*& cursor, size_t& bytes, bool dry) {
     cg_field g;
     std::memset(&g, 0, sizeof(g));
     g.dtype = CG_F32;
@@ -171,6 +173,7 @@ cg_field like32(const cg_field& f, long pitch, char*& cursor, size_t& bytes, boo
         if (d < f.ndim) ext[d] = f.n[d] + 4;
     }
     if (f.ndim > 1) ext[0] = pitch;
+    if (f.ndim > 2) ext[1] = rows;
     g.stride[0] = 1;
     g.stride[1] = f.ndim > 1 ? ext[0] : 0;
     g.stride[2] = f.ndim > 2 ? ext[0] * ext[1] : 0;
@@ -185,25 +188,27 @@ int make_work(cg_ctx* ctx, const cg_stokes_fields* f, int nd, Work* w) {
     const int nt = nd == 2 ? 3 : 6;
     // the widest x extent (V.x is Vertex in x), rounded up to 32 elements (128 bytes)
     const long pitch = ((long)f->V[0].n[0] + 4 + 31) / 32 * 32;
+    // the widest y extent (V.y is Vertex in y): rows per plane in 3D
+    const long rows = (long)f->V[1].n[1] + 4;
     for (int pass = 0; pass < 2; ++pass) {
         const bool dry = pass == 0;
         char* cur = dry ? nullptr : static_cast<char*>(ctx->dc_pool);
         size_t bytes = 0;
         for (int d = 0; d < nd; ++d) {
-            w->dV[d] = like32(f->V[d], pitch, cur, bytes, dry);
-            w->dV2[d] = like32(f->V[d], pitch, cur, bytes, dry);
-            w->rho[d] = like32(f->V[d], pitch, cur, bytes, dry);
-            w->rV[d] = like32(f->V[d], pitch, cur, bytes, dry);
+            w->dV[d] = like32(f->V[d], pitch, rows, cur, bytes, dry);
+            w->dV2[d] = like32(f->V[d], pitch, rows, cur, bytes, dry);
+            w->rho[d] = like32(f->V[d], pitch, rows, cur, bytes, dry);
+            w->rV[d] = like32(f->V[d], pitch, rows, cur, bytes, dry);
         }
-        w->dP = like32(f->P, pitch, cur, bytes, dry);
-        w->dP2 = like32(f->P, pitch, cur, bytes, dry);
-        w->fP = like32(f->P, pitch, cur, bytes, dry);
-        w->ieta = like32(f->P, pitch, cur, bytes, dry);
-        w->divV = like32(f->P, pitch, cur, bytes, dry);
+        w->dP = like32(f->P, pitch, rows, cur, bytes, dry);
+        w->dP2 = like32(f->P, pitch, rows, cur, bytes, dry);
+        w->fP = like32(f->P, pitch, rows, cur, bytes, dry);
+        w->ieta = like32(f->P, pitch, rows, cur, bytes, dry);
+        w->divV = like32(f->P, pitch, rows, cur, bytes, dry);
         for (int c = 0; c < nt; ++c) {
-            w->dtau[c] = like32(f->tau[c], pitch, cur, bytes, dry);
-            w->dtau2[c] = like32(f->tau[c], pitch, cur, bytes, dry);
-            w->told[c] = like32(f->tau[c], pitch, cur, bytes, dry);
+            w->dtau[c] = like32(f->tau[c], pitch, rows, cur, bytes, dry);
+            w->dtau2[c] = like32(f->tau[c], pitch, rows, cur, bytes, dry);
+            w->told[c] = like32(f->tau[c], pitch, rows, cur, bytes, dry);
         }
         if (dry && bytes > ctx->dc_pool_bytes) {
             if (ctx->dc_pool) {
@@ -225,6 +230,70 @@ size_t padded_count(const cg_field& f) {
     if (f.ndim == 1) return (size_t)f.n[0] + 4;
     if (f.ndim == 2) return (size_t)f.stride[1] * (f.n[1] + 4);
     return (size_t)f.stride[2] * (f.n[2] + 4);
+}
+
+// max |r_tau| of the FP32 correction over the interior of every stress component: the inner
+// loop's constitutive measure, the FP32 counterpart of the outer err_tau. Without it, a state
+// whose momentum and continuity residuals vanish (a uniform stress correction) would end the
+// inner loop at its first check. The maximum is kept as the bits of |r| (a NaN's bits exceed
+// every finite value's, so a non-finite residual is reported).
+template <int ND>
+__global__ void tau_res_kernel(const SV<float> v, const SP<float> s, int e0, int e1, int n0, int n1, int n2,
+                               unsigned long long* slot) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = ND > 2 ? blockIdx.z : 0;
+    unsigned m = 0;
+    if (i <= e0 && j <= e1) {
+        // interior test per location: index <= n - 1 (Center) or n (Vertex) along each dim
+        auto in = [&](int li, int lj, int lk) {
+            return i <= n0 - 1 + li && j <= n1 - 1 + lj && (ND < 3 || k <= n2 - 1 + lk);
+        };
+        auto take = [&](float r) { m = max(m, __float_as_uint(fabsf(r))); };
+        const float exx = (v.V[0](i + 1, j, k) - v.V[0](i, j, k)) * s.idx[0];
+        const float eyy = (v.V[1](i, j + 1, k) - v.V[1](i, j, k)) * s.idx[1];
+        float ezz = 0.f, dv = exx + eyy;
+        if (ND > 2) {
+            ezz = (v.V[2](i, j, k + 1) - v.V[2](i, j, k)) * s.idx[2];
+            dv = dv + ezz;
+        }
+        const float ie = v.ieta(i, j, k);
+        auto diag = [&](int c, float e) {
+            const float t = v.tau[c](i, j, k);
+            take(-(t - v.tau_old[c](i, j, k)) * s.inv_Gdt - t * ie + 2.f * (e - dv * s.third));
+        };
+        auto shear = [&](int c, float e, int a, int b) {
+            const float t = v.tau[c](i, j, k);
+            const float iev = shear_inv_eta(v, i, j, k, a, b);
+            take(-(t - v.tau_old[c](i, j, k)) * s.inv_Gdt - t * iev + 2.f * e);
+        };
+        const float exy = 0.5f * ((v.V[0](i, j, k) - v.V[0](i, j - 1, k)) * s.idx[1] +
+                                  (v.V[1](i, j, k) - v.V[1](i - 1, j, k)) * s.idx[0]);
+        if (in(0, 0, 0)) {
+            diag(0, exx);
+            diag(1, eyy);
+            if (ND > 2) diag(2, ezz);
+        }
+        if (ND == 2) {
+            if (in(1, 1, 0)) shear(2, exy, 0, 1);
+        } else {
+            const float exz = 0.5f * ((v.V[0](i, j, k) - v.V[0](i, j, k - 1)) * s.idx[2] +
+                                      (v.V[2](i, j, k) - v.V[2](i - 1, j, k)) * s.idx[0]);
+            const float eyz = 0.5f * ((v.V[1](i, j, k) - v.V[1](i, j, k - 1)) * s.idx[2] +
+                                      (v.V[2](i, j, k) - v.V[2](i, j - 1, k)) * s.idx[1]);
+            if (in(1, 1, 0)) shear(3, exy, 0, 1);
+            if (in(1, 0, 1)) shear(4, exz, 0, 2);
+            if (in(0, 1, 1)) shear(5, eyz, 1, 2);
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0 && m) atomicMax(slot, (unsigned long long)m);
+}
+
+__global__ void fill_kernel(float* dst, float v, size_t count) {
+    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < count; q += (size_t)gridDim.x * blockDim.x)
+        dst[q] = v;
 }
 
 __global__ void reciprocal_kernel(float* dst, const double* src, long dst_s1, long dst_s2, long src_s1, long src_s2,
@@ -270,6 +339,11 @@ int cg_stokes_solve_dc(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f,
             return cg_fail(ctx, CG_ERR_UNSUPPORTED, "stokes_solve (FP32): pass eta (inv_eta alone is not enough)");
         }
         CG_CHECK_LAUNCH(ctx);
+    } else {
+        // scalar viscosity: the fused kernels take 1/eta per cell, here a constant
+        fill_kernel<<<ctx->num_sms * 4, 256, 0, ctx->stream>>>(static_cast<float*>(w.ieta.data),
+                                                               (float)(1.0 / p->eta), padded_count(w.ieta));
+        CG_CHECK_LAUNCH(ctx);
     }
 
     // FP64 views of the state and FP32 views of the correction
@@ -296,10 +370,8 @@ int cg_stokes_solve_dc(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f,
         f32.tau[c] = w.dtau[c];
         f32.tau_old[c] = w.told[c];
     }
-    if (var) f32.inv_eta = w.ieta;
-    SV<float> v32 = views<float>(&f32, nd);
-    v32.fP = cg_view<float>(w.fP);
-    v32.has_fP = 1;
+    f32.inv_eta = w.ieta;
+    const SV<float> v32 = views<float>(&f32, nd);
     const SP<float> s32 = scalars<float>(g, p);
 
     cg_bc bc0[3];
@@ -310,14 +382,15 @@ int cg_stokes_solve_dc(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f,
     // FP64 measures: divV, r_V (the reference's) and the constitutive residuals, read from the
     // FP32 forcing tau_old' = G dt R_tau (the initial guess of a PT solve can have zero divV and
     // r_V while tau is far from its constitutive value)
-    cg_field red64[4 + 6], red32[4];
+    cg_field red64[4 + 6], red32[5];
     red64[0] = f->divV;
     red32[0] = w.divV;
     for (int d = 0; d < nd; ++d) {
         red64[1 + d] = f->r_V[d];
-    for (int c = 0; c < nt; ++c) red64[1 + nd + c] = w.told[c];
         red32[1 + d] = w.rV[d];
     }
+    for (int c = 0; c < nt; ++c) red64[1 + nd + c] = w.told[c];
+    red32[nd + 1] = w.told[0];  // FP32 slot of the constitutive measure (only its dtype is read)
     cg_bc rbc[3];
     std::memset(rbc, 0, sizeof(rbc));
     for (int d = 0; d < nd; ++d) rbc[d].kind[d][0] = rbc[d].kind[d][1] = CG_BC_DIRICHLET;
@@ -380,7 +453,33 @@ int cg_stokes_solve_dc(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f,
         fa.txy_out = fb.txy_in = cg_view<float>(w.dtau2[2]);
         fa.P_out = fb.P_in = cg_view<float>(w.dP2);
     }
-    const int nchunk = nd == 2 ? ncheck + (ncheck & 1) : ncheck;
+    // 3D: the z-marching fused kernel, ping-pong the same way
+    Fused3D<float> ga, gb;
+    std::memset(&ga, 0, sizeof(ga));
+    if (nd == 3) {
+        for (int c = 0; c < 6; ++c) ga.tau_o[c] = cg_view<float>(w.told[c]);
+        ga.ieta = cg_view<float>(w.ieta);
+        ga.fP = cg_view<float>(w.fP);
+        ga.has_fP = 1;
+        for (int d = 0; d < 3; ++d) {
+            ga.rho[d] = cg_view<float>(w.rho[d]);
+            ga.has_rho[d] = 1;
+            ga.rV[d] = cg_view<float>(w.rV[d]);
+        }
+        ga.divV = cg_view<float>(w.divV);
+        gb = ga;
+        for (int d = 0; d < 3; ++d) {
+            ga.V_in[d] = gb.V_out[d] = cg_view<float>(w.dV[d]);
+            ga.V_out[d] = gb.V_in[d] = cg_view<float>(w.dV2[d]);
+        }
+        for (int c = 0; c < 6; ++c) {
+            ga.tau_in[c] = gb.tau_out[c] = cg_view<float>(w.dtau[c]);
+            ga.tau_out[c] = gb.tau_in[c] = cg_view<float>(w.dtau2[c]);
+        }
+        ga.P_in = gb.P_out = cg_view<float>(w.dP);
+        ga.P_out = gb.P_in = cg_view<float>(w.dP2);
+    }
+    const int nchunk = ncheck + (ncheck & 1);
     cg_key_add(key, nchunk);
     auto chunk = [&]() {
         return cg_graph_run(ctx, key, [&](cudaStream_t st) {
@@ -395,12 +494,13 @@ int cg_stokes_solve_dc(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f,
                     int r = cg_bc_apply_impl(ctx, g, nd, (it % 2 == 0) ? w.dV2 : w.dV, bc0);
                     if (r) return r;
                 } else {
-                    if (last) stress_kernel<float, 3, true><<<grid3, block, 0, st>>>(v32, s32, e0, e1);
-                    else stress_kernel<float, 3, false><<<grid3, block, 0, st>>>(v32, s32, e0, e1);
-                    if (last) velocity_kernel<float, 3, true><<<grid3, block, 0, st>>>(v32, s32, e0, e1);
-                    else velocity_kernel<float, 3, false><<<grid3, block, 0, st>>>(v32, s32, e0, e1);
-                    CG_CHECK_LAUNCH(ctx);
-                    int r = cg_bc_apply_impl(ctx, g, nd, f32.V, bc0);
+                    const Fused3D<float>& fk = (it % 2 == 0) ? ga : gb;
+                    const int nsm = ctx->num_sms;
+                    const cudaError_t le =
+                        last ? launch_march3d<float, true>(fk, s32, g->n[0], g->n[1], g->n[2], nsm, 0, st)
+                             : launch_march3d<float, false>(fk, s32, g->n[0], g->n[1], g->n[2], nsm, 0, st);
+                    if (le != cudaSuccess) return cg_fail(ctx, CG_ERR_CUDA, "fused3d launch: %s", cudaGetErrorString(le));
+                    int r = cg_bc_apply_impl(ctx, g, nd, (it % 2 == 0) ? w.dV2 : w.dV, bc0);
                     if (r) return r;
                 }
             }
@@ -462,15 +562,24 @@ int cg_stokes_solve_dc(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f,
             total_iter += nchunk;
             if ((rc = cg_bc_apply_impl(ctx, g, nd, f32.r_V, rbc))) return rc;
             if ((rc = cg_maxabs_enqueue(ctx, nd + 1, red32))) return rc;
-            double e32[4];
-            if ((rc = cg_maxabs_collect(ctx, nd + 1, red32, e32, &bad))) return rc;
+            // the constitutive measure into the next reduction slot
+            CG_CUDA(ctx, cudaMemsetAsync(ctx->d_red + nd + 1, 0, sizeof(unsigned long long), ctx->stream));
+            if (nd == 2)
+                tau_res_kernel<2><<<grid3, block, 0, ctx->stream>>>(v32, s32, e0, e1, g->n[0], g->n[1], 1,
+                                                                     ctx->d_red + nd + 1);
+            else
+                tau_res_kernel<3><<<grid3, block, 0, ctx->stream>>>(v32, s32, e0, e1, g->n[0], g->n[1], g->n[2],
+                                                                     ctx->d_red + nd + 1);
+            CG_CHECK_LAUNCH(ctx);
+            double e32[5];
+            if ((rc = cg_maxabs_collect(ctx, nd + 2, red32, e32, &bad))) return rc;
             res->checks++;
             if (bad) {
                 status = CG_ERR_NONFINITE;
                 cg_fail(ctx, CG_ERR_NONFINITE, "stokes_solve (FP32): non-finite correction residual");
                 break;
             }
-            double em = e32[0] * o->tau_scale;
+            double em = std::max(e32[0], e32[nd + 1]) * o->tau_scale;
             for (int d = 0; d < nd; ++d) em = std::max(em, e32[1 + d] * o->v_scale);
             if (em < target) break;
             if (em < 0.9 * best) {

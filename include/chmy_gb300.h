@@ -239,12 +239,14 @@ CG_API int cg_stokes_update_thermal(cg_ctx* ctx, const cg_grid* grid, const cg_s
 CG_API int cg_stokes_pt_iterations(cg_ctx* ctx, const cg_grid* grid, const cg_stokes_fields* f,
                             const cg_stokes_params* p, const cg_bc* bc_V, int niter);
 
-/* Ping-pong form of cg_stokes_pt_iterations for 2D variable viscosity: one fused launch per
- * iteration (update_stress! and update_velocity! together, tiles in shared memory) reading
- * V, P, tau from `a` and writing them to `b`, then from `b` to `a`, each followed by bc!(V).
- * `niter` must be even (the result is in `a`). All other fields (tau_old, inv_eta, rho_g,
- * divV, r_V) are taken from `a`; inv_eta is required. divV and r_V are written on the last
- * iteration. Values equal the two-kernel form up to FMA contraction. */
+/* Ping-pong form of cg_stokes_pt_iterations for 2D and 3D variable viscosity. Each
+ * iteration is one fused launch: update_stress! and update_velocity! together, in a kernel
+ * that marches over rows (2D) or planes (3D). It reads V, P, tau from `a` and writes them to
+ * `b`, then from `b` to `a`, and each launch is followed by bc!(V). `niter` must be even (the
+ * result is in `a`). All other fields (tau_old, inv_eta, rho_g, divV, r_V) are taken from
+ * `a`; inv_eta is required. divV and r_V are written on the last iteration. Every operation
+ * is rounded once, in the order of the reference kernels, with no contraction into FMA: the
+ * values are those of a CPU evaluation with -ffp-contract=off. */
 CG_API int cg_stokes_pt_iterations_pp(cg_ctx* ctx, const cg_grid* grid, const cg_stokes_fields* a,
                                       const cg_stokes_fields* b, const cg_stokes_params* p,
                                       const cg_bc* bc_V, int niter);

@@ -109,6 +109,60 @@ def test_fp32_defect_correction_reaches_fp64_tolerance(arch, n):
     assert np.max(np.abs(pa - pb_)) <= 1e-5 * np.abs(pa).max()
 
 
+def _compare_states(ref, dc, nd, rtol=1e-5):
+    for name in ("V", "tau"):
+        for fa, fb in zip(ref.fields[name], dc.fields[name]):
+            a, b = fa.to_numpy(), fb.to_numpy()
+            assert np.max(np.abs(a - b)) <= rtol * max(np.abs(a).max(), 1.0), name
+    sl = (slice(2, -2),) * nd
+    pa, pb_ = ref.fields["P"].to_numpy()[sl], dc.fields["P"].to_numpy()[sl]
+    pa, pb_ = pa - pa.mean(), pb_ - pb_.mean()
+    assert np.max(np.abs(pa - pb_)) <= rtol * max(np.abs(pa).max(), 1.0)
+
+
+def test_fp32_defect_correction_scalar_viscosity(arch):
+    """Scalar eta (the examples' form) with a buoyant disc: the FP32 correction runs the fused
+    kernel on a constant 1/eta and reaches the FP64 solve's tolerance and state."""
+    import dataclasses
+
+    from chmy_gb300.configs import padded_mesh
+
+    pb = stokes2d_inclusions(64, ncheck=16)
+    host = {k: v for k, v in pb.host.items() if k != "eta"}
+    x, y = padded_mesh(pb.grid, (Center(), Vertex()))
+    host["rho_g"] = [None, np.where(x**2 + y**2 < 0.1**2, 1.0, 0.0)]
+    pb = dataclasses.replace(pb, host=host)
+    ref = StokesSolver(arch, pb)
+    ref.apply_bc()
+    r64 = ref.solve(precision=_abi.CG_F64)
+    assert r64.converged == 1
+    dc = StokesSolver(arch, pb)
+    dc.apply_bc()
+    r32 = dc.solve(precision=_abi.CG_F32, max_outer=8, inner_rtol=1e-5)
+    assert r32.converged == 1, (r32.outer, r32.iterations, list(r32.err))
+    assert max(r32.err[i] for i in range(3)) < pb.eps
+    _compare_states(ref, dc, 2)
+
+
+def test_fp32_defect_correction_3d(arch):
+    """3D VE Stokes (Gaussian random log-viscosity, buoyant sphere, free slip): FP32 PT in the
+    z-marching fused kernel inside FP64 defect correction reaches the FP64 solve's tolerance
+    and state."""
+    from chmy_gb300.configs import stokes3d_grf
+
+    pb = stokes3d_grf(24, ncheck=24)
+    ref = StokesSolver(arch, pb)
+    ref.apply_bc()
+    r64 = ref.solve(precision=_abi.CG_F64)
+    assert r64.converged == 1, (r64.iterations, list(r64.err))
+    dc = StokesSolver(arch, pb)
+    dc.apply_bc()
+    r32 = dc.solve(precision=_abi.CG_F32, max_outer=8, inner_rtol=1e-5)
+    assert r32.converged == 1, (r32.outer, r32.iterations, list(r32.err))
+    assert max(r32.err[i] for i in range(4)) < pb.eps
+    _compare_states(ref, dc, 3)
+
+
 def test_fp32_solve_rejects_fp32_state(arch):
     pb = stokes2d_inclusions(32, dtype=np.float32)
     s = StokesSolver(arch, pb)

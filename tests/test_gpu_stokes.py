@@ -170,7 +170,7 @@ def test_pt_iterations_graph(arch, T, dims, var_eta):
 
 
 @pytest.mark.parametrize("T", TYPES)
-@pytest.mark.parametrize("dims", [(45, 38), (70, 33), (33, 97), (257, 300)])
+@pytest.mark.parametrize("dims", [(45, 38), (70, 33), (33, 97), (257, 300), (13, 12, 11), (31, 20, 70), (61, 7, 33)])
 def test_fused_pingpong_iterations(arch, T, dims):
     """cg_stokes_pt_iterations_pp (one fused launch per iteration, ping-pong buffers) ==
     niter x (update_stress!, update_velocity!, bc!(V)) on the oracle, bit for bit."""
@@ -185,7 +185,7 @@ def test_fused_pingpong_iterations(arch, T, dims):
     s.d["inv_eta"] = to_gpu(arch, ie)
     p = pt_params(g2, True)
     g = g2.desc()
-    bcs = _bc_V(2)
+    bcs = _bc_V(len(dims))
     bc_apply(g2, s.h["V"], bcs)
     for f, d in zip(s.h["V"], s.d["V"]):
         d.from_numpy(f.a)
