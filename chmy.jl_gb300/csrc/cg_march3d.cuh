@@ -74,46 +74,62 @@ __device__ __forceinline__ M3Row<T> m3_load(const Fused3D<T>& f, const MAt3<T, I
     return r;
 }
 
+// ---- point arithmetic (V: the value type, S: its scalar parameters' type) -------------------
+__device__ __forceinline__ float vneg(float a) { return -a; }
+__device__ __forceinline__ double vneg(double a) { return -a; }
+__device__ __forceinline__ float vmin(float a, float b) { return fminf(a, b); }
+__device__ __forceinline__ double vmin(double a, double b) { return fmin(a, b); }
+template <class V, class S>
+__device__ __forceinline__ V bcast(S x) {
+    return x;
+}
+
+// -(t - t_old) * inv_Gdt - t * ieta + 2 * e: the VE stress residual, left to right.
+template <class V, class S>
+__device__ __forceinline__ V m3_res(const SP<S>& s, V t, V to, V ie, V e) {
+    return radd(rsub(rmul(vneg(rsub(t, to)), s.inv_Gdt), rmul(t, ie)), rmul(e, S(2.0)));
+}
+
 // New shear stress on an (a, b) edge from its strain rate and the four cells' 1/eta around it
 // (e00 = both indices decremented, e10 = b decremented, e01 = a decremented, e11 = none),
 // interpolated with the Linear rule, a innermost.
-template <class T>
-__device__ __forceinline__ T m3_shear(const SP<T>& s, T e, T e00, T e10, T e01, T e11, T t, T to) {
-    const T half = T(0.5);
-    const T lo = rfma(half, rsub(e10, e00), e00);
-    const T hi = rfma(half, rsub(e11, e01), e01);
-    const T iev = rfma(half, rsub(hi, lo), lo);
-    const T eve = rdiv(T(1), radd(iev, s.inv_Gdt));
-    return radd(t, rmul(rmul(stress_res(s, t, to, iev, e), eve), s.dtau_r));
+template <class V, class S>
+__device__ __forceinline__ V m3_shear(const SP<S>& s, V e, V e00, V e10, V e01, V e11, V t, V to) {
+    const V half = bcast<V>(S(0.5));
+    const V lo = rfma(half, rsub(e10, e00), e00);
+    const V hi = rfma(half, rsub(e11, e01), e01);
+    const V iev = rfma(half, rsub(hi, lo), lo);
+    const V eve = rrcp(radd(iev, s.inv_Gdt));
+    return radd(t, rmul(rmul(m3_res(s, t, to, iev, e), eve), s.dtau_r));
 }
 
 // 0.5 * (d_b(V_a) + d_a(V_b)) with each derivative (right - left) * inverse spacing.
-template <class T>
-__device__ __forceinline__ T m3_rate(T a1, T a0, T ia, T b1, T b0, T ib) {
-    return rmul(T(0.5), radd(rmul(rsub(a1, a0), ia), rmul(rsub(b1, b0), ib)));
+template <class V, class S>
+__device__ __forceinline__ V m3_rate(V a1, V a0, S ia, V b1, V b0, S ib) {
+    return rmul(radd(rmul(rsub(a1, a0), ia), rmul(rsub(b1, b0), ib)), S(0.5));
 }
 
-template <class T>
+template <class V>
 struct Cell3 {
-    T P, txx, tyy, tzz, dvP;
+    V P, txx, tyy, tzz, dvP;
 };
 
 // New P and diagonal stresses at a cell from its velocity differences (update_stress!).
-template <class T>
-__device__ __forceinline__ Cell3<T> m3_cell(const SP<T>& s, bool has_fP, T dvx, T dvy, T dvz, T ie, T P, T txx, T txo,
-                                            T tyy, T tyo, T tzz, T tzo, T fp) {
-    const T exx = rmul(dvx, s.idx[0]);
-    const T eyy = rmul(dvy, s.idx[1]);
-    const T ezz = rmul(dvz, s.idx[2]);
-    const T dv = radd(radd(exx, eyy), ezz);
-    const T dvt = rmul(dv, s.third);
-    const T eve = rdiv(T(1), radd(ie, s.inv_Gdt));
-    Cell3<T> c;
+template <class V, class S>
+__device__ __forceinline__ Cell3<V> m3_cell(const SP<S>& s, bool has_fP, V dvx, V dvy, V dvz, V ie, V P, V txx, V txo,
+                                            V tyy, V tyo, V tzz, V tzo, V fp) {
+    const V exx = rmul(dvx, s.idx[0]);
+    const V eyy = rmul(dvy, s.idx[1]);
+    const V ezz = rmul(dvz, s.idx[2]);
+    const V dv = radd(radd(exx, eyy), ezz);
+    const V dvt = rmul(dv, s.third);
+    const V eve = rrcp(radd(ie, s.inv_Gdt));
+    Cell3<V> c;
     c.dvP = has_fP ? radd(dv, fp) : dv;
     c.P = rsub(P, rmul(rmul(c.dvP, eve), s.dtau_Pr));
-    c.txx = radd(txx, rmul(rmul(stress_res(s, txx, txo, ie, rsub(exx, dvt)), eve), s.dtau_r));
-    c.tyy = radd(tyy, rmul(rmul(stress_res(s, tyy, tyo, ie, rsub(eyy, dvt)), eve), s.dtau_r));
-    c.tzz = radd(tzz, rmul(rmul(stress_res(s, tzz, tzo, ie, rsub(ezz, dvt)), eve), s.dtau_r));
+    c.txx = radd(txx, rmul(rmul(m3_res(s, txx, txo, ie, rsub(exx, dvt)), eve), s.dtau_r));
+    c.tyy = radd(tyy, rmul(rmul(m3_res(s, tyy, tyo, ie, rsub(eyy, dvt)), eve), s.dtau_r));
+    c.tzz = radd(tzz, rmul(rmul(m3_res(s, tzz, tzo, ie, rsub(ezz, dvt)), eve), s.dtau_r));
     return c;
 }
 
@@ -132,7 +148,7 @@ struct M3Smem {
 // store the new values the neighbours need and the block syncs; the owned rows update the
 // velocity at plane k. x-neighbours come from shuffles, z-neighbours from registers. The
 // arithmetic rounds every operation as the CPU oracle does (see radd/rmul).
-template <class T, class Ix, bool UNI, bool WRITE_RES, int NW, int MINB>
+template <class T, class Ix, bool UNI, bool WRITE_RES, int NW, int MINB, bool PREF = true>
 __global__ void __launch_bounds__(32 * NW, MINB)
     march3d_kernel(const Fused3D<T> f, const SP<T> s, int e0, int e1, int e2, int nstrip, int ntile_y, int seg_len,
                    long s1u, long s2u) {
@@ -212,11 +228,16 @@ __global__ void __launch_bounds__(32 * NW, MINB)
         __syncthreads();  // the prologue's reads of A before the first step's writes
     }
 
-    // the next step's loads are issued before the current step is computed
-    M3Row<T> cur = m3_load(f, at, ks, e2, inV, inC, nd);
+    // PREF: the next step's loads are issued before the current step is computed
+    M3Row<T> cur;
+    if (PREF) cur = m3_load(f, at, ks, e2, inV, inC, nd);
     for (int k = ks; k <= ke; ++k) {
         M3Row<T> nxt;
-        if (k < ke) nxt = m3_load(f, at, k + 1, e2, inV, inC, nd);
+        if (PREF) {
+            if (k < ke) nxt = m3_load(f, at, k + 1, e2, inV, inC, nd);
+        } else {
+            cur = m3_load(f, at, k, e2, inV, inC, nd);
+        }
         // (A) old values for the y-neighbours
         sm.vx[w][lane] = vx_c;
         sm.vy[w][lane] = vy_c;
@@ -316,7 +337,7 @@ __global__ void __launch_bounds__(32 * NW, MINB)
         tzzn_p = c.tzz;
         txz_c = txzn;
         tyz_c = tyzn;
-        cur = nxt;
+        if (PREF) cur = nxt;
     }
 }
 
@@ -374,43 +395,44 @@ inline bool march3_uniform(const Fused3D<T>& f, long* s1, long* s2) {
     return *s1 != 0;
 }
 
-constexpr int kM3Warps = 8;  // y-rows per block: 6 owned + 2 halo
+constexpr int kM3Warps = 8;  // default y-rows per block (owned rows + 2 halo rows)
 
-template <class T, class Ix, bool UNI, bool WRITE_RES, int MINB>
+// Z-segment length: the number of segments whose blocks fill the resident slots best (whole
+// waves), with segments of at least 16 planes.
+inline int m3_seg_len(long tiles, int planes, long cap) {
+    int best = 1;
+    double best_eff = 0;
+    for (int ns = 1; ns <= 64 && (ns == 1 || planes / ns >= 16); ++ns) {
+        const int len = cg_div_up(planes, ns);
+        const long items = tiles * cg_div_up(planes, len);
+        const long waves = (items + cap - 1) / cap;
+        const double eff = (double)items / (double)(waves * cap) * (double)len / (double)(len + 1);
+        if (eff > best_eff + 1e-3) {
+            best_eff = eff;
+            best = ns;
+        }
+    }
+    return cg_div_up(planes, best);
+}
+
+template <class T, class Ix, bool UNI, bool WRITE_RES, int MINB, int NW = kM3Warps, bool PREF = true>
 inline cudaError_t launch_march3d_ix(const Fused3D<T>& f, const SP<T>& s, int n0, int n1, int n2, int num_sms,
                                      int seg_len, long s1u, long s2u, cudaStream_t st) {
-    constexpr int NW = kM3Warps;
     const int e0 = n0 + 1, e1 = n1 + 1, e2 = n2 + 1;
     const int nstrip = cg_div_up(e0 + 1, 30), nty = cg_div_up(e1 + 1, NW - 2);
     const long tiles = (long)nstrip * nty;
     if (seg_len <= 0) {
-        // the number of z segments whose blocks fill the resident slots best (whole waves),
-        // with segments of at least 16 planes
         static const int bps = [] {
             int nb = 0;
-            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march3d_kernel<T, Ix, UNI, WRITE_RES, NW, MINB>,
-                                                              32 * NW, 0) != cudaSuccess)
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                    &nb, march3d_kernel<T, Ix, UNI, WRITE_RES, NW, MINB, PREF>, 32 * NW, 0) != cudaSuccess)
                 nb = 0;
             return nb > 0 ? nb : 1;
         }();
-        const long cap = (long)num_sms * bps;
-        const int planes = e2 + 1;
-        int best = 1;
-        double best_eff = 0;
-        for (int ns = 1; ns <= 64 && (ns == 1 || planes / ns >= 16); ++ns) {
-            const int len = cg_div_up(planes, ns);
-            const long items = tiles * cg_div_up(planes, len);
-            const long waves = (items + cap - 1) / cap;
-            const double eff = (double)items / (double)(waves * cap) * (double)len / (double)(len + 1);
-            if (eff > best_eff + 1e-3) {
-                best_eff = eff;
-                best = ns;
-            }
-        }
-        seg_len = cg_div_up(planes, best);
+        seg_len = m3_seg_len(tiles, e2 + 1, (long)num_sms * bps);
     }
     const int nseg = cg_div_up(e2 + 1, seg_len);
-    march3d_kernel<T, Ix, UNI, WRITE_RES, NW, MINB>
+    march3d_kernel<T, Ix, UNI, WRITE_RES, NW, MINB, PREF>
         <<<(unsigned)(tiles * nseg), 32 * NW, 0, st>>>(f, s, e0, e1, e2, nstrip, nty, seg_len, s1u, s2u);
     return cudaGetLastError();
 }
@@ -421,8 +443,14 @@ inline cudaError_t launch_march3d(const Fused3D<T>& f, const SP<T>& s, int n0, i
                                   cudaStream_t st) {
     long s1 = 0, s2 = 0;
     const bool uni = march3_uniform(f, &s1, &s2);
+    // FP32 with shared strides: 12 rows per block at 80 registers, 2 blocks (24 warps) per SM,
+    // no spills (the best measured of 4-16 rows per block and 1-5 blocks per SM at 256^3)
     if (march3_fits_int(f, n0 + 1, n1 + 1, n2 + 1)) {
-        if (uni) return launch_march3d_ix<T, int, true, WRITE_RES, 1>(f, s, n0, n1, n2, num_sms, seg_len, s1, s2, st);
+        if (uni) {
+            if constexpr (sizeof(T) == 4)
+                return launch_march3d_ix<T, int, true, WRITE_RES, 2, 12>(f, s, n0, n1, n2, num_sms, seg_len, s1, s2, st);
+            return launch_march3d_ix<T, int, true, WRITE_RES, 1>(f, s, n0, n1, n2, num_sms, seg_len, s1, s2, st);
+        }
         return launch_march3d_ix<T, int, false, WRITE_RES, 1>(f, s, n0, n1, n2, num_sms, seg_len, 0, 0, st);
     }
     if (uni) return launch_march3d_ix<T, long, true, WRITE_RES, 1>(f, s, n0, n1, n2, num_sms, seg_len, s1, s2, st);
