@@ -301,7 +301,10 @@ def run_ours(args, rank, world, dist):
         iters_all = float(iters)
     bytes_per_iter = A32 * n * n * 4
     value = bytes_per_iter * iters_all / (ms * 1e-3) / 1e9
-    launches = sum(2 * r.iterations + 2 * r.checks + 6 * (r.outer + 1) for r in results)
+    # kernels in the timed solves: per PT iteration the fused kernel and bc!(V); per check bc!(r_V),
+    # the max-norm and (inner checks) the constitutive measure, or (outer checks) the FP64
+    # defect; per correction the FP64 update and bc!(V); one 1/eta conversion per solve
+    launches = sum(2 * r.iterations + 3 * r.checks + 2 * r.outer + 1 for r in results)
 
     # e2e through the public API with host buffers: upload the initial state from pinned host
     # memory, solve, read the velocity and pressure back every step
@@ -365,6 +368,36 @@ def run_ours(args, rank, world, dist):
     peak, peak_kind = measured_peaks()
     traffic = committed_traffic(f"march2d_f32_{n}")
 
+    # the 3D fused kernel on the 3D random-viscosity problem at 256^3, timed alone the same way
+    stokes3d = None
+    if not args.skip_3d:
+        from chmy_gb300.configs import stokes3d_grf
+
+        n3 = 256
+        pb3 = stokes3d_grf(n3, dtype=np.float32)
+        d3a, d3b, keep3 = fused3d_kernel_fields(arch, pb3)
+        g3 = pb3.grid.desc()
+        arch.call("cg_stokes_pt_iterations_pp", ctypes.byref(g3), ctypes.byref(d3a), ctypes.byref(d3b), ctypes.byref(pb3.params), None, 4)
+        torch.cuda.synchronize()
+        reps3 = 50
+        k0.record(stream)
+        arch.call("cg_stokes_pt_iterations_pp", ctypes.byref(g3), ctypes.byref(d3a), ctypes.byref(d3b), ctypes.byref(pb3.params), None, reps3)
+        k1.record(stream)
+        torch.cuda.synchronize()
+        ms3 = k0.elapsed_time(k1) / reps3
+        b3 = FUSED3_ARRAYS * n3**3 * 4
+        stokes3d = {
+            "workload": "3D VE Stokes 256^3, log-viscosity Gaussian random field (correlation length 0.1, std 1, seed 4), FP32 fused PT iteration",
+            "kernel": "march3d_kernel<float>",
+            "kernel_ms": ms3,
+            "algorithmic_bytes_per_launch": b3,
+            "t_eff_gbs": b3 / (ms3 * 1e-3) / 1e9,
+            "frac": b3 / (ms3 * 1e-3) / 1e9 / peak,
+            "traffic": committed_traffic(f"march3d_f32_{n3}"),
+        }
+        del keep3, d3a, d3b
+        torch.cuda.empty_cache()
+
     # plain FP64 GPU solve of the same problem, once (time_to_solution comparison)
     fp64 = None
     if not args.skip_fp64:
@@ -422,6 +455,7 @@ def run_ours(args, rank, world, dist):
                 "kernel_ms": fused_ms,
                 "algorithmic_bytes_per_launch": fused_bytes,
             },
+            "stokes3d": stokes3d,
             "cpu_baseline": {
                 "value": cpu_teff,
                 "unit": "GB/s",
@@ -544,6 +578,7 @@ def main():
     ap.add_argument("--ref-iters", type=int, default=400)
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--skip-fp64", action="store_true", help="skip the one-off plain FP64 GPU solve")
+    ap.add_argument("--skip-3d", action="store_true", help="skip the 3D fused-kernel measurement")
     args = ap.parse_args()
     if args.kernel:
         run_kernel(args)

@@ -202,6 +202,26 @@ SIGNATURES: dict[str, list] = {
         P(cg_solve_opts),
         P(cg_solve_result),
     ],
+    "cg_stokes_thermal_step": [_vp, P(cg_grid), P(cg_stokes_fields), P(cg_stokes_params), P(cg_bc), P(cg_field)],
+    "cg_stokes_pt_iterations_thermal": [
+        _vp,
+        P(cg_grid),
+        P(cg_stokes_fields),
+        P(cg_stokes_params),
+        P(cg_bc),
+        P(cg_bc),
+        C.c_int,
+    ],
+    "cg_stokes_solve_thermal": [
+        _vp,
+        P(cg_grid),
+        P(cg_stokes_fields),
+        P(cg_stokes_params),
+        P(cg_bc),
+        P(cg_bc),
+        P(cg_solve_opts),
+        P(cg_solve_result),
+    ],
     "cg_ptdiff_update_q": [_vp, P(cg_grid), P(cg_ptdiff_fields), P(cg_ptdiff_params)],
     "cg_ptdiff_update_C": [_vp, P(cg_grid), P(cg_ptdiff_fields), P(cg_ptdiff_params)],
     "cg_ptdiff_run": [_vp, P(cg_grid), P(cg_ptdiff_fields), P(cg_ptdiff_params), P(cg_bc), C.c_int, C.c_int],

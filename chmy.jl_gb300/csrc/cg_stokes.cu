@@ -195,6 +195,28 @@ int launch_thermal(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f, con
     return CG_OK;
 }
 
+// Fused thermal step Tin -> Tout (update_thermal_flux! + update_thermal!) over the launch range.
+template <class T, int ND>
+int launch_thermal_step(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f, const cg_stokes_params* p,
+                        const cg_field& Tin, const cg_field& Tout, cudaStream_t st) {
+    ThermalStep<T> a;
+    std::memset(&a, 0, sizeof(a));
+    a.Tin = cg_view<T>(Tin);
+    a.Told = cg_view<T>(f->T_old);
+    a.Tout = cg_view<T>(Tout);
+    for (int d = 0; d < ND; ++d) {
+        a.V[d] = cg_view<T>(f->V[d]);
+        a.idx[d] = (T)g->inv_spacing[d];
+    }
+    a.mlam = -(T)p->lambda_rhoCp;
+    a.dt = (T)p->dt;
+    dim3 block(32, 8);
+    thermal_step_kernel<T, ND><<<range_grid<ND>(g, block), block, 0, st>>>(a, g->n[0] + 1, g->n[1] + 1,
+                                                                          ND > 2 ? g->n[2] + 1 : 0);
+    CG_CHECK_LAUNCH(ctx);
+    return CG_OK;
+}
+
 #define SDISPATCH(fn, dtype, nd, ...)                                                              \
     ((dtype) == CG_F64 ? ((nd) == 2 ? fn<double, 2>(__VA_ARGS__) : fn<double, 3>(__VA_ARGS__))    \
                        : ((nd) == 2 ? fn<float, 2>(__VA_ARGS__) : fn<float, 3>(__VA_ARGS__)))
@@ -205,8 +227,34 @@ int apply_bc_V(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f, const c
     return cg_bc_apply_impl(ctx, g, g->ndim, f->V, bc_V);
 }
 
+// Bytes from a field's first stored element to its last (the whole padded array).
+size_t padded_span_bytes(const cg_field& f) {
+    size_t span = 1;
+    for (int d = 0; d < f.ndim; ++d) span += (size_t)(f.n[d] + 4 * f.halo[d] - 1) * (size_t)f.stride[d];
+    return span * (f.dtype == CG_F64 ? 8 : 4);
+}
+
+// The library's partner buffer of T for the thermal ping-pong (scratch slot 0, T's layout).
+int thermal_partner(cg_ctx* ctx, const cg_field& Tf, cg_field* out) {
+    int rc = 0;
+    void* p = cg_scratch(ctx, 0, padded_span_bytes(Tf), &rc);
+    if (rc) return rc;
+    *out = Tf;
+    out->data = p;
+    return CG_OK;
+}
+
+// `niter` PT iterations: update_stress!, update_velocity!, bc!(V) and, with bc_T, the thermal
+// step and bc!(T) (examples/stokes_2d_inc_ve_T.jl:144-152). T alternates with the library's
+// partner buffer and ends in f->T.
 int pt_iterations(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f, const cg_stokes_params* p,
-                  const cg_bc* bc_V, int niter, int dtype, const Pre* pr = nullptr) {
+                  const cg_bc* bc_V, int niter, int dtype, const Pre* pr = nullptr, const cg_bc* bc_T = nullptr) {
+    cg_field Tw;
+    std::memset(&Tw, 0, sizeof(Tw));
+    if (bc_T) {
+        int rc = thermal_partner(ctx, f->T, &Tw);
+        if (rc) return rc;
+    }
     std::string key = "stokes_pt";
     cg_key_add(key, *g);
     cg_key_add(key, *f);
@@ -216,8 +264,16 @@ int pt_iterations(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f, cons
     std::memset(none, 0, sizeof(none));
     for (int d = 0; d < g->ndim; ++d) cg_key_add(key, bc_V ? bc_V[d] : none[d]);
     cg_key_add(key, pr ? pr->base : nullptr);
+    cg_key_add(key, bc_T ? 1 : 0);
+    if (bc_T) {
+        cg_key_add(key, *bc_T);
+        cg_key_add(key, Tw.data);
+    }
     const int nd = g->ndim;
-    return cg_graph_run(ctx, key, [&](cudaStream_t) {
+    const size_t tbytes = bc_T ? padded_span_bytes(f->T) : 0;
+    return cg_graph_run(ctx, key, [&](cudaStream_t st) {
+        // the partner starts as a copy, so that points no step writes agree in both buffers
+        if (bc_T) CG_CUDA(ctx, cudaMemcpyAsync(Tw.data, f->T.data, tbytes, cudaMemcpyDeviceToDevice, st));
         for (int it = 0; it < niter; ++it) {
             const bool last = it == niter - 1;
             int rc = SDISPATCH(launch_stress, dtype, nd, ctx, g, f, p, last, pr);
@@ -226,7 +282,14 @@ int pt_iterations(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f, cons
             if (rc) return rc;
             rc = apply_bc_V(ctx, g, f, bc_V);
             if (rc) return rc;
+            if (bc_T) {
+                const cg_field& src = (it % 2 == 0) ? f->T : Tw;
+                const cg_field& dst = (it % 2 == 0) ? Tw : f->T;
+                if ((rc = SDISPATCH(launch_thermal_step, dtype, nd, ctx, g, f, p, src, dst, st))) return rc;
+                if ((rc = cg_bc_apply_impl(ctx, g, 1, &dst, bc_T))) return rc;
+            }
         }
+        if (bc_T && (niter & 1)) CG_CUDA(ctx, cudaMemcpyAsync(f->T.data, Tw.data, tbytes, cudaMemcpyDeviceToDevice, st));
         return (int)CG_OK;
     });
 }
@@ -477,20 +540,28 @@ extern "C" int cg_stokes_residual(cg_ctx* ctx, const cg_grid* grid, const cg_sto
     return bad ? cg_fail(ctx, CG_ERR_NONFINITE, "stokes_residual: non-finite residual") : CG_OK;
 }
 
-extern "C" int cg_stokes_solve(cg_ctx* ctx, const cg_grid* grid, const cg_stokes_fields* f, const cg_stokes_params* p,
-                               const cg_bc* bc_V, const cg_solve_opts* o, cg_solve_result* res) {
-    int dtype;
-    int rc = check_stokes(ctx, grid, f, NEED_V | NEED_TAU | NEED_TAU_OLD | NEED_P, &dtype);
+namespace {
+
+int check_solve(cg_ctx* ctx, const cg_grid* grid, const cg_stokes_fields* f, const cg_stokes_params* p,
+                const cg_solve_opts* o, cg_solve_result* res, int* dtype) {
+    int rc = check_stokes(ctx, grid, f, NEED_V | NEED_TAU | NEED_TAU_OLD | NEED_P, dtype);
     if (rc) return rc;
     if (!p || !o || !res) return cg_fail(ctx, CG_ERR_ARG, "stokes_solve: NULL argument");
     if (o->ncheck < 1 || o->max_iter < 1) return cg_fail(ctx, CG_ERR_ARG, "stokes_solve: ncheck/max_iter < 1");
     if (!cg_present(f->divV) || !cg_present(f->r_V[0]))
         return cg_fail(ctx, CG_ERR_ARG, "stokes_solve: divV and r_V are required for the convergence check");
-    if (dtype != CG_F64) return cg_fail(ctx, CG_ERR_UNSUPPORTED, "stokes_solve: the solution fields must be FP64");
+    if (*dtype != CG_F64) return cg_fail(ctx, CG_ERR_UNSUPPORTED, "stokes_solve: the solution fields must be FP64");
     if (o->precision != CG_F64 && o->precision != CG_F32)
         return cg_fail(ctx, CG_ERR_ARG, "stokes_solve: precision must be CG_F64 or CG_F32");
-    cudaSetDevice(ctx->device);
-    if (o->precision == CG_F32) return cg_stokes_solve_dc(ctx, grid, f, p, bc_V, o, res);
+    return CG_OK;
+}
+
+// The reference PT loop in FP64 (examples/stokes_2d_inc_ve_T.jl:144-163): graph-replayed
+// chunks of ncheck iterations, then the convergence measures. With bc_T, every iteration also
+// takes the thermal step.
+int solve_fp64(cg_ctx* ctx, const cg_grid* grid, const cg_stokes_fields* f, const cg_stokes_params* p,
+               const cg_bc* bc_V, const cg_bc* bc_T, const cg_solve_opts* o, cg_solve_result* res, int dtype) {
+    int rc;
     // variable viscosity: precompute the viscosity terms once for the whole solve
     Pre pre;
     const bool var = cg_present(f->eta) || cg_present(f->inv_eta);
@@ -501,7 +572,7 @@ extern "C" int cg_stokes_solve(cg_ctx* ctx, const cg_grid* grid, const cg_stokes
     int status = CG_ERR_NOCONV;
     while (iter < o->max_iter) {
         const int chunk = std::min(o->ncheck, o->max_iter - iter);
-        if ((rc = pt_iterations(ctx, grid, f, p, bc_V, chunk, dtype, var ? &pre : nullptr))) return rc;
+        if ((rc = pt_iterations(ctx, grid, f, p, bc_V, chunk, dtype, var ? &pre : nullptr, bc_T))) return rc;
         iter += chunk;
         if (chunk < o->ncheck) break;  // the reference only checks at multiples of ncheck
         int32_t bad = 0;
@@ -528,4 +599,65 @@ extern "C" int cg_stokes_solve(cg_ctx* ctx, const cg_grid* grid, const cg_stokes
     res->iterations = iter;
     if (status == CG_ERR_NOCONV) cg_fail(ctx, CG_ERR_NOCONV, "stokes_solve: not converged after %d iterations", iter);
     return status;
+}
+
+int check_thermal(cg_ctx* ctx, const cg_grid* grid, const cg_stokes_fields* f, int dtype) {
+    int rc;
+    if ((rc = cg_check_field(ctx, grid, f->T, dtype, 0, "T"))) return rc;
+    if ((rc = cg_check_field(ctx, grid, f->T_old, dtype, 0, "T_old"))) return rc;
+    return CG_OK;
+}
+
+}  // namespace
+
+extern "C" int cg_stokes_solve(cg_ctx* ctx, const cg_grid* grid, const cg_stokes_fields* f, const cg_stokes_params* p,
+                               const cg_bc* bc_V, const cg_solve_opts* o, cg_solve_result* res) {
+    int dtype;
+    int rc = check_solve(ctx, grid, f, p, o, res, &dtype);
+    if (rc) return rc;
+    cudaSetDevice(ctx->device);
+    if (o->precision == CG_F32) return cg_stokes_solve_dc(ctx, grid, f, p, bc_V, o, res);
+    return solve_fp64(ctx, grid, f, p, bc_V, nullptr, o, res, dtype);
+}
+
+extern "C" int cg_stokes_solve_thermal(cg_ctx* ctx, const cg_grid* grid, const cg_stokes_fields* f,
+                                       const cg_stokes_params* p, const cg_bc* bc_V, const cg_bc* bc_T,
+                                       const cg_solve_opts* o, cg_solve_result* res) {
+    int dtype;
+    int rc = check_solve(ctx, grid, f, p, o, res, &dtype);
+    if (rc) return rc;
+    if (!bc_T) return cg_fail(ctx, CG_ERR_ARG, "stokes_solve_thermal: bc_T is NULL");
+    if ((rc = check_thermal(ctx, grid, f, dtype))) return rc;
+    if (o->precision != CG_F64)
+        return cg_fail(ctx, CG_ERR_UNSUPPORTED, "stokes_solve_thermal: FP64 PT only (precision CG_F64)");
+    cudaSetDevice(ctx->device);
+    return solve_fp64(ctx, grid, f, p, bc_V, bc_T, o, res, dtype);
+}
+
+extern "C" int cg_stokes_pt_iterations_thermal(cg_ctx* ctx, const cg_grid* grid, const cg_stokes_fields* f,
+                                               const cg_stokes_params* p, const cg_bc* bc_V, const cg_bc* bc_T,
+                                               int niter) {
+    int dtype;
+    int rc = check_stokes(ctx, grid, f, NEED_V | NEED_TAU | NEED_TAU_OLD | NEED_P, &dtype);
+    if (rc) return rc;
+    if (!p || !bc_T) return cg_fail(ctx, CG_ERR_ARG, "pt_iterations_thermal: NULL argument");
+    if ((rc = check_thermal(ctx, grid, f, dtype))) return rc;
+    if (niter < 0) return cg_fail(ctx, CG_ERR_ARG, "pt_iterations_thermal: niter < 0");
+    if (niter == 0) return CG_OK;
+    cudaSetDevice(ctx->device);
+    return pt_iterations(ctx, grid, f, p, bc_V, niter, dtype, nullptr, bc_T);
+}
+
+extern "C" int cg_stokes_thermal_step(cg_ctx* ctx, const cg_grid* grid, const cg_stokes_fields* f,
+                                      const cg_stokes_params* p, const cg_bc* bc_T, const cg_field* T_out) {
+    int dtype;
+    int rc = check_stokes(ctx, grid, f, NEED_V, &dtype);
+    if (rc) return rc;
+    if (!p || !T_out) return cg_fail(ctx, CG_ERR_ARG, "thermal_step: NULL argument");
+    if ((rc = check_thermal(ctx, grid, f, dtype))) return rc;
+    if ((rc = cg_check_field(ctx, grid, *T_out, dtype, 0, "T_out"))) return rc;
+    if (T_out->data == f->T.data) return cg_fail(ctx, CG_ERR_ARG, "thermal_step: T_out must not be T");
+    cudaSetDevice(ctx->device);
+    if ((rc = SDISPATCH(launch_thermal_step, dtype, grid->ndim, ctx, grid, f, p, f->T, *T_out, ctx->stream))) return rc;
+    return bc_T ? cg_bc_apply_impl(ctx, grid, 1, T_out, bc_T) : CG_OK;
 }

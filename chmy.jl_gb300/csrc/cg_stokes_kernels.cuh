@@ -7,6 +7,24 @@
 namespace cgk {
 
 
+// Arithmetic with explicit round-to-nearest and no contraction into FMA: every operation
+// rounds once, in the order the CPU oracle (built with -ffp-contract=off) evaluates it, so the
+// marching kernel matches it bitwise and a value recomputed at a segment edge rounds exactly
+// like the owner's copy.
+__device__ __forceinline__ float radd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double radd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float rsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double rsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float rmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double rmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float rdiv(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ double rdiv(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ float rfma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double rfma(double a, double b, double c) { return __fma_rn(a, b, c); }
+// 1/x correctly rounded: the same value as the IEEE division 1/x, with fewer instructions
+__device__ __forceinline__ float rrcp(float x) { return __frcp_rn(x); }
+__device__ __forceinline__ double rrcp(double x) { return __drcp_rn(x); }
+
 template <class T>
 struct SV {  // device views of the Stokes field set
     DF<T> V[3], rV[3], P, divV, tau[6], tau_old[6], eta, ieta, rho[3], Tt, To, qT[3];
@@ -303,6 +321,47 @@ __global__ void thermal_kernel(const SV<T> v, const SP<T> s, int e0, int e1) {
     v.Tt(i, j, k) = v.To(i, j, k) - s.dt * dv;
 }
 
+// ---- fused thermal step: update_thermal_flux! + update_thermal! ------------------------------
+//
+// T_out = T_old - dt * divg(qT) with qT_d = -lambda * d_d(T) + max(V_d, 0) * T_left +
+// min(V_d, 0) * T_right (examples/stokes_2d_inc_ve_T.jl:35-50, 3D :59-77) computed on the fly
+// at the two faces of each cell, over Chmy's launch range. A face flux at index n+2 lies beyond
+// the flux kernel's launch range, so in the two-kernel form it reads the untouched allocation:
+// zero here. Every operation is rounded once in the oracle's order (max/min as std::max/min).
+template <class T>
+__device__ __forceinline__ T heat_flux(T mlam, T tl, T tr, T v, T idx) {
+    const T vp = v < T(0) ? T(0) : v;  // std::max(v, 0)
+    const T vm = T(0) < v ? T(0) : v;  // std::min(v, 0)
+    return radd(radd(rmul(mlam, rmul(rsub(tr, tl), idx)), rmul(vp, tl)), rmul(vm, tr));
+}
+
+template <class T>
+struct ThermalStep {
+    DF<T> Tin, Told, Tout, V[3];
+    T mlam, dt, idx[3];
+};
+
+template <class T, int ND>
+__global__ void thermal_step_kernel(const ThermalStep<T> a, int e0, int e1, int e2) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = ND > 2 ? blockIdx.z : 0;
+    if (i > e0 || j > e1) return;
+    const T c = a.Tin(i, j, k);
+    const T qx0 = heat_flux(a.mlam, a.Tin(i - 1, j, k), c, a.V[0](i, j, k), a.idx[0]);
+    const T qx1 = i + 1 <= e0 ? heat_flux(a.mlam, c, a.Tin(i + 1, j, k), a.V[0](i + 1, j, k), a.idx[0]) : T(0);
+    T dq = rmul(rsub(qx1, qx0), a.idx[0]);
+    const T qy0 = heat_flux(a.mlam, a.Tin(i, j - 1, k), c, a.V[1](i, j, k), a.idx[1]);
+    const T qy1 = j + 1 <= e1 ? heat_flux(a.mlam, c, a.Tin(i, j + 1, k), a.V[1](i, j + 1, k), a.idx[1]) : T(0);
+    dq = radd(dq, rmul(rsub(qy1, qy0), a.idx[1]));
+    if (ND > 2) {
+        const T qz0 = heat_flux(a.mlam, a.Tin(i, j, k - 1), c, a.V[2](i, j, k), a.idx[2]);
+        const T qz1 = k + 1 <= e2 ? heat_flux(a.mlam, c, a.Tin(i, j, k + 1), a.V[2](i, j, k + 1), a.idx[2]) : T(0);
+        dq = radd(dq, rmul(rsub(qz1, qz0), a.idx[2]));
+    }
+    a.Tout(i, j, k) = rsub(a.Told(i, j, k), rmul(a.dt, dq));
+}
+
 // ---- fused 2D PT iteration (variable viscosity): update_stress! + update_velocity! -----------
 //
 // One launch per PT iteration, reading the `in` buffers and writing the `out` buffers
@@ -371,24 +430,6 @@ __device__ __forceinline__ MarchRow<T> march_load(const Fused2D<T>& f, const MAt
     r.rhoy = f.has_rho ? at.ld(f.rhoy, j, c) : T(0);
     return r;
 }
-
-// Arithmetic with explicit round-to-nearest and no contraction into FMA: every operation
-// rounds once, in the order the CPU oracle (built with -ffp-contract=off) evaluates it, so the
-// marching kernel matches it bitwise and a value recomputed at a segment edge rounds exactly
-// like the owner's copy.
-__device__ __forceinline__ float radd(float a, float b) { return __fadd_rn(a, b); }
-__device__ __forceinline__ double radd(double a, double b) { return __dadd_rn(a, b); }
-__device__ __forceinline__ float rsub(float a, float b) { return __fsub_rn(a, b); }
-__device__ __forceinline__ double rsub(double a, double b) { return __dsub_rn(a, b); }
-__device__ __forceinline__ float rmul(float a, float b) { return __fmul_rn(a, b); }
-__device__ __forceinline__ double rmul(double a, double b) { return __dmul_rn(a, b); }
-__device__ __forceinline__ float rdiv(float a, float b) { return __fdiv_rn(a, b); }
-__device__ __forceinline__ double rdiv(double a, double b) { return __ddiv_rn(a, b); }
-__device__ __forceinline__ float rfma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
-__device__ __forceinline__ double rfma(double a, double b, double c) { return __fma_rn(a, b, c); }
-// 1/x correctly rounded: the same value as the IEEE division 1/x, with fewer instructions
-__device__ __forceinline__ float rrcp(float x) { return __frcp_rn(x); }
-__device__ __forceinline__ double rrcp(double x) { return __drcp_rn(x); }
 
 // -(t - t_old) * inv_Gdt - t * ieta + 2 * e: the VE stress residual, left to right.
 template <class T>

@@ -287,6 +287,33 @@ CG_API int cg_stokes_solve(cg_ctx* ctx, const cg_grid* grid, const cg_stokes_fie
                     const cg_stokes_params* p, const cg_bc* bc_V, const cg_solve_opts* o,
                     cg_solve_result* res);
 
+/* ---- thermal coupling (examples/stokes_2d_inc_ve_T.jl:35-60,147-152) ----------------------
+ * From the second time step on, every PT iteration of the reference also takes the thermal
+ * step: qT_d = -lambda_rhoCp * d_d(T) + max(V_d, 0) * T_left + min(V_d, 0) * T_right
+ * (update_thermal_flux!), T = T_old - dt * divg(qT) (update_thermal!), bc!(T => bc_T). */
+
+/* The two thermal kernels fused: T_out = T_old - dt * divg(qT(T, V)) over [0, n+1]^N, with the
+ * fluxes computed on the fly and not stored, then bc!(T_out => bc_T) when bc_T is not NULL.
+ * f supplies T (read only), T_old and V; p supplies lambda_rhoCp and dt. T_out must not be T.
+ * A flux at face index n+2 (beyond the flux kernel's launch range) counts as zero, as a freshly
+ * allocated qT reads there. Every operation is rounded once in the reference's order: the
+ * values equal a CPU evaluation of the two kernels with -ffp-contract=off. */
+CG_API int cg_stokes_thermal_step(cg_ctx* ctx, const cg_grid* grid, const cg_stokes_fields* f,
+                           const cg_stokes_params* p, const cg_bc* bc_T, const cg_field* T_out);
+
+/* `niter` PT iterations with thermal coupling: update_stress!, update_velocity!, bc!(V), the
+ * thermal step and bc!(T), as one graph. T alternates with a library-owned partner buffer and
+ * the result is in f->T. */
+CG_API int cg_stokes_pt_iterations_thermal(cg_ctx* ctx, const cg_grid* grid, const cg_stokes_fields* f,
+                                    const cg_stokes_params* p, const cg_bc* bc_V, const cg_bc* bc_T,
+                                    int niter);
+
+/* cg_stokes_solve with the thermal step in every PT iteration (the reference's solve for time
+ * steps after the first). FP64 PT only: o->precision must be CG_F64. */
+CG_API int cg_stokes_solve_thermal(cg_ctx* ctx, const cg_grid* grid, const cg_stokes_fields* f,
+                            const cg_stokes_params* p, const cg_bc* bc_V, const cg_bc* bc_T,
+                            const cg_solve_opts* o, cg_solve_result* res);
+
 /* ---- pseudo-transient variable-coefficient diffusion -------------------------------------
  * Implicit (backward Euler) diffusion step (C - C_old)/dt = divg(D grad C) solved by damped
  * PT iterations in the pattern of the Stokes PT loop; the flux is Chmy's ∂k∂/divg_grad form

@@ -811,12 +811,15 @@ int or_stokes_update_velocity(const cg_grid* grid, const cg_stokes_fields* f, co
 }
 
 int or_stokes_update_thermal_flux(const cg_grid* grid, const cg_stokes_fields* f, const cg_stokes_params* p) {
+    if (!f->T.data || !f->qT[0].data || !f->qT[1].data || (grid->ndim > 2 && !f->qT[2].data)) return CG_ERR_ARG;
     if (f->T.dtype == CG_F64) stokes_update_thermal_flux_t<double>(grid, f, p);
     else stokes_update_thermal_flux_t<float>(grid, f, p);
     return CG_OK;
 }
 
 int or_stokes_update_thermal(const cg_grid* grid, const cg_stokes_fields* f, const cg_stokes_params* p) {
+    if (!f->T.data || !f->T_old.data || !f->qT[0].data || !f->qT[1].data || (grid->ndim > 2 && !f->qT[2].data))
+        return CG_ERR_ARG;
     if (f->T.dtype == CG_F64) stokes_update_thermal_t<double>(grid, f, p);
     else stokes_update_thermal_t<float>(grid, f, p);
     return CG_OK;

@@ -170,3 +170,140 @@ def test_fp32_solve_rejects_fp32_state(arch):
     res = _abi.cg_solve_result()
     rc = arch.lib.cg_stokes_solve(arch.ctx, ctypes.byref(s.grid_desc), ctypes.byref(s.desc), ctypes.byref(pb.params), s.bc_arr, ctypes.byref(o), ctypes.byref(res))
     assert rc == _abi.CG_ERR_UNSUPPORTED
+
+
+def _example_setup(nxy, T):
+    """examples/stokes_2d_inc_ve_T.jl:62-110 (scalar eta = 10, buoyant disc, hot disc)."""
+    from chmy_gb300.configs import padded_mesh
+    from chmy_gb300.grids import UniformGrid
+
+    lx = ly = 2.0
+    eta, G = 10.0, 1.0
+    psc, tsc = G, eta / G
+    T0, Ta = 1.0, 0.1
+    lam = 1e-4 * ly**2 / tsc
+    grid = UniformGrid(origin=(-lx / 2, -ly / 2), extent=(lx, ly), dims=(nxy, nxy), dtype=T)
+    C_, V_ = Center(), Vertex()
+    r = 0.1 * lx
+    xc, yc = padded_mesh(grid, C_)
+    xv, yv = padded_mesh(grid, (C_, V_))
+
+    def z(loc):
+        return np.zeros_like(padded_mesh(grid, loc)[0], dtype=T)
+
+    tl = [(C_, C_), (C_, C_), (V_, V_)]
+    host = {
+        "V": [z((V_, C_)), z((C_, V_))],
+        "r_V": [z((V_, C_)), z((C_, V_))],
+        "P": z(C_),
+        "divV": z(C_),
+        "tau": [z(l) for l in tl],
+        "tau_old": [z(l) for l in tl],
+        "T": np.where(xc**2 + yc**2 < r * r, T0, Ta).astype(T),
+        "T_old": z(C_),
+        "rho_g": [None, np.where(xv**2 + yv**2 < r * r, 1.0, 0.0).astype(T)],
+        "qT": [z((V_, C_)), z((C_, V_))],  # the oracle's two-kernel form stores the fluxes
+    }
+    dx = float(grid.spacing()[0])
+    re_m, rr = 2.3 * np.pi, 0.5
+    lt = min(lx, ly) / re_m
+    vdt = dx / np.sqrt(2 * 1.1)
+    th = lt * (rr + 4.0 / 3.0) / vdt
+    consts = dict(eta=eta, G=G, lam=lam, dtau_r=1.0 / (th + 1.0), nu_dtau=vdt * lt, dtau_Pr=rr / th, tsc=tsc,
+                  vsc=ly / psc, dx=dx)
+    return grid, host, consts
+
+
+def test_example_time_loop_with_thermal_coupling(arch):
+    """Two time steps of examples/stokes_2d_inc_ve_T.jl:134-164 at 62^2 in FP64: update_old!,
+    dt from max|V|, the PT solve (with the thermal step from the second time step on), on the
+    GPU through the library and on the oracle. Iteration counts agree and so does T."""
+    from chmy_gb300.bcs import Neumann
+    from chmy_gb300.fields import Field
+    from chmy_gb300.kernels import stokes_fields, stokes_params
+
+    T = np.float64
+    nxy = 62
+    grid, host, c = _example_setup(nxy, T)
+    g = grid.desc()
+    bc_V = [to_cg_bc(2, {"x": Dirichlet(), "y": Neumann()}), to_cg_bc(2, {"x": Neumann(), "y": Dirichlet()})]
+    bcT = to_cg_bc(2, {"x": Neumann(), "y": Neumann()})
+    eps = 1e-6
+    C_, V_ = Center(), Vertex()
+    locs = {"V": [(V_, C_), (C_, V_)], "r_V": [(V_, C_), (C_, V_)], "tau": [(C_, C_), (C_, C_), (V_, V_)],
+            "tau_old": [(C_, C_), (C_, C_), (V_, V_)], "rho_g": [None, (C_, V_)], "qT": [(V_, C_), (C_, V_)]}
+    dev, hst = {}, {}
+    for k, v in host.items():
+        if isinstance(v, list):
+            dev[k], hst[k] = [], []
+            for a, loc in zip(v, locs[k]):
+                if a is None:
+                    dev[k].append(None)
+                    hst[k].append(None)
+                    continue
+                f = Field(arch, grid, loc, T)
+                f.from_numpy(a)
+                dev[k].append(f)
+                h = NpField(grid, loc, T)
+                h.a[...] = a
+                hst[k].append(h)
+        else:
+            f = Field(arch, grid, C_, T)
+            f.from_numpy(v)
+            dev[k] = f
+            h = NpField(grid, C_, T)
+            h.a[...] = v
+            hst[k] = h
+    dd = stokes_fields(**dev)
+    hd = stokes_desc(**hst)
+    bc_apply(grid, [hst["T"]], [bcT])
+    arch.call("cg_bc_apply", ctypes.byref(g), 1, ctypes.byref(dev["T"].desc()), ctypes.byref(bcT))
+    rb = [to_cg_bc(2, {"x": Dirichlet()}), to_cg_bc(2, {"y": Dirichlet()})]
+    dx = c["dx"]
+    for it in (1, 2):
+        arch.call("cg_stokes_update_old", ctypes.byref(g), ctypes.byref(dd))
+        lib().or_stokes_update_old(ctypes.byref(g), ctypes.byref(hd))
+        vmax = [max(np.abs(f.interior()).max(), 1e-300) for f in hst["V"]]
+        dt_diff = dx * dx / c["lam"] / 2 / 2.1
+        dt_adv = 0.1 * min(dx / vmax[0], dx / vmax[1]) / 2 / 2.1
+        dt = min(dt_diff, dt_adv)
+        eta_ve = 1.0 / (1.0 / c["eta"] + 1.0 / (c["G"] * dt))
+        p = stokes_params(eta=c["eta"], eta_ve=eta_ve, G=c["G"], dt=dt, dtau_Pr=c["dtau_Pr"], dtau_r=c["dtau_r"],
+                          nu_dtau=c["nu_dtau"], lambda_rhoCp=c["lam"])
+        ncheck = 2 * nxy
+        niter = 50 * nxy
+        # oracle: the reference loop
+        it_ref = None
+        for k in range(1, niter + 1):
+            lib().or_stokes_update_stress(ctypes.byref(g), ctypes.byref(hd), ctypes.byref(p))
+            lib().or_stokes_update_velocity(ctypes.byref(g), ctypes.byref(hd), ctypes.byref(p))
+            bc_apply(grid, hst["V"], bc_V)
+            if it > 1:
+                lib().or_stokes_update_thermal_flux(ctypes.byref(g), ctypes.byref(hd), ctypes.byref(p))
+                lib().or_stokes_update_thermal(ctypes.byref(g), ctypes.byref(hd), ctypes.byref(p))
+                bc_apply(grid, [hst["T"]], [bcT])
+            if k % ncheck == 0:
+                bc_apply(grid, hst["r_V"], rb)
+                e = [np.abs(hst["divV"].interior()).max() * c["tsc"]] + [np.abs(f.interior()).max() * c["vsc"] for f in hst["r_V"]]
+                if max(e) < eps:
+                    it_ref = k
+                    break
+        assert it_ref is not None, f"oracle did not converge in time step {it}"
+        o = _abi.cg_solve_opts(max_iter=niter, ncheck=ncheck, eps=eps, tau_scale=c["tsc"], v_scale=c["vsc"], precision=_abi.CG_F64)
+        r = _abi.cg_solve_result()
+        bcv = (_abi.cg_bc * 3)(*bc_V)
+        if it == 1:
+            arch.call("cg_stokes_solve", ctypes.byref(g), ctypes.byref(dd), ctypes.byref(p), bcv, ctypes.byref(o), ctypes.byref(r))
+        else:
+            arch.call("cg_stokes_solve_thermal", ctypes.byref(g), ctypes.byref(dd), ctypes.byref(p), bcv, ctypes.byref(bcT), ctypes.byref(o), ctypes.byref(r))
+        arch.synchronize()
+        assert r.converged == 1
+        assert r.iterations == it_ref, (it, r.iterations, it_ref)
+    scale = np.abs(hst["T"].a).max()
+    err = np.abs(dev["T"].to_numpy() - hst["T"].a).max()
+    assert err <= 1e-9 * scale, err
+    assert np.abs(dev["T"].to_numpy() - host["T"]).max() > 0  # the second step moved T
+    # FP32 is not offered with thermal coupling
+    o.precision = _abi.CG_F32
+    rc = arch.lib.cg_stokes_solve_thermal(arch.ctx, ctypes.byref(g), ctypes.byref(dd), ctypes.byref(p), bcv, ctypes.byref(bcT), ctypes.byref(o), ctypes.byref(r))
+    assert rc == _abi.CG_ERR_UNSUPPORTED

@@ -213,3 +213,64 @@ def test_fused_pingpong_iterations(arch, T, dims):
     # odd niter is rejected
     rc = arch.lib.cg_stokes_pt_iterations_pp(arch.ctx, ctypes.byref(g), ctypes.byref(da), ctypes.byref(db), ctypes.byref(p), barr, 3)
     assert rc == _abi.CG_ERR_ARG
+
+
+def _thermal_set(arch, dims, T, seed):
+    s = StokesSet(arch, dims, T, seed, True, thermal=True)
+    # qT starts as a fresh (zero) field on the oracle side: the fused step reads zero beyond
+    # the flux kernel's launch range exactly as the two-kernel form reads this allocation
+    for f in s.h["qT"]:
+        f.a[...] = 0
+    return s
+
+
+@pytest.mark.parametrize("T", TYPES)
+@pytest.mark.parametrize("dims", [(37, 29), (13, 11, 9)])
+def test_thermal_step_fused_bitwise(arch, T, dims):
+    """cg_stokes_thermal_step == update_thermal_flux!, update_thermal!, bc!(T) on the oracle, bit
+    for bit (fluxes with both signs of V)."""
+    s = _thermal_set(arch, dims, T, 41)
+    p = pt_params(s.grid, True)
+    g = s.grid.desc()
+    nd = len(dims)
+    bcT = to_cg_bc(nd, {"xyz"[d]: Neumann() for d in range(nd)})
+    T_out = to_gpu(arch, s.h["T"])  # starts as a copy of T: points outside the launch range agree
+    T0 = s.h["T"].a.copy()
+    hd = s.host_desc()
+    assert lib().or_stokes_update_thermal_flux(ctypes.byref(g), ctypes.byref(hd), ctypes.byref(p)) == 0
+    assert lib().or_stokes_update_thermal(ctypes.byref(g), ctypes.byref(hd), ctypes.byref(p)) == 0
+    bc_apply(s.grid, [s.h["T"]], [bcT])
+    arch.call("cg_stokes_thermal_step", ctypes.byref(g), ctypes.byref(s.dev_desc()), ctypes.byref(p), ctypes.byref(bcT), ctypes.byref(T_out.desc()))
+    arch.synchronize()
+    assert_close(T_out, s.h["T"], 0.0, "thermal step", exact=True)
+    assert np.array_equal(s.d["T"].to_numpy(), T0), "T is read only"
+
+
+@pytest.mark.parametrize("T", TYPES)
+@pytest.mark.parametrize("dims", [(31, 26), (12, 10, 11)])
+@pytest.mark.parametrize("niter", [4, 5])
+def test_pt_iterations_thermal(arch, T, dims, niter):
+    """cg_stokes_pt_iterations_thermal == niter x (update_stress!, update_velocity!, bc!(V),
+    update_thermal_flux!, update_thermal!, bc!(T)) on the oracle (odd niter ends in the partner
+    buffer and is copied back)."""
+    s = _thermal_set(arch, dims, T, 43)
+    p = pt_params(s.grid, True)
+    g = s.grid.desc()
+    nd = len(dims)
+    bcs = _bc_V(nd)
+    bcT = to_cg_bc(nd, {"xyz"[d]: Neumann() for d in range(nd)})
+    hd = s.host_desc()
+    for _ in range(niter):
+        lib().or_stokes_update_stress(ctypes.byref(g), ctypes.byref(hd), ctypes.byref(p))
+        lib().or_stokes_update_velocity(ctypes.byref(g), ctypes.byref(hd), ctypes.byref(p))
+        bc_apply(s.grid, s.h["V"], bcs)
+        lib().or_stokes_update_thermal_flux(ctypes.byref(g), ctypes.byref(hd), ctypes.byref(p))
+        lib().or_stokes_update_thermal(ctypes.byref(g), ctypes.byref(hd), ctypes.byref(p))
+        bc_apply(s.grid, [s.h["T"]], [bcT])
+    arch.call("cg_stokes_pt_iterations_thermal", ctypes.byref(g), ctypes.byref(s.dev_desc()), ctypes.byref(p), (_abi.cg_bc * 3)(*bcs), ctypes.byref(bcT), niter)
+    arch.synchronize()
+    for name in ("V", "P", "tau", "T"):
+        hv = s.h[name] if isinstance(s.h[name], list) else [s.h[name]]
+        dv = s.d[name] if isinstance(s.d[name], list) else [s.d[name]]
+        for a, b in zip(dv, hv):
+            assert_close(a, b, rtol_for(T) * niter * 10, f"thermal PT {name}")
