@@ -202,6 +202,7 @@ SIGNATURES: dict[str, list] = {
         P(cg_solve_opts),
         P(cg_solve_result),
     ],
+    "cg_stokes_gradient_log_eta": [_vp, P(cg_grid), P(cg_stokes_fields), P(cg_field), P(cg_stokes_params), P(cg_field)],
     "cg_stokes_thermal_step": [_vp, P(cg_grid), P(cg_stokes_fields), P(cg_stokes_params), P(cg_bc), P(cg_field)],
     "cg_stokes_pt_iterations_thermal": [
         _vp,

@@ -123,6 +123,57 @@ class StokesSolver:
             _abi.check(self.arch.lib, rc, "cg_stokes_solve", self.arch.ctx)
         return res
 
+    def gradient_log_eta(self, dJdV, precision: int = _abi.CG_F64, eps: float | None = None, max_iter: int | None = None):
+        """dJ/d log(eta) at every cell for a misfit J(V) of the converged state this solver holds
+        (call solve() first). `dJdV` lists per velocity component a padded host array, or None.
+
+        The adjoint velocity solves the same Stokes problem (the discrete operator is
+        symmetric): body force -dJ/dV, tau_old = 0, zero initial state and the forward's
+        boundary-condition kinds with zero values, by cg_stokes_solve in `precision`. The
+        library then forms the gradient from the adjoint velocity and the forward stress
+        (cg_stokes_gradient_log_eta). Returns (grad Field, adjoint solve result)."""
+        import dataclasses
+
+        pb = self.pb
+        g = pb.grid
+        nd = g.ndim
+        if "eta" not in pb.host:
+            raise ValueError("gradient_log_eta: the problem needs a viscosity field")
+        zero = {}
+        for name, val in pb.host.items():
+            if name in ("eta", "T", "T_old", "qT"):
+                continue
+            if isinstance(val, list):
+                zero[name] = [None if a is None else np.zeros_like(a) for a in val]
+            else:
+                zero[name] = np.zeros_like(val)
+        zero["eta"] = pb.host["eta"]
+        ref = pb.host["V"]
+        zero["rho_g"] = [None if a is None else -np.asarray(a, dtype=ref[d].dtype) for d, a in enumerate(list(dJdV) + [None] * (3 - len(dJdV)))][:nd]
+        bcs = []
+        for b in pb.bc_V:
+            b0 = _abi.cg_bc()
+            ctypes.memmove(ctypes.byref(b0), ctypes.byref(b), ctypes.sizeof(b0))
+            for d in range(3):
+                for side in range(2):
+                    b0.value[d][side] = 0.0
+            bcs.append(b0)
+        adj_pb = dataclasses.replace(pb, host=zero, bc_V=bcs, eps=float(eps if eps is not None else pb.eps))
+        adj = StokesSolver(self.arch, adj_pb)
+        adj.apply_bc()
+        res = adj.solve(precision=precision, max_iter=max_iter)
+        grad = Field(self.arch, g, Center(), self.fields["eta"].dtype)
+        mu = (_abi.cg_field * 3)(*[f.desc() for f in adj.fields["V"]])
+        self.arch.call(
+            "cg_stokes_gradient_log_eta",
+            ctypes.byref(self.grid_desc),
+            ctypes.byref(self.desc),
+            mu,
+            ctypes.byref(pb.params),
+            ctypes.byref(grad.desc()),
+        )
+        return grad, res
+
     def apply_bc(self) -> None:
         fa = (_abi.cg_field * 3)(*[f.desc() for f in self.fields["V"]])
         self.arch.call("cg_bc_apply", ctypes.byref(self.grid_desc), self.pb.grid.ndim, fa, self.bc_arr)

@@ -245,9 +245,10 @@ __global__ void tau_res_kernel(const SV<float> v, const SP<float> s, int e0, int
     const int k = ND > 2 ? blockIdx.z : 0;
     unsigned m = 0;
     if (i <= e0 && j <= e1) {
-        // interior test per location: index <= n - 1 (Center) or n (Vertex) along each dim
+        // interior test per location: logical index 1..n (Center) or 1..n+1 (Vertex) along each
+        // dim (0 is the lower ghost layer of the launch range)
         auto in = [&](int li, int lj, int lk) {
-            return i <= n0 - 1 + li && j <= n1 - 1 + lj && (ND < 3 || k <= n2 - 1 + lk);
+            return i >= 1 && j >= 1 && i <= n0 + li && j <= n1 + lj && (ND < 3 || (k >= 1 && k <= n2 + lk));
         };
         auto take = [&](float r) { m = max(m, __float_as_uint(fabsf(r))); };
         const float exx = (v.V[0](i + 1, j, k) - v.V[0](i, j, k)) * s.idx[0];

@@ -287,6 +287,21 @@ CG_API int cg_stokes_solve(cg_ctx* ctx, const cg_grid* grid, const cg_stokes_fie
                     const cg_stokes_params* p, const cg_bc* bc_V, const cg_solve_opts* o,
                     cg_solve_result* res);
 
+/* ---- adjoint: gradient of a velocity misfit with respect to log-viscosity ------------------
+ * For a misfit J(V) of the converged VE Stokes step, the adjoint velocity mu solves the same
+ * Stokes problem (the discrete operator is symmetric): cg_stokes_solve on a field set with
+ * rho_g = -dJ/dV, tau_old = 0, V = P = tau = 0 initially and the forward's boundary-condition
+ * kinds with zero values. This entry then writes, at every interior cell c,
+ *   grad_c = dJ/d log(eta_c) = -(1/eta)_c [ eta_ve_c sum_d eps_dd(mu) tau_dd(V)
+ *                                           + 1/2 sum_{shear edges e at c} eta_ve_e eps_e(mu) tau_e(V) ]
+ * with tau(V) = eta_ve (2 dev(eps(V)) + tau_old/(G dt)) the constitutive stress of the forward's
+ * converged velocity `fwd->V` (and `fwd->tau_old` when present), its viscosity `fwd->inv_eta`
+ * (else `fwd->eta`), eta_ve = 1/(1/eta + 1/(G dt)) at cells and the edges' 1/eta the
+ * Linear-rule mean of their 4 cells, as in the forward kernels. `mu` holds ndim velocity
+ * fields. No reference counterpart: the reference has no adjoint. */
+CG_API int cg_stokes_gradient_log_eta(cg_ctx* ctx, const cg_grid* grid, const cg_stokes_fields* fwd,
+                               const cg_field* mu, const cg_stokes_params* p, const cg_field* grad);
+
 /* ---- thermal coupling (examples/stokes_2d_inc_ve_T.jl:35-60,147-152) ----------------------
  * From the second time step on, every PT iteration of the reference also takes the thermal
  * step: qT_d = -lambda_rhoCp * d_d(T) + max(V_d, 0) * T_left + min(V_d, 0) * T_right
