@@ -1,0 +1,122 @@
+"""Adjoint of the implicit variable-coefficient diffusion steps (cg_ptdiff_run): the gradient of
+a misfit of the final state with respect to the per-cell diffusivity D and to the initial state,
+by reverse time stepping over checkpoints.
+
+One step is C' = S C with S = (I - dt L_D)^-1, L_D C = divg(lerp(D) d C). I - dt L_D is symmetric
+on the interior cells (the boundary rules folded in), so the adjoint of a step is the same PT
+step: lambda^n = S lambda^{n+1}. The gradient with respect to D sums one term per step,
+cg_ptdiff_gradient_D(lambda^n, C^{n+1}, dt). The reverse sweep needs C^{n+1} in reverse order:
+every `checkpoint_every`-th state (with the PT flux, the rest of the state) is kept during the
+forward sweep, and each segment is recomputed from its checkpoint before it is swept back.
+Memory: nsteps / checkpoint_every + checkpoint_every states.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import math
+
+import numpy as np
+
+from . import _abi
+from .fields import Field
+from .grids import Center, Vertex
+
+
+def _zero_bc(bc: _abi.cg_bc) -> _abi.cg_bc:
+    b = _abi.cg_bc()
+    ctypes.memmove(ctypes.byref(b), ctypes.byref(bc), ctypes.sizeof(b))
+    for d in range(3):
+        for s in range(2):
+            b.value[d][s] = 0.0
+    return b
+
+
+class PTDiffusion:
+    """Implicit diffusion steps on device fields (C, C_old, D, q) with their adjoint."""
+
+    def __init__(self, arch, grid, D: np.ndarray, params, bc: _abi.cg_bc, npt: int, dtype=np.float64):
+        self.arch, self.grid, self.params, self.bc, self.npt = arch, grid, params, bc, int(npt)
+        self.bc0 = _zero_bc(bc)
+        nd = grid.ndim
+        self.nd = nd
+        C = Center()
+        qloc = [tuple(Vertex() if e == d else C for e in range(nd)) for d in range(nd)]
+
+        def fset():
+            return {
+                "C": Field(arch, grid, C, dtype),
+                "C_old": Field(arch, grid, C, dtype),
+                "q": [Field(arch, grid, l, dtype) for l in qloc],
+            }
+
+        self.D = Field(arch, grid, C, dtype)
+        self.D.from_numpy(D)
+        self.fwd, self.adj = fset(), fset()
+        self.gD = Field(arch, grid, C, dtype)
+
+    def _desc(self, fs):
+        s = _abi.cg_ptdiff_fields()
+        s.C, s.C_old, s.D = fs["C"].desc(), fs["C_old"].desc(), self.D.desc()
+        s.q = (_abi.cg_field * 3)(*[f.desc() for f in fs["q"]])
+        return s
+
+    def _steps(self, fs, bc, nsteps: int) -> None:
+        if nsteps <= 0:
+            return
+        self.arch.call("cg_ptdiff_run", ctypes.byref(self.grid.desc()), ctypes.byref(self._desc(fs)), ctypes.byref(self.params),
+                       ctypes.byref(bc), int(nsteps), self.npt)
+
+    def _save(self):
+        return [self.fwd["C"].data.clone()] + [f.data.clone() for f in self.fwd["q"]]
+
+    def _restore(self, st) -> None:
+        self.fwd["C"].data.copy_(st[0])
+        for f, s in zip(self.fwd["q"], st[1:]):
+            f.data.copy_(s)
+
+    def run(self, C0: np.ndarray, nsteps: int) -> np.ndarray:
+        """Forward: `nsteps` implicit steps from C0 (flux starting at zero); returns C^N."""
+        self.fwd["C"].from_numpy(C0)
+        for f in self.fwd["q"]:
+            f.data.zero_()
+        self._steps(self.fwd, self.bc, nsteps)
+        return self.fwd["C"].to_numpy()
+
+    def gradient(self, C0: np.ndarray, nsteps: int, misfit_grad, checkpoint_every: int | None = None):
+        """Gradients of J(C^N) with respect to D (per cell) and to C0. `misfit_grad(CN)` returns
+        dJ/dC^N as a padded host array (zero outside the interior). Returns (dJ/dD, dJ/dC0, C^N)
+        as padded host arrays."""
+        K = int(checkpoint_every or max(1, math.ceil(math.sqrt(nsteps))))
+        self.fwd["C"].from_numpy(C0)
+        for f in self.fwd["q"]:
+            f.data.zero_()
+        checkpoints = {}
+        for n in range(nsteps):
+            if n % K == 0:
+                checkpoints[n] = self._save()
+            self._steps(self.fwd, self.bc, 1)
+        CN = self.fwd["C"].to_numpy()
+        self.adj["C"].from_numpy(misfit_grad(CN))
+        self.gD.data.zero_()
+        dt = float(self.params.dt)
+        g = self.grid.desc()
+        for start in sorted(checkpoints, reverse=True):
+            stop = min(start + K, nsteps)
+            # recompute this segment's states C^{start+1} .. C^{stop}
+            self._restore(checkpoints[start])
+            states = []
+            for _ in range(start, stop):
+                self._steps(self.fwd, self.bc, 1)
+                states.append(self.fwd["C"].data.clone())
+            for n in range(stop - 1, start - 1, -1):
+                # lambda^n = S lambda^{n+1}: one PT step with C_old = lambda^{n+1}, zero boundary values
+                for f in self.adj["q"]:
+                    f.data.zero_()
+                self._steps(self.adj, self.bc0, 1)
+                Cn1 = self.fwd["C"]
+                Cn1.data.copy_(states[n - start])
+                self.arch.call("cg_ptdiff_gradient_D", ctypes.byref(g), ctypes.byref(self.adj["C"].desc()), ctypes.byref(Cn1.desc()),
+                               dt, ctypes.byref(self.gD.desc()))
+            del states
+        return self.gD.to_numpy(), self.adj["C"].to_numpy(), CN

@@ -176,3 +176,73 @@ extern "C" int cg_ptdiff_run(cg_ctx* ctx, const cg_grid* grid, const cg_ptdiff_f
         return (int)CG_OK;
     });
 }
+
+// ---- adjoint: gradient with respect to the diffusivity ------------------------------------
+//
+// One implicit step is C' = S C with S = (I - dt L_D)^-1 and L_D C = divg(lerp(D) d C). With
+// the boundary rules folded in, I - dt L_D is symmetric on the interior cells, so the adjoint
+// of a step is the same step: lambda^n = S lambda^{n+1} (a PT step with C_old = lambda^{n+1} and
+// zero boundary values). For a misfit J(C^N), perturbing D gives
+//   dJ = sum_n dt lambda^n . (dL_D C^{n+1}),
+// and, collecting the terms of each face f between cells l and r = l + e_d (the face's D is the
+// mean of its two cells, so each cell carries half of it),
+//   dJ/dD_c = dt sum_n sum_{faces f of c} 1/2 (C_r - C_l) idx_d^2 (lambda_l [l interior]
+//                                                                  - lambda_r [r interior]).
+// This kernel adds `scale` times one step's term (scale = dt) for lambda = lambda^n and
+// C = C^{n+1} at every interior cell (logical indices 1..n).
+namespace {
+
+template <class T, int ND>
+__global__ void ptdiff_grad_kernel(const DF<T> lam, const DF<T> C, const DF<T> grad, T scale, T idx0, T idx1,
+                                   T idx2, int n0, int n1, int n2) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = ND > 1 ? blockIdx.y * blockDim.y + threadIdx.y + 1 : 0;
+    const int k = ND > 2 ? blockIdx.z + 1 : 0;
+    if (i > n0 || (ND > 1 && j > n1) || (ND > 2 && k > n2)) return;
+    const int c[3] = {i, j, k}, n[3] = {n0, n1, n2};
+    const T idx[3] = {idx0, idx1, idx2};
+    T s = T(0);
+#pragma unroll
+    for (int d = 0; d < ND; ++d) {
+        for (int side = 0; side < 2; ++side) {
+            int l[3] = {c[0], c[1], c[2]}, r[3] = {c[0], c[1], c[2]};
+            if (side == 0) l[d] -= 1;  // lower face: (c - e_d, c)
+            else r[d] += 1;            // upper face: (c, c + e_d)
+            const T dC = (C(r[0], r[1], r[2]) - C(l[0], l[1], l[2])) * idx[d];
+            const T ll = l[d] >= 1 ? lam(l[0], l[1], l[2]) : T(0);
+            const T lr = r[d] <= n[d] ? lam(r[0], r[1], r[2]) : T(0);
+            s += T(0.5) * dC * (ll - lr) * idx[d];
+        }
+    }
+    grad(i, j, k) = grad(i, j, k) + scale * s;
+}
+
+}  // namespace
+
+extern "C" int cg_ptdiff_gradient_D(cg_ctx* ctx, const cg_grid* grid, const cg_field* lam, const cg_field* C,
+                                    double scale, const cg_field* grad) {
+    if (!ctx) return cg_fail(nullptr, CG_ERR_ARG, "ptdiff_gradient_D: ctx is NULL");
+    if (!grid || !lam || !C || !grad) return cg_fail(ctx, CG_ERR_ARG, "ptdiff_gradient_D: NULL argument");
+    int rc = cg_check_grid(ctx, grid);
+    if (rc) return rc;
+    const int dtype = grad->dtype, nd = grid->ndim;
+    if ((rc = cg_check_field(ctx, grid, *grad, dtype, 0, "grad"))) return rc;
+    if ((rc = cg_check_field(ctx, grid, *lam, dtype, 0, "lambda"))) return rc;
+    if ((rc = cg_check_field(ctx, grid, *C, dtype, 0, "C"))) return rc;
+    cudaSetDevice(ctx->device);
+    const int n0 = grid->n[0], n1 = nd > 1 ? grid->n[1] : 1, n2 = nd > 2 ? grid->n[2] : 1;
+    const dim3 block(nd == 1 ? 256 : 32, nd == 1 ? 1 : 8);
+    const dim3 gr(cg_div_up(n0, block.x), nd > 1 ? cg_div_up(n1, block.y) : 1, nd > 2 ? n2 : 1);
+    auto go = [&](auto tag) {
+        using T = decltype(tag);
+        const DF<T> l = cg_view<T>(*lam), c = cg_view<T>(*C), g = cg_view<T>(*grad);
+        const T i0 = (T)grid->inv_spacing[0], i1 = (T)grid->inv_spacing[1], i2 = (T)grid->inv_spacing[2];
+        if (nd == 1) ptdiff_grad_kernel<T, 1><<<gr, block, 0, ctx->stream>>>(l, c, g, (T)scale, i0, i1, i2, n0, n1, n2);
+        else if (nd == 2) ptdiff_grad_kernel<T, 2><<<gr, block, 0, ctx->stream>>>(l, c, g, (T)scale, i0, i1, i2, n0, n1, n2);
+        else ptdiff_grad_kernel<T, 3><<<gr, block, 0, ctx->stream>>>(l, c, g, (T)scale, i0, i1, i2, n0, n1, n2);
+    };
+    if (dtype == CG_F64) go(double(0));
+    else go(float(0));
+    CG_CHECK_LAUNCH(ctx);
+    return CG_OK;
+}

@@ -359,6 +359,18 @@ CG_API int cg_ptdiff_update_C(cg_ctx* ctx, const cg_grid* grid, const cg_ptdiff_
 CG_API int cg_ptdiff_run(cg_ctx* ctx, const cg_grid* grid, const cg_ptdiff_fields* f,
                          const cg_ptdiff_params* p, const cg_bc* bc, int nsteps, int npt);
 
+/* Adjoint of the implicit diffusion steps (no reference counterpart). I - dt L_D is symmetric
+ * on the interior cells, so the adjoint of a step is the same step: lambda^n = S lambda^{n+1}
+ * is cg_ptdiff_run (1 step) on a field set with C = lambda^{n+1} and zero boundary values. For
+ * a misfit J(C^N), dJ/dD = sum over steps of this entry's term, which adds at every interior
+ * cell c
+ *   scale * sum_{faces f of c} 1/2 (C_r - C_l) idx^2 (lambda_l [l interior] - lambda_r [r interior])
+ * (f between cells l and r; a face's D is the mean of its two cells) with lambda = lambda^n,
+ * C = C^{n+1} and scale = dt. The reverse sweep needs the states C^{n+1} in reverse order:
+ * store them or recompute them from checkpoints (chmy_gb300.adjoint does both). */
+CG_API int cg_ptdiff_gradient_D(cg_ctx* ctx, const cg_grid* grid, const cg_field* lam, const cg_field* C,
+                                double scale, const cg_field* grad);
+
 /* ---- shallow ice (examples/sia.jl) ----------------------------------------------------- */
 
 /* Parameters of the SIA step. examples/sia.jl:24-54 is Gamma = 1, As = 0.5, n = 3, beta = 0.5,
