@@ -42,6 +42,16 @@ struct cg_ctx {
 // not preserved across growth). Sets *rc on failure and returns NULL.
 void* cg_scratch(cg_ctx* ctx, int slot, size_t bytes, int* rc);
 
+// Launch layouts chosen by timing (autotuner): a process-wide cache keyed by problem shape.
+// CG_AUTOTUNE=0 in the environment turns the timing off (the launchers' fixed rules apply).
+struct cg_tune_cfg {
+    int seg;      // rows (2D) or planes (3D) per segment; 0 = the launcher's rule
+    int variant;  // kernel variant (3D: block shape)
+};
+bool cg_autotune_enabled();
+bool cg_tune_lookup(const std::string& key, cg_tune_cfg* out);
+void cg_tune_store(const std::string& key, const cg_tune_cfg& cfg);
+
 // Record an error message on ctx and return `code`.
 int cg_fail(cg_ctx* ctx, int code, const char* fmt, ...);
 

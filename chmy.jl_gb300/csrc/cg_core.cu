@@ -1,6 +1,7 @@
 // cg_core.cu — context, memory, argument checks, the fused boundary-condition kernel and the
 // max-norm reduction of libchmy_gb300.
 #include <cstdarg>
+#include <map>
 #include <mutex>
 #include <vector>
 
@@ -67,6 +68,32 @@ extern "C" int cg_destroy(cg_ctx* ctx) {
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     delete ctx;
     return CG_OK;
+}
+
+namespace {
+std::mutex g_tune_mu;
+std::map<std::string, cg_tune_cfg> g_tune;
+}  // namespace
+
+bool cg_autotune_enabled() {
+    static const bool on = [] {
+        const char* e = std::getenv("CG_AUTOTUNE");
+        return !(e && e[0] == '0');
+    }();
+    return on;
+}
+
+bool cg_tune_lookup(const std::string& key, cg_tune_cfg* out) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(key);
+    if (it == g_tune.end()) return false;
+    *out = it->second;
+    return true;
+}
+
+void cg_tune_store(const std::string& key, const cg_tune_cfg& cfg) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune[key] = cfg;
 }
 
 void* cg_scratch(cg_ctx* ctx, int slot, size_t bytes, int* rc) {

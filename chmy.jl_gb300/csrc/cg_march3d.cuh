@@ -438,23 +438,109 @@ inline cudaError_t launch_march3d_ix(const Fused3D<T>& f, const SP<T>& s, int n0
 }
 
 // Launch of the z-marching kernel over [0, n+1]^3; seg_len <= 0 picks the z-segment length.
+// For FP32 with shared strides, variant 0 is 12 rows per block at 2 blocks per SM and variant 1
+// is 8 rows per block at 3 blocks per SM (both 80 registers, no spills; the two best measured
+// of 4-16 rows per block and 1-5 blocks per SM at 256^3).
 template <class T, bool WRITE_RES>
 inline cudaError_t launch_march3d(const Fused3D<T>& f, const SP<T>& s, int n0, int n1, int n2, int num_sms, int seg_len,
-                                  cudaStream_t st) {
+                                  cudaStream_t st, int variant = 0) {
     long s1 = 0, s2 = 0;
     const bool uni = march3_uniform(f, &s1, &s2);
-    // FP32 with shared strides: 12 rows per block at 80 registers, 2 blocks (24 warps) per SM,
-    // no spills (the best measured of 4-16 rows per block and 1-5 blocks per SM at 256^3)
     if (march3_fits_int(f, n0 + 1, n1 + 1, n2 + 1)) {
         if (uni) {
-            if constexpr (sizeof(T) == 4)
+            if constexpr (sizeof(T) == 4) {
+                if (variant == 1)
+                    return launch_march3d_ix<T, int, true, WRITE_RES, 3, 8>(f, s, n0, n1, n2, num_sms, seg_len, s1, s2, st);
                 return launch_march3d_ix<T, int, true, WRITE_RES, 2, 12>(f, s, n0, n1, n2, num_sms, seg_len, s1, s2, st);
+            }
             return launch_march3d_ix<T, int, true, WRITE_RES, 1>(f, s, n0, n1, n2, num_sms, seg_len, s1, s2, st);
         }
         return launch_march3d_ix<T, int, false, WRITE_RES, 1>(f, s, n0, n1, n2, num_sms, seg_len, 0, 0, st);
     }
     if (uni) return launch_march3d_ix<T, long, true, WRITE_RES, 1>(f, s, n0, n1, n2, num_sms, seg_len, s1, s2, st);
     return launch_march3d_ix<T, long, false, WRITE_RES, 1>(f, s, n0, n1, n2, num_sms, seg_len, 0, 0, st);
+}
+
+// ---- autotuner: the segment length (2D) or segment length and block shape (3D) with the
+// shortest launch, timed with CUDA events on the caller's own buffers before a graph is
+// captured. Only the `out` buffers of the ping-pong view are written (the first real iteration
+// writes them again); the residual outputs are not touched. Results are cached per shape,
+// precision and layout for the process.
+template <class F>
+inline float time_launches(F&& launch, cudaStream_t st) {
+    cudaEvent_t a, b;
+    if (cudaEventCreate(&a) != cudaSuccess) return -1.f;
+    if (cudaEventCreate(&b) != cudaSuccess) {
+        cudaEventDestroy(a);
+        return -1.f;
+    }
+    float ms = -1.f;
+    if (launch() == cudaSuccess && cudaEventRecord(a, st) == cudaSuccess) {
+        bool ok = true;
+        for (int r = 0; r < 3 && ok; ++r) ok = launch() == cudaSuccess;
+        if (ok && cudaEventRecord(b, st) == cudaSuccess && cudaEventSynchronize(b) == cudaSuccess)
+            cudaEventElapsedTime(&ms, a, b);
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return ms;
+}
+
+template <class T>
+inline cg_tune_cfg tune_march2d(const Fused2D<T>& f, const SP<T>& s, int n0, int n1, int nsm, cudaStream_t st) {
+    cg_tune_cfg best{0, 0};
+    if (!cg_autotune_enabled()) return best;
+    std::string key = "march2d";
+    cg_key_add(key, n0);
+    cg_key_add(key, n1);
+    cg_key_add(key, (int)sizeof(T));
+    cg_key_add(key, march_uniform_stride(f));
+    cg_key_add(key, nsm);
+    if (cg_tune_lookup(key, &best)) return best;
+    float tbest = 1e30f;
+    for (int seg : {0, 8, 16, 24, 32, 48, 64}) {
+        if (seg > n1 + 2) continue;
+        const float t = time_launches([&] { return launch_march2d<T, false>(f, s, n0, n1, nsm, seg, st); }, st);
+        if (t >= 0.f && t < tbest) {
+            tbest = t;
+            best = cg_tune_cfg{seg, 0};
+        }
+    }
+    cudaGetLastError();
+    cg_tune_store(key, best);
+    return best;
+}
+
+template <class T>
+inline cg_tune_cfg tune_march3d(const Fused3D<T>& f, const SP<T>& s, int n0, int n1, int n2, int nsm, cudaStream_t st) {
+    cg_tune_cfg best{0, 0};
+    if (!cg_autotune_enabled()) return best;
+    long s1 = 0, s2 = 0;
+    const bool uni = march3_uniform(f, &s1, &s2);
+    std::string key = "march3d";
+    cg_key_add(key, n0);
+    cg_key_add(key, n1);
+    cg_key_add(key, n2);
+    cg_key_add(key, (int)sizeof(T));
+    cg_key_add(key, uni ? s1 : 0L);
+    cg_key_add(key, uni ? s2 : 0L);
+    cg_key_add(key, nsm);
+    if (cg_tune_lookup(key, &best)) return best;
+    const int nvar = (sizeof(T) == 4 && uni) ? 2 : 1;
+    float tbest = 1e30f;
+    for (int v = 0; v < nvar; ++v)
+        for (int seg : {0, 16, 32, 64}) {
+            if (seg > n2 + 2) continue;
+            const float t =
+                time_launches([&] { return launch_march3d<T, false>(f, s, n0, n1, n2, nsm, seg, st, v); }, st);
+            if (t >= 0.f && t < tbest) {
+                tbest = t;
+                best = cg_tune_cfg{seg, v};
+            }
+        }
+    cudaGetLastError();
+    cg_tune_store(key, best);
+    return best;
 }
 
 }  // namespace cgk

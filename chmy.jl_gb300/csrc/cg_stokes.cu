@@ -445,7 +445,9 @@ int pp_iterations_3d(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* a, c
     const Fused3D<T> fab = fused3_view<T>(a, b, a), fba = fused3_view<T>(b, a, a);
     const SP<T> s = scalars<T>(g, p);
     const bool res = cg_present(a->divV) && cg_present(a->r_V[0]);
+    const cg_tune_cfg tc = tune_march3d(fab, s, g->n[0], g->n[1], g->n[2], ctx->num_sms, ctx->stream);
     std::string key = "stokes_pp3";
+    cg_key_add(key, tc);
     cg_key_add(key, *g);
     cg_key_add(key, *a);
     cg_key_add(key, *b);
@@ -459,8 +461,8 @@ int pp_iterations_3d(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* a, c
             const Fused3D<T>& fk = (it % 2 == 0) ? fab : fba;
             const int nsm = ctx->num_sms;
             const cudaError_t le = (res && it == niter - 1)
-                                       ? launch_march3d<T, true>(fk, s, g->n[0], g->n[1], g->n[2], nsm, 0, st)
-                                       : launch_march3d<T, false>(fk, s, g->n[0], g->n[1], g->n[2], nsm, 0, st);
+                                       ? launch_march3d<T, true>(fk, s, g->n[0], g->n[1], g->n[2], nsm, tc.seg, st, tc.variant)
+                                       : launch_march3d<T, false>(fk, s, g->n[0], g->n[1], g->n[2], nsm, tc.seg, st, tc.variant);
             if (le != cudaSuccess) return cg_fail(ctx, CG_ERR_CUDA, "fused3d launch: %s", cudaGetErrorString(le));
             if (bc_V) {
                 int r = cg_bc_apply_impl(ctx, g, 3, (it % 2 == 0) ? b->V : a->V, bc_V);
@@ -478,7 +480,9 @@ int pp_iterations_t(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* a, co
     const Fused2D<T> fab = fused_view<T>(a, b, a), fba = fused_view<T>(b, a, a);
     const SP<T> s = scalars<T>(g, p);
     const bool res = cg_present(a->divV) && cg_present(a->r_V[0]);
+    const cg_tune_cfg tc = tune_march2d(fab, s, g->n[0], g->n[1], ctx->num_sms, ctx->stream);
     std::string key = "stokes_pp";
+    cg_key_add(key, tc);
     cg_key_add(key, *g);
     cg_key_add(key, *a);
     cg_key_add(key, *b);
@@ -492,8 +496,8 @@ int pp_iterations_t(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* a, co
             const Fused2D<T>& fk = (it % 2 == 0) ? fab : fba;
             const int nsm = ctx->num_sms;
             const cudaError_t le = (res && it == niter - 1)
-                                       ? launch_march2d<T, true>(fk, s, g->n[0], g->n[1], nsm, 0, st)
-                                       : launch_march2d<T, false>(fk, s, g->n[0], g->n[1], nsm, 0, st);
+                                       ? launch_march2d<T, true>(fk, s, g->n[0], g->n[1], nsm, tc.seg, st)
+                                       : launch_march2d<T, false>(fk, s, g->n[0], g->n[1], nsm, tc.seg, st);
             if (le != cudaSuccess) return cg_fail(ctx, CG_ERR_CUDA, "fused2d launch: %s", cudaGetErrorString(le));
             if (bc_V) {
                 int r = cg_bc_apply_impl(ctx, g, 2, (it % 2 == 0) ? b->V : a->V, bc_V);

@@ -482,6 +482,10 @@ int cg_stokes_solve_dc(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f,
     }
     const int nchunk = ncheck + (ncheck & 1);
     cg_key_add(key, nchunk);
+    // launch layout of the fused kernel, timed on the work buffers (A -> B) before capture
+    const cg_tune_cfg tc = nd == 2 ? tune_march2d(fa, s32, g->n[0], g->n[1], ctx->num_sms, ctx->stream)
+                                   : tune_march3d(ga, s32, g->n[0], g->n[1], g->n[2], ctx->num_sms, ctx->stream);
+    cg_key_add(key, tc);
     auto chunk = [&]() {
         return cg_graph_run(ctx, key, [&](cudaStream_t st) {
             for (int it = 0; it < nchunk; ++it) {
@@ -489,8 +493,8 @@ int cg_stokes_solve_dc(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f,
                 if (nd == 2) {
                     const Fused2D<float>& fk = (it % 2 == 0) ? fa : fb;
                     const int nsm = ctx->num_sms;
-                    const cudaError_t le = last ? launch_march2d<float, true>(fk, s32, g->n[0], g->n[1], nsm, 0, st)
-                                                : launch_march2d<float, false>(fk, s32, g->n[0], g->n[1], nsm, 0, st);
+                    const cudaError_t le = last ? launch_march2d<float, true>(fk, s32, g->n[0], g->n[1], nsm, tc.seg, st)
+                                                : launch_march2d<float, false>(fk, s32, g->n[0], g->n[1], nsm, tc.seg, st);
                     if (le != cudaSuccess) return cg_fail(ctx, CG_ERR_CUDA, "fused2d launch: %s", cudaGetErrorString(le));
                     int r = cg_bc_apply_impl(ctx, g, nd, (it % 2 == 0) ? w.dV2 : w.dV, bc0);
                     if (r) return r;
@@ -498,8 +502,8 @@ int cg_stokes_solve_dc(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f,
                     const Fused3D<float>& fk = (it % 2 == 0) ? ga : gb;
                     const int nsm = ctx->num_sms;
                     const cudaError_t le =
-                        last ? launch_march3d<float, true>(fk, s32, g->n[0], g->n[1], g->n[2], nsm, 0, st)
-                             : launch_march3d<float, false>(fk, s32, g->n[0], g->n[1], g->n[2], nsm, 0, st);
+                        last ? launch_march3d<float, true>(fk, s32, g->n[0], g->n[1], g->n[2], nsm, tc.seg, st, tc.variant)
+                             : launch_march3d<float, false>(fk, s32, g->n[0], g->n[1], g->n[2], nsm, tc.seg, st, tc.variant);
                     if (le != cudaSuccess) return cg_fail(ctx, CG_ERR_CUDA, "fused3d launch: %s", cudaGetErrorString(le));
                     int r = cg_bc_apply_impl(ctx, g, nd, (it % 2 == 0) ? w.dV2 : w.dV, bc0);
                     if (r) return r;
