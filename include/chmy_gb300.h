@@ -98,7 +98,9 @@ CG_API int cg_abi_version(void);
 
 /* Arch(backend; device_id) + activate! (src/Architectures.jl:46-49,71-74): binds the calling
  * thread to `device` (0-based CUDA ordinal; Chmy's device_id is 1-based) and creates a
- * context with its own non-blocking stream. */
+ * context with its own stream. The stream is a blocking one, ordered with work on the legacy
+ * default stream (host-side copies of PyTorch's default stream, for instance); cg_set_stream
+ * replaces it. */
 CG_API int cg_init(int device, cg_ctx** out);
 CG_API int cg_destroy(cg_ctx* ctx);
 /* Message of the last failing call on `ctx` (or of the last cg_init failure if ctx == NULL). */
