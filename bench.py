@@ -301,10 +301,15 @@ def run_ours(args, rank, world, dist):
         iters_all = float(iters)
     bytes_per_iter = A32 * n * n * 4
     value = bytes_per_iter * iters_all / (ms * 1e-3) / 1e9
-    # kernels in the timed solves: per PT iteration the fused kernel and bc!(V); per check bc!(r_V),
-    # the max-norm and (inner checks) the constitutive measure, or (outer checks) the FP64
-    # defect; per correction the FP64 update and bc!(V); one 1/eta conversion per solve
-    launches = sum(2 * r.iterations + 3 * r.checks + 2 * r.outer + 1 for r in results)
+    # kernels in the timed solves: per PT iteration the fused kernel (bc!(V) folded into its
+    # reads; one bc!(V) launch per chunk of ncheck iterations, or one per iteration with
+    # CG_BC_FOLD=0); per check bc!(r_V), the max-norm and (inner checks) the constitutive
+    # measure, or (outer checks) the FP64 defect; per correction the FP64 update and bc!(V);
+    # one 1/eta conversion per solve
+    nchunk = pb.ncheck + (pb.ncheck & 1)
+    fold = os.environ.get("CG_BC_FOLD", "1")[:1] != "0"
+    launches = sum(r.iterations + (r.iterations // nchunk if fold else r.iterations) + 3 * r.checks + 2 * r.outer + 1
+                   for r in results)
 
     # e2e through the public API with host buffers: upload the initial state from pinned host
     # memory, solve, read the velocity and pressure back every step

@@ -8,6 +8,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <utility>
 
 #include "../../include/chmy_gb300.h"
 
@@ -51,6 +52,43 @@ struct cg_tune_cfg {
 bool cg_autotune_enabled();
 bool cg_tune_lookup(const std::string& key, cg_tune_cfg* out);
 void cg_tune_store(const std::string& key, const cg_tune_cfg& cfg);
+
+// Programmatic dependent launch. A kernel launched by cg_launch(..., dep = true) may be
+// scheduled while the kernel before it on the stream is still running; it calls cg_dep_wait()
+// before its first global-memory access, which returns once that kernel has completed and its
+// writes are visible. A kernel that calls cg_dep_wait() runs unchanged when launched the
+// ordinary way (the wait returns at once). cg_dep_release() lets the next dependent launch be
+// scheduled before this grid ends. CG_PDL=0 in the environment turns the overlap off.
+__device__ __forceinline__ void cg_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void cg_dep_release() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+bool cg_pdl_enabled();
+// bc!(V) folded into the velocity reads of the 2D marching kernel (one boundary-condition
+// launch per run of PT iterations); CG_BC_FOLD=0 in the environment launches it every iteration.
+bool cg_bc_fold_enabled();
+
+template <class... P, class... A>
+inline cudaError_t cg_launch(void (*kern)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, bool dep,
+                             A&&... args) {
+    if (!dep || !cg_pdl_enabled()) {
+        kern<<<grid, block, smem, st>>>(std::forward<A>(args)...);
+        return cudaGetLastError();
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, std::forward<A>(args)...);
+}
+
+// bc! over a batch of fields (one launch); dep = true launches it as a dependent launch.
+int cg_bc_apply_impl(cg_ctx* ctx, const cg_grid* grid, int nfields, const cg_field* fields, const cg_bc* bcs,
+                     bool dep = false);
 
 // Record an error message on ctx and return `code`.
 int cg_fail(cg_ctx* ctx, int code, const char* fmt, ...);

@@ -83,6 +83,22 @@ bool cg_autotune_enabled() {
     return on;
 }
 
+bool cg_pdl_enabled() {
+    static const bool on = [] {
+        const char* e = std::getenv("CG_PDL");
+        return !(e && e[0] == '0');
+    }();
+    return on;
+}
+
+bool cg_bc_fold_enabled() {
+    static const bool on = [] {
+        const char* e = std::getenv("CG_BC_FOLD");
+        return !(e && e[0] == '0');
+    }();
+    return on;
+}
+
 bool cg_tune_lookup(const std::string& key, cg_tune_cfg* out) {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune.find(key);
@@ -364,6 +380,8 @@ __device__ inline bool phase_member(const BcField<T>& F, int nd, const int* n, i
 
 template <class T>
 __global__ void bc_apply_kernel(const BcBatch<T> b) {
+    cg_dep_wait();
+    cg_dep_release();
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
     if (tid >= b.total) return;
     int it = 0;
@@ -427,7 +445,7 @@ __global__ void bc_apply_kernel(const BcBatch<T> b) {
 }
 
 template <class T>
-int bc_apply_t(cg_ctx* ctx, const cg_grid* grid, int nfields, const cg_field* fields, const cg_bc* bcs) {
+int bc_apply_t(cg_ctx* ctx, const cg_grid* grid, int nfields, const cg_field* fields, const cg_bc* bcs, bool dep) {
     BcBatch<T> b;
     std::memset(&b, 0, sizeof(b));
     b.nd = grid->ndim;
@@ -470,14 +488,13 @@ int bc_apply_t(cg_ctx* ctx, const cg_grid* grid, int nfields, const cg_field* fi
     b.total = total;
     if (total == 0) return CG_OK;
     const int threads = 256;
-    bc_apply_kernel<T><<<cg_div_up(total, threads), threads, 0, ctx->stream>>>(b);
-    CG_CHECK_LAUNCH(ctx);
+    CG_CUDA(ctx, cg_launch(bc_apply_kernel<T>, dim3(cg_div_up(total, threads)), dim3(threads), 0, ctx->stream, dep, b));
     return CG_OK;
 }
 
 }  // namespace
 
-int cg_bc_apply_impl(cg_ctx* ctx, const cg_grid* grid, int nfields, const cg_field* fields, const cg_bc* bcs) {
+int cg_bc_apply_impl(cg_ctx* ctx, const cg_grid* grid, int nfields, const cg_field* fields, const cg_bc* bcs, bool dep) {
     int rc = cg_check_grid(ctx, grid);
     if (rc) return rc;
     if (nfields < 0 || nfields > kBcMaxFields)
@@ -492,8 +509,8 @@ int cg_bc_apply_impl(cg_ctx* ctx, const cg_grid* grid, int nfields, const cg_fie
         rc = cg_check_field(ctx, grid, fields[i], dtype, -1, "cg_bc_apply field");
         if (rc) return rc;
     }
-    return dtype == CG_F64 ? bc_apply_t<double>(ctx, grid, nfields, fields, bcs)
-                           : bc_apply_t<float>(ctx, grid, nfields, fields, bcs);
+    return dtype == CG_F64 ? bc_apply_t<double>(ctx, grid, nfields, fields, bcs, dep)
+                           : bc_apply_t<float>(ctx, grid, nfields, fields, bcs, dep);
 }
 
 extern "C" int cg_bc_apply(cg_ctx* ctx, const cg_grid* grid, int nfields, const cg_field* fields, const cg_bc* bcs) {

@@ -1,7 +1,6 @@
 // cg_diffusion.cu — explicit linear diffusion (Chmy.jl examples/diffusion_2d.jl:8-19).
 #include "cg_common.cuh"
 
-int cg_bc_apply_impl(cg_ctx* ctx, const cg_grid* grid, int nfields, const cg_field* fields, const cg_bc* bcs);
 
 namespace {
 

@@ -154,6 +154,8 @@ __global__ void __launch_bounds__(32 * NW, MINB)
                    long s1u, long s2u) {
     constexpr unsigned FULL = 0xffffffffu;
     __shared__ M3Smem<T, NW> sm;
+    cg_dep_wait();
+    cg_dep_release();
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int b = blockIdx.x;
     const int strip = b % nstrip, ty = (b / nstrip) % ntile_y, seg = b / (nstrip * ntile_y);
@@ -417,7 +419,7 @@ inline int m3_seg_len(long tiles, int planes, long cap) {
 
 template <class T, class Ix, bool UNI, bool WRITE_RES, int MINB, int NW = kM3Warps, bool PREF = true>
 inline cudaError_t launch_march3d_ix(const Fused3D<T>& f, const SP<T>& s, int n0, int n1, int n2, int num_sms,
-                                     int seg_len, long s1u, long s2u, cudaStream_t st) {
+                                     int seg_len, long s1u, long s2u, cudaStream_t st, bool dep = false) {
     const int e0 = n0 + 1, e1 = n1 + 1, e2 = n2 + 1;
     const int nstrip = cg_div_up(e0 + 1, 30), nty = cg_div_up(e1 + 1, NW - 2);
     const long tiles = (long)nstrip * nty;
@@ -432,33 +434,33 @@ inline cudaError_t launch_march3d_ix(const Fused3D<T>& f, const SP<T>& s, int n0
         seg_len = m3_seg_len(tiles, e2 + 1, (long)num_sms * bps);
     }
     const int nseg = cg_div_up(e2 + 1, seg_len);
-    march3d_kernel<T, Ix, UNI, WRITE_RES, NW, MINB, PREF>
-        <<<(unsigned)(tiles * nseg), 32 * NW, 0, st>>>(f, s, e0, e1, e2, nstrip, nty, seg_len, s1u, s2u);
-    return cudaGetLastError();
+    return cg_launch(march3d_kernel<T, Ix, UNI, WRITE_RES, NW, MINB, PREF>, dim3((unsigned)(tiles * nseg)), dim3(32 * NW),
+                     0, st, dep, f, s, e0, e1, e2, nstrip, nty, seg_len, s1u, s2u);
 }
 
-// Launch of the z-marching kernel over [0, n+1]^3; seg_len <= 0 picks the z-segment length.
+// Launch of the z-marching kernel over [0, n+1]^3; seg_len <= 0 picks the z-segment length;
+// dep = true makes it a dependent launch (cg_launch).
 // For FP32 with shared strides, variant 0 is 12 rows per block at 2 blocks per SM and variant 1
 // is 8 rows per block at 3 blocks per SM (both 80 registers, no spills; the two best measured
 // of 4-16 rows per block and 1-5 blocks per SM at 256^3).
 template <class T, bool WRITE_RES>
 inline cudaError_t launch_march3d(const Fused3D<T>& f, const SP<T>& s, int n0, int n1, int n2, int num_sms, int seg_len,
-                                  cudaStream_t st, int variant = 0) {
+                                  cudaStream_t st, int variant = 0, bool dep = false) {
     long s1 = 0, s2 = 0;
     const bool uni = march3_uniform(f, &s1, &s2);
     if (march3_fits_int(f, n0 + 1, n1 + 1, n2 + 1)) {
         if (uni) {
             if constexpr (sizeof(T) == 4) {
                 if (variant == 1)
-                    return launch_march3d_ix<T, int, true, WRITE_RES, 3, 8>(f, s, n0, n1, n2, num_sms, seg_len, s1, s2, st);
-                return launch_march3d_ix<T, int, true, WRITE_RES, 2, 12>(f, s, n0, n1, n2, num_sms, seg_len, s1, s2, st);
+                    return launch_march3d_ix<T, int, true, WRITE_RES, 3, 8>(f, s, n0, n1, n2, num_sms, seg_len, s1, s2, st, dep);
+                return launch_march3d_ix<T, int, true, WRITE_RES, 2, 12>(f, s, n0, n1, n2, num_sms, seg_len, s1, s2, st, dep);
             }
-            return launch_march3d_ix<T, int, true, WRITE_RES, 1>(f, s, n0, n1, n2, num_sms, seg_len, s1, s2, st);
+            return launch_march3d_ix<T, int, true, WRITE_RES, 1>(f, s, n0, n1, n2, num_sms, seg_len, s1, s2, st, dep);
         }
-        return launch_march3d_ix<T, int, false, WRITE_RES, 1>(f, s, n0, n1, n2, num_sms, seg_len, 0, 0, st);
+        return launch_march3d_ix<T, int, false, WRITE_RES, 1>(f, s, n0, n1, n2, num_sms, seg_len, 0, 0, st, dep);
     }
-    if (uni) return launch_march3d_ix<T, long, true, WRITE_RES, 1>(f, s, n0, n1, n2, num_sms, seg_len, s1, s2, st);
-    return launch_march3d_ix<T, long, false, WRITE_RES, 1>(f, s, n0, n1, n2, num_sms, seg_len, 0, 0, st);
+    if (uni) return launch_march3d_ix<T, long, true, WRITE_RES, 1>(f, s, n0, n1, n2, num_sms, seg_len, s1, s2, st, dep);
+    return launch_march3d_ix<T, long, false, WRITE_RES, 1>(f, s, n0, n1, n2, num_sms, seg_len, 0, 0, st, dep);
 }
 
 // ---- autotuner: the segment length (2D) or segment length and block shape (3D) with the

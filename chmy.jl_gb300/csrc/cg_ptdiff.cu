@@ -2,7 +2,6 @@
 // damped PT iterations; flux in Chmy's ∂k∂ form, src/GridOperators/partial_derivatives.jl:14-21).
 #include "cg_common.cuh"
 
-int cg_bc_apply_impl(cg_ctx* ctx, const cg_grid* grid, int nfields, const cg_field* fields, const cg_bc* bcs);
 
 namespace {
 

@@ -1,7 +1,6 @@
 // cg_sia.cu — shallow-ice flow (Chmy.jl examples/sia.jl:7-16,30-54,71-81).
 #include "cg_common.cuh"
 
-int cg_bc_apply_impl(cg_ctx* ctx, const cg_grid* grid, int nfields, const cg_field* fields, const cg_bc* bcs);
 int cg_maxabs_collect(cg_ctx* ctx, int nfields, const cg_field* fields, double* out, int32_t* nonfinite);
 void* cg_scratch(cg_ctx* ctx, int slot, size_t bytes, int* rc);
 

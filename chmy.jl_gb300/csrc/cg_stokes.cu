@@ -2,7 +2,6 @@
 // (Chmy.jl examples/stokes_2d_inc_ve_T.jl:11-60, examples/stokes_3d_inc_ve_T.jl:11-77).
 #include "cg_common.cuh"
 
-int cg_bc_apply_impl(cg_ctx* ctx, const cg_grid* grid, int nfields, const cg_field* fields, const cg_bc* bcs);
 int cg_maxabs_enqueue(cg_ctx* ctx, int nfields, const cg_field* fields);
 int cg_maxabs_collect(cg_ctx* ctx, int nfields, const cg_field* fields, double* out, int32_t* nonfinite);
 int cg_stokes_solve_dc(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f, const cg_stokes_params* p,
@@ -461,11 +460,11 @@ int pp_iterations_3d(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* a, c
             const Fused3D<T>& fk = (it % 2 == 0) ? fab : fba;
             const int nsm = ctx->num_sms;
             const cudaError_t le = (res && it == niter - 1)
-                                       ? launch_march3d<T, true>(fk, s, g->n[0], g->n[1], g->n[2], nsm, tc.seg, st, tc.variant)
-                                       : launch_march3d<T, false>(fk, s, g->n[0], g->n[1], g->n[2], nsm, tc.seg, st, tc.variant);
+                                       ? launch_march3d<T, true>(fk, s, g->n[0], g->n[1], g->n[2], nsm, tc.seg, st, tc.variant, it > 0)
+                                       : launch_march3d<T, false>(fk, s, g->n[0], g->n[1], g->n[2], nsm, tc.seg, st, tc.variant, it > 0);
             if (le != cudaSuccess) return cg_fail(ctx, CG_ERR_CUDA, "fused3d launch: %s", cudaGetErrorString(le));
             if (bc_V) {
-                int r = cg_bc_apply_impl(ctx, g, 3, (it % 2 == 0) ? b->V : a->V, bc_V);
+                int r = cg_bc_apply_impl(ctx, g, 3, (it % 2 == 0) ? b->V : a->V, bc_V, true);
                 if (r) return r;
             }
         }
@@ -477,7 +476,13 @@ template <class T>
 int pp_iterations_t(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* a, const cg_stokes_fields* b,
                     const cg_stokes_params* p, const cg_bc* bc_V, int niter) {
     if (g->ndim == 3) return pp_iterations_3d<T>(ctx, g, a, b, p, bc_V, niter);
-    const Fused2D<T> fab = fused_view<T>(a, b, a), fba = fused_view<T>(b, a, a);
+    Fused2D<T> fab = fused_view<T>(a, b, a), fba = fused_view<T>(b, a, a);
+    // from the second iteration on, bc!(V) of the previous one is folded into the velocity
+    // reads; one launch at the end patches the outputs of the last two iterations
+    const Fused2D<T> fab0 = fab;
+    VFold<T> vf;
+    const bool fold = cg_bc_fold_enabled() && make_vfold(g, bc_V, &vf);
+    if (fold) fab.bc = fba.bc = vf;
     const SP<T> s = scalars<T>(g, p);
     const bool res = cg_present(a->divV) && cg_present(a->r_V[0]);
     const cg_tune_cfg tc = tune_march2d(fab, s, g->n[0], g->n[1], ctx->num_sms, ctx->stream);
@@ -491,18 +496,25 @@ int pp_iterations_t(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* a, co
     cg_bc none[2];
     std::memset(none, 0, sizeof(none));
     for (int d = 0; d < 2; ++d) cg_key_add(key, bc_V ? bc_V[d] : none[d]);
+    cg_key_add(key, (int)fold);
     return cg_graph_run(ctx, key, [&](cudaStream_t st) {
         for (int it = 0; it < niter; ++it) {
-            const Fused2D<T>& fk = (it % 2 == 0) ? fab : fba;
+            const Fused2D<T>& fk = it == 0 ? fab0 : (it % 2 == 0) ? fab : fba;
             const int nsm = ctx->num_sms;
             const cudaError_t le = (res && it == niter - 1)
-                                       ? launch_march2d<T, true>(fk, s, g->n[0], g->n[1], nsm, tc.seg, st)
-                                       : launch_march2d<T, false>(fk, s, g->n[0], g->n[1], nsm, tc.seg, st);
+                                       ? launch_march2d<T, true>(fk, s, g->n[0], g->n[1], nsm, tc.seg, st, it > 0)
+                                       : launch_march2d<T, false>(fk, s, g->n[0], g->n[1], nsm, tc.seg, st, it > 0);
             if (le != cudaSuccess) return cg_fail(ctx, CG_ERR_CUDA, "fused2d launch: %s", cudaGetErrorString(le));
-            if (bc_V) {
-                int r = cg_bc_apply_impl(ctx, g, 2, (it % 2 == 0) ? b->V : a->V, bc_V);
+            if (bc_V && !fold) {
+                int r = cg_bc_apply_impl(ctx, g, 2, (it % 2 == 0) ? b->V : a->V, bc_V, true);
                 if (r) return r;
             }
+        }
+        if (fold) {
+            const cg_field fl[4] = {b->V[0], b->V[1], a->V[0], a->V[1]};
+            const cg_bc bl[4] = {bc_V[0], bc_V[1], bc_V[0], bc_V[1]};
+            int r = cg_bc_apply_impl(ctx, g, niter > 1 ? 4 : 2, fl, bl, true);
+            if (r) return r;
         }
         return (int)CG_OK;
     });

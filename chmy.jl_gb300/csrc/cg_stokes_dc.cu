@@ -14,7 +14,6 @@
 #include "cg_march3d.cuh"
 #include "cg_stokes_kernels.cuh"
 
-int cg_bc_apply_impl(cg_ctx* ctx, const cg_grid* grid, int nfields, const cg_field* fields, const cg_bc* bcs);
 int cg_maxabs_enqueue(cg_ctx* ctx, int nfields, const cg_field* fields);
 int cg_maxabs_collect(cg_ctx* ctx, int nfields, const cg_field* fields, double* out, int32_t* nonfinite);
 
@@ -482,6 +481,13 @@ int cg_stokes_solve_dc(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f,
     }
     const int nchunk = ncheck + (ncheck & 1);
     cg_key_add(key, nchunk);
+    // 2D: bc!(dV) folded into the velocity reads from the chunk's second iteration on; the
+    // chunk's last output (dV: nchunk is even) is patched once at its end
+    const Fused2D<float> fa0 = fa;
+    VFold<float> vf;
+    const bool fold = nd == 2 && cg_bc_fold_enabled() && make_vfold(g, bc0, &vf);
+    if (fold) fa.bc = fb.bc = vf;
+    cg_key_add(key, (int)fold);
     // launch layout of the fused kernel, timed on the work buffers (A -> B) before capture
     const cg_tune_cfg tc = nd == 2 ? tune_march2d(fa, s32, g->n[0], g->n[1], ctx->num_sms, ctx->stream)
                                    : tune_march3d(ga, s32, g->n[0], g->n[1], g->n[2], ctx->num_sms, ctx->stream);
@@ -491,21 +497,23 @@ int cg_stokes_solve_dc(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f,
             for (int it = 0; it < nchunk; ++it) {
                 const bool last = it == nchunk - 1;
                 if (nd == 2) {
-                    const Fused2D<float>& fk = (it % 2 == 0) ? fa : fb;
+                    const Fused2D<float>& fk = it == 0 ? fa0 : (it % 2 == 0) ? fa : fb;
                     const int nsm = ctx->num_sms;
-                    const cudaError_t le = last ? launch_march2d<float, true>(fk, s32, g->n[0], g->n[1], nsm, tc.seg, st)
-                                                : launch_march2d<float, false>(fk, s32, g->n[0], g->n[1], nsm, tc.seg, st);
+                    const cudaError_t le = last ? launch_march2d<float, true>(fk, s32, g->n[0], g->n[1], nsm, tc.seg, st, it > 0)
+                                                : launch_march2d<float, false>(fk, s32, g->n[0], g->n[1], nsm, tc.seg, st, it > 0);
                     if (le != cudaSuccess) return cg_fail(ctx, CG_ERR_CUDA, "fused2d launch: %s", cudaGetErrorString(le));
-                    int r = cg_bc_apply_impl(ctx, g, nd, (it % 2 == 0) ? w.dV2 : w.dV, bc0);
-                    if (r) return r;
+                    if (!fold || last) {
+                        int r = cg_bc_apply_impl(ctx, g, nd, (it % 2 == 0) ? w.dV2 : w.dV, bc0, true);
+                        if (r) return r;
+                    }
                 } else {
                     const Fused3D<float>& fk = (it % 2 == 0) ? ga : gb;
                     const int nsm = ctx->num_sms;
                     const cudaError_t le =
-                        last ? launch_march3d<float, true>(fk, s32, g->n[0], g->n[1], g->n[2], nsm, tc.seg, st, tc.variant)
-                             : launch_march3d<float, false>(fk, s32, g->n[0], g->n[1], g->n[2], nsm, tc.seg, st, tc.variant);
+                        last ? launch_march3d<float, true>(fk, s32, g->n[0], g->n[1], g->n[2], nsm, tc.seg, st, tc.variant, it > 0)
+                             : launch_march3d<float, false>(fk, s32, g->n[0], g->n[1], g->n[2], nsm, tc.seg, st, tc.variant, it > 0);
                     if (le != cudaSuccess) return cg_fail(ctx, CG_ERR_CUDA, "fused3d launch: %s", cudaGetErrorString(le));
-                    int r = cg_bc_apply_impl(ctx, g, nd, (it % 2 == 0) ? w.dV2 : w.dV, bc0);
+                    int r = cg_bc_apply_impl(ctx, g, nd, (it % 2 == 0) ? w.dV2 : w.dV, bc0, true);
                     if (r) return r;
                 }
             }

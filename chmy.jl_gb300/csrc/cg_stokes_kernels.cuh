@@ -362,6 +362,82 @@ __global__ void thermal_step_kernel(const ThermalStep<T> a, int e0, int e1, int 
     a.Tout(i, j, k) = rsub(a.Told(i, j, k), rmul(a.dt, dq));
 }
 
+// ---- bc!(V) folded into the velocity reads of the marching kernels -------------------------
+//
+// A PT iteration ends with bc!(V) (examples/stokes_2d_inc_ve_T.jl:81-89): its boundary planes
+// are functions of the interior the iteration just wrote. The marching kernel can instead read
+// the unpatched velocity of the previous iteration and apply the same rules to each value it
+// uses, which leaves one boundary-condition launch at the end of a run of iterations instead
+// of one per iteration. The rules are those of cg_bc_apply for Dirichlet and Neumann kinds
+// (Chmy's FirstOrderBC): per velocity component a, dimension d and side s, the planes g (an
+// index along d) become a constant (Dirichlet on a Vertex dimension), 2 v - F[src]
+// (Dirichlet on a Center dimension) or F[src] -/+ h v (Neumann), applied over the tangential
+// range 0..n+2, dimension y (then z in 3D) before x, side 0 before side 1, with the same
+// fused multiply-adds, so the folded value equals the patched one bit for bit. Periodic
+// kinds are not folded. A value the later phase reads (a corner) is the earlier phase's
+// result, exactly as in the chain the boundary-condition kernel walks.
+enum { FOLD_NONE = 0, FOLD_CONST = 1, FOLD_DIRC = 2, FOLD_NEU = 3 };
+
+template <class T>
+struct VFold {
+    int on;
+    signed char rule[3][3][2];  // [component][dimension][side]
+    int g[3][3][2], src[3][3][2];
+    T val[3][3][2];             // Dirichlet value; Neumann: -v on side 0, +v on side 1
+    T h[3];
+    int lim[3];                 // tangential range 0..n+2 of each dimension
+};
+
+template <class T>
+__device__ __forceinline__ T fold_rule(int r, T base, T v, T h) {
+    return r == FOLD_DIRC ? rfma(T(2), rsub(v, base), base) : rfma(h, v, base);
+}
+
+// The rules of cg_bc_apply for velocity component a (Vertex along a, Center along the others)
+// of a grid with n[d] cells. Returns false when a kind cannot be folded (periodic).
+template <class T>
+inline bool make_vfold(const cg_grid* g, const cg_bc* bc_V, VFold<T>* out) {
+    std::memset(out, 0, sizeof(*out));
+    if (!bc_V) return false;
+    const int nd = g->ndim;
+    for (int d = 0; d < nd; ++d) {
+        out->h[d] = (T)g->spacing[d];
+        out->lim[d] = g->n[d] + 2;
+    }
+    for (int a = 0; a < nd; ++a)
+        for (int d = 0; d < nd; ++d) {
+            const bool vtx = d == a;
+            const int ext = vtx ? g->n[d] + 1 : g->n[d];
+            for (int s = 0; s < 2; ++s) {
+                const T v = (T)bc_V[a].value[d][s];
+                signed char& r = out->rule[a][d][s];
+                switch (bc_V[a].kind[d][s]) {
+                    case CG_BC_NONE: r = FOLD_NONE; break;
+                    case CG_BC_DIRICHLET:
+                        if (vtx) {
+                            r = FOLD_CONST;
+                            out->g[a][d][s] = s ? ext : 1;
+                        } else {
+                            r = FOLD_DIRC;
+                            out->g[a][d][s] = s ? ext + 1 : 0;
+                            out->src[a][d][s] = s ? ext : 1;
+                        }
+                        out->val[a][d][s] = v;
+                        break;
+                    case CG_BC_NEUMANN:
+                        r = FOLD_NEU;
+                        out->g[a][d][s] = s ? ext + 1 : 0;
+                        out->src[a][d][s] = s ? ext : 1;
+                        out->val[a][d][s] = s ? v : -v;
+                        break;
+                    default: return false;
+                }
+            }
+        }
+    out->on = 1;
+    return true;
+}
+
 // ---- fused 2D PT iteration (variable viscosity): update_stress! + update_velocity! -----------
 //
 // One launch per PT iteration, reading the `in` buffers and writing the `out` buffers
@@ -373,6 +449,7 @@ struct Fused2D {
     DF<T> txx_in, tyy_in, txy_in, txx_out, tyy_out, txy_out, P_in, P_out;
     DF<T> txx_o, tyy_o, txy_o, ieta, fP, rhox, rhoy, divV, rVx, rVy;
     int has_fP, has_rho;
+    VFold<T> bc;  // bc.on: the V_in values are read through bc!(V)
 };
 
 // ---- warp-marching fused 2D PT iteration --------------------------------------------------
@@ -431,6 +508,46 @@ __device__ __forceinline__ MarchRow<T> march_load(const Fused2D<T>& f, const MAt
     return r;
 }
 
+// Velocity component a at column i, row j of a marching warp, read through bc!(V), in two
+// steps. fold_y (rows; the caller tests that row j can hold a y-plane, uniformly in the warp):
+// v is the stored value, vprev the folded value of row j-1 and vnext the stored value of row
+// j+1. A y-plane's source row is always the adjacent one (row 0 from row 1, row n+1 from n,
+// row n+2 from n+1; rows 1 and n+1 of a Vertex dimension are constants) and never a y-plane
+// itself. The previous row's folded value equals its stored one except in an x-plane column,
+// where fold_x overrides the y result anyway.
+template <class T>
+__device__ __forceinline__ T fold_y(const VFold<T>& b, int a, int i, int j, T v, T vprev, T vnext) {
+    if (i >= 0 && i <= b.lim[0]) {
+        const int r0 = b.rule[a][1][0], r1 = b.rule[a][1][1];
+        if (r0 != FOLD_NONE && j == b.g[a][1][0])
+            v = r0 == FOLD_CONST ? b.val[a][1][0] : fold_rule(r0, vnext, b.val[a][1][0], b.h[1]);
+        if (r1 != FOLD_NONE && j == b.g[a][1][1])
+            v = r1 == FOLD_CONST ? b.val[a][1][1] : fold_rule(r1, vprev, b.val[a][1][1], b.h[1]);
+    }
+    return v;
+}
+
+// fold_x (columns; called by the whole warp when its strip holds an x-plane, for a row in the
+// tangential range 0..n+2): an x-plane takes its neighbour lane's y-folded value. Lanes 0 and
+// 31 are halos: a left plane (column 0 or 1) sits at lane >= 1 with its source one lane up, a
+// right plane (column n+1 or n+2) at lane >= 1 of any strip that owns a column, its source one
+// lane down.
+template <class T>
+__device__ __forceinline__ T fold_x(const VFold<T>& b, int a, int i, T v) {
+    constexpr unsigned FULL = 0xffffffffu;
+    const int r0 = b.rule[a][0][0], r1 = b.rule[a][0][1];
+    T vr = v, vl = v;
+    if (r0 > FOLD_CONST || r1 > FOLD_CONST) {  // a rule with a source: the neighbours' values
+        vr = __shfl_down_sync(FULL, v, 1);
+        vl = __shfl_up_sync(FULL, v, 1);
+    }
+    if (r0 != FOLD_NONE && i == b.g[a][0][0])
+        v = r0 == FOLD_CONST ? b.val[a][0][0] : fold_rule(r0, vr, b.val[a][0][0], b.h[0]);
+    if (r1 != FOLD_NONE && i == b.g[a][0][1])
+        v = r1 == FOLD_CONST ? b.val[a][0][1] : fold_rule(r1, vl, b.val[a][0][1], b.h[0]);
+    return v;
+}
+
 // -(t - t_old) * inv_Gdt - t * ieta + 2 * e: the VE stress residual, left to right.
 template <class T>
 __device__ __forceinline__ T stress_res(const SP<T>& s, T t, T to, T ie, T e) {
@@ -479,6 +596,8 @@ template <class T, class Ix, bool UNI, bool WRITE_RES, int MINB = 1>
 __global__ void __launch_bounds__(128, MINB) march2d_kernel(const Fused2D<T> f, const SP<T> s, int e0, int e1,
                                                             int nstrip, int nwarps, int seg_rows, long s1u) {
     constexpr unsigned FULL = 0xffffffffu;
+    cg_dep_wait();
+    cg_dep_release();
     const int lane = threadIdx.x & 31;
     const int gw = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     if (gw >= nwarps) return;  // whole warp
@@ -492,13 +611,21 @@ __global__ void __launch_bounds__(128, MINB) march2d_kernel(const Fused2D<T> f, 
     const bool inV = i <= e0 + 1;  // V, 1/eta, tau_xy readable
     const bool inC = i <= e0;      // cell inputs, tau_xy_old readable
     const bool oldcell = i < 0;    // column -1 keeps its old cell values
+    // bc!(V) folded into the reads: the strip holds an x-plane (columns 0, 1, n+1, n+2) / the
+    // rows js-1 .. je+1 hold a y-plane (rows 0, 1, n+1, n+2)
+    const bool xb = f.bc.on && (strip == 0 || strip * 30 + 30 >= e0);
+    const bool ylow = js <= 2, yhigh = je + 2 >= e1;
+    const bool yb = f.bc.on && (ylow || yhigh);
+    // rows ylo..yhi of the marching steps can hold a y-plane (0..1, n+1..n+2, or all)
+    const int ylo = ylow ? 0 : e1, yhi = yhigh ? e1 + 1 : 1;
 
     // ---- prologue: new cell row js-1 (P and tau_yy only) and new vertex row js ----
     T Vx_c, Vy_c, ie_c, ieL_c, ie_p, Pn_p, Tyyn_p, txy_c;
+    MarchRow<T> cur;
     {
         const int jp = js - 1;  // >= -1
-        const T vxp = at.ld(f.Vx_in, jp, inV);
-        const T vyp = at.ld(f.Vy_in, jp, inV);
+        T vxp = at.ld(f.Vx_in, jp, inV);
+        T vyp = at.ld(f.Vy_in, jp, inV);
         const T iep = at.ld(f.ieta, jp, inV);
         const T pp = at.ld(f.P_in, jp, inC);
         const T typ = at.ld(f.tyy_in, jp, inC);
@@ -509,6 +636,25 @@ __global__ void __launch_bounds__(128, MINB) march2d_kernel(const Fused2D<T> f, 
         ie_c = at.ld(f.ieta, js, inV);
         const T t2 = at.ld(f.txy_in, js, inV);
         const T o2 = at.ld(f.txy_o, js, inC);
+        // the first marching step's loads (row js+1) are issued before the prologue computes
+        cur = march_load(f, at, js, e1, inV, inC);
+        if (yb) {
+            // row js+1 is the source of a plane at row js = 0; row js-1 can be no side-1 plane
+            vxp = fold_y(f.bc, 0, i, jp, vxp, T(0), Vx_c);
+            vyp = fold_y(f.bc, 1, i, jp, vyp, T(0), Vy_c);
+        }
+        if (xb && jp >= 0) {
+            vxp = fold_x(f.bc, 0, i, vxp);
+            vyp = fold_x(f.bc, 1, i, vyp);
+        }
+        if (yb) {
+            Vx_c = fold_y(f.bc, 0, i, js, Vx_c, vxp, cur.Vx);
+            Vy_c = fold_y(f.bc, 1, i, js, Vy_c, vyp, cur.Vy);
+        }
+        if (xb) {
+            Vx_c = fold_x(f.bc, 0, i, Vx_c);
+            Vy_c = fold_x(f.bc, 1, i, Vy_c);
+        }
         // cell (i, js-1); row -1 and column -1 keep their old values
         const T vxpR = __shfl_down_sync(FULL, vxp, 1);
         const CellNew<T> cp = march_cell(s, f.has_fP != 0, vxp, vxpR, vyp, Vy_c, iep, pp, T(0), T(0), typ, tyop, fpp);
@@ -525,10 +671,18 @@ __global__ void __launch_bounds__(128, MINB) march2d_kernel(const Fused2D<T> f, 
     }
 
     // the next row's loads are issued before the current row is computed
-    MarchRow<T> cur = march_load(f, at, js, e1, inV, inC);
     for (int j = js; j <= je; ++j) {
         MarchRow<T> nxt;
         if (j < je) nxt = march_load(f, at, j + 1, e1, inV, inC);
+        // row j+1 in 1..n+2: a side-0 y-plane there is a constant (row 1 of a Vertex dimension)
+        if (yb && j + 1 >= ylo && j + 1 <= yhi) {
+            cur.Vx = fold_y(f.bc, 0, i, j + 1, cur.Vx, Vx_c, T(0));
+            cur.Vy = fold_y(f.bc, 1, i, j + 1, cur.Vy, Vy_c, T(0));
+        }
+        if (xb) {
+            cur.Vx = fold_x(f.bc, 0, i, cur.Vx);
+            cur.Vy = fold_x(f.bc, 1, i, cur.Vy);
+        }
         // new cell (i, j)
         const T vxR = __shfl_down_sync(FULL, Vx_c, 1);
         CellNew<T> c = march_cell(s, f.has_fP != 0, Vx_c, vxR, Vy_c, cur.Vy, ie_c, cur.P, cur.txx, cur.txo, cur.tyy,
@@ -640,31 +794,30 @@ inline int march_seg_rows(int num_sms, int nstrip, int rows) {
 
 template <class T, class Ix, bool UNI, bool WRITE_RES, int MINB = 1>
 inline cudaError_t launch_march2d_ix(const Fused2D<T>& f, const SP<T>& s, int n0, int n1, int num_sms, int seg_rows,
-                                     long s1u, cudaStream_t st) {
+                                     long s1u, cudaStream_t st, bool dep = false) {
     const int e0 = n0 + 1, e1 = n1 + 1;
     const int nstrip = cg_div_up(e0 + 1, 30);
     if (seg_rows <= 0) seg_rows = march_seg_rows<T, Ix, UNI, WRITE_RES, MINB>(num_sms, nstrip, e1 + 1);
     const int nseg = cg_div_up(e1 + 1, seg_rows);
     const int nwarps = nstrip * nseg;
-    march2d_kernel<T, Ix, UNI, WRITE_RES, MINB>
-        <<<cg_div_up(nwarps, 4), 128, 0, st>>>(f, s, e0, e1, nstrip, nwarps, seg_rows, s1u);
-    return cudaGetLastError();
+    return cg_launch(march2d_kernel<T, Ix, UNI, WRITE_RES, MINB>, dim3(cg_div_up(nwarps, 4)), dim3(128), 0, st, dep, f,
+                     s, e0, e1, nstrip, nwarps, seg_rows, s1u);
 }
 
 // Launch of the warp-marching kernel over [0, n0+1] x [0, n1+1]; seg_rows <= 0 picks the
-// segment length from the occupancy.
+// segment length from the occupancy; dep = true makes it a dependent launch (cg_launch).
 template <class T, bool WRITE_RES>
 inline cudaError_t launch_march2d(const Fused2D<T>& f, const SP<T>& s, int n0, int n1, int num_sms, int seg_rows,
-                                  cudaStream_t st) {
+                                  cudaStream_t st, bool dep = false) {
     const long s1u = march_uniform_stride(f);
     // FP32 with one shared stride fits in 64 registers without spills: 8 blocks (32 warps) per SM
     constexpr int minb = sizeof(T) == 4 ? 8 : 1;
     if (march_fits_int(f, n0 + 1, n1 + 1)) {
-        if (s1u) return launch_march2d_ix<T, int, true, WRITE_RES, minb>(f, s, n0, n1, num_sms, seg_rows, s1u, st);
-        return launch_march2d_ix<T, int, false, WRITE_RES>(f, s, n0, n1, num_sms, seg_rows, 0, st);
+        if (s1u) return launch_march2d_ix<T, int, true, WRITE_RES, minb>(f, s, n0, n1, num_sms, seg_rows, s1u, st, dep);
+        return launch_march2d_ix<T, int, false, WRITE_RES>(f, s, n0, n1, num_sms, seg_rows, 0, st, dep);
     }
-    if (s1u) return launch_march2d_ix<T, long, true, WRITE_RES>(f, s, n0, n1, num_sms, seg_rows, s1u, st);
-    return launch_march2d_ix<T, long, false, WRITE_RES>(f, s, n0, n1, num_sms, seg_rows, 0, st);
+    if (s1u) return launch_march2d_ix<T, long, true, WRITE_RES>(f, s, n0, n1, num_sms, seg_rows, s1u, st, dep);
+    return launch_march2d_ix<T, long, false, WRITE_RES>(f, s, n0, n1, num_sms, seg_rows, 0, st, dep);
 }
 
 }  // namespace cgk

@@ -169,12 +169,11 @@ def test_pt_iterations_graph(arch, T, dims, var_eta):
         assert abs(err[i] - want[i]) <= rtol_for(T) * niter * 10 * max(abs(want[i]), 1.0)
 
 
-@pytest.mark.parametrize("T", TYPES)
-@pytest.mark.parametrize("dims", [(45, 38), (70, 33), (33, 97), (257, 300), (13, 12, 11), (31, 20, 70), (61, 7, 33)])
-def test_fused_pingpong_iterations(arch, T, dims):
-    """cg_stokes_pt_iterations_pp (one fused launch per iteration, ping-pong buffers) ==
-    niter x (update_stress!, update_velocity!, bc!(V)) on the oracle, bit for bit."""
-    s = StokesSet(arch, dims, T, 31, True, rho=True)
+def _pp_run(arch, T, dims, bcs, niter, seed=31):
+    """niter fused ping-pong iterations (cg_stokes_pt_iterations_pp) against niter x
+    (update_stress!, update_velocity!, bc!(V)) on the oracle. Returns the set, the partner
+    buffers and the oracle's V after niter - 1 iterations."""
+    s = StokesSet(arch, dims, T, seed, True, rho=True)
     g2 = s.grid
     rho_full = [random_field(g2, f.loc, T, np.random.default_rng(5)) for f in vec_fields(g2, T)]
     s.h["rho_g"] = rho_full
@@ -185,7 +184,6 @@ def test_fused_pingpong_iterations(arch, T, dims):
     s.d["inv_eta"] = to_gpu(arch, ie)
     p = pt_params(g2, True)
     g = g2.desc()
-    bcs = _bc_V(len(dims))
     bc_apply(g2, s.h["V"], bcs)
     for f, d in zip(s.h["V"], s.d["V"]):
         d.from_numpy(f.a)
@@ -195,14 +193,25 @@ def test_fused_pingpong_iterations(arch, T, dims):
     from _oracle import stokes_desc as sd
 
     db = sd(V=partner["V"], P=partner["P"], tau=partner["tau"])
-    niter = 6
-    for _ in range(niter):
+    prev = None
+    for it in range(niter):
+        if it == niter - 1:
+            prev = [f.a.copy() for f in s.h["V"]]
         lib().or_stokes_update_stress(ctypes.byref(g), ctypes.byref(hd), ctypes.byref(p))
         lib().or_stokes_update_velocity(ctypes.byref(g), ctypes.byref(hd), ctypes.byref(p))
         bc_apply(g2, s.h["V"], bcs)
     barr = (_abi.cg_bc * 3)(*bcs)
     arch.call("cg_stokes_pt_iterations_pp", ctypes.byref(g), ctypes.byref(da), ctypes.byref(db), ctypes.byref(p), barr, niter)
     arch.synchronize()
+    return s, partner, prev, (g, da, db, p, barr)
+
+
+@pytest.mark.parametrize("T", TYPES)
+@pytest.mark.parametrize("dims", [(45, 38), (70, 33), (33, 97), (257, 300), (13, 12, 11), (31, 20, 70), (61, 7, 33)])
+def test_fused_pingpong_iterations(arch, T, dims):
+    """cg_stokes_pt_iterations_pp (one fused launch per iteration, ping-pong buffers) ==
+    niter x (update_stress!, update_velocity!, bc!(V)) on the oracle, bit for bit."""
+    s, _, _, (g, da, db, p, barr) = _pp_run(arch, T, dims, _bc_V(len(dims)), 6)
     for name in ("V", "P", "tau", "divV", "r_V"):
         hv = s.h[name] if isinstance(s.h[name], list) else [s.h[name]]
         dv = s.d[name] if isinstance(s.d[name], list) else [s.d[name]]
@@ -213,6 +222,40 @@ def test_fused_pingpong_iterations(arch, T, dims):
     # odd niter is rejected
     rc = arch.lib.cg_stokes_pt_iterations_pp(arch.ctx, ctypes.byref(g), ctypes.byref(da), ctypes.byref(db), ctypes.byref(p), barr, 3)
     assert rc == _abi.CG_ERR_ARG
+
+
+def _bc_mix(kind):
+    """Velocity boundary conditions with every foldable rule: Dirichlet on a Vertex dimension
+    (a constant plane), Dirichlet on a Center dimension (2v - interior), Neumann on either,
+    and sides left untouched."""
+    if kind == "neumann_vertex":
+        return [to_cg_bc(2, {"x": (Neumann(0.3), Neumann(-0.2)), "y": (Dirichlet(0.7), Dirichlet(-0.1))}),
+                to_cg_bc(2, {"x": (Dirichlet(0.25), Dirichlet(0.5)), "y": (Neumann(-0.4), Neumann(0.6))})]
+    if kind == "one_sided":
+        return [to_cg_bc(2, {"x": (Dirichlet(0.2), None), "y": (None, Neumann(0.4))}),
+                to_cg_bc(2, {"x": (None, Neumann(-0.3)), "y": (Dirichlet(0.1), None)})]
+    return [to_cg_bc(2, {"x": (Neumann(0.1), Dirichlet(-0.6)), "y": Neumann(0.2)}),
+            to_cg_bc(2, {"x": Dirichlet(0.3), "y": (Dirichlet(0.9), Neumann(0.05))})]
+
+
+@pytest.mark.parametrize("T", TYPES)
+@pytest.mark.parametrize("kind", ["neumann_vertex", "one_sided", "mixed"])
+@pytest.mark.parametrize("dims", [(28, 29), (29, 30), (30, 28), (58, 33), (59, 7), (60, 61), (2, 3)])
+@pytest.mark.parametrize("niter", [2, 6])
+def test_fused_pingpong_boundary_rules(arch, T, kind, dims, niter):
+    """The fused iterations read the previous iteration's velocity through bc!(V) and patch the
+    boundary planes once at the end: both ping-pong buffers equal the oracle's states after
+    niter and niter - 1 iterations bit for bit, for every Dirichlet/Neumann rule and for grids
+    whose boundary planes fall on the edges of the kernel's 30-column strips."""
+    s, partner, prev, _ = _pp_run(arch, T, dims, _bc_mix(kind), niter, seed=37)
+    for name in ("V", "P", "tau"):
+        hv = s.h[name] if isinstance(s.h[name], list) else [s.h[name]]
+        dv = s.d[name] if isinstance(s.d[name], list) else [s.d[name]]
+        for a, b in zip(dv, hv):
+            assert_close(a, b, 0.0, f"pp {kind} {name}", exact=True)
+    for a, b in zip(partner["V"], prev):
+        got = a.to_numpy()
+        assert np.array_equal(got.view(np.uint8), b.view(np.uint8)), f"partner V {kind}: max diff {np.max(np.abs(got - b))}"
 
 
 def _thermal_set(arch, dims, T, seed):
