@@ -403,6 +403,8 @@ def run_ours(args, rank, world, dist):
         del keep3, d3a, d3b
         torch.cuda.empty_cache()
 
+    suite = None if args.skip_suite else config_suite(arch, stream, peak)
+
     # plain FP64 GPU solve of the same problem, once (time_to_solution comparison)
     fp64 = None
     if not args.skip_fp64:
@@ -461,6 +463,7 @@ def run_ours(args, rank, world, dist):
                 "algorithmic_bytes_per_launch": fused_bytes,
             },
             "stokes3d": stokes3d,
+            "configs": suite,
             "cpu_baseline": {
                 "value": cpu_teff,
                 "unit": "GB/s",
@@ -473,6 +476,136 @@ def run_ours(args, rank, world, dist):
         }
         print(json.dumps(line), flush=True)
     arch.close()
+
+
+def _timed(fn, stream, reps=1):
+    """CUDA-event time (ms) of `reps` calls of fn on `stream`, after one untimed call (which
+    captures the call's CUDA graph)."""
+    import torch
+
+    fn()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(reps):
+        fn()
+    b.record(stream)
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / reps
+
+
+def config_suite(arch, stream, peak):
+    """The other configurations' hot loops, each timed with CUDA events on synthetic inputs of
+    the configuration's shape: explicit diffusion 1024^2 (2000 steps), PT variable diffusion
+    512^3 (a bounded sample of PT iterations, FP64 and FP32) and the SIA ensemble (64 members,
+    1000 steps). T_eff counts the minimum unique traffic of one unit (step or PT iteration)."""
+    import torch
+
+    from chmy_gb300 import Field, _abi
+    from chmy_gb300.bcs import Dirichlet, Neumann, to_cg_bc
+    from chmy_gb300.configs import padded_mesh, ptdiff_params, sia_ensemble
+    from chmy_gb300.grids import Center, UniformGrid, Vertex
+
+    out = {}
+    Cl, Vl = Center(), Vertex()
+
+    # config 1: 2D explicit diffusion, FP64, 1024^2 over [-1, 1]^2, D = 1, dt = h^2/(4.1 D)
+    n1 = 1024
+    g1 = UniformGrid(origin=(-1.0, -1.0), extent=(2.0, 2.0), dims=(n1, n1), dtype=np.float64)
+    x, y = padded_mesh(g1, Cl)
+    C0 = np.exp(-(x * x + y * y) / 0.02) + np.random.default_rng(1).uniform(0.0, 1e-3, x.shape)
+    A, B = Field(arch, g1, Cl, np.float64), Field(arch, g1, Cl, np.float64)
+    A.from_numpy(C0)
+    B.from_numpy(C0)
+    bc1 = to_cg_bc(2, Neumann())
+    h = float(g1.spacing()[0])
+    dt1, steps1 = h * h / 4.1, 2000
+    gd1 = g1.desc()
+    ms1 = _timed(lambda: arch.call("cg_diffusion_run", ctypes.byref(gd1), ctypes.byref(A.desc()), ctypes.byref(B.desc()),
+                                   1.0, dt1, ctypes.byref(bc1), steps1), stream)
+    cells1 = n1 * n1
+    out["diffusion2d"] = {
+        "workload": "2D explicit diffusion 1024^2, FP64, Neumann, 2000 steps (fused flux + update + bc!, one launch per step)",
+        "ms_per_run": ms1,
+        "us_per_step": 1e3 * ms1 / steps1,
+        "t_eff_gbs": 2 * cells1 * 8 * steps1 / (ms1 * 1e-3) / 1e9,
+        "t_eff_gbs_7_arrays": 7 * cells1 * 8 * steps1 / (ms1 * 1e-3) / 1e9,
+        "bytes": "2 arrays x n^2 x 8 B per step (read C, write C'); the reference's 7-array convention beside it",
+        "l2": "L2-resident (2 x 8.4 MB): HBM fraction not meaningful",
+    }
+    del A, B
+
+    # config 2: 3D PT variable diffusion at 512^3, a sample of PT iterations of one step
+    n2, npt = 512, 100
+    g2 = UniformGrid(origin=(-0.5,) * 3, extent=(1.0,) * 3, dims=(n2,) * 3, dtype=np.float64)
+    rng = np.random.default_rng(2)
+    gn = rng.standard_normal((n2 + 4,) * 3, dtype=np.float32)
+    for _ in range(5):
+        for ax in range(3):
+            gn = (np.roll(gn, 1, ax) + gn + np.roll(gn, -1, ax)) / np.float32(3)
+    D = np.exp(gn)
+    del gn
+    xs = padded_mesh(g2, Cl)
+    Cb = np.exp(-(xs[0] * xs[0] + xs[1] * xs[1] + xs[2] * xs[2]) / 0.01)
+    del xs
+    bc2 = to_cg_bc(3, {"x": Dirichlet(0.0), "y": Neumann(), "z": Neumann()})
+    p2 = ptdiff_params(g2, 1e-3, float(D.max()))
+    gd2 = g2.desc()
+    cfg2 = {}
+    for T, name in ((np.float64, "fp64"), (np.float32, "fp32")):
+        fs = {k: Field(arch, g2, Cl, T) for k in ("C", "C_old", "D")}
+        q = [Field(arch, g2, tuple(Vl if e == d else Cl for e in range(3)), T) for d in range(3)]
+        fs["C"].from_numpy(Cb.astype(T))
+        fs["D"].from_numpy(D.astype(T))
+        f = _abi.cg_ptdiff_fields()
+        f.C, f.C_old, f.D = fs["C"].desc(), fs["C_old"].desc(), fs["D"].desc()
+        f.q = (_abi.cg_field * 3)(*[qq.desc() for qq in q])
+        ms2 = _timed(lambda: arch.call("cg_ptdiff_run", ctypes.byref(gd2), ctypes.byref(f), ctypes.byref(p2), ctypes.byref(bc2), 1, npt),
+                     stream)
+        sz = np.dtype(T).itemsize
+        teff = 10 * n2**3 * sz * npt / (ms2 * 1e-3) / 1e9
+        cfg2[name] = {"ms_per_iteration": ms2 / npt, "t_eff_gbs": teff, "frac": teff / peak}
+        del fs, q, f
+        torch.cuda.empty_cache()
+    del D, Cb
+    out["ptdiff3d"] = {
+        "workload": f"3D PT variable diffusion 512^3, D = exp(box-smoothed Gaussian noise), Dirichlet x / Neumann y z; one step of {npt} PT iterations",
+        "bytes": "10 arrays x n^3 x sizeof(T) per PT iteration (read/write C, q x3; read C_old, D)",
+        **cfg2,
+    }
+
+    # config 5: SIA ensemble, 64 members of 128^2..1024^2, FP64, 1000 steps in one batched run
+    ens = sia_ensemble(members=64)
+    keep, mem = [], (_abi.cg_sia_member * len(ens))()
+    params = (_abi.cg_sia_params * len(ens))()
+    cells5 = 0
+    for k, (grid, hh, p) in enumerate(ens):
+        H = Field(arch, grid, Cl, np.float64)
+        Bf = Field(arch, grid, Cl, np.float64)
+        H.from_numpy(hh["H"])
+        Bf.from_numpy(hh["B"])
+        qq = [Field(arch, grid, (Vl, Cl), np.float64), Field(arch, grid, (Cl, Vl), np.float64)]
+        keep.append((H, Bf, qq))
+        mem[k].grid = grid.desc()
+        mem[k].H, mem[k].B = H.desc(), Bf.desc()
+        mem[k].q[0], mem[k].q[1] = qq[0].desc(), qq[1].desc()
+        params[k] = p
+        cells5 += grid.dims[0] * grid.dims[1]
+    ts = (ctypes.c_double * len(ens))()
+    steps5 = 1000
+    ms5 = _timed(lambda: arch.call("cg_sia_ensemble_run", len(ens), mem, params, steps5, ts), stream)
+    teff5 = 3 * cells5 * 8 * steps5 / (ms5 * 1e-3) / 1e9
+    out["sia_ensemble"] = {
+        "workload": "SIA ensemble: 64 members of 128^2..1024^2 (seed 6), flux -Gamma H^5 |grad S|^2 grad S, ELA mass balance, FP64, 1000 steps, one batched run",
+        "cells": cells5,
+        "ms_per_run": ms5,
+        "t_eff_gbs": teff5,
+        "frac": teff5 / peak,
+        "bytes": "3 arrays x cells x 8 B per step (read H, B; write H')",
+    }
+    del keep
+    torch.cuda.empty_cache()
+    return out
 
 
 def fused_kernel_fields(arch, pb):
@@ -584,9 +717,20 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--skip-fp64", action="store_true", help="skip the one-off plain FP64 GPU solve")
     ap.add_argument("--skip-3d", action="store_true", help="skip the 3D fused-kernel measurement")
+    ap.add_argument("--skip-suite", action="store_true", help="skip the other configurations' measurements")
+    ap.add_argument("--suite-only", action="store_true", help="print only the other configurations' measurements")
     args = ap.parse_args()
     if args.kernel:
         run_kernel(args)
+        return
+    if args.suite_only:
+        from chmy_gb300 import Arch, GB300Backend
+
+        import torch
+
+        arch = Arch(GB300Backend(), device_id=1)
+        print(json.dumps({"configs": config_suite(arch, torch.cuda.current_stream(), measured_peaks()[0])}), flush=True)
+        arch.close()
         return
     world = _env_int("WORLD_SIZE", 1)
     rank = _env_int("RANK", 0)

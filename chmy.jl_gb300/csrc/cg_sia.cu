@@ -1,5 +1,6 @@
 // cg_sia.cu — shallow-ice flow (Chmy.jl examples/sia.jl:7-16,30-54,71-81).
 #include "cg_common.cuh"
+#include "cg_sia_kernels.cuh"
 
 int cg_maxabs_collect(cg_ctx* ctx, int nfields, const cg_field* fields, double* out, int32_t* nonfinite);
 void* cg_scratch(cg_ctx* ctx, int slot, size_t bytes, int* rc);
@@ -13,14 +14,6 @@ struct SiaV {
     T idx, idy;
     int n;
 };
-
-template <class T>
-__device__ __forceinline__ T ipow(T x, int m) {
-    if (m <= 0) return T(1);
-    T r = x;
-    for (int k = 1; k < m; ++k) r = r * x;
-    return r;
-}
 
 template <class T>
 __device__ __forceinline__ T S_at(const SiaV<T>& v, int i, int j) {
@@ -37,13 +30,10 @@ __device__ __forceinline__ T D_at(const SiaV<T>& v, int i, int j) {
     const T b1 = (S_at(v, i, j + 1) - s) * v.idy;
     const T ax = fma(T(0.5), a1 - a0, a0);
     const T ay = fma(T(0.5), b1 - b0, b0);
-    const T vm = sqrt(ax * ax + ay * ay);
-    const T h = v.H(i, j, 0);
-    return (v.Gamma * ipow(h, v.n + 2) + v.As * ipow(h, v.n)) * ipow(vm, v.n - 1);
+    return cgsia::D_cell(v.H(i, j, 0), ax, ay, v.Gamma, v.As, v.n);
 }
 
-__device__ __forceinline__ unsigned long long bits_of(double d) { return (unsigned long long)__double_as_longlong(d); }
-__device__ __forceinline__ unsigned long long bits_of(float f) { return (unsigned long long)(unsigned)__float_as_int(f); }
+using cgsia::bits_of;
 
 // update_q! over [1, n]^2 with D evaluated on the fly (the reference's FunctionField);
 // optional max(interior D) into *dmax_bits (D >= 0, so the bit patterns order like values).
@@ -51,14 +41,18 @@ template <class T>
 __global__ void sia_q_kernel(const SiaV<T> v, int nx, int ny, unsigned long long* dmax_bits) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
-    if (i > nx || j > ny) return;
-    const T dc = D_at(v, i, j), dl = D_at(v, i - 1, j), dd = D_at(v, i, j - 1);
-    const T Dx = fma(T(0.5), dc - dl, dl);
-    const T Dy = fma(T(0.5), dc - dd, dd);
-    const T sc = S_at(v, i, j);
-    v.qx(i, j, 0) = -Dx * ((sc - S_at(v, i - 1, j)) * v.idx);
-    v.qy(i, j, 0) = -Dy * ((sc - S_at(v, i, j - 1)) * v.idy);
-    if (dmax_bits) atomicMax(dmax_bits, bits_of(dc));
+    const bool in = i <= nx && j <= ny;
+    T dc = T(0);
+    if (in) {
+        dc = D_at(v, i, j);
+        const T dl = D_at(v, i - 1, j), dd = D_at(v, i, j - 1);
+        const T Dx = fma(T(0.5), dc - dl, dl);
+        const T Dy = fma(T(0.5), dc - dd, dd);
+        const T sc = S_at(v, i, j);
+        v.qx(i, j, 0) = -Dx * ((sc - S_at(v, i - 1, j)) * v.idx);
+        v.qy(i, j, 0) = -Dy * ((sc - S_at(v, i, j - 1)) * v.idy);
+    }
+    if (dmax_bits) cgsia::block_max_bits(in ? bits_of(dc) : 0ull, dmax_bits);
 }
 
 // D over cells [0, n]^2 into v.D and max over the interior [1, n]^2.
@@ -66,10 +60,13 @@ template <class T>
 __global__ void sia_D_kernel(const SiaV<T> v, int nx, int ny, unsigned long long* dmax_bits) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    if (i > nx || j > ny) return;
-    const T d = D_at(v, i, j);
-    v.D(i, j, 0) = d;
-    if (i >= 1 && j >= 1) atomicMax(dmax_bits, bits_of(d));
+    const bool in = i <= nx && j <= ny;
+    T d = T(0);
+    if (in) {
+        d = D_at(v, i, j);
+        v.D(i, j, 0) = d;
+    }
+    cgsia::block_max_bits(in && i >= 1 && j >= 1 ? bits_of(d) : 0ull, dmax_bits);
 }
 
 // update_q! from the precomputed D (same arithmetic as sia_q_kernel).

@@ -8,9 +8,16 @@
 // q.x => (x = Dirichlet()) writes 0 on the boundary faces i = 1, n+1 (q.y likewise), and
 // H => Neumann() copies the first interior value into the ghost layer, corners taking the
 // value of the diagonal interior cell (the x rule runs last and reads the y ghost).
+//
+// The step is bound by the FP64 pipe, so FP64 work is traded for memory traffic:
+// - S = B + H is kept per cell in a scratch array. The H kernel updates it with the new
+//   thickness, including the ghost layer; the cells beyond it never change.
+// - The D kernel hands its lower-face surface gradients to the q kernel through the q arrays.
+// Every value is the one the direct form computes, with the same operations in the same order.
 #include <vector>
 
 #include "cg_common.cuh"
+#include "cg_sia_kernels.cuh"
 
 void* cg_scratch(cg_ctx* ctx, int slot, size_t bytes, int* rc);
 
@@ -18,7 +25,7 @@ namespace {
 
 template <class T>
 struct Member {
-    DF<T> H, B, qx, qy, D;
+    DF<T> H, B, qx, qy, D, S;
     T Gamma, As, beta, ela, m_max, idx, idy;
     double dx2, cfl, dt_max;
     int n, nx, ny;
@@ -32,35 +39,19 @@ struct Words {
     double pad;
 };
 
-template <class T>
-__device__ __forceinline__ T ipow(T x, int m) {
-    if (m <= 0) return T(1);
-    T r = x;
-    for (int k = 1; k < m; ++k) r = r * x;
-    return r;
-}
+using cgsia::bits_of;
 
+// The block's member descriptor, copied once into shared memory (every thread of the block
+// calls it before reading the member).
 template <class T>
-__device__ __forceinline__ T S_at(const Member<T>& v, int i, int j) {
-    return v.B(i, j, 0) + v.H(i, j, 0);
+__device__ __forceinline__ const Member<T>& member_of(const Member<T>* mem, int m) {
+    __shared__ __align__(16) unsigned long long words[(sizeof(Member<T>) + 7) / 8];
+    const int tid = threadIdx.x + blockDim.x * threadIdx.y;
+    const unsigned long long* src = reinterpret_cast<const unsigned long long*>(mem + m);
+    for (int k = tid; k < (int)((sizeof(Member<T>) + 7) / 8); k += blockDim.x * blockDim.y) words[k] = src[k];
+    __syncthreads();
+    return *reinterpret_cast<const Member<T>*>(words);
 }
-
-template <class T>
-__device__ __forceinline__ T D_at(const Member<T>& v, int i, int j) {
-    const T s = S_at(v, i, j);
-    const T a0 = (s - S_at(v, i - 1, j)) * v.idx;
-    const T a1 = (S_at(v, i + 1, j) - s) * v.idx;
-    const T b0 = (s - S_at(v, i, j - 1)) * v.idy;
-    const T b1 = (S_at(v, i, j + 1) - s) * v.idy;
-    const T ax = fma(T(0.5), a1 - a0, a0);
-    const T ay = fma(T(0.5), b1 - b0, b0);
-    const T vm = sqrt(ax * ax + ay * ay);
-    const T h = v.H(i, j, 0);
-    return (v.Gamma * ipow(h, v.n + 2) + v.As * ipow(h, v.n)) * ipow(vm, v.n - 1);
-}
-
-__device__ __forceinline__ unsigned long long bits_of(double d) { return (unsigned long long)__double_as_longlong(d); }
-__device__ __forceinline__ unsigned long long bits_of(float f) { return (unsigned long long)(unsigned)__float_as_int(f); }
 
 // block -> (member, tile) through the inclusive prefix of per-member tile counts
 __device__ __forceinline__ int find_member(const int* prefix, int nm, int blk) {
@@ -76,21 +67,49 @@ __device__ __forceinline__ int find_member(const int* prefix, int nm, int blk) {
 template <class T>
 __global__ void ens_D_kernel(const Member<T>* mem, const int* prefix, int nm, Words* w) {
     const int m = find_member(prefix, nm, blockIdx.x);
-    const Member<T> v = mem[m];
+    const Member<T>& v = member_of(mem, m);
     const int t = blockIdx.x - (m ? prefix[m - 1] : 0);
     const int tx = (v.nx + 1 + 31) / 32;
     const int i = (t % tx) * 32 + threadIdx.x;
     const int j = (t / tx) * 8 + threadIdx.y;
-    if (i > v.nx || j > v.ny) return;
-    const T d = D_at(v, i, j);
-    v.D(i, j, 0) = d;
-    if (i >= 1 && j >= 1) atomicMax(&w[m].dmax, bits_of(d));
+    const bool in = i <= v.nx && j <= v.ny;
+    T d = T(0);
+    if (in) {
+        // ∇S at the cell's faces, interpolated to the cell; vmag and D (examples/sia.jl:43-49)
+        const T s = v.S(i, j, 0);
+        const T a0 = (s - v.S(i - 1, j, 0)) * v.idx;
+        const T a1 = (v.S(i + 1, j, 0) - s) * v.idx;
+        const T b0 = (s - v.S(i, j - 1, 0)) * v.idy;
+        const T b1 = (v.S(i, j + 1, 0) - s) * v.idy;
+        const T ax = fma(T(0.5), a1 - a0, a0);
+        const T ay = fma(T(0.5), b1 - b0, b0);
+        d = cgsia::D_cell(v.H(i, j, 0), ax, ay, v.Gamma, v.As, v.n);
+        v.D(i, j, 0) = d;
+        if (i >= 1 && j >= 1) {  // the lower faces' gradients, for the q kernel
+            v.qx(i, j, 0) = a0;
+            v.qy(i, j, 0) = b0;
+        }
+    }
+    cgsia::block_max_bits(in && i >= 1 && j >= 1 ? bits_of(d) : 0ull, &w[m].dmax);
+}
+
+// S = B + H over [-1, n+1]^2 (the D kernel's stencil), once per run
+template <class T>
+__global__ void ens_S_kernel(const Member<T>* mem, const int* prefix, int nm) {
+    const int m = find_member(prefix, nm, blockIdx.x);
+    const Member<T>& v = member_of(mem, m);
+    const int t = blockIdx.x - (m ? prefix[m - 1] : 0);
+    const int tx = (v.nx + 3 + 31) / 32;
+    const int i = (t % tx) * 32 + threadIdx.x - 1;
+    const int j = (t / tx) * 8 + threadIdx.y - 1;
+    if (i > v.nx + 1 || j > v.ny + 1) return;
+    v.S(i, j, 0) = v.B(i, j, 0) + v.H(i, j, 0);
 }
 
 template <class T>
 __global__ void ens_q_kernel(const Member<T>* mem, const int* prefix, int nm) {
     const int m = find_member(prefix, nm, blockIdx.x);
-    const Member<T> v = mem[m];
+    const Member<T>& v = member_of(mem, m);
     const int t = blockIdx.x - (m ? prefix[m - 1] : 0);
     const int tx = (v.nx + 31) / 32;
     const int i = (t % tx) * 32 + threadIdx.x + 1;
@@ -99,10 +118,12 @@ __global__ void ens_q_kernel(const Member<T>* mem, const int* prefix, int nm) {
     const T dc = v.D(i, j, 0), dl = v.D(i - 1, j, 0), dd = v.D(i, j - 1, 0);
     const T Dx = fma(T(0.5), dc - dl, dl);
     const T Dy = fma(T(0.5), dc - dd, dd);
-    const T sc = S_at(v, i, j);
-    // bc!(q.x => (x = Dirichlet())): the boundary face i = 1 is 0 (i = n+1 is never written)
-    v.qx(i, j, 0) = i == 1 ? T(0) : -Dx * ((sc - S_at(v, i - 1, j)) * v.idx);
-    v.qy(i, j, 0) = j == 1 ? T(0) : -Dy * ((sc - S_at(v, i, j - 1)) * v.idy);
+    // q = -lerp(D) ∂S with ∂S left in q by the D kernel; bc!(q.x => (x = Dirichlet())): the
+    // boundary faces i = 1 and n+1 are 0 (q.y likewise)
+    v.qx(i, j, 0) = i == 1 ? T(0) : -Dx * v.qx(i, j, 0);
+    v.qy(i, j, 0) = j == 1 ? T(0) : -Dy * v.qy(i, j, 0);
+    if (i == v.nx) v.qx(i + 1, j, 0) = T(0);
+    if (j == v.ny) v.qy(i, j + 1, 0) = T(0);
 }
 
 template <class T>
@@ -123,7 +144,7 @@ __global__ void ens_dt_kernel(const Member<T>* mem, int nm, Words* w) {
 template <class T>
 __global__ void ens_H_kernel(const Member<T>* mem, const int* prefix, int nm, const Words* w) {
     const int m = find_member(prefix, nm, blockIdx.x);
-    const Member<T> v = mem[m];
+    const Member<T>& v = member_of(mem, m);
     const int t = blockIdx.x - (m ? prefix[m - 1] : 0);
     const int tx = (v.nx + 31) / 32;
     const int i = (t % tx) * 32 + threadIdx.x + 1;
@@ -131,21 +152,30 @@ __global__ void ens_H_kernel(const Member<T>* mem, const int* prefix, int nm, co
     if (i > v.nx || j > v.ny) return;
     const T dt = (T)w[m].dt;
     const T h = v.H(i, j, 0);
-    const T mb = fmin(v.beta * (S_at(v, i, j) - v.ela), v.m_max);
+    // M = min(beta (S - ela), m_max) and H = max(H + dt (-divg q + M), 0), as std::min/max
+    // (a NaN propagates as in the reference)
+    T mb = v.beta * (v.S(i, j, 0) - v.ela);
+    mb = v.m_max < mb ? v.m_max : mb;
     T dv = (v.qx(i + 1, j, 0) - v.qx(i, j, 0)) * v.idx;
     dv = dv + (v.qy(i, j + 1, 0) - v.qy(i, j, 0)) * v.idy;
-    const T hn = fmax(h + dt * (-dv + mb), T(0.0));
+    T hn = h + dt * (-dv + mb);
+    hn = hn < T(0.0) ? T(0.0) : hn;
     v.H(i, j, 0) = hn;
+    v.S(i, j, 0) = v.B(i, j, 0) + hn;
     // bc!(H => Neumann()): ghost layer and corners from the first interior cells
     const bool l = i == 1, r = i == v.nx, b = j == 1, tp = j == v.ny;
-    if (l) v.H(0, j, 0) = hn;
-    if (r) v.H(v.nx + 1, j, 0) = hn;
-    if (b) v.H(i, 0, 0) = hn;
-    if (tp) v.H(i, v.ny + 1, 0) = hn;
-    if (l && b) v.H(0, 0, 0) = hn;
-    if (r && b) v.H(v.nx + 1, 0, 0) = hn;
-    if (l && tp) v.H(0, v.ny + 1, 0) = hn;
-    if (r && tp) v.H(v.nx + 1, v.ny + 1, 0) = hn;
+    auto ghost = [&](int gi, int gj) {
+        v.H(gi, gj, 0) = hn;
+        v.S(gi, gj, 0) = v.B(gi, gj, 0) + hn;
+    };
+    if (l) ghost(0, j);
+    if (r) ghost(v.nx + 1, j);
+    if (b) ghost(i, 0);
+    if (tp) ghost(i, v.ny + 1);
+    if (l && b) ghost(0, 0);
+    if (r && b) ghost(v.nx + 1, 0);
+    if (l && tp) ghost(0, v.ny + 1);
+    if (r && tp) ghost(v.nx + 1, v.ny + 1);
 }
 
 template <class T>
@@ -158,21 +188,25 @@ int run_t(cg_ctx* ctx, int nm, const cg_sia_member* ms, const cg_sia_params* ps,
     off += ((size_t)nm * sizeof(int) + 255) & ~(size_t)255;
     const size_t pI_off = off;
     off += ((size_t)nm * sizeof(int) + 255) & ~(size_t)255;
+    const size_t pS_off = off;
+    off += ((size_t)nm * sizeof(int) + 255) & ~(size_t)255;
     const size_t w_off = off;
     off += ((size_t)nm * sizeof(Words) + 255) & ~(size_t)255;
-    std::vector<size_t> d_off(nm);
+    std::vector<size_t> d_off(nm), s_off(nm);
     for (int m = 0; m < nm; ++m) {
         const cg_field& H = ms[m].H;
         const size_t cnt = (size_t)H.stride[1] * (H.n[1] + 4 * H.halo[1]);
         d_off[m] = off;
+        off += (cnt * sizeof(T) + 255) & ~(size_t)255;
+        s_off[m] = off;
         off += (cnt * sizeof(T) + 255) & ~(size_t)255;
     }
     int rc = CG_OK;
     char* base = static_cast<char*>(cg_scratch(ctx, 3, off, &rc));
     if (rc) return rc;
     std::vector<Member<T>> hm(nm);
-    std::vector<int> pD(nm), pI(nm);
-    int totD = 0, totI = 0;
+    std::vector<int> pD(nm), pI(nm), pS(nm);
+    int totD = 0, totI = 0, totS = 0;
     for (int m = 0; m < nm; ++m) {
         const cg_sia_member& s = ms[m];
         const cg_sia_params& p = ps[m];
@@ -184,6 +218,8 @@ int run_t(cg_ctx* ctx, int nm, const cg_sia_member* ms, const cg_sia_params* ps,
         v.qy = cg_view<T>(s.q[1]);
         v.D = v.H;
         v.D.p = reinterpret_cast<T*>(base + d_off[m]) + cg_origin_offset(s.H);
+        v.S = v.H;
+        v.S.p = reinterpret_cast<T*>(base + s_off[m]) + cg_origin_offset(s.H);
         v.Gamma = (T)p.Gamma;
         v.As = (T)p.As;
         v.beta = (T)p.beta;
@@ -202,16 +238,20 @@ int run_t(cg_ctx* ctx, int nm, const cg_sia_member* ms, const cg_sia_params* ps,
         v.tiles_I = cg_div_up(v.nx, 32) * cg_div_up(v.ny, 8);
         totD += v.tiles_D;
         totI += v.tiles_I;
+        totS += cg_div_up(v.nx + 3, 32) * cg_div_up(v.ny + 3, 8);
         pD[m] = totD;
         pI[m] = totI;
+        pS[m] = totS;
     }
     Member<T>* dmem = reinterpret_cast<Member<T>*>(base + mem_off);
     int* dpD = reinterpret_cast<int*>(base + pD_off);
     int* dpI = reinterpret_cast<int*>(base + pI_off);
+    int* dpS = reinterpret_cast<int*>(base + pS_off);
     Words* dw = reinterpret_cast<Words*>(base + w_off);
     CG_CUDA(ctx, cudaMemcpyAsync(dmem, hm.data(), nm * sizeof(Member<T>), cudaMemcpyHostToDevice, ctx->stream));
     CG_CUDA(ctx, cudaMemcpyAsync(dpD, pD.data(), nm * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
     CG_CUDA(ctx, cudaMemcpyAsync(dpI, pI.data(), nm * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    CG_CUDA(ctx, cudaMemcpyAsync(dpS, pS.data(), nm * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
     CG_CUDA(ctx, cudaMemsetAsync(dw, 0, nm * sizeof(Words), ctx->stream));
     std::string key = "sia_ensemble";
     cg_key_add(key, nm);
@@ -220,6 +260,7 @@ int run_t(cg_ctx* ctx, int nm, const cg_sia_member* ms, const cg_sia_params* ps,
     key.append(reinterpret_cast<const char*>(hm.data()), nm * sizeof(Member<T>));
     const dim3 block(32, 8);
     rc = cg_graph_run(ctx, key, [&](cudaStream_t st) {
+        ens_S_kernel<T><<<totS, block, 0, st>>>(dmem, dpS, nm);
         for (int s = 0; s < nsteps; ++s) {
             ens_D_kernel<T><<<totD, block, 0, st>>>(dmem, dpD, nm, dw);
             ens_q_kernel<T><<<totI, block, 0, st>>>(dmem, dpI, nm);
