@@ -553,8 +553,10 @@ def config_suite(arch, stream, peak):
     gd2 = g2.desc()
     cfg2 = {}
     for T, name in ((np.float64, "fp64"), (np.float32, "fp32")):
-        fs = {k: Field(arch, g2, Cl, T) for k in ("C", "C_old", "D")}
-        q = [Field(arch, g2, tuple(Vl if e == d else Cl for e in range(3)), T) for d in range(3)]
+        # FP32: one row pitch and plane height for every array (the fused single-pass kernel)
+        lay = dict(pitch_align=128, plane_rows=n2 + 5) if T == np.float32 else {}
+        fs = {k: Field(arch, g2, Cl, T, **lay) for k in ("C", "C_old", "D")}
+        q = [Field(arch, g2, tuple(Vl if e == d else Cl for e in range(3)), T, **lay) for d in range(3)]
         fs["C"].from_numpy(Cb.astype(T))
         fs["D"].from_numpy(D.astype(T))
         f = _abi.cg_ptdiff_fields()
@@ -567,11 +569,57 @@ def config_suite(arch, stream, peak):
         cfg2[name] = {"ms_per_iteration": ms2 / npt, "t_eff_gbs": teff, "frac": teff / peak}
         del fs, q, f
         torch.cuda.empty_cache()
-    del D, Cb
+    # one implicit step: 500 FP64 PT iterations (the configuration's step), then the FP32 PT
+    # solve inside FP64 defect correction to the residual those 500 iterations reach
+    fs = {k: Field(arch, g2, Cl, np.float64) for k in ("C", "C_old", "D")}
+    q = [Field(arch, g2, tuple(Vl if e == d else Cl for e in range(3)), np.float64) for d in range(3)]
+    fs["D"].from_numpy(D.astype(np.float64))
+    f = _abi.cg_ptdiff_fields()
+    f.C, f.C_old, f.D = fs["C"].desc(), fs["C_old"].desc(), fs["D"].desc()
+    f.q = (_abi.cg_field * 3)(*[qq.desc() for qq in q])
+
+    def reset():
+        fs["C"].from_numpy(Cb)
+        arch.call("cg_bc_apply", ctypes.byref(gd2), 1, ctypes.byref(fs["C"].desc()), ctypes.byref(bc2))
+        fs["C_old"].data.copy_(fs["C"].data)
+        for qq in q:
+            qq.data.zero_()
+
+    def solve(prec, eps, max_iter, ncheck):
+        # inner_rtol 1e-3: the FP32 measure of the correction bottoms out near 1e-5 of the
+        # outer error here (eps_32 D dt / h^2 ~ 260 eps_32)
+        o = _abi.cg_solve_opts()
+        o.max_iter, o.ncheck, o.eps, o.precision, o.max_outer, o.inner_rtol = max_iter, ncheck, eps, prec, 20, 1e-3
+        r = _abi.cg_solve_result()
+        rc = arch.lib.cg_ptdiff_solve(arch.ctx, ctypes.byref(gd2), ctypes.byref(f), ctypes.byref(p2), ctypes.byref(bc2),
+                                      ctypes.byref(o), ctypes.byref(r))
+        if rc not in (0, _abi.CG_ERR_NOCONV):
+            raise RuntimeError(f"cg_ptdiff_solve: {arch.lib.cg_last_error(arch.ctx)}")
+        return r
+
+    reset()
+    r64 = solve(_abi.CG_F64, 1e-300, 500, 500)  # exactly 500 iterations, then the step's residual
+    target = float(r64.err[0])
+    times = []
+    for _ in range(2):  # the first call captures the correction loop's graph and tunes its kernel
+        reset()
+        rdc = solve(_abi.CG_F32, target, 100000, 100)
+        times.append(rdc.seconds)
+    fp64_step_s = cfg2["fp64"]["ms_per_iteration"] * 500 * 1e-3
+    del fs, q, f, D, Cb
+    torch.cuda.empty_cache()
     out["ptdiff3d"] = {
-        "workload": f"3D PT variable diffusion 512^3, D = exp(box-smoothed Gaussian noise), Dirichlet x / Neumann y z; one step of {npt} PT iterations",
+        "workload": f"3D PT variable diffusion 512^3, D = exp(box-smoothed Gaussian noise), Dirichlet x / Neumann y z; "
+        f"per-iteration rates from one step of {npt} PT iterations; the step comparison solves one implicit step",
         "bytes": "10 arrays x n^3 x sizeof(T) per PT iteration (read/write C, q x3; read C_old, D)",
         **cfg2,
+        "step": {
+            "fp64_500_iterations": {"s": fp64_step_s, "err": target},
+            "fp32_defect_correction": {"s": times[-1], "err": float(rdc.err[0]), "fp32_iterations": int(rdc.iterations),
+                                       "fp64_cycles": int(rdc.outer), "converged": int(rdc.converged)},
+            "speedup": fp64_step_s / times[-1],
+            "err": "max |R| dt over the interior, R = -(C - C_old)/dt - divg(-lerp(D) grad C)",
+        },
     }
 
     # config 5: SIA ensemble, 64 members of 128^2..1024^2, FP64, 1000 steps in one batched run
@@ -664,6 +712,53 @@ def fused3d_kernel_fields(arch, pb):
     return stokes_fields(V=A["V"], P=A["P"], tau=A["tau"], **extra), stokes_fields(V=B["V"], P=B["P"], tau=B["tau"]), keep
 
 
+def run_kernel_ptdiff(arch, args):
+    """--kernel ptdiff3d: the fused FP32 PT-diffusion iteration on an n^3 grid (random C, q and
+    D = exp(U[-1, 1]), Dirichlet x / Neumann y z), one step of `--reps` iterations timed with
+    CUDA events."""
+    import torch
+
+    from chmy_gb300 import Field, _abi
+    from chmy_gb300.bcs import Dirichlet, Neumann, to_cg_bc
+    from chmy_gb300.configs import ptdiff_params
+    from chmy_gb300.grids import Center, UniformGrid, Vertex
+
+    n = args.n
+    T = np.float32
+    g = UniformGrid(origin=(-0.5,) * 3, extent=(1.0,) * 3, dims=(n,) * 3, dtype=T)
+    Cl, Vl = Center(), Vertex()
+    rng = np.random.default_rng(2)
+    lay = dict(pitch_align=128, plane_rows=n + 5)
+    fs = {k: Field(arch, g, Cl, T, **lay) for k in ("C", "C_old", "D")}
+    q = [Field(arch, g, tuple(Vl if e == d else Cl for e in range(3)), T, **lay) for d in range(3)]
+    fs["C"].from_numpy(rng.random(fs["C"].data.shape, dtype=T))
+    D = np.exp(rng.uniform(-1, 1, fs["D"].data.shape)).astype(T)
+    fs["D"].from_numpy(D)
+    f = _abi.cg_ptdiff_fields()
+    f.C, f.C_old, f.D = fs["C"].desc(), fs["C_old"].desc(), fs["D"].desc()
+    f.q = (_abi.cg_field * 3)(*[qq.desc() for qq in q])
+    p = ptdiff_params(g, 1e-3, float(D.max()))
+    bc = to_cg_bc(3, {"x": Dirichlet(0.0), "y": Neumann(), "z": Neumann()})
+    gd = g.desc()
+    reps = args.reps
+
+    def run(k):
+        arch.call("cg_ptdiff_run", ctypes.byref(gd), ctypes.byref(f), ctypes.byref(p), ctypes.byref(bc), 1, k)
+
+    run(4)
+    run(reps)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    run(reps)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    byt = 10 * n**3 * 4
+    print(json.dumps({"kernel": "ptd_march3d_kernel<float>", "n": n, "arrays": 10, "us_per_iteration": ms * 1e3,
+                      "algorithmic_gbs": byt / (ms * 1e-3) / 1e9, "frac_of_measured_hbm": byt / (ms * 1e-3) / 1e9 / measured_peaks()[0]}))
+
+
 def run_kernel(args):
     """--kernel fused2d | fused3d: only the fused FP32 PT kernel (2D inclusions n^2, or 3D random
     viscosity n^3), `--reps` launches timed with CUDA events (the command the committed ncu
@@ -674,6 +769,10 @@ def run_kernel(args):
     from chmy_gb300.configs import stokes2d_inclusions, stokes3d_grf
 
     arch = Arch(GB300Backend())
+    if args.kernel == "ptdiff3d":
+        run_kernel_ptdiff(arch, args)
+        arch.close()
+        return
     if args.kernel == "fused3d":
         pb = stokes3d_grf(args.n, dtype=np.float32)
         da, db, keep = fused3d_kernel_fields(arch, pb)
@@ -704,7 +803,7 @@ def run_kernel(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--kernel", choices=["fused2d", "fused3d"], help="time one kernel alone (profiling driver)")
+    ap.add_argument("--kernel", choices=["fused2d", "fused3d", "ptdiff3d"], help="time one kernel alone (profiling driver)")
     ap.add_argument("--reps", type=int, default=200)
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)

@@ -227,6 +227,7 @@ SIGNATURES: dict[str, list] = {
     "cg_ptdiff_update_C": [_vp, P(cg_grid), P(cg_ptdiff_fields), P(cg_ptdiff_params)],
     "cg_ptdiff_gradient_D": [_vp, P(cg_grid), P(cg_field), P(cg_field), C.c_double, P(cg_field)],
     "cg_ptdiff_run": [_vp, P(cg_grid), P(cg_ptdiff_fields), P(cg_ptdiff_params), P(cg_bc), C.c_int, C.c_int],
+    "cg_ptdiff_solve": [_vp, P(cg_grid), P(cg_ptdiff_fields), P(cg_ptdiff_params), P(cg_bc), P(cg_solve_opts), P(cg_solve_result)],
     "cg_sia_update_q": [_vp, P(cg_grid), P(cg_field), P(cg_field), P(cg_field), P(cg_sia_params), P(C.c_double)],
     "cg_sia_update_H": [_vp, P(cg_grid), P(cg_field), P(cg_field), P(cg_field), C.c_double, P(cg_sia_params)],
     "cg_sia_ensemble_run": [_vp, C.c_int, P(cg_sia_member), P(cg_sia_params), C.c_int, P(C.c_double)],

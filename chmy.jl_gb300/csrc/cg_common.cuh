@@ -34,9 +34,11 @@ struct cg_ctx {
     void* dc_pool = nullptr;
     size_t dc_pool_bytes = 0;
     // numbered scratch buffers of the time-stepping loops (grown on demand, freed by cg_destroy)
-    static constexpr int kScratchSlots = 4;
-    void* scratch[kScratchSlots] = {nullptr, nullptr, nullptr, nullptr};
-    size_t scratch_bytes[kScratchSlots] = {0, 0, 0, 0};
+    // slots: 0 thermal partner, 1 SIA D, 2 PT-diffusion partners, 3 SIA ensemble,
+    // 4 PT-diffusion defect-correction pool
+    static constexpr int kScratchSlots = 6;
+    void* scratch[kScratchSlots] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    size_t scratch_bytes[kScratchSlots] = {0, 0, 0, 0, 0, 0};
 };
 
 // Device scratch buffer `slot` of at least `bytes` (reallocated when too small; contents are
@@ -65,6 +67,9 @@ bool cg_pdl_enabled();
 // bc!(V) folded into the velocity reads of the 2D marching kernel (one boundary-condition
 // launch per run of PT iterations); CG_BC_FOLD=0 in the environment launches it every iteration.
 bool cg_bc_fold_enabled();
+// The fused single-pass PT-diffusion iteration (3D FP32); CG_PTDIFF_FUSED=0 keeps the
+// two-kernel form.
+bool cg_ptdiff_fused_enabled();
 
 template <class... P, class... A>
 inline cudaError_t cg_launch(void (*kern)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, bool dep,
@@ -89,6 +94,80 @@ inline cudaError_t cg_launch(void (*kern)(P...), dim3 grid, dim3 block, size_t s
 // bc! over a batch of fields (one launch); dep = true launches it as a dependent launch.
 int cg_bc_apply_impl(cg_ctx* ctx, const cg_grid* grid, int nfields, const cg_field* fields, const cg_bc* bcs,
                      bool dep = false);
+
+namespace cgk {
+
+// Arithmetic with explicit round-to-nearest and no contraction into FMA: every operation
+// rounds once, in the order the CPU oracle (built with -ffp-contract=off) evaluates it, so the
+// marching kernel matches it bitwise and a value recomputed at a segment edge rounds exactly
+// like the owner's copy.
+__device__ __forceinline__ float radd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double radd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float rsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double rsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float rmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double rmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float rdiv(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ double rdiv(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ float rfma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double rfma(double a, double b, double c) { return __fma_rn(a, b, c); }
+// 1/x correctly rounded: the same value as the IEEE division 1/x, with fewer instructions
+__device__ __forceinline__ float rrcp(float x) { return __frcp_rn(x); }
+__device__ __forceinline__ double rrcp(double x) { return __drcp_rn(x); }
+
+__device__ __forceinline__ unsigned long long bits_of(double d) { return (unsigned long long)__double_as_longlong(d); }
+__device__ __forceinline__ unsigned long long bits_of(float f) { return (unsigned long long)(unsigned)__float_as_int(f); }
+
+// Largest of the block's `bits` into *slot with one atomicMax. Every thread of the block
+// calls it. Values are >= 0 (D, or |x|), so the bit patterns order like the values; a NaN orders above every
+// number, as it does in an atomicMax per cell.
+__device__ __forceinline__ void block_max_bits(unsigned long long bits, unsigned long long* slot) {
+    constexpr unsigned FULL = 0xffffffffu;
+    __shared__ unsigned long long part[32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long other = __shfl_xor_sync(FULL, bits, o);
+        bits = other > bits ? other : bits;
+    }
+    const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+    const int nthreads = blockDim.x * blockDim.y * blockDim.z;
+    const int lane = tid & 31, warp = tid >> 5, nwarps = (nthreads + 31) >> 5;
+    if (lane == 0) part[warp] = bits;
+    __syncthreads();
+    if (warp == 0) {
+        bits = lane < nwarps ? part[lane] : 0ull;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long other = __shfl_xor_sync(FULL, bits, o);
+            bits = other > bits ? other : bits;
+        }
+        if (lane == 0 && bits) atomicMax(slot, bits);
+    }
+}
+
+// Mean time (ms) of three launches after one untimed launch, with CUDA events on `st`;
+// -1 if a launch fails (the autotuners' measurement).
+template <class F>
+inline float time_launches(F&& launch, cudaStream_t st) {
+    cudaEvent_t a, b;
+    if (cudaEventCreate(&a) != cudaSuccess) return -1.f;
+    if (cudaEventCreate(&b) != cudaSuccess) {
+        cudaEventDestroy(a);
+        return -1.f;
+    }
+    float ms = -1.f;
+    if (launch() == cudaSuccess && cudaEventRecord(a, st) == cudaSuccess) {
+        bool ok = true;
+        for (int r = 0; r < 3 && ok; ++r) ok = launch() == cudaSuccess;
+        if (ok && cudaEventRecord(b, st) == cudaSuccess && cudaEventSynchronize(b) == cudaSuccess)
+            cudaEventElapsedTime(&ms, a, b);
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return ms;
+}
+
+}  // namespace cgk
 
 // Record an error message on ctx and return `code`.
 int cg_fail(cg_ctx* ctx, int code, const char* fmt, ...);

@@ -99,6 +99,14 @@ bool cg_bc_fold_enabled() {
     return on;
 }
 
+bool cg_ptdiff_fused_enabled() {
+    static const bool on = [] {
+        const char* e = std::getenv("CG_PTDIFF_FUSED");
+        return !(e && e[0] == '0');
+    }();
+    return on;
+}
+
 bool cg_tune_lookup(const std::string& key, cg_tune_cfg* out) {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune.find(key);

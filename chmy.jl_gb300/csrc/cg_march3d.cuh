@@ -468,26 +468,6 @@ inline cudaError_t launch_march3d(const Fused3D<T>& f, const SP<T>& s, int n0, i
 // captured. Only the `out` buffers of the ping-pong view are written (the first real iteration
 // writes them again); the residual outputs are not touched. Results are cached per shape,
 // precision and layout for the process.
-template <class F>
-inline float time_launches(F&& launch, cudaStream_t st) {
-    cudaEvent_t a, b;
-    if (cudaEventCreate(&a) != cudaSuccess) return -1.f;
-    if (cudaEventCreate(&b) != cudaSuccess) {
-        cudaEventDestroy(a);
-        return -1.f;
-    }
-    float ms = -1.f;
-    if (launch() == cudaSuccess && cudaEventRecord(a, st) == cudaSuccess) {
-        bool ok = true;
-        for (int r = 0; r < 3 && ok; ++r) ok = launch() == cudaSuccess;
-        if (ok && cudaEventRecord(b, st) == cudaSuccess && cudaEventSynchronize(b) == cudaSuccess)
-            cudaEventElapsedTime(&ms, a, b);
-    }
-    cudaEventDestroy(a);
-    cudaEventDestroy(b);
-    return ms;
-}
-
 template <class T>
 inline cg_tune_cfg tune_march2d(const Fused2D<T>& f, const SP<T>& s, int n0, int n1, int nsm, cudaStream_t st) {
     cg_tune_cfg best{0, 0};

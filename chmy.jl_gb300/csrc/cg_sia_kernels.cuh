@@ -42,34 +42,8 @@ __device__ __forceinline__ T D_cell(T h, T ax, T ay, T Gamma, T As, int n) {
     return pow_int(h, n) * fma(Gamma, h * h, As) * vp;
 }
 
-__device__ __forceinline__ unsigned long long bits_of(double d) { return (unsigned long long)__double_as_longlong(d); }
-__device__ __forceinline__ unsigned long long bits_of(float f) { return (unsigned long long)(unsigned)__float_as_int(f); }
+using cgk::bits_of;
 
-// Largest of the block's `bits` into *slot with one atomicMax. Every thread of the block
-// calls it. D >= 0, so the bit patterns order like the values; a NaN orders above every
-// number, as it does in an atomicMax per cell.
-__device__ __forceinline__ void block_max_bits(unsigned long long bits, unsigned long long* slot) {
-    constexpr unsigned FULL = 0xffffffffu;
-    __shared__ unsigned long long part[32];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        const unsigned long long other = __shfl_xor_sync(FULL, bits, o);
-        bits = other > bits ? other : bits;
-    }
-    const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
-    const int nthreads = blockDim.x * blockDim.y * blockDim.z;
-    const int lane = tid & 31, warp = tid >> 5, nwarps = (nthreads + 31) >> 5;
-    if (lane == 0) part[warp] = bits;
-    __syncthreads();
-    if (warp == 0) {
-        bits = lane < nwarps ? part[lane] : 0ull;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const unsigned long long other = __shfl_xor_sync(FULL, bits, o);
-            bits = other > bits ? other : bits;
-        }
-        if (lane == 0 && bits) atomicMax(slot, bits);
-    }
-}
+using cgk::block_max_bits;
 
 }  // namespace cgsia

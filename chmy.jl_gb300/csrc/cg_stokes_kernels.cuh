@@ -7,24 +7,6 @@
 namespace cgk {
 
 
-// Arithmetic with explicit round-to-nearest and no contraction into FMA: every operation
-// rounds once, in the order the CPU oracle (built with -ffp-contract=off) evaluates it, so the
-// marching kernel matches it bitwise and a value recomputed at a segment edge rounds exactly
-// like the owner's copy.
-__device__ __forceinline__ float radd(float a, float b) { return __fadd_rn(a, b); }
-__device__ __forceinline__ double radd(double a, double b) { return __dadd_rn(a, b); }
-__device__ __forceinline__ float rsub(float a, float b) { return __fsub_rn(a, b); }
-__device__ __forceinline__ double rsub(double a, double b) { return __dsub_rn(a, b); }
-__device__ __forceinline__ float rmul(float a, float b) { return __fmul_rn(a, b); }
-__device__ __forceinline__ double rmul(double a, double b) { return __dmul_rn(a, b); }
-__device__ __forceinline__ float rdiv(float a, float b) { return __fdiv_rn(a, b); }
-__device__ __forceinline__ double rdiv(double a, double b) { return __ddiv_rn(a, b); }
-__device__ __forceinline__ float rfma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
-__device__ __forceinline__ double rfma(double a, double b, double c) { return __fma_rn(a, b, c); }
-// 1/x correctly rounded: the same value as the IEEE division 1/x, with fewer instructions
-__device__ __forceinline__ float rrcp(float x) { return __frcp_rn(x); }
-__device__ __forceinline__ double rrcp(double x) { return __drcp_rn(x); }
-
 template <class T>
 struct SV {  // device views of the Stokes field set
     DF<T> V[3], rV[3], P, divV, tau[6], tau_old[6], eta, ieta, rho[3], Tt, To, qT[3];

@@ -361,6 +361,25 @@ CG_API int cg_ptdiff_update_C(cg_ctx* ctx, const cg_grid* grid, const cg_ptdiff_
 CG_API int cg_ptdiff_run(cg_ctx* ctx, const cg_grid* grid, const cg_ptdiff_fields* f,
                          const cg_ptdiff_params* p, const cg_bc* bc, int nsteps, int npt);
 
+/* One implicit step (C - C_old)/dt = divg(lerp(D) grad C) solved to a tolerance on FP64 fields
+ * (3D): C holds the initial guess, C_old the previous step. The measure is
+ * err[0] = max |R| dt over the interior cells (logical 1..n), where
+ * R = -(C - C_old)/dt - divg(q(C)) and q(C) = -lerp(D) grad C is the exact flux; bc! sets the
+ * ghost planes, and every side must carry a Dirichlet or Neumann rule.
+ *   o->precision == CG_F64: the PT iterations of cg_ptdiff_run, checked every ncheck.
+ *   o->precision == CG_F32: FP64 defect correction. The correction d solves
+ *     d/dt - divg(lerp(D) grad d) = R with the rules' homogeneous form, by FP32 PT iterations
+ *     (the fused single-pass kernel) on internal FP32 arrays, until its own measure falls
+ *     below max(eps/2, inner_rtol err) or stops improving. Then C += d and bc!(C), for at most
+ *     max_outer cycles. q is then set to the exact flux of the converged C.
+ * Uses max_iter, ncheck, eps, precision, max_outer and inner_rtol of `o`. `res` receives the
+ * iteration, check and cycle counts, err[0] and the device time. Returns CG_ERR_NOCONV when
+ * the budget runs out and CG_ERR_NONFINITE on NaN/Inf. No reference counterpart: the
+ * reference has no solver for this configuration. */
+CG_API int cg_ptdiff_solve(cg_ctx* ctx, const cg_grid* grid, const cg_ptdiff_fields* f,
+                    const cg_ptdiff_params* p, const cg_bc* bc, const cg_solve_opts* o,
+                    cg_solve_result* res);
+
 /* Adjoint of the implicit diffusion steps (no reference counterpart). I - dt L_D is symmetric
  * on the interior cells, so the adjoint of a step is the same step: lambda^n = S lambda^{n+1}
  * is cg_ptdiff_run (1 step) on a field set with C = lambda^{n+1} and zero boundary values. For

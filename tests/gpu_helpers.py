@@ -8,8 +8,8 @@ from _oracle import NpField
 from chmy_gb300 import Field
 
 
-def to_gpu(arch, f: NpField, pitch_align: int = 0) -> Field:
-    g = Field(arch, f.grid, f.loc, f.dtype, f.halo, pitch_align=pitch_align)
+def to_gpu(arch, f: NpField, pitch_align: int = 0, plane_rows: int = 0) -> Field:
+    g = Field(arch, f.grid, f.loc, f.dtype, f.halo, pitch_align=pitch_align, plane_rows=plane_rows)
     g.from_numpy(f.a)
     return g
 
