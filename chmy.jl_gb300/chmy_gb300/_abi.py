@@ -231,6 +231,7 @@ SIGNATURES: dict[str, list] = {
     "cg_sia_update_q": [_vp, P(cg_grid), P(cg_field), P(cg_field), P(cg_field), P(cg_sia_params), P(C.c_double)],
     "cg_sia_update_H": [_vp, P(cg_grid), P(cg_field), P(cg_field), P(cg_field), C.c_double, P(cg_sia_params)],
     "cg_sia_ensemble_run": [_vp, C.c_int, P(cg_sia_member), P(cg_sia_params), C.c_int, P(C.c_double)],
+    "cg_sia_adjoint_step": [_vp, P(cg_grid), P(cg_field), P(cg_field), P(cg_sia_params), P(cg_field), P(cg_field), P(C.c_double)],
     "cg_sia_run": [_vp, P(cg_grid), P(cg_field), P(cg_field), P(cg_field), P(cg_sia_params), C.c_int, P(C.c_double)],
 }
 _RESTYPES = {"cg_last_error": C.c_char_p}

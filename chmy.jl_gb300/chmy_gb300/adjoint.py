@@ -1,6 +1,7 @@
-"""Adjoint of the implicit variable-coefficient diffusion steps (cg_ptdiff_run): the gradient of
-a misfit of the final state with respect to the per-cell diffusivity D and to the initial state,
-by reverse time stepping over checkpoints.
+"""Adjoints of the time loops, by reverse time stepping over checkpoints.
+
+PTDiffusion: the implicit variable-coefficient diffusion steps (cg_ptdiff_run). The gradient of
+a misfit of the final state with respect to the per-cell diffusivity D and to the initial state.
 
 One step is C' = S C with S = (I - dt L_D)^-1, L_D C = divg(lerp(D) d C). I - dt L_D is symmetric
 on the interior cells (the boundary rules folded in), so the adjoint of a step is the same PT
@@ -120,3 +121,68 @@ class PTDiffusion:
                                dt, ctypes.byref(self.gD.desc()))
             del states
         return self.gD.to_numpy(), self.adj["C"].to_numpy(), CN
+
+
+class SIA:
+    """The shallow-ice time loop of cg_sia_run (examples/sia.jl:71-81 with the flux
+    -Gamma H^(n+2) |∇S|^(n-1) ∇S, adaptive Δt and linear mass balance capped at m_max) and its
+    adjoint: the gradient of a misfit J(H^N) with respect to Gamma and ela, and to the initial
+    thickness, by reverse time stepping over checkpoints.
+
+    A step reads only H (the flux is recomputed from it), so a checkpoint is one copy of H. The
+    forward sweep keeps every `checkpoint_every`-th state. The reverse sweep recomputes each
+    segment's states from its checkpoint, then runs cg_sia_adjoint_step over them backwards.
+    Memory: nsteps / checkpoint_every + checkpoint_every states."""
+
+    def __init__(self, arch, grid, B: np.ndarray, params, dtype=np.float64):
+        self.arch, self.grid, self.params = arch, grid, params
+        C = Center()
+        self.H = Field(arch, grid, C, dtype)
+        self.B = Field(arch, grid, C, dtype)
+        self.B.from_numpy(B)
+        self.q = [Field(arch, grid, (Vertex(), C), dtype), Field(arch, grid, (C, Vertex()), dtype)]
+        self.lam = [Field(arch, grid, C, dtype), Field(arch, grid, C, dtype)]
+        self._q = (_abi.cg_field * 3)(self.q[0].desc(), self.q[1].desc(), _abi.cg_field())
+
+    def _steps(self, nsteps: int) -> float:
+        t = ctypes.c_double()
+        if nsteps > 0:
+            self.arch.call("cg_sia_run", ctypes.byref(self.grid.desc()), ctypes.byref(self.H.desc()), ctypes.byref(self.B.desc()),
+                           self._q, ctypes.byref(self.params), int(nsteps), ctypes.byref(t))
+        return t.value
+
+    def run(self, H0: np.ndarray, nsteps: int) -> np.ndarray:
+        """Forward: `nsteps` steps from H0; returns H^N (padded)."""
+        self.H.from_numpy(H0)
+        self._steps(nsteps)
+        return self.H.to_numpy()
+
+    def gradient(self, H0: np.ndarray, nsteps: int, misfit_grad, checkpoint_every: int | None = None):
+        """(dJ/dGamma, dJ/dela, dJ/dH0, H^N). `misfit_grad(HN)` returns dJ/dH^N as a padded host
+        array (its interior is used)."""
+        K = int(checkpoint_every or max(1, math.ceil(math.sqrt(nsteps))))
+        self.H.from_numpy(H0)
+        checkpoints = {}
+        for n in range(nsteps):
+            if n % K == 0:
+                checkpoints[n] = self.H.data.clone()
+            self._steps(1)
+        HN = self.H.to_numpy()
+        self.lam[0].from_numpy(misfit_grad(HN))
+        dJ = (ctypes.c_double * 2)(0.0, 0.0)
+        g = self.grid.desc()
+        cur = 0
+        for start in sorted(checkpoints, reverse=True):
+            stop = min(start + K, nsteps)
+            self.H.data.copy_(checkpoints[start])
+            states = []
+            for _ in range(start, stop):
+                states.append(self.H.data.clone())
+                self._steps(1)
+            for n in range(stop - 1, start - 1, -1):
+                self.H.data.copy_(states[n - start])
+                self.arch.call("cg_sia_adjoint_step", ctypes.byref(g), ctypes.byref(self.H.desc()), ctypes.byref(self.B.desc()),
+                               ctypes.byref(self.params), ctypes.byref(self.lam[cur].desc()), ctypes.byref(self.lam[1 - cur].desc()), dJ)
+                cur = 1 - cur
+            del states
+        return dJ[0], dJ[1], self.lam[cur].to_numpy(), HN

@@ -2,6 +2,7 @@
 variable viscosity) against central finite differences of the forward solve, in 2D and 3D: the
 differences agree with the adjoint gradient to 1e-6 of its largest value."""
 
+import ctypes
 import dataclasses
 
 import numpy as np
@@ -156,3 +157,69 @@ def test_ptdiff_gradient_D_matches_finite_differences(arch):
         Jpm.append(J(PTDiffusion(arch, grid, D, p, bc, npt).run(C0p, nsteps)))
     fd = (Jpm[0] - Jpm[1]) / 2e-4
     assert abs(gC0[idx] - fd) <= 1e-6 * max(abs(fd), np.abs(gC0[inner]).max()), (gC0[idx], fd)
+
+
+def _sia_problem(n=(48, 40), dt_max=0.5):
+    from chmy_gb300.configs import gaussian_random_field, padded_mesh
+    from chmy_gb300.grids import Center, UniformGrid
+
+    T = np.float64
+    grid = UniformGrid(origin=(T(-1), T(-1)), extent=(T(2), T(2)), dims=n, dtype=T)
+    x, y = padded_mesh(grid, Center())
+    bed = 0.4 + 0.3 * gaussian_random_field(x.shape, 0.25, 2.0 / n[0], 7)
+    H0 = np.clip(0.35 - 0.25 * (x * x + y * y), 0.0, None)
+    p = _abi.cg_sia_params()
+    p.Gamma, p.As, p.n, p.beta, p.ela, p.m_max, p.dt_max, p.cfl = 1.0, 0.0, 3, 0.5, 0.55, 0.25, dt_max, 4.1
+    return grid, bed.astype(T), H0.astype(T), p
+
+
+@pytest.mark.parametrize("dt_max", [0.5, 1e-3])
+def test_sia_gradient_gamma_ela_matches_finite_differences(arch, dt_max):
+    """SIA time loop (config 5 form, 2D 48 x 40, 60 steps): the adjoint gradients of
+    J = 1/2 |H^N - H_obs|^2 with respect to log(Gamma) and ela agree with central differences
+    to 1e-6, with the adaptive time step (dt_max = 0.5: dt from max D) and with dt capped
+    (dt_max = 1e-3); checkpointing every 1, 7 and sqrt(N) steps gives the same bits."""
+    from chmy_gb300.adjoint import SIA
+
+    grid, bed, H0, p = _sia_problem(dt_max=dt_max)
+    nsteps = 60
+    inner = (slice(2, -2), slice(2, -2))
+    sia = SIA(arch, grid, bed, p)
+    HN = sia.run(H0, nsteps)
+    rng = np.random.default_rng(3)
+    obs = HN[inner] + 0.01 * rng.standard_normal(HN[inner].shape)
+
+    def J(h):
+        r = h[inner] - obs
+        return 0.5 * float(np.sum(r * r))
+
+    def dJ(h):
+        g = np.zeros_like(h)
+        g[inner] = h[inner] - obs
+        return g
+
+    gG, gE, gH0, HN2 = sia.gradient(H0, nsteps, dJ)
+    assert np.array_equal(HN, HN2)
+    for K in (1, 7):
+        a, b, c, _ = sia.gradient(H0, nsteps, dJ, checkpoint_every=K)
+        assert (a, b) == (gG, gE) and np.array_equal(c, gH0)
+
+    def J_at(H=H0, **kw):
+        q = _abi.cg_sia_params()
+        ctypes.memmove(ctypes.byref(q), ctypes.byref(p), ctypes.sizeof(q))
+        for k, v in kw.items():
+            setattr(q, k, v)
+        return J(SIA(arch, grid, bed, q).run(H, nsteps))
+
+    h = 1e-6
+    fdG = (J_at(Gamma=p.Gamma * np.exp(h)) - J_at(Gamma=p.Gamma * np.exp(-h))) / (2 * h)
+    fdE = (J_at(ela=p.ela + h) - J_at(ela=p.ela - h)) / (2 * h)
+    assert abs(gG * p.Gamma - fdG) <= 1e-6 * abs(fdG), (gG * p.Gamma, fdG)
+    assert abs(gE - fdE) <= 1e-6 * abs(fdE), (gE, fdE)
+    # the initial thickness at an ice-covered interior cell
+    idx = (H0.shape[0] // 2, H0.shape[1] // 2 + 3)
+    Hp, Hm = H0.copy(), H0.copy()
+    Hp[idx] += 1e-6
+    Hm[idx] -= 1e-6
+    fdH = (J_at(H=Hp) - J_at(H=Hm)) / 2e-6
+    assert abs(gH0[idx] - fdH) <= 1e-6 * max(abs(fdH), float(np.abs(gH0).max())), (gH0[idx], fdH)
