@@ -15,7 +15,7 @@ PKG_DIR = Path(__file__).resolve().parent
 LIB_PATH = PKG_DIR / "lib" / "libchmy_gb300.so"
 HEADER = PKG_DIR.parent.parent / "include" / "chmy_gb300.h"
 
-ABI_VERSION = 1
+ABI_VERSION = 2
 
 # status codes
 CG_OK = 0
@@ -71,7 +71,7 @@ class cg_grid(C.Structure):
 
 
 class cg_bc(C.Structure):
-    _fields_ = [("kind", (C.c_int32 * 2) * 3), ("value", (C.c_double * 2) * 3)]
+    _fields_ = [("kind", (C.c_int32 * 2) * 3), ("value", (C.c_double * 2) * 3), ("values", (C.c_void_p * 2) * 3)]
 
 
 class cg_stokes_fields(C.Structure):

@@ -30,6 +30,7 @@ def _zero_bc(bc: _abi.cg_bc) -> _abi.cg_bc:
     for d in range(3):
         for s in range(2):
             b.value[d][s] = 0.0
+            b.values[d][s] = None
     return b
 
 

@@ -4,14 +4,24 @@ Python spelling of Chmy's pairs: `(field, Neumann())` for all sides, or
 `(field, {"x": Dirichlet(), "y": (Neumann(), Neumann(1.0))})` per dimension and side.
 A batch applies as ONE library launch (cg_bc_apply) with the result of Chmy's 2N
 per-side launches.
+
+A condition's value is `None` (0), a number, a BoundaryFunction, or per-point values: a
+lower-dimensional Field (Chmy's FirstOrderBC{<:AbstractField}, read at remove_dim(dim, I)) or
+a host array over the tangential logical indices 0..n_t+2 ([z, y, x] storage order without
+the condition's dimension). Functions and arrays become per-point value arrays of the
+field's type, passed to the library in cg_bc.values.
 """
 
 from __future__ import annotations
 
 import ctypes
+import numbers
 from dataclasses import dataclass
 
+import numpy as np
+
 from . import _abi
+from .grids import Center, Vertex, expand_loc, flip
 
 _AXES = ("x", "y", "z")
 
@@ -41,6 +51,61 @@ class Periodic:
     kind = _abi.CG_BC_PERIODIC
 
 
+class Dim:
+    """Chmy's Dim(D) (1-based), which tells coord(grid, loc, Dim(d), i) apart from
+    coord(grid, loc, I...)."""
+
+    def __init__(self, d: int):
+        self.d = int(d)
+
+    def __index__(self):
+        return self.d
+
+    def __repr__(self):
+        return f"Dim({self.d})"
+
+
+def coord(grid, loc, *args):
+    """coord(grid, loc, I...) -> the point's coordinates, every dimension at location `loc`
+    (src/Grids/structured_grid.jl:103-107); coord(grid, loc, Dim(d), i) -> the coordinate along
+    dimension d at index i (:115-119). Indices are Chmy's (1-based interior)."""
+    if args and isinstance(args[0], Dim):
+        return grid.coord(loc, args[0].d, int(args[1]))
+    locs = expand_loc(grid.ndim, loc)
+    return tuple(grid.axes[k].coord(locs[k], int(i)) for k, i in enumerate(args))
+
+
+class BoundaryFunction:
+    """BoundaryFunction(fun; discrete=false, parameters=nothing, reduce_dims=true)
+    (src/BoundaryConditions/boundary_function.jl:34-76). Called as bf(grid, loc, dim, I...)
+    with dim a Dim (or a 1-based int) and I the point's indices, one per dimension.
+    - Continuous: fun(coords..., params...) at coord(grid, loc, I...), with the coordinate
+      along `dim` removed when reduce_dims.
+    - Discrete: fun(grid, loc, dim, I..., params...), with the index along `dim` removed when
+      reduce_dims.
+    `parameters` is a value or a tuple of values, splatted after the coordinates."""
+
+    def __init__(self, fun, discrete: bool = False, parameters=None, reduce_dims: bool = True):
+        self.fun, self.discrete, self.parameters, self.reduce_dims = fun, bool(discrete), parameters, bool(reduce_dims)
+
+    def _params(self) -> tuple:
+        p = self.parameters
+        if p is None:
+            return ()
+        return tuple(p) if isinstance(p, (tuple, list)) else (p,)
+
+    def __call__(self, grid, loc, dim, *I):
+        d0 = int(dim) - 1
+        dimv = dim if isinstance(dim, Dim) else Dim(int(dim))
+        if self.discrete:
+            idx = tuple(i for k, i in enumerate(I) if not (self.reduce_dims and k == d0))
+            return self.fun(grid, loc, dimv, *idx, *self._params())
+        c = coord(grid, loc, *I)
+        if self.reduce_dims:
+            c = tuple(x for k, x in enumerate(c) if k != d0)
+        return self.fun(*c, *self._params())
+
+
 def _expand(bc):
     if bc is None:
         return (None, None)
@@ -66,7 +131,13 @@ def regularise(ndim: int, spec) -> list[tuple]:
     raise TypeError(f"unsupported boundary-condition spec {spec!r}")
 
 
+def _constant(v) -> bool:
+    return v is None or isinstance(v, numbers.Number)
+
+
 def to_cg_bc(ndim: int, spec) -> _abi.cg_bc:
+    """Conditions with constant values (`None` or a number) as a cg_bc; per-point values
+    need the field: materialize_bc."""
     b = _abi.cg_bc()
     for d, (l, r) in enumerate(regularise(ndim, spec)):
         for s, bc in enumerate((l, r)):
@@ -74,9 +145,86 @@ def to_cg_bc(ndim: int, spec) -> _abi.cg_bc:
                 b.kind[d][s] = _abi.CG_BC_NONE
                 b.value[d][s] = 0.0
             else:
+                if not _constant(bc.value):
+                    raise TypeError("a per-point boundary value needs its field: use materialize_bc or a Batch")
                 b.kind[d][s] = bc.kind
                 b.value[d][s] = 0.0 if bc.value is None else float(bc.value)
     return b
+
+
+def bc_values(grid, loc, dtype, d: int, side: int, bc) -> np.ndarray:
+    """The per-point values of condition `bc` on side `side` of dimension d (0-based) for a
+    field at `loc`: a host array over the tangential logical indices 0..n_t+2 ([z, y, x] order
+    without dimension d), as the library's cg_bc.values reads it.
+    - BoundaryFunction: evaluated at the points the condition writes
+      (first_order_boundary_condition.jl:46-84). The location is the field's along d for
+      Dirichlet and its flip for Neumann, applied to every dimension. The index along d is
+      the boundary node (Vertex Dirichlet: 1 or n+1), else the ghost (0 or n+1 for Center,
+      0 or n+2 for Vertex).
+    - A lower-dimensional Field: its logical indices 0..n_t+2.
+    - An array: taken as is (shape checked)."""
+    nd = grid.ndim
+    locs = expand_loc(nd, loc)
+    tdims = [t for t in range(nd) if t != d]
+    shape = tuple(grid.dims[t] + 3 for t in reversed(tdims))
+    v = bc.value
+    if isinstance(v, BoundaryFunction):
+        ext = grid.axes[d].size(locs[d])
+        vtx = isinstance(locs[d], Vertex)
+        if bc.kind == _abi.CG_BC_DIRICHLET and vtx:
+            gi = 1 if side == 0 else ext
+        else:
+            gi = 0 if side == 0 else ext + 1
+        eval_loc = locs[d] if bc.kind == _abi.CG_BC_DIRICHLET else flip(locs[d])
+        out = np.empty(shape, dtype=dtype)
+        for flat in range(out.size):
+            rem = flat
+            I = [0] * nd
+            I[d] = gi
+            for t in tdims:
+                I[t] = rem % (grid.dims[t] + 3)
+                rem //= grid.dims[t] + 3
+            out.reshape(-1)[flat] = v(grid, eval_loc, Dim(d + 1), *I)
+        return out
+    if hasattr(v, "to_numpy") and hasattr(v, "halo"):
+        a = v.to_numpy()
+        sl = tuple(slice(2 * h - 1, 2 * h - 1 + n) for h, n in zip(reversed(v.halo), shape))
+        out = np.ascontiguousarray(a[sl], dtype=dtype)
+    else:
+        out = np.ascontiguousarray(np.asarray(v, dtype=dtype))
+    if out.shape != shape:
+        raise ValueError(f"per-point boundary values on dimension {d + 1}: expected shape {shape}, got {out.shape}")
+    return out
+
+
+def materialize_bc(grid, loc, dtype, spec, device=None):
+    """A cg_bc for a field at `loc` whose conditions may carry per-point values. The value
+    arrays live in host memory (device=None, for the oracle) or on `device` (a torch device).
+    Returns (cg_bc, keep): `keep` holds the arrays, and must stay alive while the cg_bc is
+    used."""
+    nd = grid.ndim
+    b = _abi.cg_bc()
+    keep = []
+    for d, (l, r) in enumerate(regularise(nd, spec)):
+        for s, bc in enumerate((l, r)):
+            if bc is None:
+                b.kind[d][s] = _abi.CG_BC_NONE
+                continue
+            b.kind[d][s] = bc.kind
+            if _constant(bc.value):
+                b.value[d][s] = 0.0 if bc.value is None else float(bc.value)
+                continue
+            arr = bc_values(grid, loc, dtype, d, s, bc)
+            if device is not None:
+                import torch
+
+                t = torch.from_numpy(arr).to(device)
+                keep.append(t)
+                b.values[d][s] = t.data_ptr()
+            else:
+                keep.append(arr)
+                b.values[d][s] = arr.ctypes.data
+    return b, keep
 
 
 class Batch:
@@ -86,8 +234,11 @@ class Batch:
         self.grid = grid
         self.fields = []
         self.bcs = []
+        self._keep = []  # per-point value arrays on the fields' device
         for f, spec in pairs:
-            b = to_cg_bc(grid.ndim, spec)
+            dev = getattr(getattr(f, "arch", None), "device", None)
+            b, keep = materialize_bc(grid, f.loc, f.dtype, spec, dev)
+            self._keep.extend(keep)
             if all(b.kind[d][s] == _abi.CG_BC_NONE for d in range(grid.ndim) for s in range(2)):
                 continue  # prune (batch.jl:235-239)
             self.fields.append(f)

@@ -303,8 +303,24 @@ struct BcField {
     int loc[3];
     int kind[3][2];
     T val[3][2];
+    const T* va[3][2];  // per-point values over the tangential indices 0..n_t+2, or NULL
     T h[3];
 };
+
+// The value of phase (d, s) at the point q: the per-point array at q's tangential indices
+// (remove_dim(dim, I)), else the constant.
+template <class T>
+__device__ __forceinline__ T bc_value(const BcField<T>& F, int nd, const int* n, int d, int s, const int* q) {
+    const T* a = F.va[d][s];
+    if (!a) return F.val[d][s];
+    long idx = 0, mul = 1;
+    for (int t = 0; t < nd; ++t) {
+        if (t == d) continue;
+        idx += (long)q[t] * mul;
+        mul *= n[t] + 3;
+    }
+    return a[idx];
+}
 
 struct BcItem {
     int field, d, s, plane, start;
@@ -414,6 +430,7 @@ __global__ void bc_apply_kernel(const BcBatch<T> b) {
         if (phase_member(F, nd, b.n, k, p, &src, &rule)) return;
     // walk the chain of rules back to an unwritten point or a constant
     int stack_k[6], stack_r[6], depth = 0;
+    T stack_v[6];  // each rule's value, at the point that rule writes
     int q[3] = {p[0], p[1], p[2]};
     int k = k0;
     T base;
@@ -421,11 +438,12 @@ __global__ void bc_apply_kernel(const BcBatch<T> b) {
     for (;;) {
         const int d = nd - 1 - (k >> 1), s = k & 1;
         if (rule == R_CONST) {
-            base = F.val[d][s];
+            base = bc_value(F, nd, b.n, d, s, q);
             break;
         }
         stack_k[depth] = k;
         stack_r[depth] = rule;
+        stack_v[depth] = bc_value(F, nd, b.n, d, s, q);
         ++depth;
         q[d] = src;
         int kn = -1;
@@ -443,9 +461,10 @@ __global__ void bc_apply_kernel(const BcBatch<T> b) {
     for (int i = depth - 1; i >= 0; --i) {
         const int kk = stack_k[i];
         const int d = nd - 1 - (kk >> 1), s = kk & 1;
+        const T v = stack_v[i];
         switch (stack_r[i]) {
-            case R_DIR_C: base = fma(T(2), F.val[d][s] - base, base); break;
-            case R_NEU: base = fma(F.h[d], s == 0 ? -F.val[d][s] : F.val[d][s], base); break;
+            case R_DIR_C: base = fma(T(2), v - base, base); break;
+            case R_NEU: base = fma(F.h[d], s == 0 ? -v : v, base); break;
             default: break;
         }
     }
@@ -471,6 +490,7 @@ int bc_apply_t(cg_ctx* ctx, const cg_grid* grid, int nfields, const cg_field* fi
             for (int s = 0; s < 2; ++s) {
                 F.kind[d][s] = d < f.ndim ? bcs[fi].kind[d][s] : CG_BC_NONE;
                 F.val[d][s] = (T)bcs[fi].value[d][s];
+                F.va[d][s] = d < f.ndim ? static_cast<const T*>(bcs[fi].values[d][s]) : nullptr;
             }
         }
         for (int d = 0; d < b.nd; ++d) {

@@ -772,7 +772,10 @@ int solve_dc(cg_ctx* ctx, const cg_grid* g, const cg_ptdiff_fields* f, const cg_
     }
     // the correction's boundary rules: the caller's kinds with zero values
     cg_bc bc0 = *bc;
-    for (int d = 0; d < 3; ++d) bc0.value[d][0] = bc0.value[d][1] = 0.0;
+    for (int d = 0; d < 3; ++d) {
+        bc0.value[d][0] = bc0.value[d][1] = 0.0;
+        bc0.values[d][0] = bc0.values[d][1] = nullptr;
+    }
     const PDM<float> ab = make_pdm<float>(g, dA, qA, dB, qB, &w, p);
     const PDM<float> ba = make_pdm<float>(g, dB, qB, dA, qA, &w, p);
     const int variant = tune_pd<float>(ab, g, ctx->num_sms, ctx->stream);

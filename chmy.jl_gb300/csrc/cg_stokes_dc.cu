@@ -377,7 +377,10 @@ int cg_stokes_solve_dc(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f,
     cg_bc bc0[3];
     for (int d = 0; d < nd; ++d) {
         bc0[d] = bc_V ? bc_V[d] : cg_bc{};
-        for (int a = 0; a < 3; ++a) bc0[d].value[a][0] = bc0[d].value[a][1] = 0.0;
+        for (int a = 0; a < 3; ++a) {
+            bc0[d].value[a][0] = bc0[d].value[a][1] = 0.0;
+            bc0[d].values[a][0] = bc0[d].values[a][1] = nullptr;
+        }
     }
     // FP64 measures: divV, r_V (the reference's) and the constitutive residuals, read from the
     // FP32 forcing tau_old' = G dt R_tau (the initial guess of a PT solve can have zero divV and

@@ -391,6 +391,7 @@ inline bool make_vfold(const cg_grid* g, const cg_bc* bc_V, VFold<T>* out) {
             const bool vtx = d == a;
             const int ext = vtx ? g->n[d] + 1 : g->n[d];
             for (int s = 0; s < 2; ++s) {
+                if (bc_V[a].values[d][s]) return false;  // per-point values: not folded
                 const T v = (T)bc_V[a].value[d][s];
                 signed char& r = out->rule[a][d][s];
                 switch (bc_V[a].kind[d][s]) {

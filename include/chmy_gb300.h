@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define CG_ABI_VERSION 1
+#define CG_ABI_VERSION 2
 
 /* ---- status codes --------------------------------------------------------------- */
 enum {
@@ -81,12 +81,21 @@ typedef struct cg_grid {
     double  inv_spacing[3];
 } cg_grid;
 
-/* Boundary conditions of one field: kind and constant value per dimension and side
- * (side 0 = Side(1) = left, side 1 = Side(2) = right). Dirichlet value `nothing` and
- * Neumann value `nothing` are 0 (first_order_boundary_condition.jl:34). */
+/* Boundary conditions of one field: kind and value per dimension and side (side 0 =
+ * Side(1) = left, side 1 = Side(2) = right). Dirichlet value `nothing` and Neumann value
+ * `nothing` are 0 (first_order_boundary_condition.jl:34).
+ * values[d][s]: NULL, or per-point values that replace value[d][s]. These are Chmy's
+ * Field-valued conditions, value(bc::FirstOrderBC{<:AbstractField}, ...) =
+ * bc.value[remove_dim(dim, I)...] (first_order_boundary_condition.jl:38-40), and
+ * BoundaryFunction values evaluated at the condition's points (boundary_function.jl:34-44).
+ * The array has the field's element type over the logical indices 0..n_t+2 of the grid's
+ * other dimensions, in ascending dimension order with the first fastest, so
+ * (n_t0 + 3) x (n_t1 + 3) values in 3D and n_t0 + 3 in 2D. It is device memory for the library
+ * and host memory for the oracle. */
 typedef struct cg_bc {
     int32_t kind[3][2];
     double  value[3][2];
+    const void* values[3][2];
 } cg_bc;
 
 typedef struct cg_ctx cg_ctx;

@@ -213,15 +213,18 @@ template <class T>
 void bc_phase(const Gd& g, const Fd<T>& f, const cg_bc& bc, int d, int s, T spacing_d) {
     const int kind = bc.kind[d][s];
     if (kind == CG_BC_NONE) return;
-    const T val = (T)bc.value[d][s];
     const int ext = f.n[d]; /* firstindex = 1, lastindex = ext */
     int tdims[2], nt = 0;
     for (int t = 0; t < g.nd; ++t)
         if (t != d) tdims[nt++] = t;
     const int e0 = nt > 0 ? g.n[tdims[0]] + 2 : 0;
     const int e1 = nt > 1 ? g.n[tdims[1]] + 2 : 0;
+    /* the value: bc.value[remove_dim(dim, I)...] for per-point values
+       (first_order_boundary_condition.jl:38-40), else the constant */
+    const T* vals = static_cast<const T*>(bc.values[d][s]);
     for (int b = 0; b <= e1; ++b)
         for (int a = 0; a <= e0; ++a) {
+            const T val = vals ? vals[a + (long)b * (e0 + 1)] : (T)bc.value[d][s];
             int I[3] = {0, 0, 0};
             if (nt > 0) I[tdims[0]] = a;
             if (nt > 1) I[tdims[1]] = b;

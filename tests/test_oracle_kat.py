@@ -351,3 +351,79 @@ def test_cg_bc_struct_roundtrip():
     assert b.kind[0][0] == _abi.CG_BC_DIRICHLET and b.value[0][1] == 1.0
     assert b.kind[1][0] == _abi.CG_BC_NONE and b.kind[2][1] == _abi.CG_BC_NONE
     assert b.kind[2][0] == _abi.CG_BC_NEUMANN and b.value[2][0] == 2.0
+
+
+# ---- test/test_boundary_functions.jl and Field-valued conditions -----------------------------
+
+
+@pytest.mark.parametrize("T", TYPES)
+def test_boundary_function_kats(T):
+    """BoundaryFunction values at grid points (the checks of test_boundary_functions.jl:13-95):
+    continuous/discrete, reduced/full dimensions, with parameters, on an 8 x 8 grid over
+    [-pi, pi]^2."""
+    from chmy_gb300.bcs import BoundaryFunction, Dim, coord
+
+    nx = ny = 8
+    grid = UniformGrid(origin=(T(-math.pi),) * 2, extent=(T(2 * math.pi),) * 2, dims=(nx, ny), dtype=T)
+    tol = 1e-6 if T == np.float32 else 1e-12
+    V = Vertex()
+
+    def close(a, b):
+        return abs(float(a) - float(b)) <= tol * max(1.0, abs(float(b)))
+
+    for bf in (BoundaryFunction(np.cos),
+               BoundaryFunction(lambda g, loc, dim, i: np.cos(coord(g, loc, dim, i)), discrete=True)):
+        assert close(bf(grid, V, Dim(1), 1, 1), -1.0) and close(bf(grid, V, Dim(1), 1, ny + 1), -1.0)
+        assert close(bf(grid, V, Dim(1), 1, ny // 2 + 1), 1.0)
+        assert close(bf(grid, V, Dim(2), 1, 1), -1.0) and close(bf(grid, V, Dim(2), nx + 1, 1), -1.0)
+        assert close(bf(grid, V, Dim(2), nx // 2 + 1, 1), 1.0)
+        # the index along the condition's own dimension does not matter
+        assert close(bf(grid, V, Dim(1), ny + 1, 1), bf(grid, V, Dim(1), 1, 1))
+        assert close(bf(grid, V, Dim(2), 1, ny // 2 + 1), bf(grid, V, Dim(2), 1, 1))
+    full = (BoundaryFunction(lambda x, y: np.cos(x) * y, reduce_dims=False),
+            BoundaryFunction(lambda g, loc, dim, ix, iy: np.cos(coord(g, loc, ix, iy)[0]) * coord(g, loc, ix, iy)[1],
+                             discrete=True, reduce_dims=False))
+    for bf in full:
+        assert close(bf(grid, V, Dim(1), 1, 1), math.pi) and close(bf(grid, V, Dim(1), 1, ny + 1), -math.pi)
+        assert abs(float(bf(grid, V, Dim(1), 1, ny // 2 + 1))) <= tol
+        assert close(bf(grid, V, Dim(2), 1, 1), math.pi) and close(bf(grid, V, Dim(2), nx // 2 + 1, 1), -math.pi)
+    for bf in (BoundaryFunction(lambda x, eta: np.cos(x) * eta, parameters=math.pi),
+               BoundaryFunction(lambda g, loc, dim, i, eta: np.cos(coord(g, loc, dim, i)) * eta, discrete=True,
+                                parameters=math.pi)):
+        assert close(bf(grid, V, Dim(1), 1, 1), -math.pi) and close(bf(grid, V, Dim(1), 1, ny // 2 + 1), math.pi)
+        assert close(bf(grid, V, Dim(2), nx + 1, 1), -math.pi) and close(bf(grid, V, Dim(2), nx // 2 + 1, 1), math.pi)
+
+
+@pytest.mark.parametrize("T", TYPES)
+def test_bc_per_point_values_oracle(T):
+    """Per-point condition values (a BoundaryFunction and an array) through the oracle: the
+    ghost and boundary planes follow the same rules as constants, with the value of each
+    tangential index (a direct numpy evaluation of first_order_boundary_condition.jl:46-84)."""
+    from chmy_gb300.bcs import BoundaryFunction, materialize_bc
+
+    nx, ny = 9, 7
+    grid = UniformGrid(origin=(T(-1), T(-1)), extent=(T(2), T(2)), dims=(nx, ny), dtype=T)
+    rng = np.random.default_rng(3)
+    f = NpField(grid, (Vertex(), Center()))
+    f.a[...] = rng.standard_normal(f.a.shape).astype(T)
+    before = f.copy()
+    arr = rng.standard_normal(nx + 3).astype(T)  # y-sides: values over x indices 0..nx+2
+    bfun = BoundaryFunction(lambda y: 1.0 + y * y)
+    spec = {"x": (Dirichlet(bfun), Neumann(bfun)), "y": (Dirichlet(arr), Neumann(T(0.5)))}
+    b, keep = materialize_bc(grid, f.loc, T, spec)
+    bc_apply(grid, [f], [b])
+    a = before.a.copy()  # padded [y, x], logical I at I + 1
+    dx, dy = (float(v) for v in grid.spacing())
+    # y first: side 0 Dirichlet on a Center dimension (ghost row 0) from the array; side 1 Neumann
+    for i in range(0, nx + 3):
+        a[1, i + 1] = T(2) * (arr[i] - a[2, i + 1]) + a[2, i + 1]
+        a[ny + 2, i + 1] = T(dy) * T(0.5) + a[ny + 1, i + 1]
+    # then x: side 0 Dirichlet on a Vertex dimension (boundary node 1) = bfun(y of the Vertex point),
+    # side 1 Neumann on the Vertex dimension (ghost n+2) from node n+1 with the flipped (Center) location
+    for j in range(0, ny + 3):
+        yv = grid.axes[1].coord(Vertex(), j)
+        yc = grid.axes[1].coord(Center(), j)
+        a[j + 1, 2] = T(1.0 + yv * yv)
+        a[j + 1, nx + 3] = T(dx) * T(1.0 + yc * yc) + a[j + 1, nx + 2]
+    assert approx(f.a, a, T)
+    assert any(np.array_equal(k, arr) for k in keep)  # the array itself is what the library reads
