@@ -114,6 +114,48 @@ def interior(f: Field, with_halo: bool = False) -> torch.Tensor:
     return v.permute(*reversed(range(f.ndim)))
 
 
+def gather(f: Field, dst: np.ndarray | None = None, path=None) -> np.ndarray:
+    """gather!(arch, dst, src::Field) (src/Distributed/gather.jl:36-42) on one GPU: the interior
+    of `f` in a host array, x fastest (Julia's column-major order of the [x, y, z] interior,
+    stored here as a C-ordered [z, y, x] array). With `dst`, the values go there (its shape must
+    match). With `path`, the bytes are also written as a headless dump in that order."""
+    sl = tuple(slice(2 * h, 2 * h + n) for n, h in zip(reversed(f.dims), reversed(f.halo)))
+    a = f.data[sl].detach().cpu().numpy()
+    if dst is None:
+        dst = np.ascontiguousarray(a)
+    else:
+        if dst.shape != a.shape:
+            raise ValueError(f"gather: destination shape {dst.shape} != interior {a.shape}")
+        dst[...] = a
+    if path is not None:
+        np.ascontiguousarray(dst).tofile(path)
+    return dst
+
+
+def gather_blocks(blocks, dims) -> np.ndarray:
+    """The global array that gather! assembles from the local interiors of a Cartesian
+    decomposition (src/Distributed/gather.jl:9-33). `blocks[r]` is rank r's interior ([z, y, x]
+    stored, all of one shape). Rank r sits at the coordinates MPI_Cart_coords gives it for the
+    topology `dims` (x first): row-major, so the last dimension varies fastest. This is the
+    order of gather!'s displacements, which it builds over the reversed dims. The block at
+    coordinates (cx, cy, cz) fills [cz*nz:(cz+1)*nz, cy*ny:..., cx*nx:...]."""
+    dims = tuple(int(d) for d in dims)
+    nd = len(dims)
+    shp = blocks[0].shape
+    if len(blocks) != int(np.prod(dims)) or any(b.shape != shp for b in blocks):
+        raise ValueError("gather_blocks: one block of one shape per rank")
+    out = np.empty(tuple(s * d for s, d in zip(shp, reversed(dims))), dtype=blocks[0].dtype)
+    for r, b in enumerate(blocks):
+        c, rem = [], r
+        for d in reversed(range(nd)):  # row-major over (dims[0], ..., dims[N-1]): the last dim fastest
+            c.append(rem % dims[d])
+            rem //= dims[d]
+        c = list(reversed(c))  # c[d] = coordinate along dimension d
+        sl = tuple(slice(c[d] * shp[nd - 1 - d], (c[d] + 1) * shp[nd - 1 - d]) for d in reversed(range(nd)))
+        out[sl] = b
+    return out
+
+
 def evaluate(grid: UniformGrid, loc, dims, fun, discrete: bool = False, parameters=(), dtype=np.float64) -> np.ndarray:
     """Values of `fun` on the interior points of a field at `loc`, [x, y, z] indexed: the
     continuous form calls fun(coords..., params...) (_set_continuous!, field.jl:121-124); the

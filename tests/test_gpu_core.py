@@ -194,3 +194,21 @@ def test_bc_per_point_values_bitwise(arch, T, dims):
     arch.synchronize()
     for i, (a, b) in enumerate(zip(gpu, fields)):
         assert_close(a, b, 0, f"field {i}", exact=True)
+
+
+def test_gather_interior_and_dump(arch, tmp_path):
+    """gather! on one GPU: the interior of a (pitched) field as a host array, x fastest, and
+    the same bytes as a headless dump."""
+    from chmy_gb300 import gather
+
+    rng = np.random.default_rng(2)
+    grid = _grid((7, 5, 4), np.float64)
+    f = random_field(grid, (V_, C_, C_), np.float64, rng)
+    g = to_gpu(arch, f, pitch_align=128)
+    path = tmp_path / "interior.bin"
+    a = gather(g, path=str(path))
+    assert np.array_equal(a, f.interior())
+    assert np.array_equal(np.fromfile(path, dtype=np.float64), f.interior().ravel())
+    dst = np.empty_like(a)
+    gather(g, dst)
+    assert np.array_equal(dst, a)

@@ -427,3 +427,20 @@ def test_bc_per_point_values_oracle(T):
         a[j + 1, nx + 3] = T(dx) * T(1.0 + yc * yc) + a[j + 1, nx + 2]
     assert approx(f.a, a, T)
     assert any(np.array_equal(k, arr) for k in keep)  # the array itself is what the library reads
+
+
+def test_gather_blocks_cartesian_order():
+    """gather! (src/Distributed/gather.jl:9-33) places rank r's interior at the Cartesian
+    coordinates of r, row-major over the topology dims (the last dim fastest)."""
+    from chmy_gb300.fields import gather_blocks
+
+    rng = np.random.default_rng(1)
+    for dims, local in (((2, 3), (4, 5)), ((2, 2, 3), (3, 4, 2))):
+        nd = len(dims)
+        glob = rng.standard_normal(tuple(n * d for n, d in zip(reversed(local), reversed(dims))))
+        blocks = []
+        for r in range(int(np.prod(dims))):
+            c = np.unravel_index(r, dims)  # row-major rank -> coordinates (x first)
+            sl = tuple(slice(c[d] * local[d], (c[d] + 1) * local[d]) for d in reversed(range(nd)))
+            blocks.append(glob[sl].copy())
+        assert np.array_equal(gather_blocks(blocks, dims), glob)
