@@ -207,8 +207,9 @@ def test_gather_interior_and_dump(arch, tmp_path):
     g = to_gpu(arch, f, pitch_align=128)
     path = tmp_path / "interior.bin"
     a = gather(g, path=str(path))
-    assert np.array_equal(a, f.interior())
-    assert np.array_equal(np.fromfile(path, dtype=np.float64), f.interior().ravel())
+    ref = f.interior().transpose(2, 1, 0)  # [x, y, z] view -> stored [z, y, x]
+    assert np.array_equal(a, ref)
+    assert np.array_equal(np.fromfile(path, dtype=np.float64), np.ascontiguousarray(ref).ravel())
     dst = np.empty_like(a)
     gather(g, dst)
     assert np.array_equal(dst, a)
