@@ -11,7 +11,7 @@ Julia-to-Python name map: `set!` -> `set_`, `bc!` -> `bc_`, `f => bc` -> `(f, bc
 from ._abi import ChmyError, header_symbols, load_library
 from .architecture import Arch, GB300Backend, get_backend, get_device, heuristic_groupsize
 from .bcs import Batch, Dirichlet, Neumann, Periodic, batch, bc_
-from .fields import Field, TensorField, VectorField, gather, gather_blocks, interior, set_
+from .fields import Field, FieldMask, TensorField, VectorField, gather, gather_blocks, interior, set_
 from .grids import Center, Dim, Side, UniformGrid, Vertex, flip
 from .kernels import (
     CellViscosity,
@@ -55,6 +55,7 @@ __all__ = [
     "heuristic_groupsize",
     "interior",
     "gather",
+    "FieldMask",
     "gather_blocks",
     "load_library",
     "set_",

@@ -74,6 +74,10 @@ class cg_bc(C.Structure):
     _fields_ = [("kind", (C.c_int32 * 2) * 3), ("value", (C.c_double * 2) * 3), ("values", (C.c_void_p * 2) * 3)]
 
 
+class cg_mask(C.Structure):
+    _fields_ = [("at", cg_field * 8)]
+
+
 class cg_stokes_fields(C.Structure):
     _fields_ = [
         ("V", cg_field * 3),
@@ -177,6 +181,9 @@ SIGNATURES: dict[str, list] = {
     "cg_diffusion_update_C": [_vp, P(cg_grid), P(cg_field), P(cg_field), C.c_double],
     "cg_diffusion_step": [_vp, P(cg_grid), P(cg_field), P(cg_field), C.c_double, C.c_double, P(cg_bc)],
     "cg_diffusion_run": [_vp, P(cg_grid), P(cg_field), P(cg_field), C.c_double, C.c_double, P(cg_bc), C.c_int],
+    "cg_diffusion_compute_q_masked": [_vp, P(cg_grid), P(cg_field), P(cg_field), C.c_double, P(cg_mask)],
+    "cg_diffusion_update_C_masked": [_vp, P(cg_grid), P(cg_field), P(cg_field), C.c_double, P(cg_mask)],
+    "cg_diffusion_run_masked": [_vp, P(cg_grid), P(cg_field), P(cg_field), C.c_double, C.c_double, P(cg_bc), P(cg_mask), C.c_int],
     "cg_stokes_update_old": [_vp, P(cg_grid), P(cg_stokes_fields)],
     "cg_stokes_update_stress": [_vp, P(cg_grid), P(cg_stokes_fields), P(cg_stokes_params)],
     "cg_stokes_update_velocity": [_vp, P(cg_grid), P(cg_stokes_fields), P(cg_stokes_params)],

@@ -114,6 +114,35 @@ def interior(f: Field, with_halo: bool = False) -> torch.Tensor:
     return v.permute(*reversed(range(f.ndim)))
 
 
+class FieldMask:
+    """FieldMask(arch, grid, type) (src/GridOperators/field_mask.jl:1-117): one weight field at
+    each of the 2^N locations, read by the masked operators as at(ω, loc, I). `at(loc)` returns
+    the field at a location; `desc()` is the library's cg_mask, indexed by location bits
+    (Vertex along d = bit d)."""
+
+    def __init__(self, arch, grid: UniformGrid, dtype=None, **field_kwargs):
+        from .grids import Center, Vertex
+
+        self.grid = grid
+        nd = grid.ndim
+        self.fields = {}
+        for bits in range(1 << nd):
+            loc = tuple(Vertex() if (bits >> d) & 1 else Center() for d in range(nd))
+            self.fields[bits] = Field(arch, grid, loc, dtype, **field_kwargs)
+
+    def at(self, loc) -> Field:
+        from .grids import Vertex, expand_loc
+
+        locs = expand_loc(self.grid.ndim, loc)
+        return self.fields[sum(1 << d for d, l in enumerate(locs) if isinstance(l, Vertex))]
+
+    def desc(self) -> _abi.cg_mask:
+        m = _abi.cg_mask()
+        for bits, f in self.fields.items():
+            m.at[bits] = f.desc()
+        return m
+
+
 def gather(f: Field, dst: np.ndarray | None = None, path=None) -> np.ndarray:
     """gather!(arch, dst, src::Field) (src/Distributed/gather.jl:36-42) on one GPU: the interior
     of `f` in a host array, x fastest (Julia's column-major order of the [x, y, z] interior,

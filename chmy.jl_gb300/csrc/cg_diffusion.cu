@@ -73,6 +73,69 @@ __global__ void diffusion_step_kernel(DF<T> Co, DF<T> Ci, T mchi, T dt, Spacing<
     Co(i, j, k) = c - dt * dv;
 }
 
+// ---- masked operators (src/GridOperators/masked_operators.jl:11-39) --------------------------
+// A masked operator multiplies every operand value by the mask at the operand's location and
+// index: the masked ∂_d of Center C at face I is (C[I] w_c[I] - C[I-e_d] w_c[I-e_d]) iΔ_d, and
+// the masked divg of q is Σ_d (q_d[I+e_d] w_d[I+e_d] - q_d[I] w_d[I]) iΔ_d (masked_field_
+// operators.jl:52-57). w_c is the Center mask, w_d the mask at the d-face location (Vertex
+// along d).
+template <class T>
+struct MaskV {
+    DF<T> c, f[3];
+};
+
+template <class T, int ND>
+__global__ void compute_q_masked_kernel(DF<T> q0, DF<T> q1, DF<T> q2, DF<T> C, const MaskV<T> w, T mchi, Spacing<T> s,
+                                        int e0, int e1) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = ND > 1 ? blockIdx.y * blockDim.y + threadIdx.y : 0;
+    const int k = ND > 2 ? blockIdx.z : 0;
+    if (i > e0 || j > e1) return;
+    const T cw = C(i, j, k) * w.c(i, j, k);
+    q0(i, j, k) = mchi * ((cw - C(i - 1, j, k) * w.c(i - 1, j, k)) * s.i[0]);
+    if (ND > 1) q1(i, j, k) = mchi * ((cw - C(i, j - 1, k) * w.c(i, j - 1, k)) * s.i[1]);
+    if (ND > 2) q2(i, j, k) = mchi * ((cw - C(i, j, k - 1) * w.c(i, j, k - 1)) * s.i[2]);
+}
+
+template <class T, int ND>
+__global__ void update_C_masked_kernel(DF<T> C, DF<T> q0, DF<T> q1, DF<T> q2, const MaskV<T> w, T dt, Spacing<T> s,
+                                       int e0, int e1) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = ND > 1 ? blockIdx.y * blockDim.y + threadIdx.y : 0;
+    const int k = ND > 2 ? blockIdx.z : 0;
+    if (i > e0 || j > e1) return;
+    T dv = (q0(i + 1, j, k) * w.f[0](i + 1, j, k) - q0(i, j, k) * w.f[0](i, j, k)) * s.i[0];
+    if (ND > 1) dv = dv + (q1(i, j + 1, k) * w.f[1](i, j + 1, k) - q1(i, j, k) * w.f[1](i, j, k)) * s.i[1];
+    if (ND > 2) dv = dv + (q2(i, j, k + 1) * w.f[2](i, j, k + 1) - q2(i, j, k) * w.f[2](i, j, k)) * s.i[2];
+    C(i, j, k) = C(i, j, k) - dt * dv;
+}
+
+// Fused masked compute_q! + update_C! (a flux at index n+2 reads as zero, as in the unmasked
+// fused step)
+template <class T, int ND>
+__global__ void diffusion_step_masked_kernel(DF<T> Co, DF<T> Ci, const MaskV<T> w, T mchi, T dt, Spacing<T> s, int e0,
+                                             int e1, int e2) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = ND > 1 ? blockIdx.y * blockDim.y + threadIdx.y : 0;
+    const int k = ND > 2 ? blockIdx.z : 0;
+    if (i > e0 || j > e1) return;
+    const T c = Ci(i, j, k);
+    const T cw = c * w.c(i, j, k);
+    const int I[3] = {i, j, k}, E[3] = {e0, e1, e2};
+    T dv = T(0);
+#pragma unroll
+    for (int d = 0; d < ND; ++d) {
+        const int di = d == 0, dj = d == 1, dk = d == 2;
+        const T ql = mchi * ((cw - Ci(i - di, j - dj, k - dk) * w.c(i - di, j - dj, k - dk)) * s.i[d]);
+        const T qr = I[d] + 1 <= E[d]
+                         ? mchi * ((Ci(i + di, j + dj, k + dk) * w.c(i + di, j + dj, k + dk) - cw) * s.i[d])
+                         : T(0);
+        const T t = (qr * w.f[d](i + di, j + dj, k + dk) - ql * w.f[d](i, j, k)) * s.i[d];
+        dv = d == 0 ? t : dv + t;
+    }
+    Co(i, j, k) = c - dt * dv;
+}
+
 template <class T>
 Spacing<T> spacing_of(const cg_grid* g) {
     Spacing<T> s;
@@ -115,6 +178,58 @@ int step_t(cg_ctx* ctx, const cg_grid* g, const cg_field* Co, const cg_field* Ci
         cg_view<T>(*Co), cg_view<T>(*Ci), -(T)chi, (T)dt, spacing_of<T>(g), g->n[0] + 1,
         ND > 1 ? g->n[1] + 1 : 0, ND > 2 ? g->n[2] + 1 : 0);
     CG_CHECK_LAUNCH(ctx);
+    return CG_OK;
+}
+
+template <class T>
+MaskV<T> mask_view(const cg_mask* m, int nd) {
+    MaskV<T> w;
+    std::memset(&w, 0, sizeof(w));
+    w.c = cg_view<T>(m->at[0]);
+    for (int d = 0; d < nd; ++d) w.f[d] = cg_view<T>(m->at[1 << d]);
+    return w;
+}
+
+template <class T, int ND>
+int compute_q_masked_t(cg_ctx* ctx, const cg_grid* g, const cg_field* q, const cg_field* C, double chi, const cg_mask* m) {
+    const dim3 block = block_for<ND>();
+    DF<T> Q[3] = {cg_view<T>(q[0]), ND > 1 ? cg_view<T>(q[1]) : DF<T>{}, ND > 2 ? cg_view<T>(q[2]) : DF<T>{}};
+    compute_q_masked_kernel<T, ND><<<range_grid<ND>(g, block), block, 0, ctx->stream>>>(
+        Q[0], Q[1], Q[2], cg_view<T>(*C), mask_view<T>(m, ND), -(T)chi, spacing_of<T>(g), g->n[0] + 1,
+        ND > 1 ? g->n[1] + 1 : 0);
+    CG_CHECK_LAUNCH(ctx);
+    return CG_OK;
+}
+
+template <class T, int ND>
+int update_C_masked_t(cg_ctx* ctx, const cg_grid* g, const cg_field* C, const cg_field* q, double dt, const cg_mask* m) {
+    const dim3 block = block_for<ND>();
+    DF<T> Q[3] = {cg_view<T>(q[0]), ND > 1 ? cg_view<T>(q[1]) : DF<T>{}, ND > 2 ? cg_view<T>(q[2]) : DF<T>{}};
+    update_C_masked_kernel<T, ND><<<range_grid<ND>(g, block), block, 0, ctx->stream>>>(
+        cg_view<T>(*C), Q[0], Q[1], Q[2], mask_view<T>(m, ND), (T)dt, spacing_of<T>(g), g->n[0] + 1,
+        ND > 1 ? g->n[1] + 1 : 0);
+    CG_CHECK_LAUNCH(ctx);
+    return CG_OK;
+}
+
+template <class T, int ND>
+int step_masked_t(cg_ctx* ctx, const cg_grid* g, const cg_field* Co, const cg_field* Ci, double chi, double dt,
+                  const cg_mask* m) {
+    const dim3 block = block_for<ND>();
+    diffusion_step_masked_kernel<T, ND><<<range_grid<ND>(g, block), block, 0, ctx->stream>>>(
+        cg_view<T>(*Co), cg_view<T>(*Ci), mask_view<T>(m, ND), -(T)chi, (T)dt, spacing_of<T>(g), g->n[0] + 1,
+        ND > 1 ? g->n[1] + 1 : 0, ND > 2 ? g->n[2] + 1 : 0);
+    CG_CHECK_LAUNCH(ctx);
+    return CG_OK;
+}
+
+// The mask entries the diffusion kernels read: Center and the ndim face locations.
+int check_mask(cg_ctx* ctx, const cg_grid* grid, const cg_mask* m, int dtype) {
+    if (!m) return cg_fail(ctx, CG_ERR_ARG, "masked diffusion: NULL mask");
+    int rc = cg_check_field(ctx, grid, m->at[0], dtype, 0, "mask (Center)");
+    if (rc) return rc;
+    for (int d = 0; d < grid->ndim; ++d)
+        if ((rc = cg_check_field(ctx, grid, m->at[1 << d], dtype, 1 << d, "mask (face)"))) return rc;
     return CG_OK;
 }
 
@@ -197,6 +312,63 @@ extern "C" int cg_diffusion_run(cg_ctx* ctx, const cg_grid* grid, const cg_field
             const cg_field* out = (s % 2 == 0) ? B : A;
             int r = step_checked(ctx, grid, out, in, chi, dt, bc);
             if (r) return r;
+        }
+        return (int)CG_OK;
+    });
+}
+
+// ---- masked forms -------------------------------------------------------------------------
+
+extern "C" int cg_diffusion_compute_q_masked(cg_ctx* ctx, const cg_grid* grid, const cg_field* q, const cg_field* C,
+                                             double chi, const cg_mask* mask) {
+    int rc = cg_check_grid(ctx, grid);
+    if (rc) return rc;
+    if (!q || !C) return cg_fail(ctx, CG_ERR_ARG, "cg_diffusion_compute_q_masked: NULL field");
+    cudaSetDevice(ctx->device);
+    if ((rc = cg_check_field(ctx, grid, *C, C->dtype, 0, "C"))) return rc;
+    if ((rc = check_q(ctx, grid, q, C->dtype))) return rc;
+    if ((rc = check_mask(ctx, grid, mask, C->dtype))) return rc;
+    return CG_DISPATCH(compute_q_masked_t, C->dtype, grid->ndim, ctx, grid, q, C, chi, mask);
+}
+
+extern "C" int cg_diffusion_update_C_masked(cg_ctx* ctx, const cg_grid* grid, const cg_field* C, const cg_field* q,
+                                            double dt, const cg_mask* mask) {
+    int rc = cg_check_grid(ctx, grid);
+    if (rc) return rc;
+    if (!q || !C) return cg_fail(ctx, CG_ERR_ARG, "cg_diffusion_update_C_masked: NULL field");
+    cudaSetDevice(ctx->device);
+    if ((rc = cg_check_field(ctx, grid, *C, C->dtype, 0, "C"))) return rc;
+    if ((rc = check_q(ctx, grid, q, C->dtype))) return rc;
+    if ((rc = check_mask(ctx, grid, mask, C->dtype))) return rc;
+    return CG_DISPATCH(update_C_masked_t, C->dtype, grid->ndim, ctx, grid, C, q, dt, mask);
+}
+
+extern "C" int cg_diffusion_run_masked(cg_ctx* ctx, const cg_grid* grid, const cg_field* A, const cg_field* B,
+                                       double chi, double dt, const cg_bc* bc, const cg_mask* mask, int nsteps) {
+    int rc = step_args(ctx, grid, B, A);
+    if (rc) return rc;
+    if (nsteps < 0) return cg_fail(ctx, CG_ERR_ARG, "cg_diffusion_run_masked: nsteps < 0");
+    if ((rc = check_mask(ctx, grid, mask, A->dtype))) return rc;
+    if (nsteps == 0) return CG_OK;
+    cudaSetDevice(ctx->device);
+    std::string key = "diffusion_run_masked";
+    cg_key_add(key, *grid);
+    cg_key_add(key, *A);
+    cg_key_add(key, *B);
+    cg_key_add(key, *mask);
+    cg_key_add(key, chi);
+    cg_key_add(key, dt);
+    cg_key_add(key, nsteps);
+    cg_bc none;
+    std::memset(&none, 0, sizeof(none));
+    cg_key_add(key, bc ? *bc : none);
+    return cg_graph_run(ctx, key, [&](cudaStream_t) {
+        for (int s = 0; s < nsteps; ++s) {
+            const cg_field* in = (s % 2 == 0) ? A : B;
+            const cg_field* out = (s % 2 == 0) ? B : A;
+            int r = CG_DISPATCH(step_masked_t, in->dtype, grid->ndim, ctx, grid, out, in, chi, dt, mask);
+            if (r) return r;
+            if (bc && (r = cg_bc_apply_impl(ctx, grid, 1, out, bc))) return r;
         }
         return (int)CG_OK;
     });

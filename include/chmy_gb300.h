@@ -98,6 +98,15 @@ typedef struct cg_bc {
     const void* values[3][2];
 } cg_bc;
 
+/* FieldMask (src/GridOperators/field_mask.jl:1-117): one weight field per location. at[m] is
+ * the mask at the location whose bit d is set for Vertex along dimension d (2D: 0 = (C,C),
+ * 1 = (V,C), 2 = (C,V), 3 = (V,V); 3D up to 7 = (V,V,V)). Entries an operation does not read
+ * may be empty. A masked operator multiplies every operand value by the mask at the operand's
+ * location and index (src/GridOperators/masked_operators.jl:11-39). */
+typedef struct cg_mask {
+    cg_field at[8];
+} cg_mask;
+
 typedef struct cg_ctx cg_ctx;
 
 /* ---- context and memory ----------------------------------------------------------- */
@@ -184,6 +193,17 @@ CG_API int cg_diffusion_step(cg_ctx* ctx, const cg_grid* grid, const cg_field* C
  * else in B), captured once into a CUDA graph and replayed. */
 CG_API int cg_diffusion_run(cg_ctx* ctx, const cg_grid* grid, const cg_field* A, const cg_field* B,
                      double chi, double dt, const cg_bc* bc, int nsteps);
+
+/* The same with the masked operators: q.d = -chi * ∂d(C, ω) and C -= dt * divg(q, ω)
+ * (masked_field_operators.jl:20-57): the Center mask at[0] weighs C, the d-face mask at[1 << d]
+ * weighs q.d. No reference example runs them; the oracle restates the operators. */
+CG_API int cg_diffusion_compute_q_masked(cg_ctx* ctx, const cg_grid* grid, const cg_field* q,
+                                         const cg_field* C, double chi, const cg_mask* mask);
+CG_API int cg_diffusion_update_C_masked(cg_ctx* ctx, const cg_grid* grid, const cg_field* C,
+                                        const cg_field* q, double dt, const cg_mask* mask);
+/* nsteps fused masked steps A -> B -> A ... with bc!(C => bc) after each, one CUDA graph. */
+CG_API int cg_diffusion_run_masked(cg_ctx* ctx, const cg_grid* grid, const cg_field* A, const cg_field* B,
+                                   double chi, double dt, const cg_bc* bc, const cg_mask* mask, int nsteps);
 
 /* ---- viscoelastic Stokes (examples/stokes_{2,3}d_inc_ve_T.jl) ---------------------- */
 

@@ -285,6 +285,44 @@ int bc_apply_t(const cg_grid* grid, int nfields, const cg_field* fields, const c
     return CG_OK;
 }
 
+/* ---- masked operators (src/GridOperators/masked_operators.jl:11-39) --------------------
+ * Every operand value is multiplied by the mask at the operand's location and index:
+ * left(f, ω) = f[Il] at(ω, loc(f), Il), right likewise, δ = right - left, ∂ = δ iΔ. The mask
+ * is one weight field per location, indexed by the location's bits (Vertex along d = bit d). */
+struct Mask {
+    const cg_mask* m;
+    template <class T>
+    T at(const Fd<T>& f, const int* I) const {
+        int bits = 0;
+        for (int d = 0; d < 3; ++d)
+            if (f.loc[d] == CG_VERTEX) bits |= 1 << d;
+        return Fd<T>(m->at[bits]).at(I);
+    }
+};
+template <class T>
+inline T mleft(const Fd<T>& f, const Mask& w, int d, int i, int j, int k) {
+    int I[3] = {i, j, k};
+    if (f.loc[d] == CG_CENTER) I[d] -= 1;
+    return f.at(I) * w.at(f, I);
+}
+template <class T>
+inline T mright(const Fd<T>& f, const Mask& w, int d, int i, int j, int k) {
+    int I[3] = {i, j, k};
+    if (f.loc[d] == CG_VERTEX) I[d] += 1;
+    return f.at(I) * w.at(f, I);
+}
+template <class T>
+inline T mpartial(const Fd<T>& f, const Mask& w, const GridT<T>& g, int d, int i, int j, int k) {
+    return (mright(f, w, d, i, j, k) - mleft(f, w, d, i, j, k)) * g.idx[d];
+}
+/* divg(V, ω, grid, I) = Σ_d ∂(V_d, ω, grid, d, I) in dim order (masked_field_operators.jl:52-57) */
+template <class T>
+inline T mdivg(const Fd<T>* V, const Mask& w, const GridT<T>& g, int i, int j, int k) {
+    T s = mpartial(V[0], w, g, 0, i, j, k);
+    for (int d = 1; d < g.nd; ++d) s = s + mpartial(V[d], w, g, d, i, j, k);
+    return s;
+}
+
 /* ---- explicit diffusion (examples/diffusion_2d.jl:8-19) ---------------------------- */
 
 template <class T>
@@ -307,6 +345,33 @@ void diffusion_update_C_t(const cg_grid* grid, const cg_field* C, const cg_field
     for (int d = 0; d < g.nd; ++d) Q[d] = Fd<T>(q[d]);
     const T Dt = (T)dt;
     launch_range(g, [&](int i, int j, int k) { c(i, j, k) = c(i, j, k) - Dt * divg(Q, g, i, j, k); });
+}
+
+/* the same kernels with the masked operators: q.d = -χ ∂d(C, ω), C -= dt divg(q, ω) */
+template <class T>
+void diffusion_compute_q_masked_t(const cg_grid* grid, const cg_field* q, const cg_field* C, double chi,
+                                  const cg_mask* m) {
+    GridT<T> g(*grid);
+    Fd<T> c(*C);
+    Fd<T> Q[3];
+    for (int d = 0; d < g.nd; ++d) Q[d] = Fd<T>(q[d]);
+    const Mask w{m};
+    const T mchi = -(T)chi;
+    launch_range(g, [&](int i, int j, int k) {
+        for (int d = 0; d < g.nd; ++d) Q[d](i, j, k) = mchi * mpartial(c, w, g, d, i, j, k);
+    });
+}
+
+template <class T>
+void diffusion_update_C_masked_t(const cg_grid* grid, const cg_field* C, const cg_field* q, double dt,
+                                 const cg_mask* m) {
+    GridT<T> g(*grid);
+    Fd<T> c(*C);
+    Fd<T> Q[3];
+    for (int d = 0; d < g.nd; ++d) Q[d] = Fd<T>(q[d]);
+    const Mask w{m};
+    const T Dt = (T)dt;
+    launch_range(g, [&](int i, int j, int k) { c(i, j, k) = c(i, j, k) - Dt * mdivg(Q, w, g, i, j, k); });
 }
 
 /* ---- VE Stokes (examples/stokes_{2,3}d_inc_ve_T.jl) -------------------------------- */
@@ -786,6 +851,20 @@ int or_maxabs(int nfields, const cg_field* fields, double* out, int32_t* nonfini
 int or_diffusion_compute_q(const cg_grid* grid, const cg_field* q, const cg_field* C, double chi) {
     if (C->dtype == CG_F64) diffusion_compute_q_t<double>(grid, q, C, chi);
     else diffusion_compute_q_t<float>(grid, q, C, chi);
+    return CG_OK;
+}
+
+int or_diffusion_compute_q_masked(const cg_grid* grid, const cg_field* q, const cg_field* C, double chi,
+                                  const cg_mask* m) {
+    if (C->dtype == CG_F64) diffusion_compute_q_masked_t<double>(grid, q, C, chi, m);
+    else diffusion_compute_q_masked_t<float>(grid, q, C, chi, m);
+    return CG_OK;
+}
+
+int or_diffusion_update_C_masked(const cg_grid* grid, const cg_field* C, const cg_field* q, double dt,
+                                 const cg_mask* m) {
+    if (C->dtype == CG_F64) diffusion_update_C_masked_t<double>(grid, C, q, dt, m);
+    else diffusion_update_C_masked_t<float>(grid, C, q, dt, m);
     return CG_OK;
 }
 

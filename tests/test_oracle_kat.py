@@ -444,3 +444,72 @@ def test_gather_blocks_cartesian_order():
             sl = tuple(slice(c[d] * local[d], (c[d] + 1) * local[d]) for d in reversed(range(nd)))
             blocks.append(glob[sl].copy())
         assert np.array_equal(gather_blocks(blocks, dims), glob)
+
+
+def _np_mask_set(grid, T, rng, ones=False):
+    """Host mask fields at every location (the oracle's cg_mask), random in [0, 1] or ones."""
+    nd = grid.ndim
+    fields = {}
+    for bits in range(1 << nd):
+        loc = tuple(Vertex() if (bits >> d) & 1 else Center() for d in range(nd))
+        f = NpField(grid, loc, T)
+        f.a[...] = 1 if ones else rng.random(f.a.shape).astype(T)
+        fields[bits] = f
+    m = _abi.cg_mask()
+    for bits, f in fields.items():
+        m.at[bits] = f.desc()
+    return fields, m
+
+
+@pytest.mark.parametrize("T", TYPES)
+def test_masked_diffusion_oracle(T):
+    """Masked operators (masked_operators.jl:11-39) in the oracle's diffusion kernels: with
+    ones they equal the unmasked kernels bit for bit; with random weights they equal a numpy
+    evaluation of q.x = -chi ∂x(C, ω) and C -= dt divg(q, ω)."""
+    import ctypes
+
+    from _oracle import lib
+
+    rng = np.random.default_rng(5)
+    grid = UniformGrid(origin=(T(-1), T(-1)), extent=(T(2), T(2)), dims=(9, 7), dtype=T)
+    g = grid.desc()
+    C0 = NpField(grid, Center(), T)
+    C0.a[...] = rng.standard_normal(C0.a.shape).astype(T)
+    chi, dt = 1.3, 1e-3
+
+    def run(masked, m):
+        C = C0.copy()
+        q = vec_fields(grid, T)
+        qa = (_abi.cg_field * 3)(q[0].desc(), q[1].desc(), _abi.cg_field())
+        if masked:
+            assert lib().or_diffusion_compute_q_masked(ctypes.byref(g), qa, ctypes.byref(C.desc()), chi, ctypes.byref(m)) == 0
+            assert lib().or_diffusion_update_C_masked(ctypes.byref(g), ctypes.byref(C.desc()), qa, dt, ctypes.byref(m)) == 0
+        else:
+            assert lib().or_diffusion_compute_q(ctypes.byref(g), qa, ctypes.byref(C.desc()), chi) == 0
+            assert lib().or_diffusion_update_C(ctypes.byref(g), ctypes.byref(C.desc()), qa, dt) == 0
+        return C, q
+
+    _, ones = _np_mask_set(grid, T, rng, ones=True)
+    Cm, qm = run(True, ones)
+    Cu, qu = run(False, None)
+    assert np.array_equal(Cm.a, Cu.a) and np.array_equal(qm[0].a, qu[0].a) and np.array_equal(qm[1].a, qu[1].a)
+    wf, wm = _np_mask_set(grid, T, rng)
+    Cm, qm = run(True, wm)
+    c, wc, wx, wy = C0.a, wf[0].a, wf[1].a, wf[2].a
+    idx, idy = (float(v) for v in grid.inv_spacing())
+    nx, ny = grid.dims
+    qx = np.zeros_like(qm[0].a)
+    qy = np.zeros_like(qm[1].a)
+    for j in range(0, ny + 2):  # launch range [0, n+1], logical I at padded I + 1
+        for i in range(0, nx + 2):
+            J, Ip = j + 1, i + 1
+            qx[J, Ip] = -chi * ((c[J, Ip] * wc[J, Ip] - c[J, Ip - 1] * wc[J, Ip - 1]) * idx)
+            qy[J, Ip] = -chi * ((c[J, Ip] * wc[J, Ip] - c[J - 1, Ip] * wc[J - 1, Ip]) * idy)
+    cn = c.copy()
+    for j in range(0, ny + 2):
+        for i in range(0, nx + 2):
+            J, Ip = j + 1, i + 1
+            dv = (qx[J, Ip + 1] * wx[J, Ip + 1] - qx[J, Ip] * wx[J, Ip]) * idx
+            dv += (qy[J + 1, Ip] * wy[J + 1, Ip] - qy[J, Ip] * wy[J, Ip]) * idy
+            cn[J, Ip] = c[J, Ip] - dt * dv
+    assert approx(qm[0].a, qx, T) and approx(qm[1].a, qy, T) and approx(Cm.a, cn, T)
