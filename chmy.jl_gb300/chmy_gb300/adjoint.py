@@ -133,7 +133,8 @@ class SIA:
     A step reads only H (the flux is recomputed from it), so a checkpoint is one copy of H. The
     forward sweep keeps every `checkpoint_every`-th state. The reverse sweep recomputes each
     segment's states from its checkpoint, then runs cg_sia_adjoint_step over them backwards.
-    Memory: nsteps / checkpoint_every + checkpoint_every states."""
+    Memory: nsteps / checkpoint_every + checkpoint_every states. checkpoint_every = 1 keeps
+    every state and recomputes nothing."""
 
     def __init__(self, arch, grid, B: np.ndarray, params, dtype=np.float64):
         self.arch, self.grid, self.params = arch, grid, params
@@ -145,11 +146,12 @@ class SIA:
         self.lam = [Field(arch, grid, C, dtype), Field(arch, grid, C, dtype)]
         self._q = (_abi.cg_field * 3)(self.q[0].desc(), self.q[1].desc(), _abi.cg_field())
 
-    def _steps(self, nsteps: int) -> float:
+    def _steps(self, nsteps: int, timed: bool = False) -> float:
+        """`nsteps` forward steps in one call; the model time (which synchronises) if `timed`."""
         t = ctypes.c_double()
         if nsteps > 0:
             self.arch.call("cg_sia_run", ctypes.byref(self.grid.desc()), ctypes.byref(self.H.desc()), ctypes.byref(self.B.desc()),
-                           self._q, ctypes.byref(self.params), int(nsteps), ctypes.byref(t))
+                           self._q, ctypes.byref(self.params), int(nsteps), ctypes.byref(t) if timed else None)
         return t.value
 
     def run(self, H0: np.ndarray, nsteps: int) -> np.ndarray:
@@ -158,16 +160,22 @@ class SIA:
         self._steps(nsteps)
         return self.H.to_numpy()
 
+    def reset_accumulators(self) -> None:
+        """Drop dJ/dGamma and dJ/dela sums left on the device by an interrupted reverse sweep."""
+        tmp = (ctypes.c_double * 2)()
+        self.arch.call("cg_sia_adjoint_step", ctypes.byref(self.grid.desc()), ctypes.byref(self.H.desc()), ctypes.byref(self.B.desc()),
+                       ctypes.byref(self.params), ctypes.byref(self.lam[0].desc()), ctypes.byref(self.lam[1].desc()), tmp)
+
     def gradient(self, H0: np.ndarray, nsteps: int, misfit_grad, checkpoint_every: int | None = None):
         """(dJ/dGamma, dJ/dela, dJ/dH0, H^N). `misfit_grad(HN)` returns dJ/dH^N as a padded host
         array (its interior is used)."""
         K = int(checkpoint_every or max(1, math.ceil(math.sqrt(nsteps))))
         self.H.from_numpy(H0)
+        self.reset_accumulators()
         checkpoints = {}
-        for n in range(nsteps):
-            if n % K == 0:
-                checkpoints[n] = self.H.data.clone()
-            self._steps(1)
+        for n in range(0, nsteps, K):
+            checkpoints[n] = self.H.data.clone()
+            self._steps(min(K, nsteps - n))
         HN = self.H.to_numpy()
         self.lam[0].from_numpy(misfit_grad(HN))
         dJ = (ctypes.c_double * 2)(0.0, 0.0)
@@ -176,14 +184,16 @@ class SIA:
         for start in sorted(checkpoints, reverse=True):
             stop = min(start + K, nsteps)
             self.H.data.copy_(checkpoints[start])
-            states = []
-            for _ in range(start, stop):
-                states.append(self.H.data.clone())
+            states = [self.H.data.clone()]
+            for _ in range(start + 1, stop):  # H^start+1 .. H^stop-1 (H^stop is not needed)
                 self._steps(1)
+                states.append(self.H.data.clone())
             for n in range(stop - 1, start - 1, -1):
                 self.H.data.copy_(states[n - start])
+                # dJ/dGamma and dJ/dela accumulate on the device; the last step reads them
                 self.arch.call("cg_sia_adjoint_step", ctypes.byref(g), ctypes.byref(self.H.desc()), ctypes.byref(self.B.desc()),
-                               ctypes.byref(self.params), ctypes.byref(self.lam[cur].desc()), ctypes.byref(self.lam[1 - cur].desc()), dJ)
+                               ctypes.byref(self.params), ctypes.byref(self.lam[cur].desc()), ctypes.byref(self.lam[1 - cur].desc()),
+                               dJ if n == 0 else None)
                 cur = 1 - cur
             del states
         return dJ[0], dJ[1], self.lam[cur].to_numpy(), HN

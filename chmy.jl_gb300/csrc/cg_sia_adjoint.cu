@@ -28,6 +28,7 @@
 // neighbours, so no two threads write one address. The forward quantities are recomputed
 // from H with the arithmetic of cg_sia_run, so the masks and Dmax match the forward step.
 #include <cmath>
+#include <cstddef>
 
 #include "cg_common.cuh"
 #include "cg_sia_kernels.cuh"
@@ -43,8 +44,8 @@ struct SiaAdj {
     int n, nx, ny;
 };
 
-// device words: [0] Dmax bits, [1] argmax index, [2] dt, [3] capped, [4] dJ/ddt, [5] dJ/dGamma,
-// [6] dJ/dela
+// device words: the step's Dmax bits, argmax index, dt, capped flag and dJ/ddt (reset every
+// step), then dJ/dGamma and dJ/dela accumulated over the steps until a call reads them
 struct SiaWords {
     unsigned long long dmax;
     unsigned long long arg;
@@ -150,10 +151,11 @@ __device__ __forceinline__ double block_sum(double x) {
 }
 
 // Sums over the blocks' partials in a fixed order (one block of 256 threads): for each of the
-// `narr` arrays part[k][0..nblocks), dst_k (+)= sum_b part[k][b].
+// `narr` arrays part[k][0..nblocks), dst_k = (acc_k ? dst_k : 0) + sum_b part[k][b].
 // The per-block partials and this ordered sum keep the gradients reproducible bit for bit,
 // where atomic adds would round in arrival order.
-__global__ void adj_sum_kernel(const double* part, int nblocks, int narr, double* dst0, double* dst1, int accumulate) {
+__global__ void adj_sum_kernel(const double* part, int nblocks, int narr, double* dst0, double* dst1, int acc0,
+                               int acc1) {
     __shared__ double red[256];
     for (int k = 0; k < narr; ++k) {
         const double* a = part + (size_t)k * nblocks;
@@ -167,7 +169,8 @@ __global__ void adj_sum_kernel(const double* part, int nblocks, int narr, double
         }
         if (threadIdx.x == 0) {
             double* d = k == 0 ? dst0 : dst1;
-            if (d) *d = accumulate ? *d + red[0] : red[0];
+            const int acc = k == 0 ? acc0 : acc1;
+            if (d) *d = acc ? *d + red[0] : red[0];
         }
         __syncthreads();
     }
@@ -339,21 +342,37 @@ int adjoint_step_t(cg_ctx* ctx, const cg_grid* g, const cg_field* H, const cg_fi
     v.ny = g->n[1];
     const double dx = std::min(g->spacing[0], g->spacing[1]);
     const double dx2 = (double)((T)dx * (T)dx);
-    CG_CUDA(ctx, cudaMemsetAsync(w, 0, sizeof(SiaWords), ctx->stream));
-    adj_D_kernel<T><<<grid, block, 0, ctx->stream>>>(v, w);
-    adj_dt_kernel<T><<<1, 1, 0, ctx->stream>>>(w, dx2, p->cfl, p->dt_max);
-    adj_arg_kernel<T><<<grid, block, 0, ctx->stream>>>(v, w);
-    adj_mu_kernel<T><<<grid, block, 0, ctx->stream>>>(v, w, part, nblocks);
-    adj_sum_kernel<<<1, 256, 0, ctx->stream>>>(part, nblocks, 2, &w->dJdt, &w->gE, 0);
-    adj_D_back_kernel<T><<<grid, block, 0, ctx->stream>>>(v, w, part + 2 * (size_t)nblocks);
-    adj_sum_kernel<<<1, 256, 0, ctx->stream>>>(part + 2 * (size_t)nblocks, nblocks, 1, &w->gG, nullptr, 0);
-    adj_out_kernel<T><<<grid, block, 0, ctx->stream>>>(v);
-    CG_CHECK_LAUNCH(ctx);
-    SiaWords hw;
-    CG_CUDA(ctx, cudaMemcpyAsync(&hw, w, sizeof(hw), cudaMemcpyDeviceToHost, ctx->stream));
-    CG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    dJ[0] += hw.gG;
-    dJ[1] += hw.gE;
+    // one graph per argument set: reset the step's words, then the reverse step's kernels
+    std::string key = "sia_adjoint_step";
+    cg_key_add(key, *g);
+    cg_key_add(key, *H);
+    cg_key_add(key, *B);
+    cg_key_add(key, *lam);
+    cg_key_add(key, *lam_out);
+    cg_key_add(key, *p);
+    cg_key_add(key, base);
+    rc = cg_graph_run(ctx, key, [&](cudaStream_t st) {
+        CG_CUDA(ctx, cudaMemsetAsync(w, 0, offsetof(SiaWords, gG), st));
+        adj_D_kernel<T><<<grid, block, 0, st>>>(v, w);
+        adj_dt_kernel<T><<<1, 1, 0, st>>>(w, dx2, p->cfl, p->dt_max);
+        adj_arg_kernel<T><<<grid, block, 0, st>>>(v, w);
+        adj_mu_kernel<T><<<grid, block, 0, st>>>(v, w, part, nblocks);
+        adj_sum_kernel<<<1, 256, 0, st>>>(part, nblocks, 2, &w->dJdt, &w->gE, 0, 1);
+        adj_D_back_kernel<T><<<grid, block, 0, st>>>(v, w, part + 2 * (size_t)nblocks);
+        adj_sum_kernel<<<1, 256, 0, st>>>(part + 2 * (size_t)nblocks, nblocks, 1, &w->gG, nullptr, 1, 0);
+        adj_out_kernel<T><<<grid, block, 0, st>>>(v);
+        CG_CHECK_LAUNCH(ctx);
+        return (int)CG_OK;
+    });
+    if (rc) return rc;
+    if (dJ) {  // hand the accumulated sums over and start again from zero
+        double acc[2];
+        CG_CUDA(ctx, cudaMemcpyAsync(acc, &w->gG, sizeof(acc), cudaMemcpyDeviceToHost, ctx->stream));
+        CG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        CG_CUDA(ctx, cudaMemsetAsync(&w->gG, 0, sizeof(acc), ctx->stream));
+        dJ[0] += acc[0];
+        dJ[1] += acc[1];
+    }
     return CG_OK;
 }
 
@@ -362,7 +381,7 @@ int adjoint_step_t(cg_ctx* ctx, const cg_grid* g, const cg_field* H, const cg_fi
 extern "C" int cg_sia_adjoint_step(cg_ctx* ctx, const cg_grid* grid, const cg_field* H, const cg_field* B,
                                    const cg_sia_params* p, const cg_field* lam, const cg_field* lam_out, double* dJ) {
     if (!ctx) return cg_fail(nullptr, CG_ERR_ARG, "sia_adjoint_step: ctx is NULL");
-    if (!grid || !H || !B || !p || !lam || !lam_out || !dJ) return cg_fail(ctx, CG_ERR_ARG, "sia_adjoint_step: NULL argument");
+    if (!grid || !H || !B || !p || !lam || !lam_out) return cg_fail(ctx, CG_ERR_ARG, "sia_adjoint_step: NULL argument");
     int rc = cg_check_grid(ctx, grid);
     if (rc) return rc;
     if (grid->ndim != 2) return cg_fail(ctx, CG_ERR_UNSUPPORTED, "sia_adjoint_step: 2D grids only");

@@ -476,11 +476,13 @@ CG_API int cg_sia_ensemble_run(cg_ctx* ctx, int nmembers, const cg_sia_member* m
  * no adjoint). H is the state H_n at the start of the forward step, with the ghost layer the
  * forward step read (bc! Neumann copies after every step). lam holds dJ/dH_{n+1} at the
  * interior cells. The entry writes dJ/dH_n at the interior cells into lam_out (the ghost
- * cells' terms folded into the cells they copy), and adds this step's dJ/dGamma to dJ[0] and
- * dJ/dela to dJ[1]. The step's quantities (D, its maximum and dt, the fluxes, the masks of
- * max(H, 0) and of the mass balance's cap) are recomputed from H with the forward's
+ * cells' terms folded into the cells they copy). The step's dJ/dGamma and dJ/dela accumulate
+ * on the device: a call with dJ == NULL only adds to them, and a call with dJ (host memory)
+ * adds the accumulated sums to dJ[0] (Gamma) and dJ[1] (ela), starts them again from zero and
+ * synchronises the stream. The step's quantities (D, its maximum and dt, the fluxes, the masks
+ * of max(H, 0) and of the mass balance's cap) are recomputed from H with the forward's
  * arithmetic. The adaptive dt is differentiated through max D at the cell attaining it when
- * dt is below dt_max. Synchronises the stream (dJ is host memory). */
+ * dt is below dt_max. The kernels replay from one CUDA graph per argument set. */
 CG_API int cg_sia_adjoint_step(cg_ctx* ctx, const cg_grid* grid, const cg_field* H, const cg_field* B,
                                const cg_sia_params* p, const cg_field* lam, const cg_field* lam_out,
                                double* dJ);
