@@ -759,6 +759,54 @@ def run_kernel_ptdiff(arch, args):
                       "algorithmic_gbs": byt / (ms * 1e-3) / 1e9, "frac_of_measured_hbm": byt / (ms * 1e-3) / 1e9 / measured_peaks()[0]}))
 
 
+def run_kernel_misc(arch, args):
+    """--kernel sia_ensemble: `--members` members of the SIA ensemble (sizes 128..1024), `--reps`
+    steps in one batched run. --kernel diffusion2d: the explicit diffusion step at n^2 (FP64,
+    Neumann), `--reps` steps. Timed with CUDA events after one untimed run."""
+    import torch
+
+    from chmy_gb300 import Field, _abi
+    from chmy_gb300.bcs import Neumann, to_cg_bc
+    from chmy_gb300.configs import padded_mesh, sia_ensemble
+    from chmy_gb300.grids import Center, UniformGrid, Vertex
+
+    stream = torch.cuda.current_stream()
+    Cl, Vl = Center(), Vertex()
+    if args.kernel == "sia_ensemble":
+        ens = sia_ensemble(members=args.members)
+        keep, mem = [], (_abi.cg_sia_member * len(ens))()
+        params = (_abi.cg_sia_params * len(ens))()
+        cells = 0
+        for k, (grid, hh, p) in enumerate(ens):
+            H, Bf = Field(arch, grid, Cl, np.float64), Field(arch, grid, Cl, np.float64)
+            H.from_numpy(hh["H"])
+            Bf.from_numpy(hh["B"])
+            qq = [Field(arch, grid, (Vl, Cl), np.float64), Field(arch, grid, (Cl, Vl), np.float64)]
+            keep.append((H, Bf, qq))
+            mem[k].grid = grid.desc()
+            mem[k].H, mem[k].B = H.desc(), Bf.desc()
+            mem[k].q[0], mem[k].q[1] = qq[0].desc(), qq[1].desc()
+            params[k] = p
+            cells += grid.dims[0] * grid.dims[1]
+        ts = (ctypes.c_double * len(ens))()
+        ms = _timed(lambda: arch.call("cg_sia_ensemble_run", len(ens), mem, params, args.reps, ts), stream)
+        print(json.dumps({"kernel": "ens_D/q/H_kernel<double>", "members": len(ens), "cells": cells, "steps": args.reps,
+                          "ms_per_step": ms / args.reps}))
+        return
+    n = args.n
+    g = UniformGrid(origin=(-1.0, -1.0), extent=(2.0, 2.0), dims=(n, n), dtype=np.float64)
+    x, y = padded_mesh(g, Cl)
+    A, B = Field(arch, g, Cl, np.float64), Field(arch, g, Cl, np.float64)
+    A.from_numpy(np.exp(-(x * x + y * y) / 0.02))
+    B.from_numpy(np.exp(-(x * x + y * y) / 0.02))
+    bc = to_cg_bc(2, Neumann())
+    h = float(g.spacing()[0])
+    gd = g.desc()
+    ms = _timed(lambda: arch.call("cg_diffusion_run", ctypes.byref(gd), ctypes.byref(A.desc()), ctypes.byref(B.desc()), 1.0,
+                                  h * h / 4.1, ctypes.byref(bc), args.reps), stream)
+    print(json.dumps({"kernel": "diffusion_step_kernel<double,2>", "n": n, "steps": args.reps, "us_per_step": 1e3 * ms / args.reps}))
+
+
 def run_kernel(args):
     """--kernel fused2d | fused3d: only the fused FP32 PT kernel (2D inclusions n^2, or 3D random
     viscosity n^3), `--reps` launches timed with CUDA events (the command the committed ncu
@@ -771,6 +819,10 @@ def run_kernel(args):
     arch = Arch(GB300Backend())
     if args.kernel == "ptdiff3d":
         run_kernel_ptdiff(arch, args)
+        arch.close()
+        return
+    if args.kernel in ("sia_ensemble", "diffusion2d"):
+        run_kernel_misc(arch, args)
         arch.close()
         return
     if args.kernel == "fused3d":
@@ -803,7 +855,9 @@ def run_kernel(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--kernel", choices=["fused2d", "fused3d", "ptdiff3d"], help="time one kernel alone (profiling driver)")
+    ap.add_argument("--kernel", choices=["fused2d", "fused3d", "ptdiff3d", "sia_ensemble", "diffusion2d"],
+                    help="time one kernel alone (profiling driver)")
+    ap.add_argument("--members", type=int, default=64, help="--kernel sia_ensemble: ensemble members")
     ap.add_argument("--reps", type=int, default=200)
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
