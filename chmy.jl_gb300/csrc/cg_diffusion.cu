@@ -50,13 +50,25 @@ __global__ void update_C_kernel(DF<T> C, DF<T> q0, DF<T> q1, DF<T> q2, T dt, Spa
 
 // Fused compute_q! + update_C!: the face fluxes are recomputed from C_in; a face with index
 // n+2 along its dimension is outside compute_q!'s range and reads as zero (fresh q arrays).
+// At the cells whose faces all lie inside that range (indices 1..n along every dimension) the
+// flux difference is the same stencil in the form C + sum_d a_d (C[I+e_d] - 2 C + C[I-e_d]),
+// a_d = dt chi / Δ_d^2: 7 FP64 operations in 2D where the flux form takes 15. The FP64 step is
+// bound by the FP64 pipe, and the two forms differ only by rounding, a few ulp of C per step.
 template <class T, int ND>
-__global__ void diffusion_step_kernel(DF<T> Co, DF<T> Ci, T mchi, T dt, Spacing<T> s, int e0, int e1, int e2) {
+__global__ void diffusion_step_kernel(DF<T> Co, DF<T> Ci, T mchi, T dt, Spacing<T> s, int e0, int e1, int e2,
+                                      Spacing<T> a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = ND > 1 ? blockIdx.y * blockDim.y + threadIdx.y : 0;
     const int k = ND > 2 ? blockIdx.z : 0;
     if (i > e0 || j > e1) return;
     const T c = Ci(i, j, k);
+    if (i >= 1 && i < e0 && (ND < 2 || (j >= 1 && j < e1)) && (ND < 3 || (k >= 1 && k < e2))) {
+        T acc = a.i[0] * fma(T(-2), c, Ci(i + 1, j, k) + Ci(i - 1, j, k));
+        if (ND > 1) acc = fma(a.i[1], fma(T(-2), c, Ci(i, j + 1, k) + Ci(i, j - 1, k)), acc);
+        if (ND > 2) acc = fma(a.i[2], fma(T(-2), c, Ci(i, j, k + 1) + Ci(i, j, k - 1)), acc);
+        Co(i, j, k) = c + acc;
+        return;
+    }
     const T qxl = mchi * ((c - Ci(i - 1, j, k)) * s.i[0]);
     const T qxr = i + 1 <= e0 ? mchi * ((Ci(i + 1, j, k) - c) * s.i[0]) : T(0);
     T dv = (qxr - qxl) * s.i[0];
@@ -174,9 +186,11 @@ int update_C_t(cg_ctx* ctx, const cg_grid* g, const cg_field* C, const cg_field*
 template <class T, int ND>
 int step_t(cg_ctx* ctx, const cg_grid* g, const cg_field* Co, const cg_field* Ci, double chi, double dt) {
     const dim3 block = block_for<ND>();
+    Spacing<T> a;
+    for (int d = 0; d < 3; ++d) a.i[d] = (T)(dt * chi * g->inv_spacing[d] * g->inv_spacing[d]);
     diffusion_step_kernel<T, ND><<<range_grid<ND>(g, block), block, 0, ctx->stream>>>(
         cg_view<T>(*Co), cg_view<T>(*Ci), -(T)chi, (T)dt, spacing_of<T>(g), g->n[0] + 1,
-        ND > 1 ? g->n[1] + 1 : 0, ND > 2 ? g->n[2] + 1 : 0);
+        ND > 1 ? g->n[1] + 1 : 0, ND > 2 ? g->n[2] + 1 : 0, a);
     CG_CHECK_LAUNCH(ctx);
     return CG_OK;
 }
