@@ -211,6 +211,7 @@ T partial_k_partial(const Fd<T>& f, const Fd<T>& kk, const GridT<T>& g, int d, i
  * (worksize remove_dim(dim, size(grid, Vertex()) .+ 2), index J-1, batch.jl:243,265). */
 template <class T>
 void bc_phase(const Gd& g, const Fd<T>& f, const cg_bc& bc, int d, int s, T spacing_d) {
+    using std::fma;
     const int kind = bc.kind[d][s];
     if (kind == CG_BC_NONE) return;
     const int ext = f.n[d]; /* firstindex = 1, lastindex = ext */
@@ -263,11 +264,11 @@ void bc_phase(const Gd& g, const Fd<T>& f, const cg_bc& bc, int d, int s, T spac
             const T b0 = f.at(In);
             if (kind == CG_BC_DIRICHLET) {
                 /* Center: muladd(t, a - b, b), t = 2 on a UniformGrid */
-                f.at(I) = std::fma(T(2), val - b0, b0);
+                f.at(I) = fma(T(2), val - b0, b0);
             } else {
                 /* Neumann: muladd(h, ±q, f[in]), minus on Side(1) */
                 const T qs = s == 0 ? -val : val;
-                f.at(I) = std::fma(spacing_d, qs, b0);
+                f.at(I) = fma(spacing_d, qs, b0);
             }
         }
 }
@@ -745,11 +746,13 @@ struct Sia {
     T gy(int i, int j) const { return (S(i, j) - S(i, j - 1)) * g.idx[1]; }
     /* vmag(∇S) at cell (i, j): sqrt(lerp(∇S.x → C)^2 + lerp(∇S.y → C)^2) (field_operators.jl:187-191) */
     T vmag(int i, int j) const {
+        using std::fma;
+        using std::sqrt;
         const T a0 = gx(i, j), a1 = gx(i + 1, j);
-        const T ax = std::fma(T(0.5), a1 - a0, a0);
+        const T ax = fma(T(0.5), a1 - a0, a0);
         const T b0 = gy(i, j), b1 = gy(i, j + 1);
-        const T ay = std::fma(T(0.5), b1 - b0, b0);
-        return std::sqrt(ax * ax + ay * ay);
+        const T ay = fma(T(0.5), b1 - b0, b0);
+        return sqrt(ax * ax + ay * ay);
     }
     /* D = (Gamma H^(n+2) + As H^n) vmag^(n-1) (:46-49) */
     T D(int i, int j) const {
@@ -759,6 +762,56 @@ struct Sia {
     /* M = min(beta (S - ela), m_max) (:51-54) */
     T M(int i, int j) const { return std::min(beta * (S(i, j) - ela), m_max); }
 };
+
+/* update_q! and bc!(q) for a prepared Sia (its parameters may carry tangents); *dmax gets
+   maximum(interior(D)), the first cell (j outer, i inner) attaining it */
+template <class T>
+void sia_update_q_body(const cg_grid* grid, const Sia<T>& s, const cg_field* q, T* dmax) {
+    using std::fma;
+    Fd<T> qx(q[0]), qy(q[1]);
+    const int nx = s.g.n[0], ny = s.g.n[1];
+#pragma omp parallel for schedule(static)
+    for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i) {
+            const T dl = s.D(i - 1, j), dc = s.D(i, j), dd = s.D(i, j - 1);
+            const T Dx = fma(T(0.5), dc - dl, dl);
+            const T Dy = fma(T(0.5), dc - dd, dd);
+            qx(i, j, 0) = -Dx * s.gx(i, j);
+            qy(i, j, 0) = -Dy * s.gy(i, j);
+        }
+    if (dmax) {
+        T m = T(0.0);
+        for (int j = 1; j <= ny; ++j)
+            for (int i = 1; i <= nx; ++i) {
+                const T d = s.D(i, j);
+                if (m < d) m = d;
+            }
+        *dmax = m;
+    }
+    cg_bc b[2];
+    std::memset(b, 0, sizeof(b));
+    b[0].kind[0][0] = b[0].kind[0][1] = CG_BC_DIRICHLET;
+    b[1].kind[1][0] = b[1].kind[1][1] = CG_BC_DIRICHLET;
+    bc_apply_t<T>(grid, 2, q, b);
+}
+
+/* update_H! and bc!(H) for a prepared Sia, with a T-typed time step */
+template <class T>
+void sia_update_H_body(const cg_grid* grid, Sia<T>& s, const cg_field* Hf, const cg_field* q, T Dt) {
+    Fd<T> Q[3] = {Fd<T>(q[0]), Fd<T>(q[1]), Fd<T>()};
+    const int nx = s.g.n[0], ny = s.g.n[1];
+#pragma omp parallel for schedule(static)
+    for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i) {
+            const T h = s.H(i, j, 0);
+            const T m = s.M(i, j);
+            s.H(i, j, 0) = std::max(h + Dt * (-divg(Q, s.g, i, j, 0) + m), T(0.0));
+        }
+    cg_bc b;
+    std::memset(&b, 0, sizeof(b));
+    b.kind[0][0] = b.kind[0][1] = b.kind[1][0] = b.kind[1][1] = CG_BC_NEUMANN;
+    bc_apply_t<T>(grid, 1, Hf, &b);
+}
 
 template <class T>
 void sia_update_q_t(const cg_grid* grid, const cg_field* q, const cg_field* Hf, const cg_field* Bf,
@@ -813,6 +866,67 @@ void sia_update_H_t(const cg_grid* grid, const cg_field* Hf, const cg_field* q, 
     bc_apply_t<T>(grid, 1, Hf, &b);
 }
 
+/* ---- forward-mode dual numbers: exact tangents of the restated loop ---------------------
+ * A value and its derivatives along two directions; every operation is the value's own plus
+ * its first-order rule. Comparisons (max, min, the kinks) act on the value. The restated SIA
+ * step runs on it unchanged (its fma and sqrt calls are unqualified), so the tangents are the
+ * derivatives of exactly the arithmetic above. */
+struct Dual {
+    double v = 0.0;
+    double d[2] = {0.0, 0.0};
+    Dual() = default;
+    Dual(double x) : v(x) {}
+    explicit operator double() const { return v; }
+};
+inline Dual operator+(const Dual& a, const Dual& b) {
+    Dual r(a.v + b.v);
+    for (int k = 0; k < 2; ++k) r.d[k] = a.d[k] + b.d[k];
+    return r;
+}
+inline Dual operator-(const Dual& a, const Dual& b) {
+    Dual r(a.v - b.v);
+    for (int k = 0; k < 2; ++k) r.d[k] = a.d[k] - b.d[k];
+    return r;
+}
+inline Dual operator-(const Dual& a) {
+    Dual r(-a.v);
+    for (int k = 0; k < 2; ++k) r.d[k] = -a.d[k];
+    return r;
+}
+inline Dual operator*(const Dual& a, const Dual& b) {
+    Dual r(a.v * b.v);
+    for (int k = 0; k < 2; ++k) r.d[k] = a.d[k] * b.v + a.v * b.d[k];
+    return r;
+}
+inline Dual operator/(const Dual& a, const Dual& b) {
+    Dual r(a.v / b.v);
+    for (int k = 0; k < 2; ++k) r.d[k] = (a.d[k] - r.v * b.d[k]) / b.v;
+    return r;
+}
+inline bool operator<(const Dual& a, const Dual& b) { return a.v < b.v; }
+inline bool operator>(const Dual& a, const Dual& b) { return a.v > b.v; }
+inline Dual fma(const Dual& a, const Dual& b, const Dual& c) {
+    Dual r(std::fma(a.v, b.v, c.v));
+    for (int k = 0; k < 2; ++k) r.d[k] = a.d[k] * b.v + a.v * b.d[k] + c.d[k];
+    return r;
+}
+inline Dual sqrt(const Dual& a) {
+    Dual r(std::sqrt(a.v));
+    for (int k = 0; k < 2; ++k) r.d[k] = r.v > 0.0 ? a.d[k] / (2.0 * r.v) : 0.0;
+    return r;
+}
+
+/* A field descriptor over `storage` with the layout of `like` (same strides and halo). */
+template <class T>
+cg_field like_field(const cg_field& like, std::vector<T>& storage) {
+    long span = 1;
+    for (int d = 0; d < like.ndim; ++d) span += (long)(like.n[d] + 4 * like.halo[d] - 1) * like.stride[d];
+    storage.assign((size_t)span, T(0.0));
+    cg_field f = like;
+    f.data = storage.data();
+    return f;
+}
+
 }  // namespace
 
 /* ==== extern "C" surface (names mirror the library's cg_* entry points) =============== */
@@ -845,6 +959,44 @@ int or_maxabs(int nfields, const cg_field* fields, double* out, int32_t* nonfini
     for (int i = 0; i < nfields; ++i)
         out[i] = fields[i].dtype == CG_F64 ? maxabs_t<double>(fields[i], &bad) : maxabs_t<float>(fields[i], &bad);
     if (nonfinite) *nonfinite = bad;
+    return CG_OK;
+}
+
+/* The SIA time loop of examples/sia.jl:71-81 (update_q!, bc!, dt = min(Δ²/max D/cfl,
+   dt_max), update_H!, bc!) in dual numbers: H (FP64) is advanced `nsteps` steps, and
+   dH_dGamma, dH_dela (FP64, H's layout, zero on entry) receive the exact derivatives of the
+   final H with respect to Gamma and ela. q (2 fields, FP64) is the loop's flux storage. */
+int or_sia_run_tangent(const cg_grid* grid, const cg_field* H, const cg_field* B, const cg_field* q,
+                       const cg_sia_params* p, int nsteps, const cg_field* dH_dGamma, const cg_field* dH_dela) {
+    std::vector<Dual> hs, bs, q0s, q1s;
+    const cg_field Hd = like_field(*H, hs), Bd = like_field(*B, bs);
+    cg_field Qd[3] = {like_field(q[0], q0s), like_field(q[1], q1s), cg_field()};
+    Fd<double> h(*H), b(*B);
+    Fd<Dual> hD(Hd), bD(Bd);
+    const int nx = grid->n[0], ny = grid->n[1];
+    for (int j = -1; j <= ny + 2; ++j)
+        for (int i = -1; i <= nx + 2; ++i) {
+            hD(i, j, 0) = Dual(h(i, j, 0));
+            bD(i, j, 0) = Dual(b(i, j, 0));
+        }
+    Sia<Dual> s(grid, &Hd, &Bd, p);
+    s.Gamma.d[0] = 1.0;  // direction 0: Gamma
+    s.ela.d[1] = 1.0;    // direction 1: ela
+    const double dx = std::min(grid->spacing[0], grid->spacing[1]);
+    for (int step = 0; step < nsteps; ++step) {
+        Dual dmax;
+        sia_update_q_body<Dual>(grid, s, Qd, &dmax);
+        const Dual qdt = Dual(dx * dx) / dmax / Dual(p->cfl);
+        const Dual dt = (dmax.v > 0.0 && qdt.v < p->dt_max) ? qdt : Dual(p->dt_max);
+        sia_update_H_body<Dual>(grid, s, &Hd, Qd, dt);
+    }
+    Fd<double> gG(*dH_dGamma), gE(*dH_dela);
+    for (int j = -1; j <= ny + 2; ++j)
+        for (int i = -1; i <= nx + 2; ++i) {
+            h(i, j, 0) = hD(i, j, 0).v;
+            gG(i, j, 0) = hD(i, j, 0).d[0];
+            gE(i, j, 0) = hD(i, j, 0).d[1];
+        }
     return CG_OK;
 }
 

@@ -29,6 +29,8 @@ _SIGS = {
     "or_maxabs": ([C.c_int, P(_abi.cg_field), P(C.c_double), P(C.c_int32)], C.c_int),
     "or_diffusion_compute_q": ([P(_abi.cg_grid), P(_abi.cg_field), P(_abi.cg_field), C.c_double], C.c_int),
     "or_diffusion_update_C": ([P(_abi.cg_grid), P(_abi.cg_field), P(_abi.cg_field), C.c_double], C.c_int),
+    "or_sia_run_tangent": ([P(_abi.cg_grid), P(_abi.cg_field), P(_abi.cg_field), P(_abi.cg_field), P(_abi.cg_sia_params), C.c_int,
+                            P(_abi.cg_field), P(_abi.cg_field)], C.c_int),
     "or_diffusion_compute_q_masked": ([P(_abi.cg_grid), P(_abi.cg_field), P(_abi.cg_field), C.c_double, P(_abi.cg_mask)], C.c_int),
     "or_diffusion_update_C_masked": ([P(_abi.cg_grid), P(_abi.cg_field), P(_abi.cg_field), C.c_double, P(_abi.cg_mask)], C.c_int),
     "or_stokes_update_old": ([P(_abi.cg_grid), P(_abi.cg_stokes_fields)], C.c_int),

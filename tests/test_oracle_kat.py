@@ -513,3 +513,56 @@ def test_masked_diffusion_oracle(T):
             dv += (qy[J + 1, Ip] * wy[J + 1, Ip] - qy[J, Ip] * wy[J, Ip]) * idy
             cn[J, Ip] = c[J, Ip] - dt * dv
     assert approx(qm[0].a, qx, T) and approx(qm[1].a, qy, T) and approx(Cm.a, cn, T)
+
+
+def test_sia_dual_tangents_match_oracle_differences():
+    """The oracle's dual-number SIA loop (or_sia_run_tangent): its value equals the plain
+    restated loop bit for bit, and its tangents along Gamma and ela agree with central
+    differences of that loop."""
+    import ctypes
+
+    from _oracle import desc_array, lib
+
+    T = np.float64
+    grid = UniformGrid(origin=(T(-1), T(-1)), extent=(T(2), T(2)), dims=(20, 16), dtype=T)
+    x, y = np.meshgrid(*[np.array([grid.axes[d].coord(Center(), i) for i in range(-1, grid.dims[d] + 3)]) for d in (1, 0)], indexing="ij")
+    y, x = x, y  # [y, x] meshes of the padded Center coordinates
+    bed = 0.4 + 0.2 * np.sin(2 * x) * np.cos(3 * y)
+    H0 = np.clip(0.35 - 0.25 * (x * x + y * y), 0.0, None)
+    p = _abi.cg_sia_params()
+    p.Gamma, p.As, p.n, p.beta, p.ela, p.m_max, p.dt_max, p.cfl = 1.0, 0.0, 3, 0.5, 0.55, 0.25, 0.5, 4.1
+    g = grid.desc()
+    nsteps = 20
+
+    def plain(Gamma, ela):
+        q_ = _abi.cg_sia_params()
+        ctypes.memmove(ctypes.byref(q_), ctypes.byref(p), ctypes.sizeof(q_))
+        q_.Gamma, q_.ela = Gamma, ela
+        H = NpField(grid, Center(), T)
+        H.a[...] = H0
+        B = NpField(grid, Center(), T)
+        B.a[...] = bed
+        q = [NpField(grid, (Vertex(), Center()), T), NpField(grid, (Center(), Vertex()), T)]
+        dx = min(grid.spacing())
+        for _ in range(nsteps):
+            dmax = ctypes.c_double()
+            lib().or_sia_update_q(ctypes.byref(g), desc_array(q, 3), ctypes.byref(H.desc()), ctypes.byref(B.desc()), ctypes.byref(q_), ctypes.byref(dmax))
+            qd = T(dx * dx) / T(dmax.value) / T(q_.cfl)
+            dt = float(qd) if (dmax.value > 0 and qd < q_.dt_max) else q_.dt_max
+            lib().or_sia_update_H(ctypes.byref(g), ctypes.byref(H.desc()), desc_array(q, 3), ctypes.byref(B.desc()), dt, ctypes.byref(q_))
+        return H.a.copy()
+
+    H = NpField(grid, Center(), T)
+    H.a[...] = H0
+    B = NpField(grid, Center(), T)
+    B.a[...] = bed
+    q = [NpField(grid, (Vertex(), Center()), T), NpField(grid, (Center(), Vertex()), T)]
+    tG, tE = NpField(grid, Center(), T), NpField(grid, Center(), T)
+    assert lib().or_sia_run_tangent(ctypes.byref(g), ctypes.byref(H.desc()), ctypes.byref(B.desc()), desc_array(q, 3),
+                                    ctypes.byref(p), nsteps, ctypes.byref(tG.desc()), ctypes.byref(tE.desc())) == 0
+    assert np.array_equal(H.a, plain(p.Gamma, p.ela))
+    h = 1e-6
+    fdG = (plain(p.Gamma + h, p.ela) - plain(p.Gamma - h, p.ela)) / (2 * h)
+    fdE = (plain(p.Gamma, p.ela + h) - plain(p.Gamma, p.ela - h)) / (2 * h)
+    assert np.max(np.abs(tG.a - fdG)) <= 1e-6 * np.max(np.abs(fdG))
+    assert np.max(np.abs(tE.a - fdE)) <= 1e-6 * np.max(np.abs(fdE))
