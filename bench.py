@@ -760,7 +760,7 @@ def run_kernel_ptdiff(arch, args):
 
 
 def run_kernel_misc(arch, args):
-    """--kernel sia_ensemble: `--members` members of the SIA ensemble (sizes 128..1024), `--reps`
+    """--kernel sia_ensemble: `--members` members of the SIA ensemble (sizes --nmin..--nmax), `--reps`
     steps in one batched run. --kernel diffusion2d: the explicit diffusion step at n^2 (FP64,
     Neumann), `--reps` steps. Timed with CUDA events after one untimed run."""
     import torch
@@ -773,7 +773,7 @@ def run_kernel_misc(arch, args):
     stream = torch.cuda.current_stream()
     Cl, Vl = Center(), Vertex()
     if args.kernel == "sia_ensemble":
-        ens = sia_ensemble(members=args.members)
+        ens = sia_ensemble(members=args.members, nmin=args.nmin, nmax=args.nmax)
         keep, mem = [], (_abi.cg_sia_member * len(ens))()
         params = (_abi.cg_sia_params * len(ens))()
         cells = 0
@@ -858,6 +858,8 @@ def main():
     ap.add_argument("--kernel", choices=["fused2d", "fused3d", "ptdiff3d", "sia_ensemble", "diffusion2d"],
                     help="time one kernel alone (profiling driver)")
     ap.add_argument("--members", type=int, default=64, help="--kernel sia_ensemble: ensemble members")
+    ap.add_argument("--nmin", type=int, default=128, help="--kernel sia_ensemble: smallest member size")
+    ap.add_argument("--nmax", type=int, default=1024, help="--kernel sia_ensemble: largest member size")
     ap.add_argument("--reps", type=int, default=200)
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)

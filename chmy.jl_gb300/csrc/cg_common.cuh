@@ -70,6 +70,9 @@ bool cg_bc_fold_enabled();
 // The fused single-pass PT-diffusion iteration (3D FP32); CG_PTDIFF_FUSED=0 keeps the
 // two-kernel form.
 bool cg_ptdiff_fused_enabled();
+// The SIA ensemble as one persistent cooperative launch (CG_SIA_PERSISTENT=1) instead of one
+// launch per phase replayed from a CUDA graph (the default, measured faster).
+bool cg_sia_persistent_enabled();
 
 template <class... P, class... A>
 inline cudaError_t cg_launch(void (*kern)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, bool dep,

@@ -107,6 +107,12 @@ bool cg_ptdiff_fused_enabled() {
     return on;
 }
 
+bool cg_sia_persistent_enabled() {
+    // read on every call (once per run), so that a process can compare both forms
+    const char* e = std::getenv("CG_SIA_PERSISTENT");
+    return e && e[0] == '1';
+}
+
 bool cg_tune_lookup(const std::string& key, cg_tune_cfg* out) {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune.find(key);

@@ -1,8 +1,13 @@
 // cg_sia_ensemble.cu — an ensemble of independent shallow-ice solves of uneven grid sizes
-// (examples/sia.jl:7-16,71-81 per member) advanced together: every phase of a time step is ONE
-// launch over the tiles of all members (a per-member tile prefix table maps blocks to
-// members), the adaptive Δt of every member is computed on the device, and the whole
-// `nsteps` loop is replayed from one CUDA graph.
+// (examples/sia.jl:7-16,71-81 per member) advanced together. Every phase of a time step covers
+// the tiles of all members (a per-member tile prefix table maps tiles to members), and the
+// adaptive Δt of every member is computed on the device. The `nsteps` loop is one launch per
+// phase, replayed from a CUDA graph. With CG_SIA_PERSISTENT=1 (and cooperative launch support)
+// it is instead ONE persistent cooperative launch with grid barriers between the phases. Both
+// forms give the same bits. The graph is the default: on GB300 the tiles are bound by the FP64
+// pipe, so residency saves nothing, and a grid barrier costs more than a kernel boundary in a
+// replayed graph (64 members of 128^2..1024^2: 2.49 vs 2.41 ms per step; of 32^2..128^2:
+// 70 vs 62 us).
 //
 // Boundary conditions are folded into the kernels with the values of the reference's bc!:
 // q.x => (x = Dirichlet()) writes 0 on the boundary faces i = 1, n+1 (q.y likewise), and
@@ -43,9 +48,12 @@ using cgsia::bits_of;
 
 // The block's member descriptor, copied once into shared memory (every thread of the block
 // calls it before reading the member).
+// The leading barrier lets a block that loops over tiles (the persistent kernel) call it once
+// per tile: the previous tile's reads of the descriptor and of the block-max scratch are done.
 template <class T>
 __device__ __forceinline__ const Member<T>& member_of(const Member<T>* mem, int m) {
     __shared__ __align__(16) unsigned long long words[(sizeof(Member<T>) + 7) / 8];
+    __syncthreads();
     const int tid = threadIdx.x + blockDim.x * threadIdx.y;
     const unsigned long long* src = reinterpret_cast<const unsigned long long*>(mem + m);
     for (int k = tid; k < (int)((sizeof(Member<T>) + 7) / 8); k += blockDim.x * blockDim.y) words[k] = src[k];
@@ -65,10 +73,10 @@ __device__ __forceinline__ int find_member(const int* prefix, int nm, int blk) {
 }
 
 template <class T>
-__global__ void ens_D_kernel(const Member<T>* mem, const int* prefix, int nm, Words* w) {
-    const int m = find_member(prefix, nm, blockIdx.x);
+__device__ __forceinline__ void ens_D_tile(const Member<T>* mem, const int* prefix, int nm, Words* w, int blk) {
+    const int m = find_member(prefix, nm, blk);
     const Member<T>& v = member_of(mem, m);
-    const int t = blockIdx.x - (m ? prefix[m - 1] : 0);
+    const int t = blk - (m ? prefix[m - 1] : 0);
     const int tx = (v.nx + 1 + 31) / 32;
     const int i = (t % tx) * 32 + threadIdx.x;
     const int j = (t / tx) * 8 + threadIdx.y;
@@ -95,10 +103,10 @@ __global__ void ens_D_kernel(const Member<T>* mem, const int* prefix, int nm, Wo
 
 // S = B + H over [-1, n+1]^2 (the D kernel's stencil), once per run
 template <class T>
-__global__ void ens_S_kernel(const Member<T>* mem, const int* prefix, int nm) {
-    const int m = find_member(prefix, nm, blockIdx.x);
+__device__ __forceinline__ void ens_S_tile(const Member<T>* mem, const int* prefix, int nm, int blk) {
+    const int m = find_member(prefix, nm, blk);
     const Member<T>& v = member_of(mem, m);
-    const int t = blockIdx.x - (m ? prefix[m - 1] : 0);
+    const int t = blk - (m ? prefix[m - 1] : 0);
     const int tx = (v.nx + 3 + 31) / 32;
     const int i = (t % tx) * 32 + threadIdx.x - 1;
     const int j = (t / tx) * 8 + threadIdx.y - 1;
@@ -107,10 +115,10 @@ __global__ void ens_S_kernel(const Member<T>* mem, const int* prefix, int nm) {
 }
 
 template <class T>
-__global__ void ens_q_kernel(const Member<T>* mem, const int* prefix, int nm) {
-    const int m = find_member(prefix, nm, blockIdx.x);
+__device__ __forceinline__ void ens_q_tile(const Member<T>* mem, const int* prefix, int nm, int blk) {
+    const int m = find_member(prefix, nm, blk);
     const Member<T>& v = member_of(mem, m);
-    const int t = blockIdx.x - (m ? prefix[m - 1] : 0);
+    const int t = blk - (m ? prefix[m - 1] : 0);
     const int tx = (v.nx + 31) / 32;
     const int i = (t % tx) * 32 + threadIdx.x + 1;
     const int j = (t / tx) * 8 + threadIdx.y + 1;
@@ -127,9 +135,7 @@ __global__ void ens_q_kernel(const Member<T>* mem, const int* prefix, int nm) {
 }
 
 template <class T>
-__global__ void ens_dt_kernel(const Member<T>* mem, int nm, Words* w) {
-    const int m = blockIdx.x * blockDim.x + threadIdx.x;
-    if (m >= nm) return;
+__device__ __forceinline__ void ens_dt_member(const Member<T>* mem, Words* w, int m) {
     const Member<T>& v = mem[m];
     const unsigned long long b = w[m].dmax;
     const double dmax = sizeof(T) == 8 ? __longlong_as_double((long long)b) : (double)__int_as_float((int)(unsigned)b);
@@ -142,10 +148,10 @@ __global__ void ens_dt_kernel(const Member<T>* mem, int nm, Words* w) {
 }
 
 template <class T>
-__global__ void ens_H_kernel(const Member<T>* mem, const int* prefix, int nm, const Words* w) {
-    const int m = find_member(prefix, nm, blockIdx.x);
+__device__ __forceinline__ void ens_H_tile(const Member<T>* mem, const int* prefix, int nm, const Words* w, int blk) {
+    const int m = find_member(prefix, nm, blk);
     const Member<T>& v = member_of(mem, m);
-    const int t = blockIdx.x - (m ? prefix[m - 1] : 0);
+    const int t = blk - (m ? prefix[m - 1] : 0);
     const int tx = (v.nx + 31) / 32;
     const int i = (t % tx) * 32 + threadIdx.x + 1;
     const int j = (t / tx) * 8 + threadIdx.y + 1;
@@ -179,6 +185,91 @@ __global__ void ens_H_kernel(const Member<T>* mem, const int* prefix, int nm, co
 }
 
 template <class T>
+__global__ void ens_D_kernel(const Member<T>* mem, const int* prefix, int nm, Words* w) {
+    ens_D_tile(mem, prefix, nm, w, blockIdx.x);
+}
+template <class T>
+__global__ void ens_S_kernel(const Member<T>* mem, const int* prefix, int nm) {
+    ens_S_tile(mem, prefix, nm, blockIdx.x);
+}
+template <class T>
+__global__ void ens_q_kernel(const Member<T>* mem, const int* prefix, int nm) {
+    ens_q_tile(mem, prefix, nm, blockIdx.x);
+}
+template <class T>
+__global__ void ens_dt_kernel(const Member<T>* mem, int nm, Words* w) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m < nm) ens_dt_member(mem, w, m);
+}
+template <class T>
+__global__ void ens_H_kernel(const Member<T>* mem, const int* prefix, int nm, const Words* w) {
+    ens_H_tile(mem, prefix, nm, w, blockIdx.x);
+}
+
+// ---- one persistent launch for the whole run ------------------------------------------------
+//
+// The same tiles and arithmetic as the per-phase kernels: the resident blocks of a cooperative
+// launch loop over each phase's tiles, with a grid barrier between the phases. Per step:
+// D and the block maxima; barrier; Δt of every member (block 0) and the fluxes; barrier; the
+// thickness; barrier. The barrier counts arrivals on one monotonic word. Its waits give up
+// after two seconds (of the GPU's global timer) and set a timeout flag: the kernel then returns, and the
+// host reports the error. A cooperative launch keeps every block resident, so the waits end.
+struct GridBar {
+    unsigned long long arrived;  // arrivals since the launch: barrier k completes at (k + 1) x blocks
+    int timeout;
+};
+
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Barrier `k` (0, 1, ...) of the launch: one relaxed add per block, then a bounded wait until
+// all blocks have added. Nothing is reset, so the last block to arrive has no extra work.
+__device__ __forceinline__ bool grid_barrier(GridBar* b, unsigned nblocks, unsigned long long& k) {
+    __syncthreads();
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        const unsigned long long target = (++k) * nblocks;
+        __threadfence();
+        atomicAdd(&b->arrived, 1ull);
+        volatile unsigned long long* va = &b->arrived;
+        const unsigned long long t0 = globaltimer_ns();
+        while (*va < target) {
+            if (globaltimer_ns() - t0 > 2000000000ull) {  // 2 s
+                atomicExch(&b->timeout, 1);
+                break;
+            }
+            __nanosleep(32);
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return *(volatile int*)&b->timeout == 0;
+}
+
+template <class T>
+__global__ void __launch_bounds__(256, 8) ens_persistent_kernel(const Member<T>* mem, const int* pD, const int* pI,
+                                                             const int* pS, int nm, int totD, int totI, int totS,
+                                                             Words* w, int nsteps, GridBar* bar) {
+    const unsigned nb = gridDim.x;
+    unsigned long long k = 0;
+    for (int b = blockIdx.x; b < totS; b += nb) ens_S_tile(mem, pS, nm, b);
+    if (!grid_barrier(bar, nb, k)) return;
+    for (int s = 0; s < nsteps; ++s) {
+        for (int b = blockIdx.x; b < totD; b += nb) ens_D_tile(mem, pD, nm, w, b);
+        if (!grid_barrier(bar, nb, k)) return;
+        if (blockIdx.x == 0)
+            for (int m = threadIdx.x + blockDim.x * threadIdx.y; m < nm; m += blockDim.x * blockDim.y)
+                ens_dt_member(mem, w, m);
+        for (int b = blockIdx.x; b < totI; b += nb) ens_q_tile(mem, pI, nm, b);
+        if (!grid_barrier(bar, nb, k)) return;
+        for (int b = blockIdx.x; b < totI; b += nb) ens_H_tile(mem, pI, nm, w, b);
+        if (!grid_barrier(bar, nb, k)) return;
+    }
+}
+
+template <class T>
 int run_t(cg_ctx* ctx, int nm, const cg_sia_member* ms, const cg_sia_params* ps, int nsteps, double* t_host) {
     // scratch slot 3: [members][prefix D][prefix I][words][D arrays...]
     size_t off = 0;
@@ -192,6 +283,8 @@ int run_t(cg_ctx* ctx, int nm, const cg_sia_member* ms, const cg_sia_params* ps,
     off += ((size_t)nm * sizeof(int) + 255) & ~(size_t)255;
     const size_t w_off = off;
     off += ((size_t)nm * sizeof(Words) + 255) & ~(size_t)255;
+    const size_t bar_off = off;
+    off += 256;
     std::vector<size_t> d_off(nm), s_off(nm);
     for (int m = 0; m < nm; ++m) {
         const cg_field& H = ms[m].H;
@@ -253,12 +346,38 @@ int run_t(cg_ctx* ctx, int nm, const cg_sia_member* ms, const cg_sia_params* ps,
     CG_CUDA(ctx, cudaMemcpyAsync(dpI, pI.data(), nm * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
     CG_CUDA(ctx, cudaMemcpyAsync(dpS, pS.data(), nm * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
     CG_CUDA(ctx, cudaMemsetAsync(dw, 0, nm * sizeof(Words), ctx->stream));
+    const dim3 block(32, 8);
+    static const int coop = [] {
+        int dev = 0, v = 0;
+        cudaGetDevice(&dev);
+        return cudaDeviceGetAttribute(&v, cudaDevAttrCooperativeLaunch, dev) == cudaSuccess ? v : 0;
+    }();
+    if (coop && cg_sia_persistent_enabled()) {
+        // the whole run in one cooperative launch of the resident blocks
+        static const int bps = [] {
+            int nb = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, ens_persistent_kernel<T>, 256, 0) != cudaSuccess) nb = 0;
+            return nb;
+        }();
+        if (bps < 1) return cg_fail(ctx, CG_ERR_CUDA, "sia_ensemble_run: the persistent kernel does not fit on an SM");
+        GridBar* bar = reinterpret_cast<GridBar*>(base + bar_off);
+        CG_CUDA(ctx, cudaMemsetAsync(bar, 0, sizeof(GridBar), ctx->stream));
+        const Member<T>* cmem = dmem;
+        const int *cpD = dpD, *cpI = dpI, *cpS = dpS;
+        int anm = nm, atD = totD, atI = totI, atS = totS, ans = nsteps;
+        void* args[] = {&cmem, &cpD, &cpI, &cpS, &anm, &atD, &atI, &atS, &dw, &ans, &bar};
+        CG_CUDA(ctx, cudaLaunchCooperativeKernel((const void*)ens_persistent_kernel<T>, dim3(bps * ctx->num_sms), block,
+                                                 args, 0, ctx->stream));
+        int timed_out = 0;
+        CG_CUDA(ctx, cudaMemcpyAsync(&timed_out, &bar->timeout, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        CG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        if (timed_out) return cg_fail(ctx, CG_ERR_TIMEOUT, "sia_ensemble_run: a grid barrier of the persistent kernel timed out");
+    } else {
     std::string key = "sia_ensemble";
     cg_key_add(key, nm);
     cg_key_add(key, nsteps);
     cg_key_add(key, base);
     key.append(reinterpret_cast<const char*>(hm.data()), nm * sizeof(Member<T>));
-    const dim3 block(32, 8);
     rc = cg_graph_run(ctx, key, [&](cudaStream_t st) {
         ens_S_kernel<T><<<totS, block, 0, st>>>(dmem, dpS, nm);
         for (int s = 0; s < nsteps; ++s) {
@@ -271,6 +390,7 @@ int run_t(cg_ctx* ctx, int nm, const cg_sia_member* ms, const cg_sia_params* ps,
         return (int)CG_OK;
     });
     if (rc) return rc;
+    }
     if (t_host) {
         std::vector<Words> hw(nm);
         CG_CUDA(ctx, cudaMemcpyAsync(hw.data(), dw, nm * sizeof(Words), cudaMemcpyDeviceToHost, ctx->stream));

@@ -127,3 +127,45 @@ def test_ensemble_matches_members(arch):
         a, b = Ha.to_numpy()[1:-1, 1:-1], Hb.to_numpy()[1:-1, 1:-1]
         assert np.max(np.abs(a - b)) <= 1e-12 * nsteps * max(np.abs(a).max(), 1e-30), k
         assert abs(ts[k] - t_single[k]) <= 1e-12 * nsteps * t_single[k]
+
+
+@pytest.mark.parametrize("T", TYPES)
+def test_ensemble_persistent_launch_equals_phase_launches(arch, monkeypatch, T):
+    """The ensemble's single persistent cooperative launch (grid barriers between phases) gives
+    the same bits as one launch per phase (CG_SIA_PERSISTENT=0), for H, q and t."""
+    from chmy_gb300.configs import sia_ensemble
+
+    ens = sia_ensemble(members=7, nmin=33, nmax=150, seed=5, dtype=T)
+    nsteps = 40
+    rng = np.random.default_rng(2)
+    start = []
+    for grid, h, p in ens:
+        H0 = NpField(grid, Center(), T)
+        H0.interior()[...] = (rng.random(H0.dims) * 0.3).astype(T)
+        B = NpField(grid, Center(), T)
+        B.a[...] = h["B"].astype(T)
+        start.append((grid, H0, B, p))
+
+    def run(persistent):
+        monkeypatch.setenv("CG_SIA_PERSISTENT", "1" if persistent else "0")
+        mem = (_abi.cg_sia_member * len(start))()
+        params = (_abi.cg_sia_params * len(start))()
+        keep = []
+        for k, (grid, H0, B, p) in enumerate(start):
+            Hg, Bg = to_gpu(arch, H0), to_gpu(arch, B)
+            qg = [to_gpu(arch, NpField(grid, (Vertex(), Center()), T)), to_gpu(arch, NpField(grid, (Center(), Vertex()), T))]
+            keep.append((Hg, qg, Bg))
+            mem[k].grid = grid.desc()
+            mem[k].H, mem[k].B = Hg.desc(), Bg.desc()
+            mem[k].q[0], mem[k].q[1] = qg[0].desc(), qg[1].desc()
+            params[k] = p
+        ts = (ctypes.c_double * len(start))()
+        arch.call("cg_sia_ensemble_run", len(start), mem, params, nsteps, ts)
+        arch.synchronize()
+        return [(Hg.to_numpy(), qg[0].to_numpy(), qg[1].to_numpy()) for Hg, qg, _ in keep], list(ts)
+
+    (fa, ta), (fb, tb) = run(True), run(False)
+    assert ta == tb
+    for k, (a, b) in enumerate(zip(fa, fb)):
+        for x, y in zip(a, b):
+            np.testing.assert_array_equal(x, y, err_msg=f"member {k}")
