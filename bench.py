@@ -653,7 +653,63 @@ def config_suite(arch, stream, peak):
     }
     del keep
     torch.cuda.empty_cache()
+    out["sia_adjoint"] = sia_adjoint_cost(arch)
+    torch.cuda.empty_cache()
     return out
+
+
+def sia_adjoint_cost(arch, n=1024, nsteps=1000):
+    """Cost of the SIA gradient (dJ/dGamma, dJ/dela, dJ/dH0 of J = 1/2 |H^N|^2) over the
+    forward run, on the largest member size of the ensemble configuration: n^2 cells, nsteps
+    steps, FP64, from host arrays to host arrays. The taped reverse sweep (one segment when
+    the tape fits half the free device memory) and the recomputing sweep with sqrt(N)
+    checkpoints. Wall clock around synchronised calls, after one untimed run of each."""
+    import math
+    import time
+
+    import torch
+
+    from chmy_gb300 import _abi
+    from chmy_gb300.adjoint import SIA
+    from chmy_gb300.configs import gaussian_random_field, padded_mesh
+    from chmy_gb300.grids import Center, UniformGrid
+
+    T = np.float64
+    grid = UniformGrid(origin=(T(-1), T(-1)), extent=(T(2), T(2)), dims=(n, n), dtype=T)
+    x, y = padded_mesh(grid, Center())
+    bed = 0.4 + 0.3 * gaussian_random_field(x.shape, 0.25, 2.0 / n, 7)
+    H0 = np.clip(0.35 - 0.25 * (x * x + y * y), 0.0, None)
+    p = _abi.cg_sia_params()
+    p.Gamma, p.As, p.n, p.beta, p.ela, p.m_max, p.dt_max, p.cfl = 1.0, 0.0, 3, 0.5, 0.55, 0.25, 0.5, 4.1
+    sia = SIA(arch, grid, bed, p)
+
+    def dJ(h):
+        return np.where(np.isfinite(h), h, 0.0)
+
+    def wall(f):
+        f()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        f()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) * 1e3
+
+    fwd = wall(lambda: sia.run(H0, nsteps))
+    taped = wall(lambda: sia.gradient(H0, nsteps, dJ))
+    K = int(math.ceil(math.sqrt(nsteps)))
+    recomp = wall(lambda: sia.gradient(H0, nsteps, dJ, tape=False, checkpoint_every=K))
+    tape_gb = sia.tape_bytes(nsteps) / 1e9
+    del sia
+    return {
+        "workload": f"SIA gradient w.r.t. Gamma, ela and H0: {n}^2 cells, {nsteps} steps, FP64, host arrays in and out",
+        "forward_ms": fwd,
+        "gradient_taped_ms": taped,
+        "ratio_taped": taped / fwd,
+        "tape_gb": tape_gb,
+        "gradient_recomputing_ms": recomp,
+        "ratio_recomputing": recomp / fwd,
+        "recomputing_checkpoint_every": K,
+    }
 
 
 def fused_kernel_fields(arch, pb):

@@ -130,11 +130,17 @@ class SIA:
     adjoint: the gradient of a misfit J(H^N) with respect to Gamma and ela, and to the initial
     thickness, by reverse time stepping over checkpoints.
 
-    A step reads only H (the flux is recomputed from it), so a checkpoint is one copy of H. The
-    forward sweep keeps every `checkpoint_every`-th state. The reverse sweep recomputes each
-    segment's states from its checkpoint, then runs cg_sia_adjoint_step over them backwards.
-    Memory: nsteps / checkpoint_every + checkpoint_every states. checkpoint_every = 1 keeps
-    every state and recomputes nothing."""
+    A step reads only H (the flux is recomputed from it), so a checkpoint is one copy of H.
+    Two reverse sweeps:
+    - taped (default): cg_sia_run_taped records, per step, what the reverse step needs (about
+      9 arrays of H's size), and cg_sia_adjoint_run sweeps a whole segment in one call without
+      recomputing anything. The whole run is one segment when its tape fits `tape_budget`
+      bytes (default: half the free device memory), else segments of as many steps as fit,
+      each re-run taped from its checkpoint.
+    - recomputing (tape=False): the forward keeps every `checkpoint_every`-th state; the
+      reverse recomputes each segment's states from its checkpoint and runs
+      cg_sia_adjoint_step over them backwards. Memory: nsteps / checkpoint_every +
+      checkpoint_every states."""
 
     def __init__(self, arch, grid, B: np.ndarray, params, dtype=np.float64):
         self.arch, self.grid, self.params = arch, grid, params
@@ -145,6 +151,37 @@ class SIA:
         self.q = [Field(arch, grid, (Vertex(), C), dtype), Field(arch, grid, (C, Vertex()), dtype)]
         self.lam = [Field(arch, grid, C, dtype), Field(arch, grid, C, dtype)]
         self._q = (_abi.cg_field * 3)(self.q[0].desc(), self.q[1].desc(), _abi.cg_field())
+        self._tape = None
+
+    def tape_bytes(self, nsteps: int) -> int:
+        """Device bytes of a tape of `nsteps` steps."""
+        b = ctypes.c_size_t()
+        rc = self.arch.lib.cg_sia_tape_bytes(ctypes.byref(self.grid.desc()), ctypes.byref(self.H.desc()), int(nsteps), ctypes.byref(b))
+        if rc != 0:
+            raise ValueError("cg_sia_tape_bytes: bad arguments")
+        return int(b.value)
+
+    def _tape_buffer(self, nbytes: int):
+        import torch
+
+        if self._tape is None or self._tape.numel() < nbytes:
+            self._tape = None
+            self._tape = torch.empty(nbytes, dtype=torch.uint8, device=self.H.data.device)
+            if self._tape.data_ptr() % 256:
+                raise RuntimeError("the tape allocation is not 256-byte aligned")
+        return self._tape
+
+    def _steps_taped(self, nsteps: int) -> None:
+        nbytes = self.tape_bytes(nsteps)
+        tape = self._tape_buffer(nbytes)
+        self.arch.call("cg_sia_run_taped", ctypes.byref(self.grid.desc()), ctypes.byref(self.H.desc()), ctypes.byref(self.B.desc()),
+                       self._q, ctypes.byref(self.params), int(nsteps), ctypes.c_void_p(tape.data_ptr()), nbytes, None)
+
+    def _reverse_taped(self, dJ) -> None:
+        """Reverse sweep over the tape of the last _steps_taped call: lam[0] in and out."""
+        self.arch.call("cg_sia_adjoint_run", ctypes.byref(self.grid.desc()), ctypes.byref(self.params),
+                       ctypes.c_void_p(self._tape.data_ptr()), self._tape.numel(), ctypes.byref(self.lam[0].desc()),
+                       ctypes.byref(self.lam[1].desc()), dJ)
 
     def _steps(self, nsteps: int, timed: bool = False) -> float:
         """`nsteps` forward steps in one call; the model time (which synchronises) if `timed`."""
@@ -166,9 +203,13 @@ class SIA:
         self.arch.call("cg_sia_adjoint_step", ctypes.byref(self.grid.desc()), ctypes.byref(self.H.desc()), ctypes.byref(self.B.desc()),
                        ctypes.byref(self.params), ctypes.byref(self.lam[0].desc()), ctypes.byref(self.lam[1].desc()), tmp)
 
-    def gradient(self, H0: np.ndarray, nsteps: int, misfit_grad, checkpoint_every: int | None = None):
+    def gradient(self, H0: np.ndarray, nsteps: int, misfit_grad, checkpoint_every: int | None = None, tape: bool = True,
+                 tape_budget: int | None = None):
         """(dJ/dGamma, dJ/dela, dJ/dH0, H^N). `misfit_grad(HN)` returns dJ/dH^N as a padded host
-        array (its interior is used)."""
+        array (its interior is used). With `tape`, `checkpoint_every` caps the segment length
+        (default: the whole run if its tape fits `tape_budget`)."""
+        if tape:
+            return self._gradient_taped(H0, nsteps, misfit_grad, checkpoint_every, tape_budget)
         K = int(checkpoint_every or max(1, math.ceil(math.sqrt(nsteps))))
         self.H.from_numpy(H0)
         self.reset_accumulators()
@@ -197,3 +238,31 @@ class SIA:
                 cur = 1 - cur
             del states
         return dJ[0], dJ[1], self.lam[cur].to_numpy(), HN
+
+    def _gradient_taped(self, H0, nsteps, misfit_grad, checkpoint_every, tape_budget):
+        import torch
+
+        if tape_budget is None:
+            free, _ = torch.cuda.mem_get_info(self.H.data.device)
+            tape_budget = free // 2
+        per_step = self.tape_bytes(1) - self.tape_bytes(0)
+        K = max(1, min(nsteps, (int(tape_budget) - self.tape_bytes(0)) // per_step))
+        if checkpoint_every:
+            K = min(K, int(checkpoint_every))
+        self.H.from_numpy(H0)
+        starts = list(range(0, nsteps, K))
+        checkpoints = {}
+        for start in starts[:-1]:  # plain forward up to the last segment, keeping its start states
+            checkpoints[start] = self.H.data.clone()
+            self._steps(K)
+        last = starts[-1]
+        self._steps_taped(nsteps - last)
+        HN = self.H.to_numpy()
+        self.lam[0].from_numpy(misfit_grad(HN))
+        dJ = (ctypes.c_double * 2)(0.0, 0.0)
+        self._reverse_taped(dJ)
+        for start in reversed(starts[:-1]):
+            self.H.data.copy_(checkpoints.pop(start))
+            self._steps_taped(K)
+            self._reverse_taped(dJ)
+        return dJ[0], dJ[1], self.lam[0].to_numpy(), HN

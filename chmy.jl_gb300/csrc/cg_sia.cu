@@ -20,17 +20,56 @@ __device__ __forceinline__ T S_at(const SiaV<T>& v, int i, int j) {
     return v.B(i, j, 0) + v.H(i, j, 0);
 }
 
+// ∇S at the cell's lower faces (a0, b0) and interpolated to the cell (ax, ay) (sia.jl:43-45)
+template <class T>
+__device__ __forceinline__ void grads_at(const SiaV<T>& v, int i, int j, T* a0, T* b0, T* ax, T* ay) {
+    const T s = S_at(v, i, j);
+    *a0 = (s - S_at(v, i - 1, j)) * v.idx;
+    const T a1 = (S_at(v, i + 1, j) - s) * v.idx;
+    *b0 = (s - S_at(v, i, j - 1)) * v.idy;
+    const T b1 = (S_at(v, i, j + 1) - s) * v.idy;
+    *ax = fma(T(0.5), a1 - *a0, *a0);
+    *ay = fma(T(0.5), b1 - *b0, *b0);
+}
+
 // D = (Gamma H^(n+2) + As H^n) vmag(∇S)^(n-1) at cell (i, j) (sia.jl:43-49)
 template <class T>
 __device__ __forceinline__ T D_at(const SiaV<T>& v, int i, int j) {
-    const T s = S_at(v, i, j);
-    const T a0 = (s - S_at(v, i - 1, j)) * v.idx;
-    const T a1 = (S_at(v, i + 1, j) - s) * v.idx;
-    const T b0 = (s - S_at(v, i, j - 1)) * v.idy;
-    const T b1 = (S_at(v, i, j + 1) - s) * v.idy;
-    const T ax = fma(T(0.5), a1 - a0, a0);
-    const T ay = fma(T(0.5), b1 - b0, b0);
+    T a0, b0, ax, ay;
+    grads_at(v, i, j, &a0, &b0, &ax, &ay);
     return cgsia::D_cell(v.H(i, j, 0), ax, ay, v.Gamma, v.As, v.n);
+}
+
+// The tape arrays of one step, in H's layout (cgsia::TapeArray), and its word block.
+template <class T>
+struct TapeV {
+    DF<T> a[cgsia::kArrays];
+    cgsia::TapeWords* w;
+};
+
+// The derivative factors of D at a cell for the tape, from the forward's own intermediates:
+// dD/dh, dD/dV 2 ax, dD/dV 2 ay and dD/dGamma.
+template <class T>
+__device__ __forceinline__ void tape_D_factors(const SiaV<T>& v, const TapeV<T>& tp, int i, int j, T h, T ax, T ay) {
+    const int n = v.n;
+    const T V = ax * ax + ay * ay;
+    T vp = cgsia::pow_int(V, (n - 1) >> 1);
+    if ((n - 1) & 1) vp = vp * sqrt(V);
+    const T hn1 = cgsia::pow_int(h, n - 1);
+    const T hn = hn1 * h;
+    const T A = hn * fma(v.Gamma, h * h, v.As);
+    T dDdV = T(0);
+    if (n >= 3) {
+        T vq = cgsia::pow_int(V, (n - 3) >> 1);
+        if ((n - 3) & 1) vq = vq * sqrt(V);
+        dDdV = A * T(0.5) * T(n - 1) * vq;
+    } else if (n == 2 && V > T(0)) {
+        dDdV = A * T(0.5) / sqrt(V);
+    }
+    tp.a[cgsia::kDH](i, j, 0) = (v.Gamma * T(n + 2) * h * h + v.As * T(n)) * hn1 * vp;
+    tp.a[cgsia::kEX](i, j, 0) = dDdV * T(2) * ax;
+    tp.a[cgsia::kEY](i, j, 0) = dDdV * T(2) * ay;
+    tp.a[cgsia::kGF](i, j, 0) = hn * h * h * vp;
 }
 
 using cgsia::bits_of;
@@ -55,16 +94,25 @@ __global__ void sia_q_kernel(const SiaV<T> v, int nx, int ny, unsigned long long
     if (dmax_bits) cgsia::block_max_bits(in ? bits_of(dc) : 0ull, dmax_bits);
 }
 
-// D over cells [0, n]^2 into v.D and max over the interior [1, n]^2.
-template <class T>
-__global__ void sia_D_kernel(const SiaV<T> v, int nx, int ny, unsigned long long* dmax_bits) {
+// D over cells [0, n]^2 into v.D and max over the interior [1, n]^2. TAPE: v.D is the tape's
+// D, and the interior cells also record their lower faces' gradients and D's derivatives.
+template <class T, bool TAPE = false>
+__global__ void sia_D_kernel(const SiaV<T> v, int nx, int ny, unsigned long long* dmax_bits, const TapeV<T> tp) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const bool in = i <= nx && j <= ny;
     T d = T(0);
     if (in) {
-        d = D_at(v, i, j);
+        T a0, b0, ax, ay;
+        grads_at(v, i, j, &a0, &b0, &ax, &ay);
+        const T h = v.H(i, j, 0);
+        d = cgsia::D_cell(h, ax, ay, v.Gamma, v.As, v.n);
         v.D(i, j, 0) = d;
+        if (TAPE && i >= 1 && j >= 1) {
+            tp.a[cgsia::kGX](i, j, 0) = a0;
+            tp.a[cgsia::kGY](i, j, 0) = b0;
+            tape_D_factors(v, tp, i, j, h, ax, ay);
+        }
     }
     cgsia::block_max_bits(in && i >= 1 && j >= 1 ? bits_of(d) : 0ull, dmax_bits);
 }
@@ -83,24 +131,34 @@ __global__ void sia_q_from_D_kernel(const SiaV<T> v, int nx, int ny) {
     v.qy(i, j, 0) = -Dy * ((sc - S_at(v, i, j - 1)) * v.idy);
 }
 
-// update_H! over [1, n]^2; dt from a scalar or from device memory.
-template <class T>
-__global__ void sia_H_kernel(const SiaV<T> v, int nx, int ny, T dt_scalar, const double* dt_dev) {
+// update_H! over [1, n]^2; dt from a scalar or from device memory. TAPE: also W, the two
+// masks, and the first interior cell where D attains the step's maximum.
+template <class T, bool TAPE = false>
+__global__ void sia_H_kernel(const SiaV<T> v, int nx, int ny, T dt_scalar, const double* dt_dev, const TapeV<T> tp) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
     if (i > nx || j > ny) return;
     const T dt = dt_dev ? (T)*dt_dev : dt_scalar;
     const T h = v.H(i, j, 0);
-    const T m = fmin(v.beta * (S_at(v, i, j) - v.ela), v.m_max);
+    const T x = v.beta * (S_at(v, i, j) - v.ela);
+    const T m = fmin(x, v.m_max);
     T dv = (v.qx(i + 1, j, 0) - v.qx(i, j, 0)) * v.idx;
     dv = dv + (v.qy(i, j + 1, 0) - v.qy(i, j, 0)) * v.idy;
-    v.H(i, j, 0) = fmax(h + dt * (-dv + m), T(0.0));
+    const T W = -dv + m;
+    const T u = h + dt * W;
+    v.H(i, j, 0) = fmax(u, T(0.0));
+    if (TAPE) {
+        tp.a[cgsia::kW](i, j, 0) = W;
+        tp.a[cgsia::kFL](i, j, 0) = T((u > T(0) ? 1 : 0) + (x < v.m_max ? 2 : 0));
+        if (bits_of(v.D(i, j, 0)) == tp.w->dmax) atomicMin(&tp.w->arg, (unsigned long long)((long)j * (nx + 2) + i));
+    }
 }
 
 // Δt = min(min(Δ)^2 / max(D) / cfl, dt_max); t += Δt; reset the max slot for the next step.
+// `tw` (optional): the step's tape words.
 template <class T>
 __global__ void sia_dt_kernel(unsigned long long* dmax_bits, double* dt, double* t, double dx2, double cfl,
-                              double dt_max) {
+                              double dt_max, cgsia::TapeWords* tw) {
     const unsigned long long b = *dmax_bits;
     double dmax;
     if (sizeof(T) == 8) {
@@ -111,9 +169,19 @@ __global__ void sia_dt_kernel(unsigned long long* dmax_bits, double* dt, double*
     // Julia: Δ^2 / maximum(D) / 4.1 in the grid type
     const T v = (T)dx2 / (T)dmax / (T)cfl;
     double d = fmin((double)v, dt_max);
-    if (!(dmax > 0.0)) d = dt_max;
+    bool capped = !((double)v < dt_max);
+    if (!(dmax > 0.0)) {
+        d = dt_max;
+        capped = true;
+    }
     *dt = d;
     *t = *t + d;
+    if (tw) {
+        tw->dmax = b;
+        tw->arg = ~0ull;
+        tw->dt = d;
+        tw->capped = capped ? 1.0 : 0.0;
+    }
     *dmax_bits = 0ull;
 }
 
@@ -192,7 +260,7 @@ int update_H_t(cg_ctx* ctx, const cg_grid* g, const cg_field* H, const cg_field*
                const cg_sia_params* p) {
     const SiaV<T> v = make_view<T>(g, H, B, q, p, nullptr);
     const dim3 block(32, 8), grid(cg_div_up(g->n[0], 32), cg_div_up(g->n[1], 8));
-    sia_H_kernel<T><<<grid, block, 0, ctx->stream>>>(v, g->n[0], g->n[1], (T)dt, nullptr);
+    sia_H_kernel<T><<<grid, block, 0, ctx->stream>>>(v, g->n[0], g->n[1], (T)dt, nullptr, TapeV<T>{});
     CG_CHECK_LAUNCH(ctx);
     cg_bc qb[2], hb;
     sia_bcs(qb, &hb);
@@ -201,7 +269,7 @@ int update_H_t(cg_ctx* ctx, const cg_grid* g, const cg_field* H, const cg_field*
 
 template <class T>
 int run_t(cg_ctx* ctx, const cg_grid* g, const cg_field* H, const cg_field* B, const cg_field* q,
-          const cg_sia_params* p, int nsteps, double* t_host) {
+          const cg_sia_params* p, int nsteps, double* t_host, char* tape = nullptr) {
     // scratch: D (same padded layout as H) + 3 words (max bits, dt, t)
     long cnt = 1;
     for (int d = 0; d < 2; ++d) cnt *= (H->n[d] + 4L * H->halo[d]);
@@ -230,15 +298,33 @@ int run_t(cg_ctx* ctx, const cg_grid* g, const cg_field* H, const cg_field* B, c
     cg_key_add(key, *p);
     cg_key_add(key, nsteps);
     cg_key_add(key, base);
+    cg_key_add(key, tape);
+    const cgsia::TapeGeom tg = cgsia::tape_geom(*H, sizeof(T));
     rc = cg_graph_run(ctx, key, [&](cudaStream_t st) {
         for (int s = 0; s < nsteps; ++s) {
-            sia_D_kernel<T><<<gD, block, 0, st>>>(v, nx, ny, words);
-            sia_q_from_D_kernel<T><<<gI, block, 0, st>>>(v, nx, ny);
+            SiaV<T> vs = v;
+            TapeV<T> tp{};
+            if (tape) {
+                char* sb = tape + 256 + (size_t)s * tg.step_bytes;
+                tp.w = reinterpret_cast<cgsia::TapeWords*>(sb);
+                for (int k = 0; k < cgsia::kArrays; ++k) {
+                    tp.a[k] = v.H;
+                    tp.a[k].p = reinterpret_cast<T*>(sb + 256 + (size_t)k * tg.abytes) + cg_origin_offset(*H);
+                }
+                vs.D = tp.a[cgsia::kD];
+                sia_D_kernel<T, true><<<gD, block, 0, st>>>(vs, nx, ny, words, tp);
+            } else {
+                sia_D_kernel<T><<<gD, block, 0, st>>>(vs, nx, ny, words, tp);
+            }
+            sia_q_from_D_kernel<T><<<gI, block, 0, st>>>(vs, nx, ny);
             CG_CHECK_LAUNCH(ctx);
             int r = cg_bc_apply_impl(ctx, g, 2, q, qb);
             if (r) return r;
-            sia_dt_kernel<T><<<1, 1, 0, st>>>(words, dt, t, dx2, p->cfl, p->dt_max);
-            sia_H_kernel<T><<<gI, block, 0, st>>>(v, nx, ny, T(0), dt);
+            sia_dt_kernel<T><<<1, 1, 0, st>>>(words, dt, t, dx2, p->cfl, p->dt_max, tp.w);
+            if (tape)
+                sia_H_kernel<T, true><<<gI, block, 0, st>>>(vs, nx, ny, T(0), dt, tp);
+            else
+                sia_H_kernel<T><<<gI, block, 0, st>>>(vs, nx, ny, T(0), dt, tp);
             CG_CHECK_LAUNCH(ctx);
             r = cg_bc_apply_impl(ctx, g, 1, H, &hb);
             if (r) return r;
@@ -273,6 +359,59 @@ extern "C" int cg_sia_update_H(cg_ctx* ctx, const cg_grid* grid, const cg_field*
     cudaSetDevice(ctx->device);
     return H->dtype == CG_F64 ? update_H_t<double>(ctx, grid, H, q, B, dt, p)
                               : update_H_t<float>(ctx, grid, H, q, B, dt, p);
+}
+
+extern "C" int cg_sia_tape_bytes(const cg_grid* grid, const cg_field* H, int nsteps, size_t* bytes) {
+    if (!grid || !H || !bytes || nsteps < 0) return CG_ERR_ARG;
+    if (grid->ndim != 2 || (H->dtype != CG_F32 && H->dtype != CG_F64)) return CG_ERR_ARG;
+    const cgsia::TapeGeom tg = cgsia::tape_geom(*H, H->dtype == CG_F64 ? 8 : 4);
+    *bytes = 256 + (size_t)nsteps * tg.step_bytes;
+    return CG_OK;
+}
+
+extern "C" int cg_sia_run_taped(cg_ctx* ctx, const cg_grid* grid, const cg_field* H, const cg_field* B,
+                                const cg_field* q, const cg_sia_params* p, int nsteps, void* tape, size_t tape_bytes,
+                                double* t_host) {
+    int rc = check_sia(ctx, grid, H, B, q, p);
+    if (rc) return rc;
+    if (!q) return cg_fail(ctx, CG_ERR_ARG, "sia_run_taped: q is NULL");
+    if (nsteps < 1) return cg_fail(ctx, CG_ERR_ARG, "sia_run_taped: nsteps < 1");
+    if (p->cfl <= 0 || p->dt_max <= 0) return cg_fail(ctx, CG_ERR_ARG, "sia_run_taped: cfl and dt_max must be > 0");
+    size_t need = 0;
+    cg_sia_tape_bytes(grid, H, nsteps, &need);
+    if (!tape || tape_bytes < need)
+        return cg_fail(ctx, CG_ERR_ARG, "sia_run_taped: the tape holds %zu bytes, %d steps need %zu", tape_bytes, nsteps, need);
+    if (reinterpret_cast<uintptr_t>(tape) & 255) return cg_fail(ctx, CG_ERR_ARG, "sia_run_taped: the tape is not 256-byte aligned");
+    cudaSetDevice(ctx->device);
+    const size_t elem = H->dtype == CG_F64 ? 8 : 4;
+    const cgsia::TapeGeom tg = cgsia::tape_geom(*H, elem);
+    cgsia::TapeHeader hd;
+    std::memset(&hd, 0, sizeof(hd));
+    hd.magic = cgsia::kTapeMagic;
+    hd.dtype = H->dtype;
+    hd.nx = grid->n[0];
+    hd.ny = grid->n[1];
+    hd.nsteps = nsteps;
+    hd.stride0 = H->stride[0];
+    hd.stride1 = H->stride[1];
+    hd.halo0 = H->halo[0];
+    hd.halo1 = H->halo[1];
+    hd.n0 = H->n[0];
+    hd.n1 = H->n[1];
+    hd.cnt = (long long)tg.cnt;
+    hd.step_bytes = (long long)tg.step_bytes;
+    hd.Gamma = p->Gamma;
+    hd.As = p->As;
+    hd.beta = p->beta;
+    hd.ela = p->ela;
+    hd.m_max = p->m_max;
+    hd.cfl = p->cfl;
+    hd.dt_max = p->dt_max;
+    hd.n = p->n;
+    CG_CUDA(ctx, cudaMemcpyAsync(tape, &hd, sizeof(hd), cudaMemcpyHostToDevice, ctx->stream));
+    char* tp = static_cast<char*>(tape);
+    return H->dtype == CG_F64 ? run_t<double>(ctx, grid, H, B, q, p, nsteps, t_host, tp)
+                              : run_t<float>(ctx, grid, H, B, q, p, nsteps, t_host, tp);
 }
 
 extern "C" int cg_sia_run(cg_ctx* ctx, const cg_grid* grid, const cg_field* H, const cg_field* B, const cg_field* q,

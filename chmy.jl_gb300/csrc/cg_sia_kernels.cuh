@@ -46,4 +46,54 @@ using cgk::bits_of;
 
 using cgk::block_max_bits;
 
+// ---- tape of a forward run, read by the reverse sweep ---------------------------------------
+//
+// A taped forward step records what the reverse step would otherwise recompute in FP64. This
+// trades HBM traffic, which the SIA kernels barely use, for FP64 instructions, which bound them.
+// Layout: a 256-byte header, then per step a 256-byte word block and kArrays arrays of `cnt`
+// elements in H's padded layout (each rounded up to 256 bytes).
+enum TapeArray {
+    kD = 0,   // D over cells [0, n]^2
+    kGX = 1,  // dS/dx at the cell's lower x face ((S_i - S_i-1)/dx)
+    kGY = 2,  // dS/dy at the lower y face
+    kDH = 3,  // dD/dh
+    kEX = 4,  // dD/dV 2 ax  (V = ax^2 + ay^2)
+    kEY = 5,  // dD/dV 2 ay
+    kGF = 6,  // dD/dGamma = h^(n+2) V^((n-1)/2)
+    kW = 7,   // W = -divg(q) + M
+    kFL = 8,  // 1 if H + dt W > 0, plus 2 if beta (S - ela) < m_max
+    kArrays = 9
+};
+
+struct TapeHeader {
+    unsigned long long magic;
+    int dtype, nx, ny, nsteps;
+    long long stride0, stride1, halo0, halo1, n0, n1, cnt, step_bytes;
+    double Gamma, As, beta, ela, m_max, cfl, dt_max;
+    int n, pad;
+};
+constexpr unsigned long long kTapeMagic = 0x3145504154414953ull;  // "SIATAPE1"
+
+// per step: the forward's Dmax bits, the first interior argmax (j (nx+2) + i), dt and whether
+// dt was capped at dt_max
+struct TapeWords {
+    unsigned long long dmax;
+    unsigned long long arg;
+    double dt;
+    double capped;
+};
+
+struct TapeGeom {
+    size_t cnt, abytes, step_bytes;
+};
+
+// elements per array: H's allocation (row stride x padded rows)
+inline TapeGeom tape_geom(const cg_field& H, size_t elem) {
+    TapeGeom g;
+    g.cnt = (size_t)H.stride[1] * (size_t)(H.n[1] + 4 * H.halo[1]);
+    g.abytes = (g.cnt * elem + 255) & ~(size_t)255;
+    g.step_bytes = 256 + (size_t)kArrays * g.abytes;
+    return g;
+}
+
 }  // namespace cgsia

@@ -20,6 +20,7 @@
 #ifndef CHMY_GB300_H
 #define CHMY_GB300_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #if defined(__GNUC__)
@@ -486,6 +487,28 @@ CG_API int cg_sia_ensemble_run(cg_ctx* ctx, int nmembers, const cg_sia_member* m
 CG_API int cg_sia_adjoint_step(cg_ctx* ctx, const cg_grid* grid, const cg_field* H, const cg_field* B,
                                const cg_sia_params* p, const cg_field* lam, const cg_field* lam_out,
                                double* dJ);
+
+/* Bytes of a tape that records `nsteps` steps of cg_sia_run_taped for an H of this layout:
+ * a 256-byte header, then per step 256 bytes of words and 9 arrays of H's allocation. No
+ * context and no device work. */
+CG_API int cg_sia_tape_bytes(const cg_grid* grid, const cg_field* H, int nsteps, size_t* bytes);
+
+/* cg_sia_run (same arguments, same results bit for bit) that also records, for each of its
+ * `nsteps` (>= 1) steps, what the reverse step needs: D, the face gradients, the derivatives
+ * of D, W = -divg(q) + M, the two masks, and the step's Dmax, argmax and dt. `tape` is device
+ * memory of at least cg_sia_tape_bytes bytes, 256-byte aligned (no reference counterpart). */
+CG_API int cg_sia_run_taped(cg_ctx* ctx, const cg_grid* grid, const cg_field* H, const cg_field* B,
+                            const cg_field* q, const cg_sia_params* p, int nsteps, void* tape,
+                            size_t tape_bytes, double* t_host);
+
+/* The reverse sweep over a tape of cg_sia_run_taped, in one call: on entry lam holds dJ/dH at
+ * the interior cells after the taped run's last step; on return it holds dJ/dH at its start.
+ * dJ (host, may be NULL) gains dJ/dGamma in dJ[0] and dJ/dela in dJ[1]; the call synchronises
+ * the stream. `work` is a field of lam's layout, overwritten. lam, work and p must match the
+ * taped run's layout and parameters (the tape's header is checked). The sweep reads the
+ * tape and recomputes nothing; its arithmetic is that of cg_sia_adjoint_step. */
+CG_API int cg_sia_adjoint_run(cg_ctx* ctx, const cg_grid* grid, const cg_sia_params* p, const void* tape,
+                              size_t tape_bytes, const cg_field* lam, const cg_field* work, double* dJ);
 
 #ifdef __cplusplus
 }

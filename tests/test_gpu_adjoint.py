@@ -173,12 +173,16 @@ def _sia_problem(n=(48, 40), dt_max=0.5):
     return grid, bed.astype(T), H0.astype(T), p
 
 
+@pytest.mark.parametrize("tape", [True, False], ids=["taped", "recomputing"])
 @pytest.mark.parametrize("dt_max", [0.5, 1e-3])
-def test_sia_gradient_gamma_ela_matches_finite_differences(arch, dt_max):
+def test_sia_gradient_gamma_ela_matches_finite_differences(arch, dt_max, tape):
     """SIA time loop (config 5 form, 2D 48 x 40, 60 steps): the adjoint gradients of
     J = 1/2 |H^N - H_obs|^2 with respect to log(Gamma) and ela agree with central differences
     to 1e-6, with the adaptive time step (dt_max = 0.5: dt from max D) and with dt capped
-    (dt_max = 1e-3); checkpointing every 1, 7 and sqrt(N) steps gives the same bits."""
+    (dt_max = 1e-3), for the taped and the recomputing reverse sweeps. Recomputing with
+    checkpoints every 1, 7 and sqrt(N) steps gives the same bits; taped segments of 1 and 7
+    steps give the same dJ/dH0 bits and dJ/dGamma, dJ/dela to 1e-13 (the per-segment sums
+    associate differently)."""
     from chmy_gb300.adjoint import SIA
 
     grid, bed, H0, p = _sia_problem(dt_max=dt_max)
@@ -198,11 +202,14 @@ def test_sia_gradient_gamma_ela_matches_finite_differences(arch, dt_max):
         g[inner] = h[inner] - obs
         return g
 
-    gG, gE, gH0, HN2 = sia.gradient(H0, nsteps, dJ)
+    gG, gE, gH0, HN2 = sia.gradient(H0, nsteps, dJ, tape=tape)
     assert np.array_equal(HN, HN2)
     for K in (1, 7):
-        a, b, c, _ = sia.gradient(H0, nsteps, dJ, checkpoint_every=K)
-        assert (a, b) == (gG, gE) and np.array_equal(c, gH0)
+        a, b, c, _ = sia.gradient(H0, nsteps, dJ, checkpoint_every=K, tape=tape)
+        if tape:
+            assert abs(a - gG) <= 1e-13 * abs(gG) and abs(b - gE) <= 1e-13 * abs(gE) and np.array_equal(c, gH0)
+        else:
+            assert (a, b) == (gG, gE) and np.array_equal(c, gH0)
 
     def J_at(H=H0, **kw):
         q = _abi.cg_sia_params()
@@ -225,8 +232,9 @@ def test_sia_gradient_gamma_ela_matches_finite_differences(arch, dt_max):
     assert abs(gH0[idx] - fdH) <= 1e-6 * max(abs(fdH), float(np.abs(gH0).max())), (gH0[idx], fdH)
 
 
+@pytest.mark.parametrize("tape", [True, False], ids=["taped", "recomputing"])
 @pytest.mark.parametrize("dt_max", [0.5, 1e-3])
-def test_sia_gradient_matches_dual_numbers(arch, dt_max):
+def test_sia_gradient_matches_dual_numbers(arch, dt_max, tape):
     """The SIA adjoint gradients (GPU, reverse sweep) against forward-mode dual numbers run
     through the oracle's restated time loop (exact tangents of its arithmetic, including the
     adaptive dt through max D): dJ/dGamma and dJ/dela agree to 1e-9 relative. The remaining
@@ -260,7 +268,91 @@ def test_sia_gradient_matches_dual_numbers(arch, dt_max):
         return out
 
     sia = SIA(arch, grid, bed, p)
-    gG, gE, _, HN = sia.gradient(H0, nsteps, dJ)
+    gG, gE, _, HN = sia.gradient(H0, nsteps, dJ, tape=tape)
     assert np.max(np.abs(HN[inner] - H.a[inner])) <= 1e-12 * np.max(np.abs(H.a[inner]))
     assert abs(gG - dual_G) <= 1e-9 * abs(dual_G), (gG, dual_G)
     assert abs(gE - dual_E) <= 1e-9 * abs(dual_E), (gE, dual_E)
+
+
+@pytest.mark.parametrize("T", [np.float32, np.float64])
+def test_sia_taped_run_equals_plain_run_and_sweeps_agree(arch, T):
+    """cg_sia_run_taped gives cg_sia_run's H and t bit for bit, and the taped reverse sweep
+    (cg_sia_adjoint_run, nothing recomputed) agrees with the recomputing one
+    (cg_sia_adjoint_step per step): dJ/dH0, dJ/dGamma and dJ/dela to 1e-12 (FP64) / 1e-4
+    (FP32) relative. An odd step count ends the ping-pong in the work field."""
+    import torch
+
+    from chmy_gb300 import Field
+    from chmy_gb300.adjoint import SIA
+    from chmy_gb300.grids import Center, UniformGrid, Vertex
+
+    grid0, bed, H0, p = _sia_problem(n=(45, 38))
+    grid = UniformGrid(origin=(T(-1), T(-1)), extent=(T(2), T(2)), dims=(45, 38), dtype=T)
+    nsteps = 33
+    C = Center()
+    H, B = Field(arch, grid, C, T), Field(arch, grid, C, T)
+    q = [Field(arch, grid, (Vertex(), C), T), Field(arch, grid, (C, Vertex()), T)]
+    qd = (_abi.cg_field * 3)(q[0].desc(), q[1].desc(), _abi.cg_field())
+    B.from_numpy(bed.astype(T))
+    g = grid.desc()
+    H.from_numpy(H0.astype(T))
+    t_plain = ctypes.c_double()
+    arch.call("cg_sia_run", ctypes.byref(g), ctypes.byref(H.desc()), ctypes.byref(B.desc()), qd, ctypes.byref(p), nsteps,
+              ctypes.byref(t_plain))
+    H_plain = H.to_numpy()
+    nbytes = ctypes.c_size_t()
+    assert arch.lib.cg_sia_tape_bytes(ctypes.byref(g), ctypes.byref(H.desc()), nsteps, ctypes.byref(nbytes)) == 0
+    tape = torch.empty(nbytes.value, dtype=torch.uint8, device=H.data.device)
+    H.from_numpy(H0.astype(T))
+    t_taped = ctypes.c_double()
+    arch.call("cg_sia_run_taped", ctypes.byref(g), ctypes.byref(H.desc()), ctypes.byref(B.desc()), qd, ctypes.byref(p), nsteps,
+              ctypes.c_void_p(tape.data_ptr()), nbytes.value, ctypes.byref(t_taped))
+    assert np.array_equal(H.to_numpy(), H_plain, equal_nan=True)
+    assert t_taped.value == t_plain.value
+
+    inner = (slice(2, -2), slice(2, -2))
+    obs = H_plain[inner] * 0.9
+
+    def dJ(h):
+        out = np.zeros_like(h)
+        out[inner] = h[inner] - obs
+        return out
+
+    sia = SIA(arch, grid, bed.astype(T), p, dtype=T)
+    a = sia.gradient(H0.astype(T), nsteps, dJ, tape=True)
+    b = sia.gradient(H0.astype(T), nsteps, dJ, tape=False, checkpoint_every=1)
+    tol = 1e-12 if T == np.float64 else 1e-4
+    assert abs(a[0] - b[0]) <= tol * abs(b[0]), (a[0], b[0])
+    assert abs(a[1] - b[1]) <= tol * abs(b[1]), (a[1], b[1])
+    ga, gb = a[2][2:-2, 2:-2].astype(np.float64), b[2][2:-2, 2:-2].astype(np.float64)
+    assert np.max(np.abs(ga - gb)) <= tol * np.max(np.abs(gb))
+
+
+def test_sia_adjoint_run_argument_errors(arch):
+    """cg_sia_adjoint_run refuses a buffer without a tape header, parameters other than the taped
+    run's, and aliased lambda and work."""
+    import torch
+
+    from chmy_gb300 import _abi as abi
+    from chmy_gb300.adjoint import SIA
+
+    grid, bed, H0, p = _sia_problem(n=(40, 32))
+    sia = SIA(arch, grid, bed, p)
+    sia.H.from_numpy(H0)
+    sia._steps_taped(3)
+    g = grid.desc()
+    lam, work = sia.lam[0].desc(), sia.lam[1].desc()
+    tp = ctypes.c_void_p(sia._tape.data_ptr())
+    n = sia._tape.numel()
+    blank = torch.zeros(4096, dtype=torch.uint8, device=sia.H.data.device)
+    rc = arch.lib.cg_sia_adjoint_run(arch.ctx, ctypes.byref(g), ctypes.byref(p), ctypes.c_void_p(blank.data_ptr()), 4096,
+                                     ctypes.byref(lam), ctypes.byref(work), None)
+    assert rc == abi.CG_ERR_ARG
+    q = abi.cg_sia_params()
+    ctypes.memmove(ctypes.byref(q), ctypes.byref(p), ctypes.sizeof(q))
+    q.ela = p.ela + 0.1
+    assert arch.lib.cg_sia_adjoint_run(arch.ctx, ctypes.byref(g), ctypes.byref(q), tp, n, ctypes.byref(lam), ctypes.byref(work), None) == abi.CG_ERR_ARG
+    assert arch.lib.cg_sia_adjoint_run(arch.ctx, ctypes.byref(g), ctypes.byref(p), tp, n, ctypes.byref(lam), ctypes.byref(lam), None) == abi.CG_ERR_ARG
+    assert arch.lib.cg_sia_adjoint_run(arch.ctx, ctypes.byref(g), ctypes.byref(p), tp, 100, ctypes.byref(lam), ctypes.byref(work), None) == abi.CG_ERR_ARG
+    dJ = (ctypes.c_double * 2)()
+    arch.call("cg_sia_adjoint_run", ctypes.byref(g), ctypes.byref(p), tp, n, ctypes.byref(lam), ctypes.byref(work), dJ)
