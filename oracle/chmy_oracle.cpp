@@ -148,9 +148,10 @@ T itp_rec(const Fd<T>& f, const int* to, const int* dims, int m, const int* I, i
     const T a = itp_rec(f, to, dims, m - 1, Il, rule);
     const T b = itp_rec(f, to, dims, m - 1, Ir, rule);
     const T t = T(0.5);
-    if (rule == 0) return std::fma(t, b - a, a);
+    using std::fma;  // unqualified below: the dual type's overload is found by ADL
+    if (rule == 0) return fma(t, b - a, a);
     const T ia = T(1) / a, ib = T(1) / b;
-    return T(1) / std::fma(t, ib - ia, ia);
+    return T(1) / fma(t, ib - ia, ia);
 }
 template <class T>
 T itp(const Fd<T>& f, const int* to, int i, int j, int k, int rule) {
@@ -467,9 +468,10 @@ void stokes_update_stress_t(const cg_grid* grid, const cg_stokes_fields* f, cons
                 I10[b] -= 1;
                 I01[a] -= 1;
                 const T e00 = ie.at(I00), e10 = ie.at(I10), e01 = ie.at(I01), e11 = ie.at(I11);
-                const T lo = std::fma(T(0.5), e10 - e00, e00);
-                const T hi = std::fma(T(0.5), e11 - e01, e01);
-                const T iev = std::fma(T(0.5), hi - lo, lo);
+                using std::fma;
+                const T lo = fma(T(0.5), e10 - e00, e00);
+                const T hi = fma(T(0.5), e11 - e01, e01);
+                const T iev = fma(T(0.5), hi - lo, lo);
                 const T eve = T(1) / (iev + inv_Gdt);
                 const T r = -(t - to_) * inv_Gdt - t * iev + T(2.0) * eod;
                 tau[c](i, j, k) = t + r * eve * dtau_r;
@@ -960,6 +962,113 @@ int or_maxabs(int nfields, const cg_field* fields, double* out, int32_t* nonfini
         out[i] = fields[i].dtype == CG_F64 ? maxabs_t<double>(fields[i], &bad) : maxabs_t<float>(fields[i], &bad);
     if (nonfinite) *nonfinite = bad;
     return CG_OK;
+}
+
+/* The PT iterations of the VE Stokes step with a viscosity field (update_stress!,
+   update_velocity!, bc!(V => bc_V[d]) each; examples/stokes_2d_inc_ve_T.jl:20-43 with the
+   variable-viscosity rules above) run in dual numbers until the value and both tangents reach
+   their fixed point. The tangents are the exact derivatives of the converged discrete state
+   with respect to log(eta) along the directions dir[0], dir[1] (FP64 fields of eta's layout;
+   eta.d[k] = eta dir[k] at every point, so a direction that is zero outside the interior
+   leaves the ghost viscosities fixed). `f` holds the FP64 initial state (V, r_V, P, divV, tau,
+   tau_old and eta are required; inv_eta must be absent). Every `ncheck` iterations the
+   residuals are read: max |r_V| over the points not fixed by bc_V (interior points, boundary
+   nodes excluded) and max |divV| over the cells. Converged when the value's are <= tol and
+   each tangent's are <= tol max(1, max |dV_k|). dV[k nd + d] (FP64, V[d]'s layout) receive
+   the tangents of V[d]; the value stays in f. Returns 0 when converged within max_iter, else
+   4 (timeout); *iterations gets the count. */
+int or_stokes_solve_tangent(const cg_grid* grid, const cg_stokes_fields* f, const cg_stokes_params* p,
+                            const cg_bc* bc_V, const cg_field* dir, double tol, int max_iter, int ncheck,
+                            const cg_field* dV, int* iterations) {
+    const int nd = grid->ndim, nt = nd == 2 ? 3 : 6;
+    if (!f->eta.data || f->inv_eta.data || !f->divV.data || !f->P.data) return CG_ERR_ARG;
+    std::vector<std::vector<Dual>> store;
+    store.reserve(40);
+    cg_stokes_fields fD;
+    std::memset(&fD, 0, sizeof(fD));
+    auto span_of = [](const cg_field& a) {
+        long span = 1;
+        for (int d = 0; d < a.ndim; ++d) span += (long)(a.n[d] + 4 * a.halo[d] - 1) * a.stride[d];
+        return span;
+    };
+    auto dualize = [&](const cg_field& src, cg_field& dst) {
+        if (!src.data) return;
+        store.emplace_back();
+        dst = like_field(src, store.back());
+        const double* s = static_cast<const double*>(src.data);
+        Dual* t = store.back().data();
+        for (long q = 0; q < span_of(src); ++q) t[q] = Dual(s[q]);
+    };
+    for (int d = 0; d < nd; ++d) {
+        dualize(f->V[d], fD.V[d]);
+        dualize(f->r_V[d], fD.r_V[d]);
+        dualize(f->rho_g[d], fD.rho_g[d]);
+        if (!f->V[d].data || !f->r_V[d].data) return CG_ERR_ARG;
+    }
+    for (int c = 0; c < nt; ++c) {
+        dualize(f->tau[c], fD.tau[c]);
+        dualize(f->tau_old[c], fD.tau_old[c]);
+        if (!f->tau[c].data || !f->tau_old[c].data) return CG_ERR_ARG;
+    }
+    dualize(f->P, fD.P);
+    dualize(f->divV, fD.divV);
+    dualize(f->eta, fD.eta);
+    {
+        Dual* e = static_cast<Dual*>(fD.eta.data);
+        for (int k = 0; k < 2; ++k) {
+            const double* w = static_cast<const double*>(dir[k].data);
+            for (long q = 0; q < span_of(f->eta); ++q) e[q].d[k] = e[q].v * w[q];
+        }
+    }
+    const int n0 = grid->n[0], n1 = nd > 1 ? grid->n[1] : 1, n2 = nd > 2 ? grid->n[2] : 1;
+    auto residuals = [&](double* out /* value, tangent 0, tangent 1, max |dV_0|, max |dV_1| */) {
+        for (int k = 0; k < 5; ++k) out[k] = 0.0;
+        auto take = [&](const Dual& r) {
+            out[0] = std::max(out[0], std::fabs(r.v));
+            out[1] = std::max(out[1], std::fabs(r.d[0]));
+            out[2] = std::max(out[2], std::fabs(r.d[1]));
+        };
+        for (int d = 0; d < nd; ++d) {
+            Fd<Dual> r(fD.r_V[d]), v(fD.V[d]);
+            for (int k = (nd > 2 ? 1 : 0); k <= (nd > 2 ? n2 : 0); ++k)
+                for (int j = 1; j <= n1; ++j)
+                    for (int i = 1; i <= n0; ++i) {
+                        const int I[3] = {i, j, k};
+                        if (I[d] == 1) continue;  // the boundary node of V[d] along d
+                        take(r(i, j, k));
+                        out[3] = std::max(out[3], std::fabs(v(i, j, k).d[0]));
+                        out[4] = std::max(out[4], std::fabs(v(i, j, k).d[1]));
+                    }
+        }
+        Fd<Dual> dv(fD.divV);
+        for (int k = (nd > 2 ? 1 : 0); k <= (nd > 2 ? n2 : 0); ++k)
+            for (int j = 1; j <= n1; ++j)
+                for (int i = 1; i <= n0; ++i) take(dv(i, j, k));
+    };
+    bc_apply_t<Dual>(grid, nd, fD.V, bc_V);
+    int it = 0;
+    bool conv = false;
+    while (it < max_iter && !conv) {
+        for (int c = 0; c < ncheck && it < max_iter; ++c, ++it) {
+            stokes_update_stress_t<Dual>(grid, &fD, p);
+            stokes_update_velocity_t<Dual>(grid, &fD, p);
+            bc_apply_t<Dual>(grid, nd, fD.V, bc_V);
+        }
+        double r[5];
+        residuals(r);
+        conv = r[0] <= tol && r[1] <= tol * std::max(1.0, r[3]) && r[2] <= tol * std::max(1.0, r[4]);
+    }
+    for (int d = 0; d < nd; ++d) {
+        const Dual* v = static_cast<const Dual*>(fD.V[d].data);
+        double* val = static_cast<double*>(f->V[d].data);
+        for (long q = 0; q < span_of(f->V[d]); ++q) val[q] = v[q].v;
+        for (int k = 0; k < 2; ++k) {
+            double* o = static_cast<double*>(dV[k * nd + d].data);
+            for (long q = 0; q < span_of(f->V[d]); ++q) o[q] = v[q].d[k];
+        }
+    }
+    if (iterations) *iterations = it;
+    return conv ? CG_OK : CG_ERR_TIMEOUT;
 }
 
 /* The SIA time loop of examples/sia.jl:71-81 (update_q!, bc!, dt = min(Δ²/max D/cfl,

@@ -31,6 +31,8 @@ _SIGS = {
     "or_diffusion_update_C": ([P(_abi.cg_grid), P(_abi.cg_field), P(_abi.cg_field), C.c_double], C.c_int),
     "or_sia_run_tangent": ([P(_abi.cg_grid), P(_abi.cg_field), P(_abi.cg_field), P(_abi.cg_field), P(_abi.cg_sia_params), C.c_int,
                             P(_abi.cg_field), P(_abi.cg_field)], C.c_int),
+    "or_stokes_solve_tangent": ([P(_abi.cg_grid), P(_abi.cg_stokes_fields), P(_abi.cg_stokes_params), P(_abi.cg_bc),
+                                 P(_abi.cg_field), C.c_double, C.c_int, C.c_int, P(_abi.cg_field), P(C.c_int)], C.c_int),
     "or_diffusion_compute_q_masked": ([P(_abi.cg_grid), P(_abi.cg_field), P(_abi.cg_field), C.c_double, P(_abi.cg_mask)], C.c_int),
     "or_diffusion_update_C_masked": ([P(_abi.cg_grid), P(_abi.cg_field), P(_abi.cg_field), C.c_double, P(_abi.cg_mask)], C.c_int),
     "or_stokes_update_old": ([P(_abi.cg_grid), P(_abi.cg_stokes_fields)], C.c_int),
@@ -185,3 +187,65 @@ def op(opcode, grid, Cf=None, C1=None, C2=None, V=None, chi=None):
     Va = desc_array(V, 3) if V is not None else None
     rc = lib().or_op_kernel(opcode, C.byref(g), ref(Cf), ref(C1), ref(C2), Va, ref(chi))
     assert rc == 0
+
+
+def stokes_problem_fields(pb):
+    """Host NpFields (FP64) of a StokesProblem's initial state, for the oracle: a dict with
+    V, r_V, tau, tau_old (lists), P, divV, eta and rho_g (list, None where absent), and the
+    cg_stokes_fields over them under "desc"."""
+    grid = pb.grid
+    nd = grid.ndim
+    Cl, Vl = Center(), Vertex()
+    vlocs = [tuple(Vl if e == d else Cl for e in range(nd)) for d in range(nd)]
+    if nd == 2:
+        tlocs = [(Cl, Cl), (Cl, Cl), (Vl, Vl)]
+    else:
+        tlocs = [(Cl, Cl, Cl)] * 3 + [(Vl, Vl, Cl), (Vl, Cl, Vl), (Cl, Vl, Vl)]
+
+    def nf(loc, arr):
+        f = NpField(grid, loc, np.float64)
+        f.a[...] = arr
+        return f
+
+    h = pb.host
+    out = {
+        "V": [nf(l, a) for l, a in zip(vlocs, h["V"])],
+        "r_V": [nf(l, a) for l, a in zip(vlocs, h["r_V"])],
+        "tau": [nf(l, a) for l, a in zip(tlocs, h["tau"])],
+        "tau_old": [nf(l, a) for l, a in zip(tlocs, h["tau_old"])],
+        "P": nf(Cl, h["P"]),
+        "divV": nf(Cl, h["divV"]),
+        "eta": nf(Cl, h["eta"]),
+        "rho_g": [None if a is None else nf(l, a) for l, a in zip(vlocs, list(h.get("rho_g", [])) + [None] * nd)],
+    }
+    rho = out["rho_g"] if any(r is not None for r in out["rho_g"]) else None
+    s = stokes_desc(V=out["V"], r_V=out["r_V"], P=out["P"], divV=out["divV"], tau=out["tau"], tau_old=out["tau_old"],
+                    eta=out["eta"])
+    if rho is not None:
+        for d, r in enumerate(rho):
+            if r is not None:
+                s.rho_g[d] = r.desc()
+    out["desc"] = s
+    out["vlocs"] = vlocs
+    return out
+
+
+def stokes_tangent_solve(pb, dirs, tol=1e-11, max_iter=400000, ncheck=100):
+    """or_stokes_solve_tangent on pb's initial state along the two log-viscosity directions
+    `dirs` (host arrays of eta's padded shape). Returns (fields dict with the converged value,
+    tangents [k][d] as padded arrays, iterations)."""
+    grid = pb.grid
+    nd = grid.ndim
+    fs = stokes_problem_fields(pb)
+    dfields = []
+    for a in dirs:
+        f = NpField(grid, Center(), np.float64)
+        f.a[...] = a
+        dfields.append(f)
+    dV = [NpField(grid, fs["vlocs"][d], np.float64) for _ in range(2) for d in range(nd)]
+    it = C.c_int()
+    bcs = (_abi.cg_bc * nd)(*pb.bc_V)
+    rc = lib().or_stokes_solve_tangent(C.byref(grid.desc()), C.byref(fs["desc"]), C.byref(pb.params), bcs,
+                                       desc_array(dfields), tol, max_iter, ncheck, desc_array(dV), C.byref(it))
+    assert rc == 0, (rc, it.value)
+    return fs, [[dV[k * nd + d].a for d in range(nd)] for k in range(2)], it.value

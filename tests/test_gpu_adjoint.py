@@ -1,6 +1,9 @@
-"""Adjoint gradient of a velocity misfit with respect to log-viscosity (steady VE Stokes step,
-variable viscosity) against central finite differences of the forward solve, in 2D and 3D: the
-differences agree with the adjoint gradient to 1e-6 of its largest value."""
+"""Adjoint gradients against central finite differences and forward-mode dual numbers:
+- a velocity misfit of the steady VE Stokes step with respect to log-viscosity, 2D and 3D
+  (differences to 1e-6 of the largest gradient; the dual-number tangents of the oracle's PT
+  iterations to 1e-7 along random directions);
+- implicit diffusion with respect to D and the initial state;
+- the SIA time loop with respect to Gamma, ela and the initial thickness."""
 
 import ctypes
 import dataclasses
@@ -87,6 +90,45 @@ def test_gradient_log_eta_3d_matches_finite_differences(arch):
     pb = stokes3d_grf(16, ncheck=8)
     pb = dataclasses.replace(pb, eps=1e-12, max_iter=2000 * 16)
     _check(arch, pb, [(3, 4, 5), (8, 8, 8), (12, 2, 10), (0, 15, 7)])
+
+
+def _check_dual(arch, pb, tol=1e-7):
+    """The adjoint gradient's directional derivatives along two random log-viscosity
+    directions (zero in the ghost cells) against forward-mode dual numbers run through the
+    oracle's PT iterations to their fixed point (or_stokes_solve_tangent)."""
+    from _oracle import stokes_tangent_solve
+
+    nd, n = pb.grid.ndim, pb.grid.dims[0]
+    fwd = _solve(arch, pb)
+    rng = np.random.default_rng(7)
+    v = fwd.fields["V"][nd - 1].to_numpy()
+    obs = v[_sensor(nd, n)] + 0.1 * rng.standard_normal(v[_sensor(nd, n)].shape)
+    _, dJ = _misfit(fwd, nd, n, obs)
+    grad, res = fwd.gradient_log_eta([None] * (nd - 1) + [dJ], eps=pb.eps)
+    assert res.converged == 1
+    inner = (slice(2, n + 2),) * nd
+    g = grad.to_numpy()[inner]
+    shape = pb.host["eta"].shape
+    dirs = []
+    for _ in range(2):
+        d = np.zeros(shape)
+        d[inner] = rng.standard_normal((n,) * nd)
+        dirs.append(d)
+    _, tan, iters = stokes_tangent_solve(pb, dirs)
+    for k in range(2):
+        adj = float(np.sum(g * dirs[k][inner]))
+        dual = float(np.sum(dJ * tan[k][nd - 1]))
+        assert abs(adj - dual) <= tol * abs(dual), (k, adj, dual, iters)
+
+
+def test_gradient_log_eta_2d_matches_dual_numbers(arch):
+    pb = stokes2d_inclusions(32, ncheck=8)
+    _check_dual(arch, dataclasses.replace(pb, eps=1e-12, max_iter=2000 * 32))
+
+
+def test_gradient_log_eta_3d_matches_dual_numbers(arch):
+    pb = stokes3d_grf(16, ncheck=8)
+    _check_dual(arch, dataclasses.replace(pb, eps=1e-12, max_iter=2000 * 16))
 
 
 def _ptdiff_problem(n, T=np.float64):

@@ -566,3 +566,38 @@ def test_sia_dual_tangents_match_oracle_differences():
     fdE = (plain(p.Gamma, p.ela + h) - plain(p.Gamma, p.ela - h)) / (2 * h)
     assert np.max(np.abs(tG.a - fdG)) <= 1e-6 * np.max(np.abs(fdG))
     assert np.max(np.abs(tE.a - fdE)) <= 1e-6 * np.max(np.abs(fdE))
+
+
+def test_stokes_dual_tangents_match_oracle_differences():
+    """The oracle's dual-number VE Stokes solve (or_stokes_solve_tangent, 2D 16^2 with 8
+    viscous inclusions): a zero direction leaves the tangents zero, and the tangent of a
+    velocity misfit along a random log-viscosity direction agrees with central differences
+    of the oracle's own converged solve to 1e-6."""
+    import dataclasses
+
+    from _oracle import stokes_tangent_solve
+
+    from chmy_gb300.configs import stokes2d_inclusions
+
+    pb = stokes2d_inclusions(16, ncheck=8)
+    shape = pb.host["eta"].shape
+    rng = np.random.default_rng(4)
+    dirv = np.zeros(shape)
+    dirv[2:-2, 2:-2] = rng.standard_normal((16, 16))
+    zero = np.zeros(shape)
+    fs, tan, iters = stokes_tangent_solve(pb, [dirv, zero])
+    assert iters > 0 and not np.any(tan[1][0]) and not np.any(tan[1][1])
+    vy = fs["V"][1].a
+    sens = (slice(2, 18), 10)  # Vy on one interior vertex row
+    obs = vy[sens] * 0.7
+    dual = float(np.sum((vy[sens] - obs) * tan[0][1][sens]))
+
+    def J(scale):
+        e = pb.host["eta"] * np.exp(scale * dirv)
+        f, _, _ = stokes_tangent_solve(dataclasses.replace(pb, host={**pb.host, "eta": e}), [zero, zero])
+        r = f["V"][1].a[sens] - obs
+        return 0.5 * float(np.sum(r * r))
+
+    h = 1e-5
+    fd = (J(h) - J(-h)) / (2 * h)
+    assert abs(dual - fd) <= 1e-6 * abs(fd), (dual, fd)
