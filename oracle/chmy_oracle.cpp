@@ -693,7 +693,8 @@ void ptdiff_update_q_t(const cg_grid* grid, const cg_ptdiff_fields* f, const cg_
             int Il[3] = {i, j, k};
             Il[d] -= 1;
             const T dl = D.at(Il), dc = D(i, j, k);
-            const T Df = std::fma(T(0.5), dc - dl, dl);
+            using std::fma;  // unqualified: the dual type's overload is found by ADL
+            const T Df = fma(T(0.5), dc - dl, dl);
             const T gC = partial(C, g, d, i, j, k);
             const T qo = q[d](i, j, k);
             q[d](i, j, k) = qo + (-(Df * gC) - qo) * om;
@@ -1069,6 +1070,66 @@ int or_stokes_solve_tangent(const cg_grid* grid, const cg_stokes_fields* f, cons
     }
     if (iterations) *iterations = it;
     return conv ? CG_OK : CG_ERR_TIMEOUT;
+}
+
+/* The time loop of cg_ptdiff_run (nsteps implicit steps: C_old <- C, then npt PT iterations
+   of update_q, update_C and bc!(C => bc)) in dual numbers, with tangents along the two
+   log-diffusivity directions dir[0], dir[1] (FP64, D's layout: D.d[k] = D dir[k] at every
+   point). f holds FP64 host fields C, C_old, D and q (R must be absent); C advances in place.
+   dC[k] (FP64, C's layout) receive the exact derivatives of the final C of this discrete loop
+   (with its npt iterations per step) along dir[k]. */
+int or_ptdiff_run_tangent(const cg_grid* grid, const cg_ptdiff_fields* f, const cg_ptdiff_params* p,
+                          const cg_bc* bc, int nsteps, int npt, const cg_field* dir, const cg_field* dC) {
+    const int nd = grid->ndim;
+    if (!f->C.data || !f->C_old.data || !f->D.data || f->R.data) return CG_ERR_ARG;
+    auto span_of = [](const cg_field& a) {
+        long span = 1;
+        for (int d = 0; d < a.ndim; ++d) span += (long)(a.n[d] + 4 * a.halo[d] - 1) * a.stride[d];
+        return span;
+    };
+    std::vector<std::vector<Dual>> store;
+    store.reserve(8);
+    cg_ptdiff_fields fD;
+    std::memset(&fD, 0, sizeof(fD));
+    auto dualize = [&](const cg_field& src, cg_field& dst) {
+        store.emplace_back();
+        dst = like_field(src, store.back());
+        const double* s = static_cast<const double*>(src.data);
+        Dual* t = store.back().data();
+        for (long q = 0; q < span_of(src); ++q) t[q] = Dual(s[q]);
+    };
+    dualize(f->C, fD.C);
+    dualize(f->C_old, fD.C_old);
+    dualize(f->D, fD.D);
+    for (int d = 0; d < nd; ++d) {
+        if (!f->q[d].data) return CG_ERR_ARG;
+        dualize(f->q[d], fD.q[d]);
+    }
+    {
+        Dual* e = static_cast<Dual*>(fD.D.data);
+        for (int k = 0; k < 2; ++k) {
+            const double* w = static_cast<const double*>(dir[k].data);
+            for (long q = 0; q < span_of(f->D); ++q) e[q].d[k] = e[q].v * w[q];
+        }
+    }
+    Dual* c = static_cast<Dual*>(fD.C.data);
+    Dual* co = static_cast<Dual*>(fD.C_old.data);
+    const long cspan = std::min(span_of(f->C), span_of(f->C_old));
+    for (int step = 0; step < nsteps; ++step) {
+        for (long q = 0; q < cspan; ++q) co[q] = c[q];
+        for (int it = 0; it < npt; ++it) {
+            ptdiff_update_q_t<Dual>(grid, &fD, p);
+            ptdiff_update_C_t<Dual>(grid, &fD, p);
+            bc_apply_t<Dual>(grid, 1, &fD.C, bc);
+        }
+    }
+    double* cv = static_cast<double*>(f->C.data);
+    for (long q = 0; q < span_of(f->C); ++q) cv[q] = c[q].v;
+    for (int k = 0; k < 2; ++k) {
+        double* o = static_cast<double*>(dC[k].data);
+        for (long q = 0; q < span_of(f->C); ++q) o[q] = c[q].d[k];
+    }
+    return CG_OK;
 }
 
 /* The SIA time loop of examples/sia.jl:71-81 (update_q!, bc!, dt = min(Δ²/max D/cfl,

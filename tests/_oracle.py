@@ -33,6 +33,8 @@ _SIGS = {
                             P(_abi.cg_field), P(_abi.cg_field)], C.c_int),
     "or_stokes_solve_tangent": ([P(_abi.cg_grid), P(_abi.cg_stokes_fields), P(_abi.cg_stokes_params), P(_abi.cg_bc),
                                  P(_abi.cg_field), C.c_double, C.c_int, C.c_int, P(_abi.cg_field), P(C.c_int)], C.c_int),
+    "or_ptdiff_run_tangent": ([P(_abi.cg_grid), P(_abi.cg_ptdiff_fields), P(_abi.cg_ptdiff_params), P(_abi.cg_bc), C.c_int, C.c_int,
+                               P(_abi.cg_field), P(_abi.cg_field)], C.c_int),
     "or_diffusion_compute_q_masked": ([P(_abi.cg_grid), P(_abi.cg_field), P(_abi.cg_field), C.c_double, P(_abi.cg_mask)], C.c_int),
     "or_diffusion_update_C_masked": ([P(_abi.cg_grid), P(_abi.cg_field), P(_abi.cg_field), C.c_double, P(_abi.cg_mask)], C.c_int),
     "or_stokes_update_old": ([P(_abi.cg_grid), P(_abi.cg_stokes_fields)], C.c_int),
@@ -249,3 +251,28 @@ def stokes_tangent_solve(pb, dirs, tol=1e-11, max_iter=400000, ncheck=100):
                                        desc_array(dfields), tol, max_iter, ncheck, desc_array(dV), C.byref(it))
     assert rc == 0, (rc, it.value)
     return fs, [[dV[k * nd + d].a for d in range(nd)] for k in range(2)], it.value
+
+
+def ptdiff_tangent_run(grid, D, C0, params, bc, nsteps, npt, dirs):
+    """or_ptdiff_run_tangent from C0 (flux starting at zero) with diffusivity D (host arrays,
+    FP64, padded) along the two log-D directions `dirs`. Returns (C^N, [dC^N/d eps_k])."""
+    nd = grid.ndim
+    Cl, Vl = Center(), Vertex()
+
+    def nf(loc, arr=None):
+        f = NpField(grid, loc, np.float64)
+        if arr is not None:
+            f.a[...] = arr
+        return f
+
+    Cf, Co, Df = nf(Cl, C0), nf(Cl, C0), nf(Cl, D)
+    q = [nf(tuple(Vl if e == d else Cl for e in range(nd))) for d in range(nd)]
+    fs = _abi.cg_ptdiff_fields()
+    fs.C, fs.C_old, fs.D = Cf.desc(), Co.desc(), Df.desc()
+    fs.q = desc_array(q, 3)
+    dfields = [nf(Cl, a) for a in dirs]
+    dC = [nf(Cl), nf(Cl)]
+    rc = lib().or_ptdiff_run_tangent(C.byref(grid.desc()), C.byref(fs), C.byref(params), C.byref(bc), int(nsteps), int(npt),
+                                     desc_array(dfields), desc_array(dC))
+    assert rc == 0, rc
+    return Cf.a.copy(), [d.a.copy() for d in dC]

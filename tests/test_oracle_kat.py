@@ -601,3 +601,41 @@ def test_stokes_dual_tangents_match_oracle_differences():
     h = 1e-5
     fd = (J(h) - J(-h)) / (2 * h)
     assert abs(dual - fd) <= 1e-6 * abs(fd), (dual, fd)
+
+
+def test_ptdiff_dual_tangents_match_oracle_differences():
+    """The oracle's dual-number PT-diffusion loop (or_ptdiff_run_tangent, 2D 16^2, 3 implicit
+    steps of 400 PT iterations): a zero direction leaves the tangent zero, and the tangent of a
+    misfit of C^N along a random log-diffusivity direction agrees with central differences of
+    the same loop to 1e-6."""
+    from _oracle import ptdiff_tangent_run
+
+    from chmy_gb300.bcs import Dirichlet, Neumann, to_cg_bc
+    from chmy_gb300.configs import box_smooth, padded_mesh, ptdiff_params
+
+    T = np.float64
+    n, nsteps, npt = 16, 3, 400
+    grid = UniformGrid(origin=(T(-0.5), T(-0.5)), extent=(T(1), T(1)), dims=(n, n), dtype=T)
+    x, y = padded_mesh(grid, Center())
+    rng = np.random.default_rng(2)
+    D = np.exp(box_smooth(rng.standard_normal(x.shape)))
+    C0 = np.exp(-(x * x + y * y) / 0.01)
+    bc = to_cg_bc(2, {"x": Dirichlet(0.0), "y": Neumann()})
+    p = ptdiff_params(grid, 1e-3, float(D.max()))
+    dirv = np.zeros(x.shape)
+    dirv[2:-2, 2:-2] = rng.standard_normal((n, n))
+    zero = np.zeros(x.shape)
+    CN, tan = ptdiff_tangent_run(grid, D, C0, p, bc, nsteps, npt, [dirv, zero])
+    assert not np.any(tan[1])
+    inner = (slice(2, n + 2), slice(2, n + 2))
+    obs = CN[inner] * 0.8
+    dual = float(np.sum((CN[inner] - obs) * tan[0][inner]))
+
+    def J(scale):
+        c, _ = ptdiff_tangent_run(grid, D * np.exp(scale * dirv), C0, p, bc, nsteps, npt, [zero, zero])
+        r = c[inner] - obs
+        return 0.5 * float(np.sum(r * r))
+
+    h = 1e-5
+    fd = (J(h) - J(-h)) / (2 * h)
+    assert abs(dual - fd) <= 1e-6 * abs(fd), (dual, fd)
