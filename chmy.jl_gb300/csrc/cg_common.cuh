@@ -52,6 +52,8 @@ struct cg_tune_cfg {
     int variant;  // kernel variant (3D: block shape)
 };
 bool cg_autotune_enabled();
+// CG_TUNE_VERBOSE=1: the autotuners print every candidate's time to stderr
+bool cg_tune_verbose();
 bool cg_tune_lookup(const std::string& key, cg_tune_cfg* out);
 void cg_tune_store(const std::string& key, const cg_tune_cfg& cfg);
 

@@ -113,6 +113,14 @@ bool cg_sia_persistent_enabled() {
     return e && e[0] == '1';
 }
 
+bool cg_tune_verbose() {
+    static const bool on = [] {
+        const char* e = std::getenv("CG_TUNE_VERBOSE");
+        return e && e[0] == '1';
+    }();
+    return on;
+}
+
 bool cg_tune_lookup(const std::string& key, cg_tune_cfg* out) {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune.find(key);

@@ -483,6 +483,8 @@ inline cg_tune_cfg tune_march2d(const Fused2D<T>& f, const SP<T>& s, int n0, int
     for (int seg : {0, 8, 16, 24, 32, 48, 64}) {
         if (seg > n1 + 2) continue;
         const float t = time_launches([&] { return launch_march2d<T, false>(f, s, n0, n1, nsm, seg, st); }, st);
+        if (cg_tune_verbose())
+            std::fprintf(stderr, "march2d tune %dx%d: seg %d: %.1f us\n", n0, n1, seg, t >= 0.f ? 1e3f * t / 3 : -1.f);
         if (t >= 0.f && t < tbest) {
             tbest = t;
             best = cg_tune_cfg{seg, 0};
@@ -515,6 +517,9 @@ inline cg_tune_cfg tune_march3d(const Fused3D<T>& f, const SP<T>& s, int n0, int
             if (seg > n2 + 2) continue;
             const float t =
                 time_launches([&] { return launch_march3d<T, false>(f, s, n0, n1, n2, nsm, seg, st, v); }, st);
+            if (cg_tune_verbose())
+                std::fprintf(stderr, "march3d tune %dx%dx%d: seg %d variant %d: %.1f us\n", n0, n1, n2, seg, v,
+                             t >= 0.f ? 1e3f * t / 3 : -1.f);
             if (t >= 0.f && t < tbest) {
                 tbest = t;
                 best = cg_tune_cfg{seg, v};
