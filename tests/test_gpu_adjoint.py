@@ -127,8 +127,9 @@ def test_gradient_log_eta_2d_matches_dual_numbers(arch):
 
 
 def test_gradient_log_eta_3d_matches_dual_numbers(arch):
-    pb = stokes3d_grf(16, ncheck=8)
-    _check_dual(arch, dataclasses.replace(pb, eps=1e-12, max_iter=2000 * 16))
+    """The 32^3 copy of the 3D VE Stokes configuration (random log-viscosity field)."""
+    pb = stokes3d_grf(32, ncheck=8)
+    _check_dual(arch, dataclasses.replace(pb, eps=1e-12, max_iter=2000 * 32))
 
 
 def _ptdiff_problem(n, T=np.float64):
