@@ -655,6 +655,53 @@ def config_suite(arch, stream, peak):
     torch.cuda.empty_cache()
     out["sia_adjoint"] = sia_adjoint_cost(arch)
     torch.cuda.empty_cache()
+    out["stokes3d_adjoint"] = stokes3d_adjoint_cost(arch)
+    torch.cuda.empty_cache()
+    return out
+
+
+def stokes3d_adjoint_cost(arch, n=256):
+    """The 3D VE Stokes configuration (n^3, random log-viscosity field, buoyant sphere): the
+    forward solve to residual 1e-8 and the adjoint solve for dJ/d log(eta) of a misfit of Vz on
+    the middle vertex plane (scaled so that max |dJ/dV| = 1), both in FP32 PT iterations inside
+    FP64 defect correction. Wall clock around synchronised calls."""
+    import time
+
+    import torch
+
+    from chmy_gb300 import _abi
+    from chmy_gb300.configs import stokes3d_grf
+    from chmy_gb300.solvers import StokesSolver
+
+    pb = stokes3d_grf(n)
+    s = StokesSolver(arch, pb)
+    s.apply_bc()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    res = s.solve(precision=_abi.CG_F32)
+    torch.cuda.synchronize()
+    tf = time.perf_counter() - t0
+    v = s.fields["V"][2].to_numpy()
+    sens = (n // 2 + 2, slice(2, n + 2), slice(2, n + 2))
+    r = np.random.default_rng(3).standard_normal(v[sens].shape)
+    dJ = np.zeros_like(v)
+    dJ[sens] = r / np.abs(r).max()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    grad, ares = s.gradient_log_eta([None, None, dJ], precision=_abi.CG_F32)
+    torch.cuda.synchronize()
+    ta = time.perf_counter() - t0
+    out = {
+        "workload": f"3D VE Stokes {n}^3, log-viscosity Gaussian random field, forward solve and adjoint solve for dJ/d log(eta), FP32 PT in FP64 defect correction, residual 1e-8",
+        "forward_s": tf,
+        "forward_iterations": int(res.iterations),
+        "forward_converged": int(res.converged),
+        "adjoint_s": ta,
+        "adjoint_iterations": int(ares.iterations),
+        "adjoint_converged": int(ares.converged),
+        "gradient_over_forward": (tf + ta) / tf,
+    }
+    del s, grad
     return out
 
 
