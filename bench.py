@@ -657,7 +657,67 @@ def config_suite(arch, stream, peak):
     torch.cuda.empty_cache()
     out["stokes3d_adjoint"] = stokes3d_adjoint_cost(arch)
     torch.cuda.empty_cache()
+    out["sia_ensemble_adjoint"] = sia_ensemble_adjoint_cost(arch)
+    torch.cuda.empty_cache()
     return out
+
+
+def sia_ensemble_adjoint_cost(arch, members=64, nsteps=1000):
+    """The SIA ensemble configuration's gradient: per member, dJ/dGamma, dJ/dela and dJ/dH0 of
+    J_m = 1/2 |H_m^N|^2 over the interior, for 64 members of 128^2..1024^2 (seed 6, FP64) over
+    1000 steps, all members in each launch (SIAEnsemble: taped segments as large as half the free
+    device memory holds, re-run from checkpoints). Wall clock from host arrays to host arrays,
+    against the ensemble's forward run timed the same way."""
+    import time
+
+    import torch
+
+    from chmy_gb300.adjoint import SIAEnsemble
+    from chmy_gb300.configs import sia_ensemble
+
+    ens_cfg = sia_ensemble(members=members)
+    H0s = []
+    for grid, hh, p in ens_cfg:  # a dome of ice on every member, so that every member flows
+        H0s.append(hh["H"] + np.clip(0.35 - 0.25 * _dome_r2(grid), 0.0, None))
+    ens = SIAEnsemble(arch, [(g, hh["B"], p) for g, hh, p in ens_cfg])
+
+    def dJ(m, h):
+        g = np.zeros_like(h)
+        g[2:-2, 2:-2] = h[2:-2, 2:-2]
+        return g
+
+    def wall(f):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = f()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) * 1e3, r
+
+    ens.run(H0s, 2)
+    fwd, _ = wall(lambda: ens.run(H0s, nsteps))
+    grad, r = wall(lambda: ens.gradient(H0s, nsteps, dJ))
+    per_step = ens.tape_bytes(1) - ens.tape_bytes(0)
+    free, _ = torch.cuda.mem_get_info()
+    cells = sum(g.dims[0] * g.dims[1] for g, _, _ in ens_cfg)
+    out = {
+        "workload": f"SIA ensemble gradient: {members} members of 128^2..1024^2 ({cells} cells), {nsteps} steps, FP64, all members per launch",
+        "forward_ms": fwd,
+        "gradient_ms": grad,
+        "ratio": grad / fwd,
+        "tape_gb_per_step": per_step / 1e9,
+        "finite": bool(all(np.isfinite(v) for v in r[0] + r[1])),
+    }
+    del ens
+    return out
+
+
+def _dome_r2(grid):
+    """x^2 + y^2 at the padded Center points of a 2D grid on [-1, 1]^2, as a [y, x] array."""
+    from chmy_gb300.configs import padded_mesh
+    from chmy_gb300.grids import Center
+
+    x, y = padded_mesh(grid, Center())
+    return x * x + y * y
 
 
 def stokes3d_adjoint_cost(arch, n=256):

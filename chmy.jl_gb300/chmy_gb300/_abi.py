@@ -238,6 +238,10 @@ SIGNATURES: dict[str, list] = {
     "cg_sia_update_q": [_vp, P(cg_grid), P(cg_field), P(cg_field), P(cg_field), P(cg_sia_params), P(C.c_double)],
     "cg_sia_update_H": [_vp, P(cg_grid), P(cg_field), P(cg_field), P(cg_field), C.c_double, P(cg_sia_params)],
     "cg_sia_ensemble_run": [_vp, C.c_int, P(cg_sia_member), P(cg_sia_params), C.c_int, P(C.c_double)],
+    "cg_sia_ensemble_tape_bytes": [C.c_int, P(cg_sia_member), C.c_int, P(C.c_size_t)],
+    "cg_sia_ensemble_run_taped": [_vp, C.c_int, P(cg_sia_member), P(cg_sia_params), C.c_int, _vp, C.c_size_t, P(C.c_double)],
+    "cg_sia_ensemble_adjoint_run": [_vp, C.c_int, P(cg_sia_member), P(cg_sia_params), _vp, C.c_size_t, P(cg_field), P(cg_field),
+                                    P(C.c_double)],
     "cg_sia_adjoint_step": [_vp, P(cg_grid), P(cg_field), P(cg_field), P(cg_sia_params), P(cg_field), P(cg_field), P(C.c_double)],
     "cg_sia_run": [_vp, P(cg_grid), P(cg_field), P(cg_field), P(cg_field), P(cg_sia_params), C.c_int, P(C.c_double)],
     "cg_sia_tape_bytes": [P(cg_grid), P(cg_field), C.c_int, P(C.c_size_t)],

@@ -266,3 +266,110 @@ class SIA:
             self._steps_taped(K)
             self._reverse_taped(dJ)
         return dJ[0], dJ[1], self.lam[0].to_numpy(), HN
+
+
+class SIAEnsemble:
+    """An ensemble of independent SIA solves of uneven sizes (cg_sia_ensemble_run: every phase of
+    a step is one launch over all members) and its adjoint: per member, the gradient of a
+    misfit J_m(H_m^N) with respect to Gamma_m, ela_m and the initial thickness.
+
+    The reverse sweep is taped: cg_sia_ensemble_run_taped records every member's reverse-step
+    quantities, and cg_sia_ensemble_adjoint_run sweeps them back, all members in each launch.
+    The whole run is one segment when its tape fits `tape_budget` bytes (default: half the free
+    device memory). Otherwise the forward keeps every member's H at the start of each segment
+    of K steps, and each segment is re-run taped before it is swept back."""
+
+    def __init__(self, arch, members, dtype=np.float64):
+        """`members`: a list of (grid, B, cg_sia_params) with B a padded host array."""
+        self.arch = arch
+        self.nm = len(members)
+        C = Center()
+        self.grids, self.params, self.H, self.B, self.q, self.lam, self.work = [], [], [], [], [], [], []
+        for grid, B, p in members:
+            self.grids.append(grid)
+            self.params.append(p)
+            H = Field(arch, grid, C, dtype)
+            Bf = Field(arch, grid, C, dtype)
+            Bf.from_numpy(B)
+            self.H.append(H)
+            self.B.append(Bf)
+            self.q.append([Field(arch, grid, (Vertex(), C), dtype), Field(arch, grid, (C, Vertex()), dtype)])
+            self.lam.append(Field(arch, grid, C, dtype))
+            self.work.append(Field(arch, grid, C, dtype))
+        self._mem = (_abi.cg_sia_member * self.nm)()
+        self._par = (_abi.cg_sia_params * self.nm)(*self.params)
+        for k in range(self.nm):
+            self._mem[k].grid = self.grids[k].desc()
+            self._mem[k].H, self._mem[k].B = self.H[k].desc(), self.B[k].desc()
+            self._mem[k].q[0], self._mem[k].q[1] = self.q[k][0].desc(), self.q[k][1].desc()
+        self._lam = (_abi.cg_field * self.nm)(*[f.desc() for f in self.lam])
+        self._work = (_abi.cg_field * self.nm)(*[f.desc() for f in self.work])
+        self._tape = None
+
+    def tape_bytes(self, nsteps: int) -> int:
+        b = ctypes.c_size_t()
+        if self.arch.lib.cg_sia_ensemble_tape_bytes(self.nm, self._mem, int(nsteps), ctypes.byref(b)) != 0:
+            raise ValueError("cg_sia_ensemble_tape_bytes: bad arguments")
+        return int(b.value)
+
+    def _set(self, H0s) -> None:
+        for H, h0 in zip(self.H, H0s):
+            H.from_numpy(h0)
+
+    def _steps(self, nsteps: int) -> None:
+        if nsteps > 0:
+            self.arch.call("cg_sia_ensemble_run", self.nm, self._mem, self._par, int(nsteps), None)
+
+    def _steps_taped(self, nsteps: int) -> None:
+        import torch
+
+        nbytes = self.tape_bytes(nsteps)
+        if self._tape is None or self._tape.numel() < nbytes:
+            self._tape = None
+            self._tape = torch.empty(nbytes, dtype=torch.uint8, device=self.H[0].data.device)
+            if self._tape.data_ptr() % 256:
+                raise RuntimeError("the tape allocation is not 256-byte aligned")
+        self.arch.call("cg_sia_ensemble_run_taped", self.nm, self._mem, self._par, int(nsteps), ctypes.c_void_p(self._tape.data_ptr()),
+                       nbytes, None)
+
+    def _reverse(self, dJ) -> None:
+        self.arch.call("cg_sia_ensemble_adjoint_run", self.nm, self._mem, self._par, ctypes.c_void_p(self._tape.data_ptr()),
+                       self._tape.numel(), self._lam, self._work, dJ)
+
+    def run(self, H0s, nsteps: int):
+        """Forward: `nsteps` steps from the padded host arrays H0s; returns the H^N arrays."""
+        self._set(H0s)
+        self._steps(nsteps)
+        return [H.to_numpy() for H in self.H]
+
+    def gradient(self, H0s, nsteps: int, misfit_grad, checkpoint_every: int | None = None, tape_budget: int | None = None):
+        """(dJ/dGamma [m], dJ/dela [m], dJ/dH0 [m], H^N [m]). `misfit_grad(m, HN_m)` returns
+        dJ/dH_m^N as a padded host array (its interior is used)."""
+        import torch
+
+        if tape_budget is None:
+            free, _ = torch.cuda.mem_get_info(self.H[0].data.device)
+            tape_budget = free // 2
+        per_step = self.tape_bytes(1) - self.tape_bytes(0)
+        K = max(1, min(nsteps, (int(tape_budget) - self.tape_bytes(0)) // per_step))
+        if checkpoint_every:
+            K = min(K, int(checkpoint_every))
+        self._set(H0s)
+        starts = list(range(0, nsteps, K))
+        checkpoints = {}
+        for start in starts[:-1]:
+            checkpoints[start] = [H.data.clone() for H in self.H]
+            self._steps(K)
+        self._steps_taped(nsteps - starts[-1])
+        HN = [H.to_numpy() for H in self.H]
+        for m in range(self.nm):
+            self.lam[m].from_numpy(misfit_grad(m, HN[m]))
+        dJ = (ctypes.c_double * (2 * self.nm))()
+        self._reverse(dJ)
+        for start in reversed(starts[:-1]):
+            for H, c in zip(self.H, checkpoints.pop(start)):
+                H.data.copy_(c)
+            self._steps_taped(K)
+            self._reverse(dJ)
+        return ([dJ[2 * m] for m in range(self.nm)], [dJ[2 * m + 1] for m in range(self.nm)],
+                [f.to_numpy() for f in self.lam], HN)

@@ -11,6 +11,7 @@ template <class T>
 struct SiaV {
     DF<T> H, B, qx, qy, D;
     T Gamma, As, beta, ela, m_max;
+    T Gn2, Asn;  // Gamma (n+2) and As n, for the taped derivatives of D
     T idx, idy;
     int n;
 };
@@ -40,37 +41,14 @@ __device__ __forceinline__ T D_at(const SiaV<T>& v, int i, int j) {
     return cgsia::D_cell(v.H(i, j, 0), ax, ay, v.Gamma, v.As, v.n);
 }
 
-// The tape arrays of one step, in H's layout (cgsia::TapeArray), and its word block.
+// The tape arrays of one step, in H's layout (cgsia::TapeArray; the masks one byte per cell),
+// and its word block.
 template <class T>
 struct TapeV {
     DF<T> a[cgsia::kArrays];
+    DF<unsigned char> fl;
     cgsia::TapeWords* w;
 };
-
-// The derivative factors of D at a cell for the tape, from the forward's own intermediates:
-// dD/dh, dD/dV 2 ax, dD/dV 2 ay and dD/dGamma.
-template <class T>
-__device__ __forceinline__ void tape_D_factors(const SiaV<T>& v, const TapeV<T>& tp, int i, int j, T h, T ax, T ay) {
-    const int n = v.n;
-    const T V = ax * ax + ay * ay;
-    T vp = cgsia::pow_int(V, (n - 1) >> 1);
-    if ((n - 1) & 1) vp = vp * sqrt(V);
-    const T hn1 = cgsia::pow_int(h, n - 1);
-    const T hn = hn1 * h;
-    const T A = hn * fma(v.Gamma, h * h, v.As);
-    T dDdV = T(0);
-    if (n >= 3) {
-        T vq = cgsia::pow_int(V, (n - 3) >> 1);
-        if ((n - 3) & 1) vq = vq * sqrt(V);
-        dDdV = A * T(0.5) * T(n - 1) * vq;
-    } else if (n == 2 && V > T(0)) {
-        dDdV = A * T(0.5) / sqrt(V);
-    }
-    tp.a[cgsia::kDH](i, j, 0) = (v.Gamma * T(n + 2) * h * h + v.As * T(n)) * hn1 * vp;
-    tp.a[cgsia::kEX](i, j, 0) = dDdV * T(2) * ax;
-    tp.a[cgsia::kEY](i, j, 0) = dDdV * T(2) * ay;
-    tp.a[cgsia::kGF](i, j, 0) = hn * h * h * vp;
-}
 
 using cgsia::bits_of;
 
@@ -106,13 +84,22 @@ __global__ void sia_D_kernel(const SiaV<T> v, int nx, int ny, unsigned long long
         T a0, b0, ax, ay;
         grads_at(v, i, j, &a0, &b0, &ax, &ay);
         const T h = v.H(i, j, 0);
-        d = cgsia::D_cell(h, ax, ay, v.Gamma, v.As, v.n);
-        v.D(i, j, 0) = d;
-        if (TAPE && i >= 1 && j >= 1) {
-            tp.a[cgsia::kGX](i, j, 0) = a0;
-            tp.a[cgsia::kGY](i, j, 0) = b0;
-            tape_D_factors(v, tp, i, j, h, ax, ay);
+        if (TAPE) {
+            using namespace cgsia;
+            T dh, ex, ey, gf;
+            d = D_and_factors(h, ax, ay, v.Gamma, v.As, v.Gn2, v.Asn, v.n, &dh, &ex, &ey, &gf);
+            if (i >= 1 && j >= 1) {
+                tp.a[kGX](i, j, 0) = a0;
+                tp.a[kGY](i, j, 0) = b0;
+                tp.a[kDH](i, j, 0) = dh;
+                tp.a[kEX](i, j, 0) = ex;
+                tp.a[kEY](i, j, 0) = ey;
+                tp.a[kGF](i, j, 0) = gf;
+            }
+        } else {
+            d = cgsia::D_cell(h, ax, ay, v.Gamma, v.As, v.n);
         }
+        v.D(i, j, 0) = d;
     }
     cgsia::block_max_bits(in && i >= 1 && j >= 1 ? bits_of(d) : 0ull, dmax_bits);
 }
@@ -149,7 +136,7 @@ __global__ void sia_H_kernel(const SiaV<T> v, int nx, int ny, T dt_scalar, const
     v.H(i, j, 0) = fmax(u, T(0.0));
     if (TAPE) {
         tp.a[cgsia::kW](i, j, 0) = W;
-        tp.a[cgsia::kFL](i, j, 0) = T((u > T(0) ? 1 : 0) + (x < v.m_max ? 2 : 0));
+        tp.fl(i, j, 0) = (unsigned char)((u > T(0) ? 1 : 0) + (x < v.m_max ? 2 : 0));
         if (bits_of(v.D(i, j, 0)) == tp.w->dmax) atomicMin(&tp.w->arg, (unsigned long long)((long)j * (nx + 2) + i));
     }
 }
@@ -205,6 +192,8 @@ SiaV<T> make_view(const cg_grid* g, const cg_field* H, const cg_field* B, const 
     v.beta = (T)p->beta;
     v.ela = (T)p->ela;
     v.m_max = (T)p->m_max;
+    v.Gn2 = v.Gamma * T(p->n + 2);
+    v.Asn = v.As * T(p->n);
     v.idx = (T)g->inv_spacing[0];
     v.idy = (T)g->inv_spacing[1];
     v.n = p->n;
@@ -311,6 +300,9 @@ int run_t(cg_ctx* ctx, const cg_grid* g, const cg_field* H, const cg_field* B, c
                     tp.a[k] = v.H;
                     tp.a[k].p = reinterpret_cast<T*>(sb + 256 + (size_t)k * tg.abytes) + cg_origin_offset(*H);
                 }
+                tp.fl.p = reinterpret_cast<unsigned char*>(sb + 256 + (size_t)cgsia::kFL * tg.abytes) + cg_origin_offset(*H);
+                tp.fl.s1 = v.H.s1;
+                tp.fl.s2 = v.H.s2;
                 vs.D = tp.a[cgsia::kD];
                 sia_D_kernel<T, true><<<gD, block, 0, st>>>(vs, nx, ny, words, tp);
             } else {

@@ -34,6 +34,8 @@
 #include "cg_sia_kernels.cuh"
 
 void* cg_scratch(cg_ctx* ctx, int slot, size_t bytes, int* rc);
+int cg_sia_reverse_impl(cg_ctx* ctx, int nm, const cg_sia_member* ms, const cg_sia_params* ps, int nsteps,
+                        const char* tape, const cg_field* lam, const cg_field* work, double* dJ);
 
 namespace {
 
@@ -131,26 +133,7 @@ __global__ void adj_arg_kernel(const SiaAdj<T> v, SiaWords* w) {
     if (cgk::bits_of(v.D(i, j, 0)) == w->dmax) atomicMin(&w->arg, (unsigned long long)((long)j * (v.nx + 2) + i));
 }
 
-// Sum over the block (valid in thread 0). Every thread calls it; it may be called more than
-// once per kernel (the leading barrier keeps a call's writes after the previous call's reads).
-__device__ __forceinline__ double block_sum(double x) {
-    constexpr unsigned FULL = 0xffffffffu;
-    __shared__ double part[32];
-    __syncthreads();
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(FULL, x, o);
-    const int tid = threadIdx.x + blockDim.x * threadIdx.y;
-    const int lane = tid & 31, warp = tid >> 5, nw = (blockDim.x * blockDim.y + 31) >> 5;
-    if (lane == 0) part[warp] = x;
-    __syncthreads();
-    x = 0.0;
-    if (warp == 0) {
-        x = lane < nw ? part[lane] : 0.0;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(FULL, x, o);
-    }
-    return x;  // valid in thread 0
-}
+using cgsia::block_sum;
 
 // Sums over the blocks' partials in a fixed order (one block of 256 threads): for each of the
 // `narr` arrays part[k][0..nblocks), dst_k = (acc_k ? dst_k : 0) + sum_b part[k][b].
@@ -381,213 +364,11 @@ int adjoint_step_t(cg_ctx* ctx, const cg_grid* g, const cg_field* H, const cg_fi
 // ---- reverse sweep over a tape -----------------------------------------------------------
 //
 // The forward quantities come from the tape that cg_sia_run_taped wrote, so a reverse step
-// needs no recomputation: about 40 FP64 instructions per cell against about 150 for the
-// recomputing step above. Per step, three kernels:
-// - adj_tape_cell: mu at the cell and its neighbours (lambda where the cell was not clipped),
-//   the face terms into dJ/dD and dJ/dS, lo = the direct term + dJ/dD dD/dh + dJ/dS, the
-//   gradient parts pax, pay, and per-block partial sums of dJ/ddt, dJ/dela and dJ/dGamma;
-// - adj_tape_sum (one block): the partial sums in a fixed order, then the dt term at the
-//   argmax cell (when dt was not capped) into lo, pax, pay and dJ/dGamma;
-// - adj_out: lambda_n from lo and the neighbours' pax, pay (as above).
-template <class T>
-struct TapeAdj {
-    DF<T> t[cgsia::kArrays];
-    DF<T> lam, lo, pax, pay;
-    T beta, idx, idy;
-    int nx, ny;
-};
-
-template <class T>
-__device__ __forceinline__ T tape_mu(const TapeAdj<T>& v, int i, int j) {
-    return ((int)v.t[cgsia::kFL](i, j, 0) & 1) ? v.lam(i, j, 0) : T(0);
-}
-
-template <class T>
-__global__ void adj_tape_cell_kernel(const TapeAdj<T> v, const cgsia::TapeWords* w, double* part, int nblocks) {
-    using namespace cgsia;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
-    const bool in = i <= v.nx && j <= v.ny;
-    double sdt = 0.0, sela = 0.0, sG = 0.0;
-    if (in) {
-        const T dt = (T)w->dt;
-        const T dtx = dt * v.idx, dty = dt * v.idy;
-        const T muc = tape_mu(v, i, j);
-        const T mM = ((int)v.t[kFL](i, j, 0) & 2) ? T(1) : T(0);
-        const T dc = v.t[kD](i, j, 0);
-        T pD = T(0), pS = T(0);
-        // x faces i (cell is upper) and i+1 (cell is lower); faces 1 and n+1 carry no flux
-        if (i >= 2) {
-            const T px = dtx * (muc - tape_mu(v, i - 1, j));
-            const T dl = v.t[kD](i - 1, j, 0);
-            pD += -T(0.5) * px * v.t[kGX](i, j, 0);
-            pS += -fma(T(0.5), dc - dl, dl) * px * v.idx;
-        }
-        if (i + 1 <= v.nx) {
-            const T px = dtx * (tape_mu(v, i + 1, j) - muc);
-            const T dr = v.t[kD](i + 1, j, 0);
-            pD += -T(0.5) * px * v.t[kGX](i + 1, j, 0);
-            pS += fma(T(0.5), dr - dc, dc) * px * v.idx;
-        }
-        if (j >= 2) {
-            const T py = dty * (muc - tape_mu(v, i, j - 1));
-            const T dl = v.t[kD](i, j - 1, 0);
-            pD += -T(0.5) * py * v.t[kGY](i, j, 0);
-            pS += -fma(T(0.5), dc - dl, dl) * py * v.idy;
-        }
-        if (j + 1 <= v.ny) {
-            const T py = dty * (tape_mu(v, i, j + 1) - muc);
-            const T dr = v.t[kD](i, j + 1, 0);
-            pD += -T(0.5) * py * v.t[kGY](i, j + 1, 0);
-            pS += fma(T(0.5), dr - dc, dc) * py * v.idy;
-        }
-        const T lo = muc * (T(1) + dt * v.beta * mM);
-        v.lo(i, j, 0) = lo + pD * v.t[kDH](i, j, 0) + pS;
-        v.pax(i, j, 0) = pD * v.t[kEX](i, j, 0);
-        v.pay(i, j, 0) = pD * v.t[kEY](i, j, 0);
-        sG = (double)(pD * v.t[kGF](i, j, 0));
-        sdt = (double)(muc * v.t[kW](i, j, 0));
-        sela = -(double)(muc * dt * v.beta * mM);
-    }
-    const double a = block_sum(sdt);
-    const double b = block_sum(sela);
-    const double c = block_sum(sG);
-    if (threadIdx.x == 0 && threadIdx.y == 0) {
-        const int blk = blockIdx.x + gridDim.x * blockIdx.y;
-        part[blk] = a;
-        part[nblocks + blk] = b;
-        part[2 * (size_t)nblocks + blk] = c;
-    }
-}
-
-// acc[0] += dJ/dGamma, acc[1] += dJ/dela of the step (one block of 256 threads)
-template <class T>
-__global__ void adj_tape_sum_kernel(const TapeAdj<T> v, const cgsia::TapeWords* w, const double* part, int nblocks,
-                                    double* acc) {
-    using namespace cgsia;
-    __shared__ double red[256];
-    double tot[3];
-    for (int k = 0; k < 3; ++k) {
-        const double* a = part + (size_t)k * nblocks;
-        double x = 0.0;
-        for (int b = threadIdx.x; b < nblocks; b += blockDim.x) x += a[b];
-        red[threadIdx.x] = x;
-        __syncthreads();
-        for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-            if ((int)threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
-            __syncthreads();
-        }
-        tot[k] = red[0];
-        __syncthreads();
-    }
-    if (threadIdx.x != 0) return;
-    double gG = tot[2];
-    // dt = dx^2 / (cfl Dmax) when not capped: the argmax cell carries dJ/dDmax = -dJ/ddt dt / Dmax
-    if (w->capped == 0.0 && w->arg != ~0ull) {
-        const unsigned long long b = w->dmax;
-        const double dmax = sizeof(T) == 8 ? __longlong_as_double((long long)b) : (double)__int_as_float((int)(unsigned)b);
-        const T pD = (T)(-tot[0] * w->dt / dmax);
-        const int i = (int)(w->arg % (unsigned long long)(v.nx + 2));
-        const int j = (int)(w->arg / (unsigned long long)(v.nx + 2));
-        v.lo(i, j, 0) = v.lo(i, j, 0) + pD * v.t[kDH](i, j, 0);
-        v.pax(i, j, 0) = v.pax(i, j, 0) + pD * v.t[kEX](i, j, 0);
-        v.pay(i, j, 0) = v.pay(i, j, 0) + pD * v.t[kEY](i, j, 0);
-        gG += (double)(pD * v.t[kGF](i, j, 0));
-    }
-    acc[0] += gG;
-    acc[1] += tot[1];
-}
-
-template <class T>
-__global__ void adj_copy_kernel(const DF<T> dst, const DF<T> src, int nx, int ny) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
-    if (i <= nx && j <= ny) dst(i, j, 0) = src(i, j, 0);
-}
-
+// recomputes nothing. The sweep is the ensemble's (cg_sia_reverse_impl) with one member: a
+// single-member tape has the same step blocks.
 bool same_layout(const cg_field& a, const cgsia::TapeHeader& h) {
     return a.stride[0] == h.stride0 && a.stride[1] == h.stride1 && a.halo[0] == h.halo0 && a.halo[1] == h.halo1 &&
            a.n[0] == h.n0 && a.n[1] == h.n1;
-}
-
-template <class T>
-int adjoint_run_t(cg_ctx* ctx, const cg_grid* g, const cgsia::TapeHeader& hd, const char* tape, const cg_field* lam,
-                  const cg_field* work, double* dJ) {
-    const int nx = g->n[0], ny = g->n[1], N = hd.nsteps;
-    const cgsia::TapeGeom tg = cgsia::tape_geom(*lam, sizeof(T));
-    const dim3 block(32, 8), grid(cg_div_up(nx, 32), cg_div_up(ny, 8));
-    const int nblocks = (int)(grid.x * grid.y);
-    const size_t pbytes = ((size_t)nblocks * 3 * sizeof(double) + 255) & ~(size_t)255;
-    int rc = CG_OK;
-    // scratch slot 6: lo, pax, pay (lambda's layout), the partial sums, then [dJ/dGamma, dJ/dela]
-    char* base = static_cast<char*>(cg_scratch(ctx, 6, 3 * tg.abytes + pbytes + 256, &rc));
-    if (rc) return rc;
-    double* part = reinterpret_cast<double*>(base + 3 * tg.abytes);
-    double* acc = reinterpret_cast<double*>(base + 3 * tg.abytes + pbytes);
-    TapeAdj<T> v;
-    std::memset(&v, 0, sizeof(v));
-    const DF<T> L = cg_view<T>(*lam), Wk = cg_view<T>(*work);
-    DF<T>* sc[3] = {&v.lo, &v.pax, &v.pay};
-    for (int a = 0; a < 3; ++a) {
-        *sc[a] = L;
-        sc[a]->p = reinterpret_cast<T*>(base + a * tg.abytes) + cg_origin_offset(*lam);
-    }
-    v.beta = (T)hd.beta;
-    v.idx = (T)g->inv_spacing[0];
-    v.idy = (T)g->inv_spacing[1];
-    v.nx = nx;
-    v.ny = ny;
-    SiaAdj<T> o;  // adj_out's view: lo, pax, pay and the output
-    std::memset(&o, 0, sizeof(o));
-    o.lo = v.lo;
-    o.pax = v.pax;
-    o.pay = v.pay;
-    o.idx = v.idx;
-    o.idy = v.idy;
-    o.nx = nx;
-    o.ny = ny;
-    std::string key = "sia_adjoint_run";
-    cg_key_add(key, *g);
-    cg_key_add(key, *lam);
-    cg_key_add(key, *work);
-    cg_key_add(key, tape);
-    cg_key_add(key, N);
-    cg_key_add(key, hd.beta);
-    cg_key_add(key, base);
-    rc = cg_graph_run(ctx, key, [&](cudaStream_t st) {
-        CG_CUDA(ctx, cudaMemsetAsync(acc, 0, 2 * sizeof(double), st));
-        for (int r = 0; r < N; ++r) {
-            const int s = N - 1 - r;
-            const char* sb = tape + 256 + (size_t)s * tg.step_bytes;
-            const cgsia::TapeWords* w = reinterpret_cast<const cgsia::TapeWords*>(sb);
-            TapeAdj<T> vs = v;
-            for (int k = 0; k < cgsia::kArrays; ++k) {
-                vs.t[k] = L;
-                vs.t[k].p = reinterpret_cast<T*>(const_cast<char*>(sb) + 256 + (size_t)k * tg.abytes) + cg_origin_offset(*lam);
-            }
-            vs.lam = (r & 1) ? Wk : L;
-            SiaAdj<T> os = o;
-            os.out = (r & 1) ? L : Wk;
-            adj_tape_cell_kernel<T><<<grid, block, 0, st>>>(vs, w, part, nblocks);
-            adj_tape_sum_kernel<T><<<1, 256, 0, st>>>(vs, w, part, nblocks, acc);
-            adj_out_kernel<T><<<grid, block, 0, st>>>(os);
-            CG_CHECK_LAUNCH(ctx);
-        }
-        if (N & 1) {
-            adj_copy_kernel<T><<<grid, block, 0, st>>>(L, Wk, nx, ny);
-            CG_CHECK_LAUNCH(ctx);
-        }
-        return (int)CG_OK;
-    });
-    if (rc) return rc;
-    double h[2];
-    CG_CUDA(ctx, cudaMemcpyAsync(h, acc, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
-    CG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    if (dJ) {
-        dJ[0] += h[0];
-        dJ[1] += h[1];
-    }
-    return CG_OK;
 }
 
 }  // namespace
@@ -618,9 +399,11 @@ extern "C" int cg_sia_adjoint_run(cg_ctx* ctx, const cg_grid* grid, const cg_sia
         return cg_fail(ctx, CG_ERR_ARG, "sia_adjoint_run: the parameters differ from the taped run's");
     if (hd.nsteps < 1 || tape_bytes < 256 + (size_t)hd.nsteps * (size_t)hd.step_bytes)
         return cg_fail(ctx, CG_ERR_ARG, "sia_adjoint_run: the tape is shorter than its %d steps", hd.nsteps);
-    const char* tp = static_cast<const char*>(tape);
-    return dt == CG_F64 ? adjoint_run_t<double>(ctx, grid, hd, tp, lam, work, dJ)
-                        : adjoint_run_t<float>(ctx, grid, hd, tp, lam, work, dJ);
+    cg_sia_member mem;
+    std::memset(&mem, 0, sizeof(mem));
+    mem.grid = *grid;
+    mem.H = *lam;  // the taped H's layout
+    return cg_sia_reverse_impl(ctx, 1, &mem, p, hd.nsteps, static_cast<const char*>(tape), lam, work, dJ);
 }
 
 extern "C" int cg_sia_adjoint_step(cg_ctx* ctx, const cg_grid* grid, const cg_field* H, const cg_field* B,

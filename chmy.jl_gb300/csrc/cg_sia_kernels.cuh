@@ -42,9 +42,60 @@ __device__ __forceinline__ T D_cell(T h, T ax, T ay, T Gamma, T As, int n) {
     return pow_int(h, n) * fma(Gamma, h * h, As) * vp;
 }
 
+// D at a cell (bit for bit the value of D_cell) and the derivatives a taped forward step
+// records, from the same subexpressions: dD/dh, c ax and c ay with c = 2 dD/dV (V = ax^2 + ay^2;
+// these are dD/dax and dD/day), and dD/dGamma = h^(n+2) V^((n-1)/2). Gn2 = Gamma (n+2) and
+// Asn = As n are the caller's constants.
+template <class T>
+__device__ __forceinline__ T D_and_factors(T h, T ax, T ay, T Gamma, T As, T Gn2, T Asn, int n, T* dh, T* ex, T* ey,
+                                           T* gf) {
+    const T V = ax * ax + ay * ay;
+    const int e = n - 1;
+    T vp = pow_int(V, e >> 1);
+    if (e & 1) vp = vp * sqrt(V);
+    const T h2 = h * h;
+    const T hn = pow_int(h, n);
+    const T A = hn * fma(Gamma, h2, As);
+    const T D = A * vp;
+    T c = T(0);
+    if (n >= 3) {
+        T vq = pow_int(V, (n - 3) >> 1);
+        if ((n - 3) & 1) vq = vq * sqrt(V);
+        c = A * T(n - 1) * vq;
+    } else if (n == 2 && V > T(0)) {
+        c = A / sqrt(V);
+    }
+    *dh = fma(Gn2, h2, Asn) * pow_int(h, n - 1) * vp;
+    *ex = c * ax;
+    *ey = c * ay;
+    *gf = hn * h2 * vp;
+    return D;
+}
+
 using cgk::bits_of;
 
 using cgk::block_max_bits;
+
+// Sum over the block (valid in thread 0). Every thread calls it; it may be called more than
+// once per kernel (the leading barrier keeps a call's writes after the previous call's reads).
+__device__ __forceinline__ double block_sum(double x) {
+    constexpr unsigned FULL = 0xffffffffu;
+    __shared__ double part[32];
+    __syncthreads();
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(FULL, x, o);
+    const int tid = threadIdx.x + blockDim.x * threadIdx.y;
+    const int lane = tid & 31, warp = tid >> 5, nw = (blockDim.x * blockDim.y + 31) >> 5;
+    if (lane == 0) part[warp] = x;
+    __syncthreads();
+    x = 0.0;
+    if (warp == 0) {
+        x = lane < nw ? part[lane] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(FULL, x, o);
+    }
+    return x;  // valid in thread 0
+}
 
 // ---- tape of a forward run, read by the reverse sweep ---------------------------------------
 //
@@ -57,11 +108,11 @@ enum TapeArray {
     kGX = 1,  // dS/dx at the cell's lower x face ((S_i - S_i-1)/dx)
     kGY = 2,  // dS/dy at the lower y face
     kDH = 3,  // dD/dh
-    kEX = 4,  // dD/dV 2 ax  (V = ax^2 + ay^2)
-    kEY = 5,  // dD/dV 2 ay
+    kEX = 4,  // dD/dax = 2 dD/dV ax  (V = ax^2 + ay^2)
+    kEY = 5,  // dD/day = 2 dD/dV ay
     kGF = 6,  // dD/dGamma = h^(n+2) V^((n-1)/2)
     kW = 7,   // W = -divg(q) + M
-    kFL = 8,  // 1 if H + dt W > 0, plus 2 if beta (S - ela) < m_max
+    kFL = 8,  // one byte per cell: 1 if H + dt W > 0, plus 2 if the mass balance is not capped
     kArrays = 9
 };
 

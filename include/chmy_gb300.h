@@ -473,6 +473,30 @@ typedef struct cg_sia_member {
 CG_API int cg_sia_ensemble_run(cg_ctx* ctx, int nmembers, const cg_sia_member* members,
                                const cg_sia_params* params, int nsteps, double* t_host);
 
+/* Bytes of an ensemble tape of `nsteps` steps for these members: a 256-byte header, then per
+ * step every member's tape in the layout of cg_sia_run_taped. No context, no device work. */
+CG_API int cg_sia_ensemble_tape_bytes(int nmembers, const cg_sia_member* members, int nsteps,
+                                      size_t* bytes);
+
+/* cg_sia_ensemble_run (same results bit for bit; always the per-phase graph form) that also
+ * records every member's reverse-step quantities for each of its `nsteps` (>= 1) steps into
+ * `tape` (device memory of at least cg_sia_ensemble_tape_bytes, 256-byte aligned). No
+ * reference counterpart. */
+CG_API int cg_sia_ensemble_run_taped(cg_ctx* ctx, int nmembers, const cg_sia_member* members,
+                                     const cg_sia_params* params, int nsteps, void* tape,
+                                     size_t tape_bytes, double* t_host);
+
+/* The reverse sweep over an ensemble tape, all members in each launch: on entry lam[m] holds
+ * dJ/dH of member m at its interior cells after the taped run; on return, at its start.
+ * dJ (host, 2 per member, may be NULL) gains dJ/dGamma in dJ[2m] and dJ/dela in dJ[2m+1];
+ * the call synchronises the stream. work[m] has lam[m]'s layout (that of members[m].H) and is
+ * overwritten. members and params must be those of the taped run: the tape's header holds a
+ * hash of their layouts and parameters. The arithmetic per member is that of
+ * cg_sia_adjoint_run. */
+CG_API int cg_sia_ensemble_adjoint_run(cg_ctx* ctx, int nmembers, const cg_sia_member* members,
+                                       const cg_sia_params* params, const void* tape, size_t tape_bytes,
+                                       const cg_field* lam, const cg_field* work, double* dJ);
+
 /* Reverse step of the SIA time loop of cg_sia_run (no reference counterpart: the reference has
  * no adjoint). H is the state H_n at the start of the forward step, with the ghost layer the
  * forward step read (bc! Neumann copies after every step). lam holds dJ/dH_{n+1} at the

@@ -437,3 +437,88 @@ def test_sia_adjoint_run_argument_errors(arch):
     assert arch.lib.cg_sia_adjoint_run(arch.ctx, ctypes.byref(g), ctypes.byref(p), tp, 100, ctypes.byref(lam), ctypes.byref(work), None) == abi.CG_ERR_ARG
     dJ = (ctypes.c_double * 2)()
     arch.call("cg_sia_adjoint_run", ctypes.byref(g), ctypes.byref(p), tp, n, ctypes.byref(lam), ctypes.byref(work), dJ)
+
+
+def _ensemble_members(T=np.float64):
+    """Three SIA members of uneven sizes (the 60-step problem above on each grid), with
+    different ela and Gamma."""
+    from chmy_gb300.grids import UniformGrid
+
+    out = []
+    for k, n in enumerate([(48, 40), (33, 57), (64, 64)]):
+        g0, bed, H0, p = _sia_problem(n=n)
+        grid = UniformGrid(origin=(T(-1), T(-1)), extent=(T(2), T(2)), dims=n, dtype=T)
+        p.ela = 0.5 + 0.05 * k
+        p.Gamma = 1.0 + 0.2 * k
+        out.append((grid, bed.astype(T), H0.astype(T), p))
+    return out
+
+
+@pytest.mark.parametrize("T", [np.float32, np.float64])
+def test_sia_ensemble_taped_run_equals_plain_run(arch, T):
+    """cg_sia_ensemble_run_taped gives cg_sia_ensemble_run's H and t bit for bit."""
+    from chmy_gb300.adjoint import SIAEnsemble
+
+    mem = _ensemble_members(T)
+    ens = SIAEnsemble(arch, [(g, b, p) for g, b, _, p in mem], dtype=T)
+    H0s = [h for _, _, h, _ in mem]
+    plain = ens.run(H0s, 25)
+    ens._set(H0s)
+    ens._steps_taped(25)
+    for a, H in zip(plain, ens.H):
+        assert np.array_equal(a, H.to_numpy(), equal_nan=True)
+
+
+def test_sia_ensemble_gradient_matches_members_and_differences(arch):
+    """The batched ensemble adjoint (cg_sia_ensemble_adjoint_run, all members per launch) against
+    (a) each member's own taped gradient (cg_sia_adjoint_run): dJ/dGamma, dJ/dela and dJ/dH0 to
+    1e-10 relative (the ensemble forward computes the same quantities in forms that differ in
+    rounding); (b) segments of 7 steps: dJ/dH0 bit for bit, the sums to 1e-13; (c) central
+    differences of one member's J in log(Gamma) and ela to 1e-6."""
+    from chmy_gb300.adjoint import SIA, SIAEnsemble
+
+    mem = _ensemble_members()
+    nsteps = 60
+    inner = (slice(2, -2), slice(2, -2))
+    ens = SIAEnsemble(arch, [(g, b, p) for g, b, _, p in mem])
+    H0s = [h for _, _, h, _ in mem]
+    HN = ens.run(H0s, nsteps)
+    rng = np.random.default_rng(4)
+    obs = [h[inner] + 0.01 * rng.standard_normal(h[inner].shape) for h in HN]
+
+    def dJ(m, h):
+        g = np.zeros_like(h)
+        g[inner] = h[inner] - obs[m]
+        return g
+
+    gG, gE, gH, HN2 = ens.gradient(H0s, nsteps, dJ)
+    for a, b in zip(HN, HN2):
+        assert np.array_equal(a, b)
+    sG, sE, sH, _ = ens.gradient(H0s, nsteps, dJ, checkpoint_every=7)
+    for m in range(len(mem)):
+        assert np.array_equal(sH[m], gH[m])
+        assert abs(sG[m] - gG[m]) <= 1e-13 * abs(gG[m]) and abs(sE[m] - gE[m]) <= 1e-13 * abs(gE[m])
+    for m, (grid, bed, H0, p) in enumerate(mem):
+        one = SIA(arch, grid, bed, p)
+        a, b, c, _ = one.gradient(H0, nsteps, lambda h: dJ(m, h))
+        assert abs(a - gG[m]) <= 1e-10 * abs(a), (m, a, gG[m])
+        assert abs(b - gE[m]) <= 1e-10 * abs(b), (m, b, gE[m])
+        assert np.max(np.abs(c[inner] - gH[m][inner])) <= 1e-10 * np.max(np.abs(c[inner]))
+
+    m = 1
+    grid, bed, H0, p = mem[m]
+
+    def J_at(**kw):
+        q = _abi.cg_sia_params()
+        ctypes.memmove(ctypes.byref(q), ctypes.byref(p), ctypes.sizeof(q))
+        for k, v in kw.items():
+            setattr(q, k, v)
+        e = SIAEnsemble(arch, [(g, b, q if i == m else pp) for i, (g, b, _, pp) in enumerate(mem)])
+        r = e.run(H0s, nsteps)[m][inner] - obs[m]
+        return 0.5 * float(np.sum(r * r))
+
+    h = 1e-6
+    fdG = (J_at(Gamma=p.Gamma * np.exp(h)) - J_at(Gamma=p.Gamma * np.exp(-h))) / (2 * h)
+    fdE = (J_at(ela=p.ela + h) - J_at(ela=p.ela - h)) / (2 * h)
+    assert abs(gG[m] * p.Gamma - fdG) <= 1e-6 * abs(fdG), (gG[m] * p.Gamma, fdG)
+    assert abs(gE[m] - fdE) <= 1e-6 * abs(fdE), (gE[m], fdE)
