@@ -970,6 +970,45 @@ def run_kernel_misc(arch, args):
     print(json.dumps({"kernel": "diffusion_step_kernel<double,2>", "n": n, "steps": args.reps, "us_per_step": 1e3 * ms / args.reps}))
 
 
+def run_kernel_sia_adjoint(arch, args):
+    """--kernel sia_adjoint: the taped SIA gradient (dJ/dGamma, dJ/dela, dJ/dH0 of 1/2 |H^N|^2) on
+    an n^2 grid over `--reps` steps, after one untimed run: the taped forward kernels and the
+    reverse sweep's kernels, for launch lists and captures."""
+    import time
+
+    import torch
+
+    from chmy_gb300 import _abi
+    from chmy_gb300.adjoint import SIA
+    from chmy_gb300.configs import gaussian_random_field, padded_mesh
+    from chmy_gb300.grids import Center, UniformGrid
+
+    n, nsteps = args.n, args.reps
+    T = np.float64
+    grid = UniformGrid(origin=(T(-1), T(-1)), extent=(T(2), T(2)), dims=(n, n), dtype=T)
+    x, y = padded_mesh(grid, Center())
+    bed = 0.4 + 0.3 * gaussian_random_field(x.shape, 0.25, 2.0 / n, 7)
+    H0 = np.clip(0.35 - 0.25 * (x * x + y * y), 0.0, None)
+    p = _abi.cg_sia_params()
+    p.Gamma, p.As, p.n, p.beta, p.ela, p.m_max, p.dt_max, p.cfl = 1.0, 0.0, 3, 0.5, 0.55, 0.25, 0.5, 4.1
+    sia = SIA(arch, grid, bed, p)
+
+    def dJ(h):
+        return np.where(np.isfinite(h), h, 0.0)
+
+    sia.gradient(H0, nsteps, dJ)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sia.run(H0, nsteps)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    sia.gradient(H0, nsteps, dJ)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    print(json.dumps({"kernel": "SIA gradient (taped)", "n": n, "steps": nsteps, "forward_ms": (t1 - t0) * 1e3,
+                      "gradient_ms": (t2 - t1) * 1e3, "ratio": (t2 - t1) / (t1 - t0)}))
+
+
 def run_kernel(args):
     """--kernel fused2d | fused3d: only the fused FP32 PT kernel (2D inclusions n^2, or 3D random
     viscosity n^3), `--reps` launches timed with CUDA events (the command the committed ncu
@@ -986,6 +1025,10 @@ def run_kernel(args):
         return
     if args.kernel in ("sia_ensemble", "diffusion2d"):
         run_kernel_misc(arch, args)
+        arch.close()
+        return
+    if args.kernel == "sia_adjoint":
+        run_kernel_sia_adjoint(arch, args)
         arch.close()
         return
     if args.kernel == "fused3d":
@@ -1018,7 +1061,7 @@ def run_kernel(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--kernel", choices=["fused2d", "fused3d", "ptdiff3d", "sia_ensemble", "diffusion2d"],
+    ap.add_argument("--kernel", choices=["fused2d", "fused3d", "ptdiff3d", "sia_ensemble", "diffusion2d", "sia_adjoint"],
                     help="time one kernel alone (profiling driver)")
     ap.add_argument("--members", type=int, default=64, help="--kernel sia_ensemble: ensemble members")
     ap.add_argument("--nmin", type=int, default=128, help="--kernel sia_ensemble: smallest member size")
