@@ -538,6 +538,7 @@ int run_t(cg_ctx* ctx, int nm, const cg_sia_member* ms, const cg_sia_params* ps,
 template <class T>
 struct AdjMember {
     DF<T> L, Wk, lo, pax, pay;  // lambda and work (in/out by turns), the step's scratch
+    DF<double> aG, aE;          // per-cell sums over the sweep's steps of dJ/dGamma and dJ/dela
     T beta, idx, idy;
     int nx, ny;
     long long toff, tab, orig;
@@ -639,7 +640,7 @@ __global__ void __launch_bounds__(256) ens_adj_cell_kernel(const AdjMember<T>* a
         tDu = fdy[row + 1][lane];
         tSu = fsy[row + 1][lane];
     }
-    double sdt = 0.0, sela = 0.0, sG = 0.0;
+    double sdt = 0.0;
     if (own) {
         T pD = T(0), pS = T(0);
         if (i >= 2) {
@@ -663,65 +664,95 @@ __global__ void __launch_bounds__(256) ens_adj_cell_kernel(const AdjMember<T>* a
         v.lo(i, j, 0) = lo + pD * adj_tape(v, sb, kDH)(i, j, 0) + pS;
         v.pax(i, j, 0) = pD * adj_tape(v, sb, kEX)(i, j, 0);
         v.pay(i, j, 0) = pD * adj_tape(v, sb, kEY)(i, j, 0);
-        sG = (double)(pD * adj_tape(v, sb, kGF)(i, j, 0));
         sdt = (double)(muc * adj_tape(v, sb, kW)(i, j, 0));
-        sela = -(double)(muc * dt * v.beta * mM);
+        v.aG(i, j, 0) += (double)(pD * adj_tape(v, sb, kGF)(i, j, 0));
+        v.aE(i, j, 0) -= (double)(muc * dt * v.beta * mM);
     }
     const double a = block_sum(sdt);
-    const double b = block_sum(sela);
-    const double c = block_sum(sG);
-    if (threadIdx.x == 0 && threadIdx.y == 0) {
-        part[blk] = a;
-        part[ntot + blk] = b;
-        part[2 * (size_t)ntot + blk] = c;
-    }
+    if (threadIdx.x == 0 && threadIdx.y == 0) part[blk] = a;
 }
 
-// Block m (1024 threads): member m's partial sums in a fixed order, the three arrays in one
-// pass, then the dt term at its argmax cell; acc[2m] += dJ/dGamma and acc[2m + 1] += dJ/dela.
+// Block m (1024 threads): dJ/ddt of member m's step, its tiles' partials summed in a fixed
+// order; then the dt term at its argmax cell (when dt was not capped) into lo, pax, pay and
+// the per-cell dJ/dGamma sum there.
 template <class T>
 __global__ void __launch_bounds__(1024) ens_adj_sum_kernel(const AdjMember<T>* am, const int* prefix, const char* sb,
-                                                           const double* part, int ntot, double* acc) {
+                                                           const double* part) {
     using namespace cgsia;
     constexpr unsigned FULL = 0xffffffffu;
-    __shared__ double red[3][32];
+    __shared__ double red[32];
     const int m = blockIdx.x;
     const int b0 = m ? prefix[m - 1] : 0, b1 = prefix[m];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    double x[3] = {0.0, 0.0, 0.0};
+    double x = 0.0;
+    for (int b = b0 + tid; b < b1; b += blockDim.x) x += part[b];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(FULL, x, o);
+    if (lane == 0) red[warp] = x;
+    __syncthreads();
+    if (warp != 0) return;
+    x = lane < (int)(blockDim.x >> 5) ? red[lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(FULL, x, o);
+    if (lane != 0) return;
+    const AdjMember<T>& v = am[m];
+    const TapeWords* w = reinterpret_cast<const TapeWords*>(sb + v.toff);
+    if (w->capped == 0.0 && w->arg != ~0ull) {
+        const unsigned long long bb = w->dmax;
+        const double dmax = sizeof(T) == 8 ? __longlong_as_double((long long)bb) : (double)__int_as_float((int)(unsigned)bb);
+        const T pD = (T)(-x * w->dt / dmax);
+        const int i = (int)(w->arg % (unsigned long long)(v.nx + 2));
+        const int j = (int)(w->arg / (unsigned long long)(v.nx + 2));
+        v.lo(i, j, 0) = v.lo(i, j, 0) + pD * adj_tape(v, sb, kDH)(i, j, 0);
+        v.pax(i, j, 0) = v.pax(i, j, 0) + pD * adj_tape(v, sb, kEX)(i, j, 0);
+        v.pay(i, j, 0) = v.pay(i, j, 0) + pD * adj_tape(v, sb, kEY)(i, j, 0);
+        v.aG(i, j, 0) += (double)(pD * adj_tape(v, sb, kGF)(i, j, 0));
+    }
+}
+
+// End of the sweep: per 32 x 8 tile, the sums of the per-cell dJ/dGamma and dJ/dela arrays,
+// then (one block per member) their ordered sums into acc[2m], acc[2m + 1].
+template <class T>
+__global__ void __launch_bounds__(256) ens_adj_tile_sums_kernel(const AdjMember<T>* am, const int* prefix, int nm,
+                                                                double* part, int ntot) {
+    const int blk = blockIdx.x;
+    const int m = find_member(prefix, nm, blk);
+    const AdjMember<T>& v = adj_member_of(am, m);
+    const int t = blk - (m ? prefix[m - 1] : 0);
+    const int tx = (v.nx + 31) / 32;
+    const int i = (t % tx) * 32 + threadIdx.x + 1;
+    const int j = (t / tx) * 8 + threadIdx.y + 1;
+    const bool in = i <= v.nx && j <= v.ny;
+    const double g = cgsia::block_sum(in ? v.aG(i, j, 0) : 0.0);
+    const double e = cgsia::block_sum(in ? v.aE(i, j, 0) : 0.0);
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        part[blk] = g;
+        part[ntot + blk] = e;
+    }
+}
+
+__global__ void __launch_bounds__(1024) ens_adj_final_kernel(const int* prefix, const double* part, int ntot, double* acc) {
+    constexpr unsigned FULL = 0xffffffffu;
+    __shared__ double red[2][32];
+    const int m = blockIdx.x;
+    const int b0 = m ? prefix[m - 1] : 0, b1 = prefix[m];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    double x[2] = {0.0, 0.0};
     for (int b = b0 + tid; b < b1; b += blockDim.x)
-        for (int k = 0; k < 3; ++k) x[k] += part[(size_t)k * ntot + b];
-    for (int k = 0; k < 3; ++k) {
+        for (int k = 0; k < 2; ++k) x[k] += part[(size_t)k * ntot + b];
+    for (int k = 0; k < 2; ++k) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) x[k] += __shfl_xor_sync(FULL, x[k], o);
         if (lane == 0) red[k][warp] = x[k];
     }
     __syncthreads();
     if (warp != 0) return;
-    double tot[3];
-    for (int k = 0; k < 3; ++k) {
+    for (int k = 0; k < 2; ++k) {
         double y = lane < (int)(blockDim.x >> 5) ? red[k][lane] : 0.0;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) y += __shfl_xor_sync(FULL, y, o);
-        tot[k] = y;
+        if (lane == 0) acc[2 * m + k] = y;
     }
-    if (lane != 0) return;
-    const AdjMember<T>& v = am[m];
-    const TapeWords* w = reinterpret_cast<const TapeWords*>(sb + v.toff);
-    double gG = tot[2];
-    if (w->capped == 0.0 && w->arg != ~0ull) {
-        const unsigned long long bb = w->dmax;
-        const double dmax = sizeof(T) == 8 ? __longlong_as_double((long long)bb) : (double)__int_as_float((int)(unsigned)bb);
-        const T pD = (T)(-tot[0] * w->dt / dmax);
-        const int i = (int)(w->arg % (unsigned long long)(v.nx + 2));
-        const int j = (int)(w->arg / (unsigned long long)(v.nx + 2));
-        v.lo(i, j, 0) = v.lo(i, j, 0) + pD * adj_tape(v, sb, kDH)(i, j, 0);
-        v.pax(i, j, 0) = v.pax(i, j, 0) + pD * adj_tape(v, sb, kEX)(i, j, 0);
-        v.pay(i, j, 0) = v.pay(i, j, 0) + pD * adj_tape(v, sb, kEY)(i, j, 0);
-        gG += (double)(pD * adj_tape(v, sb, kGF)(i, j, 0));
-    }
-    acc[2 * m] += gG;
-    acc[2 * m + 1] += tot[1];
 }
 
 // lambda_n of every member from lo and the neighbours' pax, pay (the ghost cells' terms folded
@@ -774,13 +805,21 @@ int adjoint_run_t(cg_ctx* ctx, int nm, const cg_sia_member* ms, const cg_sia_par
         pC[m] = totC;
     }
     const size_t part_off = off;
-    off += ((size_t)3 * totC * sizeof(double) + 255) & ~(size_t)255;
+    off += ((size_t)std::max(totC, 2 * totI) * sizeof(double) + 255) & ~(size_t)255;
     const size_t acc_off = off;
     off += ((size_t)2 * nm * sizeof(double) + 255) & ~(size_t)255;
     for (int m = 0; m < nm; ++m) {
         aoff[m] = off;
         off += 3 * (size_t)et.tab[m];
     }
+    // the per-cell FP64 sums of every member, in one region (zeroed once per sweep)
+    std::vector<size_t> doff(nm);
+    const size_t sums_off = off;
+    for (int m = 0; m < nm; ++m) {
+        doff[m] = off;
+        off += 2 * cgsia::tape_geom(ms[m].H, sizeof(double)).abytes;
+    }
+    const size_t sums_bytes = off - sums_off;
     int rc = CG_OK;
     char* base = static_cast<char*>(cg_scratch(ctx, 7, off, &rc));
     if (rc) return rc;
@@ -794,6 +833,13 @@ int adjoint_run_t(cg_ctx* ctx, int nm, const cg_sia_member* ms, const cg_sia_par
         for (int a = 0; a < 3; ++a) {
             *sc[a] = v.L;
             sc[a]->p = reinterpret_cast<T*>(base + aoff[m] + (size_t)a * et.tab[m]) + cg_origin_offset(lam[m]);
+        }
+        const size_t dab = cgsia::tape_geom(ms[m].H, sizeof(double)).abytes;
+        DF<double>* sd[2] = {&v.aG, &v.aE};
+        for (int a = 0; a < 2; ++a) {
+            sd[a]->p = reinterpret_cast<double*>(base + doff[m] + (size_t)a * dab) + cg_origin_offset(lam[m]);
+            sd[a]->s1 = v.L.s1;
+            sd[a]->s2 = v.L.s2;
         }
         v.beta = (T)ps[m].beta;
         v.idx = (T)ms[m].grid.inv_spacing[0];
@@ -820,18 +866,18 @@ int adjoint_run_t(cg_ctx* ctx, int nm, const cg_sia_member* ms, const cg_sia_par
     key.append(reinterpret_cast<const char*>(hm.data()), nm * sizeof(AdjMember<T>));
     const dim3 block(32, 8);
     rc = cg_graph_run(ctx, key, [&](cudaStream_t st) {
-        CG_CUDA(ctx, cudaMemsetAsync(acc, 0, 2 * (size_t)nm * sizeof(double), st));
+        CG_CUDA(ctx, cudaMemsetAsync(base + sums_off, 0, sums_bytes, st));
         for (int r = 0; r < N; ++r) {
             const char* sb = tape + 256 + (size_t)(N - 1 - r) * et.step_bytes;
             ens_adj_cell_kernel<T><<<totC, block, 0, st>>>(dmem, dpc, nm, sb, r & 1, part, totC);
-            ens_adj_sum_kernel<T><<<nm, 1024, 0, st>>>(dmem, dpc, sb, part, totC, acc);
+            ens_adj_sum_kernel<T><<<nm, 1024, 0, st>>>(dmem, dpc, sb, part);
             ens_adj_out_kernel<T><<<totI, block, 0, st>>>(dmem, dp, nm, r & 1, 0);
             CG_CHECK_LAUNCH(ctx);
         }
-        if (N & 1) {
-            ens_adj_out_kernel<T><<<totI, block, 0, st>>>(dmem, dp, nm, 0, 1);
-            CG_CHECK_LAUNCH(ctx);
-        }
+        if (N & 1) ens_adj_out_kernel<T><<<totI, block, 0, st>>>(dmem, dp, nm, 0, 1);
+        ens_adj_tile_sums_kernel<T><<<totI, block, 0, st>>>(dmem, dp, nm, part, totI);
+        ens_adj_final_kernel<<<nm, 1024, 0, st>>>(dp, part, totI, acc);
+        CG_CHECK_LAUNCH(ctx);
         return (int)CG_OK;
     });
     if (rc) return rc;
