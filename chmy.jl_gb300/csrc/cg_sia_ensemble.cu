@@ -586,7 +586,7 @@ constexpr int kCW = 31;
 
 template <class T>
 __global__ void __launch_bounds__(256) ens_adj_cell_kernel(const AdjMember<T>* am, const int* prefix, int nm,
-                                                           const char* sb, int parity, double* part, int ntot) {
+                                                           const char* sb, int parity, double* part) {
     using namespace cgsia;
     constexpr unsigned FULL = 0xffffffffu;
     __shared__ T fdy[8][32], fsy[8][32];
@@ -869,7 +869,7 @@ int adjoint_run_t(cg_ctx* ctx, int nm, const cg_sia_member* ms, const cg_sia_par
         CG_CUDA(ctx, cudaMemsetAsync(base + sums_off, 0, sums_bytes, st));
         for (int r = 0; r < N; ++r) {
             const char* sb = tape + 256 + (size_t)(N - 1 - r) * et.step_bytes;
-            ens_adj_cell_kernel<T><<<totC, block, 0, st>>>(dmem, dpc, nm, sb, r & 1, part, totC);
+            ens_adj_cell_kernel<T><<<totC, block, 0, st>>>(dmem, dpc, nm, sb, r & 1, part);
             ens_adj_sum_kernel<T><<<nm, 1024, 0, st>>>(dmem, dpc, sb, part);
             ens_adj_out_kernel<T><<<totI, block, 0, st>>>(dmem, dp, nm, r & 1, 0);
             CG_CHECK_LAUNCH(ctx);

@@ -522,3 +522,33 @@ def test_sia_ensemble_gradient_matches_members_and_differences(arch):
     fdE = (J_at(ela=p.ela + h) - J_at(ela=p.ela - h)) / (2 * h)
     assert abs(gG[m] * p.Gamma - fdG) <= 1e-6 * abs(fdG), (gG[m] * p.Gamma, fdG)
     assert abs(gE[m] - fdE) <= 1e-6 * abs(fdE), (gE[m], fdE)
+
+
+def test_sia_ensemble_adjoint_run_argument_errors(arch):
+    """cg_sia_ensemble_adjoint_run refuses a buffer without an ensemble tape header, parameters
+    or members other than the taped run's (the header's hash), aliased lambda and work, and a
+    tape shorter than its steps."""
+    import torch
+
+    from chmy_gb300.adjoint import SIAEnsemble
+
+    mem = _ensemble_members()
+    ens = SIAEnsemble(arch, [(g, b, p) for g, b, _, p in mem])
+    ens._set([h for _, _, h, _ in mem])
+    ens._steps_taped(3)
+    tp, n = ctypes.c_void_p(ens._tape.data_ptr()), ens._tape.numel()
+
+    def call(par=None, tape=tp, nbytes=n, lam=None, nm=None):
+        return arch.lib.cg_sia_ensemble_adjoint_run(arch.ctx, nm or ens.nm, ens._mem, par or ens._par, tape, nbytes,
+                                                    lam or ens._lam, ens._work, None)
+
+    blank = torch.zeros(4096, dtype=torch.uint8, device=ens.H[0].data.device)
+    assert call(tape=ctypes.c_void_p(blank.data_ptr()), nbytes=4096) == _abi.CG_ERR_ARG
+    par = (_abi.cg_sia_params * ens.nm)(*ens.params)
+    par[1].Gamma = par[1].Gamma * 1.5
+    assert call(par=par) == _abi.CG_ERR_ARG
+    assert call(nm=ens.nm - 1) == _abi.CG_ERR_ARG
+    assert call(lam=ens._work) == _abi.CG_ERR_ARG
+    assert call(nbytes=n // 2) == _abi.CG_ERR_ARG
+    dJ = (ctypes.c_double * (2 * ens.nm))()
+    arch.call("cg_sia_ensemble_adjoint_run", ens.nm, ens._mem, ens._par, tp, n, ens._lam, ens._work, dJ)
