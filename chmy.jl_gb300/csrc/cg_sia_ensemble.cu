@@ -659,14 +659,17 @@ __global__ void __launch_bounds__(256) ens_adj_cell_kernel(const AdjMember<T>* a
             pD += tDu;
             pS += tSu;
         }
-        const T mM = (FL(i, j, 0) & 2) ? T(1) : T(0);
-        const T lo = muc * (T(1) + dt * v.beta * mM);
+        // the mass balance's direct terms: d H'/d H = 1 + dt beta and d H'/d ela = -dt beta
+        // where it is not capped (the step's constants, once per thread)
+        const bool mM = (FL(i, j, 0) & 2) != 0;
+        const T dtb = dt * v.beta;
+        const T lo = mM ? muc * (T(1) + dtb) : muc;
         v.lo(i, j, 0) = lo + pD * adj_tape(v, sb, kDH)(i, j, 0) + pS;
         v.pax(i, j, 0) = pD * adj_tape(v, sb, kEX)(i, j, 0);
         v.pay(i, j, 0) = pD * adj_tape(v, sb, kEY)(i, j, 0);
         sdt = (double)(muc * adj_tape(v, sb, kW)(i, j, 0));
         v.aG(i, j, 0) += (double)(pD * adj_tape(v, sb, kGF)(i, j, 0));
-        v.aE(i, j, 0) -= (double)(muc * dt * v.beta * mM);
+        if (mM) v.aE(i, j, 0) -= (double)(muc * dtb);
     }
     const double a = block_sum(sdt);
     if (threadIdx.x == 0 && threadIdx.y == 0) part[blk] = a;
