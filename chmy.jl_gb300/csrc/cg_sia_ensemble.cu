@@ -362,7 +362,8 @@ struct EnsTapeHeader {
 };
 constexpr unsigned long long kEnsTapeMagic = 0x31534e4541544953ull;  // "SIATENS1"
 
-// FNV-1a over the members' layouts and parameters: a reverse sweep checks it against its own
+// FNV-1a over the members' layouts, grid spacings and parameters: a reverse sweep checks it
+// against its own
 inline unsigned long long ens_tape_hash(int nm, const cg_sia_member* ms, const cg_sia_params* ps) {
     unsigned long long h = 1469598103934665603ull;
     auto mix = [&](const void* p, size_t n) {
@@ -374,7 +375,9 @@ inline unsigned long long ens_tape_hash(int nm, const cg_sia_member* ms, const c
         const long long lay[8] = {ms[m].grid.n[0], ms[m].grid.n[1], H.n[0], H.n[1], H.halo[0], H.halo[1],
                                   (long long)H.stride[0], (long long)H.stride[1]};
         mix(lay, sizeof(lay));
-        const double pr[7] = {ps[m].Gamma, ps[m].As, ps[m].beta, ps[m].ela, ps[m].m_max, ps[m].cfl, ps[m].dt_max};
+        const double pr[9] = {ps[m].Gamma,  ps[m].As,     ps[m].beta,
+                              ps[m].ela,    ps[m].m_max,  ps[m].cfl,
+                              ps[m].dt_max, ms[m].grid.inv_spacing[0], ms[m].grid.inv_spacing[1]};
         mix(pr, sizeof(pr));
         mix(&ps[m].n, sizeof(int));
     }
