@@ -509,7 +509,7 @@ def config_suite(arch, stream, peak):
     out = {}
     Cl, Vl = Center(), Vertex()
 
-    # config 1: 2D explicit diffusion, FP64, 1024^2 over [-1, 1]^2, D = 1, dt = h^2/(4.1 D)
+    # 2D explicit diffusion, FP64, 1024^2 over [-1, 1]^2, D = 1, dt = h^2/(4.1 D)
     n1 = 1024
     g1 = UniformGrid(origin=(-1.0, -1.0), extent=(2.0, 2.0), dims=(n1, n1), dtype=np.float64)
     x, y = padded_mesh(g1, Cl)
@@ -535,7 +535,7 @@ def config_suite(arch, stream, peak):
     }
     del A, B
 
-    # config 2: 3D PT variable diffusion at 512^3, a sample of PT iterations of one step
+    # 3D PT variable diffusion at 512^3, a sample of PT iterations of one step
     n2, npt = 512, 100
     g2 = UniformGrid(origin=(-0.5,) * 3, extent=(1.0,) * 3, dims=(n2,) * 3, dtype=np.float64)
     rng = np.random.default_rng(2)
@@ -622,7 +622,7 @@ def config_suite(arch, stream, peak):
         },
     }
 
-    # config 5: SIA ensemble, 64 members of 128^2..1024^2, FP64, 1000 steps in one batched run
+    # SIA ensemble, 64 members of 128^2..1024^2, FP64, 1000 steps in one batched run
     ens = sia_ensemble(members=64)
     keep, mem = [], (_abi.cg_sia_member * len(ens))()
     params = (_abi.cg_sia_params * len(ens))()

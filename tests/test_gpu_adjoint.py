@@ -147,7 +147,7 @@ def _ptdiff_problem(n, T=np.float64):
 
 
 def test_ptdiff_gradient_D_matches_finite_differences(arch):
-    """Implicit diffusion steps (config 2 form, 2D 24^2): the adjoint gradient of
+    """Implicit variable-diffusivity steps (2D 24^2): the adjoint gradient of
     J = 1/2 |C^N - C_obs|^2 with respect to log(D) agrees with central differences; the
     checkpointed reverse sweep gives the same bits for 1, 2 and sqrt(N) steps per segment."""
     from chmy_gb300.adjoint import PTDiffusion
@@ -257,7 +257,7 @@ def _sia_problem(n=(48, 40), dt_max=0.5):
 @pytest.mark.parametrize("tape", [True, False], ids=["taped", "recomputing"])
 @pytest.mark.parametrize("dt_max", [0.5, 1e-3])
 def test_sia_gradient_gamma_ela_matches_finite_differences(arch, dt_max, tape):
-    """SIA time loop (config 5 form, 2D 48 x 40, 60 steps): the adjoint gradients of
+    """SIA time loop (flux -Gamma H^5 |grad S|^2 grad S, ELA mass balance; 2D 48 x 40, 60 steps): the adjoint gradients of
     J = 1/2 |H^N - H_obs|^2 with respect to log(Gamma) and ela agree with central differences
     to 1e-6, with the adaptive time step (dt_max = 0.5: dt from max D) and with dt capped
     (dt_max = 1e-3), for the taped and the recomputing reverse sweeps. Recomputing with
