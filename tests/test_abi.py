@@ -88,3 +88,56 @@ def test_no_closed_copy_calls_in_sources():
     pat = re.compile(r"Memcpy\w*Batch")
     for p in list((ROOT / "chmy.jl_gb300" / "csrc").glob("*")) + [ROOT / "include" / "chmy_gb300.h"]:
         assert not pat.search(p.read_text()), p
+
+
+def _field2d(nx, ny, loc=(0, 0), dtype=_abi.CG_F64, halo=1, pitch=None):
+    """A host descriptor with no data (layout only), as the size queries read it."""
+    f = _abi.cg_field()
+    f.dtype, f.ndim = dtype, 2
+    ext = [nx + loc[0], ny + loc[1]]
+    f.n[0], f.n[1], f.n[2] = ext[0], ext[1], 1
+    f.loc[0], f.loc[1] = loc
+    f.halo[0], f.halo[1] = halo, halo
+    f.stride[0], f.stride[1] = 1, pitch or (ext[0] + 4 * halo)
+    return f
+
+
+def _grid2d(nx, ny):
+    g = _abi.cg_grid()
+    g.ndim = 2
+    g.n[0], g.n[1], g.n[2] = nx, ny, 1
+    for d in range(2):
+        g.extent[d] = 2.0
+        g.spacing[d] = 2.0 / (nx, ny)[d]
+        g.inv_spacing[d] = 1.0 / g.spacing[d]
+    return g
+
+
+def test_sia_tape_sizes(lib):
+    """The tape-size queries (no context, no device work) follow the documented layouts: a
+    256-byte header, then per step 256 bytes of words and 9 arrays of H's allocation (row
+    stride x (n_y + 4 halo) elements), each rounded up to 256 bytes; an ensemble tape holds
+    every member's step block in turn. Bad arguments give CG_ERR_ARG."""
+
+    def r256(b):
+        return (b + 255) // 256 * 256
+
+    for dt, el in ((_abi.CG_F64, 8), (_abi.CG_F32, 4)):
+        H = _field2d(37, 21, dtype=dt, pitch=64)
+        g = _grid2d(37, 21)
+        step = 256 + 9 * r256(64 * (21 + 4) * el)
+        out = ctypes.c_size_t()
+        assert lib.cg_sia_tape_bytes(ctypes.byref(g), ctypes.byref(H), 5, ctypes.byref(out)) == 0
+        assert out.value == 256 + 5 * step
+        assert lib.cg_sia_tape_bytes(ctypes.byref(g), ctypes.byref(H), 0, ctypes.byref(out)) == 0
+        assert out.value == 256
+        assert lib.cg_sia_tape_bytes(ctypes.byref(g), ctypes.byref(H), -1, ctypes.byref(out)) == _abi.CG_ERR_ARG
+        mem = (_abi.cg_sia_member * 2)()
+        sizes = [(37, 21, 64), (50, 33, 57)]
+        for k, (nx, ny, pitch) in enumerate(sizes):
+            mem[k].grid = _grid2d(nx, ny)
+            mem[k].H = _field2d(nx, ny, dtype=dt, pitch=pitch)
+        per = sum(256 + 9 * r256(p * (ny + 4) * el) for nx, ny, p in sizes)
+        assert lib.cg_sia_ensemble_tape_bytes(2, mem, 7, ctypes.byref(out)) == 0
+        assert out.value == 256 + 7 * per
+        assert lib.cg_sia_ensemble_tape_bytes(0, mem, 7, ctypes.byref(out)) == _abi.CG_ERR_ARG
