@@ -55,6 +55,20 @@ def _env_int(name, default):
         return default
 
 
+def reduce_over_ranks(dist, ms: float, work: float, device="cpu"):
+    """The N > 1 replica aggregation: the slowest rank's time (max) and the ranks' total work
+    (sum). With dist None (one rank) the inputs come back unchanged."""
+    if dist is None:
+        return float(ms), float(work)
+    import torch
+
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    w = torch.tensor([float(work)], dtype=torch.float64, device=device)
+    dist.all_reduce(w, op=dist.ReduceOp.SUM)
+    return float(t.item()), float(w.item())
+
+
 def measured_peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -290,15 +304,7 @@ def run_ours(args, rank, world, dist):
     barrier()
     ms = ev0.elapsed_time(ev1)
     iters = sum(r.iterations for r in results)
-    if dist is not None:
-        t = torch.tensor([ms], device=arch.device)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-        tot = torch.tensor([float(iters)], device=arch.device)
-        dist.all_reduce(tot, op=dist.ReduceOp.SUM)
-        iters_all = float(tot.item())
-    else:
-        iters_all = float(iters)
+    ms, iters_all = reduce_over_ranks(dist, ms, iters, arch.device)
     bytes_per_iter = A32 * n * n * 4
     value = bytes_per_iter * iters_all / (ms * 1e-3) / 1e9
     # kernels in the timed solves: per PT iteration the fused kernel (bc!(V) folded into its
@@ -348,11 +354,8 @@ def run_ours(args, rank, world, dist):
     e1.record(stream)
     torch.cuda.synchronize()
     ms_e2e = e0.elapsed_time(e1)
-    if dist is not None:
-        t = torch.tensor([ms_e2e], device=arch.device)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_e2e = float(t.item())
-    e2e_value = bytes_per_iter * e2e_iters * world / (ms_e2e * 1e-3) / 1e9
+    ms_e2e, e2e_iters_all = reduce_over_ranks(dist, ms_e2e, e2e_iters, arch.device)
+    e2e_value = bytes_per_iter * e2e_iters_all / (ms_e2e * 1e-3) / 1e9
 
     # roofline: the fused FP32 PT kernel timed alone (public ping-pong entry, no bc), CUDA events
     # on the launching stream, algorithmic bytes per launch over the mean launch time
