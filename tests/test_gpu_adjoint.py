@@ -313,18 +313,21 @@ def test_sia_gradient_gamma_ela_matches_finite_differences(arch, dt_max, tape):
     assert abs(gH0[idx] - fdH) <= 1e-6 * max(abs(fdH), float(np.abs(gH0).max())), (gH0[idx], fdH)
 
 
+@pytest.mark.parametrize("glen_n", [3, 2, 4])
 @pytest.mark.parametrize("tape", [True, False], ids=["taped", "recomputing"])
 @pytest.mark.parametrize("dt_max", [0.5, 1e-3])
-def test_sia_gradient_matches_dual_numbers(arch, dt_max, tape):
+def test_sia_gradient_matches_dual_numbers(arch, dt_max, tape, glen_n):
     """The SIA adjoint gradients (GPU, reverse sweep) against forward-mode dual numbers run
     through the oracle's restated time loop (exact tangents of its arithmetic, including the
-    adaptive dt through max D): dJ/dGamma and dJ/dela agree to 1e-9 relative. The remaining
-    difference is the rounding of two forward evaluations of the same discrete model."""
+    adaptive dt through max D), for Glen exponents 3, 2 and 4: dJ/dGamma and dJ/dela agree
+    to 1e-9 relative. The remaining difference is the rounding of two forward evaluations of
+    the same discrete model."""
     from _oracle import NpField, desc_array, lib
     from chmy_gb300.adjoint import SIA
     from chmy_gb300.grids import Center, Vertex
 
     grid, bed, H0, p = _sia_problem(dt_max=dt_max)
+    p.n = glen_n  # n = 2 and 4 reach the square-root forms of the derivatives of D
     nsteps = 60
     inner = (slice(2, -2), slice(2, -2))
     T = np.float64
