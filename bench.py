@@ -207,6 +207,21 @@ def workload_name(n):
     )
 
 
+def reference_workload_name(n):
+    return (
+        f"2D VE Stokes {n}^2, 8 circular inclusions (log10 eta U[-3,3], seed 3), pure shear: "
+        "FP64 PT iterations (update_stress!, update_velocity!, bc!(V)), bounded sample; no solve"
+    )
+
+
+# PT iterations of the plain FP64 solve of the 2048^2 inclusion problem to residual 1e-8 with
+# the PT parameters below (re_m = 4 pi, a check every n/4 iterations), as the FP64 GPU solve
+# counts them (the GPU's FP64 iteration counts match the oracle's PT loop within 1 %). The
+# reference arm cannot solve in its time budget; it extrapolates its time to solution with this
+# count. Our arm measures the count itself on every run.
+FP64_ITERATIONS_2048 = 96256
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -217,6 +232,9 @@ def run_reference(args, rank, world):
             its += it
             secs += el
     value = A64 * args.n * args.n * 8 * its / secs / 1e9
+    # the FP64 solve's iteration count scales with n (PT iterations per grid point are constant)
+    iters_to_solve = int(round(FP64_ITERATIONS_2048 * args.n / 2048))
+    tts_ref = secs / max(its, 1) * iters_to_solve
     line = {
         "impl": "reference",
         "metric": "T_eff GB/s",
@@ -231,7 +249,12 @@ def run_reference(args, rank, world):
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic (seeded inclusions)",
-        "config": {"workload": workload_name(args.n), "n": args.n, "sample_per_step": f"{args.ref_seconds:.0f} s of FP64 PT iterations"},
+        "config": {"workload": reference_workload_name(args.n), "n": args.n,
+                   "sample_per_step": f"{args.ref_seconds:.0f} s of FP64 PT iterations",
+                   "bytes": "T_eff counts 16 arrays x n^2 x 8 B per FP64 PT iteration"},
+        "time_to_solution_s": tts_ref,
+        "time_to_solution": {"kind": "extrapolated", "fp64_iterations": iters_to_solve,
+                             "note": "sampled seconds per FP64 PT iteration x the FP64 solve's iteration count"},
         "cpu_baseline": {
             "value": value,
             "unit": "GB/s",
@@ -321,8 +344,12 @@ def run_ours(args, rank, world, dist):
     # memory, solve, read the velocity and pressure back every step
     pinned = {}
     h2d = 0
-    for k in state_names + ("eta",):
-        v = pb.host[k]
+    host_in = dict(pb.host)
+    # 1/eta is an input of the kernels, prepared on the host (as StokesSolver does) and uploaded
+    # with the other arrays: no device compute outside the library in the timed region
+    host_in["inv_eta"] = 1.0 / np.asarray(pb.host["eta"])
+    for k in state_names + ("eta", "inv_eta"):
+        v = host_in[k]
         if isinstance(v, list):
             pinned[k] = [torch.from_numpy(a).pin_memory() for a in v]
             h2d += sum(a.nbytes for a in v)
@@ -335,7 +362,6 @@ def run_ours(args, rank, world, dist):
 
     def e2e_step():
         solver.upload(pinned)
-        solver.fields["inv_eta"].data.copy_(1.0 / solver.fields["eta"].data)
         solver.apply_bc()
         r = solver.solve(precision=_abi.CG_F32, max_outer=12, inner_rtol=1e-5)
         for o, f in zip(outs, list(solver.fields["V"]) + [solver.fields["P"]]):
@@ -406,13 +432,16 @@ def run_ours(args, rank, world, dist):
         del keep3, d3a, d3b
         torch.cuda.empty_cache()
 
-    suite = None if args.skip_suite else config_suite(arch, stream, peak)
+    suite = None if args.skip_suite else config_suite(arch, stream, peak, fp64=not args.skip_fp64)
 
     # plain FP64 GPU solve of the same problem, once (time_to_solution comparison)
     fp64 = None
+    err_vs_fp64 = None
     if not args.skip_fp64:
+        dc_state = snapshot_state(solver)  # the last timed FP32-DC solve's converged state
         reset_device()
         r64 = solver.solve(precision=_abi.CG_F64)
+        err_vs_fp64 = state_difference(dc_state, snapshot_state(solver), 2)
         fp64 = {"s": r64.seconds, "iterations": r64.iterations, "converged": r64.converged, "err": [r64.err[i] for i in range(3)],
                 "t_eff_gbs": A64 * n * n * 8 * r64.iterations / r64.seconds / 1e9}
     dc_s = np.array([r.seconds for r in results])
@@ -424,10 +453,14 @@ def run_ours(args, rank, world, dist):
     }
     if fp64:
         tts.update({"fp64_s": fp64["s"], "fp64_iterations": fp64["iterations"], "fp64_err": fp64["err"],
-                    "fp64_t_eff_gbs": fp64["t_eff_gbs"], "speedup_fp32dc_vs_fp64": fp64["s"] / tts["fp32_dc_s"]})
+                    "fp64_t_eff_gbs": fp64["t_eff_gbs"], "speedup_fp32dc_vs_fp64": fp64["s"] / tts["fp32_dc_s"],
+                    "err_vs_fp64": err_vs_fp64})
 
     if rank == 0:
         cpu_teff, cpu_it, cpu_s, cpu_threads = cpu_sample(n, seconds=args.cpu_seconds, max_iters=args.ref_iters)
+        if tts.get("fp64_iterations"):
+            tts["cpu_fp64_s_extrapolated"] = cpu_s / max(cpu_it, 1) * tts["fp64_iterations"]
+            tts["speedup_vs_cpu_fp64"] = tts["cpu_fp64_s_extrapolated"] / tts["fp32_dc_s"]
         line = {
             "metric": "T_eff GB/s",
             "value": value,
@@ -446,11 +479,16 @@ def run_ours(args, rank, world, dist):
                 "n": n,
                 "eps": pb.eps,
                 "ncheck": pb.ncheck,
+                "re_m": "4 pi",
+                "pt_constants": "examples/stokes_2d_inc_ve_T.jl:86-93 formulas with re_m = 4 pi (the example's 2.3 pi "
+                "takes more iterations on this inclusion problem) and a check every n/4 iterations (the example: 2 nx); "
+                "the reference's own constants are checked against the oracle in tests/test_gpu_solve.py",
                 "arrays_per_iteration": A32,
                 "l2": "working set larger than L2 (no flush)",
                 "step": "one PT solve from the initial state to 1e-8",
             },
             "time_to_solution": tts,
+            "time_to_solution_s": tts["fp32_dc_s"],
             "e2e": {"value": e2e_value, "unit": "GB/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "steps": e2e_steps},
             "gpu_launches": launches,
             "roofline": {
@@ -481,6 +519,32 @@ def run_ours(args, rank, world, dist):
     arch.close()
 
 
+def snapshot_state(solver):
+    """Device copies of a solver's V, tau and P (for solution comparisons outside timed regions)."""
+    return {
+        "V": [f.data.clone() for f in solver.fields["V"]],
+        "tau": [f.data.clone() for f in solver.fields["tau"]],
+        "P": solver.fields["P"].data.clone(),
+    }
+
+
+def state_difference(a, b, nd):
+    """Max relative difference of two converged states per quantity: max|a - b| / max|b| over the
+    interior for every V and tau component, and for P after subtracting each state's interior
+    mean (normal velocity is prescribed on every side, so P is defined up to a constant)."""
+    sl = (slice(2, -2),) * nd
+    out = {}
+    for name in ("V", "tau"):
+        for k, (x, y) in enumerate(zip(a[name], b[name])):
+            xi, yi = x[sl].double(), y[sl].double()
+            out[f"{name}{k}"] = float((xi - yi).abs().max() / yi.abs().max().clamp_min(1e-300))
+    pa, pb_ = a["P"][sl].double(), b["P"][sl].double()
+    pa, pb_ = pa - pa.mean(), pb_ - pb_.mean()
+    out["P_minus_mean"] = float((pa - pb_).abs().max() / pb_.abs().max().clamp_min(1e-300))
+    out["max"] = max(out.values())
+    return out
+
+
 def _timed(fn, stream, reps=1):
     """CUDA-event time (ms) of `reps` calls of fn on `stream`, after one untimed call (which
     captures the call's CUDA graph)."""
@@ -497,7 +561,7 @@ def _timed(fn, stream, reps=1):
     return a.elapsed_time(b) / reps
 
 
-def config_suite(arch, stream, peak):
+def config_suite(arch, stream, peak, fp64=True):
     """The other configurations' hot loops, each timed with CUDA events on synthetic inputs of
     the configuration's shape: explicit diffusion 1024^2 (2000 steps), PT variable diffusion
     512^3 (a bounded sample of PT iterations, FP64 and FP32) and the SIA ensemble (64 members,
@@ -658,7 +722,7 @@ def config_suite(arch, stream, peak):
     torch.cuda.empty_cache()
     out["sia_adjoint"] = sia_adjoint_cost(arch)
     torch.cuda.empty_cache()
-    out["stokes3d_adjoint"] = stokes3d_adjoint_cost(arch)
+    out["stokes3d_adjoint"] = stokes3d_adjoint_cost(arch, fp64=fp64)
     torch.cuda.empty_cache()
     out["sia_ensemble_adjoint"] = sia_ensemble_adjoint_cost(arch)
     torch.cuda.empty_cache()
@@ -723,11 +787,13 @@ def _dome_r2(grid):
     return x * x + y * y
 
 
-def stokes3d_adjoint_cost(arch, n=256):
+def stokes3d_adjoint_cost(arch, n=256, fp64=True):
     """The 3D VE Stokes configuration (n^3, random log-viscosity field, buoyant sphere): the
     forward solve to residual 1e-8 and the adjoint solve for dJ/d log(eta) of a misfit of Vz on
     the middle vertex plane (scaled so that max |dJ/dV| = 1), both in FP32 PT iterations inside
-    FP64 defect correction. Wall clock around synchronised calls."""
+    FP64 defect correction. With `fp64`, the same forward and adjoint solves in plain FP64 PT
+    (the configuration's precision) beside them: their times, and the FP32-DC results' errors
+    against them. Wall clock around synchronised calls."""
     import time
 
     import torch
@@ -737,25 +803,36 @@ def stokes3d_adjoint_cost(arch, n=256):
     from chmy_gb300.solvers import StokesSolver
 
     pb = stokes3d_grf(n)
-    s = StokesSolver(arch, pb)
-    s.apply_bc()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    res = s.solve(precision=_abi.CG_F32)
-    torch.cuda.synchronize()
-    tf = time.perf_counter() - t0
-    v = s.fields["V"][2].to_numpy()
     sens = (n // 2 + 2, slice(2, n + 2), slice(2, n + 2))
-    r = np.random.default_rng(3).standard_normal(v[sens].shape)
-    dJ = np.zeros_like(v)
-    dJ[sens] = r / np.abs(r).max()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    grad, ares = s.gradient_log_eta([None, None, dJ], precision=_abi.CG_F32)
-    torch.cuda.synchronize()
-    ta = time.perf_counter() - t0
+
+    def run(precision):
+        s = StokesSolver(arch, pb)
+        s.apply_bc()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = s.solve(precision=precision)
+        torch.cuda.synchronize()
+        tf = time.perf_counter() - t0
+        v = s.fields["V"][2].to_numpy()
+        r = np.random.default_rng(3).standard_normal(v[sens].shape)
+        dJ = np.zeros_like(v)
+        dJ[sens] = r / np.abs(r).max()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        grad, ares = s.gradient_log_eta([None, None, dJ], precision=precision)
+        torch.cuda.synchronize()
+        ta = time.perf_counter() - t0
+        state = snapshot_state(s)
+        g = grad.data.clone()
+        del s, grad
+        torch.cuda.empty_cache()
+        return res, tf, ares, ta, state, g
+
+    res, tf, ares, ta, st_dc, g_dc = run(_abi.CG_F32)
     out = {
         "workload": f"3D VE Stokes {n}^3, log-viscosity Gaussian random field, forward solve and adjoint solve for dJ/d log(eta), FP32 PT in FP64 defect correction, residual 1e-8",
+        "misfit": "1/2 |Vz - Vz_obs|^2 on the middle vertex plane z = n/2 (Vz on the top plane is a Dirichlet value, "
+        "so its misfit has no sensitivity); Vz_obs - Vz = seeded normal noise scaled to max 1",
         "forward_s": tf,
         "forward_iterations": int(res.iterations),
         "forward_converged": int(res.converged),
@@ -764,7 +841,22 @@ def stokes3d_adjoint_cost(arch, n=256):
         "adjoint_converged": int(ares.converged),
         "gradient_over_forward": (tf + ta) / tf,
     }
-    del s, grad
+    if fp64:
+        r64, tf64, a64, ta64, st64, g64 = run(_abi.CG_F64)
+        sl = (slice(2, -2),) * 3
+        gd, gr = g_dc[sl], g64[sl]
+        out["fp64"] = {
+            "forward_s": tf64,
+            "forward_iterations": int(r64.iterations),
+            "forward_converged": int(r64.converged),
+            "adjoint_s": ta64,
+            "adjoint_iterations": int(a64.iterations),
+            "adjoint_converged": int(a64.converged),
+            "speedup_fp32dc_forward": tf64 / tf,
+            "speedup_fp32dc_gradient": (tf64 + ta64) / (tf + ta),
+            "err_vs_fp64_forward": state_difference(st_dc, st64, 3),
+            "err_vs_fp64_gradient": float((gd - gr).abs().max() / gr.abs().max().clamp_min(1e-300)),
+        }
     return out
 
 

@@ -76,6 +76,16 @@ bool cg_ptdiff_fused_enabled();
 // The SIA ensemble as one persistent cooperative launch (CG_SIA_PERSISTENT=1) instead of one
 // launch per phase replayed from a CUDA graph (the default, measured faster).
 bool cg_sia_persistent_enabled();
+// Grid barriers of the persistent SIA ensemble kernel: the time limit of every wait
+// (CG_SIA_BARRIER_LIMIT_MS, default 2000 ms) and a number of arrivals that the barrier expects
+// beyond the grid's blocks (CG_SIA_BARRIER_WITHHELD, default 0). A withheld arrival never
+// comes, so every wait runs out: the failure-detection test uses this to check that the kernel
+// returns on its limit and the call reports CG_ERR_TIMEOUT.
+struct cg_barrier_cfg {
+    unsigned long long limit_ns = 2000000000ull;
+    int withheld = 0;
+};
+cg_barrier_cfg cg_sia_barrier_cfg();
 
 template <class... P, class... A>
 inline cudaError_t cg_launch(void (*kern)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, bool dep,

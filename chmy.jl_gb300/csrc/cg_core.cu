@@ -1,13 +1,17 @@
 // cg_core.cu — context, memory, argument checks, the fused boundary-condition kernel and the
 // max-norm reduction of libchmy_gb300.
 #include <cstdarg>
+#include <cstdlib>
 #include <map>
 #include <mutex>
 #include <vector>
 
 #include "cg_common.cuh"
 
-static char g_init_err[512] = "";
+// Message of the calling thread's last failure in a call without a context (cg_init,
+// cg_maxabs_noalloc, ...): one buffer per host thread, so concurrent callers never garble
+// each other's text.
+static thread_local char g_init_err[512] = "";
 
 int cg_fail(cg_ctx* ctx, int code, const char* fmt, ...) {
     char* dst = ctx ? ctx->err : g_init_err;
@@ -111,6 +115,20 @@ bool cg_sia_persistent_enabled() {
     // read on every call (once per run), so that a process can compare both forms
     const char* e = std::getenv("CG_SIA_PERSISTENT");
     return e && e[0] == '1';
+}
+
+cg_barrier_cfg cg_sia_barrier_cfg() {
+    // read on every call, like CG_SIA_PERSISTENT
+    cg_barrier_cfg c;
+    if (const char* e = std::getenv("CG_SIA_BARRIER_LIMIT_MS")) {
+        const long ms = std::strtol(e, nullptr, 10);
+        if (ms >= 1 && ms <= 60000) c.limit_ns = (unsigned long long)ms * 1000000ull;
+    }
+    if (const char* e = std::getenv("CG_SIA_BARRIER_WITHHELD")) {
+        const long w = std::strtol(e, nullptr, 10);
+        if (w >= 0 && w <= 1024) c.withheld = (int)w;
+    }
+    return c;
 }
 
 bool cg_tune_verbose() {
@@ -695,27 +713,25 @@ extern "C" int cg_maxabs(cg_ctx* ctx, int nfields, const cg_field* fields, doubl
 
 // ---- max-norm without any allocation ----------------------------------------------------------
 //
-// For callers that cannot allocate device memory: hosts whose memory is owned by their own pool
-// (a Julia or Python runtime that forbids foreign cudaMalloc), code running while a stream is
-// being captured into a CUDA graph, or embedded settings with a fixed memory budget. The
-// reduction slots live in this file-scope device array instead of a context's buffer. Every
-// GPU that loads the library holds these 128 bytes until the process exits.
+// For callers that cannot allocate device memory: a host runtime that owns all device memory
+// through its own pool and forbids a library's cudaMalloc (a Julia or Python runtime with a
+// caching allocator, for instance), or an embedded deployment with a fixed device-memory
+// budget. The reduction slots live in this file-scope device array instead of a context's
+// buffer. Every GPU that loads the library holds these 128 bytes until the process exits.
 
 constexpr int kNoAllocMaxFields = CG_MAXABS_NOALLOC_MAX_FIELDS;
+static_assert(kNoAllocMaxFields <= kMaxRedFields, "the allocation-free slots must fit one RedBatch");
 static __device__ __align__(256) unsigned long long g_noalloc_red[kNoAllocMaxFields];
 
 namespace {
 constexpr int kNoAllocMaxDevices = 64;
 std::mutex g_noalloc_mu;
 unsigned long long* g_noalloc_addr[kNoAllocMaxDevices] = {};  // device address per device
-char g_noalloc_err[256] = "";
 
-int noalloc_fail(int code, const char* fmt, ...) {
-    va_list ap;
-    va_start(ap, fmt);
-    vsnprintf(g_noalloc_err, sizeof(g_noalloc_err), fmt, ap);
-    va_end(ap);
-    return cg_fail(nullptr, code, "%s", g_noalloc_err);
+// errors of this context-free entry go to the calling thread's own message buffer
+template <typename... A>
+int noalloc_fail(int code, const char* fmt, A... args) {
+    return cg_fail(nullptr, code, fmt, args...);
 }
 }  // namespace
 
@@ -774,6 +790,16 @@ extern "C" int cg_maxabs_noalloc(int device, void* stream, int nfields, const cg
         biggest = std::max(biggest, (long)R.n0 * R.n1 * R.n2);
     }
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    // the call ends by synchronising the stream to hand the maxima to the host; on a stream
+    // that is being captured that would fail and void the caller's capture, so refuse first
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    e = cudaStreamIsCapturing(st, &cap);
+    if (e != cudaSuccess || cap != cudaStreamCaptureStatusNone) {
+        restore();
+        return noalloc_fail(CG_ERR_ARG, "cg_maxabs_noalloc: the stream is being captured (or cannot be queried: %s); "
+                            "the call blocks until the maxima are on the host",
+                            cudaGetErrorString(e));
+    }
     int sms = 1;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     // the slots keep the previous call's maxima: clear them first

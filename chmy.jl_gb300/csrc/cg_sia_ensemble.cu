@@ -272,10 +272,11 @@ __global__ void ens_H_kernel(const Member<T>* mem, const int* prefix, int nm, co
 // launch loop over each phase's tiles, with a grid barrier between the phases. Per step:
 // D and the block maxima; barrier; Δt of every member (block 0) and the fluxes; barrier; the
 // thickness; barrier. The barrier counts arrivals on one monotonic word. Its waits give up
-// after two seconds (of the GPU's global timer) and set a timeout flag: the kernel then returns, and the
-// host reports the error. A cooperative launch keeps every block resident, so the waits end.
+// after a time limit (two seconds of the GPU's global timer unless the host sets another) and
+// set a timeout flag: the kernel then returns, and the host reports the error. A cooperative
+// launch keeps every block resident, so the waits end.
 struct GridBar {
-    unsigned long long arrived;  // arrivals since the launch: barrier k completes at (k + 1) x blocks
+    unsigned long long arrived;  // arrivals since the launch: barrier k completes at (k + 1) x expect
     int timeout;
 };
 
@@ -285,18 +286,20 @@ __device__ __forceinline__ unsigned long long globaltimer_ns() {
     return t;
 }
 
-// Barrier `k` (0, 1, ...) of the launch: one relaxed add per block, then a bounded wait until
-// all blocks have added. Nothing is reset, so the last block to arrive has no extra work.
-__device__ __forceinline__ bool grid_barrier(GridBar* b, unsigned nblocks, unsigned long long& k) {
+// Barrier `k` (0, 1, ...) of the launch: one relaxed add per block, then a wait of at most
+// `limit_ns` until `expect` blocks (the grid's size) have added. Nothing is reset, so the last
+// block to arrive has no extra work.
+__device__ __forceinline__ bool grid_barrier(GridBar* b, unsigned expect, unsigned long long limit_ns,
+                                             unsigned long long& k) {
     __syncthreads();
     if (threadIdx.x == 0 && threadIdx.y == 0) {
-        const unsigned long long target = (++k) * nblocks;
+        const unsigned long long target = (++k) * expect;
         __threadfence();
         atomicAdd(&b->arrived, 1ull);
         volatile unsigned long long* va = &b->arrived;
         const unsigned long long t0 = globaltimer_ns();
         while (*va < target) {
-            if (globaltimer_ns() - t0 > 2000000000ull) {  // 2 s
+            if (globaltimer_ns() - t0 > limit_ns) {
                 atomicExch(&b->timeout, 1);
                 break;
             }
@@ -311,21 +314,22 @@ __device__ __forceinline__ bool grid_barrier(GridBar* b, unsigned nblocks, unsig
 template <class T>
 __global__ void __launch_bounds__(256, 8) ens_persistent_kernel(const Member<T>* mem, const int* pD, const int* pI,
                                                              const int* pS, int nm, int totD, int totI, int totS,
-                                                             Words* w, int nsteps, GridBar* bar) {
+                                                             Words* w, int nsteps, GridBar* bar, unsigned expect,
+                                                             unsigned long long limit_ns) {
     const unsigned nb = gridDim.x;
     unsigned long long k = 0;
     for (int b = blockIdx.x; b < totS; b += nb) ens_S_tile(mem, pS, nm, b);
-    if (!grid_barrier(bar, nb, k)) return;
+    if (!grid_barrier(bar, expect, limit_ns, k)) return;
     for (int s = 0; s < nsteps; ++s) {
         for (int b = blockIdx.x; b < totD; b += nb) ens_D_tile(mem, pD, nm, w, b);
-        if (!grid_barrier(bar, nb, k)) return;
+        if (!grid_barrier(bar, expect, limit_ns, k)) return;
         if (blockIdx.x == 0)
             for (int m = threadIdx.x + blockDim.x * threadIdx.y; m < nm; m += blockDim.x * blockDim.y)
                 ens_dt_member(mem, w, m);
         for (int b = blockIdx.x; b < totI; b += nb) ens_q_tile(mem, pI, nm, b);
-        if (!grid_barrier(bar, nb, k)) return;
+        if (!grid_barrier(bar, expect, limit_ns, k)) return;
         for (int b = blockIdx.x; b < totI; b += nb) ens_H_tile(mem, pI, nm, w, b);
-        if (!grid_barrier(bar, nb, k)) return;
+        if (!grid_barrier(bar, expect, limit_ns, k)) return;
     }
 }
 
@@ -471,26 +475,26 @@ int run_t(cg_ctx* ctx, int nm, const cg_sia_member* ms, const cg_sia_params* ps,
     CG_CUDA(ctx, cudaMemcpyAsync(dpS, pS.data(), nm * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
     CG_CUDA(ctx, cudaMemsetAsync(dw, 0, nm * sizeof(Words), ctx->stream));
     const dim3 block(32, 8);
-    static const int coop = [] {
-        int dev = 0, v = 0;
-        cudaGetDevice(&dev);
-        return cudaDeviceGetAttribute(&v, cudaDevAttrCooperativeLaunch, dev) == cudaSuccess ? v : 0;
-    }();
+    // cooperative-launch support and residency of the persistent kernel on this context's
+    // device (queried per call: a process may hold contexts on different GPU models)
+    int coop = 0;
+    if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device) != cudaSuccess) coop = 0;
     if (coop && !tape && cg_sia_persistent_enabled()) {
         // the whole run in one cooperative launch of the resident blocks
-        static const int bps = [] {
-            int nb = 0;
-            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, ens_persistent_kernel<T>, 256, 0) != cudaSuccess) nb = 0;
-            return nb;
-        }();
+        int bps = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ens_persistent_kernel<T>, 256, 0) != cudaSuccess) bps = 0;
         if (bps < 1) return cg_fail(ctx, CG_ERR_CUDA, "sia_ensemble_run: the persistent kernel does not fit on an SM");
         GridBar* bar = reinterpret_cast<GridBar*>(base + bar_off);
         CG_CUDA(ctx, cudaMemsetAsync(bar, 0, sizeof(GridBar), ctx->stream));
         const Member<T>* cmem = dmem;
         const int *cpD = dpD, *cpI = dpI, *cpS = dpS;
         int anm = nm, atD = totD, atI = totI, atS = totS, ans = nsteps;
-        void* args[] = {&cmem, &cpD, &cpI, &cpS, &anm, &atD, &atI, &atS, &dw, &ans, &bar};
-        CG_CUDA(ctx, cudaLaunchCooperativeKernel((const void*)ens_persistent_kernel<T>, dim3(bps * ctx->num_sms), block,
+        const unsigned nblocks = (unsigned)(bps * ctx->num_sms);
+        const cg_barrier_cfg bcfg = cg_sia_barrier_cfg();
+        unsigned expect = nblocks + (unsigned)bcfg.withheld;
+        unsigned long long limit_ns = bcfg.limit_ns;
+        void* args[] = {&cmem, &cpD, &cpI, &cpS, &anm, &atD, &atI, &atS, &dw, &ans, &bar, &expect, &limit_ns};
+        CG_CUDA(ctx, cudaLaunchCooperativeKernel((const void*)ens_persistent_kernel<T>, dim3(nblocks), block,
                                                  args, 0, ctx->stream));
         int timed_out = 0;
         CG_CUDA(ctx, cudaMemcpyAsync(&timed_out, &bar->timeout, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));

@@ -122,7 +122,8 @@ CG_API int cg_abi_version(void);
  * replaces it. */
 CG_API int cg_init(int device, cg_ctx** out);
 CG_API int cg_destroy(cg_ctx* ctx);
-/* Message of the last failing call on `ctx` (or of the last cg_init failure if ctx == NULL). */
+/* Message of the last failing call on `ctx`. With ctx == NULL: the calling thread's last
+ * failure of a call that takes no context (cg_init, cg_maxabs_noalloc, ...). */
 CG_API const char* cg_last_error(const cg_ctx* ctx);
 /* Use `stream` (a cudaStream_t; NULL restores the context's own stream) for later calls. */
 CG_API int cg_set_stream(cg_ctx* ctx, void* stream);
@@ -159,20 +160,23 @@ CG_API int cg_maxabs(cg_ctx* ctx, int nfields, const cg_field* fields, double* o
               int32_t* nonfinite);
 
 /* The same max-norm reduction for callers that cannot allocate device memory: a host
- * runtime that owns all device memory through its own pool, code issued while a stream is
- * being captured into a CUDA graph, or a deployment with a fixed memory budget. It needs no
- * context and calls no cudaMalloc/cudaFree (nor any allocating library routine): its
- * reduction slots are a fixed array of CG_MAXABS_NOALLOC_MAX_FIELDS 64-bit words in the
- * library's device memory, which every GPU that loads the library keeps until exit.
+ * runtime that owns all device memory through its own pool and does not let a library call
+ * cudaMalloc (a Julia or Python runtime with a caching allocator, for instance), or a
+ * deployment with a fixed device-memory budget. It needs no context and calls no
+ * cudaMalloc/cudaFree (nor any allocating library routine): its reduction slots are a fixed
+ * array of CG_MAXABS_NOALLOC_MAX_FIELDS 64-bit words in the library's device memory, which
+ * every GPU that loads the library keeps until exit.
  * This entry point has no counterpart in the reference.
  * - `device`: CUDA ordinal to run on (made current for the call, then restored); `stream`:
- *   a cudaStream_t or NULL. Blocks until the values are on the host.
+ *   a cudaStream_t or NULL. The call blocks until the values are on the host (it
+ *   synchronises `stream`); a stream that is being captured is rejected with CG_ERR_ARG
+ *   before anything is enqueued.
  * - nfields above CG_MAXABS_NOALLOC_MAX_FIELDS is rejected with CG_ERR_ARG.
- * - The first call on a device looks up the array's device address (once per device); make
- *   that first call before any stream capture.
+ * - The first call on a device looks up the array's device address (once per device, with
+ *   that device current); make that first call before any stream capture.
  * - All calls share the array (the slots are cleared at the start of each call): calls
  *   that overlap on the GPU race and must not be issued concurrently.
- * Errors are reported through cg_last_error(NULL). */
+ * Errors are reported through cg_last_error(NULL), per calling thread. */
 #define CG_MAXABS_NOALLOC_MAX_FIELDS 16
 CG_API int cg_maxabs_noalloc(int device, void* stream, int nfields, const cg_field* fields,
                              double* out_host, int32_t* nonfinite);

@@ -169,3 +169,62 @@ def test_ensemble_persistent_launch_equals_phase_launches(arch, monkeypatch, T):
     for k, (a, b) in enumerate(zip(fa, fb)):
         for x, y in zip(a, b):
             np.testing.assert_array_equal(x, y, err_msg=f"member {k}")
+
+
+def test_ensemble_persistent_barrier_wait_runs_out(arch, monkeypatch):
+    """Failure detection of the persistent launch's grid barriers, without a GPU fault: the host
+    makes every barrier expect one arrival more than the grid has blocks (an arrival that never
+    comes) and sets a 20 ms limit on each wait. Every block's wait runs out, the kernel returns,
+    and the call reports CG_ERR_TIMEOUT. The context stays usable: the same run without the
+    withheld arrival then matches the per-phase launches bit for bit."""
+    import time
+
+    from chmy_gb300.configs import sia_ensemble
+
+    T = np.float64
+    ens = sia_ensemble(members=3, nmin=40, nmax=80, seed=9, dtype=T)
+    nsteps = 5
+    rng = np.random.default_rng(4)
+    start = []
+    for grid, h, p in ens:
+        H0 = NpField(grid, Center(), T)
+        H0.interior()[...] = rng.random(H0.dims) * 0.3
+        B = NpField(grid, Center(), T)
+        B.a[...] = h["B"]
+        start.append((grid, H0, B, p))
+
+    def run():
+        mem = (_abi.cg_sia_member * len(start))()
+        params = (_abi.cg_sia_params * len(start))()
+        keep = []
+        for k, (grid, H0, B, p) in enumerate(start):
+            Hg, Bg = to_gpu(arch, H0), to_gpu(arch, B)
+            qg = [to_gpu(arch, NpField(grid, (Vertex(), Center()), T)), to_gpu(arch, NpField(grid, (Center(), Vertex()), T))]
+            keep.append((Hg, qg, Bg))
+            mem[k].grid = grid.desc()
+            mem[k].H, mem[k].B = Hg.desc(), Bg.desc()
+            mem[k].q[0], mem[k].q[1] = qg[0].desc(), qg[1].desc()
+            params[k] = p
+        ts = (ctypes.c_double * len(start))()
+        rc = arch.lib.cg_sia_ensemble_run(arch.ctx, len(start), mem, params, nsteps, ts)
+        arch.synchronize()
+        return rc, [Hg.to_numpy() for Hg, _, _ in keep]
+
+    monkeypatch.setenv("CG_SIA_PERSISTENT", "1")
+    monkeypatch.setenv("CG_SIA_BARRIER_LIMIT_MS", "20")
+    monkeypatch.setenv("CG_SIA_BARRIER_WITHHELD", "1")
+    t0 = time.perf_counter()
+    rc, _ = run()
+    waited = time.perf_counter() - t0
+    assert rc == _abi.CG_ERR_TIMEOUT, (rc, arch.lib.cg_last_error(arch.ctx))
+    assert b"timed out" in arch.lib.cg_last_error(arch.ctx)
+    assert waited < 1.5, waited  # the 20 ms limit applied, not the 2 s default
+    monkeypatch.delenv("CG_SIA_BARRIER_WITHHELD")
+    monkeypatch.delenv("CG_SIA_BARRIER_LIMIT_MS")
+    rc, Hp = run()
+    assert rc == _abi.CG_OK, arch.lib.cg_last_error(arch.ctx)
+    monkeypatch.setenv("CG_SIA_PERSISTENT", "0")
+    rc, Hg = run()
+    assert rc == _abi.CG_OK
+    for a, b in zip(Hp, Hg):
+        np.testing.assert_array_equal(a, b)

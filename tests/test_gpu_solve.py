@@ -6,7 +6,7 @@ import ctypes
 import numpy as np
 import pytest
 
-from _oracle import NpField, bc_apply, lib, stokes_desc
+from _oracle import NpField, bc_apply, lib, stokes_desc, stokes_problem_fields
 from chmy_gb300 import _abi
 from chmy_gb300.bcs import Dirichlet, to_cg_bc
 from chmy_gb300.configs import stokes2d_inclusions
@@ -17,36 +17,30 @@ pytestmark = pytest.mark.gpu
 
 
 def oracle_solve(pb):
-    """The reference PT loop (examples/stokes_2d_inc_ve_T.jl:144-163) on the oracle."""
+    """The reference PT loop (examples/stokes_2d_inc_ve_T.jl:144-163; 3D
+    examples/stokes_3d_inc_ve_T.jl:163-183) on the oracle, in 2D or 3D: update_stress!,
+    update_velocity!, bc!(V) per iteration; every ncheck iterations bc!(r_V.d => Dirichlet on
+    dim d) and the measures max|divV|*tau_scale, max|r_V.d|*v_scale against eps."""
     g = pb.grid
-    Cl, Vl = Center(), Vertex()
-
-    def mk(a, loc):
-        f = NpField(g, loc)
-        f.a[...] = a
-        return f
-
-    h = pb.host
-    V = [mk(h["V"][0], (Vl, Cl)), mk(h["V"][1], (Cl, Vl))]
-    rV = [mk(h["r_V"][0], (Vl, Cl)), mk(h["r_V"][1], (Cl, Vl))]
-    tau = [mk(h["tau"][0], Cl), mk(h["tau"][1], Cl), mk(h["tau"][2], Vl)]
-    tauo = [mk(h["tau_old"][0], Cl), mk(h["tau_old"][1], Cl), mk(h["tau_old"][2], Vl)]
-    P, divV, eta = mk(h["P"], Cl), mk(h["divV"], Cl), mk(h["eta"], Cl)
-    d = stokes_desc(V=V, r_V=rV, P=P, divV=divV, tau=tau, tau_old=tauo, eta=eta)
+    nd = g.ndim
+    f = stokes_problem_fields(pb)
+    d = f["desc"]
     gd = g.desc()
     p = pb.params
+    V, rV, divV = f["V"], f["r_V"], f["divV"]
     bc_apply(g, V, pb.bc_V)
-    rb = [to_cg_bc(2, {"x": Dirichlet()}), to_cg_bc(2, {"y": Dirichlet()})]
+    rb = [to_cg_bc(nd, {"xyz"[k]: Dirichlet()}) for k in range(nd)]
+    e = None
     for it in range(1, pb.max_iter + 1):
         lib().or_stokes_update_stress(ctypes.byref(gd), ctypes.byref(d), ctypes.byref(p))
         lib().or_stokes_update_velocity(ctypes.byref(gd), ctypes.byref(d), ctypes.byref(p))
         bc_apply(g, V, pb.bc_V)
         if it % pb.ncheck == 0:
             bc_apply(g, rV, rb)
-            e = [np.abs(divV.interior()).max() * pb.tau_scale] + [np.abs(f.interior()).max() * pb.v_scale for f in rV]
+            e = [np.abs(divV.interior()).max() * pb.tau_scale] + [np.abs(x.interior()).max() * pb.v_scale for x in rV]
             if max(e) < pb.eps:
-                return it, e, V, P
-    return None, e, V, P
+                return it, e, V, f["P"]
+    return None, e, V, f["P"]
 
 
 @pytest.fixture(scope="module")
@@ -71,6 +65,66 @@ def test_fp64_iteration_count_matches_oracle(arch, problem64, oracle64):
     vx = s.fields["V"][0].to_numpy()
     scale = np.abs(V_ref[0].a).max()
     assert np.max(np.abs(vx - V_ref[0].a)) <= 1e-6 * scale
+
+
+def test_fp64_iteration_count_with_the_reference_pt_constants(arch):
+    """The example's own PT constants (examples/stokes_2d_inc_ve_T.jl:84-93): re_m = 2.3 pi and a
+    check every 2 nx iterations, on the 64^2 inclusion problem. The GPU's FP64 solve stops at
+    the oracle's check, and the states agree."""
+    pb = stokes2d_inclusions(64, ncheck=2 * 64, re_m_pi=2.3)
+    it_ref, e_ref, V_ref, P_ref = oracle_solve(pb)
+    assert it_ref is not None, ("oracle did not converge", e_ref)
+    s = StokesSolver(arch, pb, precompute_inv_eta=False)
+    s.apply_bc()
+    res = s.solve(precision=_abi.CG_F64)
+    assert res.converged == 1
+    assert abs(res.iterations - it_ref) <= 0.01 * it_ref, (res.iterations, it_ref)
+    for d in range(2):
+        a = s.fields["V"][d].to_numpy()
+        assert np.max(np.abs(a - V_ref[d].a)) <= 1e-6 * np.abs(V_ref[d].a).max()
+
+
+def test_fp64_iteration_count_3d_matches_oracle(arch):
+    """3D VE Stokes (random log-viscosity field, buoyant sphere, free slip) at 24^3: the GPU's
+    FP64 PT solve and the oracle's PT loop stop within 1 % of each other's iteration count,
+    and their velocities agree."""
+    from chmy_gb300.configs import stokes3d_grf
+
+    pb = stokes3d_grf(24, ncheck=24)
+    it_ref, e_ref, V_ref, P_ref = oracle_solve(pb)
+    assert it_ref is not None, ("oracle did not converge", e_ref)
+    s = StokesSolver(arch, pb, precompute_inv_eta=False)
+    s.apply_bc()
+    res = s.solve(precision=_abi.CG_F64)
+    assert res.converged == 1, (res.iterations, list(res.err))
+    assert abs(res.iterations - it_ref) <= max(0.01 * it_ref, pb.ncheck), (res.iterations, it_ref)
+    for d in range(3):
+        a = s.fields["V"][d].to_numpy()
+        assert np.max(np.abs(a - V_ref[d].a)) <= 1e-6 * max(np.abs(V_ref[d].a).max(), 1e-30), d
+
+
+@pytest.mark.parametrize("precision", [_abi.CG_F64, _abi.CG_F32])
+@pytest.mark.parametrize("nd", [2, 3])
+def test_solve_reports_nonfinite_viscosity(arch, precision, nd):
+    """A NaN viscosity in one interior cell: the solve returns CG_ERR_NONFINITE, as the
+    reference loop raises on a non-finite residual (examples/stokes_2d_inc_ve_T.jl:161), and
+    the context stays usable."""
+    import dataclasses
+
+    from chmy_gb300.configs import stokes3d_grf
+
+    pb = stokes2d_inclusions(32, ncheck=8) if nd == 2 else stokes3d_grf(16, ncheck=16)
+    eta = pb.host["eta"].copy()
+    eta[(7,) * nd] = np.nan
+    bad = dataclasses.replace(pb, host={**pb.host, "eta": eta})
+    s = StokesSolver(arch, bad)
+    s.apply_bc()
+    with pytest.raises(_abi.ChmyError) as exc:
+        s.solve(precision=precision, max_iter=4 * pb.ncheck)
+    assert exc.value.code == _abi.CG_ERR_NONFINITE, str(exc.value)
+    ok = StokesSolver(arch, pb)
+    ok.apply_bc()
+    assert ok.solve(precision=precision).converged == 1
 
 
 def test_fp64_with_precomputed_inverse_is_bitwise_same(arch, problem64):
