@@ -184,6 +184,10 @@ SIGNATURES: dict[str, list] = {
     "cg_diffusion_compute_q_masked": [_vp, P(cg_grid), P(cg_field), P(cg_field), C.c_double, P(cg_mask)],
     "cg_diffusion_update_C_masked": [_vp, P(cg_grid), P(cg_field), P(cg_field), C.c_double, P(cg_mask)],
     "cg_diffusion_run_masked": [_vp, P(cg_grid), P(cg_field), P(cg_field), C.c_double, C.c_double, P(cg_bc), P(cg_mask), C.c_int],
+    "cg_diffusion_tape_bytes": [P(cg_grid), P(cg_field), C.c_int, P(C.c_size_t)],
+    "cg_diffusion_run_taped": [_vp, P(cg_grid), P(cg_field), C.c_double, C.c_double, P(cg_bc), C.c_int, _vp, C.c_size_t],
+    "cg_diffusion_adjoint_run": [_vp, P(cg_grid), _vp, C.c_size_t, P(cg_field), P(cg_field), C.c_double, C.c_double, P(cg_bc),
+                                 P(C.c_double)],
     "cg_stokes_update_old": [_vp, P(cg_grid), P(cg_stokes_fields)],
     "cg_stokes_update_stress": [_vp, P(cg_grid), P(cg_stokes_fields), P(cg_stokes_params)],
     "cg_stokes_update_velocity": [_vp, P(cg_grid), P(cg_stokes_fields), P(cg_stokes_params)],
@@ -211,6 +215,8 @@ SIGNATURES: dict[str, list] = {
     ],
     "cg_stokes_gradient_log_eta": [_vp, P(cg_grid), P(cg_stokes_fields), P(cg_field), P(cg_stokes_params), P(cg_field)],
     "cg_stokes_thermal_step": [_vp, P(cg_grid), P(cg_stokes_fields), P(cg_stokes_params), P(cg_bc), P(cg_field)],
+    "cg_stokes_thermal_step_adjoint": [_vp, P(cg_grid), P(cg_stokes_fields), P(cg_stokes_params), P(cg_bc), P(cg_field), P(cg_field),
+                                       P(cg_field), P(cg_field), P(C.c_double)],
     "cg_stokes_pt_iterations_thermal": [
         _vp,
         P(cg_grid),

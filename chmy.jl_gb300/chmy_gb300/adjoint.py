@@ -124,6 +124,113 @@ class PTDiffusion:
         return self.gD.to_numpy(), self.adj["C"].to_numpy(), CN
 
 
+class ExplicitDiffusion:
+    """The explicit diffusion loop of examples/diffusion_2d.jl:43-47 (cg_diffusion_run: the fused
+    flux + update step, then bc!(C)) and its adjoint: the gradient of a misfit J(C^N) with respect
+    to the diffusivity chi and to the initial state, by reverse time stepping.
+
+    cg_diffusion_run_taped records the states C^0 .. C^N (the reverse step needs C^n and C^{n+1}
+    for dJ/dchi), and cg_diffusion_adjoint_run sweeps them back in one call. The whole run is one
+    taped segment when its tape fits `tape_budget` bytes (default: half the free device memory).
+    Otherwise a plain forward run keeps the start state of every segment of K steps, and each
+    segment, from the last, is re-run taped from its checkpoint and swept back (checkpointed
+    reverse time stepping with recomputation; K = the most steps whose tape fits)."""
+
+    def __init__(self, arch, grid, chi: float, dt: float, bc: _abi.cg_bc, dtype=np.float64):
+        self.arch, self.grid, self.chi, self.dt, self.bc = arch, grid, float(chi), float(dt), bc
+        C = Center()
+        self.C = Field(arch, grid, C, dtype)
+        self.B = Field(arch, grid, C, dtype)
+        self.lam = [Field(arch, grid, C, dtype), Field(arch, grid, C, dtype)]
+        self._tape = None
+
+    def tape_bytes(self, nsteps: int) -> int:
+        """Device bytes of a tape of `nsteps` steps."""
+        b = ctypes.c_size_t()
+        rc = self.arch.lib.cg_diffusion_tape_bytes(ctypes.byref(self.grid.desc()), ctypes.byref(self.C.desc()), int(nsteps),
+                                                   ctypes.byref(b))
+        if rc != 0:
+            raise ValueError("cg_diffusion_tape_bytes: bad arguments")
+        return int(b.value)
+
+    def _tape_buffer(self, nbytes: int):
+        import torch
+
+        if self._tape is None or self._tape.numel() < nbytes:
+            self._tape = None
+            self._tape = torch.empty(nbytes, dtype=torch.uint8, device=self.C.data.device)
+            if self._tape.data_ptr() % 256:
+                raise RuntimeError("the tape allocation is not 256-byte aligned")
+        return self._tape
+
+    def _apply_bc(self) -> None:
+        self.arch.call("cg_bc_apply", ctypes.byref(self.grid.desc()), 1, ctypes.byref(self.C.desc()), ctypes.byref(self.bc))
+
+    def _steps(self, nsteps: int) -> None:
+        """`nsteps` plain steps of C in place (ping-pong with B)."""
+        if nsteps <= 0:
+            return
+        self.arch.call("cg_diffusion_run", ctypes.byref(self.grid.desc()), ctypes.byref(self.C.desc()), ctypes.byref(self.B.desc()),
+                       self.chi, self.dt, ctypes.byref(self.bc), int(nsteps))
+        if nsteps % 2:
+            self.C.data.copy_(self.B.data)
+
+    def run(self, C0: np.ndarray, nsteps: int) -> np.ndarray:
+        """Forward: bc!(C0), then `nsteps` steps; returns C^N (padded)."""
+        self.C.from_numpy(C0)
+        self._apply_bc()
+        self._steps(nsteps)
+        return self.C.to_numpy()
+
+    def _segment(self, nsteps: int) -> int:
+        """`nsteps` taped steps of C in place; returns the tape's size."""
+        nbytes = self.tape_bytes(nsteps)
+        tape = self._tape_buffer(nbytes)
+        self.arch.call("cg_diffusion_run_taped", ctypes.byref(self.grid.desc()), ctypes.byref(self.C.desc()), self.chi, self.dt,
+                       ctypes.byref(self.bc), int(nsteps), ctypes.c_void_p(tape.data_ptr()), nbytes)
+        return nbytes
+
+    def gradient(self, C0: np.ndarray, nsteps: int, misfit_grad, checkpoint_every: int | None = None,
+                 tape_budget: int | None = None):
+        """(dJ/dchi, dJ/dC0, C^N). `misfit_grad(CN)` returns dJ/dC^N as a padded host array (its
+        interior is used); dJ/dC0 is a padded host array whose interior holds the gradient with
+        respect to the interior of C0 (the ghost cells follow it through bc!).
+        `checkpoint_every` caps the taped segment length."""
+        import torch
+
+        if tape_budget is None:
+            free, _ = torch.cuda.mem_get_info(self.C.data.device)
+            tape_budget = free // 2
+        per_step = self.tape_bytes(1) - self.tape_bytes(0)
+        K = max(1, min(nsteps, (int(tape_budget) - self.tape_bytes(0)) // per_step))
+        if checkpoint_every:
+            K = min(K, int(checkpoint_every))
+        self.C.from_numpy(C0)
+        self._apply_bc()
+        starts = list(range(0, nsteps, K))
+        checkpoints = {}
+        for start in starts[:-1]:  # plain forward up to the last segment, keeping its start states
+            checkpoints[start] = self.C.data.clone()
+            self._steps(K)
+        last = starts[-1]
+        nbytes = self._segment(nsteps - last)
+        CN = self.C.to_numpy()
+        self.lam[0].from_numpy(misfit_grad(CN))
+        dJ = (ctypes.c_double * 1)(0.0)
+        g = self.grid.desc()
+
+        def sweep(nb):
+            self.arch.call("cg_diffusion_adjoint_run", ctypes.byref(g), ctypes.c_void_p(self._tape.data_ptr()), nb,
+                           ctypes.byref(self.lam[0].desc()), ctypes.byref(self.lam[1].desc()), self.chi, self.dt,
+                           ctypes.byref(self.bc), dJ)
+
+        sweep(nbytes)
+        for start in reversed(starts[:-1]):
+            self.C.data.copy_(checkpoints.pop(start))
+            sweep(self._segment(K))
+        return dJ[0], self.lam[0].to_numpy(), CN
+
+
 class SIA:
     """The shallow-ice time loop of cg_sia_run (examples/sia.jl:71-81 with the flux
     -Gamma H^(n+2) |∇S|^(n-1) ∇S, adaptive Δt and linear mass balance capped at m_max) and its

@@ -36,10 +36,10 @@ struct cg_ctx {
     // numbered scratch buffers of the time-stepping loops (grown on demand, freed by cg_destroy)
     // slots: 0 thermal partner, 1 SIA D, 2 PT-diffusion partners, 3 SIA ensemble,
     // 4 PT-diffusion defect-correction pool, 5 SIA reverse step, 6 SIA reverse sweep over a tape,
-    // 7 SIA ensemble reverse sweep
-    static constexpr int kScratchSlots = 8;
-    void* scratch[kScratchSlots] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
-    size_t scratch_bytes[kScratchSlots] = {0, 0, 0, 0, 0, 0, 0, 0};
+    // 7 SIA ensemble reverse sweep, 8 explicit-diffusion reverse sweep, 9 thermal-step adjoint
+    static constexpr int kScratchSlots = 10;
+    void* scratch[kScratchSlots] = {};
+    size_t scratch_bytes[kScratchSlots] = {};
 };
 
 // Device scratch buffer `slot` of at least `bytes` (reallocated when too small; contents are

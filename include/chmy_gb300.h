@@ -210,6 +210,32 @@ CG_API int cg_diffusion_update_C_masked(cg_ctx* ctx, const cg_grid* grid, const 
 CG_API int cg_diffusion_run_masked(cg_ctx* ctx, const cg_grid* grid, const cg_field* A, const cg_field* B,
                                    double chi, double dt, const cg_bc* bc, const cg_mask* mask, int nsteps);
 
+/* ---- adjoint of the explicit diffusion loop (no reference counterpart: the reference has no
+ * adjoint) --------------------------------------------------------------------------------
+ * The loop C^{n+1} = bc!(C^n - dt divg(-chi grad C^n)) of cg_diffusion_run, differentiated for a
+ * misfit J(C^N) of the final interior: dJ/dC^0 at the interior cells and dJ/dchi. The ghost
+ * cells follow the interior through the boundary rules, so every side must carry a Dirichlet,
+ * Neumann or Periodic rule (CG_ERR_UNSUPPORTED otherwise); the fields are at Center. */
+
+/* Bytes of a tape of `nsteps` steps for a C of this layout: a 256-byte header, then the states
+ * C^0 .. C^nsteps, each C's padded allocation rounded up to 256 bytes. No context, no device work. */
+CG_API int cg_diffusion_tape_bytes(const cg_grid* grid, const cg_field* C, int nsteps, size_t* bytes);
+/* cg_diffusion_run's loop (the same steps, bit for bit) that records every state on `tape`
+ * (device memory of at least cg_diffusion_tape_bytes, 256-byte aligned): on entry C holds C^0
+ * with its ghost cells set by bc!, on return C^nsteps. */
+CG_API int cg_diffusion_run_taped(cg_ctx* ctx, const cg_grid* grid, const cg_field* C, double chi, double dt,
+                                  const cg_bc* bc, int nsteps, void* tape, size_t tape_bytes);
+/* The reverse sweep over a tape of cg_diffusion_run_taped: on entry lam holds dJ/dC^N at the
+ * interior cells, on return dJ/dC^0 there (the ghost cells' dependence folded in); dJ (host, may
+ * be NULL) gains dJ/dchi in dJ[0]. lam and work have C's layout (work is overwritten); chi, dt
+ * and the boundary kinds must be the taped run's (the tape's header is checked). Per step the
+ * reverse kernel applies the transposed stencil in gather form and adds lam (C^{n+1} - C^n) to a
+ * per-cell FP64 sum; the sums are added once, in a fixed order, at the end (dJ/dchi is
+ * reproducible bit for bit). The call synchronises the stream. */
+CG_API int cg_diffusion_adjoint_run(cg_ctx* ctx, const cg_grid* grid, const void* tape, size_t tape_bytes,
+                                    const cg_field* lam, const cg_field* work, double chi, double dt, const cg_bc* bc,
+                                    double* dJ);
+
 /* ---- viscoelastic Stokes (examples/stokes_{2,3}d_inc_ve_T.jl) ---------------------- */
 
 /* Field set of the VE Stokes examples. Tensor order: 2D (xx, yy, xy); 3D (xx, yy, zz,
@@ -351,6 +377,24 @@ CG_API int cg_stokes_gradient_log_eta(cg_ctx* ctx, const cg_grid* grid, const cg
  * values equal a CPU evaluation of the two kernels with -ffp-contract=off. */
 CG_API int cg_stokes_thermal_step(cg_ctx* ctx, const cg_grid* grid, const cg_stokes_fields* f,
                            const cg_stokes_params* p, const cg_bc* bc_T, const cg_field* T_out);
+
+/* Vector-Jacobian product of the fused thermal step (cg_stokes_thermal_step with bc_T), the
+ * transposed stencil of update_thermal_flux! + update_thermal! (no reference counterpart: the
+ * reference has no adjoint). For a misfit J of T_out at the interior cells, with mu = dJ/dT_out
+ * there, it writes
+ *   gT      dJ/dT at the interior cells; T's ghost cells are the bc_T rules' functions of the
+ *           interior (T came from a step that ended with bc!(T)), and their terms are folded in
+ *           (every side of bc_T must carry a Dirichlet, Neumann or Periodic rule);
+ *   gT_old  dJ/dT_old = mu at the interior cells (may be NULL);
+ *   gV[d]   dJ/dV.d at the faces an interior cell reads (normal index 1..n+1, tangential 1..n),
+ *           with the upwind branches the forward took (max(V, 0) and min(V, 0) both follow V at
+ *           V = 0, as the kernel's comparisons do);
+ * and dJ (host, may be NULL) gains dJ/dlambda_rhoCp in dJ[0] (summed per cell in FP64, then in a
+ * fixed order; the call then synchronises the stream). f supplies T and V at the step's input;
+ * p supplies lambda_rhoCp and dt. */
+CG_API int cg_stokes_thermal_step_adjoint(cg_ctx* ctx, const cg_grid* grid, const cg_stokes_fields* f,
+                                          const cg_stokes_params* p, const cg_bc* bc_T, const cg_field* mu,
+                                          const cg_field* gT, const cg_field* gT_old, const cg_field* gV, double* dJ);
 
 /* `niter` PT iterations with thermal coupling: update_stress!, update_velocity!, bc!(V), the
  * thermal step and bc!(T), as one graph. T alternates with a library-owned partner buffer and

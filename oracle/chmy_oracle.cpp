@@ -1170,6 +1170,129 @@ int or_sia_run_tangent(const cg_grid* grid, const cg_field* H, const cg_field* B
     return CG_OK;
 }
 
+/* The explicit diffusion loop of examples/diffusion_2d.jl:43-47 (compute_q!, update_C!, then
+   bc!(C => bc)) in dual numbers, restated from the flux form of :8-19: tangent 0 along chi,
+   tangent 1 along the initial-state direction `dir` (FP64, C's layout, read at every padded
+   point; bc!(C) is applied once before the loop, so the ghost cells' tangents follow the
+   interior's). C (FP64) advances `nsteps` steps in place; q (ndim FP64 face fields) is the loop's
+   flux storage (the update reads its index n+2, which compute_q! never writes: keep it zero).
+   dC[k] (FP64, C's layout) receive the exact derivatives of the final C along the two tangents. */
+int or_diffusion_run_tangent(const cg_grid* grid, const cg_field* C, const cg_field* q, double chi, double dt,
+                             const cg_bc* bc, int nsteps, const cg_field* dir, const cg_field* dC) {
+    const int nd = grid->ndim;
+    if (C->dtype != CG_F64 || dir->dtype != CG_F64) return CG_ERR_ARG;
+    auto span_of = [](const cg_field& a) {
+        long span = 1;
+        for (int d = 0; d < a.ndim; ++d) span += (long)(a.n[d] + 4 * a.halo[d] - 1) * a.stride[d];
+        return span;
+    };
+    std::vector<Dual> cs, qs[3];
+    const cg_field Cd = like_field(*C, cs);
+    cg_field Qd[3];
+    for (int d = 0; d < nd; ++d) {
+        if (!q[d].data || q[d].dtype != CG_F64) return CG_ERR_ARG;
+        Qd[d] = like_field(q[d], qs[d]);
+        const double* src = static_cast<const double*>(q[d].data);
+        for (long e = 0; e < span_of(q[d]); ++e) qs[d][e] = Dual(src[e]);
+    }
+    {
+        const double* c0 = static_cast<const double*>(C->data);
+        const double* w = static_cast<const double*>(dir->data);
+        for (long e = 0; e < span_of(*C); ++e) {
+            cs[e] = Dual(c0[e]);
+            cs[e].d[1] = w[e];
+        }
+    }
+    bc_apply_t<Dual>(grid, 1, &Cd, bc);
+    GridT<Dual> g(*grid);
+    Fd<Dual> c(Cd);
+    Fd<Dual> Q[3];
+    for (int d = 0; d < nd; ++d) Q[d] = Fd<Dual>(Qd[d]);
+    Dual chiD(chi);
+    chiD.d[0] = 1.0;
+    const Dual mchi = -chiD, Dt(dt);
+    for (int step = 0; step < nsteps; ++step) {
+        launch_range(g, [&](int i, int j, int k) {
+            for (int d = 0; d < nd; ++d) Q[d](i, j, k) = mchi * partial(c, g, d, i, j, k);
+        });
+        launch_range(g, [&](int i, int j, int k) { c(i, j, k) = c(i, j, k) - Dt * divg(Q, g, i, j, k); });
+        bc_apply_t<Dual>(grid, 1, &Cd, bc);
+    }
+    double* cv = static_cast<double*>(C->data);
+    for (long e = 0; e < span_of(*C); ++e) cv[e] = cs[e].v;
+    for (int k = 0; k < 2; ++k) {
+        double* o = static_cast<double*>(dC[k].data);
+        for (long e = 0; e < span_of(*C); ++e) o[e] = cs[e].d[k];
+    }
+    return CG_OK;
+}
+
+/* One thermal step of examples/stokes_2d_inc_ve_T.jl:45-60 (update_thermal_flux!,
+   update_thermal!, then bc!(T => bc_T)) in dual numbers: tangent 0 along the directions dT,
+   dT_old and dV[d] (FP64, in the layouts of T, T_old and V[d], read at every padded point; bc!(T)
+   is applied to T first, so its ghost cells' tangents follow the interior), tangent 1 along
+   lambda_rhoCp. f holds FP64 host fields T (the step's input; receives T_out), T_old, V and qT
+   (flux storage, zero at the face index n+2 the flux kernel never writes). dTout[k] (FP64, T's
+   layout) receive the tangents of T_out. */
+int or_thermal_step_tangent(const cg_grid* grid, const cg_stokes_fields* f, const cg_stokes_params* p,
+                            const cg_bc* bc_T, const cg_field* dT, const cg_field* dTold, const cg_field* dV,
+                            const cg_field* dTout) {
+    const int nd = grid->ndim;
+    auto span_of = [](const cg_field& a) {
+        long span = 1;
+        for (int d = 0; d < a.ndim; ++d) span += (long)(a.n[d] + 4 * a.halo[d] - 1) * a.stride[d];
+        return span;
+    };
+    std::vector<std::vector<Dual>> store;
+    store.reserve(16);
+    auto dualize = [&](const cg_field& src, const cg_field* dir) {
+        store.emplace_back();
+        cg_field dst = like_field(src, store.back());
+        const double* s = static_cast<const double*>(src.data);
+        const double* w = dir ? static_cast<const double*>(dir->data) : nullptr;
+        Dual* t = store.back().data();
+        for (long q = 0; q < span_of(src); ++q) {
+            t[q] = Dual(s[q]);
+            if (w) t[q].d[0] = w[q];
+        }
+        return dst;
+    };
+    if (f->T.dtype != CG_F64) return CG_ERR_ARG;
+    const cg_field Td = dualize(f->T, dT), Tod = dualize(f->T_old, dTold);
+    cg_field Vd[3], Qd[3];
+    for (int d = 0; d < nd; ++d) {
+        Vd[d] = dualize(f->V[d], &dV[d]);
+        Qd[d] = dualize(f->qT[d], nullptr);
+    }
+    bc_apply_t<Dual>(grid, 1, &Td, bc_T);
+    GridT<Dual> g(*grid);
+    Fd<Dual> Tt(Td), To(Tod), V[3], qT[3];
+    for (int d = 0; d < nd; ++d) {
+        V[d] = Fd<Dual>(Vd[d]);
+        qT[d] = Fd<Dual>(Qd[d]);
+    }
+    Dual lam(p->lambda_rhoCp);
+    lam.d[1] = 1.0;
+    const Dual dt(p->dt), zero(0.0);
+    launch_range(g, [&](int i, int j, int k) {
+        for (int d = 0; d < nd; ++d) {
+            const Dual v = V[d](i, j, k);
+            qT[d](i, j, k) = -lam * partial(Tt, g, d, i, j, k) + std::max(v, zero) * left(Tt, d, i, j, k) +
+                             std::min(v, zero) * right(Tt, d, i, j, k);
+        }
+    });
+    launch_range(g, [&](int i, int j, int k) { Tt(i, j, k) = To(i, j, k) - dt * divg(qT, g, i, j, k); });
+    bc_apply_t<Dual>(grid, 1, &Td, bc_T);
+    const Dual* tv = static_cast<const Dual*>(Td.data);
+    double* out = static_cast<double*>(f->T.data);
+    for (long q = 0; q < span_of(f->T); ++q) out[q] = tv[q].v;
+    for (int k = 0; k < 2; ++k) {
+        double* o = static_cast<double*>(dTout[k].data);
+        for (long q = 0; q < span_of(f->T); ++q) o[q] = tv[q].d[k];
+    }
+    return CG_OK;
+}
+
 int or_diffusion_compute_q(const cg_grid* grid, const cg_field* q, const cg_field* C, double chi) {
     if (C->dtype == CG_F64) diffusion_compute_q_t<double>(grid, q, C, chi);
     else diffusion_compute_q_t<float>(grid, q, C, chi);

@@ -35,6 +35,10 @@ _SIGS = {
                                  P(_abi.cg_field), C.c_double, C.c_int, C.c_int, P(_abi.cg_field), P(C.c_int)], C.c_int),
     "or_ptdiff_run_tangent": ([P(_abi.cg_grid), P(_abi.cg_ptdiff_fields), P(_abi.cg_ptdiff_params), P(_abi.cg_bc), C.c_int, C.c_int,
                                P(_abi.cg_field), P(_abi.cg_field)], C.c_int),
+    "or_diffusion_run_tangent": ([P(_abi.cg_grid), P(_abi.cg_field), P(_abi.cg_field), C.c_double, C.c_double, P(_abi.cg_bc), C.c_int,
+                                  P(_abi.cg_field), P(_abi.cg_field)], C.c_int),
+    "or_thermal_step_tangent": ([P(_abi.cg_grid), P(_abi.cg_stokes_fields), P(_abi.cg_stokes_params), P(_abi.cg_bc), P(_abi.cg_field),
+                                 P(_abi.cg_field), P(_abi.cg_field), P(_abi.cg_field)], C.c_int),
     "or_diffusion_compute_q_masked": ([P(_abi.cg_grid), P(_abi.cg_field), P(_abi.cg_field), C.c_double, P(_abi.cg_mask)], C.c_int),
     "or_diffusion_update_C_masked": ([P(_abi.cg_grid), P(_abi.cg_field), P(_abi.cg_field), C.c_double, P(_abi.cg_mask)], C.c_int),
     "or_stokes_update_old": ([P(_abi.cg_grid), P(_abi.cg_stokes_fields)], C.c_int),
@@ -276,3 +280,115 @@ def ptdiff_tangent_run(grid, D, C0, params, bc, nsteps, npt, dirs):
                                      desc_array(dfields), desc_array(dC))
     assert rc == 0, rc
     return Cf.a.copy(), [d.a.copy() for d in dC]
+
+
+def diffusion_tangent_run(grid, C0, chi, dt, bc, nsteps, direction):
+    """or_diffusion_run_tangent from C0 (FP64 padded host array; bc! is applied first): the
+    explicit diffusion loop's final state and its derivatives along chi and along the
+    initial-state direction `direction` (a padded host array). Returns (C^N, dC^N/dchi,
+    dC^N/d direction)."""
+    nd = grid.ndim
+    Cl, Vl = Center(), Vertex()
+    Cf = NpField(grid, Cl, np.float64)
+    Cf.a[...] = C0
+    w = NpField(grid, Cl, np.float64)
+    w.a[...] = direction
+    q = [NpField(grid, tuple(Vl if e == d else Cl for e in range(nd)), np.float64) for d in range(nd)]
+    dC = [NpField(grid, Cl, np.float64), NpField(grid, Cl, np.float64)]
+    rc = lib().or_diffusion_run_tangent(C.byref(grid.desc()), C.byref(Cf.desc()), desc_array(q, 3), float(chi), float(dt),
+                                        C.byref(bc), int(nsteps), C.byref(w.desc()), desc_array(dC))
+    assert rc == 0, rc
+    return Cf.a.copy(), dC[0].a.copy(), dC[1].a.copy()
+
+
+def diffusion_run(grid, C0, chi, dt, bc, nsteps):
+    """The oracle's explicit diffusion loop (compute_q!, update_C!, bc!) from bc!(C0): C^N."""
+    nd = grid.ndim
+    Cl, Vl = Center(), Vertex()
+    Cf = NpField(grid, Cl, np.float64)
+    Cf.a[...] = C0
+    q = [NpField(grid, tuple(Vl if e == d else Cl for e in range(nd)), np.float64) for d in range(nd)]
+    g = grid.desc()
+    bc_apply(grid, [Cf], [bc])
+    for _ in range(nsteps):
+        assert lib().or_diffusion_compute_q(C.byref(g), desc_array(q, 3), C.byref(Cf.desc()), float(chi)) == 0
+        assert lib().or_diffusion_update_C(C.byref(g), C.byref(Cf.desc()), desc_array(q, 3), float(dt)) == 0
+        bc_apply(grid, [Cf], [bc])
+    return Cf.a.copy()
+
+
+def thermal_problem(grid, seed, bc_T):
+    """Host fields of one thermal step: T (random, bc_T applied), T_old, V (random at every face),
+    zero flux storage qT, and random tangent directions of T (interior), T_old (interior) and V
+    (every face). Returns a dict of NpFields and direction arrays."""
+    nd = grid.ndim
+    Cl, Vl = Center(), Vertex()
+    rng = np.random.default_rng(seed)
+    vlocs = [tuple(Vl if e == d else Cl for e in range(nd)) for d in range(nd)]
+    Tf = NpField(grid, Cl, np.float64)
+    Tf.a[...] = 1.0 + rng.standard_normal(Tf.a.shape)
+    bc_apply(grid, [Tf], [bc_T])
+    To = NpField(grid, Cl, np.float64)
+    To.a[...] = rng.standard_normal(To.a.shape)
+    V = [NpField(grid, l, np.float64) for l in vlocs]
+    for v in V:
+        v.a[...] = rng.standard_normal(v.a.shape)
+    inner = (slice(2, -2),) * nd
+    dT = np.zeros_like(Tf.a)
+    dT[inner] = rng.standard_normal(dT[inner].shape)
+    dTo = np.zeros_like(To.a)
+    dTo[inner] = rng.standard_normal(dTo[inner].shape)
+    dV = [rng.standard_normal(v.a.shape) for v in V]
+    mu = np.zeros_like(Tf.a)
+    mu[inner] = rng.standard_normal(mu[inner].shape)
+    return {"T": Tf, "T_old": To, "V": V, "vlocs": vlocs, "dT": dT, "dT_old": dTo, "dV": dV, "mu": mu, "inner": inner}
+
+
+def thermal_tangent_step(grid, pr, params, bc_T):
+    """or_thermal_step_tangent on copies of a thermal_problem: (T_out, [dT_out along the
+    directions, dT_out / d lambda_rhoCp])."""
+    nd = grid.ndim
+    T = pr["T"].copy()
+    To = pr["T_old"].copy()
+    V = [v.copy() for v in pr["V"]]
+    qT = [NpField(grid, l, np.float64) for l in pr["vlocs"]]
+    s = stokes_desc(V=V, T=T, T_old=To, qT=qT)
+
+    def nf(arr, loc):
+        f = NpField(grid, loc, np.float64)
+        f.a[...] = arr
+        return f
+
+    dT = nf(pr["dT"], Center())
+    dTo = nf(pr["dT_old"], Center())
+    dV = [nf(a, l) for a, l in zip(pr["dV"], pr["vlocs"])]
+    out = [NpField(grid, Center(), np.float64), NpField(grid, Center(), np.float64)]
+    rc = lib().or_thermal_step_tangent(C.byref(grid.desc()), C.byref(s), C.byref(params), C.byref(bc_T), C.byref(dT.desc()),
+                                       C.byref(dTo.desc()), desc_array(dV, 3), desc_array(out))
+    assert rc == 0, rc
+    return T.a.copy(), [out[0].a.copy(), out[1].a.copy()]
+
+
+def thermal_step(grid, T0, T_old, V, params, bc_T):
+    """The oracle's plain thermal step (update_thermal_flux!, update_thermal!, bc!(T)) on host
+    arrays: T_out."""
+    nd = grid.ndim
+    Cl, Vl = Center(), Vertex()
+    vlocs = [tuple(Vl if e == d else Cl for e in range(nd)) for d in range(nd)]
+
+    def nf(arr, loc):
+        f = NpField(grid, loc, np.float64)
+        f.a[...] = arr
+        return f
+
+    T = nf(T0, Cl)
+    To = nf(T_old, Cl)
+    Vf = [nf(a, l) for a, l in zip(V, vlocs)]
+    qT = [NpField(grid, l, np.float64) for l in vlocs]
+    s = stokes_desc(V=Vf, T=T, T_old=To, qT=qT)
+    g = grid.desc()
+    bc_apply(grid, [T], [bc_T])
+    assert lib().or_stokes_update_thermal_flux(C.byref(g), C.byref(s), C.byref(params)) == 0
+    assert lib().or_stokes_update_thermal(C.byref(g), C.byref(s), C.byref(params)) == 0
+    bc_apply(grid, [T], [bc_T])
+    return T.a.copy()

@@ -555,3 +555,179 @@ def test_sia_ensemble_adjoint_run_argument_errors(arch):
     assert call(nbytes=n // 2) == _abi.CG_ERR_ARG
     dJ = (ctypes.c_double * (2 * ens.nm))()
     arch.call("cg_sia_ensemble_adjoint_run", ens.nm, ens._mem, ens._par, tp, n, ens._lam, ens._work, dJ)
+
+
+def _explicit_setup(nd, kinds, seed=7):
+    from chmy_gb300.bcs import Dirichlet, Neumann, Periodic, to_cg_bc
+    from chmy_gb300.configs import padded_mesh
+    from chmy_gb300.grids import Center, UniformGrid
+
+    T = np.float64
+    dims = (20, 16) if nd == 2 else (12, 10, 9)
+    grid = UniformGrid(origin=(T(-1),) * nd, extent=(T(2),) * nd, dims=dims, dtype=T)
+    xs = padded_mesh(grid, Center())
+    r2 = sum(x * x for x in xs)
+    rng = np.random.default_rng(seed)
+    C0 = np.exp(-r2 / 0.1) + 0.01 * rng.standard_normal(xs[0].shape)
+    if kinds == "neumann_dirichlet":
+        spec = {"x": Neumann(0.3), "y": Dirichlet(0.2)}
+    else:
+        spec = {"x": Periodic(), "y": Neumann()}
+    if nd == 3:
+        spec["z"] = (Dirichlet(0.1), Neumann())
+    bc = to_cg_bc(nd, spec)
+    h = float(min(grid.spacing()))
+    dt = h * h / (2.05 * nd)
+    inner = (slice(2, -2),) * nd
+    w = np.zeros_like(C0)
+    w[inner] = rng.standard_normal(w[inner].shape)
+    dirv = np.zeros_like(C0)
+    dirv[inner] = rng.standard_normal(dirv[inner].shape)
+    return grid, C0, bc, dt, inner, w, dirv
+
+
+@pytest.mark.parametrize("nd,kinds", [(2, "neumann_dirichlet"), (2, "periodic"), (3, "neumann_dirichlet")])
+def test_explicit_diffusion_gradient_matches_dual_numbers_and_differences(arch, nd, kinds):
+    """The explicit diffusion loop's adjoint (taped forward, one reverse sweep) for
+    J = 1/2 sum w C^N^2 over the interior: dJ/dchi and the directional derivative of J along an
+    initial-state direction agree with the dual-number tangents of the oracle's loop to 1e-9, and
+    with central differences of the GPU's own forward runs to 1e-6. Segments of 7 steps give the
+    same dJ/dC0 bits, and dJ/dchi to 1e-13."""
+    from _oracle import diffusion_tangent_run
+
+    from chmy_gb300.adjoint import ExplicitDiffusion
+
+    grid, C0, bc, dt, inner, w, dirv = _explicit_setup(nd, kinds)
+    chi, nsteps = 1.0, 30
+    ed = ExplicitDiffusion(arch, grid, chi, dt, bc)
+
+    def J(c):
+        return 0.5 * float(np.sum(w[inner] * c[inner] ** 2))
+
+    gchi, gC0, CN = ed.gradient(C0, nsteps, lambda c: w * c)
+    CN_ref, dchi, ddir = diffusion_tangent_run(grid, C0, chi, dt, bc, nsteps, dirv)
+    assert np.max(np.abs(CN - CN_ref)) <= 1e-12 * nsteps * np.abs(CN_ref).max()
+    dual_chi = float(np.sum(w[inner] * CN_ref[inner] * dchi[inner]))
+    dual_dir = float(np.sum(w[inner] * CN_ref[inner] * ddir[inner]))
+    adj_dir = float(np.sum(gC0[inner] * dirv[inner]))
+    assert abs(gchi - dual_chi) <= 1e-9 * abs(dual_chi), (gchi, dual_chi)
+    assert abs(adj_dir - dual_dir) <= 1e-9 * abs(dual_dir), (adj_dir, dual_dir)
+    e = 1e-6
+    fd_chi = (J(ExplicitDiffusion(arch, grid, chi + e, dt, bc).run(C0, nsteps))
+              - J(ExplicitDiffusion(arch, grid, chi - e, dt, bc).run(C0, nsteps))) / (2 * e)
+    assert abs(gchi - fd_chi) <= 1e-6 * abs(fd_chi), (gchi, fd_chi)
+    cell = tuple(s.start + 3 for s in inner)
+    bump = np.zeros_like(C0)
+    bump[cell] = 1.0
+    fd_cell = (J(ed.run(C0 + e * bump, nsteps)) - J(ed.run(C0 - e * bump, nsteps))) / (2 * e)
+    assert abs(gC0[cell] - fd_cell) <= 1e-6 * np.abs(gC0[inner]).max(), (gC0[cell], fd_cell)
+    gchi7, gC07, _ = ed.gradient(C0, nsteps, lambda c: w * c, checkpoint_every=7)
+    np.testing.assert_array_equal(gC07[inner], gC0[inner])
+    assert abs(gchi7 - gchi) <= 1e-13 * abs(gchi)
+
+
+def test_explicit_diffusion_adjoint_checks_the_tape(arch):
+    """The reverse sweep refuses a tape whose header does not match its arguments (another chi,
+    another boundary kind), and a boundary side without a rule."""
+    import ctypes as C
+
+    import torch
+
+    from chmy_gb300.adjoint import ExplicitDiffusion
+    from chmy_gb300.bcs import Neumann, to_cg_bc
+
+    grid, C0, bc, dt, inner, w, dirv = _explicit_setup(2, "neumann_dirichlet")
+    ed = ExplicitDiffusion(arch, grid, 1.0, dt, bc)
+    ed.C.from_numpy(C0)
+    nb = ed.tape_bytes(4)
+    tape = torch.empty(nb, dtype=torch.uint8, device=ed.C.data.device)
+    g = grid.desc()
+    arch.call("cg_diffusion_run_taped", C.byref(g), C.byref(ed.C.desc()), 1.0, dt, C.byref(bc), 4, C.c_void_p(tape.data_ptr()), nb)
+    dJ = (C.c_double * 1)()
+    args = (C.byref(g), C.c_void_p(tape.data_ptr()), nb, C.byref(ed.lam[0].desc()), C.byref(ed.lam[1].desc()))
+    assert arch.lib.cg_diffusion_adjoint_run(arch.ctx, *args, 1.5, dt, C.byref(bc), dJ) == _abi.CG_ERR_ARG
+    other = to_cg_bc(2, Neumann())
+    assert arch.lib.cg_diffusion_adjoint_run(arch.ctx, *args, 1.0, dt, C.byref(other), dJ) == _abi.CG_ERR_ARG
+    assert arch.lib.cg_diffusion_adjoint_run(arch.ctx, *args, 1.0, dt, C.byref(bc), dJ) == _abi.CG_OK
+    none = to_cg_bc(2, {"x": Neumann()})
+    assert arch.lib.cg_diffusion_adjoint_run(arch.ctx, *args, 1.0, dt, C.byref(none), dJ) == _abi.CG_ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("nd,kinds", [(2, "neumann_dirichlet"), (2, "periodic"), (3, "neumann_dirichlet")])
+def test_thermal_step_adjoint_matches_dual_numbers(arch, nd, kinds):
+    """The fused thermal step's vector-Jacobian product (cg_stokes_thermal_step_adjoint) against
+    the dual-number tangents of the oracle's two-kernel step: for J = sum mu T_out over the
+    interior, <dJ/dT, dT> + <dJ/dT_old, dT_old> + <dJ/dV, dV> equals the tangent along those
+    directions, and dJ/dlambda the tangent along lambda_rhoCp, to 1e-11 (FP64); the FP32 kernel's
+    gradients agree with the FP64 ones to 1e-4. dJ/dlambda also matches central differences of the
+    GPU's forward step."""
+    import ctypes as C
+
+    from _oracle import thermal_problem, thermal_tangent_step
+    from chmy_gb300.bcs import Dirichlet, Neumann, Periodic, to_cg_bc
+    from chmy_gb300.grids import Center, UniformGrid
+    from chmy_gb300.kernels import stokes_fields, stokes_params
+    from gpu_helpers import to_gpu
+
+    T = np.float64
+    dims = (18, 14) if nd == 2 else (11, 9, 8)
+    grid = UniformGrid(origin=(T(-1),) * nd, extent=(T(2),) * nd, dims=dims, dtype=T)
+    spec = {"x": Neumann(0.2), "y": Dirichlet(0.5)} if kinds == "neumann_dirichlet" else {"x": Periodic(), "y": Neumann()}
+    if nd == 3:
+        spec["z"] = (Neumann(), Dirichlet(-0.1))
+    bc_T = to_cg_bc(nd, spec)
+    pr = thermal_problem(grid, 11, bc_T)
+    p = stokes_params(G=1.0, dt=2e-3, lambda_rhoCp=0.3)
+    _, tan = thermal_tangent_step(grid, pr, p, bc_T)
+    inner, mu = pr["inner"], pr["mu"]
+
+    def adjoint(dtype):
+        def dev(arr, loc):
+            from _oracle import NpField
+
+            f = NpField(grid, loc, dtype)
+            f.a[...] = arr.astype(dtype)
+            return to_gpu(arch, f)
+
+        Tg = dev(pr["T"].a, Center())
+        Vg = [dev(v.a, l) for v, l in zip(pr["V"], pr["vlocs"])]
+        mug = dev(mu, Center())
+        gT = dev(np.zeros_like(mu), Center())
+        gTo = dev(np.zeros_like(mu), Center())
+        gV = [dev(np.zeros_like(v.a), l) for v, l in zip(pr["V"], pr["vlocs"])]
+        f = stokes_fields(V=Vg, T=Tg)
+        dl = (C.c_double * 1)(0.0)
+        arch.call("cg_stokes_thermal_step_adjoint", C.byref(grid.desc()), C.byref(f), C.byref(p), C.byref(bc_T),
+                  C.byref(mug.desc()), C.byref(gT.desc()), C.byref(gTo.desc()), (_abi.cg_field * 3)(*[g.desc() for g in gV]), dl)
+        return gT.to_numpy(), gTo.to_numpy(), [g.to_numpy() for g in gV], dl[0]
+
+    gT, gTo, gV, dlam = adjoint(np.float64)
+    lhs = float(np.sum(gT[inner] * pr["dT"][inner]) + np.sum(gTo[inner] * pr["dT_old"][inner])
+                + sum(np.sum(g * d) for g, d in zip(gV, pr["dV"])))
+    dual_dir = float(np.sum(mu[inner] * tan[0][inner]))
+    dual_lam = float(np.sum(mu[inner] * tan[1][inner]))
+    assert abs(lhs - dual_dir) <= 1e-11 * abs(dual_dir), (lhs, dual_dir)
+    assert abs(dlam - dual_lam) <= 1e-11 * abs(dual_lam), (dlam, dual_lam)
+    np.testing.assert_array_equal(gTo[inner], mu[inner])
+    # FP32 kernel
+    gT32, _, gV32, dlam32 = adjoint(np.float32)
+    assert np.max(np.abs(gT32[inner] - gT[inner])) <= 1e-4 * np.abs(gT[inner]).max()
+    for a, b in zip(gV32, gV):
+        assert np.max(np.abs(a - b)) <= 1e-4 * np.abs(b).max()
+    assert abs(dlam32 - dlam) <= 1e-4 * abs(dlam)
+    # central differences of the GPU's forward step in lambda_rhoCp
+    from _oracle import NpField
+
+    def J(lam):
+        q = stokes_params(G=1.0, dt=2e-3, lambda_rhoCp=lam)
+        Tg = to_gpu(arch, pr["T"])
+        Tog = to_gpu(arch, pr["T_old"])
+        Vg = [to_gpu(arch, v) for v in pr["V"]]
+        out = to_gpu(arch, NpField(grid, Center(), np.float64))
+        arch.call("cg_stokes_thermal_step", C.byref(grid.desc()), C.byref(stokes_fields(V=Vg, T=Tg, T_old=Tog)), C.byref(q),
+                  C.byref(bc_T), C.byref(out.desc()))
+        return float(np.sum(mu[inner] * out.to_numpy()[inner]))
+
+    e = 1e-6
+    fd = (J(0.3 + e) - J(0.3 - e)) / (2 * e)
+    assert abs(dlam - fd) <= 1e-6 * abs(fd), (dlam, fd)
