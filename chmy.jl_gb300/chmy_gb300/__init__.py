@@ -12,6 +12,7 @@ from ._abi import ChmyError, header_symbols, load_library
 from .architecture import Arch, GB300Backend, get_backend, get_device, heuristic_groupsize
 from .bcs import Batch, Dirichlet, Neumann, Periodic, batch, bc_
 from .fields import Field, FieldMask, TensorField, VectorField, gather, gather_blocks, interior, set_
+from .functions import FunctionField
 from .grids import Center, Dim, Side, UniformGrid, Vertex, flip
 from .kernels import (
     CellViscosity,
@@ -56,6 +57,7 @@ __all__ = [
     "interior",
     "gather",
     "FieldMask",
+    "FunctionField",
     "gather_blocks",
     "load_library",
     "set_",

@@ -15,7 +15,7 @@ PKG_DIR = Path(__file__).resolve().parent
 LIB_PATH = PKG_DIR / "lib" / "libchmy_gb300.so"
 HEADER = PKG_DIR.parent.parent / "include" / "chmy_gb300.h"
 
-ABI_VERSION = 2
+ABI_VERSION = 3
 
 # status codes
 CG_OK = 0
@@ -95,6 +95,13 @@ class cg_stokes_fields(C.Structure):
     ]
 
 
+CG_FN_NONE, CG_FN_CONST, CG_FN_BALL, CG_FN_AFFINE = 0, 1, 2, 3
+
+
+class cg_function(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("pad_", C.c_int32), ("p", C.c_double * 8)]
+
+
 class cg_stokes_params(C.Structure):
     _fields_ = [
         ("eta", C.c_double),
@@ -105,6 +112,7 @@ class cg_stokes_params(C.Structure):
         ("dtau_r", C.c_double),
         ("nu_dtau", C.c_double),
         ("lambda_rhoCp", C.c_double),
+        ("rho_g_fn", cg_function * 3),
     ]
 
 
@@ -188,6 +196,7 @@ SIGNATURES: dict[str, list] = {
     "cg_diffusion_run_taped": [_vp, P(cg_grid), P(cg_field), C.c_double, C.c_double, P(cg_bc), C.c_int, _vp, C.c_size_t],
     "cg_diffusion_adjoint_run": [_vp, P(cg_grid), _vp, C.c_size_t, P(cg_field), P(cg_field), C.c_double, C.c_double, P(cg_bc),
                                  P(C.c_double)],
+    "cg_function_fill": [_vp, P(cg_grid), P(cg_function), P(cg_field)],
     "cg_stokes_update_old": [_vp, P(cg_grid), P(cg_stokes_fields)],
     "cg_stokes_update_stress": [_vp, P(cg_grid), P(cg_stokes_fields), P(cg_stokes_params)],
     "cg_stokes_update_velocity": [_vp, P(cg_grid), P(cg_stokes_fields), P(cg_stokes_params)],

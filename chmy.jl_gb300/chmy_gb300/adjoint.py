@@ -158,7 +158,8 @@ class ExplicitDiffusion:
 
         if self._tape is None or self._tape.numel() < nbytes:
             self._tape = None
-            self._tape = torch.empty(nbytes, dtype=torch.uint8, device=self.C.data.device)
+            # zeroed: the states' outer halo layer, which no step writes, then holds zeros
+            self._tape = torch.zeros(nbytes, dtype=torch.uint8, device=self.C.data.device)
             if self._tape.data_ptr() % 256:
                 raise RuntimeError("the tape allocation is not 256-byte aligned")
         return self._tape
@@ -170,6 +171,7 @@ class ExplicitDiffusion:
         """`nsteps` plain steps of C in place (ping-pong with B)."""
         if nsteps <= 0:
             return
+        self.B.data.copy_(self.C.data)  # the partner's outer halo (never written) matches C's
         self.arch.call("cg_diffusion_run", ctypes.byref(self.grid.desc()), ctypes.byref(self.C.desc()), ctypes.byref(self.B.desc()),
                        self.chi, self.dt, ctypes.byref(self.bc), int(nsteps))
         if nsteps % 2:

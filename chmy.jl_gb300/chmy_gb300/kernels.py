@@ -140,20 +140,30 @@ class _UpdateStress(Kernel):
 
 class _UpdateVelocity(Kernel):
     """update_velocity!(V, r_V, Pr, τ, ρg, η_ve, νdτ, g) (examples/stokes_2d_inc_ve_T.jl:36-43;
-    3D :48-57). `ρg` is the body force of the last component (ρgy in 2D, ρgz in 3D) or None."""
+    3D :48-57). `ρg` is the body force of the last component (ρgy in 2D, ρgz in 3D): a Field, a
+    FunctionField of a device form (evaluated in the kernel, as the example's
+    FunctionField(init_incl, ...) of :107), or None."""
 
     name = "update_velocity"
 
     def launch(self, arch, grid, V, r_V, Pr, tau, rho_g, eta_ve, nu_dtau, g=None):
+        from .functions import FunctionField
+
         nd = grid.ndim
         rho = [None] * 3
-        rho[nd - 1] = rho_g
+        fn = None
+        if isinstance(rho_g, FunctionField):
+            fn = rho_g.desc()  # evaluated by the kernel at every face (a device FunctionField)
+        else:
+            rho[nd - 1] = rho_g
         if isinstance(eta_ve, CellViscosity):
             s = stokes_fields(V=V, r_V=r_V, P=Pr, tau=tau, rho_g=rho, eta=eta_ve.eta)
             p = stokes_params(G=eta_ve.G, dt=eta_ve.dt, nu_dtau=nu_dtau)
         else:
             s = stokes_fields(V=V, r_V=r_V, P=Pr, tau=tau, rho_g=rho)
             p = stokes_params(eta_ve=eta_ve, nu_dtau=nu_dtau)
+        if fn is not None:
+            p.rho_g_fn[nd - 1] = fn
         arch.call("cg_stokes_update_velocity", ctypes.byref(grid.desc()), ctypes.byref(s), ctypes.byref(p))
 
 

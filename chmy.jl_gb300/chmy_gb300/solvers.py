@@ -15,6 +15,7 @@ import numpy as np
 from . import _abi
 from .configs import StokesProblem
 from .fields import Field
+from .functions import FunctionField
 from .grids import Center, Vertex
 from .kernels import stokes_fields
 
@@ -39,10 +40,18 @@ class StokesSolver:
         g = problem.grid
         nd = g.ndim
         self.fields: dict = {}
+        # body forces given as device FunctionFields are evaluated by the kernels, not stored
+        self.params = _abi.cg_stokes_params()
+        ctypes.memmove(ctypes.byref(self.params), ctypes.byref(problem.params), ctypes.sizeof(self.params))
         for name, val in problem.host.items():
             if isinstance(val, list):
                 fs = []
                 for i, a in enumerate(val):
+                    if isinstance(a, FunctionField):
+                        if name != "rho_g":
+                            raise TypeError(f"{name}[{i}]: only body forces may be FunctionFields")
+                        self.params.rho_g_fn[i] = a.desc()
+                        a = None
                     if a is None:
                         fs.append(None)
                         continue
@@ -81,7 +90,7 @@ class StokesSolver:
             "cg_stokes_pt_iterations",
             ctypes.byref(self.grid_desc),
             ctypes.byref(self.desc),
-            ctypes.byref(self.pb.params),
+            ctypes.byref(self.params),
             self.bc_arr,
             int(niter),
         )
@@ -114,7 +123,7 @@ class StokesSolver:
             self.arch.ctx,
             ctypes.byref(self.grid_desc),
             ctypes.byref(self.desc),
-            ctypes.byref(self.pb.params),
+            ctypes.byref(self.params),
             self.bc_arr,
             ctypes.byref(o),
             ctypes.byref(res),
@@ -141,7 +150,7 @@ class StokesSolver:
             raise ValueError("gradient_log_eta: the problem needs a viscosity field")
         zero = {}
         for name, val in pb.host.items():
-            if name in ("eta", "T", "T_old", "qT"):
+            if name in ("eta", "T", "T_old", "qT", "rho_g"):
                 continue
             if isinstance(val, list):
                 zero[name] = [None if a is None else np.zeros_like(a) for a in val]
@@ -150,6 +159,11 @@ class StokesSolver:
         zero["eta"] = pb.host["eta"]
         ref = pb.host["V"]
         zero["rho_g"] = [None if a is None else -np.asarray(a, dtype=ref[d].dtype) for d, a in enumerate(list(dJdV) + [None] * (3 - len(dJdV)))][:nd]
+        # the adjoint's body force is -dJ/dV alone: the forward's body-force functions drop out
+        adj_params = _abi.cg_stokes_params()
+        ctypes.memmove(ctypes.byref(adj_params), ctypes.byref(self.params), ctypes.sizeof(adj_params))
+        for d in range(3):
+            adj_params.rho_g_fn[d] = _abi.cg_function()
         bcs = []
         for b in pb.bc_V:
             b0 = _abi.cg_bc()
@@ -158,7 +172,7 @@ class StokesSolver:
                 for side in range(2):
                     b0.value[d][side] = 0.0
             bcs.append(b0)
-        adj_pb = dataclasses.replace(pb, host=zero, bc_V=bcs, eps=float(eps if eps is not None else pb.eps))
+        adj_pb = dataclasses.replace(pb, host=zero, bc_V=bcs, eps=float(eps if eps is not None else pb.eps), params=adj_params)
         adj = StokesSolver(self.arch, adj_pb)
         adj.apply_bc()
         res = adj.solve(precision=precision, max_iter=max_iter)
@@ -169,7 +183,7 @@ class StokesSolver:
             ctypes.byref(self.grid_desc),
             ctypes.byref(self.desc),
             mu,
-            ctypes.byref(pb.params),
+            ctypes.byref(self.params),
             ctypes.byref(grad.desc()),
         )
         return grad, res

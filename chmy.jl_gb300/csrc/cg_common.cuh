@@ -56,6 +56,9 @@ bool cg_autotune_enabled();
 // CG_TUNE_VERBOSE=1: the autotuners print every candidate's time to stderr
 bool cg_tune_verbose();
 bool cg_tune_lookup(const std::string& key, cg_tune_cfg* out);
+// CG_MARCH_LAYOUT=<segment length>:<variant> in the environment: the layout to use instead of
+// the autotuner's (profiling of one layout); false when unset or malformed.
+bool cg_tune_forced(cg_tune_cfg* out);
 void cg_tune_store(const std::string& key, const cg_tune_cfg& cfg);
 
 // Programmatic dependent launch. A kernel launched by cg_launch(..., dep = true) may be

@@ -236,9 +236,12 @@ extern "C" int cg_diffusion_run_taped(cg_ctx* ctx, const cg_grid* grid, const cg
     cg_key_add(key, nsteps);
     cg_key_add(key, *bc);
     cg_key_add(key, tape);
+    // the last step writes the caller's field, which so keeps its own outer halo (the layer no
+    // step writes) as the in-place loop does; its result is then recorded as state nsteps
     rc = cg_graph_run(ctx, key, [&](cudaStream_t) {
         for (int s = 0; s < nsteps; ++s) {
-            const cg_field in = state_field(*C, tape, s), out = state_field(*C, tape, s + 1);
+            const cg_field in = state_field(*C, tape, s);
+            const cg_field out = s + 1 < nsteps ? state_field(*C, tape, s + 1) : *C;
             int r = cg_diffusion_step(ctx, grid, &out, &in, chi, dt, bc);
             if (r) return r;
         }
@@ -246,7 +249,7 @@ extern "C" int cg_diffusion_run_taped(cg_ctx* ctx, const cg_grid* grid, const cg
     });
     if (rc) return rc;
     const cg_field sN = state_field(*C, tape, nsteps);
-    CG_CUDA(ctx, cudaMemcpyAsync(C->data, sN.data, span, cudaMemcpyDeviceToDevice, ctx->stream));
+    CG_CUDA(ctx, cudaMemcpyAsync(sN.data, C->data, span, cudaMemcpyDeviceToDevice, ctx->stream));
     return CG_OK;
 }
 

@@ -66,6 +66,19 @@ int check_stokes(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f, int n
     return CG_OK;
 }
 
+// The body force of every velocity component: an array rho_g[d], a device FunctionField
+// p->rho_g_fn[d] of a known kind, or neither.
+int check_body(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f, const cg_stokes_params* p) {
+    for (int d = 0; d < 3; ++d) {
+        const int k = p->rho_g_fn[d].kind;
+        if (k < CG_FN_NONE || k > CG_FN_AFFINE) return cg_fail(ctx, CG_ERR_ARG, "rho_g_fn[%d]: unknown kind %d", d, k);
+        if (k != CG_FN_NONE && d >= g->ndim) return cg_fail(ctx, CG_ERR_ARG, "rho_g_fn[%d]: the grid has %d dims", d, g->ndim);
+        if (k != CG_FN_NONE && cg_present(f->rho_g[d]))
+            return cg_fail(ctx, CG_ERR_ARG, "rho_g[%d]: an array and a function were both given", d);
+    }
+    return CG_OK;
+}
+
 // Precomputed viscosity arrays of a solve (dense Center layout, halo 1, in the field type):
 // [inv_eta], eta_ve, and per shear component the interpolated 1/eta and its eta_ve.
 struct Pre {
@@ -343,6 +356,7 @@ extern "C" int cg_stokes_update_velocity(cg_ctx* ctx, const cg_grid* grid, const
     int rc = check_stokes(ctx, grid, f, NEED_V | NEED_TAU | NEED_P, &dtype);
     if (rc) return rc;
     if (!p) return cg_fail(ctx, CG_ERR_ARG, "update_velocity: params is NULL");
+    if ((rc = check_body(ctx, grid, f, p))) return rc;
     cudaSetDevice(ctx->device);
     return SDISPATCH(launch_velocity, dtype, grid->ndim, ctx, grid, f, p, true);
 }
@@ -374,6 +388,7 @@ extern "C" int cg_stokes_pt_iterations(cg_ctx* ctx, const cg_grid* grid, const c
     int rc = check_stokes(ctx, grid, f, NEED_V | NEED_TAU | NEED_TAU_OLD | NEED_P, &dtype);
     if (rc) return rc;
     if (!p) return cg_fail(ctx, CG_ERR_ARG, "pt_iterations: params is NULL");
+    if ((rc = check_body(ctx, grid, f, p))) return rc;
     if (niter < 0) return cg_fail(ctx, CG_ERR_ARG, "pt_iterations: niter < 0");
     if (niter == 0) return CG_OK;
     cudaSetDevice(ctx->device);
@@ -529,6 +544,9 @@ extern "C" int cg_stokes_pt_iterations_pp(cg_ctx* ctx, const cg_grid* grid, cons
     int rc = check_stokes(ctx, grid, a, NEED_V | NEED_TAU | NEED_TAU_OLD | NEED_P, &dtype);
     if (rc) return rc;
     if (!b || !p) return cg_fail(ctx, CG_ERR_ARG, "pt_iterations_pp: NULL argument");
+    for (int d = 0; d < 3; ++d)
+        if (p->rho_g_fn[d].kind != CG_FN_NONE)
+            return cg_fail(ctx, CG_ERR_UNSUPPORTED, "pt_iterations_pp: body forces are read from arrays (rho_g_fn[%d] set)", d);
     if (grid->ndim < 2) return cg_fail(ctx, CG_ERR_UNSUPPORTED, "pt_iterations_pp: 2D and 3D grids only");
     if (!cg_present(a->inv_eta)) return cg_fail(ctx, CG_ERR_ARG, "pt_iterations_pp: inv_eta is required");
     if (niter < 0 || (niter & 1)) return cg_fail(ctx, CG_ERR_ARG, "pt_iterations_pp: niter must be even and >= 0");
@@ -563,6 +581,7 @@ int check_solve(cg_ctx* ctx, const cg_grid* grid, const cg_stokes_fields* f, con
     int rc = check_stokes(ctx, grid, f, NEED_V | NEED_TAU | NEED_TAU_OLD | NEED_P, dtype);
     if (rc) return rc;
     if (!p || !o || !res) return cg_fail(ctx, CG_ERR_ARG, "stokes_solve: NULL argument");
+    if ((rc = check_body(ctx, grid, f, p))) return rc;
     if (o->ncheck < 1 || o->max_iter < 1) return cg_fail(ctx, CG_ERR_ARG, "stokes_solve: ncheck/max_iter < 1");
     if (!cg_present(f->divV) || !cg_present(f->r_V[0]))
         return cg_fail(ctx, CG_ERR_ARG, "stokes_solve: divV and r_V are required for the convergence check");
@@ -657,6 +676,7 @@ extern "C" int cg_stokes_pt_iterations_thermal(cg_ctx* ctx, const cg_grid* grid,
     int rc = check_stokes(ctx, grid, f, NEED_V | NEED_TAU | NEED_TAU_OLD | NEED_P, &dtype);
     if (rc) return rc;
     if (!p || !bc_T) return cg_fail(ctx, CG_ERR_ARG, "pt_iterations_thermal: NULL argument");
+    if ((rc = check_body(ctx, grid, f, p))) return rc;
     if ((rc = check_thermal(ctx, grid, f, dtype))) return rc;
     if (niter < 0) return cg_fail(ctx, CG_ERR_ARG, "pt_iterations_thermal: niter < 0");
     if (niter == 0) return CG_OK;

@@ -111,8 +111,11 @@ __global__ void defect_kernel(const SV<double> v, const SP<double> s, const DC32
         rz = rz + (tyz(i, j + 1, k) - tyz(i, j, k)) * s.idx[1];
     }
     if (v.has_rho[0]) rx = rx - v.rho[0](i, j, k);
+    else if (s.fn[0].kind) rx = rx - body_fn(s, 0, ND, i, j, k);
     if (v.has_rho[1]) ry = ry - v.rho[1](i, j, k);
+    else if (s.fn[1].kind) ry = ry - body_fn(s, 1, ND, i, j, k);
     if (ND > 2 && v.has_rho[2]) rz = rz - v.rho[2](i, j, k);
+    else if (ND > 2 && s.fn[2].kind) rz = rz - body_fn(s, 2, ND, i, j, k);
     v.rV[0](i, j, k) = rx;
     v.rV[1](i, j, k) = ry;
     w.rho[0](i, j, k) = (float)(-rx);
@@ -372,7 +375,9 @@ int cg_stokes_solve_dc(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f,
     }
     f32.inv_eta = w.ieta;
     const SV<float> v32 = views<float>(&f32, nd);
-    const SP<float> s32 = scalars<float>(g, p);
+    // the correction problem's momentum forcing is the FP32 array -R_V; no body-force function
+    SP<float> s32 = scalars<float>(g, p);
+    for (int d = 0; d < 3; ++d) s32.fn[d].kind = CG_FN_NONE;
 
     cg_bc bc0[3];
     for (int d = 0; d < nd; ++d) {

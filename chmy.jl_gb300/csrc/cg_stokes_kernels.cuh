@@ -24,12 +24,58 @@ struct SV {  // device views of the Stokes field set
     }
 };
 
+// A device FunctionField (cg_function) in the field precision.
+template <class T>
+struct FnDev {
+    int kind;
+    T p[8];
+};
+
 template <class T>
 struct SP {  // scalars in the field precision
     T eta, eta_ve, G, dt, dtau_Pr, dtau_r, nu_dtau, lam;
     T inv_Gdt, third;
     T idx[3];
+    // body force per velocity component as a device FunctionField, and the grid's coordinates
+    FnDev<T> fn[3];
+    T org[3], dx[3];
 };
+
+// coord(grid, loc, I) (src/Grids/uniform_axis.jl): Vertex muladd(I-1, Δ, o), Center
+// muladd(I-1, Δ, muladd(0.5, Δ, o)); muladd is a fused multiply-add, as on the CPU.
+template <class T>
+__device__ __forceinline__ T grid_coord(T org, T dx, int I, bool vertex) {
+    const T o = vertex ? org : rfma(T(0.5), dx, org);
+    return rfma(T(I - 1), dx, o);
+}
+
+// func(x...) of a device FunctionField at the point x (cg_function's forms; every operation
+// rounded once, left to right, as the CPU evaluates the Julia expression).
+template <class T>
+__device__ __forceinline__ T fn_eval(const FnDev<T>& f, int nd, const T* x) {
+    if (f.kind == CG_FN_CONST) return f.p[0];
+    if (f.kind == CG_FN_BALL) {
+        T r2 = rmul(rsub(x[0], f.p[0]), rsub(x[0], f.p[0]));
+        for (int d = 1; d < nd; ++d) r2 = radd(r2, rmul(rsub(x[d], f.p[d]), rsub(x[d], f.p[d])));
+        return r2 < rmul(f.p[3], f.p[3]) ? f.p[4] : f.p[5];
+    }
+    if (f.kind == CG_FN_AFFINE) {
+        T v = f.p[0];
+        for (int d = 0; d < nd; ++d) v = radd(v, rmul(f.p[1 + d], x[d]));
+        return v;
+    }
+    return T(0);
+}
+
+// Body-force function of velocity component `comp` at its point (i, j, k): Vertex along comp,
+// Center along the other dimensions.
+template <class T>
+__device__ __forceinline__ T body_fn(const SP<T>& s, int comp, int nd, int i, int j, int k) {
+    const int I[3] = {i, j, k};
+    T x[3] = {T(0), T(0), T(0)};
+    for (int e = 0; e < nd; ++e) x[e] = grid_coord(s.org[e], s.dx[e], I[e], e == comp);
+    return fn_eval(s.fn[comp], nd, x);
+}
 
 template <class T>
 SV<T> views(const cg_stokes_fields* f, int nd) {
@@ -82,7 +128,13 @@ SP<T> scalars(const cg_grid* g, const cg_stokes_params* p) {
     s.lam = (T)p->lambda_rhoCp;
     s.inv_Gdt = T(1) / (s.G * s.dt);
     s.third = T(1) / T(3);
-    for (int d = 0; d < 3; ++d) s.idx[d] = (T)g->inv_spacing[d];
+    for (int d = 0; d < 3; ++d) {
+        s.idx[d] = (T)g->inv_spacing[d];
+        s.org[d] = (T)g->origin[d];
+        s.dx[d] = (T)g->spacing[d];
+        s.fn[d].kind = p->rho_g_fn[d].kind;
+        for (int q = 0; q < 8; ++q) s.fn[d].p[q] = (T)p->rho_g_fn[d].p[q];
+    }
     return s;
 }
 
@@ -236,8 +288,11 @@ __global__ void velocity_kernel(const SV<T> v, const SP<T> s, int e0, int e1) {
         rz = rz + (tyz(i, j + 1, k) - tyz(i, j, k)) * s.idx[1];
     }
     if (v.has_rho[0]) rx = rx - v.rho[0](i, j, k);
+    else if (s.fn[0].kind) rx = rx - body_fn(s, 0, ND, i, j, k);
     if (v.has_rho[1]) ry = ry - v.rho[1](i, j, k);
+    else if (s.fn[1].kind) ry = ry - body_fn(s, 1, ND, i, j, k);
     if (ND > 2 && v.has_rho[2]) rz = rz - v.rho[2](i, j, k);
+    else if (ND > 2 && s.fn[2].kind) rz = rz - body_fn(s, 2, ND, i, j, k);
     if (WRITE_RES && v.has_rV) {
         v.rV[0](i, j, k) = rx;
         v.rV[1](i, j, k) = ry;

@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define CG_ABI_VERSION 2
+#define CG_ABI_VERSION 3
 
 /* ---- status codes --------------------------------------------------------------- */
 enum {
@@ -270,6 +270,24 @@ typedef struct cg_stokes_fields {
 } cg_stokes_fields;
 
 /* Scalars of the PT loop (examples/stokes_2d_inc_ve_T.jl:86-93,142). */
+/* A FunctionField evaluated on the device (src/Fields/function_field.jl:49-59, the Continuous
+ * form): the value at logical index I is func(coord(grid, loc, I)..., parameters...), computed
+ * by the kernel that uses it instead of loaded from an array. Coordinates follow
+ * src/Grids/uniform_axis.jl: Vertex muladd(I-1, Δ, o), Center muladd(I-1, Δ, muladd(0.5, Δ, o)),
+ * in the kernel's precision. The functions a kernel can evaluate (p = parameters):
+ *   CG_FN_NONE    no function
+ *   CG_FN_CONST   p[0]
+ *   CG_FN_BALL    ifelse(sum_d (x_d - p[d])^2 < p[3]^2, p[4], p[5]), the squares summed in
+ *                 dimension order: init_incl of examples/stokes_2d_inc_ve_T.jl:106 (x0 = p[0],
+ *                 y0 = p[1], z0 = p[2], r = p[3], in = p[4], out = p[5])
+ *   CG_FN_AFFINE  p[0] + p[1] x + p[2] y + p[3] z, left to right */
+enum { CG_FN_NONE = 0, CG_FN_CONST = 1, CG_FN_BALL = 2, CG_FN_AFFINE = 3 };
+typedef struct cg_function {
+    int32_t kind;
+    int32_t pad_;
+    double  p[8];
+} cg_function;
+
 typedef struct cg_stokes_params {
     double eta;          /* scalar viscosity (used when fields.eta.data == NULL)       */
     double eta_ve;       /* 1/(1/eta + 1/(G dt)) (scalar case)                          */
@@ -279,7 +297,17 @@ typedef struct cg_stokes_params {
     double dtau_r;
     double nu_dtau;
     double lambda_rhoCp; /* thermal diffusivity for the thermal kernels                  */
+    /* Body force of component d as a device FunctionField at V.d's location (Vertex along d),
+     * e.g. rho_g_fn[1] = the examples' rhogy = FunctionField(init_incl, grid, (Center(),
+     * Vertex()); ...) (examples/stokes_2d_inc_ve_T.jl:107). The velocity update and the
+     * residuals subtract it like an array rho_g[d]; a component takes an array or a function,
+     * not both. The fused ping-pong entry (cg_stokes_pt_iterations_pp) reads arrays only. */
+    cg_function rho_g_fn[3];
 } cg_stokes_params;
+
+/* set!(f, grid, func) for a device FunctionField: f (any location) gets func at every padded
+ * point (logical 1-2H .. n+2H), evaluated on the device. */
+CG_API int cg_function_fill(cg_ctx* ctx, const cg_grid* grid, const cg_function* fn, const cg_field* f);
 
 /* update_old!: T_old = T; tau_old = tau at I in [0, n+1]^N. */
 CG_API int cg_stokes_update_old(cg_ctx* ctx, const cg_grid* grid, const cg_stokes_fields* f);

@@ -930,6 +930,48 @@ cg_field like_field(const cg_field& like, std::vector<T>& storage) {
     return f;
 }
 
+/* set!(f, grid, func) of a FunctionField (src/Fields/function_field.jl:49-59, Continuous form) for
+   the function forms of cg_function, at every padded point: func(coord(grid, loc, I)...,
+   parameters...) with coord of src/Grids/uniform_axis.jl (Vertex muladd(I-1, Δ, o), Center
+   muladd(I-1, Δ, muladd(0.5, Δ, o))) in the field's precision. CG_FN_BALL is init_incl of
+   examples/stokes_2d_inc_ve_T.jl:106: ifelse((x - x0)^2 + (y - y0)^2 < r^2, in, out). */
+template <class T>
+void function_fill_t(const cg_grid* grid, const cg_function* fn, const cg_field& fd) {
+    Fd<T> f(fd);
+    const int nd = fd.ndim;
+    T p[8];
+    for (int q = 0; q < 8; ++q) p[q] = (T)fn->p[q];
+    auto coord = [&](int d, int I) {
+        const T dx = (T)grid->spacing[d], o = (T)grid->origin[d];
+        const T base = fd.loc[d] == CG_VERTEX ? o : std::fma(T(0.5), dx, o);
+        return std::fma(T(I - 1), dx, base);
+    };
+    int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    for (int d = 0; d < nd; ++d) {
+        lo[d] = 1 - 2 * fd.halo[d];
+        hi[d] = fd.n[d] + 2 * fd.halo[d];
+    }
+    for (int k = lo[2]; k <= hi[2]; ++k)
+        for (int j = lo[1]; j <= hi[1]; ++j)
+            for (int i = lo[0]; i <= hi[0]; ++i) {
+                const int I[3] = {i, j, k};
+                T x[3] = {T(0), T(0), T(0)};
+                for (int d = 0; d < nd; ++d) x[d] = coord(d, I[d]);
+                T v = T(0);
+                if (fn->kind == CG_FN_CONST) {
+                    v = p[0];
+                } else if (fn->kind == CG_FN_BALL) {
+                    T r2 = (x[0] - p[0]) * (x[0] - p[0]);
+                    for (int d = 1; d < nd; ++d) r2 = r2 + (x[d] - p[d]) * (x[d] - p[d]);
+                    v = r2 < p[3] * p[3] ? p[4] : p[5];
+                } else if (fn->kind == CG_FN_AFFINE) {
+                    v = p[0];
+                    for (int d = 0; d < nd; ++d) v = v + p[1 + d] * x[d];
+                }
+                f(i, nd > 1 ? j : 0, nd > 2 ? k : 0) = v;
+            }
+}
+
 }  // namespace
 
 /* ==== extern "C" surface (names mirror the library's cg_* entry points) =============== */
@@ -1290,6 +1332,12 @@ int or_thermal_step_tangent(const cg_grid* grid, const cg_stokes_fields* f, cons
         double* o = static_cast<double*>(dTout[k].data);
         for (long q = 0; q < span_of(f->T); ++q) o[q] = tv[q].d[k];
     }
+    return CG_OK;
+}
+
+int or_function_fill(const cg_grid* grid, const cg_function* fn, const cg_field* f) {
+    if (f->dtype == CG_F64) function_fill_t<double>(grid, fn, *f);
+    else function_fill_t<float>(grid, fn, *f);
     return CG_OK;
 }
 

@@ -39,6 +39,7 @@ _SIGS = {
                                   P(_abi.cg_field), P(_abi.cg_field)], C.c_int),
     "or_thermal_step_tangent": ([P(_abi.cg_grid), P(_abi.cg_stokes_fields), P(_abi.cg_stokes_params), P(_abi.cg_bc), P(_abi.cg_field),
                                  P(_abi.cg_field), P(_abi.cg_field), P(_abi.cg_field)], C.c_int),
+    "or_function_fill": ([P(_abi.cg_grid), P(_abi.cg_function), P(_abi.cg_field)], C.c_int),
     "or_diffusion_compute_q_masked": ([P(_abi.cg_grid), P(_abi.cg_field), P(_abi.cg_field), C.c_double, P(_abi.cg_mask)], C.c_int),
     "or_diffusion_update_C_masked": ([P(_abi.cg_grid), P(_abi.cg_field), P(_abi.cg_field), C.c_double, P(_abi.cg_mask)], C.c_int),
     "or_stokes_update_old": ([P(_abi.cg_grid), P(_abi.cg_stokes_fields)], C.c_int),

@@ -714,3 +714,29 @@ def test_thermal_step_dual_tangents_match_oracle_differences():
     assert min(np.abs(v).min() for v in Vs) > 1e-4
     assert abs(dual_dir - fd_dir) <= 1e-6 * abs(fd_dir), (dual_dir, fd_dir)
     assert abs(dual_lam - fd_lam) <= 1e-6 * abs(fd_lam), (dual_lam, fd_lam)
+
+
+def test_function_field_host_and_oracle_evaluations():
+    """FunctionField.values() (numpy, coordinates as padded_mesh rounds them) and the oracle's
+    or_function_fill (coordinates by fused multiply-adds, Chmy's muladd) agree: the affine form to
+    rounding, the ball indicator except at points within rounding of its radius."""
+    import ctypes as C
+
+    from _oracle import lib
+    from chmy_gb300.functions import FunctionField, affine, ball
+
+    T = np.float64
+    for nd, dims in ((2, (40, 33)), (3, (14, 12, 11))):
+        grid = UniformGrid(origin=(T(-0.5),) * nd, extent=(T(1),) * nd, dims=dims, dtype=T)
+        loc = tuple(Vertex() if d == 0 else Center() for d in range(nd))
+        cases = [(ball, (0.1,) * nd + (0.3, 2.0, -1.0)), (affine, (0.25,) + tuple(float(d + 1) for d in range(nd)))]
+        for func, params in cases:
+            ff = FunctionField(func, grid, loc, parameters=params)
+            ref = NpField(grid, loc, T)
+            assert lib().or_function_fill(C.byref(grid.desc()), C.byref(ff.desc()), C.byref(ref.desc())) == 0
+            host = ff.values()
+            if func is ball:
+                assert set(np.unique(ref.a)) <= {2.0, -1.0}
+                assert np.mean(host != ref.a) < 1e-3
+            else:
+                np.testing.assert_allclose(host, ref.a, rtol=0, atol=1e-14)
