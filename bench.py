@@ -621,7 +621,7 @@ def config_suite(arch, stream, peak, fp64=True):
     cfg2 = {}
     for T, name in ((np.float64, "fp64"), (np.float32, "fp32")):
         # FP32: one row pitch and plane height for every array (the fused single-pass kernel)
-        lay = dict(pitch_align=128, plane_rows=n2 + 5) if T == np.float32 else {}
+        lay = dict(pitch_align=128, plane_rows=n2 + 5, align_index=-1) if T == np.float32 else {}
         fs = {k: Field(arch, g2, Cl, T, **lay) for k in ("C", "C_old", "D")}
         q = [Field(arch, g2, tuple(Vl if e == d else Cl for e in range(3)), T, **lay) for d in range(3)]
         fs["C"].from_numpy(Cb.astype(T))
@@ -956,7 +956,8 @@ def fused3d_kernel_fields(arch, pb):
     rows = g.dims[1] + 5
 
     def f32(loc):
-        return Field(arch, g, loc, np.float32, pitch_align=128, plane_rows=rows)
+        # rows start at their first padded element on a 128-byte boundary, as in the solver's pool
+        return Field(arch, g, loc, np.float32, pitch_align=128, plane_rows=rows, align_index=-1)
 
     vl = [(Vl, Cl, Cl), (Cl, Vl, Cl), (Cl, Cl, Vl)]
     tl = [(Cl, Cl, Cl)] * 3 + [(Vl, Vl, Cl), (Vl, Cl, Vl), (Cl, Vl, Vl)]
@@ -986,7 +987,7 @@ def run_kernel_ptdiff(arch, args):
     g = UniformGrid(origin=(-0.5,) * 3, extent=(1.0,) * 3, dims=(n,) * 3, dtype=T)
     Cl, Vl = Center(), Vertex()
     rng = np.random.default_rng(2)
-    lay = dict(pitch_align=128, plane_rows=n + 5)
+    lay = dict(pitch_align=128, plane_rows=n + 5, align_index=-1)
     fs = {k: Field(arch, g, Cl, T, **lay) for k in ("C", "C_old", "D")}
     q = [Field(arch, g, tuple(Vl if e == d else Cl for e in range(3)), T, **lay) for d in range(3)]
     fs["C"].from_numpy(rng.random(fs["C"].data.shape, dtype=T))

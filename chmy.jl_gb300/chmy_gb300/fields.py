@@ -32,13 +32,15 @@ def _np_type(dtype) -> type:
 class Field:
     """Field(arch, grid, loc, type=eltype(grid); halo=1) (src/Fields/field.jl:56-62).
 
-    `pitch_align` (bytes, 0 = dense Chmy layout) pads x rows so that logical x index 0 of each
-    row is aligned, which lets kernels issue aligned vector loads. `plane_rows` (3D, with
-    `pitch_align`) pads every z plane to that many rows. Fields of different locations then
-    share their row and plane strides, and the fused kernels address them all with one
-    offset."""
+    `pitch_align` (bytes, 0 = dense Chmy layout) pads x rows so that logical x index
+    `align_index` (default 0; -1 = the first padded element) of each row is aligned. The fused
+    kernels read every row from index -1: with `align_index=-1` a row of n + 4 elements spans the
+    fewest 128-byte lines, which is what DRAM moves. `plane_rows` (3D, with `pitch_align`) pads
+    every z plane to that many rows. Fields of different locations then share their row and
+    plane strides, and the fused kernels address them all with one offset."""
 
-    def __init__(self, arch, grid: UniformGrid, loc, dtype=None, halo=1, pitch_align: int = 0, plane_rows: int = 0):
+    def __init__(self, arch, grid: UniformGrid, loc, dtype=None, halo=1, pitch_align: int = 0, plane_rows: int = 0,
+                 align_index: int = 0):
         self.arch = arch
         self.grid = grid
         nd = grid.ndim
@@ -54,7 +56,7 @@ class Field:
         dev = arch.device
         if pitch_align:
             a = pitch_align // esz
-            front = (a - (2 * self.halo[0] - 1) % a) % a
+            front = (a - (2 * self.halo[0] - 1 + align_index) % a) % a
             pitch = ((front + self.ext[0] + a - 1) // a) * a
             outer = list(reversed(self.ext[1:]))
             if nd == 3 and plane_rows:

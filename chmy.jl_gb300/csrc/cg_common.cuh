@@ -79,6 +79,9 @@ bool cg_ptdiff_fused_enabled();
 // The SIA ensemble as one persistent cooperative launch (CG_SIA_PERSISTENT=1) instead of one
 // launch per phase replayed from a CUDA graph (the default, measured faster).
 bool cg_sia_persistent_enabled();
+// CG_SIA_TILE_ROWS=4|8|16: the SIA ensemble's tile height (rows of 32-point tiles) instead of the
+// autotuned one (0 when unset); the results do not depend on it.
+int cg_sia_tile_rows_forced();
 // Grid barriers of the persistent SIA ensemble kernel: the time limit of every wait
 // (CG_SIA_BARRIER_LIMIT_MS, default 2000 ms) and a number of arrivals that the barrier expects
 // beyond the grid's blocks (CG_SIA_BARRIER_WITHHELD, default 0). A withheld arrival never

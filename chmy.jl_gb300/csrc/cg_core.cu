@@ -94,7 +94,7 @@ bool cg_tune_forced(cg_tune_cfg* out) {
     const char* e = std::getenv("CG_MARCH_LAYOUT");
     if (!e || !e[0]) return false;
     int seg = 0, var = 0;
-    if (std::sscanf(e, "%d:%d", &seg, &var) != 2 || seg < 0 || var < 0 || var > 2) return false;
+    if (std::sscanf(e, "%d:%d", &seg, &var) != 2 || seg < 0 || var < 0 || var > 4) return false;
     *out = cg_tune_cfg{seg, var};
     return true;
 }
@@ -127,6 +127,14 @@ bool cg_sia_persistent_enabled() {
     // read on every call (once per run), so that a process can compare both forms
     const char* e = std::getenv("CG_SIA_PERSISTENT");
     return e && e[0] == '1';
+}
+
+int cg_sia_tile_rows_forced() {
+    // read on every call, like CG_SIA_PERSISTENT
+    const char* e = std::getenv("CG_SIA_TILE_ROWS");
+    if (!e) return 0;
+    const long r = std::strtol(e, nullptr, 10);
+    return (r == 4 || r == 8 || r == 16) ? (int)r : 0;
 }
 
 cg_barrier_cfg cg_sia_barrier_cfg() {

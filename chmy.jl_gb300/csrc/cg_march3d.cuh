@@ -440,12 +440,9 @@ inline cudaError_t launch_march3d_ix(const Fused3D<T>& f, const SP<T>& s, int n0
 
 // Launch of the z-marching kernel over [0, n+1]^3; seg_len <= 0 picks the z-segment length;
 // dep = true makes it a dependent launch (cg_launch).
-// For FP32 with shared strides, variant 0 is 12 rows per block at 2 blocks per SM, variant 1
+// For FP32 with shared strides, variant 0 is 12 rows per block at 2 blocks per SM and variant 1
 // is 8 rows per block at 3 blocks per SM (both 80 registers, no spills; the two best measured
-// of 4-16 rows per block and 1-5 blocks per SM at 256^3), and variant 2 is 10 rows per block at
-// 2 blocks per SM: at 256^3 its 9 x 33 tiles fill the 304 resident slots in one wave, so every
-// block marches a whole column and its neighbours march beside it (their shared halo rows and
-// sectors stay in L2, and no z-segment re-reads its first planes).
+// of 4-16 rows per block and 1-5 blocks per SM at 256^3).
 template <class T, bool WRITE_RES>
 inline cudaError_t launch_march3d(const Fused3D<T>& f, const SP<T>& s, int n0, int n1, int n2, int num_sms, int seg_len,
                                   cudaStream_t st, int variant = 0, bool dep = false) {
@@ -456,8 +453,6 @@ inline cudaError_t launch_march3d(const Fused3D<T>& f, const SP<T>& s, int n0, i
             if constexpr (sizeof(T) == 4) {
                 if (variant == 1)
                     return launch_march3d_ix<T, int, true, WRITE_RES, 3, 8>(f, s, n0, n1, n2, num_sms, seg_len, s1, s2, st, dep);
-                if (variant == 2)
-                    return launch_march3d_ix<T, int, true, WRITE_RES, 2, 10>(f, s, n0, n1, n2, num_sms, seg_len, s1, s2, st, dep);
                 return launch_march3d_ix<T, int, true, WRITE_RES, 2, 12>(f, s, n0, n1, n2, num_sms, seg_len, s1, s2, st, dep);
             }
             return launch_march3d_ix<T, int, true, WRITE_RES, 1>(f, s, n0, n1, n2, num_sms, seg_len, s1, s2, st, dep);
@@ -517,7 +512,7 @@ inline cg_tune_cfg tune_march3d(const Fused3D<T>& f, const SP<T>& s, int n0, int
     cg_key_add(key, uni ? s2 : 0L);
     cg_key_add(key, nsm);
     if (cg_tune_lookup(key, &best)) return best;
-    const int nvar = (sizeof(T) == 4 && uni) ? 3 : 1;
+    const int nvar = (sizeof(T) == 4 && uni) ? 2 : 1;
     float tbest = 1e30f;
     for (int v = 0; v < nvar; ++v)
         for (int seg : {0, 16, 32, 64}) {

@@ -739,16 +739,17 @@ int solve_fp64(cg_ctx* ctx, const cg_grid* g, const cg_ptdiff_fields* f, const c
 
 int solve_dc(cg_ctx* ctx, const cg_grid* g, const cg_ptdiff_fields* f, const cg_ptdiff_params* p, const cg_bc* bc,
              const cg_solve_opts* o, cg_solve_result* res) {
-    // FP32 pool: d, d', q x3, q' x3, C_old' (dt R), D; logical x index 0 of every row on a
-    // 128-byte boundary
-    const long front = 31, pitch = ((front + g->n[0] + 5 + 31) / 32) * 32, rows = g->n[1] + 5;
+    // FP32 pool: d, d', q x3, q' x3, C_old' (dt R), D; the first padded element of every row
+    // (logical x index -1, the first the kernels read) on a 128-byte boundary, so that a row's
+    // n + 4 elements span the fewest 128-byte lines (DRAM moves whole lines)
+    const long front = 0, pitch = ((front + g->n[0] + 5 + 31) / 32) * 32, rows = g->n[1] + 5;
     const size_t per = (size_t)pitch * rows * (g->n[2] + 5) * sizeof(float);
     const size_t per_al = (per + 255) & ~(size_t)255;
     int rc = CG_OK;
     char* base = static_cast<char*>(cg_scratch(ctx, 4, per_al * 10 + 256, &rc));
     if (rc) return rc;
-    // an array's data pointer sits `front` elements into its rows, so that its logical x index 0
-    // (data + 1 element, halo 1) starts a 128-byte line
+    // an array's data pointer sits `front` elements into its rows (0: its first element starts a
+    // 128-byte line)
     base += front * sizeof(float);
     const int qm[3] = {1, 2, 4};
     cg_field dA = pool_field(base, 0, g, 0, pitch, rows), dB = pool_field(base, per_al, g, 0, pitch, rows);

@@ -35,7 +35,7 @@ struct Member {
     T Gn2, Asn;  // Gamma (n+2) and As n, for the taped derivatives of D
     double dx2, cfl, dt_max;
     int n, nx, ny;
-    int tiles_D, tiles_I;  // tiles of the [0, n] and [1, n] ranges (32 x 8 each)
+    int tiles_D, tiles_I;  // tiles of the [0, n] and [1, n] ranges (32 x blockDim.y each)
     // taped runs: the member's tape block within a step's block (cgsia layout: 256 bytes of
     // words, then kArrays arrays of `tab` bytes in H's layout, H's origin at element `orig`)
     long long toff, tab, orig;
@@ -104,7 +104,7 @@ __device__ __forceinline__ void ens_D_tile(const Member<T>* mem, const int* pref
     const int t = blk - (m ? prefix[m - 1] : 0);
     const int tx = (v.nx + 1 + 31) / 32;
     const int i = (t % tx) * 32 + threadIdx.x;
-    const int j = (t / tx) * 8 + threadIdx.y;
+    const int j = (t / tx) * (int)blockDim.y + threadIdx.y;
     const bool in = i <= v.nx && j <= v.ny;
     T d = T(0);
     if (in) {
@@ -149,7 +149,7 @@ __device__ __forceinline__ void ens_S_tile(const Member<T>* mem, const int* pref
     const int t = blk - (m ? prefix[m - 1] : 0);
     const int tx = (v.nx + 3 + 31) / 32;
     const int i = (t % tx) * 32 + threadIdx.x - 1;
-    const int j = (t / tx) * 8 + threadIdx.y - 1;
+    const int j = (t / tx) * (int)blockDim.y + threadIdx.y - 1;
     if (i > v.nx + 1 || j > v.ny + 1) return;
     v.S(i, j, 0) = v.B(i, j, 0) + v.H(i, j, 0);
 }
@@ -161,7 +161,7 @@ __device__ __forceinline__ void ens_q_tile(const Member<T>* mem, const int* pref
     const int t = blk - (m ? prefix[m - 1] : 0);
     const int tx = (v.nx + 31) / 32;
     const int i = (t % tx) * 32 + threadIdx.x + 1;
-    const int j = (t / tx) * 8 + threadIdx.y + 1;
+    const int j = (t / tx) * (int)blockDim.y + threadIdx.y + 1;
     if (i > v.nx || j > v.ny) return;
     const T dc = v.D(i, j, 0), dl = v.D(i - 1, j, 0), dd = v.D(i, j - 1, 0);
     const T Dx = fma(T(0.5), dc - dl, dl);
@@ -206,7 +206,7 @@ __device__ __forceinline__ void ens_H_tile(const Member<T>* mem, const int* pref
     const int t = blk - (m ? prefix[m - 1] : 0);
     const int tx = (v.nx + 31) / 32;
     const int i = (t % tx) * 32 + threadIdx.x + 1;
-    const int j = (t / tx) * 8 + threadIdx.y + 1;
+    const int j = (t / tx) * (int)blockDim.y + threadIdx.y + 1;
     if (i > v.nx || j > v.ny) return;
     const T dt = (T)w[m].dt;
     const T h = v.H(i, j, 0);
@@ -421,65 +421,120 @@ int run_t(cg_ctx* ctx, int nm, const cg_sia_member* ms, const cg_sia_params* ps,
     std::vector<int> pD(nm), pI(nm), pS(nm);
     const EnsTape et = ens_tape_layout(nm, ms, sizeof(T));
     int totD = 0, totI = 0, totS = 0;
-    for (int m = 0; m < nm; ++m) {
-        const cg_sia_member& s = ms[m];
-        const cg_sia_params& p = ps[m];
-        Member<T>& v = hm[m];
-        std::memset(&v, 0, sizeof(v));
-        v.H = cg_view<T>(s.H);
-        v.B = cg_view<T>(s.B);
-        v.qx = cg_view<T>(s.q[0]);
-        v.qy = cg_view<T>(s.q[1]);
-        v.D = v.H;
-        v.D.p = reinterpret_cast<T*>(base + d_off[m]) + cg_origin_offset(s.H);
-        v.S = v.H;
-        v.S.p = reinterpret_cast<T*>(base + s_off[m]) + cg_origin_offset(s.H);
-        v.Gamma = (T)p.Gamma;
-        v.As = (T)p.As;
-        v.beta = (T)p.beta;
-        v.ela = (T)p.ela;
-        v.m_max = (T)p.m_max;
-        v.Gn2 = v.Gamma * T(p.n + 2);
-        v.Asn = v.As * T(p.n);
-        v.idx = (T)s.grid.inv_spacing[0];
-        v.idy = (T)s.grid.inv_spacing[1];
-        const double dx = std::min(s.grid.spacing[0], s.grid.spacing[1]);
-        v.dx2 = (double)((T)dx * (T)dx);
-        v.cfl = p.cfl;
-        v.dt_max = p.dt_max;
-        v.n = p.n;
-        v.nx = s.grid.n[0];
-        v.ny = s.grid.n[1];
-        v.tiles_D = cg_div_up(v.nx + 1, 32) * cg_div_up(v.ny + 1, 8);
-        v.tiles_I = cg_div_up(v.nx, 32) * cg_div_up(v.ny, 8);
-        if (tape) {
-            v.toff = et.toff[m];
-            v.tab = et.tab[m];
-            v.orig = et.orig[m];
-        }
-        totD += v.tiles_D;
-        totI += v.tiles_I;
-        totS += cg_div_up(v.nx + 3, 32) * cg_div_up(v.ny + 3, 8);
-        pD[m] = totD;
-        pI[m] = totI;
-        pS[m] = totS;
-    }
     Member<T>* dmem = reinterpret_cast<Member<T>*>(base + mem_off);
     int* dpD = reinterpret_cast<int*>(base + pD_off);
     int* dpI = reinterpret_cast<int*>(base + pI_off);
     int* dpS = reinterpret_cast<int*>(base + pS_off);
     Words* dw = reinterpret_cast<Words*>(base + w_off);
-    CG_CUDA(ctx, cudaMemcpyAsync(dmem, hm.data(), nm * sizeof(Member<T>), cudaMemcpyHostToDevice, ctx->stream));
-    CG_CUDA(ctx, cudaMemcpyAsync(dpD, pD.data(), nm * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
-    CG_CUDA(ctx, cudaMemcpyAsync(dpI, pI.data(), nm * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
-    CG_CUDA(ctx, cudaMemcpyAsync(dpS, pS.data(), nm * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
-    CG_CUDA(ctx, cudaMemsetAsync(dw, 0, nm * sizeof(Words), ctx->stream));
-    const dim3 block(32, 8);
-    // cooperative-launch support and residency of the persistent kernel on this context's
-    // device (queried per call: a process may hold contexts on different GPU models)
+    // members and tile prefix tables for tiles of 32 x ty points, uploaded to the scratch
+    auto layout = [&](int ty) -> int {
+        totD = totI = totS = 0;
+        for (int m = 0; m < nm; ++m) {
+            const cg_sia_member& s = ms[m];
+            const cg_sia_params& p = ps[m];
+            Member<T>& v = hm[m];
+            std::memset(&v, 0, sizeof(v));
+            v.H = cg_view<T>(s.H);
+            v.B = cg_view<T>(s.B);
+            v.qx = cg_view<T>(s.q[0]);
+            v.qy = cg_view<T>(s.q[1]);
+            v.D = v.H;
+            v.D.p = reinterpret_cast<T*>(base + d_off[m]) + cg_origin_offset(s.H);
+            v.S = v.H;
+            v.S.p = reinterpret_cast<T*>(base + s_off[m]) + cg_origin_offset(s.H);
+            v.Gamma = (T)p.Gamma;
+            v.As = (T)p.As;
+            v.beta = (T)p.beta;
+            v.ela = (T)p.ela;
+            v.m_max = (T)p.m_max;
+            v.Gn2 = v.Gamma * T(p.n + 2);
+            v.Asn = v.As * T(p.n);
+            v.idx = (T)s.grid.inv_spacing[0];
+            v.idy = (T)s.grid.inv_spacing[1];
+            const double dx = std::min(s.grid.spacing[0], s.grid.spacing[1]);
+            v.dx2 = (double)((T)dx * (T)dx);
+            v.cfl = p.cfl;
+            v.dt_max = p.dt_max;
+            v.n = p.n;
+            v.nx = s.grid.n[0];
+            v.ny = s.grid.n[1];
+            v.tiles_D = cg_div_up(v.nx + 1, 32) * cg_div_up(v.ny + 1, ty);
+            v.tiles_I = cg_div_up(v.nx, 32) * cg_div_up(v.ny, ty);
+            if (tape) {
+                v.toff = et.toff[m];
+                v.tab = et.tab[m];
+                v.orig = et.orig[m];
+            }
+            totD += v.tiles_D;
+            totI += v.tiles_I;
+            totS += cg_div_up(v.nx + 3, 32) * cg_div_up(v.ny + 3, ty);
+            pD[m] = totD;
+            pI[m] = totI;
+            pS[m] = totS;
+        }
+        CG_CUDA(ctx, cudaMemcpyAsync(dmem, hm.data(), nm * sizeof(Member<T>), cudaMemcpyHostToDevice, ctx->stream));
+        CG_CUDA(ctx, cudaMemcpyAsync(dpD, pD.data(), nm * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+        CG_CUDA(ctx, cudaMemcpyAsync(dpI, pI.data(), nm * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+        CG_CUDA(ctx, cudaMemcpyAsync(dpS, pS.data(), nm * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+        CG_CUDA(ctx, cudaMemsetAsync(dw, 0, nm * sizeof(Words), ctx->stream));
+        // the host tables are read by the copies above before the next layout call rewrites them
+        CG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        return CG_OK;
+    };
     int coop = 0;
     if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device) != cudaSuccess) coop = 0;
-    if (coop && !tape && cg_sia_persistent_enabled()) {
+    const bool persistent = coop && !tape && cg_sia_persistent_enabled();
+    // tile height: 8 rows for the persistent kernel, else the forced or autotuned choice
+    int ty = 8;
+    if (!persistent) {
+        const int forced = cg_sia_tile_rows_forced();
+        if (forced) {
+            ty = forced;
+        } else if (cg_autotune_enabled()) {
+            std::string tkey = "sia_ensemble_tiles";
+            cg_key_add(tkey, (int)sizeof(T));
+            cg_key_add(tkey, ctx->num_sms);
+            for (int m = 0; m < nm; ++m) {
+                cg_key_add(tkey, ms[m].grid.n[0]);
+                cg_key_add(tkey, ms[m].grid.n[1]);
+            }
+            cg_tune_cfg tc{0, 0};
+            if (cg_tune_lookup(tkey, &tc)) {
+                ty = tc.variant;
+            } else {
+                // time the D and flux phases of one step for each tile height; neither changes
+                // the thickness (D, the face gradients, the fluxes and S = B + H are recomputed
+                // by the run, and the words are cleared by the next layout call)
+                float best = 1e30f;
+                for (int cand : {4, 8, 16}) {
+                    if ((rc = layout(cand))) return rc;
+                    const dim3 bk(32, cand);
+                    const float t = cgk::time_launches(
+                        [&] {
+                            ens_S_kernel<T><<<totS, bk, 0, ctx->stream>>>(dmem, dpS, nm);
+                            ens_D_kernel<T><<<totD, bk, 0, ctx->stream>>>(dmem, dpD, nm, dw, nullptr);
+                            ens_q_kernel<T><<<totI, bk, 0, ctx->stream>>>(dmem, dpI, nm);
+                            return cudaGetLastError();
+                        },
+                        ctx->stream);
+                    if (cg_tune_verbose())
+                        std::fprintf(stderr, "sia ensemble tune (%d members): 32x%d tiles: %.1f us\n", nm, cand,
+                                     t >= 0.f ? 1e3f * t / 3 : -1.f);
+                    if (t >= 0.f && t < best) {
+                        best = t;
+                        ty = cand;
+                    }
+                }
+                cudaGetLastError();
+                cg_tune_store(tkey, cg_tune_cfg{0, ty});
+            }
+        }
+    }
+    if ((rc = layout(ty))) return rc;
+    const dim3 block(32, ty);
+    // cooperative-launch support and residency of the persistent kernel are queried per call on
+    // this context's device (a process may hold contexts on different GPU models)
+    if (persistent) {
         // the whole run in one cooperative launch of the resident blocks
         int bps = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ens_persistent_kernel<T>, 256, 0) != cudaSuccess) bps = 0;
@@ -502,6 +557,7 @@ int run_t(cg_ctx* ctx, int nm, const cg_sia_member* ms, const cg_sia_params* ps,
         if (timed_out) return cg_fail(ctx, CG_ERR_TIMEOUT, "sia_ensemble_run: a grid barrier of the persistent kernel timed out");
     } else {
     std::string key = "sia_ensemble";
+    cg_key_add(key, ty);
     cg_key_add(key, nm);
     cg_key_add(key, nsteps);
     cg_key_add(key, base);

@@ -228,3 +228,54 @@ def test_ensemble_persistent_barrier_wait_runs_out(arch, monkeypatch):
     assert rc == _abi.CG_OK
     for a, b in zip(Hp, Hg):
         np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("T", TYPES)
+def test_ensemble_tile_heights_give_the_same_bits(arch, monkeypatch, T):
+    """The ensemble's tile height (rows of its 32-point tiles: 4, 8 or 16, CG_SIA_TILE_ROWS) is an
+    autotuned launch choice: H, q and every member's time are the same bits under each height, and
+    under the autotuner's choice, for 9 members of uneven sizes."""
+    from chmy_gb300.configs import sia_ensemble
+
+    ens = sia_ensemble(members=9, nmin=20, nmax=140, seed=12, dtype=T)
+    nsteps = 25
+    rng = np.random.default_rng(8)
+    start = []
+    for grid, h, p in ens:
+        H0 = NpField(grid, Center(), T)
+        H0.interior()[...] = (rng.random(H0.dims) * 0.3).astype(T)
+        B = NpField(grid, Center(), T)
+        B.a[...] = h["B"].astype(T)
+        start.append((grid, H0, B, p))
+
+    def run():
+        mem = (_abi.cg_sia_member * len(start))()
+        params = (_abi.cg_sia_params * len(start))()
+        keep = []
+        for k, (grid, H0, B, p) in enumerate(start):
+            Hg, Bg = to_gpu(arch, H0), to_gpu(arch, B)
+            qg = [to_gpu(arch, NpField(grid, (Vertex(), Center()), T)), to_gpu(arch, NpField(grid, (Center(), Vertex()), T))]
+            keep.append((Hg, qg, Bg))
+            mem[k].grid = grid.desc()
+            mem[k].H, mem[k].B = Hg.desc(), Bg.desc()
+            mem[k].q[0], mem[k].q[1] = qg[0].desc(), qg[1].desc()
+            params[k] = p
+        ts = (ctypes.c_double * len(start))()
+        arch.call("cg_sia_ensemble_run", len(start), mem, params, nsteps, ts)
+        arch.synchronize()
+        return [(Hg.to_numpy(), qg[0].to_numpy(), qg[1].to_numpy()) for Hg, qg, _ in keep], list(ts)
+
+    monkeypatch.setenv("CG_SIA_PERSISTENT", "0")
+    results = []
+    for rows in ("4", "8", "16", None):
+        if rows is None:
+            monkeypatch.delenv("CG_SIA_TILE_ROWS", raising=False)
+        else:
+            monkeypatch.setenv("CG_SIA_TILE_ROWS", rows)
+        results.append(run())
+    fa, ta = results[0]
+    for fb, tb in results[1:]:
+        assert ta == tb
+        for k, (a, b) in enumerate(zip(fa, fb)):
+            for x, y in zip(a, b):
+                np.testing.assert_array_equal(x, y, err_msg=f"member {k}")
