@@ -941,7 +941,7 @@ def fused_kernel_fields(arch, pb):
     return stokes_fields(V=A["V"], P=A["P"], tau=A["tau"], **extra), stokes_fields(V=B["V"], P=B["P"], tau=B["tau"]), keep
 
 
-def fused3d_kernel_fields(arch, pb):
+def fused3d_kernel_fields(arch, pb, align_index=-1):
     """FP32 ping-pong field sets of the fused 3D PT kernel on the problem's grid (1/eta from eta,
     rho_g from the problem, zero V/tau/P/tau_old). Every array shares its row and plane strides,
     as in the solver's work pool."""
@@ -957,7 +957,7 @@ def fused3d_kernel_fields(arch, pb):
 
     def f32(loc):
         # rows start at their first padded element on a 128-byte boundary, as in the solver's pool
-        return Field(arch, g, loc, np.float32, pitch_align=128, plane_rows=rows, align_index=-1)
+        return Field(arch, g, loc, np.float32, pitch_align=128, plane_rows=rows, align_index=align_index)
 
     vl = [(Vl, Cl, Cl), (Cl, Vl, Cl), (Cl, Cl, Vl)]
     tl = [(Cl, Cl, Cl)] * 3 + [(Vl, Vl, Cl), (Vl, Cl, Vl), (Cl, Vl, Vl)]
@@ -969,6 +969,63 @@ def fused3d_kernel_fields(arch, pb):
     extra["rho_g"][2].data.copy_(torch.from_numpy(pb.host["rho_g"][2]).float())
     keep = (A, B, extra)
     return stokes_fields(V=A["V"], P=A["P"], tau=A["tau"], **extra), stokes_fields(V=B["V"], P=B["P"], tau=B["tau"]), keep
+
+
+def run_kernel_fp64(arch, args):
+    """--kernel stokes64: `--reps` FP64 PT iterations of the 2D inclusion problem at n^2
+    (cg_stokes_pt_iterations: stress_kernel, velocity_kernel and bc!(V) per iteration).
+    --kernel ptdiff64: `--reps` FP64 PT-diffusion iterations at n^3 (ptdiff_q_kernel,
+    ptdiff_C_kernel and bc!(C) per iteration). Timed with CUDA events after warm-up; the FP64
+    FMA peak of the device (cg_fp64_peak) beside it."""
+    import torch
+
+    from chmy_gb300 import Field, _abi
+    from chmy_gb300.bcs import Dirichlet, Neumann, to_cg_bc
+    from chmy_gb300.configs import ptdiff_params, stokes2d_inclusions
+    from chmy_gb300.grids import Center, UniformGrid, Vertex
+    from chmy_gb300.solvers import StokesSolver
+
+    n, reps = args.n, args.reps
+    if args.kernel == "stokes64":
+        s = StokesSolver(arch, stokes2d_inclusions(n))
+        s.apply_bc()
+
+        def run(k):
+            s.iterate(k)
+        cells = n * n
+    else:
+        T = np.float64
+        g = UniformGrid(origin=(-0.5,) * 3, extent=(1.0,) * 3, dims=(n,) * 3, dtype=T)
+        Cl, Vl = Center(), Vertex()
+        rng = np.random.default_rng(2)
+        fs = {k: Field(arch, g, Cl, T) for k in ("C", "C_old", "D")}
+        q = [Field(arch, g, tuple(Vl if e == d else Cl for e in range(3)), T) for d in range(3)]
+        fs["C"].from_numpy(rng.random(fs["C"].data.shape))
+        D = np.exp(rng.uniform(-1, 1, fs["D"].data.shape))
+        fs["D"].from_numpy(D)
+        f = _abi.cg_ptdiff_fields()
+        f.C, f.C_old, f.D = fs["C"].desc(), fs["C_old"].desc(), fs["D"].desc()
+        f.q = (_abi.cg_field * 3)(*[qq.desc() for qq in q])
+        p = ptdiff_params(g, 1e-3, float(D.max()))
+        bc = to_cg_bc(3, {"x": Dirichlet(0.0), "y": Neumann(), "z": Neumann()})
+        gd = g.desc()
+
+        def run(k):
+            arch.call("cg_ptdiff_run", ctypes.byref(gd), ctypes.byref(f), ctypes.byref(p), ctypes.byref(bc), 1, k)
+        cells = n**3
+    run(4)
+    run(reps)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    run(reps)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    peak = ctypes.c_double()
+    arch.call("cg_fp64_peak", ctypes.byref(peak))
+    print(json.dumps({"kernel": args.kernel, "n": n, "cells": cells, "us_per_iteration": ms * 1e3,
+                      "fp64_peak_tflops": peak.value / 1e12}))
 
 
 def run_kernel_ptdiff(arch, args):
@@ -1119,6 +1176,10 @@ def run_kernel(args):
         run_kernel_ptdiff(arch, args)
         arch.close()
         return
+    if args.kernel in ("stokes64", "ptdiff64"):
+        run_kernel_fp64(arch, args)
+        arch.close()
+        return
     if args.kernel in ("sia_ensemble", "diffusion2d"):
         run_kernel_misc(arch, args)
         arch.close()
@@ -1129,7 +1190,7 @@ def run_kernel(args):
         return
     if args.kernel == "fused3d":
         pb = stokes3d_grf(args.n, dtype=np.float32)
-        da, db, keep = fused3d_kernel_fields(arch, pb)
+        da, db, keep = fused3d_kernel_fields(arch, pb, args.align_index)
         name, arrays, cells = "march3d_kernel<float>", FUSED3_ARRAYS, args.n**3
     else:
         pb = stokes2d_inclusions(args.n)
@@ -1144,25 +1205,30 @@ def run_kernel(args):
     run(4)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    run(reps)
-    e1.record()
-    torch.cuda.synchronize()
+    with ClockSampler(0) as clk:
+        e0.record()
+        run(reps)
+        e1.record()
+        torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / reps
     byt = arrays * cells * 4
     print(json.dumps({"kernel": name, "n": args.n, "arrays": arrays, "us_per_launch": ms * 1e3,
-                      "algorithmic_gbs": byt / (ms * 1e-3) / 1e9, "frac_of_measured_hbm": byt / (ms * 1e-3) / 1e9 / measured_peaks()[0]}))
+                      "algorithmic_gbs": byt / (ms * 1e-3) / 1e9, "frac_of_measured_hbm": byt / (ms * 1e-3) / 1e9 / measured_peaks()[0],
+                      "clocks": clk.summary()}))
     arch.close()
 
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--kernel", choices=["fused2d", "fused3d", "ptdiff3d", "sia_ensemble", "diffusion2d", "sia_adjoint"],
+    ap.add_argument("--kernel", choices=["fused2d", "fused3d", "ptdiff3d", "sia_ensemble", "diffusion2d", "sia_adjoint", "stokes64",
+                                         "ptdiff64"],
                     help="time one kernel alone (profiling driver)")
     ap.add_argument("--members", type=int, default=64, help="--kernel sia_ensemble: ensemble members")
     ap.add_argument("--nmin", type=int, default=128, help="--kernel sia_ensemble: smallest member size")
     ap.add_argument("--nmax", type=int, default=1024, help="--kernel sia_ensemble: largest member size")
     ap.add_argument("--reps", type=int, default=200)
+    ap.add_argument("--align-index", type=int, default=-1,
+                    help="--kernel fused3d: the logical x index each padded row aligns to 128 bytes (-1: its first element)")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)

@@ -197,6 +197,7 @@ SIGNATURES: dict[str, list] = {
     "cg_diffusion_adjoint_run": [_vp, P(cg_grid), _vp, C.c_size_t, P(cg_field), P(cg_field), C.c_double, C.c_double, P(cg_bc),
                                  P(C.c_double)],
     "cg_function_fill": [_vp, P(cg_grid), P(cg_function), P(cg_field)],
+    "cg_fp64_peak": [_vp, P(C.c_double)],
     "cg_stokes_update_old": [_vp, P(cg_grid), P(cg_stokes_fields)],
     "cg_stokes_update_stress": [_vp, P(cg_grid), P(cg_stokes_fields), P(cg_stokes_params)],
     "cg_stokes_update_velocity": [_vp, P(cg_grid), P(cg_stokes_fields), P(cg_stokes_params)],

@@ -468,10 +468,16 @@ inline cudaError_t launch_march3d(const Fused3D<T>& f, const SP<T>& s, int n0, i
 // captured. Only the `out` buffers of the ping-pong view are written (the first real iteration
 // writes them again); the residual outputs are not touched. Results are cached per shape,
 // precision and layout for the process.
+// 2D candidates: variant 0 is march2d_kernel (one iteration per launch), variants 1 and 2 the
+// two-iteration march2d_x2_kernel at 4 and 5 blocks per SM (when march_x2_ok); the time
+// compared is per iteration.
 template <class T>
 inline cg_tune_cfg tune_march2d(const Fused2D<T>& f, const SP<T>& s, int n0, int n1, int nsm, cudaStream_t st) {
     cg_tune_cfg best{0, 0};
-    if (cg_tune_forced(&best)) return cg_tune_cfg{best.seg, 0};
+    if (cg_tune_forced(&best)) {
+        if (best.variant >= 1 && !march_x2_ok(f, n0, n1)) best.variant = 0;
+        return best;
+    }
     if (!cg_autotune_enabled()) return best;
     std::string key = "march2d";
     cg_key_add(key, n0);
@@ -479,6 +485,7 @@ inline cg_tune_cfg tune_march2d(const Fused2D<T>& f, const SP<T>& s, int n0, int
     cg_key_add(key, (int)sizeof(T));
     cg_key_add(key, march_uniform_stride(f));
     cg_key_add(key, nsm);
+    cg_key_add(key, (int)march_x2_ok(f, n0, n1));
     if (cg_tune_lookup(key, &best)) return best;
     float tbest = 1e30f;
     for (int seg : {0, 8, 16, 24, 32, 48, 64}) {
@@ -491,6 +498,21 @@ inline cg_tune_cfg tune_march2d(const Fused2D<T>& f, const SP<T>& s, int n0, int
             best = cg_tune_cfg{seg, 0};
         }
     }
+    if (march_x2_ok(f, n0, n1))
+        for (int v : {1, 2})
+            for (int seg : {0, 16, 32, 48, 64, 96}) {
+                if (seg > n1 + 2) continue;
+                float t = time_launches(
+                    [&] { return launch_march2d_x2<T, false>(f, s, n0, n1, nsm, seg, true, st, false, v); }, st);
+                if (t >= 0.f) t *= 0.5f;  // per iteration
+                if (cg_tune_verbose())
+                    std::fprintf(stderr, "march2d tune %dx%d: two iterations per pass (variant %d), seg %d: %.1f us per iteration\n",
+                                 n0, n1, v, seg, t >= 0.f ? 1e3f * t / 3 : -1.f);
+                if (t >= 0.f && t < tbest) {
+                    tbest = t;
+                    best = cg_tune_cfg{seg, v};
+                }
+            }
     cudaGetLastError();
     cg_tune_store(key, best);
     return best;

@@ -173,9 +173,11 @@ int launch_velocity(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f, co
     apply_pre(v, pr);
     const SP<T> s = scalars<T>(g, p);
     if (res)
-        velocity_kernel<T, ND, true><<<range_grid<ND>(g, block), block, 0, ctx->stream>>>(v, s, g->n[0] + 1, g->n[1] + 1);
+        velocity_kernel<T, ND, true><<<range_grid<ND>(g, block), block, 0, ctx->stream>>>(v, s, body_fns<T>(g, p), g->n[0] + 1,
+                                                                                       g->n[1] + 1);
     else
-        velocity_kernel<T, ND, false><<<range_grid<ND>(g, block), block, 0, ctx->stream>>>(v, s, g->n[0] + 1, g->n[1] + 1);
+        velocity_kernel<T, ND, false><<<range_grid<ND>(g, block), block, 0, ctx->stream>>>(v, s, body_fns<T>(g, p), g->n[0] + 1,
+                                                                                        g->n[1] + 1);
     CG_CHECK_LAUNCH(ctx);
     return CG_OK;
 }
@@ -512,8 +514,23 @@ int pp_iterations_t(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* a, co
     std::memset(none, 0, sizeof(none));
     for (int d = 0; d < 2; ++d) cg_key_add(key, bc_V ? bc_V[d] : none[d]);
     cg_key_add(key, (int)fold);
+    // two iterations per pass (the tuner's variant 1) where no bc!(V) launch is needed between
+    // iterations: an even number of passes (a -> b, b -> a) leaves at least the last two
+    // iterations to the one-iteration kernel, so that a ends with the state after niter
+    // iterations and b with the state after niter - 1, as in the one-iteration form
+    const bool x2 = tc.variant >= 1 && (fold || !bc_V);
+    const int npass = x2 ? ((niter / 2 - 1) & ~1) : 0;
     return cg_graph_run(ctx, key, [&](cudaStream_t st) {
-        for (int it = 0; it < niter; ++it) {
+        for (int k = 0; k < npass; ++k) {
+            const Fused2D<T>& fk = (k % 2 == 0) ? fab : fba;
+            const int nsm = ctx->num_sms;
+            const bool last = 2 * k + 2 == niter;
+            const cudaError_t le = (res && last)
+                                       ? launch_march2d_x2<T, true>(fk, s, g->n[0], g->n[1], nsm, tc.seg, k > 0, st, k > 0, tc.variant)
+                                       : launch_march2d_x2<T, false>(fk, s, g->n[0], g->n[1], nsm, tc.seg, k > 0, st, k > 0, tc.variant);
+            if (le != cudaSuccess) return cg_fail(ctx, CG_ERR_CUDA, "fused2d x2 launch: %s", cudaGetErrorString(le));
+        }
+        for (int it = 2 * npass; it < niter; ++it) {
             const Fused2D<T>& fk = it == 0 ? fab0 : (it % 2 == 0) ? fab : fba;
             const int nsm = ctx->num_sms;
             const cudaError_t le = (res && it == niter - 1)

@@ -26,7 +26,8 @@ struct DC32 {
 
 // FP64 residuals of the current state; FP32 forcing of the correction problem.
 template <int ND>
-__global__ void defect_kernel(const SV<double> v, const SP<double> s, const DC32 w, int e0, int e1) {
+__global__ void defect_kernel(const SV<double> v, const SP<double> s, const BodyFn<double> bf, const DC32 w, int e0,
+                              int e1) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = ND > 2 ? blockIdx.z : 0;
@@ -111,11 +112,11 @@ __global__ void defect_kernel(const SV<double> v, const SP<double> s, const DC32
         rz = rz + (tyz(i, j + 1, k) - tyz(i, j, k)) * s.idx[1];
     }
     if (v.has_rho[0]) rx = rx - v.rho[0](i, j, k);
-    else if (s.fn[0].kind) rx = rx - body_fn(s, 0, ND, i, j, k);
+    else if (bf.fn[0].kind) rx = rx - body_fn(bf, 0, ND, i, j, k);
     if (v.has_rho[1]) ry = ry - v.rho[1](i, j, k);
-    else if (s.fn[1].kind) ry = ry - body_fn(s, 1, ND, i, j, k);
+    else if (bf.fn[1].kind) ry = ry - body_fn(bf, 1, ND, i, j, k);
     if (ND > 2 && v.has_rho[2]) rz = rz - v.rho[2](i, j, k);
-    else if (ND > 2 && s.fn[2].kind) rz = rz - body_fn(s, 2, ND, i, j, k);
+    else if (ND > 2 && bf.fn[2].kind) rz = rz - body_fn(bf, 2, ND, i, j, k);
     v.rV[0](i, j, k) = rx;
     v.rV[1](i, j, k) = ry;
     w.rho[0](i, j, k) = (float)(-rx);
@@ -354,6 +355,7 @@ int cg_stokes_solve_dc(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f,
     v64.has_rV = 1;
     v64.has_divV = 1;
     const SP<double> s64 = scalars<double>(g, p);
+    const BodyFn<double> bf64 = body_fns<double>(g, p);
     DC32 d32;
     std::memset(&d32, 0, sizeof(d32));
     d32.fP = cg_view<float>(w.fP);
@@ -375,9 +377,7 @@ int cg_stokes_solve_dc(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f,
     }
     f32.inv_eta = w.ieta;
     const SV<float> v32 = views<float>(&f32, nd);
-    // the correction problem's momentum forcing is the FP32 array -R_V; no body-force function
-    SP<float> s32 = scalars<float>(g, p);
-    for (int d = 0; d < 3; ++d) s32.fn[d].kind = CG_FN_NONE;
+    const SP<float> s32 = scalars<float>(g, p);
 
     cg_bc bc0[3];
     for (int d = 0; d < nd; ++d) {
@@ -500,9 +500,27 @@ int cg_stokes_solve_dc(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f,
     const cg_tune_cfg tc = nd == 2 ? tune_march2d(fa, s32, g->n[0], g->n[1], ctx->num_sms, ctx->stream)
                                    : tune_march3d(ga, s32, g->n[0], g->n[1], g->n[2], ctx->num_sms, ctx->stream);
     cg_key_add(key, tc);
+    // two iterations per pass (the tuner's variant 1) where bc!(dV) is folded into the reads:
+    // passes alternate A -> B and B -> A, and an odd count of passes leaves its last two
+    // iterations to the one-iteration kernel, so that the chunk ends in A
+    const bool x2 = nd == 2 && fold && tc.variant >= 1;
+    const int npass = x2 ? (nchunk / 2) - ((nchunk / 2) & 1) : 0;
     auto chunk = [&]() {
         return cg_graph_run(ctx, key, [&](cudaStream_t st) {
-            for (int it = 0; it < nchunk; ++it) {
+            for (int k = 0; k < npass; ++k) {
+                const bool last = 2 * k + 2 == nchunk;
+                const Fused2D<float>& fk = (k % 2 == 0) ? fa : fb;
+                const int nsm = ctx->num_sms;
+                const cudaError_t le =
+                    last ? launch_march2d_x2<float, true>(fk, s32, g->n[0], g->n[1], nsm, tc.seg, k > 0, st, k > 0, tc.variant)
+                         : launch_march2d_x2<float, false>(fk, s32, g->n[0], g->n[1], nsm, tc.seg, k > 0, st, k > 0, tc.variant);
+                if (le != cudaSuccess) return cg_fail(ctx, CG_ERR_CUDA, "fused2d x2 launch: %s", cudaGetErrorString(le));
+                if (last) {
+                    int r = cg_bc_apply_impl(ctx, g, nd, w.dV, bc0, true);
+                    if (r) return r;
+                }
+            }
+            for (int it = 2 * npass; it < nchunk; ++it) {
                 const bool last = it == nchunk - 1;
                 if (nd == 2) {
                     const Fused2D<float>& fk = it == 0 ? fa0 : (it % 2 == 0) ? fa : fb;
@@ -532,8 +550,8 @@ int cg_stokes_solve_dc(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f,
     double outer_err[4] = {0, 0, 0, 0};
     for (int outer = 0; outer <= max_outer; ++outer) {
         // FP64 defect of the current state
-        if (nd == 2) defect_kernel<2><<<grid3, block, 0, ctx->stream>>>(v64, s64, d32, e0, e1);
-        else defect_kernel<3><<<grid3, block, 0, ctx->stream>>>(v64, s64, d32, e0, e1);
+        if (nd == 2) defect_kernel<2><<<grid3, block, 0, ctx->stream>>>(v64, s64, bf64, d32, e0, e1);
+        else defect_kernel<3><<<grid3, block, 0, ctx->stream>>>(v64, s64, bf64, d32, e0, e1);
         CG_CHECK_LAUNCH(ctx);
         if ((rc = cg_bc_apply_impl(ctx, g, nd, f->r_V, rbc))) return rc;
         if ((rc = cg_maxabs_enqueue(ctx, nd + 1 + nt, red64))) return rc;

@@ -36,7 +36,13 @@ struct SP {  // scalars in the field precision
     T eta, eta_ve, G, dt, dtau_Pr, dtau_r, nu_dtau, lam;
     T inv_Gdt, third;
     T idx[3];
-    // body force per velocity component as a device FunctionField, and the grid's coordinates
+};
+
+// Body force per velocity component as a device FunctionField, and the grid's coordinates. A
+// separate kernel argument of the two kernels that evaluate it (the velocity update and the
+// FP64 defect): the march kernels keep the small SP as their scalar argument.
+template <class T>
+struct BodyFn {
     FnDev<T> fn[3];
     T org[3], dx[3];
 };
@@ -70,7 +76,7 @@ __device__ __forceinline__ T fn_eval(const FnDev<T>& f, int nd, const T* x) {
 // Body-force function of velocity component `comp` at its point (i, j, k): Vertex along comp,
 // Center along the other dimensions.
 template <class T>
-__device__ __forceinline__ T body_fn(const SP<T>& s, int comp, int nd, int i, int j, int k) {
+__device__ __forceinline__ T body_fn(const BodyFn<T>& s, int comp, int nd, int i, int j, int k) {
     const int I[3] = {i, j, k};
     T x[3] = {T(0), T(0), T(0)};
     for (int e = 0; e < nd; ++e) x[e] = grid_coord(s.org[e], s.dx[e], I[e], e == comp);
@@ -128,14 +134,20 @@ SP<T> scalars(const cg_grid* g, const cg_stokes_params* p) {
     s.lam = (T)p->lambda_rhoCp;
     s.inv_Gdt = T(1) / (s.G * s.dt);
     s.third = T(1) / T(3);
-    for (int d = 0; d < 3; ++d) {
-        s.idx[d] = (T)g->inv_spacing[d];
-        s.org[d] = (T)g->origin[d];
-        s.dx[d] = (T)g->spacing[d];
-        s.fn[d].kind = p->rho_g_fn[d].kind;
-        for (int q = 0; q < 8; ++q) s.fn[d].p[q] = (T)p->rho_g_fn[d].p[q];
-    }
+    for (int d = 0; d < 3; ++d) s.idx[d] = (T)g->inv_spacing[d];
     return s;
+}
+
+template <class T>
+BodyFn<T> body_fns(const cg_grid* g, const cg_stokes_params* p) {
+    BodyFn<T> b;
+    for (int d = 0; d < 3; ++d) {
+        b.org[d] = (T)g->origin[d];
+        b.dx[d] = (T)g->spacing[d];
+        b.fn[d].kind = p->rho_g_fn[d].kind;
+        for (int q = 0; q < 8; ++q) b.fn[d].p[q] = (T)p->rho_g_fn[d].p[q];
+    }
+    return b;
 }
 
 template <class T>
@@ -259,7 +271,7 @@ __global__ void stress_kernel(const SV<T> v, const SP<T> s, int e0, int e1) {
 
 // update_velocity! at one point.
 template <class T, int ND, bool WRITE_RES>
-__global__ void velocity_kernel(const SV<T> v, const SP<T> s, int e0, int e1) {
+__global__ void velocity_kernel(const SV<T> v, const SP<T> s, const BodyFn<T> bf, int e0, int e1) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = ND > 2 ? blockIdx.z : 0;
@@ -288,11 +300,11 @@ __global__ void velocity_kernel(const SV<T> v, const SP<T> s, int e0, int e1) {
         rz = rz + (tyz(i, j + 1, k) - tyz(i, j, k)) * s.idx[1];
     }
     if (v.has_rho[0]) rx = rx - v.rho[0](i, j, k);
-    else if (s.fn[0].kind) rx = rx - body_fn(s, 0, ND, i, j, k);
+    else if (bf.fn[0].kind) rx = rx - body_fn(bf, 0, ND, i, j, k);
     if (v.has_rho[1]) ry = ry - v.rho[1](i, j, k);
-    else if (s.fn[1].kind) ry = ry - body_fn(s, 1, ND, i, j, k);
+    else if (bf.fn[1].kind) ry = ry - body_fn(bf, 1, ND, i, j, k);
     if (ND > 2 && v.has_rho[2]) rz = rz - v.rho[2](i, j, k);
-    else if (ND > 2 && s.fn[2].kind) rz = rz - body_fn(s, 2, ND, i, j, k);
+    else if (ND > 2 && bf.fn[2].kind) rz = rz - body_fn(bf, 2, ND, i, j, k);
     if (WRITE_RES && v.has_rV) {
         v.rV[0](i, j, k) = rx;
         v.rV[1](i, j, k) = ry;
@@ -774,6 +786,228 @@ __global__ void __launch_bounds__(128, MINB) march2d_kernel(const Fused2D<T> f, 
     }
 }
 
+// ---- two PT iterations per pass (temporal blocking) -----------------------------------------
+//
+// march2d_x2_kernel takes two consecutive iterations of march2d_kernel in one pass over the
+// rows. Stage A is the first iteration: it reads the `in` buffers (through bc!(V) when f.bc.on
+// and fold_a) as march2d_kernel does and keeps its results in registers. Stage B is the second:
+// it reads A's results two rows behind A (through bc!(V) when f.bc.on, since A's velocities are
+// the ones bc!(V) would patch) and the constant inputs, and writes the `out` buffers. A pass
+// moves the bytes of one iteration for two. A warp owns 28 columns: lane l holds column
+// c0 - 2 + l. A's results are valid on lanes 1..30, B's on the owned lanes 2..29. A marches rows
+// js-2 .. je+1 and B rows js-1 .. je; each stage's first row only starts its state.
+// Points outside the launch range [0, n+1] keep their values: A passes its inputs on there (the
+// two-launch sequence passes on the intermediate buffer's values, which are the input buffer's
+// wherever the two buffers agree outside the launch range, as the callers' pairs do), and B
+// leaves the out buffers untouched there. Every operation is march2d_kernel's, in its order,
+// so a pass equals two launches of it bit for bit.
+
+// Marching state of one iteration at the current row j: V of row j (through bc!(V)), 1/eta of
+// row j (own lane and left lane) and of row j-1, the new P and tau_yy of cell row j-1 and the
+// new tau_xy of vertex row j.
+template <class T>
+struct MState {
+    T Vx, Vy, ie, ieL, ie_p, Pn_p, Tyyn_p, txy;
+};
+
+// Results of one step at row j: new cell row j, new vertex row j+1, new velocity of row j (its
+// input outside the launch range) and the momentum residuals of row j.
+template <class T>
+struct MStep {
+    CellNew<T> c;
+    T tn, vx, vy, rx, ry;
+};
+
+// One step of one iteration at row j: the body of march2d_kernel's loop. cur holds row j+1's
+// vertex inputs (Vx, Vy as stored) and row j's cell inputs; vnx, vny are row j+2's stored
+// velocities (the source of a plane at row j+1 = 0). st advances to row j+1.
+template <class T>
+__device__ __forceinline__ MStep<T> x2_step(const Fused2D<T>& f, const SP<T>& s, MState<T>& st, MarchRow<T>& cur,
+                                           T vnx, T vny, int i, int j, int e0, int e1, bool xfold, bool yfold, int ylo,
+                                           int yhi) {
+    constexpr unsigned FULL = 0xffffffffu;
+    if (yfold && j + 1 >= ylo && j + 1 <= yhi) {
+        cur.Vx = fold_y(f.bc, 0, i, j + 1, cur.Vx, st.Vx, vnx);
+        cur.Vy = fold_y(f.bc, 1, i, j + 1, cur.Vy, st.Vy, vny);
+    }
+    if (xfold && j + 1 >= 0 && j + 1 <= e1 + 1) {  // x-planes over the tangential rows 0..n+2
+        cur.Vx = fold_x(f.bc, 0, i, cur.Vx);
+        cur.Vy = fold_x(f.bc, 1, i, cur.Vy);
+    }
+    MStep<T> o;
+    // new cell (i, j)
+    const T vxR = __shfl_down_sync(FULL, st.Vx, 1);
+    o.c = march_cell(s, f.has_fP != 0, st.Vx, vxR, st.Vy, cur.Vy, st.ie, cur.P, cur.txx, cur.txo, cur.tyy, cur.tyo,
+                     cur.fp);
+    const bool in_range = i >= 0 && i <= e0 && j >= 0 && j <= e1;
+    if (!in_range) {
+        o.c.P = cur.P;
+        o.c.txx = cur.txx;
+        o.c.tyy = cur.tyy;
+    }
+    // new vertex (i, j+1)
+    const T vyL = __shfl_up_sync(FULL, cur.Vy, 1);
+    const T ieL_n = __shfl_up_sync(FULL, cur.ie, 1);
+    o.tn = (i < 0 || i > e0 || j + 1 < 0 || j + 1 > e1)
+               ? cur.txy
+               : march_vertex(s, st.Vx, cur.Vx, vyL, cur.Vy, st.ieL, st.ie, ieL_n, cur.ie, cur.txy, cur.txyo);
+    // velocity (i, j): r_V = -d(P) + d(tau_dd) + d(tau_xy) - rho g, left to right
+    const T PL = __shfl_up_sync(FULL, o.c.P, 1);
+    const T TxxL = __shfl_up_sync(FULL, o.c.txx, 1);
+    const T txyR = __shfl_down_sync(FULL, st.txy, 1);
+    T rx = radd(-rmul(rsub(o.c.P, PL), s.idx[0]), rmul(rsub(o.c.txx, TxxL), s.idx[0]));
+    rx = radd(rx, rmul(rsub(o.tn, st.txy), s.idx[1]));
+    T ry = radd(-rmul(rsub(o.c.P, st.Pn_p), s.idx[1]), rmul(rsub(o.c.tyy, st.Tyyn_p), s.idx[1]));
+    ry = radd(ry, rmul(rsub(txyR, st.txy), s.idx[0]));
+    if (f.has_rho) {
+        rx = rsub(rx, cur.rhox);
+        ry = rsub(ry, cur.rhoy);
+    }
+    o.rx = rx;
+    o.ry = ry;
+    o.vx = in_range ? radd(st.Vx, rmul(rx, rmul(s.nu_dtau, radd(fmin(st.ieL, st.ie), s.inv_Gdt)))) : st.Vx;
+    o.vy = in_range ? radd(st.Vy, rmul(ry, rmul(s.nu_dtau, radd(fmin(st.ie_p, st.ie), s.inv_Gdt)))) : st.Vy;
+    // advance one row
+    st.Vx = cur.Vx;
+    st.Vy = cur.Vy;
+    st.ie_p = st.ie;
+    st.ie = cur.ie;
+    st.ieL = ieL_n;
+    st.Pn_p = o.c.P;
+    st.Tyyn_p = o.c.tyy;
+    st.txy = o.tn;
+    return o;
+}
+
+template <class T, class Ix, bool UNI, bool WRITE_RES, int MINB = 1>
+__global__ void __launch_bounds__(128, MINB) march2d_x2_kernel(const Fused2D<T> f, const SP<T> s, int e0, int e1,
+                                                               int nstrip, int nwarps, int seg_rows, long s1u,
+                                                               int fold_a) {
+    constexpr unsigned FULL = 0xffffffffu;
+    cg_dep_wait();
+    cg_dep_release();
+    const int lane = threadIdx.x & 31;
+    const int gw = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    if (gw >= nwarps) return;  // whole warp
+    const int strip = gw % nstrip;
+    const int js = (gw / nstrip) * seg_rows;
+    if (js > e1) return;  // whole warp
+    const int je = min(js + seg_rows - 1, e1);
+    const int i = strip * 28 - 2 + lane;  // >= -2: column -2 lies outside the arrays, never read
+    const MAt<T, Ix, UNI> at{i, (Ix)s1u};
+    const bool own = lane >= 2 && lane <= 29 && i <= e0;
+    const bool inV = i >= -1 && i <= e0 + 1;  // V, 1/eta, tau_xy readable
+    const bool inC = i >= -1 && i <= e0;      // cell inputs, tau_xy_old readable
+    // bc!(V) folded into the reads: the strip holds an x-plane / the rows js-3 .. je+3 hold a y-plane
+    const bool bcon = f.bc.on != 0;
+    const bool xb = bcon && (strip == 0 || strip * 28 + 30 >= e0);
+    const bool ylow = js <= 3, yhigh = je + 3 >= e1;
+    const bool yb = bcon && (ylow || yhigh);
+    const int ylo = ylow ? 0 : e1, yhi = yhigh ? e1 + 1 : 1;
+    const bool xa = xb && fold_a, ya = yb && fold_a;
+    // row j's cell inputs and row j+1's vertex inputs; rows below -1 read as zero (the first
+    // segment's first row is -2)
+    auto load = [&](int j) { return march_load(f, at, j, e1, inV && j >= -2, inC && j >= -1); };
+
+    // stage A's state at row js-2. Segments start at 0 or at >= 4, so no y-plane lies on rows
+    // js-2 and js-1; the velocity of the first row of each stage is discarded, so its inputs
+    // from rows below are not needed.
+    MState<T> a;
+    {
+        const int j0 = js - 2;
+        const bool ok = j0 >= -1;
+        a.Vx = at.ld(f.Vx_in, j0, inV && ok);
+        a.Vy = at.ld(f.Vy_in, j0, inV && ok);
+        a.ie = at.ld(f.ieta, j0, inV && ok);
+        if (xa && j0 >= 0) {
+            a.Vx = fold_x(f.bc, 0, i, a.Vx);
+            a.Vy = fold_x(f.bc, 1, i, a.Vy);
+        }
+        a.ieL = __shfl_up_sync(FULL, a.ie, 1);
+        a.ie_p = a.Pn_p = a.Tyyn_p = a.txy = T(0);
+    }
+    MState<T> b;
+    b.Vx = b.Vy = b.ie = b.ieL = b.ie_p = b.Pn_p = b.Tyyn_p = b.txy = T(0);
+    MarchRow<T> cur = load(js - 2);
+    // A's results queued for B: velocity of the previous row, cells and vertices of two rows
+    T qVx = T(0), qVy = T(0), qT1 = T(0), qT2 = T(0);
+    CellNew<T> qC1, qC2;
+    qC1.P = qC1.txx = qC1.tyy = qC1.dvP = T(0);
+    qC2 = qC1;
+    for (int ja = js - 2; ja <= je + 2; ++ja) {
+        const bool astep = ja <= je + 1;
+        const bool more = ja + 1 <= je + 1;
+        MarchRow<T> nxt;
+        if (more) nxt = load(ja + 1);
+        const int jb = ja - 2;
+        const bool bstep = jb >= js - 1;
+        // B's constant inputs: row jb+1's 1/eta and tau_xy_old, row jb's cell inputs
+        MarchRow<T> cb;
+        if (bstep) {
+            const int jn = jb + 1;
+            cb.ie = at.ld(f.ieta, jn, inV && jn <= e1 + 1);
+            cb.txyo = at.ld(f.txy_o, jn, inC && jn <= e1);
+            const bool c = inC && jb <= e1;
+            cb.txo = at.ld(f.txx_o, jb, c);
+            cb.tyo = at.ld(f.tyy_o, jb, c);
+            cb.fp = f.has_fP ? at.ld(f.fP, jb, c) : T(0);
+            cb.rhox = f.has_rho ? at.ld(f.rhox, jb, c) : T(0);
+            cb.rhoy = f.has_rho ? at.ld(f.rhoy, jb, c) : T(0);
+        }
+        MStep<T> oa;
+        if (astep) {
+            oa = x2_step(f, s, a, cur, more ? nxt.Vx : T(0), more ? nxt.Vy : T(0), i, ja, e0, e1, xa, ya, ylo, yhi);
+        } else {
+            oa.vx = oa.vy = oa.tn = oa.rx = oa.ry = T(0);
+            oa.c = qC1;
+        }
+        if (ja == js - 1) {  // B's state at row js-1: A's velocity there
+            b.Vx = oa.vx;
+            b.Vy = oa.vy;
+            if (xb && ja >= 0) {
+                b.Vx = fold_x(f.bc, 0, i, b.Vx);
+                b.Vy = fold_x(f.bc, 1, i, b.Vy);
+            }
+            b.ie = at.ld(f.ieta, ja, inV);
+            b.ieL = __shfl_up_sync(FULL, b.ie, 1);
+        }
+        if (bstep) {
+            // row jb+1's velocities and vertex from A, row jb's cells from A
+            cb.Vx = qVx;
+            cb.Vy = qVy;
+            cb.txy = qT2;
+            cb.P = qC2.P;
+            cb.txx = qC2.txx;
+            cb.tyy = qC2.tyy;
+            const MStep<T> ob = x2_step(f, s, b, cb, oa.vx, oa.vy, i, jb, e0, e1, xb, yb, ylo, yhi);
+            if (own) {
+                if (jb >= js) {
+                    at.st(f.P_out, jb, ob.c.P);
+                    at.st(f.txx_out, jb, ob.c.txx);
+                    at.st(f.tyy_out, jb, ob.c.tyy);
+                    if (jb + 1 <= je) at.st(f.txy_out, jb + 1, ob.tn);
+                    if (WRITE_RES) {
+                        at.st(f.divV, jb, ob.c.dvP);
+                        at.st(f.rVx, jb, ob.rx);
+                        at.st(f.rVy, jb, ob.ry);
+                    }
+                    at.st(f.Vx_out, jb, ob.vx);
+                    at.st(f.Vy_out, jb, ob.vy);
+                } else {
+                    at.st(f.txy_out, js, ob.tn);  // vertex row js, computed by B's first row
+                }
+            }
+        }
+        qC2 = qC1;
+        qC1 = oa.c;
+        qT2 = qT1;
+        qT1 = oa.tn;
+        qVx = oa.vx;
+        qVy = oa.vy;
+        if (more) cur = nxt;
+    }
+}
+
 // The arrays of a fused view, for host-side checks.
 template <class T>
 inline void fused_arrays(const Fused2D<T>& f, const DF<T>* out[22]) {
@@ -856,6 +1090,57 @@ inline cudaError_t launch_march2d(const Fused2D<T>& f, const SP<T>& s, int n0, i
     }
     if (s1u) return launch_march2d_ix<T, long, true, WRITE_RES>(f, s, n0, n1, num_sms, seg_rows, s1u, st, dep);
     return launch_march2d_ix<T, long, false, WRITE_RES>(f, s, n0, n1, num_sms, seg_rows, 0, st, dep);
+}
+
+// Launch of the two-iteration kernel (march2d_x2_kernel) over [0, n0+1] x [0, n1+1]: two PT
+// iterations, `in` -> `out`; fold_a: the first iteration reads its velocities through bc!(V).
+// Only for views whose arrays share one row stride and whose offsets fit in 32 bits (the
+// callers check march_x2_ok). seg_rows <= 0 picks one wave of warps, 8..64 rows per segment.
+// MINB: 4 blocks per SM (up to 128 registers, no spills) or 5 (96 registers, 24 bytes spilled).
+template <class T, bool WRITE_RES, int MINB>
+inline cudaError_t launch_march2d_x2_mb(const Fused2D<T>& f, const SP<T>& s, int n0, int n1, int num_sms, int seg_rows,
+                                        bool fold_a, cudaStream_t st, bool dep) {
+    auto kern = march2d_x2_kernel<T, int, true, WRITE_RES, MINB>;
+    const long s1u = march_uniform_stride(f);
+    const int e0 = n0 + 1, e1 = n1 + 1;
+    const int nstrip = cg_div_up(e0 + 1, 28);
+    if (seg_rows <= 0) {
+        static const int bps = [] {
+            int nb = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march2d_x2_kernel<T, int, true, WRITE_RES, MINB>, 128,
+                                                              0) != cudaSuccess)
+                nb = 0;
+            return nb > 0 ? nb : 4;
+        }();
+        const long capacity = (long)num_sms * bps * 4;
+        const long nseg = capacity / nstrip > 1 ? capacity / nstrip : 1;
+        seg_rows = (int)((e1 + 1 + nseg - 1) / nseg);
+        seg_rows = seg_rows < 8 ? 8 : (seg_rows > 64 ? 64 : seg_rows);
+    }
+    if (seg_rows < 4) seg_rows = 4;  // no y-plane may lie on a stage's first row
+    const int nseg = cg_div_up(e1 + 1, seg_rows);
+    const int nwarps = nstrip * nseg;
+    return cg_launch(kern, dim3(cg_div_up(nwarps, 4)), dim3(128), 0, st, dep, f, s, e0, e1, nstrip, nwarps, seg_rows, s1u,
+                     (int)fold_a);
+}
+
+// variant 1: 4 blocks per SM; variant 2: 5 blocks per SM (the autotuner's 2D variants)
+template <class T, bool WRITE_RES>
+inline cudaError_t launch_march2d_x2(const Fused2D<T>& f, const SP<T>& s, int n0, int n1, int num_sms, int seg_rows,
+                                     bool fold_a, cudaStream_t st, bool dep = false, int variant = 1) {
+    if (variant == 2) return launch_march2d_x2_mb<T, WRITE_RES, 5>(f, s, n0, n1, num_sms, seg_rows, fold_a, st, dep);
+    return launch_march2d_x2_mb<T, WRITE_RES, 4>(f, s, n0, n1, num_sms, seg_rows, fold_a, st, dep);
+}
+
+// Whether the two-iteration kernel can take a view: one shared row stride, 32-bit offsets,
+// CG_MARCH_X2 not set to 0.
+template <class T>
+inline bool march_x2_ok(const Fused2D<T>& f, int n0, int n1) {
+    static const bool on = [] {
+        const char* e = std::getenv("CG_MARCH_X2");
+        return !(e && e[0] == '0');
+    }();
+    return on && march_uniform_stride(f) != 0 && march_fits_int(f, n0 + 1, n1 + 1);
 }
 
 }  // namespace cgk

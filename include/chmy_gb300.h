@@ -140,6 +140,11 @@ CG_API int cg_field_free(cg_ctx* ctx, cg_field* f);
 CG_API int cg_field_upload(cg_ctx* ctx, const cg_field* f, const void* host_dense);
 CG_API int cg_field_download(cg_ctx* ctx, const cg_field* f, void* host_dense);
 
+/* The device's FP64 FMA throughput (FLOP/s, 2 per FMA), measured with CUDA events on the
+ * context's stream: the roofline denominator of the kernels bound by the FP64 pipe. A measuring
+ * aid with no counterpart in the reference. */
+CG_API int cg_fp64_peak(cg_ctx* ctx, double* flops);
+
 /* ---- boundary conditions ---------------------------------------------------------- */
 
 /* bc!(arch, grid, batch) for a FieldBatch of `nfields` fields
@@ -333,7 +338,11 @@ CG_API int cg_stokes_pt_iterations(cg_ctx* ctx, const cg_grid* grid, const cg_st
  * iteration is one fused launch: update_stress! and update_velocity! together, in a kernel
  * that marches over rows (2D) or planes (3D). It reads V, P, tau from `a` and writes them to
  * `b`, then from `b` to `a`, and each launch is followed by bc!(V). `niter` must be even (the
- * result is in `a`). All other fields (tau_old, inv_eta, rho_g, divV, r_V) are taken from
+ * result is in `a`; `b` holds the state one iteration earlier). Points outside the launch range
+ * [0, n+1]^N are never written: `a` and `b` must agree there (b a copy of a, for instance), as
+ * the in-place reference loop keeps one value per point. In 2D the autotuner may take two
+ * iterations per launch (a kernel that keeps the intermediate state in registers) where no
+ * bc!(V) launch is needed between iterations; the results are the same bits. All other fields (tau_old, inv_eta, rho_g, divV, r_V) are taken from
  * `a`; inv_eta is required. divV and r_V are written on the last iteration. Every operation
  * is rounded once, in the order of the reference kernels, with no contraction into FMA: the
  * values are those of a CPU evaluation with -ffp-contract=off. */

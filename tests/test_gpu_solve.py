@@ -361,3 +361,23 @@ def test_example_time_loop_with_thermal_coupling(arch):
     o.precision = _abi.CG_F32
     rc = arch.lib.cg_stokes_solve_thermal(arch.ctx, ctypes.byref(g), ctypes.byref(dd), ctypes.byref(p), bcv, ctypes.byref(bcT), ctypes.byref(o), ctypes.byref(r))
     assert rc == _abi.CG_ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("n", [64, 130])
+def test_fp32_defect_correction_two_iterations_per_pass(arch, monkeypatch, n):
+    """The FP32 PT chunks of the defect-correction solve with two iterations per pass (variants 1
+    and 2 of the 2D layout) and with one (variant 0): the same iteration and cycle counts and the
+    same bits of every solution field."""
+    pb = stokes2d_inclusions(n, ncheck=n // 4)
+    out = []
+    for layout in ("0:0", "0:1", "16:2"):
+        monkeypatch.setenv("CG_MARCH_LAYOUT", layout)
+        s = StokesSolver(arch, pb)
+        s.apply_bc()
+        r = s.solve(precision=_abi.CG_F32, max_outer=8, inner_rtol=1e-5)
+        assert r.converged == 1
+        out.append((r.iterations, r.outer, [f.to_numpy() for f in s.fields["V"] + s.fields["tau"]] + [s.fields["P"].to_numpy()]))
+    for it, outer, arrays in out[1:]:
+        assert (it, outer) == (out[0][0], out[0][1])
+        for a, b in zip(arrays, out[0][2]):
+            np.testing.assert_array_equal(a, b)

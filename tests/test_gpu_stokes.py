@@ -21,7 +21,7 @@ C_, V_ = Center(), Vertex()
 class StokesSet:
     """Seeded random VE Stokes state on host and device."""
 
-    def __init__(self, arch, dims, T, seed, var_eta, rho=True, thermal=False):
+    def __init__(self, arch, dims, T, seed, var_eta, rho=True, thermal=False, pitch_align=0):
         rng = np.random.default_rng(seed)
         nd = len(dims)
         self.grid = UniformGrid(origin=(T(-1),) * nd, extent=(T(2),) * nd, dims=dims, dtype=T)
@@ -48,9 +48,9 @@ class StokesSet:
         self.d = {}
         for k, v in self.h.items():
             if isinstance(v, list):
-                self.d[k] = [to_gpu(arch, f) if f is not None else None for f in v]
+                self.d[k] = [to_gpu(arch, f, pitch_align) if f is not None else None for f in v]
             else:
-                self.d[k] = to_gpu(arch, v)
+                self.d[k] = to_gpu(arch, v, pitch_align)
 
     def host_desc(self):
         return stokes_desc(**self.h)
@@ -169,26 +169,28 @@ def test_pt_iterations_graph(arch, T, dims, var_eta):
         assert abs(err[i] - want[i]) <= rtol_for(T) * niter * 10 * max(abs(want[i]), 1.0)
 
 
-def _pp_run(arch, T, dims, bcs, niter, seed=31):
+def _pp_run(arch, T, dims, bcs, niter, seed=31, pitch_align=0):
     """niter fused ping-pong iterations (cg_stokes_pt_iterations_pp) against niter x
     (update_stress!, update_velocity!, bc!(V)) on the oracle. Returns the set, the partner
-    buffers and the oracle's V after niter - 1 iterations."""
-    s = StokesSet(arch, dims, T, seed, True, rho=True)
+    buffers and the oracle's V after niter - 1 iterations. pitch_align: the device fields' row
+    alignment (bytes; 0 = Chmy's dense layout)."""
+    s = StokesSet(arch, dims, T, seed, True, rho=True, pitch_align=pitch_align)
     g2 = s.grid
     rho_full = [random_field(g2, f.loc, T, np.random.default_rng(5)) for f in vec_fields(g2, T)]
     s.h["rho_g"] = rho_full
-    s.d["rho_g"] = [to_gpu(arch, f) for f in rho_full]
+    s.d["rho_g"] = [to_gpu(arch, f, pitch_align) for f in rho_full]
     ie = NpField(g2, C_, T)
     ie.a[...] = (1.0 / s.h["eta"].a).astype(T)
     s.h["inv_eta"] = ie
-    s.d["inv_eta"] = to_gpu(arch, ie)
+    s.d["inv_eta"] = to_gpu(arch, ie, pitch_align)
     p = pt_params(g2, True)
     g = g2.desc()
     bc_apply(g2, s.h["V"], bcs)
     for f, d in zip(s.h["V"], s.d["V"]):
         d.from_numpy(f.a)
     # partner buffers for V, P, tau hold the same initial state
-    partner = {k: ([to_gpu(arch, f) for f in s.h[k]] if isinstance(s.h[k], list) else to_gpu(arch, s.h[k])) for k in ("V", "P", "tau")}
+    partner = {k: ([to_gpu(arch, f, pitch_align) for f in s.h[k]] if isinstance(s.h[k], list) else to_gpu(arch, s.h[k], pitch_align))
+               for k in ("V", "P", "tau")}
     hd, da = s.host_desc(), s.dev_desc()
     from _oracle import stokes_desc as sd
 
@@ -317,3 +319,30 @@ def test_pt_iterations_thermal(arch, T, dims, niter):
         dv = s.d[name] if isinstance(s.d[name], list) else [s.d[name]]
         for a, b in zip(dv, hv):
             assert_close(a, b, rtol_for(T) * niter * 10, f"thermal PT {name}")
+
+
+@pytest.mark.parametrize("T", TYPES)
+@pytest.mark.parametrize("layout", ["0:1", "0:2", "8:1", "40:2"])
+@pytest.mark.parametrize("kind", ["neumann_vertex", "one_sided", "mixed"])
+@pytest.mark.parametrize("dims", [(28, 29), (57, 30), (29, 61), (2, 3), (85, 9)])
+@pytest.mark.parametrize("niter", [6, 10])
+def test_fused_two_iterations_per_pass(arch, monkeypatch, T, layout, kind, dims, niter):
+    """The two-iterations-per-pass kernel (march2d_x2_kernel, forced with CG_MARCH_LAYOUT: segment
+    length : variant) in the ping-pong loop: both buffers equal the oracle's states after niter
+    and niter - 1 iterations bit for bit, for every rule mix, strip edges of its 28-column strips
+    (28, 56, 84) and segment edges."""
+    monkeypatch.setenv("CG_MARCH_LAYOUT", layout)
+    # rows padded to 512 bytes: every array of these grids shares one row stride, which the
+    # two-iteration kernel needs
+    s, partner, prev, _ = _pp_run(arch, T, dims, _bc_mix(kind), niter, seed=53, pitch_align=512)
+    strides = {f.data.stride()[-2] for v in s.d.values() for f in (v if isinstance(v, list) else [v]) if f is not None}
+    assert len(strides) == 1, strides
+    for name in ("V", "P", "tau", "divV", "r_V"):
+        hv = s.h[name] if isinstance(s.h[name], list) else [s.h[name]]
+        dv = s.d[name] if isinstance(s.d[name], list) else [s.d[name]]
+        for a, b in zip(dv, hv):
+            if b is not None:
+                assert_close(a, b, 0.0, f"x2 {layout} {kind} {name}", exact=True)
+    for a, b in zip(partner["V"], prev):
+        got = a.to_numpy()
+        assert np.array_equal(got.view(np.uint8), b.view(np.uint8)), f"partner V {kind}: max diff {np.max(np.abs(got - b))}"
