@@ -92,6 +92,34 @@ def committed_traffic(name: str):
     return None
 
 
+def committed_fp64_flops(unit: str):
+    """FP64 FLOPs per cell of one unit (`fp64_flops_per_cell: <unit> <number>`) from
+    profiles/fp64_kernels.md: 2 x DFMA + DADD + DMUL counted by ncu on the same kernels."""
+    p = ROOT / "profiles" / "fp64_kernels.md"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        parts = line.strip().split()
+        if len(parts) == 3 and parts[0] == "fp64_flops_per_cell:" and parts[1] == unit:
+            try:
+                return float(parts[2])
+            except ValueError:
+                return None
+    return None
+
+
+def fp64_roofline(unit: str, cells: float, units: float, seconds: float, peak_flops: float):
+    """The FP64-pipe roofline of an FP64-bound entry: FLOPs (per cell x cells x units) over its
+    measured time, against the device's FP64 FMA peak measured live (cg_fp64_peak)."""
+    fpc = committed_fp64_flops(unit)
+    if fpc is None or seconds <= 0 or not peak_flops:
+        return None
+    achieved = fpc * cells * units / seconds
+    return {"bound": "fp64", "achieved": achieved / 1e12, "peak": peak_flops / 1e12, "unit": "TFLOP/s",
+            "frac": achieved / peak_flops, "flops_per_cell": fpc, "peak_kind": "measured (cg_fp64_peak)",
+            "flops_source": "profiles/fp64_kernels.md (ncu DFMA/DADD/DMUL counts)"}
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled every 200 ms in a background thread."""
 
@@ -442,8 +470,11 @@ def run_ours(args, rank, world, dist):
         reset_device()
         r64 = solver.solve(precision=_abi.CG_F64)
         err_vs_fp64 = state_difference(dc_state, snapshot_state(solver), 2)
+        fpk = ctypes.c_double()
+        arch.call("cg_fp64_peak", ctypes.byref(fpk))
         fp64 = {"s": r64.seconds, "iterations": r64.iterations, "converged": r64.converged, "err": [r64.err[i] for i in range(3)],
-                "t_eff_gbs": A64 * n * n * 8 * r64.iterations / r64.seconds / 1e9}
+                "t_eff_gbs": A64 * n * n * 8 * r64.iterations / r64.seconds / 1e9,
+                "fp64_roofline": fp64_roofline("stokes_pt_iteration_2d", (n + 2) ** 2, r64.iterations, r64.seconds, fpk.value)}
     dc_s = np.array([r.seconds for r in results])
     tts = {
         "fp32_dc_s": float(np.median(dc_s)),
@@ -453,7 +484,8 @@ def run_ours(args, rank, world, dist):
     }
     if fp64:
         tts.update({"fp64_s": fp64["s"], "fp64_iterations": fp64["iterations"], "fp64_err": fp64["err"],
-                    "fp64_t_eff_gbs": fp64["t_eff_gbs"], "speedup_fp32dc_vs_fp64": fp64["s"] / tts["fp32_dc_s"],
+                    "fp64_t_eff_gbs": fp64["t_eff_gbs"], "fp64_roofline": fp64["fp64_roofline"],
+                    "speedup_fp32dc_vs_fp64": fp64["s"] / tts["fp32_dc_s"],
                     "err_vs_fp64": err_vs_fp64})
 
     if rank == 0:
@@ -575,6 +607,10 @@ def config_suite(arch, stream, peak, fp64=True):
 
     out = {}
     Cl, Vl = Center(), Vertex()
+    fpk = ctypes.c_double()
+    arch.call("cg_fp64_peak", ctypes.byref(fpk))
+    fp64_peak = fpk.value
+    out["fp64_peak_tflops"] = fp64_peak / 1e12
 
     # 2D explicit diffusion, FP64, 1024^2 over [-1, 1]^2, D = 1, dt = h^2/(4.1 D)
     n1 = 1024
@@ -599,6 +635,7 @@ def config_suite(arch, stream, peak, fp64=True):
         "t_eff_gbs_7_arrays": 7 * cells1 * 8 * steps1 / (ms1 * 1e-3) / 1e9,
         "bytes": "2 arrays x n^2 x 8 B per step (read C, write C'); the reference's 7-array convention beside it",
         "l2": "L2-resident (2 x 8.4 MB): HBM fraction not meaningful",
+        "fp64_roofline": fp64_roofline("diffusion_step_2d", (n1 + 2) ** 2, steps1, ms1 * 1e-3, fp64_peak),
     }
     del A, B
 
@@ -634,6 +671,8 @@ def config_suite(arch, stream, peak, fp64=True):
         sz = np.dtype(T).itemsize
         teff = 10 * n2**3 * sz * npt / (ms2 * 1e-3) / 1e9
         cfg2[name] = {"ms_per_iteration": ms2 / npt, "t_eff_gbs": teff, "frac": teff / peak}
+        if T == np.float64:
+            cfg2[name]["fp64_roofline"] = fp64_roofline("ptdiff_pt_iteration_3d", (n2 + 2) ** 3, npt, ms2 * 1e-3, fp64_peak)
         del fs, q, f
         torch.cuda.empty_cache()
     # one implicit step: 500 FP64 PT iterations (the configuration's step), then the FP32 PT
@@ -744,6 +783,7 @@ def config_suite(arch, stream, peak, fp64=True):
         "t_eff_gbs": teff5,
         "frac": teff5 / peak,
         "bytes": "3 arrays x cells x 8 B per step (read H, B; write H')",
+        "fp64_roofline": fp64_roofline("sia_ensemble_step", cells5, steps5, ms5 * 1e-3, fp64_peak),
     }
     del keep
     torch.cuda.empty_cache()
@@ -968,7 +1008,7 @@ def fused_kernel_fields(arch, pb):
     return stokes_fields(V=A["V"], P=A["P"], tau=A["tau"], **extra), stokes_fields(V=B["V"], P=B["P"], tau=B["tau"]), keep
 
 
-def fused3d_kernel_fields(arch, pb, align_index=-1):
+def fused3d_kernel_fields(arch, pb, align_index=0):
     """FP32 ping-pong field sets of the fused 3D PT kernel on the problem's grid (1/eta from eta,
     rho_g from the problem, zero V/tau/P/tau_old). Every array shares its row and plane strides,
     as in the solver's work pool."""
@@ -983,7 +1023,7 @@ def fused3d_kernel_fields(arch, pb, align_index=-1):
     rows = g.dims[1] + 5
 
     def f32(loc):
-        # rows start at their first padded element on a 128-byte boundary, as in the solver's pool
+        # logical x index 0 of every row on a 128-byte boundary, as in the solver's 3D pool
         return Field(arch, g, loc, np.float32, pitch_align=128, plane_rows=rows, align_index=align_index)
 
     vl = [(Vl, Cl, Cl), (Cl, Vl, Cl), (Cl, Cl, Vl)]
@@ -1254,7 +1294,7 @@ def main():
     ap.add_argument("--nmin", type=int, default=128, help="--kernel sia_ensemble: smallest member size")
     ap.add_argument("--nmax", type=int, default=1024, help="--kernel sia_ensemble: largest member size")
     ap.add_argument("--reps", type=int, default=200)
-    ap.add_argument("--align-index", type=int, default=-1,
+    ap.add_argument("--align-index", type=int, default=0,
                     help="--kernel fused3d: the logical x index each padded row aligns to 128 bytes (-1: its first element)")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)

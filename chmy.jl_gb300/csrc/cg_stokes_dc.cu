@@ -163,7 +163,7 @@ struct Work {
 // FP32 field like `f` (same extents, locations, halo 1) with x rows of `pitch` elements and, in
 // 3D, planes of `rows` rows. All work arrays share the row and plane strides, so the fused
 // kernels address every array with one offset.
-cg_field like32(const cg_field& f, long pitch, long rows, char*& cursor, size_t& bytes, bool dry) {
+cg_field like32(const cg_field& f, long pitch, long rows, long front, char*& cursor, size_t& bytes, bool dry) {
     cg_field g;
     std::memset(&g, 0, sizeof(g));
     g.dtype = CG_F32;
@@ -180,8 +180,8 @@ cg_field like32(const cg_field& f, long pitch, long rows, char*& cursor, size_t&
     g.stride[0] = 1;
     g.stride[1] = f.ndim > 1 ? ext[0] : 0;
     g.stride[2] = f.ndim > 2 ? ext[0] * ext[1] : 0;
-    const size_t sz = ((size_t)ext[0] * ext[1] * ext[2] * 4 + 255) & ~(size_t)255;
-    if (!dry) g.data = cursor;
+    const size_t sz = (((size_t)ext[0] * ext[1] * ext[2] + (size_t)front) * 4 + 255) & ~(size_t)255;
+    if (!dry) g.data = cursor + front * 4;
     cursor += sz;
     bytes += sz;
     return g;
@@ -189,8 +189,13 @@ cg_field like32(const cg_field& f, long pitch, long rows, char*& cursor, size_t&
 
 int make_work(cg_ctx* ctx, const cg_stokes_fields* f, int nd, Work* w) {
     const int nt = nd == 2 ? 3 : 6;
-    // the widest x extent (V.x is Vertex in x), rounded up to 32 elements (128 bytes)
-    const long pitch = ((long)f->V[0].n[0] + 4 + 31) / 32 * 32;
+    // 3D: every array's data pointer sits `front` elements past a 256-byte boundary, so that
+    // logical x index 0 of every row starts a 128-byte line (measured 2 % faster for the 3D
+    // kernel than rows whose first padded element starts a line); 2D: the first padded element
+    const long front = nd == 3 ? 31 : 0;
+    // the widest x extent (V.x is Vertex in x) after the front offset, rounded up to 32
+    // elements (128 bytes)
+    const long pitch = (front + (long)f->V[0].n[0] + 4 + 31) / 32 * 32;
     // the widest y extent (V.y is Vertex in y): rows per plane in 3D
     const long rows = (long)f->V[1].n[1] + 4;
     for (int pass = 0; pass < 2; ++pass) {
@@ -198,20 +203,20 @@ int make_work(cg_ctx* ctx, const cg_stokes_fields* f, int nd, Work* w) {
         char* cur = dry ? nullptr : static_cast<char*>(ctx->dc_pool);
         size_t bytes = 0;
         for (int d = 0; d < nd; ++d) {
-            w->dV[d] = like32(f->V[d], pitch, rows, cur, bytes, dry);
-            w->dV2[d] = like32(f->V[d], pitch, rows, cur, bytes, dry);
-            w->rho[d] = like32(f->V[d], pitch, rows, cur, bytes, dry);
-            w->rV[d] = like32(f->V[d], pitch, rows, cur, bytes, dry);
+            w->dV[d] = like32(f->V[d], pitch, rows, front, cur, bytes, dry);
+            w->dV2[d] = like32(f->V[d], pitch, rows, front, cur, bytes, dry);
+            w->rho[d] = like32(f->V[d], pitch, rows, front, cur, bytes, dry);
+            w->rV[d] = like32(f->V[d], pitch, rows, front, cur, bytes, dry);
         }
-        w->dP = like32(f->P, pitch, rows, cur, bytes, dry);
-        w->dP2 = like32(f->P, pitch, rows, cur, bytes, dry);
-        w->fP = like32(f->P, pitch, rows, cur, bytes, dry);
-        w->ieta = like32(f->P, pitch, rows, cur, bytes, dry);
-        w->divV = like32(f->P, pitch, rows, cur, bytes, dry);
+        w->dP = like32(f->P, pitch, rows, front, cur, bytes, dry);
+        w->dP2 = like32(f->P, pitch, rows, front, cur, bytes, dry);
+        w->fP = like32(f->P, pitch, rows, front, cur, bytes, dry);
+        w->ieta = like32(f->P, pitch, rows, front, cur, bytes, dry);
+        w->divV = like32(f->P, pitch, rows, front, cur, bytes, dry);
         for (int c = 0; c < nt; ++c) {
-            w->dtau[c] = like32(f->tau[c], pitch, rows, cur, bytes, dry);
-            w->dtau2[c] = like32(f->tau[c], pitch, rows, cur, bytes, dry);
-            w->told[c] = like32(f->tau[c], pitch, rows, cur, bytes, dry);
+            w->dtau[c] = like32(f->tau[c], pitch, rows, front, cur, bytes, dry);
+            w->dtau2[c] = like32(f->tau[c], pitch, rows, front, cur, bytes, dry);
+            w->told[c] = like32(f->tau[c], pitch, rows, front, cur, bytes, dry);
         }
         if (dry && bytes > ctx->dc_pool_bytes) {
             if (ctx->dc_pool) {
