@@ -639,6 +639,76 @@ def config_suite(arch, stream, peak, fp64=True):
     }
     del A, B
 
+    # the same loop's gradient: dJ/dchi and dJ/dC0 of J = 1/2 |C^N|^2, host arrays in and out
+    from chmy_gb300.adjoint import ExplicitDiffusion
+
+    ed = ExplicitDiffusion(arch, g1, 1.0, dt1, bc1)
+
+    def wall(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = fn()
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0, r
+
+    wall(lambda: ed.run(C0, 8))
+    wall(lambda: ed.gradient(C0, 8, lambda c: c))
+    tf, _ = wall(lambda: ed.run(C0, steps1))
+    tg, (gchi, _, _) = wall(lambda: ed.gradient(C0, steps1, lambda c: c))
+    out["diffusion2d_adjoint"] = {
+        "workload": "gradient of 1/2 |C^N|^2 over the 2000-step 1024^2 FP64 loop w.r.t. chi and C0 (taped forward, one reverse sweep), host arrays in and out",
+        "forward_ms": tf * 1e3,
+        "gradient_ms": tg * 1e3,
+        "ratio": tg / tf,
+        "tape_gb": ed.tape_bytes(steps1) / 1e9,
+        "finite": bool(np.isfinite(gchi)),
+    }
+    del ed
+
+    # the fused thermal step (advection-diffusion of T by V) and its vector-Jacobian product,
+    # 2048^2 FP64, Neumann T, smooth random V
+    from chmy_gb300.kernels import stokes_fields, stokes_params
+
+    nt = 2048
+    gt = UniformGrid(origin=(-1.0, -1.0), extent=(2.0, 2.0), dims=(nt, nt), dtype=np.float64)
+    xt, yt = padded_mesh(gt, Cl)
+    Tf = Field(arch, gt, Cl, np.float64)
+    Tf.from_numpy(np.exp(-(xt * xt + yt * yt) / 0.05))
+    To = Field(arch, gt, Cl, np.float64)
+    To.from_numpy(np.exp(-(xt * xt + yt * yt) / 0.05))
+    Vt = [Field(arch, gt, (Vl, Cl), np.float64), Field(arch, gt, (Cl, Vl), np.float64)]
+    for d, v in enumerate(Vt):
+        xv, yv = padded_mesh(gt, v.loc)
+        v.from_numpy(np.sin(np.pi * (xv + 0.3 * d)) * np.cos(np.pi * yv))
+    del xt, yt
+    Tout = Field(arch, gt, Cl, np.float64)
+    mu = Field(arch, gt, Cl, np.float64)
+    mu.from_numpy(np.ones(Tout.data.shape))
+    gTt, gTo = Field(arch, gt, Cl, np.float64), Field(arch, gt, Cl, np.float64)
+    gVt = [Field(arch, gt, v.loc, np.float64) for v in Vt]
+    ft = stokes_fields(V=Vt, T=Tf, T_old=To)
+    pt = stokes_params(G=1.0, dt=1e-4, lambda_rhoCp=0.3)
+    bct = to_cg_bc(2, Neumann())
+    gdt = gt.desc()
+    gVa = (_abi.cg_field * 3)(gVt[0].desc(), gVt[1].desc(), _abi.cg_field())
+    reps = 50
+    msf = _timed(lambda: arch.call("cg_stokes_thermal_step", ctypes.byref(gdt), ctypes.byref(ft), ctypes.byref(pt), ctypes.byref(bct),
+                                   ctypes.byref(Tout.desc())), stream, reps)
+    msa = _timed(lambda: arch.call("cg_stokes_thermal_step_adjoint", ctypes.byref(gdt), ctypes.byref(ft), ctypes.byref(pt),
+                                   ctypes.byref(bct), ctypes.byref(mu.desc()), ctypes.byref(gTt.desc()), ctypes.byref(gTo.desc()),
+                                   gVa, None), stream, reps)
+    out["thermal_step_adjoint"] = {
+        "workload": "fused thermal step (update_thermal_flux! + update_thermal!) at 2048^2 FP64 and its vector-Jacobian product "
+                    "(dJ/dT, dJ/dT_old, dJ/dV; dJ/dlambda left out: it synchronises)",
+        "forward_us": msf * 1e3,
+        "adjoint_us": msa * 1e3,
+        "ratio": msa / msf,
+        "forward_t_eff_gbs": 5 * nt * nt * 8 / (msf * 1e-3) / 1e9,
+        "adjoint_t_eff_gbs": 8 * nt * nt * 8 / (msa * 1e-3) / 1e9,
+        "bytes": "forward: read T, T_old, V x2, write T (5 arrays); adjoint: read T, V x2, mu, write gT, gT_old, gV x2 (8 arrays)",
+    }
+    del Tf, To, Vt, Tout, mu, gTt, gTo, gVt
+
     # 3D PT variable diffusion at 512^3, a sample of PT iterations of one step
     n2, npt = 512, 100
     g2 = UniformGrid(origin=(-0.5,) * 3, extent=(1.0,) * 3, dims=(n2,) * 3, dtype=np.float64)

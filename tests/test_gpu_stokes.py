@@ -21,7 +21,7 @@ C_, V_ = Center(), Vertex()
 class StokesSet:
     """Seeded random VE Stokes state on host and device."""
 
-    def __init__(self, arch, dims, T, seed, var_eta, rho=True, thermal=False, pitch_align=0):
+    def __init__(self, arch, dims, T, seed, var_eta, rho=True, thermal=False, pitch_align=0, plane_rows=0):
         rng = np.random.default_rng(seed)
         nd = len(dims)
         self.grid = UniformGrid(origin=(T(-1),) * nd, extent=(T(2),) * nd, dims=dims, dtype=T)
@@ -48,9 +48,9 @@ class StokesSet:
         self.d = {}
         for k, v in self.h.items():
             if isinstance(v, list):
-                self.d[k] = [to_gpu(arch, f, pitch_align) if f is not None else None for f in v]
+                self.d[k] = [to_gpu(arch, f, pitch_align, plane_rows) if f is not None else None for f in v]
             else:
-                self.d[k] = to_gpu(arch, v, pitch_align)
+                self.d[k] = to_gpu(arch, v, pitch_align, plane_rows)
 
     def host_desc(self):
         return stokes_desc(**self.h)
@@ -169,27 +169,29 @@ def test_pt_iterations_graph(arch, T, dims, var_eta):
         assert abs(err[i] - want[i]) <= rtol_for(T) * niter * 10 * max(abs(want[i]), 1.0)
 
 
-def _pp_run(arch, T, dims, bcs, niter, seed=31, pitch_align=0):
+def _pp_run(arch, T, dims, bcs, niter, seed=31, pitch_align=0, plane_rows=0):
     """niter fused ping-pong iterations (cg_stokes_pt_iterations_pp) against niter x
     (update_stress!, update_velocity!, bc!(V)) on the oracle. Returns the set, the partner
     buffers and the oracle's V after niter - 1 iterations. pitch_align: the device fields' row
-    alignment (bytes; 0 = Chmy's dense layout)."""
-    s = StokesSet(arch, dims, T, seed, True, rho=True, pitch_align=pitch_align)
+    alignment (bytes; 0 = Chmy's dense layout); plane_rows: 3D rows per plane (with
+    pitch_align, one plane stride for every array)."""
+    s = StokesSet(arch, dims, T, seed, True, rho=True, pitch_align=pitch_align, plane_rows=plane_rows)
     g2 = s.grid
     rho_full = [random_field(g2, f.loc, T, np.random.default_rng(5)) for f in vec_fields(g2, T)]
     s.h["rho_g"] = rho_full
-    s.d["rho_g"] = [to_gpu(arch, f, pitch_align) for f in rho_full]
+    s.d["rho_g"] = [to_gpu(arch, f, pitch_align, plane_rows) for f in rho_full]
     ie = NpField(g2, C_, T)
     ie.a[...] = (1.0 / s.h["eta"].a).astype(T)
     s.h["inv_eta"] = ie
-    s.d["inv_eta"] = to_gpu(arch, ie, pitch_align)
+    s.d["inv_eta"] = to_gpu(arch, ie, pitch_align, plane_rows)
     p = pt_params(g2, True)
     g = g2.desc()
     bc_apply(g2, s.h["V"], bcs)
     for f, d in zip(s.h["V"], s.d["V"]):
         d.from_numpy(f.a)
     # partner buffers for V, P, tau hold the same initial state
-    partner = {k: ([to_gpu(arch, f, pitch_align) for f in s.h[k]] if isinstance(s.h[k], list) else to_gpu(arch, s.h[k], pitch_align))
+    partner = {k: ([to_gpu(arch, f, pitch_align, plane_rows) for f in s.h[k]] if isinstance(s.h[k], list)
+                   else to_gpu(arch, s.h[k], pitch_align, plane_rows))
                for k in ("V", "P", "tau")}
     hd, da = s.host_desc(), s.dev_desc()
     from _oracle import stokes_desc as sd
@@ -224,6 +226,47 @@ def test_fused_pingpong_iterations(arch, T, dims):
     # odd niter is rejected
     rc = arch.lib.cg_stokes_pt_iterations_pp(arch.ctx, ctypes.byref(g), ctypes.byref(da), ctypes.byref(db), ctypes.byref(p), barr, 3)
     assert rc == _abi.CG_ERR_ARG
+
+
+@pytest.mark.parametrize("T", TYPES)
+@pytest.mark.parametrize("layout", ["8:0", "16:0", "24:0", "32:0", "48:0", "64:0"])
+@pytest.mark.parametrize("dims", [(70, 33), (33, 97)])
+def test_fused_2d_autotuner_layouts_give_the_same_bits(arch, monkeypatch, T, layout, dims):
+    """Every one-iteration candidate of the 2D autotuner (segment lengths 8..64 rows, forced with
+    CG_MARCH_LAYOUT=<segment length>:0) leaves the oracle's states bit for bit."""
+    monkeypatch.setenv("CG_MARCH_LAYOUT", layout)
+    s, partner, prev, _ = _pp_run(arch, T, dims, _bc_V(2), 6, seed=37)
+    for name in ("V", "P", "tau", "divV", "r_V"):
+        hv = s.h[name] if isinstance(s.h[name], list) else [s.h[name]]
+        dv = s.d[name] if isinstance(s.d[name], list) else [s.d[name]]
+        for a, b in zip(dv, hv):
+            if b is not None:
+                assert_close(a, b, 0.0, f"layout {layout} {name}", exact=True)
+    for a, b in zip(partner["V"], prev):
+        assert np.array_equal(a.to_numpy().view(np.uint8), b.view(np.uint8)), f"layout {layout}: partner V"
+
+
+@pytest.mark.parametrize("layout", ["16:0", "32:0", "64:0", "0:1", "16:1", "32:1", "64:1"])
+@pytest.mark.parametrize("dims", [(31, 20, 70), (61, 7, 33)])
+def test_fused_3d_autotuner_layouts_give_the_same_bits(arch, monkeypatch, layout, dims):
+    """Every candidate of the 3D autotuner (z-segment lengths x block shapes: 12 rows at 2
+    blocks per SM, variant 0, or 8 rows at 3, variant 1; forced with CG_MARCH_LAYOUT) on FP32
+    fields that share one row and plane stride, as the defect-correction pool lays them out:
+    the oracle's states bit for bit."""
+    monkeypatch.setenv("CG_MARCH_LAYOUT", layout)
+    rows = dims[1] + 5
+    # rows padded to 512 bytes: Center and Vertex rows of these grids get one row stride
+    s, partner, prev, _ = _pp_run(arch, np.float32, dims, _bc_V(3), 4, seed=41, pitch_align=512, plane_rows=rows)
+    strides = {f.data.stride()[:2] for v in s.d.values() for f in (v if isinstance(v, list) else [v]) if f is not None}
+    assert len(strides) == 1, strides
+    for name in ("V", "P", "tau", "divV", "r_V"):
+        hv = s.h[name] if isinstance(s.h[name], list) else [s.h[name]]
+        dv = s.d[name] if isinstance(s.d[name], list) else [s.d[name]]
+        for a, b in zip(dv, hv):
+            if b is not None:
+                assert_close(a, b, 0.0, f"layout {layout} {name}", exact=True)
+    for a, b in zip(partner["V"], prev):
+        assert np.array_equal(a.to_numpy().view(np.uint8), b.view(np.uint8)), f"layout {layout}: partner V"
 
 
 def _bc_mix(kind):
