@@ -204,6 +204,10 @@ SIGNATURES: dict[str, list] = {
     "cg_stokes_update_thermal_flux": [_vp, P(cg_grid), P(cg_stokes_fields), P(cg_stokes_params)],
     "cg_stokes_update_thermal": [_vp, P(cg_grid), P(cg_stokes_fields), P(cg_stokes_params)],
     "cg_stokes_pt_iterations": [_vp, P(cg_grid), P(cg_stokes_fields), P(cg_stokes_params), P(cg_bc), C.c_int],
+    "cg_stokes_update_stress_masked": [_vp, P(cg_grid), P(cg_stokes_fields), P(cg_stokes_params), P(cg_mask)],
+    "cg_stokes_update_velocity_masked": [_vp, P(cg_grid), P(cg_stokes_fields), P(cg_stokes_params), P(cg_mask)],
+    "cg_stokes_pt_iterations_masked": [_vp, P(cg_grid), P(cg_stokes_fields), P(cg_stokes_params), P(cg_bc), P(cg_mask),
+                                       C.c_int],
     "cg_stokes_pt_iterations_pp": [
         _vp,
         P(cg_grid),

@@ -200,7 +200,8 @@ def evaluate(grid: UniformGrid, loc, dims, fun, discrete: bool = False, paramete
     axes = [grid.coords(loc, d + 1) for d in range(len(dims))]
     mesh = np.meshgrid(*axes, indexing="ij")
     out = np.asarray(fun(*mesh, *parameters), dtype=dtype)
-    return np.ascontiguousarray(np.broadcast_to(out, dims), dtype=dtype)
+    # a writable copy (broadcast_to returns a read-only view, even of a full-size array)
+    return np.array(np.broadcast_to(out, dims), dtype=dtype, order="C")
 
 
 def set_(f: Field, value, grid: UniformGrid | None = None, *, discrete: bool = False, parameters=()) -> None:

@@ -87,24 +87,34 @@ class Kernel:
 
 
 class _ComputeQ(Kernel):
-    """compute_q!(q, C, χ, g) (examples/diffusion_2d.jl:8-13)."""
+    """compute_q!(q, C, χ, g) (examples/diffusion_2d.jl:8-13); with a trailing FieldMask ω, the
+    masked form q.d = -χ ∂d(C, ω, g, I)."""
 
     name = "compute_q"
 
-    def launch(self, arch, grid, q, C, chi, g=None):
+    def launch(self, arch, grid, q, C, chi, g=None, omega=None):
         qa = _vec(q)
         c = C.desc()
+        if omega is not None:
+            arch.call("cg_diffusion_compute_q_masked", ctypes.byref(grid.desc()), qa, ctypes.byref(c), float(chi),
+                      ctypes.byref(omega.desc()))
+            return
         arch.call("cg_diffusion_compute_q", ctypes.byref(grid.desc()), qa, ctypes.byref(c), float(chi))
 
 
 class _UpdateC(Kernel):
-    """update_C!(C, q, Δt, g) (examples/diffusion_2d.jl:15-19)."""
+    """update_C!(C, q, Δt, g) (examples/diffusion_2d.jl:15-19); with a trailing FieldMask ω, the
+    masked form C -= Δt divg(q, ω, g, I)."""
 
     name = "update_C"
 
-    def launch(self, arch, grid, C, q, dt, g=None):
+    def launch(self, arch, grid, C, q, dt, g=None, omega=None):
         qa = _vec(q)
         c = C.desc()
+        if omega is not None:
+            arch.call("cg_diffusion_update_C_masked", ctypes.byref(grid.desc()), ctypes.byref(c), qa, float(dt),
+                      ctypes.byref(omega.desc()))
+            return
         arch.call("cg_diffusion_update_C", ctypes.byref(grid.desc()), ctypes.byref(c), qa, float(dt))
 
 
@@ -120,11 +130,12 @@ class _UpdateOld(Kernel):
 
 class _UpdateStress(Kernel):
     """update_stress!(τ, Pr, ∇V, V, τ_old, η, η_ve, G, dt, dτ_Pr, dτ_r, g)
-    (examples/stokes_2d_inc_ve_T.jl:20-34; 3D :23-46)."""
+    (examples/stokes_2d_inc_ve_T.jl:20-34; 3D :23-46). A trailing FieldMask ω selects the form
+    written with the masked operators: ∂(V.d, ω, g, I) for the strain rates and divg(V, ω, g, I)."""
 
     name = "update_stress"
 
-    def launch(self, arch, grid, tau, Pr, divV, V, tau_old, eta, eta_ve, G, dt, dtau_Pr, dtau_r, g=None):
+    def launch(self, arch, grid, tau, Pr, divV, V, tau_old, eta, eta_ve, G, dt, dtau_Pr, dtau_r, g=None, omega=None):
         eta_f = eta.eta if isinstance(eta, CellViscosity) else None
         s = stokes_fields(V=V, P=Pr, divV=divV, tau=tau, tau_old=tau_old, eta=eta_f)
         p = stokes_params(
@@ -135,6 +146,10 @@ class _UpdateStress(Kernel):
             dtau_Pr=dtau_Pr,
             dtau_r=dtau_r,
         )
+        if omega is not None:
+            arch.call("cg_stokes_update_stress_masked", ctypes.byref(grid.desc()), ctypes.byref(s), ctypes.byref(p),
+                      ctypes.byref(omega.desc()))
+            return
         arch.call("cg_stokes_update_stress", ctypes.byref(grid.desc()), ctypes.byref(s), ctypes.byref(p))
 
 
@@ -142,11 +157,12 @@ class _UpdateVelocity(Kernel):
     """update_velocity!(V, r_V, Pr, τ, ρg, η_ve, νdτ, g) (examples/stokes_2d_inc_ve_T.jl:36-43;
     3D :48-57). `ρg` is the body force of the last component (ρgy in 2D, ρgz in 3D): a Field, a
     FunctionField of a device form (evaluated in the kernel, as the example's
-    FunctionField(init_incl, ...) of :107), or None."""
+    FunctionField(init_incl, ...) of :107), or None. A trailing FieldMask ω selects the form
+    written with the masked operators ∂(Pr, ω, g, I) and ∂(τ.c, ω, g, I)."""
 
     name = "update_velocity"
 
-    def launch(self, arch, grid, V, r_V, Pr, tau, rho_g, eta_ve, nu_dtau, g=None):
+    def launch(self, arch, grid, V, r_V, Pr, tau, rho_g, eta_ve, nu_dtau, g=None, omega=None):
         from .functions import FunctionField
 
         nd = grid.ndim
@@ -164,6 +180,10 @@ class _UpdateVelocity(Kernel):
             p = stokes_params(eta_ve=eta_ve, nu_dtau=nu_dtau)
         if fn is not None:
             p.rho_g_fn[nd - 1] = fn
+        if omega is not None:
+            arch.call("cg_stokes_update_velocity_masked", ctypes.byref(grid.desc()), ctypes.byref(s), ctypes.byref(p),
+                      ctypes.byref(omega.desc()))
+            return
         arch.call("cg_stokes_update_velocity", ctypes.byref(grid.desc()), ctypes.byref(s), ctypes.byref(p))
 
 

@@ -60,6 +60,10 @@ bool cg_tune_lookup(const std::string& key, cg_tune_cfg* out);
 // the autotuner's (profiling of one layout); false when unset or malformed.
 bool cg_tune_forced(cg_tune_cfg* out);
 void cg_tune_store(const std::string& key, const cg_tune_cfg& cfg);
+// CG_BLOCK=<threads along x>x<threads along y> in the environment (read on every call): the
+// block shape of the per-point kernels instead of the autotuner's; false when unset or not a
+// valid shape (x a multiple of 32, x * y from 64 to 1024).
+bool cg_block_forced(dim3* out);
 
 // Programmatic dependent launch. A kernel launched by cg_launch(..., dep = true) may be
 // scheduled while the kernel before it on the stream is still running; it calls cg_dep_wait()
@@ -187,6 +191,36 @@ inline float time_launches(F&& launch, cudaStream_t st) {
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     return ms;
+}
+
+// Block shapes (threads along x, along y) the per-point kernels are timed over. Each thread
+// computes one point whatever the shape, so every shape gives the same bits.
+constexpr int kBlockShapes[7][2] = {{32, 8}, {32, 4}, {64, 4}, {128, 2}, {32, 16}, {64, 8}, {128, 4}};
+
+// The block shape of a per-point kernel: CG_BLOCK when set, else the fastest of kBlockShapes for
+// `key` (timed once per process with `launch(block)`, which must leave no state the caller
+// relies on changed), else 32 x 8 when the autotuner is off. `name` labels the verbose output.
+template <class F>
+inline dim3 tune_block(const char* name, const std::string& key, F&& launch, cudaStream_t st) {
+    dim3 b(32, 8);
+    if (cg_block_forced(&b)) return b;
+    if (!cg_autotune_enabled()) return b;
+    cg_tune_cfg c{0, 0};
+    if (cg_tune_lookup(key, &c)) return dim3((unsigned)c.seg, (unsigned)c.variant);
+    float best = 1e30f;
+    for (const auto& sh : kBlockShapes) {
+        const dim3 cand((unsigned)sh[0], (unsigned)sh[1]);
+        const float t = time_launches([&] { return launch(cand); }, st);
+        if (cg_tune_verbose())
+            std::fprintf(stderr, "%s tune: block %dx%d: %.1f us\n", name, sh[0], sh[1], t >= 0.f ? 1e3f * t / 3 : -1.f);
+        if (t >= 0.f && t < best) {
+            best = t;
+            b = cand;
+        }
+    }
+    cudaGetLastError();
+    cg_tune_store(key, cg_tune_cfg{(int)b.x, (int)b.y});
+    return b;
 }
 
 }  // namespace cgk

@@ -99,6 +99,16 @@ bool cg_tune_forced(cg_tune_cfg* out) {
     return true;
 }
 
+bool cg_block_forced(dim3* out) {
+    const char* e = std::getenv("CG_BLOCK");
+    if (!e || !e[0]) return false;
+    int bx = 0, by = 0;
+    if (std::sscanf(e, "%dx%d", &bx, &by) != 2) return false;
+    if (bx < 32 || bx % 32 || by < 1 || bx * by < 64 || bx * by > 1024) return false;
+    *out = dim3((unsigned)bx, (unsigned)by);
+    return true;
+}
+
 bool cg_pdl_enabled() {
     static const bool on = [] {
         const char* e = std::getenv("CG_PDL");

@@ -184,14 +184,44 @@ int update_C_t(cg_ctx* ctx, const cg_grid* g, const cg_field* C, const cg_field*
 }
 
 template <class T, int ND>
-int step_t(cg_ctx* ctx, const cg_grid* g, const cg_field* Co, const cg_field* Ci, double chi, double dt) {
-    const dim3 block = block_for<ND>();
+cudaError_t step_launch(const cg_grid* g, const cg_field* Co, const cg_field* Ci, double chi, double dt, dim3 block,
+                        cudaStream_t st) {
     Spacing<T> a;
     for (int d = 0; d < 3; ++d) a.i[d] = (T)(dt * chi * g->inv_spacing[d] * g->inv_spacing[d]);
-    diffusion_step_kernel<T, ND><<<range_grid<ND>(g, block), block, 0, ctx->stream>>>(
+    diffusion_step_kernel<T, ND><<<range_grid<ND>(g, block), block, 0, st>>>(
         cg_view<T>(*Co), cg_view<T>(*Ci), -(T)chi, (T)dt, spacing_of<T>(g), g->n[0] + 1,
         ND > 1 ? g->n[1] + 1 : 0, ND > 2 ? g->n[2] + 1 : 0, a);
-    CG_CHECK_LAUNCH(ctx);
+    return cudaGetLastError();
+}
+
+// The step kernel's block shape for this grid and layout: 1D keeps 256 threads; 2D and 3D take
+// the autotuner's choice, timed on C_out = step(C_in) (the first step of a run writes the same
+// points again), or its cached choice when `may_time` is false.
+template <class T, int ND>
+dim3 step_block(cg_ctx* ctx, const cg_grid* g, const cg_field* Co, const cg_field* Ci, double chi, double dt,
+                bool may_time) {
+    if (ND == 1) return block_for<ND>();
+    std::string key = "diffusion_block";
+    cg_key_add(key, *g);
+    cg_key_add(key, (int)sizeof(T));
+    cg_key_add(key, Ci->stride);
+    cg_key_add(key, Co->stride);
+    cg_key_add(key, ctx->num_sms);
+    if (!may_time) {
+        dim3 b(32, 8);
+        if (cg_block_forced(&b)) return b;
+        cg_tune_cfg c{0, 0};
+        return cg_tune_lookup(key, &c) ? dim3((unsigned)c.seg, (unsigned)c.variant) : b;
+    }
+    return cgk::tune_block("diffusion step", key,
+                           [&](dim3 b) { return step_launch<T, ND>(g, Co, Ci, chi, dt, b, ctx->stream); }, ctx->stream);
+}
+
+template <class T, int ND>
+int step_t(cg_ctx* ctx, const cg_grid* g, const cg_field* Co, const cg_field* Ci, double chi, double dt, bool may_time) {
+    const dim3 block = step_block<T, ND>(ctx, g, Co, Ci, chi, dt, may_time);
+    const cudaError_t e = step_launch<T, ND>(g, Co, Ci, chi, dt, block, ctx->stream);
+    if (e != cudaSuccess) return cg_fail(ctx, CG_ERR_CUDA, "diffusion step: %s", cudaGetErrorString(e));
     return CG_OK;
 }
 
@@ -277,9 +307,11 @@ extern "C" int cg_diffusion_update_C(cg_ctx* ctx, const cg_grid* grid, const cg_
     return CG_DISPATCH(update_C_t, C->dtype, grid->ndim, ctx, grid, C, q, dt);
 }
 
+// One step and bc!; `may_time`: the block-shape autotuner may time launches (false inside a
+// graph capture, where the cached or default shape is used).
 static int step_checked(cg_ctx* ctx, const cg_grid* grid, const cg_field* Co, const cg_field* Ci, double chi,
-                        double dt, const cg_bc* bc) {
-    int rc = CG_DISPATCH(step_t, Ci->dtype, grid->ndim, ctx, grid, Co, Ci, chi, dt);
+                        double dt, const cg_bc* bc, bool may_time) {
+    int rc = CG_DISPATCH(step_t, Ci->dtype, grid->ndim, ctx, grid, Co, Ci, chi, dt, may_time);
     if (rc) return rc;
     if (bc) return cg_bc_apply_impl(ctx, grid, 1, Co, bc);
     return CG_OK;
@@ -300,7 +332,7 @@ extern "C" int cg_diffusion_step(cg_ctx* ctx, const cg_grid* grid, const cg_fiel
     int rc = step_args(ctx, grid, C_out, C_in);
     if (rc) return rc;
     cudaSetDevice(ctx->device);
-    return step_checked(ctx, grid, C_out, C_in, chi, dt, bc);
+    return step_checked(ctx, grid, C_out, C_in, chi, dt, bc, false);
 }
 
 extern "C" int cg_diffusion_run(cg_ctx* ctx, const cg_grid* grid, const cg_field* A, const cg_field* B, double chi,
@@ -320,11 +352,19 @@ extern "C" int cg_diffusion_run(cg_ctx* ctx, const cg_grid* grid, const cg_field
     cg_bc none;
     std::memset(&none, 0, sizeof(none));
     cg_key_add(key, bc ? *bc : none);
+    // the step's block shape, timed on B = step(A) (once per shape) before the graph is captured
+    dim3 blk(256, 1);
+    if (grid->ndim > 1) blk = A->dtype == CG_F64
+                                  ? (grid->ndim == 2 ? step_block<double, 2>(ctx, grid, B, A, chi, dt, true)
+                                                     : step_block<double, 3>(ctx, grid, B, A, chi, dt, true))
+                                  : (grid->ndim == 2 ? step_block<float, 2>(ctx, grid, B, A, chi, dt, true)
+                                                     : step_block<float, 3>(ctx, grid, B, A, chi, dt, true));
+    cg_key_add(key, blk);
     return cg_graph_run(ctx, key, [&](cudaStream_t) {
         for (int s = 0; s < nsteps; ++s) {
             const cg_field* in = (s % 2 == 0) ? A : B;
             const cg_field* out = (s % 2 == 0) ? B : A;
-            int r = step_checked(ctx, grid, out, in, chi, dt, bc);
+            int r = step_checked(ctx, grid, out, in, chi, dt, bc, false);
             if (r) return r;
         }
         return (int)CG_OK;

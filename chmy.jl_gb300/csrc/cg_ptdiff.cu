@@ -93,9 +93,16 @@ int check_ptdiff(cg_ctx* ctx, const cg_grid* g, const cg_ptdiff_fields* f, const
     return CG_OK;
 }
 
+// Bytes from the first to the last element of the padded field (pitched rows included).
+size_t padded_bytes(const cg_field& f) {
+    size_t span = 1;
+    for (int d = 0; d < f.ndim; ++d) span += (size_t)(f.n[d] + 4 * f.halo[d] - 1) * (size_t)f.stride[d];
+    return span * (f.dtype == CG_F64 ? 8 : 4);
+}
+
 template <class T, int ND>
-int launch_q(cg_ctx* ctx, const cg_grid* g, const cg_ptdiff_fields* f, const cg_ptdiff_params* p) {
-    const dim3 b = block_for<ND>();
+int launch_q(cg_ctx* ctx, const cg_grid* g, const cg_ptdiff_fields* f, const cg_ptdiff_params* p,
+             dim3 b = block_for<ND>()) {
     ptdiff_q_kernel<T, ND><<<range_grid<ND>(g, b), b, 0, ctx->stream>>>(make_pv<T>(g, f, p), g->n[0] + 1,
                                                                          ND > 1 ? g->n[1] + 1 : 0);
     CG_CHECK_LAUNCH(ctx);
@@ -103,11 +110,84 @@ int launch_q(cg_ctx* ctx, const cg_grid* g, const cg_ptdiff_fields* f, const cg_
 }
 
 template <class T, int ND>
-int launch_C(cg_ctx* ctx, const cg_grid* g, const cg_ptdiff_fields* f, const cg_ptdiff_params* p) {
-    const dim3 b = block_for<ND>();
+int launch_C(cg_ctx* ctx, const cg_grid* g, const cg_ptdiff_fields* f, const cg_ptdiff_params* p,
+             dim3 b = block_for<ND>()) {
     ptdiff_C_kernel<T, ND><<<range_grid<ND>(g, b), b, 0, ctx->stream>>>(make_pv<T>(g, f, p), g->n[0] + 1,
                                                                          ND > 1 ? g->n[1] + 1 : 0);
     CG_CHECK_LAUNCH(ctx);
+    return CG_OK;
+}
+
+// Block shapes of the flux and update kernels of a PT run over this field set (tune_block;
+// cached per grid, precision and layout; 1D keeps 256 threads). The kernels update q and C in
+// place and write R, so the candidates run on copies of those fields in a temporary
+// allocation, released before the run's graph is captured; the caller's fields are untouched.
+template <class T, int ND>
+int ptdiff_blocks(cg_ctx* ctx, const cg_grid* g, const cg_ptdiff_fields* f, const cg_ptdiff_params* p, dim3* bq,
+                  dim3* bc) {
+    *bq = *bc = block_for<ND>();
+    if (ND == 1) return CG_OK;
+    dim3 forced;
+    if (cg_block_forced(&forced)) {
+        *bq = *bc = forced;
+        return CG_OK;
+    }
+    if (!cg_autotune_enabled()) return CG_OK;
+    std::string base = "ptdiff_blocks";
+    cg_key_add(base, *g);
+    cg_key_add(base, (int)sizeof(T));
+    cg_key_add(base, f->C.stride);
+    cg_key_add(base, f->q[0].stride);
+    cg_key_add(base, (int)cg_present(f->R));
+    cg_key_add(base, ctx->num_sms);
+    const std::string kq = base + "q", kc = base + "C";
+    cg_tune_cfg c1{0, 0}, c2{0, 0};
+    if (cg_tune_lookup(kq, &c1) && cg_tune_lookup(kc, &c2)) {
+        *bq = dim3((unsigned)c1.seg, (unsigned)c1.variant);
+        *bc = dim3((unsigned)c2.seg, (unsigned)c2.variant);
+        return CG_OK;
+    }
+    cg_ptdiff_fields c = *f;
+    cg_field* upd[5];
+    int nu = 0;
+    upd[nu++] = &c.C;
+    for (int d = 0; d < ND; ++d) upd[nu++] = &c.q[d];
+    if (cg_present(c.R)) upd[nu++] = &c.R;
+    size_t off[5], total = 0;
+    for (int a = 0; a < nu; ++a) {
+        off[a] = total;
+        total += (padded_bytes(*upd[a]) + 255) & ~(size_t)255;
+    }
+    char* tmp = nullptr;
+    if (cudaMalloc(&tmp, total) != cudaSuccess) {
+        cudaGetLastError();
+        return CG_OK;  // no room to time the candidates: the default shape
+    }
+    for (int a = 0; a < nu; ++a) {
+        const cudaError_t e = cudaMemcpyAsync(tmp + off[a], upd[a]->data, padded_bytes(*upd[a]), cudaMemcpyDeviceToDevice,
+                                              ctx->stream);
+        if (e != cudaSuccess) {
+            cudaFree(tmp);
+            return cg_fail(ctx, CG_ERR_CUDA, "ptdiff block tuning: %s", cudaGetErrorString(e));
+        }
+        upd[a]->data = tmp + off[a];
+    }
+    const PV<T> v = make_pv<T>(g, &c, p);
+    const int e0 = g->n[0] + 1, e1 = ND > 1 ? g->n[1] + 1 : 0;
+    *bq = cgk::tune_block("ptdiff update_q", kq,
+                          [&](dim3 b) {
+                              ptdiff_q_kernel<T, ND><<<range_grid<ND>(g, b), b, 0, ctx->stream>>>(v, e0, e1);
+                              return cudaGetLastError();
+                          },
+                          ctx->stream);
+    *bc = cgk::tune_block("ptdiff update_C", kc,
+                          [&](dim3 b) {
+                              ptdiff_C_kernel<T, ND><<<range_grid<ND>(g, b), b, 0, ctx->stream>>>(v, e0, e1);
+                              return cudaGetLastError();
+                          },
+                          ctx->stream);
+    cudaStreamSynchronize(ctx->stream);
+    cudaFree(tmp);
     return CG_OK;
 }
 
@@ -116,13 +196,6 @@ int launch_C(cg_ctx* ctx, const cg_grid* g, const cg_ptdiff_fields* f, const cg_
                                     : (nd) == 2 ? fn<double, 2>(__VA_ARGS__) : fn<double, 3>(__VA_ARGS__)) \
                        : ((nd) == 1 ? fn<float, 1>(__VA_ARGS__)                                          \
                                     : (nd) == 2 ? fn<float, 2>(__VA_ARGS__) : fn<float, 3>(__VA_ARGS__)))
-
-// Bytes from the first to the last element of the padded field (pitched rows included).
-size_t padded_bytes(const cg_field& f) {
-    size_t span = 1;
-    for (int d = 0; d < f.ndim; ++d) span += (size_t)(f.n[d] + 4 * f.halo[d] - 1) * (size_t)f.stride[d];
-    return span * (f.dtype == CG_F64 ? 8 : 4);
-}
 
 // ---- fused 3D PT iteration: update_q! + update_C! in one z-marching pass ---------------------
 //
@@ -465,14 +538,18 @@ extern "C" int cg_ptdiff_run(cg_ctx* ctx, const cg_grid* grid, const cg_ptdiff_f
     if (fused3d_ok(grid, f)) return run_fused3d<float>(ctx, grid, f, p, bc, nsteps, npt, key + "fused3d");
     const size_t cbytes = padded_bytes(f->C);
     const int dtype = f->C.dtype, nd = grid->ndim;
+    dim3 bq, bcl;
+    if ((rc = PDISPATCH(ptdiff_blocks, dtype, nd, ctx, grid, f, p, &bq, &bcl))) return rc;
+    cg_key_add(key, bq);
+    cg_key_add(key, bcl);
     return cg_graph_run(ctx, key, [&](cudaStream_t st) {
         for (int s = 0; s < nsteps; ++s) {
             // update_old: C_old <- C (whole padded array)
             CG_CUDA(ctx, cudaMemcpyAsync(f->C_old.data, f->C.data, cbytes, cudaMemcpyDeviceToDevice, st));
             for (int it = 0; it < npt; ++it) {
-                int r = PDISPATCH(launch_q, dtype, nd, ctx, grid, f, p);
+                int r = PDISPATCH(launch_q, dtype, nd, ctx, grid, f, p, bq);
                 if (r) return r;
-                r = PDISPATCH(launch_C, dtype, nd, ctx, grid, f, p);
+                r = PDISPATCH(launch_C, dtype, nd, ctx, grid, f, p, bcl);
                 if (r) return r;
                 if (bc && (r = cg_bc_apply_impl(ctx, grid, 1, &f->C, bc))) return r;
             }

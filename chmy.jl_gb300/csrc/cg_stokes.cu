@@ -150,35 +150,170 @@ int setup_pre(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f, const cg
     return CG_OK;
 }
 
+// The weight fields of a FieldMask (cg_mask.at, indexed by location bits) as kernel views.
+template <class T>
+FieldMaskW<T> mask_views(const cg_mask* m) {
+    FieldMaskW<T> w;
+    std::memset(&w, 0, sizeof(w));
+    for (int b = 0; b < 8; ++b)
+        if (cg_present(m->at[b])) w.w[b] = cg_view<T>(m->at[b]);
+    return w;
+}
+
+template <class T, int ND, class M>
+void stress_launch(const cg_grid* g, const SV<T>& v, const SP<T>& s, bool res, const M& m, dim3 block, cudaStream_t st) {
+    if (res)
+        stress_kernel<T, ND, true, M><<<range_grid<ND>(g, block), block, 0, st>>>(v, s, g->n[0] + 1, g->n[1] + 1, m);
+    else
+        stress_kernel<T, ND, false, M><<<range_grid<ND>(g, block), block, 0, st>>>(v, s, g->n[0] + 1, g->n[1] + 1, m);
+}
+
+template <class T, int ND, class M>
+void velocity_launch(const cg_grid* g, const SV<T>& v, const SP<T>& s, const BodyFn<T>& bf, bool res, const M& m,
+                     dim3 block, cudaStream_t st) {
+    if (res)
+        velocity_kernel<T, ND, true, M><<<range_grid<ND>(g, block), block, 0, st>>>(v, s, bf, g->n[0] + 1, g->n[1] + 1, m);
+    else
+        velocity_kernel<T, ND, false, M><<<range_grid<ND>(g, block), block, 0, st>>>(v, s, bf, g->n[0] + 1, g->n[1] + 1, m);
+}
+
+// update_stress! over [0, n+1]^N; with `mask`, every strain-rate derivative is the masked
+// operator ∂(V.d, ω, g, I) (src/GridOperators/masked_field_operators.jl:20-57).
 template <class T, int ND>
-int launch_stress(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f, const cg_stokes_params* p, bool res,
-                  const Pre* pr = nullptr) {
-    dim3 block(32, 8);
+cudaError_t stress_any(const cg_grid* g, const cg_stokes_fields* f, const cg_stokes_params* p, bool res, const Pre* pr,
+                       const cg_mask* mask, dim3 block, cudaStream_t st) {
     SV<T> v = views<T>(f, ND);
     apply_pre(v, pr);
     const SP<T> s = scalars<T>(g, p);
-    if (res)
-        stress_kernel<T, ND, true><<<range_grid<ND>(g, block), block, 0, ctx->stream>>>(v, s, g->n[0] + 1, g->n[1] + 1);
+    if (mask)
+        stress_launch<T, ND>(g, v, s, res, mask_views<T>(mask), block, st);
     else
-        stress_kernel<T, ND, false><<<range_grid<ND>(g, block), block, 0, ctx->stream>>>(v, s, g->n[0] + 1, g->n[1] + 1);
-    CG_CHECK_LAUNCH(ctx);
+        stress_launch<T, ND>(g, v, s, res, NoMask<T>{}, block, st);
+    return cudaGetLastError();
+}
+
+// update_velocity! over [0, n+1]^N; with `mask`, the pressure and stress derivatives are the
+// masked operators.
+template <class T, int ND>
+cudaError_t velocity_any(const cg_grid* g, const cg_stokes_fields* f, const cg_stokes_params* p, bool res,
+                         const Pre* pr, const cg_mask* mask, dim3 block, cudaStream_t st) {
+    SV<T> v = views<T>(f, ND);
+    apply_pre(v, pr);
+    const SP<T> s = scalars<T>(g, p);
+    if (mask)
+        velocity_launch<T, ND>(g, v, s, body_fns<T>(g, p), res, mask_views<T>(mask), block, st);
+    else
+        velocity_launch<T, ND>(g, v, s, body_fns<T>(g, p), res, NoMask<T>{}, block, st);
+    return cudaGetLastError();
+}
+
+template <class T, int ND>
+int launch_stress(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f, const cg_stokes_params* p, bool res,
+                  const Pre* pr = nullptr, const cg_mask* mask = nullptr, dim3 block = dim3(32, 8)) {
+    const cudaError_t e = stress_any<T, ND>(g, f, p, res, pr, mask, block, ctx->stream);
+    if (e != cudaSuccess) return cg_fail(ctx, CG_ERR_CUDA, "update_stress: %s", cudaGetErrorString(e));
     return CG_OK;
 }
 
 template <class T, int ND>
 int launch_velocity(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f, const cg_stokes_params* p, bool res,
-                    const Pre* pr = nullptr) {
-    dim3 block(32, 8);
-    SV<T> v = views<T>(f, ND);
-    apply_pre(v, pr);
-    const SP<T> s = scalars<T>(g, p);
-    if (res)
-        velocity_kernel<T, ND, true><<<range_grid<ND>(g, block), block, 0, ctx->stream>>>(v, s, body_fns<T>(g, p), g->n[0] + 1,
-                                                                                       g->n[1] + 1);
-    else
-        velocity_kernel<T, ND, false><<<range_grid<ND>(g, block), block, 0, ctx->stream>>>(v, s, body_fns<T>(g, p), g->n[0] + 1,
-                                                                                        g->n[1] + 1);
-    CG_CHECK_LAUNCH(ctx);
+                    const Pre* pr = nullptr, const cg_mask* mask = nullptr, dim3 block = dim3(32, 8)) {
+    const cudaError_t e = velocity_any<T, ND>(g, f, p, res, pr, mask, block, ctx->stream);
+    if (e != cudaSuccess) return cg_fail(ctx, CG_ERR_CUDA, "update_velocity: %s", cudaGetErrorString(e));
+    return CG_OK;
+}
+
+// Bytes from a field's first stored element to its last (the whole padded array).
+size_t padded_span_bytes(const cg_field& f) {
+    size_t span = 1;
+    for (int d = 0; d < f.ndim; ++d) span += (size_t)(f.n[d] + 4 * f.halo[d] - 1) * (size_t)f.stride[d];
+    return span * (f.dtype == CG_F64 ? 8 : 4);
+}
+
+// Block shapes of the stress and velocity kernels of a PT loop over this field set (tune_block;
+// cached per grid, precision, layout and kernel form). The kernels update P, tau, V in place
+// and write divV and r_V, so the candidates run on copies of those fields in a temporary
+// allocation, released before the loop's graph is captured; the caller's fields are untouched.
+template <class T, int ND>
+int stokes_blocks(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f, const cg_stokes_params* p, const Pre* pr,
+                  const cg_mask* mask, dim3* bs, dim3* bv) {
+    *bs = *bv = dim3(32, 8);
+    dim3 forced;
+    if (cg_block_forced(&forced)) {
+        *bs = *bv = forced;
+        return CG_OK;
+    }
+    if (!cg_autotune_enabled()) return CG_OK;
+    std::string base = "stokes_blocks";
+    cg_key_add(base, *g);
+    cg_key_add(base, (int)sizeof(T));
+    cg_key_add(base, f->V[0].stride);
+    cg_key_add(base, f->tau[0].stride);
+    cg_key_add(base, (int)cg_present(f->eta) + 2 * (int)cg_present(f->inv_eta) + 4 * (pr != nullptr) + 8 * (mask != nullptr));
+    cg_key_add(base, ctx->num_sms);
+    const std::string ks = base + "stress", kv = base + "velocity";
+    cg_tune_cfg c1{0, 0}, c2{0, 0};
+    if (cg_tune_lookup(ks, &c1) && cg_tune_lookup(kv, &c2)) {
+        *bs = dim3((unsigned)c1.seg, (unsigned)c1.variant);
+        *bv = dim3((unsigned)c2.seg, (unsigned)c2.variant);
+        return CG_OK;
+    }
+    const int nt = ND == 2 ? 3 : 6;
+    cg_stokes_fields c = *f;
+    cg_field* upd[1 + 1 + 6 + 3 + 3];
+    int nu = 0;
+    upd[nu++] = &c.P;
+    if (cg_present(c.divV)) upd[nu++] = &c.divV;
+    for (int t = 0; t < nt; ++t) upd[nu++] = &c.tau[t];
+    for (int d = 0; d < ND; ++d) {
+        upd[nu++] = &c.V[d];
+        if (cg_present(c.r_V[d])) upd[nu++] = &c.r_V[d];
+    }
+    size_t off[16], total = 0;
+    for (int a = 0; a < nu; ++a) {
+        off[a] = total;
+        total += (padded_span_bytes(*upd[a]) + 255) & ~(size_t)255;
+    }
+    char* tmp = nullptr;
+    if (cudaMalloc(&tmp, total) != cudaSuccess) {
+        cudaGetLastError();
+        return CG_OK;  // no room to time the candidates: the default shape
+    }
+    for (int a = 0; a < nu; ++a) {
+        const cudaError_t e = cudaMemcpyAsync(tmp + off[a], upd[a]->data, padded_span_bytes(*upd[a]),
+                                              cudaMemcpyDeviceToDevice, ctx->stream);
+        if (e != cudaSuccess) {
+            cudaFree(tmp);
+            return cg_fail(ctx, CG_ERR_CUDA, "stokes block tuning: %s", cudaGetErrorString(e));
+        }
+        upd[a]->data = tmp + off[a];
+    }
+    *bs = cgk::tune_block("update_stress", ks,
+                          [&](dim3 b) { return stress_any<T, ND>(g, &c, p, true, pr, mask, b, ctx->stream); }, ctx->stream);
+    *bv = cgk::tune_block("update_velocity", kv,
+                          [&](dim3 b) { return velocity_any<T, ND>(g, &c, p, true, pr, mask, b, ctx->stream); }, ctx->stream);
+    cudaStreamSynchronize(ctx->stream);
+    cudaFree(tmp);
+    return CG_OK;
+}
+
+// The mask entries the masked Stokes kernels read, checked against the grid and dtype:
+// update_stress! the velocity locations (bits 1 << d); update_velocity! the cell (0) and the
+// shear locations (2D: 3; 3D: 3, 5, 6).
+enum { MASK_STRESS = 1, MASK_VELOCITY = 2 };
+int check_stokes_mask(cg_ctx* ctx, const cg_grid* g, const cg_mask* m, int dtype, int which) {
+    if (!m) return cg_fail(ctx, CG_ERR_ARG, "masked stokes: mask is NULL");
+    const int nd = g->ndim;
+    int rc;
+    if (which & MASK_STRESS)
+        for (int d = 0; d < nd; ++d)
+            if ((rc = cg_check_field(ctx, g, m->at[1 << d], dtype, 1 << d, "mask (velocity location)"))) return rc;
+    if (which & MASK_VELOCITY) {
+        if ((rc = cg_check_field(ctx, g, m->at[0], dtype, 0, "mask (cell)"))) return rc;
+        const int shear[3] = {3, 5, 6};
+        for (int e = 0; e < (nd == 2 ? 1 : 3); ++e)
+            if ((rc = cg_check_field(ctx, g, m->at[shear[e]], dtype, shear[e], "mask (shear location)"))) return rc;
+    }
     return CG_OK;
 }
 
@@ -241,13 +376,6 @@ int apply_bc_V(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f, const c
     return cg_bc_apply_impl(ctx, g, g->ndim, f->V, bc_V);
 }
 
-// Bytes from a field's first stored element to its last (the whole padded array).
-size_t padded_span_bytes(const cg_field& f) {
-    size_t span = 1;
-    for (int d = 0; d < f.ndim; ++d) span += (size_t)(f.n[d] + 4 * f.halo[d] - 1) * (size_t)f.stride[d];
-    return span * (f.dtype == CG_F64 ? 8 : 4);
-}
-
 // The library's partner buffer of T for the thermal ping-pong (scratch slot 0, T's layout).
 int thermal_partner(cg_ctx* ctx, const cg_field& Tf, cg_field* out) {
     int rc = 0;
@@ -262,7 +390,8 @@ int thermal_partner(cg_ctx* ctx, const cg_field& Tf, cg_field* out) {
 // step and bc!(T) (examples/stokes_2d_inc_ve_T.jl:144-152). T alternates with the library's
 // partner buffer and ends in f->T.
 int pt_iterations(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f, const cg_stokes_params* p,
-                  const cg_bc* bc_V, int niter, int dtype, const Pre* pr = nullptr, const cg_bc* bc_T = nullptr) {
+                  const cg_bc* bc_V, int niter, int dtype, const Pre* pr = nullptr, const cg_bc* bc_T = nullptr,
+                  const cg_mask* mask = nullptr) {
     cg_field Tw;
     std::memset(&Tw, 0, sizeof(Tw));
     if (bc_T) {
@@ -283,16 +412,23 @@ int pt_iterations(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f, cons
         cg_key_add(key, *bc_T);
         cg_key_add(key, Tw.data);
     }
+    cg_key_add(key, mask ? 1 : 0);
+    if (mask) cg_key_add(key, *mask);
     const int nd = g->ndim;
+    dim3 bs, bv;
+    int rc0 = SDISPATCH(stokes_blocks, dtype, nd, ctx, g, f, p, pr, mask, &bs, &bv);
+    if (rc0) return rc0;
+    cg_key_add(key, bs);
+    cg_key_add(key, bv);
     const size_t tbytes = bc_T ? padded_span_bytes(f->T) : 0;
     return cg_graph_run(ctx, key, [&](cudaStream_t st) {
         // the partner starts as a copy, so that points no step writes agree in both buffers
         if (bc_T) CG_CUDA(ctx, cudaMemcpyAsync(Tw.data, f->T.data, tbytes, cudaMemcpyDeviceToDevice, st));
         for (int it = 0; it < niter; ++it) {
             const bool last = it == niter - 1;
-            int rc = SDISPATCH(launch_stress, dtype, nd, ctx, g, f, p, last, pr);
+            int rc = SDISPATCH(launch_stress, dtype, nd, ctx, g, f, p, last, pr, mask, bs);
             if (rc) return rc;
-            rc = SDISPATCH(launch_velocity, dtype, nd, ctx, g, f, p, last, pr);
+            rc = SDISPATCH(launch_velocity, dtype, nd, ctx, g, f, p, last, pr, mask, bv);
             if (rc) return rc;
             rc = apply_bc_V(ctx, g, f, bc_V);
             if (rc) return rc;
@@ -395,6 +531,44 @@ extern "C" int cg_stokes_pt_iterations(cg_ctx* ctx, const cg_grid* grid, const c
     if (niter == 0) return CG_OK;
     cudaSetDevice(ctx->device);
     return pt_iterations(ctx, grid, f, p, bc_V, niter, dtype);
+}
+
+extern "C" int cg_stokes_update_stress_masked(cg_ctx* ctx, const cg_grid* grid, const cg_stokes_fields* f,
+                                              const cg_stokes_params* p, const cg_mask* mask) {
+    int dtype;
+    int rc = check_stokes(ctx, grid, f, NEED_V | NEED_TAU | NEED_TAU_OLD | NEED_P, &dtype);
+    if (rc) return rc;
+    if (!p) return cg_fail(ctx, CG_ERR_ARG, "update_stress_masked: params is NULL");
+    if ((rc = check_stokes_mask(ctx, grid, mask, dtype, MASK_STRESS))) return rc;
+    cudaSetDevice(ctx->device);
+    return SDISPATCH(launch_stress, dtype, grid->ndim, ctx, grid, f, p, true, nullptr, mask);
+}
+
+extern "C" int cg_stokes_update_velocity_masked(cg_ctx* ctx, const cg_grid* grid, const cg_stokes_fields* f,
+                                                const cg_stokes_params* p, const cg_mask* mask) {
+    int dtype;
+    int rc = check_stokes(ctx, grid, f, NEED_V | NEED_TAU | NEED_P, &dtype);
+    if (rc) return rc;
+    if (!p) return cg_fail(ctx, CG_ERR_ARG, "update_velocity_masked: params is NULL");
+    if ((rc = check_body(ctx, grid, f, p))) return rc;
+    if ((rc = check_stokes_mask(ctx, grid, mask, dtype, MASK_VELOCITY))) return rc;
+    cudaSetDevice(ctx->device);
+    return SDISPATCH(launch_velocity, dtype, grid->ndim, ctx, grid, f, p, true, nullptr, mask);
+}
+
+extern "C" int cg_stokes_pt_iterations_masked(cg_ctx* ctx, const cg_grid* grid, const cg_stokes_fields* f,
+                                              const cg_stokes_params* p, const cg_bc* bc_V, const cg_mask* mask,
+                                              int niter) {
+    int dtype;
+    int rc = check_stokes(ctx, grid, f, NEED_V | NEED_TAU | NEED_TAU_OLD | NEED_P, &dtype);
+    if (rc) return rc;
+    if (!p) return cg_fail(ctx, CG_ERR_ARG, "pt_iterations_masked: params is NULL");
+    if ((rc = check_body(ctx, grid, f, p))) return rc;
+    if ((rc = check_stokes_mask(ctx, grid, mask, dtype, MASK_STRESS | MASK_VELOCITY))) return rc;
+    if (niter < 0) return cg_fail(ctx, CG_ERR_ARG, "pt_iterations_masked: niter < 0");
+    if (niter == 0) return CG_OK;
+    cudaSetDevice(ctx->device);
+    return pt_iterations(ctx, grid, f, p, bc_V, niter, dtype, nullptr, nullptr, mask);
 }
 
 namespace {

@@ -176,6 +176,24 @@ __device__ __forceinline__ T shear_inv_eta(const SV<T>& v, int i, int j, int k, 
     return fma(T(0.5), hi - lo, lo);
 }
 
+// Operand readers of the stress and velocity kernels. NoMask reads a value; FieldMaskW is
+// Chmy's FieldMask (src/GridOperators/field_mask.jl:1-117) seen by the masked operators
+// (src/GridOperators/masked_operators.jl:11-39): every operand of a derivative is multiplied by
+// the mask at its own location and index. `loc` is the operand's location bits (bit d set for
+// Vertex along d), the index into the mask's weight fields. With unit weights both readers give
+// the same bits (x * 1 == x, also under contraction into a fused multiply-add).
+template <class T>
+struct NoMask {
+    __device__ __forceinline__ T operator()(int, const DF<T>& f, int i, int j, int k) const { return f(i, j, k); }
+};
+template <class T>
+struct FieldMaskW {
+    DF<T> w[8];
+    __device__ __forceinline__ T operator()(int loc, const DF<T>& f, int i, int j, int k) const {
+        return f(i, j, k) * w[loc](i, j, k);
+    }
+};
+
 // Viscosity terms used by every PT iteration, computed once per solve over [0, n+1]^N with the
 // stress kernel's own expressions (so the values are bit-identical).
 template <class T, int ND>
@@ -194,8 +212,10 @@ __global__ void precompute_kernel(const SV<T> v, const SP<T> s, int e0, int e1) 
 }
 
 // update_stress! at one point. Tensor order 2D (xx, yy, xy), 3D (xx, yy, zz, xy, xz, yz).
-template <class T, int ND, bool WRITE_RES>
-__global__ void stress_kernel(const SV<T> v, const SP<T> s, int e0, int e1) {
+// M reads the operands of the strain-rate derivatives (NoMask, or FieldMaskW for the masked
+// operators ∂(V.d, ω, g, I) and divg(V, ω, g, I)); V.d sits at location bits 1 << d.
+template <class T, int ND, bool WRITE_RES, class M>
+__global__ void stress_kernel(const SV<T> v, const SP<T> s, int e0, int e1, const M m) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = ND > 2 ? blockIdx.z : 0;
@@ -203,13 +223,13 @@ __global__ void stress_kernel(const SV<T> v, const SP<T> s, int e0, int e1) {
     const DF<T>& Vx = v.V[0];
     const DF<T>& Vy = v.V[1];
     // ∂x(V.x) at Center: V.x is Vertex in x -> V.x[i+1] - V.x[i]
-    const T exx = (Vx(i + 1, j, k) - Vx(i, j, k)) * s.idx[0];
-    const T eyy = (Vy(i, j + 1, k) - Vy(i, j, k)) * s.idx[1];
+    const T exx = (m(1, Vx, i + 1, j, k) - m(1, Vx, i, j, k)) * s.idx[0];
+    const T eyy = (m(2, Vy, i, j + 1, k) - m(2, Vy, i, j, k)) * s.idx[1];
     T dv = exx + eyy;
     T ezz = T(0);
     if (ND > 2) {
         const DF<T>& Vz = v.V[2];
-        ezz = (Vz(i, j, k + 1) - Vz(i, j, k)) * s.idx[2];
+        ezz = (m(4, Vz, i, j, k + 1) - m(4, Vz, i, j, k)) * s.idx[2];
         dv = dv + ezz;
     }
     const T dvP = v.has_fP ? dv + v.fP(i, j, k) : dv;
@@ -251,15 +271,18 @@ __global__ void stress_kernel(const SV<T> v, const SP<T> s, int e0, int e1) {
         }
     };
     // ∂y(V.x) at the xy vertex: V.x is Center in y -> V.x[j] - V.x[j-1]
-    const T exy = T(0.5) * ((Vx(i, j, k) - Vx(i, j - 1, k)) * s.idx[1] + (Vy(i, j, k) - Vy(i - 1, j, k)) * s.idx[0]);
+    const T exy = T(0.5) * ((m(1, Vx, i, j, k) - m(1, Vx, i, j - 1, k)) * s.idx[1] +
+                            (m(2, Vy, i, j, k) - m(2, Vy, i - 1, j, k)) * s.idx[0]);
     if (ND == 2) {
         diag(0, exx);
         diag(1, eyy);
         shear(2, exy, 0, 1);
     } else {
         const DF<T>& Vz = v.V[2];
-        const T exz = T(0.5) * ((Vx(i, j, k) - Vx(i, j, k - 1)) * s.idx[2] + (Vz(i, j, k) - Vz(i - 1, j, k)) * s.idx[0]);
-        const T eyz = T(0.5) * ((Vy(i, j, k) - Vy(i, j, k - 1)) * s.idx[2] + (Vz(i, j, k) - Vz(i, j - 1, k)) * s.idx[1]);
+        const T exz = T(0.5) * ((m(1, Vx, i, j, k) - m(1, Vx, i, j, k - 1)) * s.idx[2] +
+                                (m(4, Vz, i, j, k) - m(4, Vz, i - 1, j, k)) * s.idx[0]);
+        const T eyz = T(0.5) * ((m(2, Vy, i, j, k) - m(2, Vy, i, j, k - 1)) * s.idx[2] +
+                                (m(4, Vz, i, j, k) - m(4, Vz, i, j - 1, k)) * s.idx[1]);
         diag(0, exx);
         diag(1, eyy);
         diag(2, ezz);
@@ -269,9 +292,10 @@ __global__ void stress_kernel(const SV<T> v, const SP<T> s, int e0, int e1) {
     }
 }
 
-// update_velocity! at one point.
-template <class T, int ND, bool WRITE_RES>
-__global__ void velocity_kernel(const SV<T> v, const SP<T> s, const BodyFn<T> bf, int e0, int e1) {
+// update_velocity! at one point. M reads the operands of the pressure and stress derivatives
+// (P and τ_dd at location bits 0, τ_xy 3, τ_xz 5, τ_yz 6).
+template <class T, int ND, bool WRITE_RES, class M>
+__global__ void velocity_kernel(const SV<T> v, const SP<T> s, const BodyFn<T> bf, int e0, int e1, const M m) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = ND > 2 ? blockIdx.z : 0;
@@ -284,20 +308,21 @@ __global__ void velocity_kernel(const SV<T> v, const SP<T> s, const BodyFn<T> bf
     const DF<T>& txy = v.tau[XY];
     // P, τ_dd are Center: at a face along d, left = I - e_d, right = I.
     // τ_xy is Vertex in x and y: ∂y(τxy) at a V.x face (Vertex x, Center y) -> τxy[j+1] - τxy[j].
-    T rx = -((P(i, j, k) - P(i - 1, j, k)) * s.idx[0]) + (txx(i, j, k) - txx(i - 1, j, k)) * s.idx[0];
-    rx = rx + (txy(i, j + 1, k) - txy(i, j, k)) * s.idx[1];
-    T ry = -((P(i, j, k) - P(i, j - 1, k)) * s.idx[1]) + (tyy(i, j, k) - tyy(i, j - 1, k)) * s.idx[1];
-    ry = ry + (txy(i + 1, j, k) - txy(i, j, k)) * s.idx[0];
+    const int LXY = 3, LXZ = 5, LYZ = 6;  // location bits of the shear components
+    T rx = -((m(0, P, i, j, k) - m(0, P, i - 1, j, k)) * s.idx[0]) + (m(0, txx, i, j, k) - m(0, txx, i - 1, j, k)) * s.idx[0];
+    rx = rx + (m(LXY, txy, i, j + 1, k) - m(LXY, txy, i, j, k)) * s.idx[1];
+    T ry = -((m(0, P, i, j, k) - m(0, P, i, j - 1, k)) * s.idx[1]) + (m(0, tyy, i, j, k) - m(0, tyy, i, j - 1, k)) * s.idx[1];
+    ry = ry + (m(LXY, txy, i + 1, j, k) - m(LXY, txy, i, j, k)) * s.idx[0];
     T rz = T(0);
     if (ND > 2) {
         const DF<T>& tzz = v.tau[2];
         const DF<T>& txz = v.tau[4];
         const DF<T>& tyz = v.tau[5];
-        rx = rx + (txz(i, j, k + 1) - txz(i, j, k)) * s.idx[2];
-        ry = ry + (tyz(i, j, k + 1) - tyz(i, j, k)) * s.idx[2];
-        rz = -((P(i, j, k) - P(i, j, k - 1)) * s.idx[2]) + (tzz(i, j, k) - tzz(i, j, k - 1)) * s.idx[2];
-        rz = rz + (txz(i + 1, j, k) - txz(i, j, k)) * s.idx[0];
-        rz = rz + (tyz(i, j + 1, k) - tyz(i, j, k)) * s.idx[1];
+        rx = rx + (m(LXZ, txz, i, j, k + 1) - m(LXZ, txz, i, j, k)) * s.idx[2];
+        ry = ry + (m(LYZ, tyz, i, j, k + 1) - m(LYZ, tyz, i, j, k)) * s.idx[2];
+        rz = -((m(0, P, i, j, k) - m(0, P, i, j, k - 1)) * s.idx[2]) + (m(0, tzz, i, j, k) - m(0, tzz, i, j, k - 1)) * s.idx[2];
+        rz = rz + (m(LXZ, txz, i + 1, j, k) - m(LXZ, txz, i, j, k)) * s.idx[0];
+        rz = rz + (m(LYZ, tyz, i, j + 1, k) - m(LYZ, tyz, i, j, k)) * s.idx[1];
     }
     if (v.has_rho[0]) rx = rx - v.rho[0](i, j, k);
     else if (bf.fn[0].kind) rx = rx - body_fn(bf, 0, ND, i, j, k);

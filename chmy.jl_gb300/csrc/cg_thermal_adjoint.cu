@@ -15,12 +15,13 @@
 // ended with bc!(T)): a ghost's term is folded into the cell it follows (Neumann +1, Dirichlet
 // on a Center field -1, Periodic: the opposite cell). Each thread owns one interior cell: its
 // left faces (and its right faces on the last cell of a dimension), so no two threads write one
-// address; dJ/dlambda is summed per cell in FP64 and once, in a fixed order, at the end.
+// address; dJ/dlambda is summed in FP64 per block in a fixed order (warp shuffles, then the
+// warps in order) and, when the caller asks for it, over the blocks in a fixed order.
 #include "cg_common.cuh"
 
 namespace {
 
-constexpr int kThermalSlot = 9;  // ctx scratch slot: per-cell dJ/dlambda terms and their sum
+constexpr int kThermalSlot = 9;  // ctx scratch slot: per-block dJ/dlambda partials and their sum
 
 template <class T>
 struct ThermalAdj {
@@ -42,12 +43,25 @@ __device__ __forceinline__ T vneg1(T v) {  // d min(v, 0)/dv
     return T(0) < v ? T(0) : T(1);
 }
 
+// Sum of a block's per-thread values in a fixed order (warp shuffles, then the warps in order),
+// written to part[block]: the same bits on every run.
+__device__ __forceinline__ void block_sum_fixed(double v, double* part) {
+    __shared__ double warp_part[32];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int t = threadIdx.x + blockDim.x * threadIdx.y;
+    const int nw = (blockDim.x * blockDim.y + 31) / 32;
+    if ((t & 31) == 0) warp_part[t >> 5] = v;
+    __syncthreads();
+    if (t == 0) {
+        double s = 0.0;
+        for (int w = 0; w < nw; ++w) s += warp_part[w];
+        part[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)] = s;
+    }
+}
+
+// The cell (i, j, k)'s outputs; returns its dJ/dlambda term.
 template <class T, int ND>
-__global__ void thermal_adjoint_kernel(const ThermalAdj<T> a) {
-    const int i = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
-    const int j = 1 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
-    const int k = ND > 2 ? 1 + (int)blockIdx.z : 0;
-    if (i > a.n[0] || j > a.n[1]) return;
+__device__ __forceinline__ double thermal_adjoint_cell(const ThermalAdj<T>& a, int i, int j, int k) {
     const int c[3] = {i, j, k};
     const T mc = a.mu(i, j, k);
     const T tc = a.Tin(i, j, k);
@@ -98,8 +112,18 @@ __global__ void thermal_adjoint_kernel(const ThermalAdj<T> a) {
     }
     a.gT(i, j, k) = g;
     if (a.has_gTold) a.gTold(i, j, k) = mc;
-    const long q = (long)(i - 1) + (long)a.n[0] * ((long)(j - 1) + (long)a.n[1] * (ND > 2 ? (long)(k - 1) : 0));
-    a.gacc[q] = dl;
+    return dl;
+}
+
+template <class T, int ND>
+__global__ void __launch_bounds__(256) thermal_adjoint_kernel(const ThermalAdj<T> a) {
+    const int i = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int j = 1 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    const int k = ND > 2 ? 1 + (int)blockIdx.z : 0;
+    // every thread reaches the block sum once; threads beyond the grid add 0 to it
+    double dl = 0.0;
+    if (i <= a.n[0] && j <= a.n[1]) dl = thermal_adjoint_cell<T, ND>(a, i, j, k);
+    block_sum_fixed(dl, a.gacc);
 }
 
 // Sum of `n` doubles in a fixed order (one block; see the diffusion adjoint's sum).
@@ -114,6 +138,11 @@ __global__ void __launch_bounds__(1024) thermal_sum_kernel(const double* __restr
         __syncthreads();
     }
     if (threadIdx.x == 0) *out = part[0];
+}
+
+inline dim3 thermal_adjoint_block() { return dim3(32, 8); }
+inline dim3 thermal_adjoint_grid(const cg_grid* g, dim3 b) {
+    return dim3(cg_div_up(g->n[0], b.x), cg_div_up(g->n[1], b.y), g->ndim > 2 ? g->n[2] : 1);
 }
 
 template <class T, int ND>
@@ -138,14 +167,14 @@ int thermal_adjoint_t(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f, 
     a.lam = (T)p->lambda_rhoCp;
     a.dt = (T)p->dt;
     a.gacc = gacc;
-    const dim3 b(32, 8);
-    const dim3 grid(cg_div_up(g->n[0], b.x), cg_div_up(g->n[1], b.y), ND > 2 ? g->n[2] : 1);
+    const dim3 b = thermal_adjoint_block();
+    const dim3 grid = thermal_adjoint_grid(g, b);
     thermal_adjoint_kernel<T, ND><<<grid, b, 0, ctx->stream>>>(a);
     CG_CHECK_LAUNCH(ctx);
-    long ncell = 1;
-    for (int d = 0; d < ND; ++d) ncell *= g->n[d];
-    thermal_sum_kernel<<<1, 1024, 0, ctx->stream>>>(gacc, ncell, sum);
-    CG_CHECK_LAUNCH(ctx);
+    if (sum) {
+        thermal_sum_kernel<<<1, 1024, 0, ctx->stream>>>(gacc, (long)grid.x * grid.y * grid.z, sum);
+        CG_CHECK_LAUNCH(ctx);
+    }
     return CG_OK;
 }
 
@@ -185,11 +214,11 @@ extern "C" int cg_stokes_thermal_step_adjoint(cg_ctx* ctx, const cg_grid* grid, 
                                "Periodic rule", s, d);
         }
     cudaSetDevice(ctx->device);
-    long ncell = 1;
-    for (int d = 0; d < nd; ++d) ncell *= grid->n[d];
-    double* gacc = static_cast<double*>(cg_scratch(ctx, kThermalSlot, (size_t)(ncell + 32) * sizeof(double), &rc));
+    const dim3 tg = thermal_adjoint_grid(grid, thermal_adjoint_block());
+    const long nblocks = (long)tg.x * tg.y * tg.z;
+    double* gacc = static_cast<double*>(cg_scratch(ctx, kThermalSlot, (size_t)(nblocks + 32) * sizeof(double), &rc));
     if (rc) return rc;
-    double* sum = gacc + ncell;
+    double* sum = dJ ? gacc + nblocks : nullptr;
     rc = dtype == CG_F64 ? (nd == 2 ? thermal_adjoint_t<double, 2>(ctx, grid, f, p, rule, *mu, *gT, gT_old, gV, gacc, sum)
                                     : thermal_adjoint_t<double, 3>(ctx, grid, f, p, rule, *mu, *gT, gT_old, gV, gacc, sum))
                          : (nd == 2 ? thermal_adjoint_t<float, 2>(ctx, grid, f, p, rule, *mu, *gT, gT_old, gV, gacc, sum)

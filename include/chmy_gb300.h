@@ -334,6 +334,23 @@ CG_API int cg_stokes_update_thermal(cg_ctx* ctx, const cg_grid* grid, const cg_s
 CG_API int cg_stokes_pt_iterations(cg_ctx* ctx, const cg_grid* grid, const cg_stokes_fields* f,
                             const cg_stokes_params* p, const cg_bc* bc_V, int niter);
 
+/* The same kernels with Chmy's masked operators (src/GridOperators/masked_operators.jl:11-39,
+ * masked_field_operators.jl), as a user writes them with a FieldMask ω (docs/src/concepts/
+ * grid_operators.md "Masking"): update_stress! with ∂(V.d, ω, g, I) for every strain rate and
+ * divg(V, ω, g, I); update_velocity! with ∂(Pr, ω, g, I) and ∂(τ.c, ω, g, I). Each operand of a
+ * derivative is multiplied by the mask at its own location and index; the viscosity terms, the
+ * stress's own values and the body force are not masked. Mask entries read (cg_mask.at by
+ * location bits): update_stress! the velocity locations 1 << d; update_velocity! the cell (0)
+ * and the shear locations (2D: 3; 3D: 3, 5, 6); the PT chunk both. With unit weights the
+ * results equal the unmasked entries' bit for bit. */
+CG_API int cg_stokes_update_stress_masked(cg_ctx* ctx, const cg_grid* grid, const cg_stokes_fields* f,
+                                          const cg_stokes_params* p, const cg_mask* mask);
+CG_API int cg_stokes_update_velocity_masked(cg_ctx* ctx, const cg_grid* grid, const cg_stokes_fields* f,
+                                            const cg_stokes_params* p, const cg_mask* mask);
+CG_API int cg_stokes_pt_iterations_masked(cg_ctx* ctx, const cg_grid* grid, const cg_stokes_fields* f,
+                                          const cg_stokes_params* p, const cg_bc* bc_V, const cg_mask* mask,
+                                          int niter);
+
 /* Ping-pong form of cg_stokes_pt_iterations for 2D and 3D variable viscosity. Each
  * iteration is one fused launch: update_stress! and update_velocity! together, in a kernel
  * that marches over rows (2D) or planes (3D). It reads V, P, tau from `a` and writes them to
@@ -426,8 +443,8 @@ CG_API int cg_stokes_thermal_step(cg_ctx* ctx, const cg_grid* grid, const cg_sto
  *   gV[d]   dJ/dV.d at the faces an interior cell reads (normal index 1..n+1, tangential 1..n),
  *           with the upwind branches the forward took (max(V, 0) and min(V, 0) both follow V at
  *           V = 0, as the kernel's comparisons do);
- * and dJ (host, may be NULL) gains dJ/dlambda_rhoCp in dJ[0] (summed per cell in FP64, then in a
- * fixed order; the call then synchronises the stream). f supplies T and V at the step's input;
+ * and dJ (host, may be NULL) gains dJ/dlambda_rhoCp in dJ[0] (summed in FP64 per block of cells
+ * and then over the blocks, both in a fixed order; the call then synchronises the stream). f supplies T and V at the step's input;
  * p supplies lambda_rhoCp and dt. */
 CG_API int cg_stokes_thermal_step_adjoint(cg_ctx* ctx, const cg_grid* grid, const cg_stokes_fields* f,
                                           const cg_stokes_params* p, const cg_bc* bc_T, const cg_field* mu,

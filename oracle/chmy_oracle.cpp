@@ -418,9 +418,16 @@ struct InvEta {
     T at(const int* I) const { return have_inv ? ieta.at(I) : T(1) / eta.at(I); }
 };
 
+/* With `mask`, every derivative is the masked operator (mpartial, mdivg): the Stokes kernels
+ * written with a FieldMask ω as in docs/src/concepts/grid_operators.md ("Masking"). */
 template <class T>
-void stokes_update_stress_t(const cg_grid* grid, const cg_stokes_fields* f, const cg_stokes_params* p) {
+void stokes_update_stress_t(const cg_grid* grid, const cg_stokes_fields* f, const cg_stokes_params* p,
+                            const cg_mask* mask = nullptr) {
     GridT<T> g(*grid);
+    const Mask w{mask};
+    auto D = [&](const Fd<T>& fld, int d, int i, int j, int k) {
+        return mask ? mpartial(fld, w, g, d, i, j, k) : partial(fld, g, d, i, j, k);
+    };
     const int nd = g.nd;
     const Tens ti = tens_index(nd);
     Fd<T> V[3], tau[6], tau_old[6];
@@ -436,9 +443,9 @@ void stokes_update_stress_t(const cg_grid* grid, const cg_stokes_fields* f, cons
     const T eta_s = (T)p->eta, eta_ve_s = (T)p->eta_ve;
     const T inv_Gdt = T(1) / (G * dt), third = T(1) / T(3);
     launch_range(g, [&](int i, int j, int k) {
-        const T exx = partial(V[0], g, 0, i, j, k);
-        const T eyy = partial(V[1], g, 1, i, j, k);
-        const T dv = divg(V, g, i, j, k);
+        const T exx = D(V[0], 0, i, j, k);
+        const T eyy = D(V[1], 1, i, j, k);
+        const T dv = mask ? mdivg(V, w, g, i, j, k) : divg(V, g, i, j, k);
         T dvm = dv;
         if (divV.ok()) {
             divV(i, j, k) = dv;
@@ -481,15 +488,15 @@ void stokes_update_stress_t(const cg_grid* grid, const cg_stokes_fields* f, cons
             }
         };
         if (nd == 2) {
-            const T exy = T(0.5) * (partial(V[0], g, 1, i, j, k) + partial(V[1], g, 0, i, j, k));
+            const T exy = T(0.5) * (D(V[0], 1, i, j, k) + D(V[1], 0, i, j, k));
             upd_diag(ti.xx, exx);
             upd_diag(ti.yy, eyy);
             upd_off(ti.xy, exy, 0, 1);
         } else {
-            const T ezz = partial(V[2], g, 2, i, j, k);
-            const T exy = T(0.5) * (partial(V[0], g, 1, i, j, k) + partial(V[1], g, 0, i, j, k));
-            const T exz = T(0.5) * (partial(V[0], g, 2, i, j, k) + partial(V[2], g, 0, i, j, k));
-            const T eyz = T(0.5) * (partial(V[1], g, 2, i, j, k) + partial(V[2], g, 1, i, j, k));
+            const T ezz = D(V[2], 2, i, j, k);
+            const T exy = T(0.5) * (D(V[0], 1, i, j, k) + D(V[1], 0, i, j, k));
+            const T exz = T(0.5) * (D(V[0], 2, i, j, k) + D(V[2], 0, i, j, k));
+            const T eyz = T(0.5) * (D(V[1], 2, i, j, k) + D(V[2], 1, i, j, k));
             upd_diag(ti.xx, exx);
             upd_diag(ti.yy, eyy);
             upd_diag(ti.zz, ezz);
@@ -501,8 +508,13 @@ void stokes_update_stress_t(const cg_grid* grid, const cg_stokes_fields* f, cons
 }
 
 template <class T>
-void stokes_update_velocity_t(const cg_grid* grid, const cg_stokes_fields* f, const cg_stokes_params* p) {
+void stokes_update_velocity_t(const cg_grid* grid, const cg_stokes_fields* f, const cg_stokes_params* p,
+                              const cg_mask* mask = nullptr) {
     GridT<T> g(*grid);
+    const Mask w{mask};
+    auto D = [&](const Fd<T>& fld, int d, int i, int j, int k) {
+        return mask ? mpartial(fld, w, g, d, i, j, k) : partial(fld, g, d, i, j, k);
+    };
     const int nd = g.nd;
     const Tens ti = tens_index(nd);
     Fd<T> V[3], rV[3], rho[3], tau[6];
@@ -529,10 +541,10 @@ void stokes_update_velocity_t(const cg_grid* grid, const cg_stokes_fields* f, co
         for (int d = 0; d < nd; ++d) {
             /* r_V.d = -∂d(P) + ∂d(τ_dd) + Σ_{e≠d} ∂e(τ_de) [- ρg_d], summed left to right in
                the examples' order: x: (xx, xy, xz); y: (yy, xy, yz); z: (zz, xz, yz). */
-            T r = -partial(P, g, d, i, j, k) + partial(tau[comp(d, d)], g, d, i, j, k);
+            T r = -D(P, d, i, j, k) + D(tau[comp(d, d)], d, i, j, k);
             for (int e = 0; e < nd; ++e) {
                 if (e == d) continue;
-                r = r + partial(tau[comp(d, e)], g, e, i, j, k);
+                r = r + D(tau[comp(d, e)], e, i, j, k);
             }
             if (rho[d].ok()) r = r - rho[d](i, j, k);
             T rv = r;
@@ -1383,6 +1395,22 @@ int or_stokes_update_velocity(const cg_grid* grid, const cg_stokes_fields* f, co
     if (f->tau[0].dtype == CG_F64) stokes_update_velocity_t<double>(grid, f, p);
     else stokes_update_velocity_t<float>(grid, f, p);
     return CG_OK;
+}
+
+/* The Stokes kernels with the masked operators (every derivative's operands weighted by the
+ * FieldMask at their location and index). */
+int or_stokes_update_stress_masked(const cg_grid* grid, const cg_stokes_fields* f, const cg_stokes_params* p,
+                                   const cg_mask* mask) {
+    if (f->tau[0].dtype == CG_F64) stokes_update_stress_t<double>(grid, f, p, mask);
+    else stokes_update_stress_t<float>(grid, f, p, mask);
+    return 0;
+}
+
+int or_stokes_update_velocity_masked(const cg_grid* grid, const cg_stokes_fields* f, const cg_stokes_params* p,
+                                     const cg_mask* mask) {
+    if (f->tau[0].dtype == CG_F64) stokes_update_velocity_t<double>(grid, f, p, mask);
+    else stokes_update_velocity_t<float>(grid, f, p, mask);
+    return 0;
 }
 
 int or_stokes_update_thermal_flux(const cg_grid* grid, const cg_stokes_fields* f, const cg_stokes_params* p) {

@@ -45,6 +45,10 @@ _SIGS = {
     "or_stokes_update_old": ([P(_abi.cg_grid), P(_abi.cg_stokes_fields)], C.c_int),
     "or_stokes_update_stress": ([P(_abi.cg_grid), P(_abi.cg_stokes_fields), P(_abi.cg_stokes_params)], C.c_int),
     "or_stokes_update_velocity": ([P(_abi.cg_grid), P(_abi.cg_stokes_fields), P(_abi.cg_stokes_params)], C.c_int),
+    "or_stokes_update_stress_masked": ([P(_abi.cg_grid), P(_abi.cg_stokes_fields), P(_abi.cg_stokes_params), P(_abi.cg_mask)],
+                                       C.c_int),
+    "or_stokes_update_velocity_masked": ([P(_abi.cg_grid), P(_abi.cg_stokes_fields), P(_abi.cg_stokes_params), P(_abi.cg_mask)],
+                                         C.c_int),
     "or_stokes_update_thermal_flux": ([P(_abi.cg_grid), P(_abi.cg_stokes_fields), P(_abi.cg_stokes_params)], C.c_int),
     "or_stokes_update_thermal": ([P(_abi.cg_grid), P(_abi.cg_stokes_fields), P(_abi.cg_stokes_params)], C.c_int),
     "or_ptdiff_update_q": ([P(_abi.cg_grid), P(_abi.cg_ptdiff_fields), P(_abi.cg_ptdiff_params)], C.c_int),

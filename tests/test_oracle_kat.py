@@ -515,6 +515,87 @@ def test_masked_diffusion_oracle(T):
     assert approx(qm[0].a, qx, T) and approx(qm[1].a, qy, T) and approx(Cm.a, cn, T)
 
 
+def test_masked_stokes_oracle_matches_numpy():
+    """The oracle's Stokes kernels with the masked operators (update_stress! with ∂(V.d, ω) and
+    divg(V, ω), update_velocity! with ∂(Pr, ω) and ∂(τ, ω); 2D, scalar η, FP64) equal a numpy
+    evaluation of the example kernels (examples/stokes_2d_inc_ve_T.jl:20-43) with every
+    derivative operand weighted by the mask at its location and index, bit for bit; with unit
+    weights they equal the unmasked oracle kernels bit for bit."""
+    import ctypes
+
+    from _oracle import lib, stokes_desc
+    from chmy_gb300.kernels import stokes_params
+
+    T = np.float64
+    rng = np.random.default_rng(21)
+    nx, ny = 11, 8
+    grid = UniformGrid(origin=(-1.0, -1.0), extent=(2.0, 1.5), dims=(nx, ny), dtype=T)
+    g = grid.desc()
+    C_, V_ = Center(), Vertex()
+
+    def rnd(loc, scale=1.0):
+        f = NpField(grid, loc, T)
+        f.a[...] = scale * rng.standard_normal(f.a.shape)
+        return f
+
+    V0 = [rnd((V_, C_)), rnd((C_, V_))]
+    P0 = rnd(C_)
+    tl = [(C_, C_), (C_, C_), (V_, V_)]
+    tau0 = [rnd(l, 0.1) for l in tl]
+    tauo = [rnd(l, 0.1) for l in tl]
+    rho = rnd((C_, V_))
+    p = stokes_params(eta=1.3, eta_ve=1.0 / (1.0 / 1.3 + 1.0 / 0.02), G=2.0, dt=1e-2, dtau_Pr=0.3, dtau_r=0.2, nu_dtau=0.05)
+
+    def run(m):
+        V = [f.copy() for f in V0]
+        rV = vec_fields(grid, T)
+        P, divV = P0.copy(), NpField(grid, C_, T)
+        tau = [f.copy() for f in tau0]
+        d = stokes_desc(V=V, r_V=rV, P=P, divV=divV, tau=tau, tau_old=tauo, rho_g=[None, rho])
+        if m is None:
+            assert lib().or_stokes_update_stress(ctypes.byref(g), ctypes.byref(d), ctypes.byref(p)) == 0
+            assert lib().or_stokes_update_velocity(ctypes.byref(g), ctypes.byref(d), ctypes.byref(p)) == 0
+        else:
+            assert lib().or_stokes_update_stress_masked(ctypes.byref(g), ctypes.byref(d), ctypes.byref(p), ctypes.byref(m)) == 0
+            assert lib().or_stokes_update_velocity_masked(ctypes.byref(g), ctypes.byref(d), ctypes.byref(p), ctypes.byref(m)) == 0
+        return V, rV, P, divV, tau
+
+    _, ones = _np_mask_set(grid, T, rng, ones=True)
+    for a, b in zip(run(ones), run(None)):
+        for fa, fb in zip(a if isinstance(a, list) else [a], b if isinstance(b, list) else [b]):
+            assert np.array_equal(fa.a, fb.a)
+    wf, wm = _np_mask_set(grid, T, rng)
+    V, rV, P, divV, tau = run(wm)
+    # numpy: logical index I at padded I + 1; the launch range [0, n+1] is padded 1 .. n+2
+    idx, idy = (float(v) for v in grid.inv_spacing())
+    G, dt, eta, eve = p.G, p.dt, p.eta, p.eta_ve
+    J, I = np.meshgrid(np.arange(1, ny + 3), np.arange(1, nx + 3), indexing="ij")
+    vx, vy = V0[0].a * wf[1].a, V0[1].a * wf[2].a
+    exx = (vx[J, I + 1] - vx[J, I]) * idx
+    eyy = (vy[J + 1, I] - vy[J, I]) * idy
+    dv = exx + eyy
+    exy = 0.5 * ((vx[J, I] - vx[J - 1, I]) * idy + (vy[J, I] - vy[J, I - 1]) * idx)
+    Pn = P0.a.copy()
+    Pn[J, I] = P0.a[J, I] - dv * eve * p.dtau_Pr
+    tn = [f.a.copy() for f in tau0]
+    for c, e in ((0, exx - dv / 3.0), (1, eyy - dv / 3.0), (2, exy)):
+        t, to = tau0[c].a[J, I], tauo[c].a[J, I]
+        r = -(t - to) / (G * dt) - t / eta + 2.0 * e
+        tn[c][J, I] = t + r * eve * p.dtau_r
+    assert np.array_equal(divV.a[J, I], dv) and np.array_equal(P.a, Pn)
+    for c in range(3):
+        assert np.array_equal(tau[c].a, tn[c]), c
+    pw, txx, tyy, txy = Pn * wf[0].a, tn[0] * wf[0].a, tn[1] * wf[0].a, tn[2] * wf[3].a
+    rx = -((pw[J, I] - pw[J, I - 1]) * idx) + (txx[J, I] - txx[J, I - 1]) * idx
+    rx = rx + (txy[J + 1, I] - txy[J, I]) * idy
+    ry = -((pw[J, I] - pw[J - 1, I]) * idy) + (tyy[J, I] - tyy[J - 1, I]) * idy
+    ry = ry + (txy[J, I + 1] - txy[J, I]) * idx
+    ry = ry - rho.a[J, I]
+    assert np.array_equal(rV[0].a[J, I], rx) and np.array_equal(rV[1].a[J, I], ry)
+    assert np.array_equal(V[0].a[J, I], V0[0].a[J, I] + rx * p.nu_dtau / eve)
+    assert np.array_equal(V[1].a[J, I], V0[1].a[J, I] + ry * p.nu_dtau / eve)
+
+
 def test_sia_dual_tangents_match_oracle_differences():
     """The oracle's dual-number SIA loop (or_sia_run_tangent): its value equals the plain
     restated loop bit for bit, and its tangents along Gamma and ela agree with central
