@@ -102,6 +102,10 @@ class cg_function(C.Structure):
     _fields_ = [("kind", C.c_int32), ("pad_", C.c_int32), ("p", C.c_double * 8)]
 
 
+class cg_bc_fn(C.Structure):
+    _fields_ = [("fn", (cg_function * 2) * 3), ("full_dims", (C.c_int32 * 2) * 3)]
+
+
 class cg_stokes_params(C.Structure):
     _fields_ = [
         ("eta", C.c_double),
@@ -183,6 +187,7 @@ SIGNATURES: dict[str, list] = {
     "cg_field_upload": [_vp, P(cg_field), _vp],
     "cg_field_download": [_vp, P(cg_field), _vp],
     "cg_bc_apply": [_vp, P(cg_grid), C.c_int, P(cg_field), P(cg_bc)],
+    "cg_bc_apply_fn": [_vp, P(cg_grid), C.c_int, P(cg_field), P(cg_bc), P(cg_bc_fn)],
     "cg_maxabs": [_vp, C.c_int, P(cg_field), P(C.c_double), P(C.c_int32)],
     "cg_maxabs_noalloc": [C.c_int, _vp, C.c_int, P(cg_field), P(C.c_double), P(C.c_int32)],
     "cg_diffusion_compute_q": [_vp, P(cg_grid), P(cg_field), P(cg_field), C.c_double],

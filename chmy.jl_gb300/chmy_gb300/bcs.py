@@ -197,11 +197,24 @@ def bc_values(grid, loc, dtype, d: int, side: int, bc) -> np.ndarray:
     return out
 
 
-def materialize_bc(grid, loc, dtype, spec, device=None):
+def device_function_of(bc):
+    """The cg_function of a condition whose value is a continuous BoundaryFunction over a form
+    the library evaluates on the device (functions.constant / ball / affine), else None."""
+    from .functions import DeviceFunction
+
+    v = getattr(bc, "value", None)
+    if isinstance(v, BoundaryFunction) and not v.discrete and isinstance(v.fun, DeviceFunction):
+        return v
+    return None
+
+
+def materialize_bc(grid, loc, dtype, spec, device=None, fns=None):
     """A cg_bc for a field at `loc` whose conditions may carry per-point values. The value
     arrays live in host memory (device=None, for the oracle) or on `device` (a torch device).
-    Returns (cg_bc, keep): `keep` holds the arrays, and must stay alive while the cg_bc is
-    used."""
+    With `fns` (a cg_bc_fn), a continuous BoundaryFunction over a device form is recorded
+    there, to be evaluated by the boundary-condition kernel (cg_bc_apply_fn), instead of being
+    evaluated on the host. Returns (cg_bc, keep): `keep` holds the arrays, and must stay alive
+    while the cg_bc is used."""
     nd = grid.ndim
     b = _abi.cg_bc()
     keep = []
@@ -213,6 +226,14 @@ def materialize_bc(grid, loc, dtype, spec, device=None):
             b.kind[d][s] = bc.kind
             if _constant(bc.value):
                 b.value[d][s] = 0.0 if bc.value is None else float(bc.value)
+                continue
+            dfn = device_function_of(bc) if fns is not None else None
+            if dfn is not None and bc.kind in (_abi.CG_BC_DIRICHLET, _abi.CG_BC_NEUMANN):
+                nargs = nd if not dfn.reduce_dims else nd - 1
+                fns.fn[d][s].kind = dfn.fun.kind
+                for q, val in enumerate(dfn.fun.pack(nargs, dfn.parameters)):
+                    fns.fn[d][s].p[q] = val
+                fns.full_dims[d][s] = 0 if dfn.reduce_dims else 1
                 continue
             arr = bc_values(grid, loc, dtype, d, s, bc)
             if device is not None:
@@ -234,15 +255,18 @@ class Batch:
         self.grid = grid
         self.fields = []
         self.bcs = []
+        self.fns = []  # BoundaryFunction sides evaluated by the kernel (cg_bc_fn per field)
         self._keep = []  # per-point value arrays on the fields' device
         for f, spec in pairs:
             dev = getattr(getattr(f, "arch", None), "device", None)
-            b, keep = materialize_bc(grid, f.loc, f.dtype, spec, dev)
+            fn = _abi.cg_bc_fn() if dev is not None else None
+            b, keep = materialize_bc(grid, f.loc, f.dtype, spec, dev, fn)
             self._keep.extend(keep)
             if all(b.kind[d][s] == _abi.CG_BC_NONE for d in range(grid.ndim) for s in range(2)):
                 continue  # prune (batch.jl:235-239)
             self.fields.append(f)
             self.bcs.append(b)
+            self.fns.append(fn if fn is not None else _abi.cg_bc_fn())
 
     def __len__(self):
         return len(self.fields)
@@ -252,6 +276,9 @@ class Batch:
         fa = (_abi.cg_field * max(n, 1))(*[f.desc() for f in self.fields])
         ba = (_abi.cg_bc * max(n, 1))(*self.bcs)
         return n, fa, ba
+
+    def has_functions(self) -> bool:
+        return any(fn.fn[d][s].kind != _abi.CG_FN_NONE for fn in self.fns for d in range(3) for s in range(2))
 
 
 def batch(grid, *pairs, exchange=None) -> Batch:
@@ -265,12 +292,17 @@ def apply_batch(arch, grid, b: Batch) -> None:
         return
     n, fa, ba = b.descs()
     g = grid.desc()
+    with_fn = b.has_functions()
     # the library takes up to 8 fields per launch
     for start in range(0, n, 8):
         cnt = min(8, n - start)
         fsub = (_abi.cg_field * cnt)(*fa[start : start + cnt])
         bsub = (_abi.cg_bc * cnt)(*ba[start : start + cnt])
-        arch.call("cg_bc_apply", ctypes.byref(g), cnt, fsub, bsub)
+        if with_fn:
+            nsub = (_abi.cg_bc_fn * cnt)(*b.fns[start : start + cnt])
+            arch.call("cg_bc_apply_fn", ctypes.byref(g), cnt, fsub, bsub, nsub)
+        else:
+            arch.call("cg_bc_apply", ctypes.byref(g), cnt, fsub, bsub)
 
 
 def bc_(arch, grid, *pairs_or_batch, exchange=None) -> None:

@@ -193,6 +193,39 @@ inline float time_launches(F&& launch, cudaStream_t st) {
     return ms;
 }
 
+// A device FunctionField (cg_function) in the field precision.
+template <class T>
+struct FnDev {
+    int kind;
+    T p[8];
+};
+
+// coord(grid, loc, I) (src/Grids/uniform_axis.jl): Vertex muladd(I-1, Δ, o), Center
+// muladd(I-1, Δ, muladd(0.5, Δ, o)); muladd is a fused multiply-add, as on the CPU.
+template <class T>
+__device__ __forceinline__ T grid_coord(T org, T dx, int I, bool vertex) {
+    const T o = vertex ? org : rfma(T(0.5), dx, org);
+    return rfma(T(I - 1), dx, o);
+}
+
+// func(x...) of a device FunctionField at the point x (cg_function's forms; every operation
+// rounded once, left to right, as the CPU evaluates the Julia expression).
+template <class T>
+__device__ __forceinline__ T fn_eval(const FnDev<T>& f, int nd, const T* x) {
+    if (f.kind == CG_FN_CONST) return f.p[0];
+    if (f.kind == CG_FN_BALL) {
+        T r2 = rmul(rsub(x[0], f.p[0]), rsub(x[0], f.p[0]));
+        for (int d = 1; d < nd; ++d) r2 = radd(r2, rmul(rsub(x[d], f.p[d]), rsub(x[d], f.p[d])));
+        return r2 < rmul(f.p[3], f.p[3]) ? f.p[4] : f.p[5];
+    }
+    if (f.kind == CG_FN_AFFINE) {
+        T v = f.p[0];
+        for (int d = 0; d < nd; ++d) v = radd(v, rmul(f.p[1 + d], x[d]));
+        return v;
+    }
+    return T(0);
+}
+
 // Block shapes (threads along x, along y) the per-point kernels are timed over. Each thread
 // computes one point whatever the shape, so every shape gives the same bits.
 constexpr int kBlockShapes[7][2] = {{32, 8}, {32, 4}, {64, 4}, {128, 2}, {32, 16}, {64, 8}, {128, 4}};

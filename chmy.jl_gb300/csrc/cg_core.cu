@@ -369,10 +369,37 @@ struct BcField {
     T h[3];
 };
 
-// The value of phase (d, s) at the point q: the per-point array at q's tangential indices
-// (remove_dim(dim, I)), else the constant.
+// BoundaryFunction sides of a batch (cg_bc_fn), a separate kernel argument of the launches that
+// have some: per field, dimension and side the function, its evaluation location (Vertex 1,
+// Center 0, the same for every dimension) and whether the coordinate along the condition's
+// dimension is an argument; and the grid's coordinates.
+template <class T, bool FN>
+struct BcFns {};
 template <class T>
-__device__ __forceinline__ T bc_value(const BcField<T>& F, int nd, const int* n, int d, int s, const int* q) {
+struct BcFns<T, true> {
+    cgk::FnDev<T> fn[kBcMaxFields][3][2];
+    unsigned char vtx[kBcMaxFields][3][2];
+    unsigned char full[kBcMaxFields][3][2];
+    T org[3], dx[3];
+};
+
+// The value of phase (d, s) of field fi at the point q: its BoundaryFunction at q's coordinates,
+// else the per-point array at q's tangential indices (remove_dim(dim, I)), else the constant.
+template <class T, bool FN>
+__device__ __forceinline__ T bc_value(const BcField<T>& F, const BcFns<T, FN>& fns, int fi, int nd, const int* n, int d,
+                                      int s, const int* q) {
+    if constexpr (FN) {
+        const cgk::FnDev<T>& fn = fns.fn[fi][d][s];
+        if (fn.kind != CG_FN_NONE) {
+            T x[3] = {T(0), T(0), T(0)};
+            int m = 0;
+            for (int t = 0; t < nd; ++t) {
+                if (t == d && !fns.full[fi][d][s]) continue;
+                x[m++] = cgk::grid_coord(fns.org[t], fns.dx[t], q[t], fns.vtx[fi][d][s] != 0);
+            }
+            return cgk::fn_eval(fn, m, x);
+        }
+    }
     const T* a = F.va[d][s];
     if (!a) return F.val[d][s];
     long idx = 0, mul = 1;
@@ -464,8 +491,8 @@ __device__ inline bool phase_member(const BcField<T>& F, int nd, const int* n, i
     return false;
 }
 
-template <class T>
-__global__ void bc_apply_kernel(const BcBatch<T> b) {
+template <class T, bool FN>
+__global__ void bc_apply_kernel(const BcBatch<T> b, const BcFns<T, FN> fns) {
     cg_dep_wait();
     cg_dep_release();
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -500,12 +527,12 @@ __global__ void bc_apply_kernel(const BcBatch<T> b) {
     for (;;) {
         const int d = nd - 1 - (k >> 1), s = k & 1;
         if (rule == R_CONST) {
-            base = bc_value(F, nd, b.n, d, s, q);
+            base = bc_value(F, fns, item.field, nd, b.n, d, s, q);
             break;
         }
         stack_k[depth] = k;
         stack_r[depth] = rule;
-        stack_v[depth] = bc_value(F, nd, b.n, d, s, q);
+        stack_v[depth] = bc_value(F, fns, item.field, nd, b.n, d, s, q);
         ++depth;
         q[d] = src;
         int kn = -1;
@@ -534,7 +561,8 @@ __global__ void bc_apply_kernel(const BcBatch<T> b) {
 }
 
 template <class T>
-int bc_apply_t(cg_ctx* ctx, const cg_grid* grid, int nfields, const cg_field* fields, const cg_bc* bcs, bool dep) {
+int bc_apply_t(cg_ctx* ctx, const cg_grid* grid, int nfields, const cg_field* fields, const cg_bc* bcs, bool dep,
+               const cg_bc_fn* fns = nullptr) {
     BcBatch<T> b;
     std::memset(&b, 0, sizeof(b));
     b.nd = grid->ndim;
@@ -578,7 +606,58 @@ int bc_apply_t(cg_ctx* ctx, const cg_grid* grid, int nfields, const cg_field* fi
     b.total = total;
     if (total == 0) return CG_OK;
     const int threads = 256;
-    CG_CUDA(ctx, cg_launch(bc_apply_kernel<T>, dim3(cg_div_up(total, threads)), dim3(threads), 0, ctx->stream, dep, b));
+    bool any_fn = false;
+    if (fns)
+        for (int fi = 0; fi < nfields; ++fi)
+            for (int d = 0; d < b.nd; ++d)
+                for (int s = 0; s < 2; ++s) any_fn = any_fn || fns[fi].fn[d][s].kind != CG_FN_NONE;
+    if (!any_fn) {
+        CG_CUDA(ctx, cg_launch(bc_apply_kernel<T, false>, dim3(cg_div_up(total, threads)), dim3(threads), 0, ctx->stream,
+                               dep, b, BcFns<T, false>{}));
+        return CG_OK;
+    }
+    BcFns<T, true> bf;
+    std::memset(&bf, 0, sizeof(bf));
+    for (int d = 0; d < 3; ++d) {
+        bf.org[d] = (T)grid->origin[d];
+        bf.dx[d] = (T)grid->spacing[d];
+    }
+    for (int fi = 0; fi < nfields; ++fi)
+        for (int d = 0; d < b.nd; ++d)
+            for (int s = 0; s < 2; ++s) {
+                const cg_function& fn = fns[fi].fn[d][s];
+                if (fn.kind == CG_FN_NONE) continue;
+                const int kind = b.f[fi].kind[d][s];
+                bf.fn[fi][d][s].kind = fn.kind;
+                for (int q = 0; q < 8; ++q) bf.fn[fi][d][s].p[q] = (T)fn.p[q];
+                // Dirichlet: the field's location along d; Neumann: its flip
+                const bool vtx = b.f[fi].loc[d] == CG_VERTEX;
+                bf.vtx[fi][d][s] = (unsigned char)(kind == CG_BC_NEUMANN ? !vtx : vtx);
+                bf.full[fi][d][s] = (unsigned char)(fns[fi].full_dims[d][s] != 0);
+            }
+    CG_CUDA(ctx, cg_launch(bc_apply_kernel<T, true>, dim3(cg_div_up(total, threads)), dim3(threads), 0, ctx->stream, dep,
+                           b, bf));
+    return CG_OK;
+}
+
+// The function sides of a batch: known forms, on Dirichlet or Neumann sides only.
+int check_bc_fns(cg_ctx* ctx, const cg_grid* grid, int nfields, const cg_bc* bcs, const cg_bc_fn* fns) {
+    for (int fi = 0; fi < nfields; ++fi)
+        for (int d = 0; d < 3; ++d)
+            for (int s = 0; s < 2; ++s) {
+                const int k = fns[fi].fn[d][s].kind;
+                if (k == CG_FN_NONE) continue;
+                if (k < CG_FN_CONST || k > CG_FN_AFFINE)
+                    return cg_fail(ctx, CG_ERR_ARG, "cg_bc_apply_fn: field %d dim %d side %d: unknown function kind %d", fi,
+                                   d, s, k);
+                if (d >= grid->ndim)
+                    return cg_fail(ctx, CG_ERR_ARG, "cg_bc_apply_fn: a function on dim %d of a %dD grid", d, grid->ndim);
+                const int kind = bcs[fi].kind[d][s];
+                if (kind != CG_BC_DIRICHLET && kind != CG_BC_NEUMANN)
+                    return cg_fail(ctx, CG_ERR_ARG,
+                                   "cg_bc_apply_fn: field %d dim %d side %d: a function needs a Dirichlet or Neumann side",
+                                   fi, d, s);
+            }
     return CG_OK;
 }
 
@@ -607,6 +686,28 @@ extern "C" int cg_bc_apply(cg_ctx* ctx, const cg_grid* grid, int nfields, const 
     if (!ctx) return cg_fail(nullptr, CG_ERR_ARG, "cg_bc_apply: ctx is NULL");
     cudaSetDevice(ctx->device);
     return cg_bc_apply_impl(ctx, grid, nfields, fields, bcs);
+}
+
+extern "C" int cg_bc_apply_fn(cg_ctx* ctx, const cg_grid* grid, int nfields, const cg_field* fields, const cg_bc* bcs,
+                              const cg_bc_fn* fns) {
+    if (!ctx) return cg_fail(nullptr, CG_ERR_ARG, "cg_bc_apply_fn: ctx is NULL");
+    if (!fns) return cg_bc_apply(ctx, grid, nfields, fields, bcs);
+    int rc = cg_check_grid(ctx, grid);
+    if (rc) return rc;
+    if (nfields < 0 || nfields > kBcMaxFields)
+        return cg_fail(ctx, CG_ERR_ARG, "cg_bc_apply_fn: nfields %d not in 0..%d", nfields, kBcMaxFields);
+    if (nfields == 0) return CG_OK;
+    if (!fields || !bcs) return cg_fail(ctx, CG_ERR_ARG, "cg_bc_apply_fn: NULL fields or bcs");
+    if ((rc = check_bc_fns(ctx, grid, nfields, bcs, fns))) return rc;
+    if (grid->ndim >= 2)
+        for (int d = 0; d < grid->ndim; ++d)
+            if (grid->n[d] < 2) return cg_fail(ctx, CG_ERR_ARG, "cg_bc_apply_fn: grid too small");
+    const int dtype = fields[0].dtype;
+    for (int i = 0; i < nfields; ++i)
+        if ((rc = cg_check_field(ctx, grid, fields[i], dtype, -1, "cg_bc_apply_fn field"))) return rc;
+    cudaSetDevice(ctx->device);
+    return dtype == CG_F64 ? bc_apply_t<double>(ctx, grid, nfields, fields, bcs, false, fns)
+                           : bc_apply_t<float>(ctx, grid, nfields, fields, bcs, false, fns);
 }
 
 // ---- max-norm over interiors: one launch for up to kRedSlots fields --------------------------

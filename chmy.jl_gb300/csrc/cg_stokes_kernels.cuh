@@ -24,13 +24,6 @@ struct SV {  // device views of the Stokes field set
     }
 };
 
-// A device FunctionField (cg_function) in the field precision.
-template <class T>
-struct FnDev {
-    int kind;
-    T p[8];
-};
-
 template <class T>
 struct SP {  // scalars in the field precision
     T eta, eta_ve, G, dt, dtau_Pr, dtau_r, nu_dtau, lam;
@@ -46,32 +39,6 @@ struct BodyFn {
     FnDev<T> fn[3];
     T org[3], dx[3];
 };
-
-// coord(grid, loc, I) (src/Grids/uniform_axis.jl): Vertex muladd(I-1, Δ, o), Center
-// muladd(I-1, Δ, muladd(0.5, Δ, o)); muladd is a fused multiply-add, as on the CPU.
-template <class T>
-__device__ __forceinline__ T grid_coord(T org, T dx, int I, bool vertex) {
-    const T o = vertex ? org : rfma(T(0.5), dx, org);
-    return rfma(T(I - 1), dx, o);
-}
-
-// func(x...) of a device FunctionField at the point x (cg_function's forms; every operation
-// rounded once, left to right, as the CPU evaluates the Julia expression).
-template <class T>
-__device__ __forceinline__ T fn_eval(const FnDev<T>& f, int nd, const T* x) {
-    if (f.kind == CG_FN_CONST) return f.p[0];
-    if (f.kind == CG_FN_BALL) {
-        T r2 = rmul(rsub(x[0], f.p[0]), rsub(x[0], f.p[0]));
-        for (int d = 1; d < nd; ++d) r2 = radd(r2, rmul(rsub(x[d], f.p[d]), rsub(x[d], f.p[d])));
-        return r2 < rmul(f.p[3], f.p[3]) ? f.p[4] : f.p[5];
-    }
-    if (f.kind == CG_FN_AFFINE) {
-        T v = f.p[0];
-        for (int d = 0; d < nd; ++d) v = radd(v, rmul(f.p[1 + d], x[d]));
-        return v;
-    }
-    return T(0);
-}
 
 // Body-force function of velocity component `comp` at its point (i, j, k): Vertex along comp,
 // Center along the other dimensions.

@@ -314,6 +314,23 @@ typedef struct cg_stokes_params {
  * point (logical 1-2H .. n+2H), evaluated on the device. */
 CG_API int cg_function_fill(cg_ctx* ctx, const cg_grid* grid, const cg_function* fn, const cg_field* f);
 
+/* BoundaryFunction values evaluated on the device (src/BoundaryConditions/boundary_function.jl:
+ * 11-44, the continuous form), per field, dimension and side. A side whose fn kind is not
+ * CG_FN_NONE takes its value at each point the condition writes from the function instead of
+ * cg_bc.value / cg_bc.values: func(x...) at coord(grid, L, I...) with I the written point (the
+ * boundary node for Dirichlet on a Vertex dimension, else the ghost) and L the field's location
+ * along the dimension for Dirichlet and its flip for Neumann, used for every dimension
+ * (first_order_boundary_condition.jl:46-84); with full_dims 0 (Chmy's reduce_dims=true) the
+ * coordinate along the condition's dimension is left out of x. Coordinates and the function are
+ * evaluated in the field's precision with fused multiply-adds, as for cg_function. */
+typedef struct cg_bc_fn {
+    cg_function fn[3][2];
+    int32_t full_dims[3][2];
+} cg_bc_fn;
+/* cg_bc_apply with BoundaryFunction sides: fns[i] belongs to fields[i] (fns may be NULL). */
+CG_API int cg_bc_apply_fn(cg_ctx* ctx, const cg_grid* grid, int nfields, const cg_field* fields,
+                          const cg_bc* bcs, const cg_bc_fn* fns);
+
 /* update_old!: T_old = T; tau_old = tau at I in [0, n+1]^N. */
 CG_API int cg_stokes_update_old(cg_ctx* ctx, const cg_grid* grid, const cg_stokes_fields* f);
 /* update_stress!: strain rates, divV, P and tau PT update at I in [0, n+1]^N. */

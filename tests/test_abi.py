@@ -48,9 +48,10 @@ def test_struct_layouts_match_header():
     #include <stddef.h>
     #include "chmy_gb300.h"
     int main(void) {
-      printf("%zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(cg_field), sizeof(cg_grid), sizeof(cg_bc),
+      printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(cg_field), sizeof(cg_grid), sizeof(cg_bc),
              sizeof(cg_stokes_fields), sizeof(cg_stokes_params), sizeof(cg_solve_opts), sizeof(cg_solve_result),
-             offsetof(cg_field, stride));
+             offsetof(cg_field, stride), sizeof(cg_function), sizeof(cg_mask), sizeof(cg_bc_fn),
+             offsetof(cg_bc_fn, full_dims));
       return 0;
     }
     """
@@ -70,6 +71,10 @@ def test_struct_layouts_match_header():
         ctypes.sizeof(_abi.cg_solve_opts),
         ctypes.sizeof(_abi.cg_solve_result),
         _abi.cg_field.stride.offset,
+        ctypes.sizeof(_abi.cg_function),
+        ctypes.sizeof(_abi.cg_mask),
+        ctypes.sizeof(_abi.cg_bc_fn),
+        _abi.cg_bc_fn.full_dims.offset,
     ]
     assert [int(x) for x in out] == want
 
