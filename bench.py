@@ -728,7 +728,7 @@ def config_suite(arch, stream, peak, fp64=True):
     cfg2 = {}
     for T, name in ((np.float64, "fp64"), (np.float32, "fp32")):
         # FP32: one row pitch and plane height for every array (the fused single-pass kernel)
-        lay = dict(pitch_align=128, plane_rows=n2 + 5, align_index=-1) if T == np.float32 else {}
+        lay = dict(pitch_align=128, plane_rows=n2 + 5, align_index=0) if T == np.float32 else {}
         fs = {k: Field(arch, g2, Cl, T, **lay) for k in ("C", "C_old", "D")}
         q = [Field(arch, g2, tuple(Vl if e == d else Cl for e in range(3)), T, **lay) for d in range(3)]
         fs["C"].from_numpy(Cb.astype(T))
@@ -1181,7 +1181,7 @@ def run_kernel_ptdiff(arch, args):
     g = UniformGrid(origin=(-0.5,) * 3, extent=(1.0,) * 3, dims=(n,) * 3, dtype=T)
     Cl, Vl = Center(), Vertex()
     rng = np.random.default_rng(2)
-    lay = dict(pitch_align=128, plane_rows=n + 5, align_index=-1)
+    lay = dict(pitch_align=128, plane_rows=n + 5, align_index=0)
     fs = {k: Field(arch, g, Cl, T, **lay) for k in ("C", "C_old", "D")}
     q = [Field(arch, g, tuple(Vl if e == d else Cl for e in range(3)), T, **lay) for d in range(3)]
     fs["C"].from_numpy(rng.random(fs["C"].data.shape, dtype=T))

@@ -36,8 +36,9 @@ struct cg_ctx {
     // numbered scratch buffers of the time-stepping loops (grown on demand, freed by cg_destroy)
     // slots: 0 thermal partner, 1 SIA D, 2 PT-diffusion partners, 3 SIA ensemble,
     // 4 PT-diffusion defect-correction pool, 5 SIA reverse step, 6 SIA reverse sweep over a tape,
-    // 7 SIA ensemble reverse sweep, 8 explicit-diffusion reverse sweep, 9 thermal-step adjoint
-    static constexpr int kScratchSlots = 10;
+    // 7 SIA ensemble reverse sweep, 8 explicit-diffusion reverse sweep, 9 thermal-step adjoint,
+    // 10 the wait flag of the TMA-fed PT-diffusion iteration
+    static constexpr int kScratchSlots = 11;
     void* scratch[kScratchSlots] = {};
     size_t scratch_bytes[kScratchSlots] = {};
 };

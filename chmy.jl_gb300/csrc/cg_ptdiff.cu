@@ -377,13 +377,72 @@ cudaError_t launch_pd_ix(const PDM<T>& f, const cg_grid* g, int num_sms, cudaStr
     return cudaGetLastError();
 }
 
-// Block shapes of the fused kernel (all without register spills for FP32): 8 rows at 4 or 5
-// blocks per SM, 16 rows at 2, 4 rows at 10. Taller blocks read fewer y-halo rows; more
-// resident warps keep more loads in flight.
-constexpr int kPdVariants = 4;
+}  // namespace
+
+#include "cg_ptd_tma.cuh"
+
+namespace {
+
+// The tensor maps of one ping-pong direction of a fused run (TMA variants), or none.
+struct PdDir {
+    const ptdt::Maps* m8 = nullptr;   // boxes of 8 + 2 rows
+    const ptdt::Maps* m16 = nullptr;  // boxes of 16 + 2 rows
+    ptdt::XO xo{};
+    int* err = nullptr;
+};
+
+inline PdDir pd_dir(const PdTma& t, bool ab) {
+    PdDir d;
+    if (!t.ok) return d;
+    d.m8 = ab ? &t.ab8 : &t.ba8;
+    d.m16 = ab ? &t.ab16 : &t.ba16;
+    d.xo = ab ? t.xab : t.xba;
+    d.err = t.err;
+    return d;
+}
+
+// Longest time a TMA variant's block waits on one barrier before it reports CG_ERR_TIMEOUT.
+constexpr unsigned long long kPdWaitLimitNs = 2000000000ull;
+
+template <int NW, int MINB>
+cudaError_t launch_pd_tma(const PDM<float>& f, const cg_grid* g, int num_sms, cudaStream_t st, const ptdt::Maps& maps,
+                          const ptdt::XO& xo, int* err) {
+    using Gm = ptdt::Geom<NW>;
+    const int e0 = g->n[0] + 1, e1 = g->n[1] + 1, e2 = g->n[2] + 1;
+    const int ntx = cg_div_up(e0 + 1, 32), nty = cg_div_up(e1 + 1, NW);
+    static const int bps = [] {
+        int nb = 0;
+        if (cudaFuncSetAttribute(ptd_tma_kernel<NW, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, Gm::smem_bytes) !=
+                cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, ptd_tma_kernel<NW, MINB>, 32 * NW, Gm::smem_bytes) !=
+                cudaSuccess)
+            nb = 0;
+        cudaGetLastError();
+        return nb > 0 ? nb : 1;
+    }();
+    const long tiles = (long)ntx * nty;
+    const int seg = pd_seg_len(tiles, e2 + 1, (long)num_sms * bps);
+    const int nseg = cg_div_up(e2 + 1, seg);
+    ptd_tma_kernel<NW, MINB><<<(unsigned)(tiles * nseg), 32 * NW, Gm::smem_bytes, st>>>(maps, f, xo, e0, e1, e2, ntx, nty,
+                                                                                      seg, kPdWaitLimitNs, err);
+    return cudaGetLastError();
+}
+
+// Launch layouts of the fused iteration. Variants 0-3, ptd_march3d_kernel (all without register
+// spills for FP32): 8 rows at 4 or 5 blocks per SM, 16 rows at 2, 4 rows at 10; taller blocks
+// read fewer y-halo rows, more resident warps keep more loads in flight. Variants 4-5,
+// ptd_tma_kernel with 8 and 16 rows (inputs staged by TMA; only with tensor maps for the
+// direction).
+constexpr int kPdVariants = 6;
+constexpr int kPdTmaFirst = 4;
 
 template <class T>
-cudaError_t launch_pd_march3d(const PDM<T>& f, const cg_grid* g, int num_sms, cudaStream_t st, int variant) {
+cudaError_t launch_pd_march3d(const PDM<T>& f, const cg_grid* g, int num_sms, cudaStream_t st, int variant,
+                              const PdDir& dir = PdDir{}) {
+    if constexpr (sizeof(T) == 4) {
+        if (variant == 4 && dir.m8) return launch_pd_tma<8, 4>(f, g, num_sms, st, *dir.m8, dir.xo, dir.err);
+        if (variant == 5 && dir.m16) return launch_pd_tma<16, 2>(f, g, num_sms, st, *dir.m16, dir.xo, dir.err);
+    }
     switch (variant) {
         case 1: return launch_pd_ix<T, 8, 5>(f, g, num_sms, st);
         case 2: return launch_pd_ix<T, 16, 2>(f, g, num_sms, st);
@@ -392,21 +451,37 @@ cudaError_t launch_pd_march3d(const PDM<T>& f, const cg_grid* g, int num_sms, cu
     }
 }
 
-// The fastest block shape for this grid and layout, timed on the run's own buffers before its
-// graph is captured (the launch writes only the partner buffers) and cached for the process.
+// CG_PTD_VARIANT=<0..5> in the environment (read on every call): the fused iteration's layout
+// instead of the autotuner's (a TMA variant only where its tensor maps exist).
+inline int pd_variant_forced() {
+    const char* e = std::getenv("CG_PTD_VARIANT");
+    if (!e || !e[0]) return -1;
+    const int v = std::atoi(e);
+    return v >= 0 && v < kPdVariants ? v : -1;
+}
+
+// The fastest layout for this grid and layout, timed on the run's own buffers before its graph
+// is captured (the launch writes only the partner buffers) and cached for the process.
 template <class T>
-int tune_pd(const PDM<T>& f, const cg_grid* g, int num_sms, cudaStream_t st) {
+int tune_pd(const PDM<T>& f, const cg_grid* g, int num_sms, cudaStream_t st, const PdDir& dir = PdDir{}) {
+    const bool tma = dir.m8 != nullptr;
+    const int forced = pd_variant_forced();
+    if (forced >= 0) return (forced >= kPdTmaFirst && !tma) ? 0 : forced;
     if (!cg_autotune_enabled()) return 0;
     std::string key = "ptdiff3d";
     for (int d = 0; d < 3; ++d) cg_key_add(key, g->n[d]);
     cg_key_add(key, f.s1);
     cg_key_add(key, f.s2);
     cg_key_add(key, num_sms);
+    cg_key_add(key, (int)tma);
     cg_tune_cfg best{0, 0};
     if (cg_tune_lookup(key, &best)) return best.variant;
     float tbest = 1e30f;
-    for (int v = 0; v < kPdVariants; ++v) {
-        const float t = cgk::time_launches([&] { return launch_pd_march3d<T>(f, g, num_sms, st, v); }, st);
+    for (int v = 0; v < (tma ? kPdVariants : kPdTmaFirst); ++v) {
+        const float t = cgk::time_launches([&] { return launch_pd_march3d<T>(f, g, num_sms, st, v, dir); }, st);
+        if (cg_tune_verbose())
+            std::fprintf(stderr, "ptdiff3d tune %dx%dx%d: variant %d: %.1f us\n", g->n[0], g->n[1], g->n[2], v,
+                         t >= 0.f ? 1e3f * t / 3 : -1.f);
         if (t >= 0.f && t < tbest) {
             tbest = t;
             best = cg_tune_cfg{0, v};
@@ -415,6 +490,26 @@ int tune_pd(const PDM<T>& f, const cg_grid* g, int num_sms, cudaStream_t st) {
     cudaGetLastError();
     cg_tune_store(key, best);
     return best.variant;
+}
+
+// The TMA variants' wait flag (scratch slot 10), cleared on the stream.
+int* pd_err_flag(cg_ctx* ctx, int* rc) {
+    int* e = static_cast<int*>(cg_scratch(ctx, 10, 256, rc));
+    if (*rc) return nullptr;
+    if (cudaMemsetAsync(e, 0, sizeof(int), ctx->stream) != cudaSuccess) {
+        *rc = cg_fail(ctx, CG_ERR_CUDA, "ptdiff: clearing the wait flag failed");
+        return nullptr;
+    }
+    return e;
+}
+
+// After a run that used a TMA variant: CG_ERR_TIMEOUT when a block's wait ran out (synchronises).
+int pd_check_flag(cg_ctx* ctx, int* e) {
+    int h = 0;
+    CG_CUDA(ctx, cudaMemcpyAsync(&h, e, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (h) return cg_fail(ctx, CG_ERR_TIMEOUT, "ptdiff fused iteration: a staged-plane wait timed out");
+    return CG_OK;
 }
 
 template <class T>
@@ -462,16 +557,28 @@ int run_fused3d(cg_ctx* ctx, const cg_grid* g, const cg_ptdiff_fields* f, const 
     }
     const PDM<T> ab = make_pdm<T>(g, f->C, f->q, part[0], part + 1, f, p);
     const PDM<T> ba = make_pdm<T>(g, part[0], part + 1, f->C, f->q, f, p);
-    const int variant = tune_pd<T>(ab, g, ctx->num_sms, ctx->stream);
+    int* err = pd_err_flag(ctx, &rc);
+    if (rc) return rc;
+    const PdTma tma = make_pd_tma(f->C, f->q, part[0], part + 1, f->D, f->C_old, err);
+    const PdDir dab = pd_dir(tma, true), dba = pd_dir(tma, false);
+    const int variant = tune_pd<T>(ab, g, ctx->num_sms, ctx->stream, dab);
     cg_key_add(key, base);
     cg_key_add(key, variant);
-    return cg_graph_run(ctx, key, [&](cudaStream_t st) {
+    if (variant >= kPdTmaFirst) {
+        // the maps encode this call's pointers: they are part of the graph's key
+        cg_key_add(key, tma.ab8);
+        cg_key_add(key, tma.ab16);
+        cg_key_add(key, tma.ba8);
+        cg_key_add(key, tma.ba16);
+    }
+    rc = cg_graph_run(ctx, key, [&](cudaStream_t st) {
         for (int a = 0; a < 4; ++a)
             CG_CUDA(ctx, cudaMemcpyAsync(part[a].data, src[a]->data, bytes[a], cudaMemcpyDeviceToDevice, st));
         for (int s = 0; s < nsteps; ++s) {
             CG_CUDA(ctx, cudaMemcpyAsync(f->C_old.data, f->C.data, bytes[0], cudaMemcpyDeviceToDevice, st));
             for (int it = 0; it < npt; ++it) {
-                const cudaError_t le = launch_pd_march3d<T>(it % 2 == 0 ? ab : ba, g, ctx->num_sms, st, variant);
+                const cudaError_t le =
+                    launch_pd_march3d<T>(it % 2 == 0 ? ab : ba, g, ctx->num_sms, st, variant, it % 2 == 0 ? dab : dba);
                 if (le != cudaSuccess) return cg_fail(ctx, CG_ERR_CUDA, "ptdiff fused launch: %s", cudaGetErrorString(le));
                 if (bc) {
                     int r = cg_bc_apply_impl(ctx, g, 1, it % 2 == 0 ? &part[0] : &f->C, bc);
@@ -484,6 +591,8 @@ int run_fused3d(cg_ctx* ctx, const cg_grid* g, const cg_ptdiff_fields* f, const 
         }
         return (int)CG_OK;
     });
+    if (rc) return rc;
+    return variant >= kPdTmaFirst ? pd_check_flag(ctx, err) : CG_OK;
 }
 
 // The fused path needs a 3D FP32 grid, no residual output, and one row and plane stride for
@@ -816,17 +925,18 @@ int solve_fp64(cg_ctx* ctx, const cg_grid* g, const cg_ptdiff_fields* f, const c
 
 int solve_dc(cg_ctx* ctx, const cg_grid* g, const cg_ptdiff_fields* f, const cg_ptdiff_params* p, const cg_bc* bc,
              const cg_solve_opts* o, cg_solve_result* res) {
-    // FP32 pool: d, d', q x3, q' x3, C_old' (dt R), D; the first padded element of every row
-    // (logical x index -1, the first the kernels read) on a 128-byte boundary, so that a row's
-    // n + 4 elements span the fewest 128-byte lines (DRAM moves whole lines)
-    const long front = 0, pitch = ((front + g->n[0] + 5 + 31) / 32) * 32, rows = g->n[1] + 5;
+    // FP32 pool: d, d', q x3, q' x3, C_old' (dt R), D; logical x index 0 of every row on a
+    // 128-byte boundary (31 elements of front), so that a warp's 32 columns store whole lines.
+    // Measured at 512^3 with a bc! launch per iteration: the TMA-fed iteration takes 1128 us
+    // per iteration in this layout and 1221 us with the first padded element aligned, where
+    // the register-fed kernel's best is 1195 us.
+    const long front = 31, pitch = ((front + g->n[0] + 5 + 31) / 32) * 32, rows = g->n[1] + 5;
     const size_t per = (size_t)pitch * rows * (g->n[2] + 5) * sizeof(float);
     const size_t per_al = (per + 255) & ~(size_t)255;
     int rc = CG_OK;
     char* base = static_cast<char*>(cg_scratch(ctx, 4, per_al * 10 + 256, &rc));
     if (rc) return rc;
-    // an array's data pointer sits `front` elements into its rows (0: its first element starts a
-    // 128-byte line)
+    // an array's data pointer sits `front` elements past the pool's 256-byte boundaries
     base += front * sizeof(float);
     const int qm[3] = {1, 2, 4};
     cg_field dA = pool_field(base, 0, g, 0, pitch, rows), dB = pool_field(base, per_al, g, 0, pitch, rows);
@@ -856,7 +966,11 @@ int solve_dc(cg_ctx* ctx, const cg_grid* g, const cg_ptdiff_fields* f, const cg_
     }
     const PDM<float> ab = make_pdm<float>(g, dA, qA, dB, qB, &w, p);
     const PDM<float> ba = make_pdm<float>(g, dB, qB, dA, qA, &w, p);
-    const int variant = tune_pd<float>(ab, g, ctx->num_sms, ctx->stream);
+    int* perr = pd_err_flag(ctx, &rc);
+    if (rc) return rc;
+    const PdTma tma = make_pd_tma(dA, qA, dB, qB, D32, co, perr);
+    const PdDir dab = pd_dir(tma, true), dba = pd_dir(tma, false);
+    const int variant = tune_pd<float>(ab, g, ctx->num_sms, ctx->stream, dab);
     const int nchunk = std::max(2, o->ncheck + (o->ncheck & 1));
     std::string key = "ptdiff_dc_chunk";
     cg_key_add(key, *g);
@@ -893,7 +1007,8 @@ int solve_dc(cg_ctx* ctx, const cg_grid* g, const cg_ptdiff_fields* f, const cg_
         while (total < o->max_iter) {
             rc = cg_graph_run(ctx, key, [&](cudaStream_t st) {
                 for (int it = 0; it < nchunk; ++it) {
-                    const cudaError_t le = launch_pd_march3d<float>(it % 2 == 0 ? ab : ba, g, ctx->num_sms, st, variant);
+                    const cudaError_t le = launch_pd_march3d<float>(it % 2 == 0 ? ab : ba, g, ctx->num_sms, st, variant,
+                                                                    it % 2 == 0 ? dab : dba);
                     if (le != cudaSuccess) return cg_fail(ctx, CG_ERR_CUDA, "ptdiff fused launch: %s", cudaGetErrorString(le));
                     int r = cg_bc_apply_impl(ctx, g, 1, it % 2 == 0 ? &dB : &dA, &bc0);
                     if (r) return r;
@@ -915,6 +1030,7 @@ int solve_dc(cg_ctx* ctx, const cg_grid* g, const cg_ptdiff_fields* f, const cg_
                 break;  // the FP32 floor: back to the FP64 defect
             }
         }
+        if (variant >= kPdTmaFirst && (rc = pd_check_flag(ctx, perr))) return rc;
         pd_update_kernel<<<ig, ib, 0, ctx->stream>>>(cg_view<double>(f->C), cg_view<float>(dA), g->n[0], g->n[1], g->n[2]);
         CG_CHECK_LAUNCH(ctx);
         if ((rc = cg_bc_apply_impl(ctx, g, 1, &f->C, bc))) return rc;

@@ -115,6 +115,38 @@ def test_fused_run_bitwise(arch, dims, npt):
         assert_close(a, b, 0.0, "q", exact=True)
 
 
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5])
+@pytest.mark.parametrize("dims", [(17, 12, 14), (64, 33, 20), (2, 2, 3), (70, 19, 41)])
+def test_fused_run_every_layout_bitwise(arch, monkeypatch, variant, dims):
+    """Every launch layout of the fused iteration, forced with CG_PTD_VARIANT — the register-fed
+    ptd_march3d_kernel at four block shapes (0-3) and the TMA-fed ptd_tma_kernel with 8 and 16
+    rows (4, 5), whose inputs stream through a ring of shared-memory planes — gives the oracle's
+    update_q!/update_C!/bc! states bit for bit. The caller's fields (first padded element 12
+    bytes past a 16-byte boundary) and the library's partner buffers (aligned) take different
+    tensor-map offsets."""
+    monkeypatch.setenv("CG_PTD_VARIANT", str(variant))
+    T = np.float32
+    grid, h, d = fields(arch, dims, T, 8, pitch_align=128)
+    p = ptdiff_params(grid, dt=1e-3, Dmax=float(h["D"].a.max()))
+    bc = to_cg_bc(3, {"x": Dirichlet(0.25), "y": Neumann(0.5), "z": (Neumann(), Dirichlet(-0.5))})
+    g = grid.desc()
+    hd = desc(h)
+    npt = 9
+    h["C_old"].a[...] = h["C"].a
+    for _ in range(npt):
+        lib().or_ptdiff_update_q(ctypes.byref(g), ctypes.byref(hd), ctypes.byref(p))
+        lib().or_ptdiff_update_C(ctypes.byref(g), ctypes.byref(hd), ctypes.byref(p))
+        bc_apply(grid, [h["C"]], [bc])
+    dd = desc(d)
+    dd.R = _abi.cg_field()
+    arch.call("cg_ptdiff_run", ctypes.byref(g), ctypes.byref(dd), ctypes.byref(p), ctypes.byref(bc), 1, npt)
+    arch.synchronize()
+    for k in ("C", "C_old"):
+        assert_close(d[k], h[k], 0.0, f"{k} variant {variant}", exact=True)
+    for a, b in zip(d["q"], h["q"]):
+        assert_close(a, b, 0.0, f"q variant {variant}", exact=True)
+
+
 def _np_residual(C, Co, D, idx, dt):
     """max |R| dt over the interior of the implicit step R = -(C - C_old)/dt - divg(q(C)),
     q(C) = -lerp(D) ∂C, on padded [z, y, x] arrays with halo 1 (logical I at padded I + 1)."""
