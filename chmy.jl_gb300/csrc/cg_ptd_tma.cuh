@@ -4,19 +4,19 @@
 // ptd_march3d_kernel waits on its own loads: each warp has one plane of loads in flight, and
 // most of its issue cycles stall on them. Here one thread of the block streams whole z-planes
 // of the block's tile — the six input arrays (C, D, q_x, q_y, q_z, C_old) over the tile's rows
-// with one halo row on each side and 40 columns — into a ring of kStages planes in shared
-// memory with cp.async.bulk.tensor, kStages - 2 planes ahead of the two the warps read. Each
+// with one halo row where it is read — into a ring of S planes in shared memory with
+// cp.async.bulk.tensor, S - 2 planes ahead of the two the warps read. Each
 // ring slot has a `full` mbarrier (the copies' bytes arrive) and an `empty` mbarrier (every warp
 // has read the plane). The warps compute exactly what ptd_march3d_kernel computes, from shared
 // memory instead of global loads, so the results are bitwise the same. Every wait is bounded by
 // %globaltimer: a wait that runs out sets the error flag and the block stops; the producing
 // thread then waits, again bounded, for its copies still in flight before the block exits.
 //
-// Layout requirements (checked on the host): FP32, every array's rows 16-byte aligned with
+// Layout requirements (checked on the host): FP32, 4-byte aligned arrays with row and plane
 // strides that are multiples of 16 bytes, and a shared row and plane stride (the fused kernel's
 // condition). The tensor map of an array starts at its first padded element rounded down to
 // 16 bytes (xo elements before it) and covers exactly its padded extent, so no copy reads past
-// the allocation; columns beyond it read as zero and are never used.
+// the allocation; box elements beyond it read as zero and are never used.
 #pragma once
 
 #include <cuda.h>  // CUtensorMap and its enums (the encoder is reached through the runtime)
@@ -24,28 +24,39 @@
 namespace ptdt {
 
 constexpr int kCols = 40;    // box width: 32 tile columns, the x halos and the 16-byte alignment slack
-constexpr int kStages = 4;   // ring slots: the two planes in use and two in flight
 constexpr int kArrays = 6;   // box order
 enum { A_C = 0, A_D = 1, A_QX = 2, A_QY = 3, A_QZ = 4, A_CO = 5 };
 
 struct Maps {
     CUtensorMap m[kArrays];
 };
-// Elements between each array's map origin (16-byte aligned) and its first padded element.
-struct XO {
-    int v[kArrays];
+// The box of each array in one launch. An array's box covers just the columns and rows the
+// iteration reads from it: C and D the tile's 32 columns with one halo column on each side and
+// one halo row on each side; q_x the columns and the upper x halo, q_y the rows and the upper y
+// halo row; q_z and C_old the tile alone. Along x the box starts on a 16-byte boundary at or
+// before the first column it needs and has a width that is a multiple of 4 elements.
+struct Boxes {
+    int x0[kArrays];   // box start along x in tensor coordinates, relative to the tile's i0
+    int y0[kArrays];   // box start along y relative to j0 (tensor y = logical y + 1): 0 or 1
+    int w[kArrays];    // box width (floats)
+    int cb[kArrays];   // box column of the lane's column = lane + cb
+    int off[kArrays];  // the box's float offset in a ring slot (128-byte aligned)
+    int sf;            // floats per ring slot
+    unsigned tx;       // bytes one slot's copies deliver
 };
 
-template <int NW>
-struct Geom {
-    static constexpr int rows = NW + 2;
-    static constexpr int box_floats = kCols * rows;
-    static constexpr int box_bytes = (box_floats * 4 + 127) / 128 * 128;  // each box 128-byte aligned
-    static constexpr int stage_bytes = kArrays * box_bytes;
-    static constexpr unsigned tx_bytes = kArrays * box_floats * 4;
-    // the ring, the 2 x kStages barriers and 128 bytes to align the ring's start
-    static constexpr int smem_bytes = kStages * stage_bytes + 2 * kStages * 8 + 128;
-};
+// Shared memory a block's ring needs: S slots of sf floats, the 2 x S barriers and 128 bytes to
+// align the ring's start.
+inline int smem_bytes(int S, int sf) { return S * sf * 4 + 2 * S * 8 + 128; }
+// The same for boxes all kCols wide and NW + 2 rows high, the largest a launch can need.
+template <int NW, int S>
+constexpr int max_smem_bytes() {
+    return S * kArrays * ((kCols * (NW + 2) * 4 + 127) / 128 * 128) + 2 * S * 8 + 128;
+}
+// Rows of array a's box for blocks of NW rows.
+__host__ __device__ constexpr int box_rows(int a, int nw) {
+    return (a == A_C || a == A_D) ? nw + 2 : (a == A_QY ? nw + 1 : nw);
+}
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -97,19 +108,19 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, i
 // segment; plane m of the ring is logical plane ks - 1 + m (tensor z = ks + m), box rows are the
 // logical rows j0 - 1 .. j0 + NW (tensor y = j0 ...), box column c is tensor x = i0 + c, i.e.
 // logical i0 - 1 - xo + c for an array whose map starts xo elements before its first element.
-template <int NW, int MINB>
+template <int NW, int MINB, int S>
 __global__ void __launch_bounds__(32 * NW, MINB)
-    ptd_tma_kernel(const __grid_constant__ ptdt::Maps maps, const PDM<float> f, const ptdt::XO xo, int e0, int e1, int e2,
+    ptd_tma_kernel(const __grid_constant__ ptdt::Maps maps, const PDM<float> f, const ptdt::Boxes bx, int e0, int e1, int e2,
                    int ntx, int nty, int seg_len, unsigned long long limit_ns, int* err) {
     using namespace cgk;
     using namespace ptdt;
-    using G = Geom<NW>;
     constexpr unsigned FULL = 0xffffffffu;
     extern __shared__ __align__(128) unsigned char smdyn[];
     // the ring starts on a 128-byte boundary of the shared window (the copies' destinations)
     unsigned char* smraw = smdyn + ((128u - (smem_u32(smdyn) & 127u)) & 127u);
-    uint64_t* full = reinterpret_cast<uint64_t*>(smraw + kStages * G::stage_bytes);
-    uint64_t* empty = full + kStages;
+    static_assert(S >= 3 && (S & (S - 1)) == 0, "the ring holds two planes in use and one in flight; its index is a mask");
+    uint64_t* full = reinterpret_cast<uint64_t*>(smraw + (size_t)S * bx.sf * 4);
+    uint64_t* empty = full + S;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int b = blockIdx.x;
     const int tx = b % ntx, ty = (b / ntx) % nty, seg = b / (ntx * nty);
@@ -128,39 +139,36 @@ __global__ void __launch_bounds__(32 * NW, MINB)
     fl.h31q = lane == 31 && row && i + 1 <= e0 + 1;
     const int nplanes = ke - ks + 3;  // planes ks-1 .. ke+1
     if (threadIdx.x == 0) {
-        for (int s = 0; s < kStages; ++s) {
+        for (int s = 0; s < S; ++s) {
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], NW);
         }
         mbar_fence_init();
     }
     __syncthreads();
-    static_assert((kStages & (kStages - 1)) == 0, "the ring's slot index is a mask");
-    auto slot = [&](int m) { return smraw + (m & (kStages - 1)) * G::stage_bytes; };
+    float* ring = reinterpret_cast<float*>(smraw);
     auto issue = [&](int m) {
-        unsigned char* dst = slot(m);
-        uint64_t* bar = &full[m & (kStages - 1)];
-        mbar_expect_tx(bar, G::tx_bytes);
-        for (int a = 0; a < kArrays; ++a) tma_load_3d(dst + a * G::box_bytes, &maps.m[a], i0, j0, ks + m, bar);
+        float* dst = ring + (m & (S - 1)) * bx.sf;
+        uint64_t* bar = &full[m & (S - 1)];
+        mbar_expect_tx(bar, bx.tx);
+        for (int a = 0; a < kArrays; ++a)
+            tma_load_3d(dst + bx.off[a], &maps.m[a], i0 + bx.x0[a], j0 + bx.y0[a], ks + m, bar);
     };
     int issued = -1, waited = -1;  // producer's bookkeeping (thread 0)
     if (threadIdx.x == 0) {
-        const int first = nplanes < kStages ? nplanes : kStages;
+        const int first = nplanes < S ? nplanes : S;
         for (int m = 0; m < first; ++m) issue(m);
         issued = first - 1;
     }
-    // the lane's element of array a, row r0 = w + 1 of the box, as a float offset into a slot;
-    // a neighbour is a compile-time displacement (dr rows, dc columns) from it
-    const int r0 = w + 1;
-    constexpr int SF = G::stage_bytes / 4, BF = G::box_bytes / 4;
+    // the lane's element of array a in the warp's row, as a float offset into a slot (the row
+    // j = j0 + w is box row w + 1 - y0); a neighbour is dr rows and dc columns away
     int col[kArrays];
 #pragma unroll
-    for (int a = 0; a < kArrays; ++a) col[a] = a * BF + r0 * kCols + lane + 1 + xo.v[a];
-    const float* ring = reinterpret_cast<const float*>(smraw);
+    for (int a = 0; a < kArrays; ++a) col[a] = bx.off[a] + (w + 1 - bx.y0[a]) * bx.w[a] + lane + bx.cb[a];
     auto V = [&](int m, int a, int dr, int dc) -> float {
-        return ring[(m & (kStages - 1)) * SF + col[a] + dr * kCols + dc];
+        return ring[(m & (S - 1)) * bx.sf + col[a] + dr * bx.w[a] + dc];
     };
-    bool ok = mbar_wait(&full[0], 0, limit_ns) && mbar_wait(&full[1 & (kStages - 1)], (1 / kStages) & 1, limit_ns);
+    bool ok = mbar_wait(&full[0], 0, limit_ns) && mbar_wait(&full[1 & (S - 1)], (1 / S) & 1, limit_ns);
     // every decision to stop is taken by the whole warp (shuffles below need all 32 lanes)
     ok = __all_sync(FULL, ok);
     waited = ok ? 1 : -1;
@@ -174,16 +182,16 @@ __global__ void __launch_bounds__(32 * NW, MINB)
     for (int t = 0; ok && t <= ke - ks; ++t, o += f.s2) {
         const int k = ks + t;
         const int mc = t + 1, mn = t + 2;  // planes k and k+1
-        // refill the slot of plane t (every warp released it) with plane t + kStages
-        if (threadIdx.x == 0 && t + kStages < nplanes) {
-            if (mbar_wait(&empty[t & (kStages - 1)], (t / kStages) & 1, limit_ns)) {
-                issue(t + kStages);
-                issued = t + kStages;
+        // refill the slot of plane t (every warp released it) with plane t + S
+        if (threadIdx.x == 0 && t + S < nplanes) {
+            if (mbar_wait(&empty[t & (S - 1)], (t / S) & 1, limit_ns)) {
+                issue(t + S);
+                issued = t + S;
             } else {
                 ok = false;
             }
         }
-        if (ok && !mbar_wait(&full[mn & (kStages - 1)], (mn / kStages) & 1, limit_ns)) ok = false;
+        if (ok && !mbar_wait(&full[mn & (S - 1)], (mn / S) & 1, limit_ns)) ok = false;
         ok = __all_sync(FULL, ok);
         if (!ok) break;
         waited = mn;
@@ -217,14 +225,14 @@ __global__ void __launch_bounds__(32 * NW, MINB)
             }
         }
         __syncwarp();
-        if (lane == 0) mbar_arrive(&empty[mc & (kStages - 1)]);
+        if (lane == 0) mbar_arrive(&empty[mc & (S - 1)]);
     }
     if (!ok) {
         atomicExch(err, 1);
         // the producing thread's copies still in flight complete before the block's shared
         // memory goes away (bounded; they complete unless the copy itself failed)
         if (threadIdx.x == 0)
-            for (int m = waited + 1; m <= issued; ++m) mbar_wait(&full[m & (kStages - 1)], (m / kStages) & 1, limit_ns);
+            for (int m = waited + 1; m <= issued; ++m) mbar_wait(&full[m & (S - 1)], (m / S) & 1, limit_ns);
     }
 }
 
@@ -248,44 +256,77 @@ inline EncodeFn encoder() {
     return fn;
 }
 
-// The tensor map of one FP32 field for boxes of kCols x rows x 1; false when its layout does not
-// allow one (16-byte row alignment and strides).
-inline bool make_map(const cg_field& f, int rows, CUtensorMap* out, int* xo) {
-    const EncodeFn enc = encoder();
-    if (!enc || f.dtype != CG_F32 || f.ndim != 3 || !f.data) return false;
+// Elements between a field's first padded element and the 16-byte boundary at or before it;
+// -1 when the field cannot have a tensor map (FP32 3D, 4-byte aligned, 16-byte row strides).
+inline int map_offset(const cg_field& f) {
+    if (f.dtype != CG_F32 || f.ndim != 3 || !f.data) return -1;
     const uintptr_t a = reinterpret_cast<uintptr_t>(f.data);
-    if ((a & 3) != 0) return false;
-    *xo = (int)((a & 15) >> 2);
-    const cuuint64_t ext0 = (cuuint64_t)(f.n[0] + 4 * f.halo[0]) + (cuuint64_t)*xo;
+    if ((a & 3) != 0 || (f.stride[1] * 4) % 16 || (f.stride[2] * 4) % 16) return -1;
+    return (int)((a & 15) >> 2);
+}
+
+// The tensor map of one field for boxes of w x h x 1 elements; it covers exactly the field's
+// padded extent, from `xo` elements before its first padded element.
+inline bool make_map(const cg_field& f, int xo, int w, int h, CUtensorMap* out) {
+    const EncodeFn enc = encoder();
+    if (!enc) return false;
+    const uintptr_t a = reinterpret_cast<uintptr_t>(f.data);
+    const cuuint64_t ext0 = (cuuint64_t)(f.n[0] + 4 * f.halo[0]) + (cuuint64_t)xo;
     const cuuint64_t ext1 = (cuuint64_t)(f.n[1] + 4 * f.halo[1]), ext2 = (cuuint64_t)(f.n[2] + 4 * f.halo[2]);
     const cuuint64_t st1 = (cuuint64_t)f.stride[1] * 4, st2 = (cuuint64_t)f.stride[2] * 4;
-    if (st1 % 16 || st2 % 16 || (cuuint64_t)f.stride[1] < ext0 || st2 < st1 * ext1) return false;
+    if ((cuuint64_t)f.stride[1] < ext0 || st2 < st1 * ext1) return false;
     const cuuint64_t dims[3] = {ext0, ext1, ext2};
     const cuuint64_t strides[2] = {st1, st2};
-    const cuuint32_t box[3] = {(cuuint32_t)kCols, (cuuint32_t)rows, 1};
+    const cuuint32_t box[3] = {(cuuint32_t)w, (cuuint32_t)h, 1};
     const cuuint32_t estr[3] = {1, 1, 1};
-    void* base = reinterpret_cast<void*>(a - (uintptr_t)(*xo) * 4);
+    void* base = reinterpret_cast<void*>(a - (uintptr_t)xo * 4);
     return enc(out, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
                CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-// The six maps of one launch direction (inputs C, q read; D and C_old shared by both).
-inline bool make_maps(const cg_field& C, const cg_field* q, const cg_field& D, const cg_field& Co, int rows, Maps* m,
-                      XO* xo) {
-    return make_map(C, rows, &m->m[A_C], &xo->v[A_C]) && make_map(D, rows, &m->m[A_D], &xo->v[A_D]) &&
-           make_map(q[0], rows, &m->m[A_QX], &xo->v[A_QX]) && make_map(q[1], rows, &m->m[A_QY], &xo->v[A_QY]) &&
-           make_map(q[2], rows, &m->m[A_QZ], &xo->v[A_QZ]) && make_map(Co, rows, &m->m[A_CO], &xo->v[A_CO]);
+// Maps and boxes of one launch direction (inputs C, q read; D and C_old shared by both) for
+// blocks of nw rows. Array a needs the logical columns i0 + lo .. i0 + hi of a tile starting at
+// column i0 (a multiple of 32), i.e. tensor columns i0 + lo + 1 + xo .. i0 + hi + 1 + xo.
+inline bool make_maps(const cg_field& C, const cg_field* q, const cg_field& D, const cg_field& Co, int nw, Maps* m,
+                      Boxes* bx) {
+    const cg_field* fs[kArrays] = {&C, &D, &q[0], &q[1], &q[2], &Co};
+    const int lo[kArrays] = {-1, -1, 0, 0, 0, 0}, hi[kArrays] = {32, 32, 32, 31, 31, 31};
+    int off = 0;
+    unsigned tx = 0;
+    for (int a = 0; a < kArrays; ++a) {
+        const int xo = map_offset(*fs[a]);
+        if (xo < 0) return false;
+        const int first = lo[a] + 1 + xo, last = hi[a] + 1 + xo;
+        const int x0 = first & ~3;
+        const int w = (last - x0 + 1 + 3) & ~3;
+        const int h = box_rows(a, nw);
+        if (w > kCols || !make_map(*fs[a], xo, w, h, &m->m[a])) return false;
+        bx->x0[a] = x0;
+        bx->y0[a] = (a == A_C || a == A_D) ? 0 : 1;
+        bx->w[a] = w;
+        bx->cb[a] = 1 + xo - x0;
+        bx->off[a] = off;
+        off += ((w * h * 4 + 127) / 128) * 32;
+        tx += (unsigned)(w * h * 4);
+    }
+    bx->sf = off;
+    bx->tx = tx;
+    return true;
 }
 
 }  // namespace ptdt
 
-// Maps for both ping-pong directions of a fused run, for the two block heights of the TMA
-// variants (8 and 16 rows), and the device error flag the kernel raises on a wait that ran out.
+// Maps and boxes for both ping-pong directions of a fused run, for the two block heights of the
+// TMA variants (8 and 16 rows), and the device error flag the kernel raises on a wait that ran
+// out.
+constexpr int kPdHeights = 4;
+constexpr int kPdHeight[kPdHeights] = {8, 16, 20, 24};  // block rows of the TMA variants
+
 struct PdTma {
     bool ok = false;
-    ptdt::Maps ab8, ba8, ab16, ba16;
-    ptdt::XO xab, xba;
+    ptdt::Maps ab[kPdHeights], ba[kPdHeights];
+    ptdt::Boxes bab[kPdHeights], bba[kPdHeights];
     int* err = nullptr;
 };
 
@@ -293,8 +334,9 @@ inline PdTma make_pd_tma(const cg_field& Ca, const cg_field* qa, const cg_field&
                          const cg_field& Co, int* err) {
     PdTma t;
     t.err = err;
-    ptdt::XO x2;
-    t.ok = err && ptdt::make_maps(Ca, qa, D, Co, 10, &t.ab8, &t.xab) && ptdt::make_maps(Cb, qb, D, Co, 10, &t.ba8, &t.xba) &&
-           ptdt::make_maps(Ca, qa, D, Co, 18, &t.ab16, &x2) && ptdt::make_maps(Cb, qb, D, Co, 18, &t.ba16, &x2);
+    t.ok = err != nullptr;
+    for (int h = 0; h < kPdHeights && t.ok; ++h)
+        t.ok = ptdt::make_maps(Ca, qa, D, Co, kPdHeight[h], &t.ab[h], &t.bab[h]) &&
+               ptdt::make_maps(Cb, qb, D, Co, kPdHeight[h], &t.ba[h], &t.bba[h]);
     return t;
 }

@@ -385,18 +385,18 @@ namespace {
 
 // The tensor maps of one ping-pong direction of a fused run (TMA variants), or none.
 struct PdDir {
-    const ptdt::Maps* m8 = nullptr;   // boxes of 8 + 2 rows
-    const ptdt::Maps* m16 = nullptr;  // boxes of 16 + 2 rows
-    ptdt::XO xo{};
+    const ptdt::Maps* m[kPdHeights] = {};  // per block height (kPdHeight)
+    const ptdt::Boxes* b[kPdHeights] = {};
     int* err = nullptr;
 };
 
 inline PdDir pd_dir(const PdTma& t, bool ab) {
     PdDir d;
     if (!t.ok) return d;
-    d.m8 = ab ? &t.ab8 : &t.ba8;
-    d.m16 = ab ? &t.ab16 : &t.ba16;
-    d.xo = ab ? t.xab : t.xba;
+    for (int h = 0; h < kPdHeights; ++h) {
+        d.m[h] = ab ? &t.ab[h] : &t.ba[h];
+        d.b[h] = ab ? &t.bab[h] : &t.bba[h];
+    }
     d.err = t.err;
     return d;
 }
@@ -404,44 +404,66 @@ inline PdDir pd_dir(const PdTma& t, bool ab) {
 // Longest time a TMA variant's block waits on one barrier before it reports CG_ERR_TIMEOUT.
 constexpr unsigned long long kPdWaitLimitNs = 2000000000ull;
 
-template <int NW, int MINB>
+// Shared memory that leaves room for at most `blocks` blocks per SM (228 KB per SM, 1 KB of it
+// reserved per block), or what the ring needs when that is more; blocks = 0: the size for the
+// widest boxes (max_smem_bytes).
+inline int pd_smem_for(int need, int blocks, int widest) {
+    if (blocks == 0) return need > widest ? need : widest;
+    const int cap = (233472 / blocks - 1024) & ~127;
+    return need > cap ? need : cap;
+}
+
+// The TMA-fed iteration with blocks of NW rows, a ring of S planes and at most B blocks per SM
+// (B = 0: the shared memory of the widest boxes). Measured at 512^3, fewer concurrent blocks
+// were faster, and the launch bounds' register budget mattered: the kept layouts are the
+// fastest of the sweep.
+template <int NW, int MINB, int S, int B>
 cudaError_t launch_pd_tma(const PDM<float>& f, const cg_grid* g, int num_sms, cudaStream_t st, const ptdt::Maps& maps,
-                          const ptdt::XO& xo, int* err) {
-    using Gm = ptdt::Geom<NW>;
+                          const ptdt::Boxes& bx, int* err) {
+    auto kern = ptd_tma_kernel<NW, MINB, S>;
+    const int smem = pd_smem_for(ptdt::smem_bytes(S, bx.sf), B, ptdt::max_smem_bytes<NW, S>());
+    static const bool attr = [&] {
+        const bool r = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 232448) == cudaSuccess;
+        cudaGetLastError();
+        return r;
+    }();
+    (void)attr;
     const int e0 = g->n[0] + 1, e1 = g->n[1] + 1, e2 = g->n[2] + 1;
     const int ntx = cg_div_up(e0 + 1, 32), nty = cg_div_up(e1 + 1, NW);
-    static const int bps = [] {
-        int nb = 0;
-        if (cudaFuncSetAttribute(ptd_tma_kernel<NW, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, Gm::smem_bytes) !=
-                cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, ptd_tma_kernel<NW, MINB>, 32 * NW, Gm::smem_bytes) !=
-                cudaSuccess)
-            nb = 0;
+    int bps = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, 32 * NW, smem) != cudaSuccess || bps < 1) {
         cudaGetLastError();
-        return nb > 0 ? nb : 1;
-    }();
+        bps = 1;
+    }
     const long tiles = (long)ntx * nty;
     const int seg = pd_seg_len(tiles, e2 + 1, (long)num_sms * bps);
     const int nseg = cg_div_up(e2 + 1, seg);
-    ptd_tma_kernel<NW, MINB><<<(unsigned)(tiles * nseg), 32 * NW, Gm::smem_bytes, st>>>(maps, f, xo, e0, e1, e2, ntx, nty,
-                                                                                      seg, kPdWaitLimitNs, err);
+    kern<<<(unsigned)(tiles * nseg), 32 * NW, smem, st>>>(maps, f, bx, e0, e1, e2, ntx, nty, seg, kPdWaitLimitNs, err);
     return cudaGetLastError();
 }
 
 // Launch layouts of the fused iteration. Variants 0-3, ptd_march3d_kernel (all without register
 // spills for FP32): 8 rows at 4 or 5 blocks per SM, 16 rows at 2, 4 rows at 10; taller blocks
-// read fewer y-halo rows, more resident warps keep more loads in flight. Variants 4-5,
-// ptd_tma_kernel with 8 and 16 rows (inputs staged by TMA; only with tensor maps for the
-// direction).
-constexpr int kPdVariants = 6;
+// read fewer y-halo rows, more resident warps keep more loads in flight. Variants 4-7,
+// ptd_tma_kernel (inputs staged by TMA; only with tensor maps for the direction), rings of 4
+// planes with the shared memory of the widest boxes: blocks of 8, 16, 20 and 24 rows (at 512^3
+// 24 rows, 2 blocks per SM, measured fastest; 32 rows, 1 block per SM, 27 % slower).
+constexpr int kPdVariants = 8;
 constexpr int kPdTmaFirst = 4;
 
 template <class T>
 cudaError_t launch_pd_march3d(const PDM<T>& f, const cg_grid* g, int num_sms, cudaStream_t st, int variant,
                               const PdDir& dir = PdDir{}) {
     if constexpr (sizeof(T) == 4) {
-        if (variant == 4 && dir.m8) return launch_pd_tma<8, 4>(f, g, num_sms, st, *dir.m8, dir.xo, dir.err);
-        if (variant == 5 && dir.m16) return launch_pd_tma<16, 2>(f, g, num_sms, st, *dir.m16, dir.xo, dir.err);
+        if (variant >= kPdTmaFirst && dir.m[0]) {
+            const int h = variant - kPdTmaFirst;
+            if (h == 0) return launch_pd_tma<8, 4, 4, 0>(f, g, num_sms, st, *dir.m[0], *dir.b[0], dir.err);
+            if (h == 1) return launch_pd_tma<16, 2, 4, 0>(f, g, num_sms, st, *dir.m[1], *dir.b[1], dir.err);
+            // launch bounds of one block for 20 and 24 rows: with two, ptxas fits the kernel in
+            // 35-36 registers instead of 38, and 24 rows measured 1224 instead of 1050 us at 512^3
+            if (h == 2) return launch_pd_tma<20, 1, 4, 0>(f, g, num_sms, st, *dir.m[2], *dir.b[2], dir.err);
+            if (h == 3) return launch_pd_tma<24, 1, 4, 0>(f, g, num_sms, st, *dir.m[3], *dir.b[3], dir.err);
+        }
     }
     switch (variant) {
         case 1: return launch_pd_ix<T, 8, 5>(f, g, num_sms, st);
@@ -451,7 +473,7 @@ cudaError_t launch_pd_march3d(const PDM<T>& f, const cg_grid* g, int num_sms, cu
     }
 }
 
-// CG_PTD_VARIANT=<0..5> in the environment (read on every call): the fused iteration's layout
+// CG_PTD_VARIANT=<0..7> in the environment (read on every call): the fused iteration's layout
 // instead of the autotuner's (a TMA variant only where its tensor maps exist).
 inline int pd_variant_forced() {
     const char* e = std::getenv("CG_PTD_VARIANT");
@@ -464,7 +486,7 @@ inline int pd_variant_forced() {
 // is captured (the launch writes only the partner buffers) and cached for the process.
 template <class T>
 int tune_pd(const PDM<T>& f, const cg_grid* g, int num_sms, cudaStream_t st, const PdDir& dir = PdDir{}) {
-    const bool tma = dir.m8 != nullptr;
+    const bool tma = dir.m[0] != nullptr;
     const int forced = pd_variant_forced();
     if (forced >= 0) return (forced >= kPdTmaFirst && !tma) ? 0 : forced;
     if (!cg_autotune_enabled()) return 0;
@@ -566,10 +588,8 @@ int run_fused3d(cg_ctx* ctx, const cg_grid* g, const cg_ptdiff_fields* f, const 
     cg_key_add(key, variant);
     if (variant >= kPdTmaFirst) {
         // the maps encode this call's pointers: they are part of the graph's key
-        cg_key_add(key, tma.ab8);
-        cg_key_add(key, tma.ab16);
-        cg_key_add(key, tma.ba8);
-        cg_key_add(key, tma.ba16);
+        cg_key_add(key, tma.ab[variant - kPdTmaFirst]);
+        cg_key_add(key, tma.ba[variant - kPdTmaFirst]);
     }
     rc = cg_graph_run(ctx, key, [&](cudaStream_t st) {
         for (int a = 0; a < 4; ++a)

@@ -115,12 +115,13 @@ def test_fused_run_bitwise(arch, dims, npt):
         assert_close(a, b, 0.0, "q", exact=True)
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5, 6, 7])
 @pytest.mark.parametrize("dims", [(17, 12, 14), (64, 33, 20), (2, 2, 3), (70, 19, 41)])
 def test_fused_run_every_layout_bitwise(arch, monkeypatch, variant, dims):
     """Every launch layout of the fused iteration, forced with CG_PTD_VARIANT — the register-fed
-    ptd_march3d_kernel at four block shapes (0-3) and the TMA-fed ptd_tma_kernel with 8 and 16
-    rows (4, 5), whose inputs stream through a ring of shared-memory planes — gives the oracle's
+    ptd_march3d_kernel at four block shapes (0-3) and the TMA-fed ptd_tma_kernel with blocks of
+    8, 16, 20 and 24 rows (4-7), whose inputs stream through a ring of shared-memory planes —
+    gives the oracle's
     update_q!/update_C!/bc! states bit for bit. The caller's fields (first padded element 12
     bytes past a 16-byte boundary) and the library's partner buffers (aligned) take different
     tensor-map offsets."""
