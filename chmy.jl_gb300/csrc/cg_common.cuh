@@ -46,6 +46,11 @@ struct cg_ctx {
 // Device scratch buffer `slot` of at least `bytes` (reallocated when too small; contents are
 // not preserved across growth). Sets *rc on failure and returns NULL.
 void* cg_scratch(cg_ctx* ctx, int slot, size_t bytes, int* rc);
+// The wait flag of the TMA-fed kernels (scratch slot 10), cleared on the context's stream: a
+// kernel whose bounded wait for staged data ran out sets it. cg_tma_check reads it after a run
+// (synchronising the stream) and reports CG_ERR_TIMEOUT for `what` when it is set.
+int* cg_tma_flag(cg_ctx* ctx, int* rc);
+int cg_tma_check(cg_ctx* ctx, int* flag, const char* what);
 
 // Launch layouts chosen by timing (autotuner): a process-wide cache keyed by problem shape.
 // CG_AUTOTUNE=0 in the environment turns the timing off (the launchers' fixed rules apply).

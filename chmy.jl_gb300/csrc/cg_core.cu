@@ -89,8 +89,9 @@ bool cg_autotune_enabled() {
 
 bool cg_tune_forced(cg_tune_cfg* out) {
     // CG_MARCH_LAYOUT=<segment length>:<variant> fixes the march kernels' launch layout (0 as
-    // the segment length keeps the launcher's rule; variant: the 3D block shape, or in 2D 1 for
-    // two iterations per pass): for profiling one layout without timing the candidates first
+    // the segment length keeps the launcher's rule; variant: the 3D block shape, or in 2D 1 and
+    // 2 for two iterations per pass): for profiling one layout without timing the candidates
+    // first
     const char* e = std::getenv("CG_MARCH_LAYOUT");
     if (!e || !e[0]) return false;
     int seg = 0, var = 0;
@@ -180,6 +181,24 @@ bool cg_tune_lookup(const std::string& key, cg_tune_cfg* out) {
 void cg_tune_store(const std::string& key, const cg_tune_cfg& cfg) {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     g_tune[key] = cfg;
+}
+
+int* cg_tma_flag(cg_ctx* ctx, int* rc) {
+    int* e = static_cast<int*>(cg_scratch(ctx, 10, 256, rc));
+    if (*rc) return nullptr;
+    if (cudaMemsetAsync(e, 0, sizeof(int), ctx->stream) != cudaSuccess) {
+        *rc = cg_fail(ctx, CG_ERR_CUDA, "clearing the TMA wait flag failed");
+        return nullptr;
+    }
+    return e;
+}
+
+int cg_tma_check(cg_ctx* ctx, int* flag, const char* what) {
+    int h = 0;
+    CG_CUDA(ctx, cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (h) return cg_fail(ctx, CG_ERR_TIMEOUT, "%s: a wait for staged data timed out", what);
+    return CG_OK;
 }
 
 void* cg_scratch(cg_ctx* ctx, int slot, size_t bytes, int* rc) {

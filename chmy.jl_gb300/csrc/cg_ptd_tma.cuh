@@ -19,9 +19,11 @@
 // the allocation; box elements beyond it read as zero and are never used.
 #pragma once
 
-#include <cuda.h>  // CUtensorMap and its enums (the encoder is reached through the runtime)
+#include "cg_tma.cuh"
 
 namespace ptdt {
+
+using namespace cgtma;
 
 constexpr int kCols = 40;    // box width: 32 tile columns, the x halos and the 16-byte alignment slack
 constexpr int kArrays = 6;   // box order
@@ -58,62 +60,18 @@ __host__ __device__ constexpr int box_rows(int a, int nw) {
     return (a == A_C || a == A_D) ? nw + 2 : (a == A_QY ? nw + 1 : nw);
 }
 
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t* b, unsigned count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, unsigned bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint64_t* b) {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* b, unsigned parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(smem_u32(b)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-__device__ __forceinline__ unsigned long long now_ns() {
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-// Wait for the phase of barrier b with the given parity; false when limit_ns ran out first.
-__device__ __forceinline__ bool mbar_wait(uint64_t* b, unsigned parity, unsigned long long limit_ns) {
-    if (mbar_try_wait(b, parity)) return true;
-    const unsigned long long t0 = now_ns();
-    for (;;) {
-        if (mbar_try_wait(b, parity)) return true;
-        if (now_ns() - t0 > limit_ns) return false;
-    }
-}
-// One box of a 3D tensor map into shared memory; its bytes complete on barrier `bar`.
-__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar) {
-    asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(
-            smem_u32(dst)),
-        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
-        : "memory");
-}
-
 }  // namespace ptdt
 
 // The TMA-fed fused iteration. Block = NW warps over a tile of 32 x NW (i, j) columns and one z
-// segment; plane m of the ring is logical plane ks - 1 + m (tensor z = ks + m), box rows are the
-// logical rows j0 - 1 .. j0 + NW (tensor y = j0 ...), box column c is tensor x = i0 + c, i.e.
-// logical i0 - 1 - xo + c for an array whose map starts xo elements before its first element.
+// segment; plane m of the ring is logical plane ks - 1 + m (tensor z = ks + m); array a's box in
+// a slot starts at tensor (i0 + x0, j0 + y0) (Boxes).
 template <int NW, int MINB, int S>
 __global__ void __launch_bounds__(32 * NW, MINB)
     ptd_tma_kernel(const __grid_constant__ ptdt::Maps maps, const PDM<float> f, const ptdt::Boxes bx, int e0, int e1, int e2,
                    int ntx, int nty, int seg_len, unsigned long long limit_ns, int* err) {
     using namespace cgk;
     using namespace ptdt;
+    using namespace cgtma;
     constexpr unsigned FULL = 0xffffffffu;
     extern __shared__ __align__(128) unsigned char smdyn[];
     // the ring starts on a 128-byte boundary of the shared window (the copies' destinations)
@@ -237,24 +195,6 @@ __global__ void __launch_bounds__(32 * NW, MINB)
 }
 
 namespace ptdt {
-
-using EncodeFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*, const cuuint64_t*,
-                              const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
-                              CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-inline EncodeFn encoder() {
-    static const EncodeFn fn = [] {
-        void* p = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
-            q != cudaDriverEntryPointSuccess) {
-            cudaGetLastError();
-            return (EncodeFn) nullptr;
-        }
-        return reinterpret_cast<EncodeFn>(p);
-    }();
-    return fn;
-}
 
 // Elements between a field's first padded element and the 16-byte boundary at or before it;
 // -1 when the field cannot have a tensor map (FP32 3D, 4-byte aligned, 16-byte row strides).

@@ -514,26 +514,6 @@ int tune_pd(const PDM<T>& f, const cg_grid* g, int num_sms, cudaStream_t st, con
     return best.variant;
 }
 
-// The TMA variants' wait flag (scratch slot 10), cleared on the stream.
-int* pd_err_flag(cg_ctx* ctx, int* rc) {
-    int* e = static_cast<int*>(cg_scratch(ctx, 10, 256, rc));
-    if (*rc) return nullptr;
-    if (cudaMemsetAsync(e, 0, sizeof(int), ctx->stream) != cudaSuccess) {
-        *rc = cg_fail(ctx, CG_ERR_CUDA, "ptdiff: clearing the wait flag failed");
-        return nullptr;
-    }
-    return e;
-}
-
-// After a run that used a TMA variant: CG_ERR_TIMEOUT when a block's wait ran out (synchronises).
-int pd_check_flag(cg_ctx* ctx, int* e) {
-    int h = 0;
-    CG_CUDA(ctx, cudaMemcpyAsync(&h, e, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-    CG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    if (h) return cg_fail(ctx, CG_ERR_TIMEOUT, "ptdiff fused iteration: a staged-plane wait timed out");
-    return CG_OK;
-}
-
 template <class T>
 PDM<T> make_pdm(const cg_grid* g, const cg_field& C, const cg_field* q, const cg_field& Cn, const cg_field* qn,
                 const cg_ptdiff_fields* f, const cg_ptdiff_params* p) {
@@ -579,7 +559,7 @@ int run_fused3d(cg_ctx* ctx, const cg_grid* g, const cg_ptdiff_fields* f, const 
     }
     const PDM<T> ab = make_pdm<T>(g, f->C, f->q, part[0], part + 1, f, p);
     const PDM<T> ba = make_pdm<T>(g, part[0], part + 1, f->C, f->q, f, p);
-    int* err = pd_err_flag(ctx, &rc);
+    int* err = cg_tma_flag(ctx, &rc);
     if (rc) return rc;
     const PdTma tma = make_pd_tma(f->C, f->q, part[0], part + 1, f->D, f->C_old, err);
     const PdDir dab = pd_dir(tma, true), dba = pd_dir(tma, false);
@@ -612,7 +592,7 @@ int run_fused3d(cg_ctx* ctx, const cg_grid* g, const cg_ptdiff_fields* f, const 
         return (int)CG_OK;
     });
     if (rc) return rc;
-    return variant >= kPdTmaFirst ? pd_check_flag(ctx, err) : CG_OK;
+    return variant >= kPdTmaFirst ? cg_tma_check(ctx, err, "ptdiff fused iteration") : CG_OK;
 }
 
 // The fused path needs a 3D FP32 grid, no residual output, and one row and plane stride for
@@ -986,7 +966,7 @@ int solve_dc(cg_ctx* ctx, const cg_grid* g, const cg_ptdiff_fields* f, const cg_
     }
     const PDM<float> ab = make_pdm<float>(g, dA, qA, dB, qB, &w, p);
     const PDM<float> ba = make_pdm<float>(g, dB, qB, dA, qA, &w, p);
-    int* perr = pd_err_flag(ctx, &rc);
+    int* perr = cg_tma_flag(ctx, &rc);
     if (rc) return rc;
     const PdTma tma = make_pd_tma(dA, qA, dB, qB, D32, co, perr);
     const PdDir dab = pd_dir(tma, true), dba = pd_dir(tma, false);
@@ -1050,7 +1030,7 @@ int solve_dc(cg_ctx* ctx, const cg_grid* g, const cg_ptdiff_fields* f, const cg_
                 break;  // the FP32 floor: back to the FP64 defect
             }
         }
-        if (variant >= kPdTmaFirst && (rc = pd_check_flag(ctx, perr))) return rc;
+        if (variant >= kPdTmaFirst && (rc = cg_tma_check(ctx, perr, "ptdiff fused iteration"))) return rc;
         pd_update_kernel<<<ig, ib, 0, ctx->stream>>>(cg_view<double>(f->C), cg_view<float>(dA), g->n[0], g->n[1], g->n[2]);
         CG_CHECK_LAUNCH(ctx);
         if ((rc = cg_bc_apply_impl(ctx, g, 1, &f->C, bc))) return rc;
