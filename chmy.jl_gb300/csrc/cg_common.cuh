@@ -102,6 +102,15 @@ struct cg_barrier_cfg {
     int withheld = 0;
 };
 cg_barrier_cfg cg_sia_barrier_cfg();
+// Waits of the TMA-fed kernels: the time limit of every wait (CG_TMA_WAIT_LIMIT_MS, default
+// 2000 ms) and a ring plane whose copies the producer does not issue (CG_TMA_WITHHOLD_PLANE,
+// default none), so that a test can make the consumers' waits run out without a fault: the
+// kernel returns and the call reports CG_ERR_TIMEOUT. Read on every call.
+struct cg_tma_cfg {
+    unsigned long long limit_ns = 2000000000ull;
+    int withhold = -1;
+};
+cg_tma_cfg cg_tma_wait_cfg();
 
 template <class... P, class... A>
 inline cudaError_t cg_launch(void (*kern)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, bool dep,

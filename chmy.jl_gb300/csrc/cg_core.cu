@@ -162,6 +162,19 @@ cg_barrier_cfg cg_sia_barrier_cfg() {
     return c;
 }
 
+cg_tma_cfg cg_tma_wait_cfg() {
+    cg_tma_cfg c;
+    if (const char* e = std::getenv("CG_TMA_WAIT_LIMIT_MS")) {
+        const long ms = std::strtol(e, nullptr, 10);
+        if (ms >= 1 && ms <= 60000) c.limit_ns = (unsigned long long)ms * 1000000ull;
+    }
+    if (const char* e = std::getenv("CG_TMA_WITHHOLD_PLANE")) {
+        const long m = std::strtol(e, nullptr, 10);
+        if (m >= 0 && m <= 1000000) c.withhold = (int)m;
+    }
+    return c;
+}
+
 bool cg_tune_verbose() {
     static const bool on = [] {
         const char* e = std::getenv("CG_TUNE_VERBOSE");

@@ -68,7 +68,7 @@ __host__ __device__ constexpr int box_rows(int a, int nw) {
 template <int NW, int MINB, int S>
 __global__ void __launch_bounds__(32 * NW, MINB)
     ptd_tma_kernel(const __grid_constant__ ptdt::Maps maps, const PDM<float> f, const ptdt::Boxes bx, int e0, int e1, int e2,
-                   int ntx, int nty, int seg_len, unsigned long long limit_ns, int* err) {
+                   int ntx, int nty, int seg_len, unsigned long long limit_ns, int withhold, int* err) {
     using namespace cgk;
     using namespace ptdt;
     using namespace cgtma;
@@ -106,6 +106,7 @@ __global__ void __launch_bounds__(32 * NW, MINB)
     __syncthreads();
     float* ring = reinterpret_cast<float*>(smraw);
     auto issue = [&](int m) {
+        if (m == withhold) return;  // a test's withheld plane: its waits run out
         float* dst = ring + (m & (S - 1)) * bx.sf;
         uint64_t* bar = &full[m & (S - 1)];
         mbar_expect_tx(bar, bx.tx);
@@ -190,7 +191,8 @@ __global__ void __launch_bounds__(32 * NW, MINB)
         // the producing thread's copies still in flight complete before the block's shared
         // memory goes away (bounded; they complete unless the copy itself failed)
         if (threadIdx.x == 0)
-            for (int m = waited + 1; m <= issued; ++m) mbar_wait(&full[m & (S - 1)], (m / S) & 1, limit_ns);
+            for (int m = waited + 1; m <= issued; ++m)
+                if (m != withhold) mbar_wait(&full[m & (S - 1)], (m / S) & 1, limit_ns);
     }
 }
 

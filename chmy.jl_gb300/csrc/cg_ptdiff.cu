@@ -401,9 +401,6 @@ inline PdDir pd_dir(const PdTma& t, bool ab) {
     return d;
 }
 
-// Longest time a TMA variant's block waits on one barrier before it reports CG_ERR_TIMEOUT.
-constexpr unsigned long long kPdWaitLimitNs = 2000000000ull;
-
 // Shared memory that leaves room for at most `blocks` blocks per SM (228 KB per SM, 1 KB of it
 // reserved per block), or what the ring needs when that is more; blocks = 0: the size for the
 // widest boxes (max_smem_bytes).
@@ -438,7 +435,9 @@ cudaError_t launch_pd_tma(const PDM<float>& f, const cg_grid* g, int num_sms, cu
     const long tiles = (long)ntx * nty;
     const int seg = pd_seg_len(tiles, e2 + 1, (long)num_sms * bps);
     const int nseg = cg_div_up(e2 + 1, seg);
-    kern<<<(unsigned)(tiles * nseg), 32 * NW, smem, st>>>(maps, f, bx, e0, e1, e2, ntx, nty, seg, kPdWaitLimitNs, err);
+    const cg_tma_cfg wc = cg_tma_wait_cfg();
+    kern<<<(unsigned)(tiles * nseg), 32 * NW, smem, st>>>(maps, f, bx, e0, e1, e2, ntx, nty, seg, wc.limit_ns, wc.withhold,
+                                                         err);
     return cudaGetLastError();
 }
 
@@ -567,9 +566,11 @@ int run_fused3d(cg_ctx* ctx, const cg_grid* g, const cg_ptdiff_fields* f, const 
     cg_key_add(key, base);
     cg_key_add(key, variant);
     if (variant >= kPdTmaFirst) {
-        // the maps encode this call's pointers: they are part of the graph's key
+        // the maps encode this call's pointers, and the wait settings are kernel arguments:
+        // both are part of the graph's key
         cg_key_add(key, tma.ab[variant - kPdTmaFirst]);
         cg_key_add(key, tma.ba[variant - kPdTmaFirst]);
+        cg_key_add(key, cg_tma_wait_cfg());
     }
     rc = cg_graph_run(ctx, key, [&](cudaStream_t st) {
         for (int a = 0; a < 4; ++a)
@@ -979,6 +980,7 @@ int solve_dc(cg_ctx* ctx, const cg_grid* g, const cg_ptdiff_fields* f, const cg_
     cg_key_add(key, bc0);
     cg_key_add(key, nchunk);
     cg_key_add(key, variant);
+    cg_key_add(key, cg_tma_wait_cfg());
     const dim3 ib(32, 8), ig(cg_div_up(g->n[0], 32), cg_div_up(g->n[1], 8), g->n[2]);
     int total = 0;
     const size_t zero_bytes = per_al * 8;  // d, d', q, q' (the first eight arrays)

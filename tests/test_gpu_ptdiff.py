@@ -148,6 +148,48 @@ def test_fused_run_every_layout_bitwise(arch, monkeypatch, variant, dims):
         assert_close(a, b, 0.0, f"q variant {variant}", exact=True)
 
 
+def test_tma_wait_runs_out_and_the_context_stays_usable(arch, monkeypatch):
+    """Failure detection of the TMA-fed iteration without a GPU fault: the producing thread
+    withholds the copies of one ring plane (CG_TMA_WITHHOLD_PLANE) and every wait is limited to
+    20 ms (CG_TMA_WAIT_LIMIT_MS). The waits for that plane run out, the blocks stop (the
+    producer first waits, bounded, for its copies in flight) and cg_ptdiff_run reports
+    CG_ERR_TIMEOUT. The same context then runs the iteration to the oracle's bits."""
+    import time
+
+    T = np.float32
+    monkeypatch.setenv("CG_PTD_VARIANT", "4")
+    monkeypatch.setenv("CG_TMA_WAIT_LIMIT_MS", "20")
+    monkeypatch.setenv("CG_TMA_WITHHOLD_PLANE", "5")
+    dims = (40, 30, 24)
+    grid, h, d = fields(arch, dims, T, 8, pitch_align=128)
+    p = ptdiff_params(grid, dt=1e-3, Dmax=float(h["D"].a.max()))
+    bc = to_cg_bc(3, {"x": Dirichlet(0.25), "y": Neumann(0.5), "z": Neumann()})
+    g = grid.desc()
+    dd = desc(d)
+    dd.R = _abi.cg_field()
+    t0 = time.perf_counter()
+    rc = arch.lib.cg_ptdiff_run(arch.ctx, ctypes.byref(g), ctypes.byref(dd), ctypes.byref(p), ctypes.byref(bc), 1, 4)
+    waited = time.perf_counter() - t0
+    assert rc == _abi.CG_ERR_TIMEOUT, (rc, arch.lib.cg_last_error(arch.ctx))
+    assert b"timed out" in arch.lib.cg_last_error(arch.ctx)
+    assert waited < 10.0, waited  # the 20 ms limits applied, not the 2 s default
+    monkeypatch.delenv("CG_TMA_WITHHOLD_PLANE")
+    monkeypatch.delenv("CG_TMA_WAIT_LIMIT_MS")
+    grid, h, d = fields(arch, dims, T, 9, pitch_align=128)
+    hd = desc(h)
+    npt = 4
+    h["C_old"].a[...] = h["C"].a
+    for _ in range(npt):
+        lib().or_ptdiff_update_q(ctypes.byref(g), ctypes.byref(hd), ctypes.byref(p))
+        lib().or_ptdiff_update_C(ctypes.byref(g), ctypes.byref(hd), ctypes.byref(p))
+        bc_apply(grid, [h["C"]], [bc])
+    dd = desc(d)
+    dd.R = _abi.cg_field()
+    arch.call("cg_ptdiff_run", ctypes.byref(g), ctypes.byref(dd), ctypes.byref(p), ctypes.byref(bc), 1, npt)
+    arch.synchronize()
+    assert_close(d["C"], h["C"], 0.0, "C after a timed-out run", exact=True)
+
+
 def _np_residual(C, Co, D, idx, dt):
     """max |R| dt over the interior of the implicit step R = -(C - C_old)/dt - divg(q(C)),
     q(C) = -lerp(D) ∂C, on padded [z, y, x] arrays with halo 1 (logical I at padded I + 1)."""
