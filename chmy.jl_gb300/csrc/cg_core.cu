@@ -89,13 +89,13 @@ bool cg_autotune_enabled() {
 
 bool cg_tune_forced(cg_tune_cfg* out) {
     // CG_MARCH_LAYOUT=<segment length>:<variant> fixes the march kernels' launch layout (0 as
-    // the segment length keeps the launcher's rule; variant: the 3D block shape, or in 2D 1 and
-    // 2 for two iterations per pass): for profiling one layout without timing the candidates
-    // first
+    // the segment length keeps the launcher's rule; variant: in 3D 0-1 the register-fed block
+    // shapes and 2-3 the TMA-fed ones, in 2D 1 and 2 for two iterations per pass): for
+    // profiling one layout without timing the candidates first
     const char* e = std::getenv("CG_MARCH_LAYOUT");
     if (!e || !e[0]) return false;
     int seg = 0, var = 0;
-    if (std::sscanf(e, "%d:%d", &seg, &var) != 2 || seg < 0 || var < 0 || var > 2) return false;
+    if (std::sscanf(e, "%d:%d", &seg, &var) != 2 || seg < 0 || var < 0 || var > 3) return false;
     *out = cg_tune_cfg{seg, var};
     return true;
 }

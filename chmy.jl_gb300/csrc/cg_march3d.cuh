@@ -475,7 +475,7 @@ template <class T>
 inline cg_tune_cfg tune_march2d(const Fused2D<T>& f, const SP<T>& s, int n0, int n1, int nsm, cudaStream_t st) {
     cg_tune_cfg best{0, 0};
     if (cg_tune_forced(&best)) {
-        if (best.variant >= 1 && !march_x2_ok(f, n0, n1)) best.variant = 0;
+        if (best.variant > 2 || (best.variant >= 1 && !march_x2_ok(f, n0, n1))) best.variant = 0;
         return best;
     }
     if (!cg_autotune_enabled()) return best;
@@ -513,42 +513,6 @@ inline cg_tune_cfg tune_march2d(const Fused2D<T>& f, const SP<T>& s, int n0, int
                     best = cg_tune_cfg{seg, v};
                 }
             }
-    cudaGetLastError();
-    cg_tune_store(key, best);
-    return best;
-}
-
-template <class T>
-inline cg_tune_cfg tune_march3d(const Fused3D<T>& f, const SP<T>& s, int n0, int n1, int n2, int nsm, cudaStream_t st) {
-    cg_tune_cfg best{0, 0};
-    if (cg_tune_forced(&best)) return best;
-    if (!cg_autotune_enabled()) return best;
-    long s1 = 0, s2 = 0;
-    const bool uni = march3_uniform(f, &s1, &s2);
-    std::string key = "march3d";
-    cg_key_add(key, n0);
-    cg_key_add(key, n1);
-    cg_key_add(key, n2);
-    cg_key_add(key, (int)sizeof(T));
-    cg_key_add(key, uni ? s1 : 0L);
-    cg_key_add(key, uni ? s2 : 0L);
-    cg_key_add(key, nsm);
-    if (cg_tune_lookup(key, &best)) return best;
-    const int nvar = (sizeof(T) == 4 && uni) ? 2 : 1;
-    float tbest = 1e30f;
-    for (int v = 0; v < nvar; ++v)
-        for (int seg : {0, 16, 32, 64}) {
-            if (seg > n2 + 2) continue;
-            const float t =
-                time_launches([&] { return launch_march3d<T, false>(f, s, n0, n1, n2, nsm, seg, st, v); }, st);
-            if (cg_tune_verbose())
-                std::fprintf(stderr, "march3d tune %dx%dx%d: seg %d variant %d: %.1f us\n", n0, n1, n2, seg, v,
-                             t >= 0.f ? 1e3f * t / 3 : -1.f);
-            if (t >= 0.f && t < tbest) {
-                tbest = t;
-                best = cg_tune_cfg{seg, v};
-            }
-        }
     cudaGetLastError();
     cg_tune_store(key, best);
     return best;

@@ -198,33 +198,12 @@ __global__ void __launch_bounds__(32 * NW, MINB)
 
 namespace ptdt {
 
-// Elements between a field's first padded element and the 16-byte boundary at or before it;
-// -1 when the field cannot have a tensor map (FP32 3D, 4-byte aligned, 16-byte row strides).
-inline int map_offset(const cg_field& f) {
-    if (f.dtype != CG_F32 || f.ndim != 3 || !f.data) return -1;
-    const uintptr_t a = reinterpret_cast<uintptr_t>(f.data);
-    if ((a & 3) != 0 || (f.stride[1] * 4) % 16 || (f.stride[2] * 4) % 16) return -1;
-    return (int)((a & 15) >> 2);
-}
-
 // The tensor map of one field for boxes of w x h x 1 elements; it covers exactly the field's
 // padded extent, from `xo` elements before its first padded element.
 inline bool make_map(const cg_field& f, int xo, int w, int h, CUtensorMap* out) {
-    const EncodeFn enc = encoder();
-    if (!enc) return false;
-    const uintptr_t a = reinterpret_cast<uintptr_t>(f.data);
-    const cuuint64_t ext0 = (cuuint64_t)(f.n[0] + 4 * f.halo[0]) + (cuuint64_t)xo;
-    const cuuint64_t ext1 = (cuuint64_t)(f.n[1] + 4 * f.halo[1]), ext2 = (cuuint64_t)(f.n[2] + 4 * f.halo[2]);
-    const cuuint64_t st1 = (cuuint64_t)f.stride[1] * 4, st2 = (cuuint64_t)f.stride[2] * 4;
-    if ((cuuint64_t)f.stride[1] < ext0 || st2 < st1 * ext1) return false;
-    const cuuint64_t dims[3] = {ext0, ext1, ext2};
-    const cuuint64_t strides[2] = {st1, st2};
-    const cuuint32_t box[3] = {(cuuint32_t)w, (cuuint32_t)h, 1};
-    const cuuint32_t estr[3] = {1, 1, 1};
-    void* base = reinterpret_cast<void*>(a - (uintptr_t)xo * 4);
-    return enc(out, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+    const cuuint64_t ext[3] = {(cuuint64_t)(f.n[0] + 4 * f.halo[0]) + (cuuint64_t)xo, (cuuint64_t)(f.n[1] + 4 * f.halo[1]),
+                               (cuuint64_t)(f.n[2] + 4 * f.halo[2])};
+    return make_map_ext(f, xo, ext, w, h, out);
 }
 
 // Maps and boxes of one launch direction (inputs C, q read; D and C_old shared by both) for

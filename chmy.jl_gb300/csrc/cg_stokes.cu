@@ -7,7 +7,7 @@ int cg_maxabs_collect(cg_ctx* ctx, int nfields, const cg_field* fields, double* 
 int cg_stokes_solve_dc(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f, const cg_stokes_params* p,
                        const cg_bc* bc_V, const cg_solve_opts* o, cg_solve_result* res);
 
-#include "cg_march3d.cuh"
+#include "cg_march3d_tma.cuh"
 #include "cg_stokes_kernels.cuh"
 
 namespace {
@@ -635,9 +635,30 @@ int pp_iterations_3d(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* a, c
     const Fused3D<T> fab = fused3_view<T>(a, b, a), fba = fused3_view<T>(b, a, a);
     const SP<T> s = scalars<T>(g, p);
     const bool res = cg_present(a->divV) && cg_present(a->r_V[0]);
-    const cg_tune_cfg tc = tune_march3d(fab, s, g->n[0], g->n[1], g->n[2], ctx->num_sms, ctx->stream);
+    // tensor maps of the TMA-fed variants (FP32 layouts that allow them)
+    m3t::Tma tma;
+    int* err = nullptr;
+    if constexpr (sizeof(T) == 4) {
+        int rc = CG_OK;
+        err = cg_tma_flag(ctx, &rc);
+        if (rc) return rc;
+        const cg_field* Va[3] = {&a->V[0], &a->V[1], &a->V[2]};
+        const cg_field* Vb[3] = {&b->V[0], &b->V[1], &b->V[2]};
+        const cg_field *ta[6], *tb[6], *to[6];
+        for (int c = 0; c < 6; ++c) {
+            ta[c] = &a->tau[c];
+            tb[c] = &b->tau[c];
+            to[c] = &a->tau_old[c];
+        }
+        const cg_field* rho[3] = {&a->rho_g[0], &a->rho_g[1], &a->rho_g[2]};
+        tma = m3t::make_tma(Va, &a->P, ta, Vb, &b->P, tb, &a->inv_eta, to, nullptr, rho, g->n, err);
+    }
+    const M3Launch lab = m3_launch_of(&tma, true), lba = m3_launch_of(&tma, false);
+    const cg_tune_cfg tc = tune_march3d(fab, s, g->n[0], g->n[1], g->n[2], ctx->num_sms, ctx->stream, lab);
+    const bool staged = tma.ok && tc.variant >= kM3TmaFirst;
     std::string key = "stokes_pp3";
     cg_key_add(key, tc);
+    if (staged) cg_key_add(key, cg_tma_wait_cfg());
     cg_key_add(key, *g);
     cg_key_add(key, *a);
     cg_key_add(key, *b);
@@ -646,13 +667,15 @@ int pp_iterations_3d(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* a, c
     cg_bc none[3];
     std::memset(none, 0, sizeof(none));
     for (int d = 0; d < 3; ++d) cg_key_add(key, bc_V ? bc_V[d] : none[d]);
-    return cg_graph_run(ctx, key, [&](cudaStream_t st) {
+    const int rc = cg_graph_run(ctx, key, [&](cudaStream_t st) {
         for (int it = 0; it < niter; ++it) {
             const Fused3D<T>& fk = (it % 2 == 0) ? fab : fba;
+            const M3Launch& lk = (it % 2 == 0) ? lab : lba;
             const int nsm = ctx->num_sms;
-            const cudaError_t le = (res && it == niter - 1)
-                                       ? launch_march3d<T, true>(fk, s, g->n[0], g->n[1], g->n[2], nsm, tc.seg, st, tc.variant, it > 0)
-                                       : launch_march3d<T, false>(fk, s, g->n[0], g->n[1], g->n[2], nsm, tc.seg, st, tc.variant, it > 0);
+            const cudaError_t le =
+                (res && it == niter - 1)
+                    ? launch_march3d_any<T, true>(fk, s, g->n[0], g->n[1], g->n[2], nsm, tc.seg, st, tc.variant, it > 0, lk)
+                    : launch_march3d_any<T, false>(fk, s, g->n[0], g->n[1], g->n[2], nsm, tc.seg, st, tc.variant, it > 0, lk);
             if (le != cudaSuccess) return cg_fail(ctx, CG_ERR_CUDA, "fused3d launch: %s", cudaGetErrorString(le));
             if (bc_V) {
                 int r = cg_bc_apply_impl(ctx, g, 3, (it % 2 == 0) ? b->V : a->V, bc_V, true);
@@ -661,6 +684,8 @@ int pp_iterations_3d(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* a, c
         }
         return (int)CG_OK;
     });
+    if (rc || !staged) return rc;
+    return cg_tma_check(ctx, err, "fused3d iteration");
 }
 
 template <class T>

@@ -11,7 +11,7 @@
 // homogeneous boundary conditions (same kinds, zero values), graph-replayed, until the
 // FP32 measures fall below max(0.5 eps, inner_rtol * outer measure) or stagnate.
 // Update (FP64): V += dV, P += dP, tau += dtau, then bc!(V).
-#include "cg_march3d.cuh"
+#include "cg_march3d_tma.cuh"
 #include "cg_stokes_kernels.cuh"
 
 int cg_maxabs_enqueue(cg_ctx* ctx, int nfields, const cg_field* fields);
@@ -492,6 +492,24 @@ int cg_stokes_solve_dc(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f,
         ga.P_in = gb.P_out = cg_view<float>(w.dP);
         ga.P_out = gb.P_in = cg_view<float>(w.dP2);
     }
+    // tensor maps of the TMA-fed 3D variants (A -> B reads dV, dP, dtau; B -> A the partners)
+    m3t::Tma tma;
+    int* terr = nullptr;
+    if (nd == 3) {
+        terr = cg_tma_flag(ctx, &rc);
+        if (rc) return rc;
+        const cg_field* Va[3] = {&w.dV[0], &w.dV[1], &w.dV[2]};
+        const cg_field* Vb[3] = {&w.dV2[0], &w.dV2[1], &w.dV2[2]};
+        const cg_field *ta[6], *tb[6], *to[6];
+        for (int c = 0; c < 6; ++c) {
+            ta[c] = &w.dtau[c];
+            tb[c] = &w.dtau2[c];
+            to[c] = &w.told[c];
+        }
+        const cg_field* rho[3] = {&w.rho[0], &w.rho[1], &w.rho[2]};
+        tma = m3t::make_tma(Va, &w.dP, ta, Vb, &w.dP2, tb, &w.ieta, to, &w.fP, rho, g->n, terr);
+    }
+    const M3Launch lga = m3_launch_of(&tma, true), lgb = m3_launch_of(&tma, false);
     const int nchunk = ncheck + (ncheck & 1);
     cg_key_add(key, nchunk);
     // 2D: bc!(dV) folded into the velocity reads from the chunk's second iteration on; the
@@ -503,8 +521,10 @@ int cg_stokes_solve_dc(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f,
     cg_key_add(key, (int)fold);
     // launch layout of the fused kernel, timed on the work buffers (A -> B) before capture
     const cg_tune_cfg tc = nd == 2 ? tune_march2d(fa, s32, g->n[0], g->n[1], ctx->num_sms, ctx->stream)
-                                   : tune_march3d(ga, s32, g->n[0], g->n[1], g->n[2], ctx->num_sms, ctx->stream);
+                                   : tune_march3d(ga, s32, g->n[0], g->n[1], g->n[2], ctx->num_sms, ctx->stream, lga);
     cg_key_add(key, tc);
+    const bool staged = nd == 3 && tma.ok && tc.variant >= kM3TmaFirst;
+    if (staged) cg_key_add(key, cg_tma_wait_cfg());
     // two iterations per pass (the tuner's variant 1) where bc!(dV) is folded into the reads:
     // passes alternate A -> B and B -> A, and an odd count of passes leaves its last two
     // iterations to the one-iteration kernel, so that the chunk ends in A
@@ -539,10 +559,13 @@ int cg_stokes_solve_dc(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f,
                     }
                 } else {
                     const Fused3D<float>& fk = (it % 2 == 0) ? ga : gb;
+                    const M3Launch& lk = (it % 2 == 0) ? lga : lgb;
                     const int nsm = ctx->num_sms;
                     const cudaError_t le =
-                        last ? launch_march3d<float, true>(fk, s32, g->n[0], g->n[1], g->n[2], nsm, tc.seg, st, tc.variant, it > 0)
-                             : launch_march3d<float, false>(fk, s32, g->n[0], g->n[1], g->n[2], nsm, tc.seg, st, tc.variant, it > 0);
+                        last ? launch_march3d_any<float, true>(fk, s32, g->n[0], g->n[1], g->n[2], nsm, tc.seg, st, tc.variant,
+                                                               it > 0, lk)
+                             : launch_march3d_any<float, false>(fk, s32, g->n[0], g->n[1], g->n[2], nsm, tc.seg, st,
+                                                                tc.variant, it > 0, lk);
                     if (le != cudaSuccess) return cg_fail(ctx, CG_ERR_CUDA, "fused3d launch: %s", cudaGetErrorString(le));
                     int r = cg_bc_apply_impl(ctx, g, nd, (it % 2 == 0) ? w.dV2 : w.dV, bc0, true);
                     if (r) return r;
@@ -603,6 +626,7 @@ int cg_stokes_solve_dc(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f,
         int since_best = 0;
         while (total_iter < o->max_iter) {
             if ((rc = chunk())) return rc;
+            if (staged && (rc = cg_tma_check(ctx, terr, "fused3d iteration"))) return rc;
             total_iter += nchunk;
             if ((rc = cg_bc_apply_impl(ctx, g, nd, f32.r_V, rbc))) return rc;
             if ((rc = cg_maxabs_enqueue(ctx, nd + 1, red32))) return rc;

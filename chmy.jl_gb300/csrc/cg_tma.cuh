@@ -9,6 +9,8 @@
 
 #include <cstdint>
 
+#include "../../include/chmy_gb300.h"  // cg_field
+
 namespace cgtma {
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -72,6 +74,36 @@ inline EncodeFn encoder() {
         return reinterpret_cast<EncodeFn>(p);
     }();
     return fn;
+}
+
+// Elements between a field's first padded element and the 16-byte boundary at or before it;
+// -1 when the field cannot have a tensor map (FP32 3D, 4-byte aligned, 16-byte row strides).
+inline int map_offset(const cg_field& f) {
+    if (f.dtype != CG_F32 || f.ndim != 3 || !f.data) return -1;
+    const uintptr_t a = reinterpret_cast<uintptr_t>(f.data);
+    if ((a & 3) != 0 || (f.stride[1] * 4) % 16 || (f.stride[2] * 4) % 16) return -1;
+    return (int)((a & 15) >> 2);
+}
+
+// The tensor map of one FP32 field for boxes of w x h x 1 elements. Tensor coordinates start
+// `xo` elements before the field's first padded element; ext (elements per dimension in those
+// coordinates) may end before the padded extent, and box elements past it read as zero.
+inline bool make_map_ext(const cg_field& f, int xo, const cuuint64_t ext[3], int w, int h, CUtensorMap* out) {
+    const EncodeFn enc = encoder();
+    if (!enc) return false;
+    const uintptr_t a = reinterpret_cast<uintptr_t>(f.data);
+    const cuuint64_t pad0 = (cuuint64_t)(f.n[0] + 4 * f.halo[0]) + (cuuint64_t)xo;
+    const cuuint64_t pad1 = (cuuint64_t)(f.n[1] + 4 * f.halo[1]), pad2 = (cuuint64_t)(f.n[2] + 4 * f.halo[2]);
+    if (ext[0] < 1 || ext[1] < 1 || ext[2] < 1 || ext[0] > pad0 || ext[1] > pad1 || ext[2] > pad2) return false;
+    const cuuint64_t st1 = (cuuint64_t)f.stride[1] * 4, st2 = (cuuint64_t)f.stride[2] * 4;
+    if ((cuuint64_t)f.stride[1] < pad0 || st2 < st1 * pad1) return false;
+    const cuuint64_t strides[2] = {st1, st2};
+    const cuuint32_t box[3] = {(cuuint32_t)w, (cuuint32_t)h, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    void* base = reinterpret_cast<void*>(a - (uintptr_t)xo * 4);
+    return enc(out, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, ext, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 }  // namespace cgtma

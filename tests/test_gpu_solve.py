@@ -217,6 +217,29 @@ def test_fp32_defect_correction_3d(arch):
     _compare_states(ref, dc, 3)
 
 
+@pytest.mark.parametrize("layout", ["0:2", "0:3"])
+def test_fp32_defect_correction_3d_staged_layouts_bitwise(arch, monkeypatch, layout):
+    """The defect-correction solve with its inner FP32 iteration in march3d_tma_kernel (inputs
+    staged by TMA, with the continuity forcing and all three body-force components) gives the
+    register-fed kernel's solve bit for bit: the same iteration count and the same state."""
+    from chmy_gb300.configs import stokes3d_grf
+
+    pb = stokes3d_grf(24, ncheck=24)
+    out = {}
+    for lay in ("0:0", layout):
+        monkeypatch.setenv("CG_MARCH_LAYOUT", lay)
+        s = StokesSolver(arch, pb)
+        s.apply_bc()
+        r = s.solve(precision=_abi.CG_F32, max_outer=8, inner_rtol=1e-5)
+        assert r.converged == 1, (lay, r.outer, r.iterations, list(r.err))
+        out[lay] = (r.iterations, r.outer, [f.to_numpy() for f in s.fields["V"]], s.fields["P"].to_numpy(),
+                    [f.to_numpy() for f in s.fields["tau"]])
+    a, b = out["0:0"], out[layout]
+    assert a[:2] == b[:2]
+    for x, y in zip(a[2] + [a[3]] + a[4], b[2] + [b[3]] + b[4]):
+        assert np.array_equal(x.view(np.uint8), y.view(np.uint8))
+
+
 def test_fp32_solve_rejects_fp32_state(arch):
     pb = stokes2d_inclusions(32, dtype=np.float32)
     s = StokesSolver(arch, pb)

@@ -246,13 +246,16 @@ def test_fused_2d_autotuner_layouts_give_the_same_bits(arch, monkeypatch, T, lay
         assert np.array_equal(a.to_numpy().view(np.uint8), b.view(np.uint8)), f"layout {layout}: partner V"
 
 
-@pytest.mark.parametrize("layout", ["16:0", "32:0", "64:0", "0:1", "16:1", "32:1", "64:1"])
-@pytest.mark.parametrize("dims", [(31, 20, 70), (61, 7, 33)])
+@pytest.mark.parametrize("layout", ["16:0", "32:0", "64:0", "0:1", "16:1", "32:1", "64:1",
+                                    "0:2", "16:2", "32:2", "64:2", "0:3", "16:3", "32:3"])
+@pytest.mark.parametrize("dims", [(31, 20, 70), (61, 7, 33), (95, 23, 17)])
 def test_fused_3d_autotuner_layouts_give_the_same_bits(arch, monkeypatch, layout, dims):
-    """Every candidate of the 3D autotuner (z-segment lengths x block shapes: 12 rows at 2
-    blocks per SM, variant 0, or 8 rows at 3, variant 1; forced with CG_MARCH_LAYOUT) on FP32
-    fields that share one row and plane stride, as the defect-correction pool lays them out:
-    the oracle's states bit for bit."""
+    """Every candidate of the 3D autotuner (z-segment lengths x block shapes; forced with
+    CG_MARCH_LAYOUT): march3d_kernel with 12 rows at 2 blocks per SM (variant 0) or 8 rows at 3
+    (variant 1), and march3d_tma_kernel, its inputs staged by TMA, with 12 rows (variant 2) or 8
+    (variant 3). On FP32 fields that share one row and plane stride, as the defect-correction
+    pool lays them out: the oracle's states bit for bit. The grids put the tiles' first columns
+    at every offset from a 16-byte boundary that strips of 30 columns reach."""
     monkeypatch.setenv("CG_MARCH_LAYOUT", layout)
     rows = dims[1] + 5
     # rows padded to 512 bytes: Center and Vertex rows of these grids get one row stride
