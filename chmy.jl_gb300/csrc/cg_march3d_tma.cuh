@@ -60,6 +60,20 @@ __host__ __device__ constexpr int box_off(int a, int nw) {
     return o;
 }
 __host__ __device__ constexpr int slot_floats(int nw) { return box_off(kArrays, nw); }
+// The arrays a segment reads at its first plane (ks - 1: the new P and tau_zz below plane ks,
+// 1/eta below it) and at its last (ke + 1: V, 1/eta and the xz, yz shear inputs above plane ke);
+// every other plane is read whole.
+constexpr unsigned kFirstPlane = (1u << VX) | (1u << VY) | (1u << VZ) | (1u << IE) | (1u << P) | (1u << TZZ) |
+                                 (1u << OZZ) | (1u << FP);
+constexpr unsigned kLastPlane = (1u << VX) | (1u << VY) | (1u << VZ) | (1u << IE) | (1u << TXZ) | (1u << OXZ) |
+                                (1u << TYZ) | (1u << OYZ);
+// Bytes the copies of the arrays in `mask` deliver into one slot.
+__host__ __device__ constexpr unsigned mask_bytes(unsigned mask, int nw) {
+    unsigned b = 0;
+    for (int a = 0; a < kArrays; ++a)
+        if ((mask >> a) & 1u) b += (unsigned)(kW * rows(a, nw) * 4);
+    return b;
+}
 // Dynamic shared memory of a block: 128 bytes to align the ring, S slots, two exchange buffers
 // (P, tau_yy, tau_xy, tau_yz of every row) and 2 x S mbarriers.
 __host__ __device__ constexpr int smem_bytes(int nw, int S) {
@@ -160,11 +174,13 @@ __global__ void __launch_bounds__(32 * (NW + 1), MINB)
                     break;
                 }
                 if (m == withhold) continue;  // a test's withheld plane: its waits run out
+                const unsigned mask =
+                    present & (m == 0 ? kFirstPlane : (m == nplanes - 1 ? kLastPlane : 0xffffffffu));
                 T* dst = ring + q * SF;
-                mbar_expect_tx(&full[q], tx);
+                mbar_expect_tx(&full[q], mask == present ? tx : mask_bytes(mask, NW));
 #pragma unroll
                 for (int a = 0; a < kArrays; ++a)
-                    if ((present >> a) & 1u)
+                    if ((mask >> a) & 1u)
                         tma_load_3d(dst + box_off(a, NW), &maps.m[a], bx0, j0 + row0(a), ks + m, &full[q]);
                 last[q] = m;
             }
