@@ -523,73 +523,100 @@ __device__ inline bool phase_member(const BcField<T>& F, int nd, const int* n, i
     return false;
 }
 
-template <class T, bool FN>
+// One thread per point of one item (a boundary plane of one field): blockIdx.z is the item, x
+// and y the plane's tangential indices (the lower dimension along x). The dimension count is a
+// template parameter, so the phase loops unroll with the phase, dimension and side known at
+// compile time and the rule chain stays in registers.
+template <class T, bool FN, int ND>
 __global__ void bc_apply_kernel(const BcBatch<T> b, const BcFns<T, FN> fns) {
     cg_dep_wait();
     cg_dep_release();
-    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-    if (tid >= b.total) return;
-    int it = 0;
-    while (it + 1 < b.nitems && b.items[it + 1].start <= tid) ++it;
-    const BcItem item = b.items[it];
-    const BcField<T>& F = b.f[item.field];
-    const int nd = b.nd;
-    // decode the tangential coordinates (extent n_t + 3 each, index 0..n_t+2)
+    const BcItem item = b.items[blockIdx.z];
+    const int dd = item.d;
+    const int ia = blockIdx.x * blockDim.x + threadIdx.x, ib = blockIdx.y * blockDim.y + threadIdx.y;
+    // the point: tangential indices 0..n_t+2, the item's plane along dd
     int p[3] = {0, 0, 0};
-    int rem = tid - item.start;
-    for (int t = 0; t < nd; ++t) {
-        if (t == item.d) continue;
-        const int e = b.n[t] + 3;
-        p[t] = rem % e;
-        rem /= e;
+    if constexpr (ND == 1) {
+        if (ia > 0 || ib > 0) return;
+        p[0] = item.plane;
+    } else if constexpr (ND == 2) {
+        const int ta = dd == 0 ? 1 : 0;
+        if (ia > b.n[ta] + 2 || ib > 0) return;
+        p[0] = dd == 0 ? item.plane : ia;
+        p[1] = dd == 1 ? item.plane : ia;
+    } else {
+        const int ta = dd == 0 ? 1 : 0, tb = dd == 2 ? 1 : 2;
+        if (ia > b.n[ta] + 2 || ib > b.n[tb] + 2) return;
+        p[0] = dd == 0 ? item.plane : ia;
+        p[1] = dd == 1 ? item.plane : (dd == 0 ? ia : ib);
+        p[2] = dd == 2 ? item.plane : ib;
     }
-    p[item.d] = item.plane;
-    const int k0 = (nd - 1 - item.d) * 2 + item.s;
+    const BcField<T>& F = b.f[item.field];
+    const int k0 = (ND - 1 - dd) * 2 + item.s;
     int src, rule;
     // only the last writing phase handles the point
-    for (int k = k0 + 1; k < 2 * nd; ++k)
-        if (phase_member(F, nd, b.n, k, p, &src, &rule)) return;
-    // walk the chain of rules back to an unwritten point or a constant
-    int stack_k[6], stack_r[6], depth = 0;
-    T stack_v[6];  // each rule's value, at the point that rule writes
+#pragma unroll
+    for (int k = 0; k < 2 * ND; ++k)
+        if (k > k0 && phase_member(F, ND, b.n, k, p, &src, &rule)) return;
+    // walk the chain of rules back from phase k0 to an unwritten point or a constant: at most
+    // one rule per phase, in decreasing phase order (the largest earlier phase that writes the
+    // current point next)
     int q[3] = {p[0], p[1], p[2]};
-    int k = k0;
-    T base;
-    phase_member(F, nd, b.n, k, q, &src, &rule);
-    for (;;) {
-        const int d = nd - 1 - (k >> 1), s = k & 1;
+    bool used[2 * ND];
+    int rk[2 * ND];
+    T vk[2 * ND];
+    bool open = true;
+    T base = T(0);
+#pragma unroll
+    for (int k = 2 * ND - 1; k >= 0; --k) {
+        used[k] = false;
+        rk[k] = R_CONST;
+        vk[k] = T(0);
+        if (!open || k > k0 || !phase_member(F, ND, b.n, k, q, &src, &rule)) continue;
+        const int d = ND - 1 - (k >> 1), s = k & 1;
+        const T v = bc_value(F, fns, item.field, ND, b.n, d, s, q);
         if (rule == R_CONST) {
-            base = bc_value(F, fns, item.field, nd, b.n, d, s, q);
-            break;
+            base = v;
+            open = false;
+            continue;
         }
-        stack_k[depth] = k;
-        stack_r[depth] = rule;
-        stack_v[depth] = bc_value(F, fns, item.field, nd, b.n, d, s, q);
-        ++depth;
+        used[k] = true;
+        rk[k] = rule;
+        vk[k] = v;
         q[d] = src;
-        int kn = -1;
-        for (int kk = k - 1; kk >= 0; --kk)
-            if (phase_member(F, nd, b.n, kk, q, &src, &rule)) {
-                kn = kk;
-                break;
-            }
-        if (kn < 0) {
-            base = F.p[q[0] + q[1] * F.s[1] + q[2] * F.s[2]];
-            break;
-        }
-        k = kn;
     }
-    for (int i = depth - 1; i >= 0; --i) {
-        const int kk = stack_k[i];
-        const int d = nd - 1 - (kk >> 1), s = kk & 1;
-        const T v = stack_v[i];
-        switch (stack_r[i]) {
-            case R_DIR_C: base = fma(T(2), v - base, base); break;
-            case R_NEU: base = fma(F.h[d], s == 0 ? -v : v, base); break;
+    if (open) base = F.p[q[0] + q[1] * F.s[1] + q[2] * F.s[2]];
+    // apply the rules from the innermost (lowest phase) out
+#pragma unroll
+    for (int k = 0; k < 2 * ND; ++k) {
+        if (!used[k]) continue;
+        const int d = ND - 1 - (k >> 1), s = k & 1;
+        switch (rk[k]) {
+            case R_DIR_C: base = fma(T(2), vk[k] - base, base); break;
+            case R_NEU: base = fma(F.h[d], s == 0 ? -vk[k] : vk[k], base); break;
             default: break;
         }
     }
     F.p[p[0] + p[1] * F.s[1] + p[2] * F.s[2]] = base;
+}
+
+// Launch of bc_apply_kernel over the batch's items: blocks of 32 x 8 points (3D), 128 (2D) or one
+// thread (1D), the grid covering the largest tangential extents of the items.
+template <class T, bool FN>
+cudaError_t bc_launch(const BcBatch<T>& b, const BcFns<T, FN>& fns, cudaStream_t st, bool dep) {
+    int ea = 1, eb = 1;
+    for (int i = 0; i < b.nitems; ++i) {
+        const int d = b.items[i].d;
+        if (b.nd >= 2) ea = std::max(ea, b.n[d == 0 ? 1 : 0] + 3);
+        if (b.nd == 3) eb = std::max(eb, b.n[d == 2 ? 1 : 2] + 3);
+    }
+    const unsigned nz = (unsigned)b.nitems;
+    if (b.nd == 3)
+        return cg_launch(bc_apply_kernel<T, FN, 3>, dim3(cg_div_up(ea, 32), cg_div_up(eb, 8), nz), dim3(32, 8), 0, st, dep,
+                         b, fns);
+    if (b.nd == 2)
+        return cg_launch(bc_apply_kernel<T, FN, 2>, dim3(cg_div_up(ea, 128), 1, nz), dim3(128), 0, st, dep, b, fns);
+    return cg_launch(bc_apply_kernel<T, FN, 1>, dim3(1, 1, nz), dim3(32), 0, st, dep, b, fns);
 }
 
 template <class T>
@@ -637,15 +664,13 @@ int bc_apply_t(cg_ctx* ctx, const cg_grid* grid, int nfields, const cg_field* fi
     b.nitems = ni;
     b.total = total;
     if (total == 0) return CG_OK;
-    const int threads = 256;
     bool any_fn = false;
     if (fns)
         for (int fi = 0; fi < nfields; ++fi)
             for (int d = 0; d < b.nd; ++d)
                 for (int s = 0; s < 2; ++s) any_fn = any_fn || fns[fi].fn[d][s].kind != CG_FN_NONE;
     if (!any_fn) {
-        CG_CUDA(ctx, cg_launch(bc_apply_kernel<T, false>, dim3(cg_div_up(total, threads)), dim3(threads), 0, ctx->stream,
-                               dep, b, BcFns<T, false>{}));
+        CG_CUDA(ctx, bc_launch(b, BcFns<T, false>{}, ctx->stream, dep));
         return CG_OK;
     }
     BcFns<T, true> bf;
@@ -667,8 +692,7 @@ int bc_apply_t(cg_ctx* ctx, const cg_grid* grid, int nfields, const cg_field* fi
                 bf.vtx[fi][d][s] = (unsigned char)(kind == CG_BC_NEUMANN ? !vtx : vtx);
                 bf.full[fi][d][s] = (unsigned char)(fns[fi].full_dims[d][s] != 0);
             }
-    CG_CUDA(ctx, cg_launch(bc_apply_kernel<T, true>, dim3(cg_div_up(total, threads)), dim3(threads), 0, ctx->stream, dep,
-                           b, bf));
+    CG_CUDA(ctx, bc_launch(b, bf, ctx->stream, dep));
     return CG_OK;
 }
 
@@ -779,22 +803,44 @@ __device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v)
 // integer max over |x| bits is the max-norm and propagates NaN.
 __global__ void maxabs_kernel(const RedBatch b, unsigned long long* out) {
     const RedField F = b.f[blockIdx.y];
-    const long plane = (long)F.n0 * F.n1;
-    const long total = plane * F.n2;
+    // warp tasks of up to 256 consecutive elements of one row: one 32-bit division per task, and
+    // a lane keeps up to 8 independent loads in flight
+    constexpr int kW = 256;
+    const int nch = (F.n0 + kW - 1) / kW;
+    const int ntask = nch * F.n1 * F.n2;
+    const int lane = threadIdx.x & 31;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
     unsigned long long m = 0;
-    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
-        const int k = (int)(t / plane);
-        const long r = t - (long)k * plane;
-        const int j = (int)(r / F.n0);
-        const int i = (int)(r - (long)j * F.n0);
-        const long off = i + j * F.s1 + k * F.s2;
-        const unsigned long long v = F.is64 ? abs_bits(static_cast<const double*>(F.p)[off])
-                                            : abs_bits(static_cast<const float*>(F.p)[off]);
-        m = v > m ? v : m;
+    for (int task = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; task < ntask; task += nw) {
+        const int row = task / nch, c = task - row * nch;
+        const int k = row / F.n1, j = row - k * F.n1;
+        const long base = (long)j * F.s1 + (long)k * F.s2;
+        const int i0 = c * kW + lane, i1 = min(F.n0, (c + 1) * kW);
+        if (F.is64) {
+            const double* q = static_cast<const double*>(F.p) + base;
+#pragma unroll
+            for (int u = 0; u < kW / 32; ++u) {
+                const int i = i0 + 32 * u;
+                if (i < i1) {
+                    const unsigned long long v = abs_bits(q[i]);
+                    m = v > m ? v : m;
+                }
+            }
+        } else {
+            const float* q = static_cast<const float*>(F.p) + base;
+#pragma unroll
+            for (int u = 0; u < kW / 32; ++u) {
+                const int i = i0 + 32 * u;
+                if (i < i1) {
+                    const unsigned long long v = abs_bits(q[i]);
+                    m = v > m ? v : m;
+                }
+            }
+        }
     }
     m = warp_max_u64(m);
     __shared__ unsigned long long sm[32];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int w = threadIdx.x >> 5;
     if (lane == 0) sm[w] = m;
     __syncthreads();
     if (w == 0) {

@@ -511,14 +511,16 @@ inline cudaError_t launch_march3d_tma(const Fused3D<float>& f, const SP<float>& 
     auto kern = march3d_tma_kernel<NW, MINB, S, WRITE_RES>;
     constexpr int smem = m3t::smem_bytes(NW, S);
     static_assert(smem <= 232448, "the ring exceeds a block's shared memory");
-    static const int bps = [&] {
-        int nb = 0;
-        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, 32 * (NW + 1), smem) != cudaSuccess)
-            nb = 0;
+    // set on every launch (launches happen while tuning and capturing graphs): each translation
+    // unit that launches the kernel has its own copy of it, while a static in this inline
+    // function would be shared by all of them
+    cudaError_t ae = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (ae != cudaSuccess) return ae;
+    int bps = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, 32 * (NW + 1), smem) != cudaSuccess || bps < 1) {
         cudaGetLastError();
-        return nb > 0 ? nb : 1;
-    }();
+        bps = 1;
+    }
     const int e0 = n0 + 1, e1 = n1 + 1, e2 = n2 + 1;
     const int nstrip = cg_div_up(e0 + 1, 30), nty = cg_div_up(e1 + 1, NW - 2);
     const long tiles = (long)nstrip * nty;
@@ -544,10 +546,13 @@ inline cudaError_t launch_march3d_any(const Fused3D<T>& f, const SP<T>& s, int n
             long s1 = 0, s2 = 0;
             if (h < m3t::kHeights && l.dir[h] && l.dir[h]->ok && l.err && march3_uniform(f, &s1, &s2) &&
                 march3_fits_int(f, n0 + 1, n1 + 1, n2 + 1)) {
+                // an ordinary launch (and the bc! launch after it too): with dependent launches around
+                // it, the defect-correction chunk measured 465-486 instead of 457-472 us per 256^3
+                // iteration
                 if (h == 0)
-                    return launch_march3d_tma<12, 2, 3, WRITE_RES>(f, s, n0, n1, n2, num_sms, seg_len, s1, s2, st, dep,
+                    return launch_march3d_tma<12, 2, 3, WRITE_RES>(f, s, n0, n1, n2, num_sms, seg_len, s1, s2, st, false,
                                                                    *l.dir[0], l.err);
-                return launch_march3d_tma<8, 3, 3, WRITE_RES>(f, s, n0, n1, n2, num_sms, seg_len, s1, s2, st, dep,
+                return launch_march3d_tma<8, 3, 3, WRITE_RES>(f, s, n0, n1, n2, num_sms, seg_len, s1, s2, st, false,
                                                               *l.dir[1], l.err);
             }
             variant = 0;

@@ -678,7 +678,8 @@ int pp_iterations_3d(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* a, c
                     : launch_march3d_any<T, false>(fk, s, g->n[0], g->n[1], g->n[2], nsm, tc.seg, st, tc.variant, it > 0, lk);
             if (le != cudaSuccess) return cg_fail(ctx, CG_ERR_CUDA, "fused3d launch: %s", cudaGetErrorString(le));
             if (bc_V) {
-                int r = cg_bc_apply_impl(ctx, g, 3, (it % 2 == 0) ? b->V : a->V, bc_V, true);
+                // no dependent launches around the TMA-fed kernel (measured slower with them)
+                int r = cg_bc_apply_impl(ctx, g, 3, (it % 2 == 0) ? b->V : a->V, bc_V, !staged);
                 if (r) return r;
             }
         }

@@ -248,56 +248,72 @@ size_t padded_count(const cg_field& f) {
 template <int ND>
 __global__ void tau_res_kernel(const SV<float> v, const SP<float> s, int e0, int e1, int n0, int n1, int n2,
                                unsigned long long* slot) {
+    // one thread per point of the launch range; the block's maximum goes into the slot, with an
+    // atomic only when it exceeds the slot's current value (one address: atomics from every warp
+    // of the grid would serialise there)
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = ND > 2 ? blockIdx.z : 0;
     unsigned m = 0;
-    if (i <= e0 && j <= e1) {
-        // interior test per location: logical index 1..n (Center) or 1..n+1 (Vertex) along each
-        // dim (0 is the lower ghost layer of the launch range)
-        auto in = [&](int li, int lj, int lk) {
-            return i >= 1 && j >= 1 && i <= n0 + li && j <= n1 + lj && (ND < 3 || (k >= 1 && k <= n2 + lk));
-        };
-        auto take = [&](float r) { m = max(m, __float_as_uint(fabsf(r))); };
-        const float exx = (v.V[0](i + 1, j, k) - v.V[0](i, j, k)) * s.idx[0];
-        const float eyy = (v.V[1](i, j + 1, k) - v.V[1](i, j, k)) * s.idx[1];
-        float ezz = 0.f, dv = exx + eyy;
-        if (ND > 2) {
-            ezz = (v.V[2](i, j, k + 1) - v.V[2](i, j, k)) * s.idx[2];
-            dv = dv + ezz;
-        }
-        const float ie = v.ieta(i, j, k);
-        auto diag = [&](int c, float e) {
-            const float t = v.tau[c](i, j, k);
-            take(-(t - v.tau_old[c](i, j, k)) * s.inv_Gdt - t * ie + 2.f * (e - dv * s.third));
-        };
-        auto shear = [&](int c, float e, int a, int b) {
-            const float t = v.tau[c](i, j, k);
-            const float iev = shear_inv_eta(v, i, j, k, a, b);
-            take(-(t - v.tau_old[c](i, j, k)) * s.inv_Gdt - t * iev + 2.f * e);
-        };
-        const float exy = 0.5f * ((v.V[0](i, j, k) - v.V[0](i, j - 1, k)) * s.idx[1] +
-                                  (v.V[1](i, j, k) - v.V[1](i - 1, j, k)) * s.idx[0]);
-        if (in(0, 0, 0)) {
-            diag(0, exx);
-            diag(1, eyy);
-            if (ND > 2) diag(2, ezz);
-        }
-        if (ND == 2) {
-            if (in(1, 1, 0)) shear(2, exy, 0, 1);
-        } else {
-            const float exz = 0.5f * ((v.V[0](i, j, k) - v.V[0](i, j, k - 1)) * s.idx[2] +
-                                      (v.V[2](i, j, k) - v.V[2](i - 1, j, k)) * s.idx[0]);
-            const float eyz = 0.5f * ((v.V[1](i, j, k) - v.V[1](i, j, k - 1)) * s.idx[2] +
-                                      (v.V[2](i, j, k) - v.V[2](i, j - 1, k)) * s.idx[1]);
-            if (in(1, 1, 0)) shear(3, exy, 0, 1);
-            if (in(1, 0, 1)) shear(4, exz, 0, 2);
-            if (in(0, 1, 1)) shear(5, eyz, 1, 2);
+    {
+        if (i <= e0 && j <= e1) {
+            // interior test per location: logical index 1..n (Center) or 1..n+1 (Vertex) along
+            // each dim (0 is the lower ghost layer of the launch range)
+            auto in = [&](int li, int lj, int lk) {
+                return i >= 1 && j >= 1 && i <= n0 + li && j <= n1 + lj && (ND < 3 || (k >= 1 && k <= n2 + lk));
+            };
+            auto take = [&](float r) { m = max(m, __float_as_uint(fabsf(r))); };
+            const float exx = (v.V[0](i + 1, j, k) - v.V[0](i, j, k)) * s.idx[0];
+            const float eyy = (v.V[1](i, j + 1, k) - v.V[1](i, j, k)) * s.idx[1];
+            float ezz = 0.f, dv = exx + eyy;
+            if (ND > 2) {
+                ezz = (v.V[2](i, j, k + 1) - v.V[2](i, j, k)) * s.idx[2];
+                dv = dv + ezz;
+            }
+            const float ie = v.ieta(i, j, k);
+            auto diag = [&](int c, float e) {
+                const float t = v.tau[c](i, j, k);
+                take(-(t - v.tau_old[c](i, j, k)) * s.inv_Gdt - t * ie + 2.f * (e - dv * s.third));
+            };
+            auto shear = [&](int c, float e, int a, int b) {
+                const float t = v.tau[c](i, j, k);
+                const float iev = shear_inv_eta(v, i, j, k, a, b);
+                take(-(t - v.tau_old[c](i, j, k)) * s.inv_Gdt - t * iev + 2.f * e);
+            };
+            const float exy = 0.5f * ((v.V[0](i, j, k) - v.V[0](i, j - 1, k)) * s.idx[1] +
+                                      (v.V[1](i, j, k) - v.V[1](i - 1, j, k)) * s.idx[0]);
+            if (in(0, 0, 0)) {
+                diag(0, exx);
+                diag(1, eyy);
+                if (ND > 2) diag(2, ezz);
+            }
+            if (ND == 2) {
+                if (in(1, 1, 0)) shear(2, exy, 0, 1);
+            } else {
+                const float exz = 0.5f * ((v.V[0](i, j, k) - v.V[0](i, j, k - 1)) * s.idx[2] +
+                                          (v.V[2](i, j, k) - v.V[2](i - 1, j, k)) * s.idx[0]);
+                const float eyz = 0.5f * ((v.V[1](i, j, k) - v.V[1](i, j, k - 1)) * s.idx[2] +
+                                          (v.V[2](i, j, k) - v.V[2](i, j - 1, k)) * s.idx[1]);
+                if (in(1, 1, 0)) shear(3, exy, 0, 1);
+                if (in(1, 0, 1)) shear(4, exz, 0, 2);
+                if (in(0, 1, 1)) shear(5, eyz, 1, 2);
+            }
         }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if ((threadIdx.x & 31) == 0 && m) atomicMax(slot, (unsigned long long)m);
+    __shared__ unsigned sm[32];
+    const int t = threadIdx.y * blockDim.x + threadIdx.x, lane = t & 31, w = t >> 5;
+    if (lane == 0) sm[w] = m;
+    __syncthreads();
+    if (w == 0) {
+        const int nwarp = (int)(blockDim.x * blockDim.y) >> 5;
+        m = lane < nwarp ? sm[lane] : 0u;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (lane == 0 && m && (unsigned long long)m > *reinterpret_cast<volatile unsigned long long*>(slot))
+            atomicMax(slot, (unsigned long long)m);
+    }
 }
 
 __global__ void fill_kernel(float* dst, float v, size_t count) {
@@ -567,7 +583,8 @@ int cg_stokes_solve_dc(cg_ctx* ctx, const cg_grid* g, const cg_stokes_fields* f,
                              : launch_march3d_any<float, false>(fk, s32, g->n[0], g->n[1], g->n[2], nsm, tc.seg, st,
                                                                 tc.variant, it > 0, lk);
                     if (le != cudaSuccess) return cg_fail(ctx, CG_ERR_CUDA, "fused3d launch: %s", cudaGetErrorString(le));
-                    int r = cg_bc_apply_impl(ctx, g, nd, (it % 2 == 0) ? w.dV2 : w.dV, bc0, true);
+                    // no dependent launches around the TMA-fed kernel (measured slower with them)
+                    int r = cg_bc_apply_impl(ctx, g, nd, (it % 2 == 0) ? w.dV2 : w.dV, bc0, !staged);
                     if (r) return r;
                 }
             }
