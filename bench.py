@@ -450,7 +450,7 @@ def run_ours(args, rank, world, dist):
         b3 = FUSED3_ARRAYS * n3**3 * 4
         stokes3d = {
             "workload": "3D VE Stokes 256^3, log-viscosity Gaussian random field (correlation length 0.1, std 1, seed 4), FP32 fused PT iteration",
-            "kernel": "march3d_kernel<float>",
+            "kernel": "fused 3D PT iteration, the autotuner's choice of march3d_tma_kernel (inputs staged by TMA) and march3d_kernel",
             "kernel_ms": ms3,
             "algorithmic_bytes_per_launch": b3,
             "t_eff_gbs": b3 / (ms3 * 1e-3) / 1e9,
@@ -1299,6 +1299,30 @@ def run_kernel_sia_adjoint(arch, args):
                       "gradient_ms": (t2 - t1) * 1e3, "ratio": (t2 - t1) / (t1 - t0)}))
 
 
+def run_kernel_stokes3d_dc(arch, args):
+    """--kernel stokes3d_dc: one forward solve of the 3D VE Stokes configuration at n^3 (random
+    log-viscosity field, buoyant sphere, free slip) to residual 1e-8, FP32 PT inside FP64 defect
+    correction; wall clock around the synchronised call, and the time per PT iteration."""
+    import time
+
+    import torch
+
+    from chmy_gb300 import _abi
+    from chmy_gb300.configs import stokes3d_grf
+    from chmy_gb300.solvers import StokesSolver
+
+    pb = stokes3d_grf(args.n)
+    s = StokesSolver(arch, pb)
+    s.apply_bc()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    res = s.solve(precision=_abi.CG_F32)
+    torch.cuda.synchronize()
+    t = time.perf_counter() - t0
+    print(json.dumps({"kernel": "stokes3d_dc", "n": args.n, "converged": int(res.converged), "iterations": int(res.iterations),
+                      "outer": int(res.outer), "s": t, "us_per_iteration": 1e6 * t / max(int(res.iterations), 1)}))
+
+
 def run_kernel(args):
     """--kernel fused2d | fused3d: only the fused FP32 PT kernel (2D inclusions n^2, or 3D random
     viscosity n^3), `--reps` launches timed with CUDA events (the command the committed ncu
@@ -1325,10 +1349,14 @@ def run_kernel(args):
         run_kernel_sia_adjoint(arch, args)
         arch.close()
         return
+    if args.kernel == "stokes3d_dc":
+        run_kernel_stokes3d_dc(arch, args)
+        arch.close()
+        return
     if args.kernel == "fused3d":
         pb = stokes3d_grf(args.n, dtype=np.float32)
         da, db, keep = fused3d_kernel_fields(arch, pb, args.align_index)
-        name, arrays, cells = "march3d_kernel<float>", FUSED3_ARRAYS, args.n**3
+        name, arrays, cells = "fused 3D PT iteration (autotuner's choice)", FUSED3_ARRAYS, args.n**3
     else:
         pb = stokes2d_inclusions(args.n)
         da, db, keep = fused_kernel_fields(arch, pb)
@@ -1357,7 +1385,7 @@ def run_kernel(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--kernel", choices=["fused2d", "fused3d", "ptdiff3d", "sia_ensemble", "diffusion2d", "sia_adjoint", "stokes64",
+    ap.add_argument("--kernel", choices=["fused2d", "fused3d", "stokes3d_dc", "ptdiff3d", "sia_ensemble", "diffusion2d", "sia_adjoint", "stokes64",
                                          "ptdiff64"],
                     help="time one kernel alone (profiling driver)")
     ap.add_argument("--members", type=int, default=64, help="--kernel sia_ensemble: ensemble members")
