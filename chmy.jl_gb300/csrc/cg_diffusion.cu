@@ -4,6 +4,13 @@
 
 namespace {
 
+using cgk::radd;
+using cgk::rmul;
+using cgk::rsub;
+
+// Every kernel here rounds each operation as the oracle does (no contraction into FMA, the
+// reference's operation order), so all of them equal the oracle bit for bit.
+
 template <class T>
 struct Spacing {
     T i[3];
@@ -30,9 +37,9 @@ __global__ void compute_q_kernel(DF<T> q0, DF<T> q1, DF<T> q2, DF<T> C, T mchi, 
     if (i > e0 || j > e1) return;
     const T c = C(i, j, k);
     // q.d = -χ * ∂d(C): C is Center, seen from the face: (C[I] - C[I - e_d]) * iΔ_d
-    q0(i, j, k) = mchi * ((c - C(i - 1, j, k)) * s.i[0]);
-    if (ND > 1) q1(i, j, k) = mchi * ((c - C(i, j - 1, k)) * s.i[1]);
-    if (ND > 2) q2(i, j, k) = mchi * ((c - C(i, j, k - 1)) * s.i[2]);
+    q0(i, j, k) = rmul(mchi, rmul(rsub(c, C(i - 1, j, k)), s.i[0]));
+    if (ND > 1) q1(i, j, k) = rmul(mchi, rmul(rsub(c, C(i, j - 1, k)), s.i[1]));
+    if (ND > 2) q2(i, j, k) = rmul(mchi, rmul(rsub(c, C(i, j, k - 1)), s.i[2]));
 }
 
 template <class T, int ND>
@@ -42,47 +49,53 @@ __global__ void update_C_kernel(DF<T> C, DF<T> q0, DF<T> q1, DF<T> q2, T dt, Spa
     const int k = ND > 2 ? blockIdx.z : 0;
     if (i > e0 || j > e1) return;
     // divg(q) = Σ_d (q_d[I + e_d] - q_d[I]) * iΔ_d, summed in dim order
-    T dv = (q0(i + 1, j, k) - q0(i, j, k)) * s.i[0];
-    if (ND > 1) dv = dv + (q1(i, j + 1, k) - q1(i, j, k)) * s.i[1];
-    if (ND > 2) dv = dv + (q2(i, j, k + 1) - q2(i, j, k)) * s.i[2];
-    C(i, j, k) = C(i, j, k) - dt * dv;
+    T dv = rmul(rsub(q0(i + 1, j, k), q0(i, j, k)), s.i[0]);
+    if (ND > 1) dv = radd(dv, rmul(rsub(q1(i, j + 1, k), q1(i, j, k)), s.i[1]));
+    if (ND > 2) dv = radd(dv, rmul(rsub(q2(i, j, k + 1), q2(i, j, k)), s.i[2]));
+    C(i, j, k) = rsub(C(i, j, k), rmul(dt, dv));
 }
 
-// Fused compute_q! + update_C!: the face fluxes are recomputed from C_in; a face with index
-// n+2 along its dimension is outside compute_q!'s range and reads as zero (fresh q arrays).
-// At the cells whose faces all lie inside that range (indices 1..n along every dimension) the
-// flux difference is the same stencil in the form C + sum_d a_d (C[I+e_d] - 2 C + C[I-e_d]),
-// a_d = dt chi / Δ_d^2: 7 FP64 operations in 2D where the flux form takes 15. The FP64 step is
-// bound by the FP64 pipe, and the two forms differ only by rounding, a few ulp of C per step.
+// Fused compute_q! + update_C! in the reference's flux form: q_d at face I is
+// -χ ((C[I] - C[I-e_d]) iΔ_d) over the launch range, a face with index n+2 along its dimension is
+// outside compute_q!'s range and reads as zero (fresh q arrays), and C' = C - dt Σ_d (q_d[I+e_d] -
+// q_d[I]) iΔ_d in dim order. Each x-face flux is computed once (a lane's right face is the next
+// lane's left face; the warp's last lane computes its own), each y-face once per block (row r of
+// the block's shared array is the lower face of its row r), z-faces by both cells. Blocks are a
+// multiple of 32 threads wide, so that a warp is 32 consecutive cells of one row.
 template <class T, int ND>
-__global__ void diffusion_step_kernel(DF<T> Co, DF<T> Ci, T mchi, T dt, Spacing<T> s, int e0, int e1, int e2,
-                                      Spacing<T> a) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = ND > 1 ? blockIdx.y * blockDim.y + threadIdx.y : 0;
+__global__ void diffusion_step_kernel(DF<T> Co, DF<T> Ci, T mchi, T dt, Spacing<T> s, int e0, int e1, int e2) {
+    extern __shared__ __align__(16) unsigned char dsm[];
+    T* qy = reinterpret_cast<T*>(dsm);  // (blockDim.y + 1) x blockDim.x y-faces (2D, 3D)
+    const int tx = threadIdx.x, ty = threadIdx.y, bx = blockDim.x;
+    const int i = blockIdx.x * bx + tx;
+    const int j = ND > 1 ? blockIdx.y * blockDim.y + ty : 0;
     const int k = ND > 2 ? blockIdx.z : 0;
-    if (i > e0 || j > e1) return;
-    const T c = Ci(i, j, k);
-    if (i >= 1 && i < e0 && (ND < 2 || (j >= 1 && j < e1)) && (ND < 3 || (k >= 1 && k < e2))) {
-        T acc = a.i[0] * fma(T(-2), c, Ci(i + 1, j, k) + Ci(i - 1, j, k));
-        if (ND > 1) acc = fma(a.i[1], fma(T(-2), c, Ci(i, j + 1, k) + Ci(i, j - 1, k)), acc);
-        if (ND > 2) acc = fma(a.i[2], fma(T(-2), c, Ci(i, j, k + 1) + Ci(i, j, k - 1)), acc);
-        Co(i, j, k) = c + acc;
-        return;
+    const bool in = i <= e0 && j <= e1;
+    auto face = [&](T a, T b, int d) { return rmul(mchi, rmul(rsub(a, b), s.i[d])); };
+    T c = T(0), qxl = T(0);
+    if (in) {
+        c = Ci(i, j, k);
+        qxl = face(c, Ci(i - 1, j, k), 0);
     }
-    const T qxl = mchi * ((c - Ci(i - 1, j, k)) * s.i[0]);
-    const T qxr = i + 1 <= e0 ? mchi * ((Ci(i + 1, j, k) - c) * s.i[0]) : T(0);
-    T dv = (qxr - qxl) * s.i[0];
-    if (ND > 1) {
-        const T ql = mchi * ((c - Ci(i, j - 1, k)) * s.i[1]);
-        const T qr = j + 1 <= e1 ? mchi * ((Ci(i, j + 1, k) - c) * s.i[1]) : T(0);
-        dv = dv + (qr - ql) * s.i[1];
+    T qxr = __shfl_down_sync(0xffffffffu, qxl, 1);
+    if ((tx & 31) == 31) qxr = (in && i + 1 <= e0) ? face(Ci(i + 1, j, k), c, 0) : T(0);
+    T qyl = T(0), qyr = T(0);
+    if constexpr (ND > 1) {
+        qy[ty * bx + tx] = in ? face(c, Ci(i, j - 1, k), 1) : T(0);
+        if (ty == (int)blockDim.y - 1) qy[(ty + 1) * bx + tx] = (in && j + 1 <= e1) ? face(Ci(i, j + 1, k), c, 1) : T(0);
+        __syncthreads();
+        qyl = qy[ty * bx + tx];
+        qyr = qy[(ty + 1) * bx + tx];
     }
-    if (ND > 2) {
-        const T ql = mchi * ((c - Ci(i, j, k - 1)) * s.i[2]);
-        const T qr = k + 1 <= e2 ? mchi * ((Ci(i, j, k + 1) - c) * s.i[2]) : T(0);
-        dv = dv + (qr - ql) * s.i[2];
+    if (!in) return;
+    T dv = rmul(rsub(qxr, qxl), s.i[0]);
+    if constexpr (ND > 1) dv = radd(dv, rmul(rsub(qyr, qyl), s.i[1]));
+    if constexpr (ND > 2) {
+        const T qzl = face(c, Ci(i, j, k - 1), 2);
+        const T qzr = k + 1 <= e2 ? face(Ci(i, j, k + 1), c, 2) : T(0);
+        dv = radd(dv, rmul(rsub(qzr, qzl), s.i[2]));
     }
-    Co(i, j, k) = c - dt * dv;
+    Co(i, j, k) = rsub(c, rmul(dt, dv));
 }
 
 // ---- masked operators (src/GridOperators/masked_operators.jl:11-39) --------------------------
@@ -103,10 +116,10 @@ __global__ void compute_q_masked_kernel(DF<T> q0, DF<T> q1, DF<T> q2, DF<T> C, c
     const int j = ND > 1 ? blockIdx.y * blockDim.y + threadIdx.y : 0;
     const int k = ND > 2 ? blockIdx.z : 0;
     if (i > e0 || j > e1) return;
-    const T cw = C(i, j, k) * w.c(i, j, k);
-    q0(i, j, k) = mchi * ((cw - C(i - 1, j, k) * w.c(i - 1, j, k)) * s.i[0]);
-    if (ND > 1) q1(i, j, k) = mchi * ((cw - C(i, j - 1, k) * w.c(i, j - 1, k)) * s.i[1]);
-    if (ND > 2) q2(i, j, k) = mchi * ((cw - C(i, j, k - 1) * w.c(i, j, k - 1)) * s.i[2]);
+    const T cw = rmul(C(i, j, k), w.c(i, j, k));
+    q0(i, j, k) = rmul(mchi, rmul(rsub(cw, rmul(C(i - 1, j, k), w.c(i - 1, j, k))), s.i[0]));
+    if (ND > 1) q1(i, j, k) = rmul(mchi, rmul(rsub(cw, rmul(C(i, j - 1, k), w.c(i, j - 1, k))), s.i[1]));
+    if (ND > 2) q2(i, j, k) = rmul(mchi, rmul(rsub(cw, rmul(C(i, j, k - 1), w.c(i, j, k - 1))), s.i[2]));
 }
 
 template <class T, int ND>
@@ -116,10 +129,12 @@ __global__ void update_C_masked_kernel(DF<T> C, DF<T> q0, DF<T> q1, DF<T> q2, co
     const int j = ND > 1 ? blockIdx.y * blockDim.y + threadIdx.y : 0;
     const int k = ND > 2 ? blockIdx.z : 0;
     if (i > e0 || j > e1) return;
-    T dv = (q0(i + 1, j, k) * w.f[0](i + 1, j, k) - q0(i, j, k) * w.f[0](i, j, k)) * s.i[0];
-    if (ND > 1) dv = dv + (q1(i, j + 1, k) * w.f[1](i, j + 1, k) - q1(i, j, k) * w.f[1](i, j, k)) * s.i[1];
-    if (ND > 2) dv = dv + (q2(i, j, k + 1) * w.f[2](i, j, k + 1) - q2(i, j, k) * w.f[2](i, j, k)) * s.i[2];
-    C(i, j, k) = C(i, j, k) - dt * dv;
+    T dv = rmul(rsub(rmul(q0(i + 1, j, k), w.f[0](i + 1, j, k)), rmul(q0(i, j, k), w.f[0](i, j, k))), s.i[0]);
+    if (ND > 1)
+        dv = radd(dv, rmul(rsub(rmul(q1(i, j + 1, k), w.f[1](i, j + 1, k)), rmul(q1(i, j, k), w.f[1](i, j, k))), s.i[1]));
+    if (ND > 2)
+        dv = radd(dv, rmul(rsub(rmul(q2(i, j, k + 1), w.f[2](i, j, k + 1)), rmul(q2(i, j, k), w.f[2](i, j, k))), s.i[2]));
+    C(i, j, k) = rsub(C(i, j, k), rmul(dt, dv));
 }
 
 // Fused masked compute_q! + update_C! (a flux at index n+2 reads as zero, as in the unmasked
@@ -132,20 +147,20 @@ __global__ void diffusion_step_masked_kernel(DF<T> Co, DF<T> Ci, const MaskV<T> 
     const int k = ND > 2 ? blockIdx.z : 0;
     if (i > e0 || j > e1) return;
     const T c = Ci(i, j, k);
-    const T cw = c * w.c(i, j, k);
+    const T cw = rmul(c, w.c(i, j, k));
     const int I[3] = {i, j, k}, E[3] = {e0, e1, e2};
     T dv = T(0);
 #pragma unroll
     for (int d = 0; d < ND; ++d) {
         const int di = d == 0, dj = d == 1, dk = d == 2;
-        const T ql = mchi * ((cw - Ci(i - di, j - dj, k - dk) * w.c(i - di, j - dj, k - dk)) * s.i[d]);
+        const T ql = rmul(mchi, rmul(rsub(cw, rmul(Ci(i - di, j - dj, k - dk), w.c(i - di, j - dj, k - dk))), s.i[d]));
         const T qr = I[d] + 1 <= E[d]
-                         ? mchi * ((Ci(i + di, j + dj, k + dk) * w.c(i + di, j + dj, k + dk) - cw) * s.i[d])
+                         ? rmul(mchi, rmul(rsub(rmul(Ci(i + di, j + dj, k + dk), w.c(i + di, j + dj, k + dk)), cw), s.i[d]))
                          : T(0);
-        const T t = (qr * w.f[d](i + di, j + dj, k + dk) - ql * w.f[d](i, j, k)) * s.i[d];
-        dv = d == 0 ? t : dv + t;
+        const T t = rmul(rsub(rmul(qr, w.f[d](i + di, j + dj, k + dk)), rmul(ql, w.f[d](i, j, k))), s.i[d]);
+        dv = d == 0 ? t : radd(dv, t);
     }
-    Co(i, j, k) = c - dt * dv;
+    Co(i, j, k) = rsub(c, rmul(dt, dv));
 }
 
 template <class T>
@@ -186,11 +201,10 @@ int update_C_t(cg_ctx* ctx, const cg_grid* g, const cg_field* C, const cg_field*
 template <class T, int ND>
 cudaError_t step_launch(const cg_grid* g, const cg_field* Co, const cg_field* Ci, double chi, double dt, dim3 block,
                         cudaStream_t st) {
-    Spacing<T> a;
-    for (int d = 0; d < 3; ++d) a.i[d] = (T)(dt * chi * g->inv_spacing[d] * g->inv_spacing[d]);
-    diffusion_step_kernel<T, ND><<<range_grid<ND>(g, block), block, 0, st>>>(
+    const size_t smem = ND > 1 ? (size_t)(block.y + 1) * block.x * sizeof(T) : 0;
+    diffusion_step_kernel<T, ND><<<range_grid<ND>(g, block), block, smem, st>>>(
         cg_view<T>(*Co), cg_view<T>(*Ci), -(T)chi, (T)dt, spacing_of<T>(g), g->n[0] + 1,
-        ND > 1 ? g->n[1] + 1 : 0, ND > 2 ? g->n[2] + 1 : 0, a);
+        ND > 1 ? g->n[1] + 1 : 0, ND > 2 ? g->n[2] + 1 : 0);
     return cudaGetLastError();
 }
 
