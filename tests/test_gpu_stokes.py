@@ -272,6 +272,38 @@ def test_fused_3d_autotuner_layouts_give_the_same_bits(arch, monkeypatch, layout
         assert np.array_equal(a.to_numpy().view(np.uint8), b.view(np.uint8)), f"layout {layout}: partner V"
 
 
+def test_staged_3d_wait_runs_out_and_the_context_stays_usable(arch, monkeypatch):
+    """Failure detection of the TMA-fed 3D iteration without a GPU fault: the producing warp
+    withholds the copies of one ring plane (CG_TMA_WITHHOLD_PLANE) and every wait is limited to
+    20 ms (CG_TMA_WAIT_LIMIT_MS). The compute warps' waits for that plane run out and they stop
+    together at their barrier; the producing warp's wait for their release runs out in turn,
+    it waits (bounded) for its copies in flight, and cg_stokes_pt_iterations_pp reports
+    CG_ERR_TIMEOUT. The same context then runs the iterations to the oracle's bits."""
+    import time
+
+    monkeypatch.setenv("CG_MARCH_LAYOUT", "16:2")
+    monkeypatch.setenv("CG_TMA_WAIT_LIMIT_MS", "20")
+    monkeypatch.setenv("CG_TMA_WITHHOLD_PLANE", "5")
+    dims = (31, 20, 70)
+    rows = dims[1] + 5
+    t0 = time.perf_counter()
+    with pytest.raises(_abi.ChmyError) as err:
+        _pp_run(arch, np.float32, dims, _bc_V(3), 4, seed=41, pitch_align=512, plane_rows=rows)
+    waited = time.perf_counter() - t0
+    assert err.value.code == _abi.CG_ERR_TIMEOUT, str(err.value)
+    assert "timed out" in str(err.value)
+    assert waited < 20.0, waited  # the 20 ms limits applied, not the 2 s default
+    monkeypatch.delenv("CG_TMA_WITHHOLD_PLANE")
+    monkeypatch.delenv("CG_TMA_WAIT_LIMIT_MS")
+    s, partner, prev, _ = _pp_run(arch, np.float32, dims, _bc_V(3), 4, seed=41, pitch_align=512, plane_rows=rows)
+    for name in ("V", "P", "tau", "divV", "r_V"):
+        hv = s.h[name] if isinstance(s.h[name], list) else [s.h[name]]
+        dv = s.d[name] if isinstance(s.d[name], list) else [s.d[name]]
+        for a, b in zip(dv, hv):
+            if b is not None:
+                assert_close(a, b, 0.0, f"after a timed-out run: {name}", exact=True)
+
+
 def _bc_mix(kind):
     """Velocity boundary conditions with every foldable rule: Dirichlet on a Vertex dimension
     (a constant plane), Dirichlet on a Center dimension (2v - interior), Neumann on either,
