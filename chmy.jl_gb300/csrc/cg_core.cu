@@ -443,8 +443,14 @@ __device__ __forceinline__ T bc_value(const BcField<T>& F, const BcFns<T, FN>& f
     return a[idx];
 }
 
+// One boundary plane of one field. lo/hi: the tangential indices (the lower tangential
+// dimension first) that lie on no phase plane of their dimension; a point inside both ranges is
+// written by this phase alone, from the interior source `src` (rule `rule`) that no earlier
+// phase writes, so the kernel takes it without walking the phase chain (lo > hi: never).
 struct BcItem {
     int field, d, s, plane, start;
+    int src, rule;
+    int lo[2], hi[2];
 };
 
 template <class T>
@@ -552,6 +558,21 @@ __global__ void bc_apply_kernel(const BcBatch<T> b, const BcFns<T, FN> fns) {
         p[2] = dd == 2 ? item.plane : ib;
     }
     const BcField<T>& F = b.f[item.field];
+    if (ia >= item.lo[0] && ia <= item.hi[0] && (ND < 3 || (ib >= item.lo[1] && ib <= item.hi[1]))) {
+        // on no other phase's plane: this phase's rule on its source, as the chain walk below
+        // takes it for such a point
+        const T v = bc_value(F, fns, item.field, ND, b.n, dd, item.s, p);
+        T base = v;
+        if (item.rule != R_CONST) {
+            int q[3] = {p[0], p[1], p[2]};
+            q[dd] = item.src;
+            base = F.p[q[0] + q[1] * F.s[1] + q[2] * F.s[2]];
+            if (item.rule == R_DIR_C) base = fma(T(2), v - base, base);
+            else if (item.rule == R_NEU) base = fma(F.h[dd], item.s == 0 ? -v : v, base);
+        }
+        F.p[p[0] + p[1] * F.s[1] + p[2] * F.s[2]] = base;
+        return;
+    }
     const int k0 = (ND - 1 - dd) * 2 + item.s;
     int src, rule;
     // only the last writing phase handles the point
@@ -619,6 +640,41 @@ cudaError_t bc_launch(const BcBatch<T>& b, const BcFns<T, FN>& fns, cudaStream_t
     return cg_launch(bc_apply_kernel<T, FN, 1>, dim3(1, 1, nz), dim3(32), 0, st, dep, b, fns);
 }
 
+// The item's fast-path ranges (BcItem::lo/hi): per tangential dimension t, the indices between
+// its lower and its upper phase planes. Empty (every point takes the chain walk) when the other
+// side of the item's own dimension shares its plane (tiny grids) or, for the upper side, holds
+// its source.
+template <class T>
+void bc_fast_ranges(const BcField<T>& F, int nd, const int* n, int d, int s, int plane, int src, int rule, BcItem* it) {
+    {
+        int g[2], sr[2], ru[2];
+        const int np = phase_planes(F, n, d, 1 - s, g, sr, ru);
+        for (int q = 0; q < np; ++q)
+            if (g[q] == plane || (s == 1 && rule != R_CONST && g[q] == src)) return;  // lo > hi: no fast path
+    }
+    int m = 0;
+    for (int t = 0; t < nd; ++t) {
+        if (t == d) continue;
+        int lo = 0, hi = n[t] + 2;
+        const int mid = (n[t] + 2) / 2;
+        for (int ss = 0; ss < 2; ++ss) {
+            int g[2], sr[2], ru[2];
+            const int np = phase_planes(F, n, t, ss, g, sr, ru);
+            for (int q = 0; q < np; ++q) {
+                if (g[q] <= mid) lo = std::max(lo, g[q] + 1);
+                else hi = std::min(hi, g[q] - 1);
+            }
+        }
+        it->lo[m] = lo;
+        it->hi[m] = hi;
+        ++m;
+    }
+    for (; m < 2; ++m) {  // dimensions the grid does not have: index 0 only
+        it->lo[m] = 0;
+        it->hi[m] = 0;
+    }
+}
+
 template <class T>
 int bc_apply_t(cg_ctx* ctx, const cg_grid* grid, int nfields, const cg_field* fields, const cg_bc* bcs, bool dep,
                const cg_bc_fn* fns = nullptr) {
@@ -655,7 +711,9 @@ int bc_apply_t(cg_ctx* ctx, const cg_grid* grid, int nfields, const cg_field* fi
                     if (t != d) cnt *= (b.n[t] + 3);
                 for (int q = 0; q < np; ++q) {
                     if (ni >= kBcMaxItems) return cg_fail(ctx, CG_ERR_ARG, "bc: too many boundary planes");
-                    b.items[ni] = BcItem{fi, d, s, g[q], total};
+                    BcItem it{fi, d, s, g[q], total, src[q], rule[q], {0, 0}, {-1, -1}};
+                    bc_fast_ranges(F, b.nd, b.n, d, s, g[q], src[q], rule[q], &it);
+                    b.items[ni] = it;
                     ++ni;
                     total += (int)cnt;
                 }
