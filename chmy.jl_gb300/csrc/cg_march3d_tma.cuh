@@ -109,11 +109,11 @@ __device__ __forceinline__ bool bar_or_compute(int n, bool p) {
     return r != 0;
 }
 
-// The TMA-fed fused iteration. Block = NW compute warps over a tile of 30 x (NW - 2) owned (i, j)
-// columns and one z segment, and one producing warp, with march3d_kernel's lane and row assignment (lanes 0 and 31,
-// warps 0 and NW-1 are one-point halos). Ring plane m is logical plane ks - 1 + m (tensor z =
-// ks + m); array a's box in a slot starts at tensor (x0, j0 + row0(a)), x0 the 16-byte
-// boundary at or before the tile's first column.
+// The TMA-fed fused iteration. Block = NW compute warps over a tile of 30 x (NW - 2) owned
+// (i, j) columns and one z segment, with march3d_kernel's lane and row assignment (lanes 0 and
+// 31, warps 0 and NW-1 are one-point halos), and one producing warp (warp NW). Ring plane m is
+// logical plane ks - 1 + m (tensor z = ks + m); array a's box in a slot starts at tensor
+// (x0, j0 + row0(a)), x0 the 16-byte boundary at or before the tile's first column.
 template <int NW, int MINB, int S, bool WRITE_RES>
 __global__ void __launch_bounds__(32 * (NW + 1), MINB)
     march3d_tma_kernel(const __grid_constant__ m3t::Maps maps, const Fused3D<float> f, const SP<float> s, int e0, int e1,
